@@ -1,0 +1,200 @@
+/*
+ * eolc.h — C ABI of the GB300-native EOL-Cloth hot path.
+ *
+ * One library (libeolc.so) replaces, for the non-EOL, non-remeshing path:
+ *   Forces::fill                     src/Forces.cpp:912-930   (Forces.h:40)
+ *   GeneralizedSolver::velocitySolve src/GeneralizedSolver.cpp:107-173
+ *                                    (GeneralizedSolver.h:26-30), for the
+ *                                    equality-constrained (pinned-corner) case
+ *   Cloth::solve / Cloth::step       src/Cloth.cpp:343-413 (minus dumps)
+ *   CD2 / btc::boxTriCollision /     src/Collisions.cpp:55-78,
+ *   btc::pointTriCollision           src/boxTriCollision.cpp:602-1224
+ *
+ * Conventions
+ *   - Plain pointers and sizes only.  Arrays suffixed _h are HOST memory
+ *     (caller-owned); arrays suffixed _d are DEVICE memory on the context's
+ *     device.  Positions are node-major: x[3*i + c].  Material coordinates
+ *     are X[2*i + c] (ArcSim Vert::u, mesh.hpp:57-80, z dropped).
+ *   - Every call returns an eolc_status; nothing throws or aborts.  The
+ *     reference aborts on solver errors (GeneralizedSolver.cpp:139-168); this
+ *     library reports them instead.  eolc_last_error() gives a message.
+ *   - A context is bound to one device and one stream and is not reentrant.
+ *   - Block-sparse matrices are 3x3 BSR in row-major block order; each block
+ *     is 9 values, row-major inside the block.  The pattern is the union of
+ *     node pairs sharing a triangle or a bending hinge, diagonal included,
+ *     columns ascending within a block row.
+ */
+#ifndef EOLC_H_
+#define EOLC_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  EOLC_OK = 0,
+  EOLC_NOT_CONVERGED = 1, /* iteration cap reached before the tolerance   */
+  EOLC_BREAKDOWN = 2,     /* p'Ap <= 0: matrix not positive definite       */
+  EOLC_NONFINITE = 3,     /* NaN/Inf in inputs or iterates                 */
+  EOLC_TIMEOUT = 4,       /* a bounded device wait gave up                  */
+  EOLC_BAD_ARG = 5,
+  EOLC_CUDA_ERROR = 6,
+  EOLC_CAPACITY = 7,      /* output buffer too small; *n_out has the need  */
+  EOLC_NO_TOPOLOGY = 8
+} eolc_status;
+
+/* Material of src/Cloth.h:28-35 (dampingA is unused by the reference). */
+typedef struct {
+  double density;   /* area density rho                      */
+  double e;         /* Young's modulus                       */
+  double nu;        /* Poisson's ratio                       */
+  double beta;      /* bending stiffness                     */
+  double damping_a; /* unused (kept for layout parity)       */
+  double damping_b; /* stiffness damping: MDK = M + d_B h^2 K */
+} eolc_material;
+
+typedef enum {
+  EOLC_PREC_FP64 = 0,  /* FP64 element math, FP64 BSR, FP64 PCG          */
+  EOLC_PREC_MIXED = 1  /* FP32 element math / BSR / PCG, FP64 dots and an
+                          FP64 iterative-refinement residual              */
+} eolc_precision;
+
+typedef enum {
+  EOLC_PC_JACOBI = 0,       /* point Jacobi (Eigen's default for CG)     */
+  EOLC_PC_BLOCK_JACOBI = 1, /* inverse of the 3x3 diagonal blocks        */
+  EOLC_PC_LEARNED = 2       /* learned block-sparse approximate inverse  */
+} eolc_precond;
+
+typedef struct {
+  double rel_tol;       /* stop when ||b - A v|| <= rel_tol ||b|| (FP64) */
+  int max_iter;         /* total inner iterations allowed                */
+  int precision;        /* eolc_precision                                */
+  int precond;          /* eolc_precond                                  */
+  int fallback_factor;  /* learned PC: fall back to Jacobi after
+                           fallback_factor * (last Jacobi count) iterations;
+                           0 disables the fallback                       */
+} eolc_solve_opts;
+
+typedef struct {
+  int status;        /* eolc_status of the solve                          */
+  int iterations;    /* inner PCG iterations (all restarts)               */
+  int refinements;   /* FP64 true-residual recomputations                 */
+  int used_fallback; /* 1 if the learned PC fell back to Jacobi           */
+  double rel_res;    /* final FP64 ||b - A v|| / ||b|| on the free DOFs    */
+} eolc_solve_info;
+
+typedef struct eolc_ctx eolc_ctx;
+
+/* ---- lifetime ---------------------------------------------------------- */
+eolc_status eolc_create(eolc_ctx **out, int device);
+void eolc_destroy(eolc_ctx *ctx);
+const char *eolc_last_error(const eolc_ctx *ctx);
+/* stream is a cudaStream_t; NULL selects the context's own stream. */
+eolc_status eolc_set_stream(eolc_ctx *ctx, void *stream);
+int eolc_version(void);
+
+/* ---- topology (Mesh::add(Face) adjacency, ArcSim mesh.cpp:356-378) -----
+ * tri_h:   n_tri x 3 node indices, face vertex order as in Face::v[0..2].
+ * hinge_h: n_hinge x 4 (x0, x1, x2, x3) for every edge with two adjacent
+ *          faces, in mesh.edges order: x0 = edge->n[0], x1 = edge->n[1],
+ *          x2 = other vertex of adjf[0], x3 = other vertex of adjf[1]
+ *          (Forces.cpp:687-697).
+ * Builds the BSR pattern and the per-block contribution lists once. */
+eolc_status eolc_set_topology(eolc_ctx *ctx, int n_nodes, const int *tri_h,
+                              int n_tri, const int *hinge_h, int n_hinge);
+/* n_blocks = number of 3x3 blocks; rowptr_h has n_nodes + 1 entries. */
+eolc_status eolc_bsr_pattern(eolc_ctx *ctx, int *n_blocks, int *rowptr_h,
+                             int *colidx_h);
+
+/* ---- Forces::fill (Forces.cpp:912-930, non-EOL branches) ----------------
+ * Computes f (3N), M and MDK (BSR values, n_blocks*9 each) for positions
+ * x_h and material coordinates X_h.  Any output pointer may be NULL.
+ * precision selects FP64 or FP32 element arithmetic; outputs are FP64. */
+eolc_status eolc_forces_fill(eolc_ctx *ctx, const double *x_h,
+                             const double *X_h, const eolc_material *mat,
+                             const double grav[3], double h, int precision,
+                             double *f_h, double *M_h, double *MDK_h);
+
+/* ---- GeneralizedSolver::velocitySolve, pinned DOFs, no contacts ---------
+ * Solves argmin 1/2 v'MDK v + b'v  s.t. v[fixed_dofs[k]] = beq[k]
+ * (GeneralizedSolver.cpp:107-173 semantics with Aeq = unit rows,
+ * Constraints.cpp:114-119) using the MDK of the last eolc_forces_fill /
+ * eolc_step on this context.  v_h is the initial guess on input and the
+ * solution on output (3N values). */
+eolc_status eolc_velocity_solve(eolc_ctx *ctx, const double *b_h,
+                                const int *fixed_dofs_h, const double *beq_h,
+                                int n_fixed, const eolc_solve_opts *opts,
+                                double *v_h, eolc_solve_info *info);
+
+/* ---- Cloth::step (Cloth.cpp:359-413, non-EOL, no remeshing, no QP) -----
+ * One implicit-Euler step on host buffers: Forces::fill, pinned-corner
+ * equality rows beq = 0.99 v + c (Constraints.cpp:114-119,472-496),
+ * b = -(M v + h f) (Cloth.cpp:345), velocity solve, x += h v.
+ * x_h and v_h (3N each) are updated in place.
+ * fixed_dofs_h/fixed_vel_h: n_fixed DOF indices and their scripted
+ * velocity offsets c(i+3). */
+eolc_status eolc_step(eolc_ctx *ctx, double *x_h, const double *X_h,
+                      double *v_h, const eolc_material *mat,
+                      const double grav[3], double h,
+                      const int *fixed_dofs_h, const double *fixed_vel_h,
+                      int n_fixed, const eolc_solve_opts *opts,
+                      eolc_solve_info *info);
+
+/* Device-resident stepping: upload the state once, step n_steps times with
+ * x, v kept in HBM, download when needed.  Same semantics as eolc_step. */
+eolc_status eolc_state_upload(eolc_ctx *ctx, const double *x_h,
+                              const double *X_h, const double *v_h);
+eolc_status eolc_state_download(eolc_ctx *ctx, double *x_h, double *v_h);
+eolc_status eolc_step_resident(eolc_ctx *ctx, int n_steps,
+                               const eolc_material *mat, const double grav[3],
+                               double h, const int *fixed_dofs_h,
+                               const double *fixed_vel_h, int n_fixed,
+                               const eolc_solve_opts *opts,
+                               eolc_solve_info *info);
+
+/* ---- collisions (CD2, Collisions.cpp:55-78) ------------------------------ */
+
+/* Box obstacle: full dimensions dim[3] (Box::dim) and 4x4 frame E1
+ * (column-major, Box::E1). */
+typedef struct {
+  double dim[3];
+  double E1[16];
+} eolc_box;
+
+/* One contact, mirroring btc::Collision (boxTriCollision.h:49-110). */
+typedef struct {
+  double dist;
+  double nor1[3];
+  double nor2[3];
+  double pos1[3];
+  double pos2[3];
+  double pos1_[3];
+  double weights1[3];
+  double weights2[3];
+  double edge_dir[3];
+  int count1;
+  int count2;
+  int verts1[3];
+  int verts2[3];
+  int tri1;
+  int tri2;
+  int edge1[3];
+  int n_edge1; /* 0, 1 or 3 entries of edge1 are valid */
+  int edge2;
+  int source;  /* 0: point obstacles, 1 + b: box b */
+} eolc_contact;
+
+/* Contact set of CD2 for the current topology: point obstacles first
+ * (pointTriCollision, EOL=false), then each box in order
+ * (boxTriCollision, EOL=false).  x_h: cloth node positions (3N).
+ * points_h / normals_h: n_points x 3.  Writes at most capacity contacts;
+ * *n_out receives the total count (EOLC_CAPACITY if it exceeds capacity). */
+eolc_status eolc_cd2(eolc_ctx *ctx, const double *x_h, const eolc_box *boxes,
+                     int n_boxes, const double *points_h,
+                     const double *normals_h, int n_points, double threshold,
+                     eolc_contact *out_h, int capacity, int *n_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EOLC_H_ */

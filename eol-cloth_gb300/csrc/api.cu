@@ -1,0 +1,415 @@
+// C ABI of libeolc (include/eolc.h): context, topology, Forces::fill,
+// velocity solve and Cloth::step on one GPU.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+using namespace eolc;
+
+namespace {
+
+#define EOLC_CHECK_CUDA(ctx, expr)                                   \
+  do {                                                               \
+    cudaError_t e_ = (expr);                                         \
+    if (e_ != cudaSuccess) {                                         \
+      (ctx)->err = std::string(#expr ": ") + cudaGetErrorString(e_); \
+      return EOLC_CUDA_ERROR;                                        \
+    }                                                                \
+  } while (0)
+
+eolc_status fail(eolc_ctx *ctx, eolc_status s, const char *msg) {
+  if (ctx) ctx->err = msg;
+  return s;
+}
+
+MaterialD make_material(const eolc_material &m, const double g[3], double h) {
+  MaterialD d;
+  d.rho = m.density;
+  d.mu = m.e / (1 + m.nu) / 2;
+  d.lam = m.e * m.nu / ((1 + m.nu) * (1 - 2 * m.nu));
+  d.beta = m.beta;
+  d.dh2 = m.damping_b * h * h;  // ((damping(1) * h) * h), Forces.cpp:105
+  d.g[0] = g[0]; d.g[1] = g[1]; d.g[2] = g[2];
+  d.h = h;
+  return d;
+}
+
+// beq_k = (1 - 0.01) v[dof_k] + c_k (addFixed, Constraints.cpp:114-119)
+__global__ void pins_kernel(int n_fixed, const int *dofs, const double *c,
+                            const double *v, double *beq_full) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_fixed) return;
+  int d = dofs[k];
+  beq_full[d] = (1 - 0.01) * v[d] + c[k];
+}
+
+// node->x = node->x + h * node->v (Cloth.cpp:394-400)
+__global__ void integrate_kernel(int n, double h, const double *v, double *x) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = x[i] + h * v[i];
+}
+
+eolc_status need_topology(eolc_ctx *ctx) {
+  if (!ctx) return EOLC_BAD_ARG;
+  if (!ctx->has_topology) return fail(ctx, EOLC_NO_TOPOLOGY, "no topology set");
+  return EOLC_OK;
+}
+
+eolc_status check_opts(eolc_ctx *ctx, const eolc_solve_opts *o) {
+  if (!o) return fail(ctx, EOLC_BAD_ARG, "null solve options");
+  if (!(o->rel_tol > 0) || o->max_iter <= 0)
+    return fail(ctx, EOLC_BAD_ARG, "rel_tol must be > 0 and max_iter > 0");
+  if (o->precision != EOLC_PREC_FP64 && o->precision != EOLC_PREC_MIXED)
+    return fail(ctx, EOLC_BAD_ARG, "unknown precision");
+  if (o->precond < EOLC_PC_JACOBI || o->precond > EOLC_PC_LEARNED)
+    return fail(ctx, EOLC_BAD_ARG, "unknown preconditioner");
+  return EOLC_OK;
+}
+
+// Uploads the fixed DOF list when it changed; rebuilds the pinned mask.
+eolc_status set_pins(eolc_ctx *ctx, const int *dofs_h, const double *vel_h,
+                     int n_fixed, cudaStream_t s) {
+  int n = 3 * ctx->topo.n_nodes;
+  if (n_fixed < 0 || (n_fixed > 0 && !dofs_h)) return fail(ctx, EOLC_BAD_ARG, "bad fixed list");
+  std::vector<uint8_t> mask(n, 0);
+  for (int k = 0; k < n_fixed; ++k) {
+    if (dofs_h[k] < 0 || dofs_h[k] >= n) return fail(ctx, EOLC_BAD_ARG, "fixed dof out of range");
+    mask[dofs_h[k]] = 1;
+  }
+  EOLC_CHECK_CUDA(ctx, ctx->pinned.upload(mask.data(), n, s));
+  EOLC_CHECK_CUDA(ctx, ctx->fixed_dofs.upload(dofs_h, n_fixed, s));
+  if (vel_h) EOLC_CHECK_CUDA(ctx, ctx->fixed_vel.upload(vel_h, n_fixed, s));
+  ctx->n_fixed_dev = n_fixed;
+  EOLC_CHECK_CUDA(ctx, ctx->beq_full.resize(n));
+  return EOLC_OK;
+}
+
+eolc_status ensure_state(eolc_ctx *ctx) {
+  size_t n = size_t(ctx->topo.n_nodes) * 3;
+  size_t nb9 = size_t(ctx->topo.n_blocks) * 9;
+  EOLC_CHECK_CUDA(ctx, ctx->x.resize(n));
+  EOLC_CHECK_CUDA(ctx, ctx->v.resize(n));
+  EOLC_CHECK_CUDA(ctx, ctx->X.resize(size_t(ctx->topo.n_nodes) * 2));
+  EOLC_CHECK_CUDA(ctx, ctx->f.resize(n));
+  EOLC_CHECK_CUDA(ctx, ctx->b.resize(n));
+  EOLC_CHECK_CUDA(ctx, ctx->A32.resize(nb9));
+  EOLC_CHECK_CUDA(ctx, ctx->beq_full.resize(n));
+  (void)nb9;
+  return EOLC_OK;
+}
+
+// Assembles MDK (and f, b) for the device state x, X, v.
+eolc_status assemble(eolc_ctx *ctx, const eolc_material &mat, const double g[3],
+                     double h, int prec, bool want_M, bool want_b,
+                     cudaStream_t s) {
+  MaterialD md = make_material(mat, g, h);
+  size_t nb9 = size_t(ctx->topo.n_blocks) * 9;
+  if (prec == EOLC_PREC_FP64) EOLC_CHECK_CUDA(ctx, ctx->A64.resize(nb9));
+  if (want_M) EOLC_CHECK_CUDA(ctx, ctx->Mblk.resize(nb9));
+  launch_assemble_blocks(ctx->topo, ctx->x.p, ctx->X.p, md, prec,
+                         prec == EOLC_PREC_FP64 ? ctx->A64.p : nullptr,
+                         prec == EOLC_PREC_FP64 ? nullptr : ctx->A32.p,
+                         want_M ? ctx->Mblk.p : nullptr, s);
+  launch_forces_rhs(ctx->topo, ctx->x.p, ctx->X.p, ctx->v.p, md, prec,
+                    ctx->f.p, want_b ? ctx->b.p : nullptr, s);
+  EOLC_CHECK_CUDA(ctx, cudaGetLastError());
+  return EOLC_OK;
+}
+
+eolc_status solve_device(eolc_ctx *ctx, const eolc_solve_opts *o,
+                         eolc_solve_info *info, cudaStream_t s) {
+  PcgArgs a;
+  a.T = &ctx->topo;
+  a.A64 = ctx->A64.p;
+  a.A32 = ctx->A32.p;
+  a.b = ctx->b.p;
+  a.pinned = ctx->pinned.p;
+  a.beq_full = ctx->beq_full.p;
+  a.v = ctx->v.p;
+  a.precision = o->precision;
+  a.precond = o->precond == EOLC_PC_LEARNED ? EOLC_PC_JACOBI : o->precond;
+  a.rel_tol = o->rel_tol;
+  a.max_iter = o->max_iter;
+  a.learned = nullptr;
+  if (o->precision == EOLC_PREC_FP64 && !ctx->A64.p)
+    return fail(ctx, EOLC_BAD_ARG, "no FP64 matrix assembled");
+  eolc_solve_info local;
+  eolc_status st = run_pcg(ctx->work, a, info ? info : &local, s, ctx->err);
+  return st;
+}
+
+cudaStream_t stream_of(eolc_ctx *ctx) { return ctx->stream; }
+
+}  // namespace
+
+extern "C" {
+
+int eolc_version(void) { return 1; }
+
+eolc_status eolc_create(eolc_ctx **out, int device) {
+  if (!out) return EOLC_BAD_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n)
+    return EOLC_CUDA_ERROR;
+  auto *ctx = new (std::nothrow) eolc_ctx();
+  if (!ctx) return EOLC_CUDA_ERROR;
+  ctx->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return EOLC_CUDA_ERROR;
+  }
+  ctx->own_stream = true;
+  *out = ctx;
+  return EOLC_OK;
+}
+
+void eolc_destroy(eolc_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  free_solve_work(ctx->work);
+  free_collide_work(ctx->cd_work);
+  if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char *eolc_last_error(const eolc_ctx *ctx) {
+  return ctx ? ctx->err.c_str() : "null context";
+}
+
+eolc_status eolc_set_stream(eolc_ctx *ctx, void *stream) {
+  if (!ctx) return EOLC_BAD_ARG;
+  cudaSetDevice(ctx->device);
+  if (!stream) {
+    if (!ctx->own_stream) {
+      if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(ctx, EOLC_CUDA_ERROR, "stream creation failed");
+      ctx->own_stream = true;
+    }
+    return EOLC_OK;
+  }
+  if (ctx->own_stream && ctx->stream) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+  }
+  ctx->stream = static_cast<cudaStream_t>(stream);
+  ctx->own_stream = false;
+  return EOLC_OK;
+}
+
+eolc_status eolc_set_topology(eolc_ctx *ctx, int n_nodes, const int *tri_h,
+                              int n_tri, const int *hinge_h, int n_hinge) {
+  if (!ctx) return EOLC_BAD_ARG;
+  if (!tri_h || n_tri <= 0 || (n_hinge > 0 && !hinge_h))
+    return fail(ctx, EOLC_BAD_ARG, "null or empty topology");
+  cudaSetDevice(ctx->device);
+  HostTopology H;
+  std::string msg = build_topology(n_nodes, tri_h, n_tri, hinge_h, n_hinge, H);
+  if (!msg.empty()) return fail(ctx, EOLC_BAD_ARG, msg.c_str());
+  cudaStream_t s = stream_of(ctx);
+  DevTopology &T = ctx->topo;
+  T.n_nodes = H.n_nodes;
+  T.n_tri = H.n_tri;
+  T.n_hinge = H.n_hinge;
+  T.n_blocks = H.n_blocks;
+  EOLC_CHECK_CUDA(ctx, T.tri.upload(tri_h, size_t(n_tri) * 3, s));
+  if (n_hinge > 0) EOLC_CHECK_CUDA(ctx, T.hinge.upload(hinge_h, size_t(n_hinge) * 4, s));
+  EOLC_CHECK_CUDA(ctx, T.rowptr.upload(H.rowptr.data(), H.rowptr.size(), s));
+  EOLC_CHECK_CUDA(ctx, T.colidx.upload(H.colidx.data(), H.colidx.size(), s));
+  EOLC_CHECK_CUDA(ctx, T.blk_row.upload(H.blk_row.data(), H.blk_row.size(), s));
+  EOLC_CHECK_CUDA(ctx, T.diag.upload(H.diag.data(), H.diag.size(), s));
+  EOLC_CHECK_CUDA(ctx, T.cptr.upload(H.cptr.data(), H.cptr.size(), s));
+  EOLC_CHECK_CUDA(ctx, T.contrib.upload(H.contrib.data(), H.contrib.size(), s));
+  EOLC_CHECK_CUDA(ctx, T.nf_ptr.upload(H.nf_ptr.data(), H.nf_ptr.size(), s));
+  EOLC_CHECK_CUDA(ctx, T.nf_list.upload(H.nf_list.data(), H.nf_list.size(), s));
+  EOLC_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
+  ctx->host = std::move(H);
+  ctx->host_tri.assign(tri_h, tri_h + size_t(n_tri) * 3);
+  free_collide_work(ctx->cd_work);
+  ctx->cd_work = nullptr;
+  ctx->has_topology = true;
+  ctx->n_fixed_dev = -1;
+  free_solve_work(ctx->work);
+  ctx->work = nullptr;
+  ctx->A64.release();
+  ctx->Mblk.release();
+  eolc_status st = ensure_state(ctx);
+  if (st != EOLC_OK) return st;
+  EOLC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->v.p, 0, sizeof(double) * ctx->v.n, s));
+  EOLC_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
+  return EOLC_OK;
+}
+
+eolc_status eolc_bsr_pattern(eolc_ctx *ctx, int *n_blocks, int *rowptr_h,
+                             int *colidx_h) {
+  eolc_status st = need_topology(ctx);
+  if (st != EOLC_OK) return st;
+  if (n_blocks) *n_blocks = ctx->host.n_blocks;
+  if (rowptr_h)
+    std::memcpy(rowptr_h, ctx->host.rowptr.data(), sizeof(int) * ctx->host.rowptr.size());
+  if (colidx_h)
+    std::memcpy(colidx_h, ctx->host.colidx.data(), sizeof(int) * ctx->host.colidx.size());
+  return EOLC_OK;
+}
+
+eolc_status eolc_forces_fill(eolc_ctx *ctx, const double *x_h,
+                             const double *X_h, const eolc_material *mat,
+                             const double grav[3], double h, int precision,
+                             double *f_h, double *M_h, double *MDK_h) {
+  eolc_status st = need_topology(ctx);
+  if (st != EOLC_OK) return st;
+  if (!x_h || !X_h || !mat || !grav) return fail(ctx, EOLC_BAD_ARG, "null input");
+  if (precision != EOLC_PREC_FP64 && precision != EOLC_PREC_MIXED)
+    return fail(ctx, EOLC_BAD_ARG, "unknown precision");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = stream_of(ctx);
+  int N = ctx->topo.n_nodes;
+  size_t nb9 = size_t(ctx->topo.n_blocks) * 9;
+  EOLC_CHECK_CUDA(ctx, ctx->x.upload(x_h, size_t(N) * 3, s));
+  EOLC_CHECK_CUDA(ctx, ctx->X.upload(X_h, size_t(N) * 2, s));
+  st = assemble(ctx, *mat, grav, h, precision, M_h != nullptr, false, s);
+  if (st != EOLC_OK) return st;
+  if (f_h) EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(f_h, ctx->f.p, sizeof(double) * 3 * N,
+                                                cudaMemcpyDeviceToHost, s));
+  if (M_h) EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(M_h, ctx->Mblk.p, sizeof(double) * nb9,
+                                                cudaMemcpyDeviceToHost, s));
+  std::vector<float> tmp;
+  if (MDK_h) {
+    if (precision == EOLC_PREC_FP64) {
+      EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(MDK_h, ctx->A64.p, sizeof(double) * nb9,
+                                           cudaMemcpyDeviceToHost, s));
+    } else {
+      tmp.resize(nb9);
+      EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(tmp.data(), ctx->A32.p, sizeof(float) * nb9,
+                                           cudaMemcpyDeviceToHost, s));
+    }
+  }
+  EOLC_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
+  if (MDK_h && precision != EOLC_PREC_FP64)
+    for (size_t k = 0; k < nb9; ++k) MDK_h[k] = tmp[k];
+  ctx->last_precision = precision;
+  return EOLC_OK;
+}
+
+eolc_status eolc_velocity_solve(eolc_ctx *ctx, const double *b_h,
+                                const int *fixed_dofs_h, const double *beq_h,
+                                int n_fixed, const eolc_solve_opts *opts,
+                                double *v_h, eolc_solve_info *info) {
+  eolc_status st = need_topology(ctx);
+  if (st != EOLC_OK) return st;
+  if ((st = check_opts(ctx, opts)) != EOLC_OK) return st;
+  if (!b_h || !v_h || (n_fixed > 0 && !beq_h)) return fail(ctx, EOLC_BAD_ARG, "null input");
+  if (ctx->last_precision < 0) return fail(ctx, EOLC_BAD_ARG, "no matrix assembled");
+  if (opts->precision != ctx->last_precision)
+    return fail(ctx, EOLC_BAD_ARG, "solve precision differs from the assembled matrix");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = stream_of(ctx);
+  int n = 3 * ctx->topo.n_nodes;
+  if ((st = set_pins(ctx, fixed_dofs_h, nullptr, n_fixed, s)) != EOLC_OK) return st;
+  std::vector<double> beq_full(n, 0.0);
+  for (int k = 0; k < n_fixed; ++k) beq_full[fixed_dofs_h[k]] = beq_h[k];
+  EOLC_CHECK_CUDA(ctx, ctx->beq_full.upload(beq_full.data(), n, s));
+  EOLC_CHECK_CUDA(ctx, ctx->b.upload(b_h, n, s));
+  st = solve_device(ctx, opts, info, s);
+  EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(v_h, ctx->v.p, sizeof(double) * n,
+                                       cudaMemcpyDeviceToHost, s));
+  EOLC_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
+  return st;
+}
+
+eolc_status eolc_state_upload(eolc_ctx *ctx, const double *x_h,
+                              const double *X_h, const double *v_h) {
+  eolc_status st = need_topology(ctx);
+  if (st != EOLC_OK) return st;
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = stream_of(ctx);
+  int N = ctx->topo.n_nodes;
+  if (x_h) EOLC_CHECK_CUDA(ctx, ctx->x.upload(x_h, size_t(N) * 3, s));
+  if (X_h) EOLC_CHECK_CUDA(ctx, ctx->X.upload(X_h, size_t(N) * 2, s));
+  if (v_h) EOLC_CHECK_CUDA(ctx, ctx->v.upload(v_h, size_t(N) * 3, s));
+  EOLC_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
+  return EOLC_OK;
+}
+
+eolc_status eolc_state_download(eolc_ctx *ctx, double *x_h, double *v_h) {
+  eolc_status st = need_topology(ctx);
+  if (st != EOLC_OK) return st;
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = stream_of(ctx);
+  int N = ctx->topo.n_nodes;
+  if (x_h) EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(x_h, ctx->x.p, sizeof(double) * 3 * N,
+                                                cudaMemcpyDeviceToHost, s));
+  if (v_h) EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(v_h, ctx->v.p, sizeof(double) * 3 * N,
+                                                cudaMemcpyDeviceToHost, s));
+  EOLC_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
+  return EOLC_OK;
+}
+
+eolc_status eolc_step_resident(eolc_ctx *ctx, int n_steps,
+                               const eolc_material *mat, const double grav[3],
+                               double h, const int *fixed_dofs_h,
+                               const double *fixed_vel_h, int n_fixed,
+                               const eolc_solve_opts *opts,
+                               eolc_solve_info *info) {
+  eolc_status st = need_topology(ctx);
+  if (st != EOLC_OK) return st;
+  if ((st = check_opts(ctx, opts)) != EOLC_OK) return st;
+  if (!mat || !grav || n_steps < 0) return fail(ctx, EOLC_BAD_ARG, "bad step arguments");
+  if (n_fixed > 0 && (!fixed_dofs_h || !fixed_vel_h)) return fail(ctx, EOLC_BAD_ARG, "null fixed list");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = stream_of(ctx);
+  int n = 3 * ctx->topo.n_nodes;
+  if ((st = set_pins(ctx, fixed_dofs_h, fixed_vel_h, n_fixed, s)) != EOLC_OK) return st;
+  eolc_solve_info agg{};
+  for (int k = 0; k < n_steps; ++k) {
+    // pins from the velocity of the previous step (Constraints.cpp:472-496)
+    EOLC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->beq_full.p, 0, sizeof(double) * n, s));
+    if (n_fixed > 0)
+      pins_kernel<<<(n_fixed + 127) / 128, 128, 0, s>>>(n_fixed, ctx->fixed_dofs.p,
+                                                       ctx->fixed_vel.p, ctx->v.p,
+                                                       ctx->beq_full.p);
+    st = assemble(ctx, *mat, grav, h, opts->precision, false, true, s);
+    if (st != EOLC_OK) return st;
+    ctx->last_precision = opts->precision;
+    eolc_solve_info si{};
+    st = solve_device(ctx, opts, &si, s);
+    agg.iterations += si.iterations;
+    agg.refinements += si.refinements;
+    agg.rel_res = si.rel_res;
+    agg.status = si.status;
+    if (st != EOLC_OK) {
+      if (info) *info = agg;
+      return st;
+    }
+    integrate_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, h, ctx->v.p, ctx->x.p);
+  }
+  EOLC_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
+  if (info) *info = agg;
+  return EOLC_OK;
+}
+
+eolc_status eolc_step(eolc_ctx *ctx, double *x_h, const double *X_h,
+                      double *v_h, const eolc_material *mat,
+                      const double grav[3], double h,
+                      const int *fixed_dofs_h, const double *fixed_vel_h,
+                      int n_fixed, const eolc_solve_opts *opts,
+                      eolc_solve_info *info) {
+  if (!x_h || !X_h || !v_h) return fail(ctx, EOLC_BAD_ARG, "null state");
+  eolc_status st = eolc_state_upload(ctx, x_h, X_h, v_h);
+  if (st != EOLC_OK) return st;
+  st = eolc_step_resident(ctx, 1, mat, grav, h, fixed_dofs_h, fixed_vel_h,
+                          n_fixed, opts, info);
+  if (st != EOLC_OK) return st;
+  return eolc_state_download(ctx, x_h, v_h);
+}
+
+}  // extern "C"

@@ -1,0 +1,139 @@
+// Internal declarations of libeolc (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/eolc.h"
+
+namespace eolc {
+
+// ---- device buffer --------------------------------------------------------
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t resize(size_t m) {
+    if (m == n && p) return cudaSuccess;
+    release();
+    if (m == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, m * sizeof(T));
+    if (e == cudaSuccess) n = m;
+    return e;
+  }
+  cudaError_t upload(const T *h, size_t m, cudaStream_t s) {
+    cudaError_t e = resize(m);
+    if (e != cudaSuccess || m == 0) return e;
+    return cudaMemcpyAsync(p, h, m * sizeof(T), cudaMemcpyHostToDevice, s);
+  }
+};
+
+// Contribution code of one element to one 3x3 block:
+//   bits 0-1: local vertex of the block's column, bits 2-3: local vertex of
+//   the block's row, bit 4: 0 = triangle (membrane + inertia),
+//   1 = hinge (bending), bits 5-31: element index.
+constexpr int kHingeBit = 1 << 4;
+__host__ __device__ inline int contrib_code(int elem, bool hinge, int lrow,
+                                            int lcol) {
+  return (elem << 5) | (hinge ? kHingeBit : 0) | (lrow << 2) | lcol;
+}
+
+// ---- topology (host build; topology.cpp) ------------------------------------
+struct HostTopology {
+  int n_nodes = 0, n_tri = 0, n_hinge = 0, n_blocks = 0;
+  std::vector<int> rowptr;   // n_nodes + 1
+  std::vector<int> colidx;   // n_blocks
+  std::vector<int> blk_row;  // n_blocks
+  std::vector<int> diag;     // n_nodes: block index of (i, i)
+  std::vector<int> cptr;     // n_blocks + 1
+  std::vector<int> contrib;  // contribution codes, faces first then hinges
+  std::vector<int> nf_ptr;   // n_nodes + 1
+  std::vector<int> nf_list;  // (face << 2) | local vertex
+};
+
+// Returns an empty string on success, else a message.
+std::string build_topology(int n_nodes, const int *tri, int n_tri,
+                           const int *hinge, int n_hinge, HostTopology &out);
+
+// ---- device state -----------------------------------------------------------
+struct DevTopology {
+  int n_nodes = 0, n_tri = 0, n_hinge = 0, n_blocks = 0;
+  DevBuf<int> tri, hinge, rowptr, colidx, blk_row, diag, cptr, contrib,
+      nf_ptr, nf_list;
+};
+
+struct MaterialD {
+  double rho, mu, lam, beta, dh2;  // dh2 = damping_b * h * h
+  double g[3];
+  double h;
+};
+
+// Kernel launchers (assemble.cu)
+void launch_assemble_blocks(const DevTopology &T, const double *x,
+                            const double *X, const MaterialD &m, int prec,
+                            double *A64, float *A32, double *Mblk,
+                            cudaStream_t s);
+void launch_forces_rhs(const DevTopology &T, const double *x, const double *X,
+                       const double *v, const MaterialD &m, int prec,
+                       double *f, double *b, cudaStream_t s);
+
+// Solver (pcg.cu)
+struct SolveWork;
+struct PcgArgs {
+  const DevTopology *T;
+  const double *A64;  // may be null in mixed mode (A32 promoted instead)
+  const float *A32;
+  const double *b;    // 3N rhs of the unconstrained system (b of Cloth.cpp)
+  const uint8_t *pinned;  // 3N mask
+  const double *beq_full; // 3N: beq on pinned DOFs, 0 elsewhere
+  double *v;          // 3N in: guess, out: solution
+  int precision, precond;
+  double rel_tol;
+  int max_iter;
+  const float *learned;  // learned approximate inverse blocks (n_blocks*9)
+};
+eolc_status run_pcg(SolveWork *&w, const PcgArgs &a, eolc_solve_info *info,
+                    cudaStream_t s, std::string &err);
+void free_solve_work(SolveWork *w);
+
+// Collisions (collide.cu)
+struct CollideWork;
+void free_collide_work(CollideWork *w);
+
+}  // namespace eolc
+
+// ---- the context ------------------------------------------------------------
+struct eolc_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  bool has_topology = false;
+  eolc::HostTopology host;
+  eolc::DevTopology topo;
+  // state and per-step buffers
+  eolc::DevBuf<double> x, X, v, f, b, A64, Mblk, beq_full;
+  eolc::DevBuf<float> A32;
+  eolc::DevBuf<uint8_t> pinned;
+  eolc::DevBuf<int> fixed_dofs;
+  eolc::DevBuf<double> fixed_vel;
+  int n_fixed_dev = -1;
+  eolc::SolveWork *work = nullptr;
+  int last_jacobi_iters = 0;
+  int last_precision = -1;  // precision of the last assembled MDK
+  std::vector<int> host_tri;  // triangle list of the current topology
+  eolc::CollideWork *cd_work = nullptr;
+};

@@ -1,0 +1,348 @@
+"""Python front end of libeolc.so (the GB300 hot path of EOL-Cloth).
+
+Two layers:
+  * Context: a thin ctypes binding of the C ABI in include/eolc.h.
+  * Forces / GeneralizedSolver / Cloth / CD2: the reference's call surface
+    (src/Forces.h:26-45, src/GeneralizedSolver.h:26-30, src/Cloth.h:75-76,
+    src/Collisions.h:9-11) on top of it, with numpy/scipy containers where
+    the reference has Eigen ones.
+
+There is no CPU fallback: importing this module without a built
+libeolc.so raises, and every call goes to the GPU.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libeolc.so")
+
+OK, NOT_CONVERGED, BREAKDOWN, NONFINITE, TIMEOUT, BAD_ARG, CUDA_ERROR, CAPACITY, NO_TOPOLOGY = range(9)
+PREC_FP64, PREC_MIXED = 0, 1
+PC_JACOBI, PC_BLOCK_JACOBI, PC_LEARNED = 0, 1, 2
+STATUS_NAMES = ["OK", "NOT_CONVERGED", "BREAKDOWN", "NONFINITE", "TIMEOUT", "BAD_ARG",
+                "CUDA_ERROR", "CAPACITY", "NO_TOPOLOGY"]
+
+
+class EolcError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (STATUS_NAMES[status] if 0 <= status < 9 else status, msg))
+        self.status = status
+
+
+class Material(ctypes.Structure):
+    """src/Cloth.h:28-35."""
+    _fields_ = [("density", ctypes.c_double), ("e", ctypes.c_double), ("nu", ctypes.c_double),
+                ("beta", ctypes.c_double), ("damping_a", ctypes.c_double),
+                ("damping_b", ctypes.c_double)]
+
+    def __init__(self, density=0.05, e=50.0, nu=0.01, beta=1e-5, damping=(0.0, 1.0)):
+        # defaults of load_matset (parseParams.cpp:193-201)
+        super().__init__(density, e, nu, beta, damping[0], damping[1])
+
+
+class SolveOpts(ctypes.Structure):
+    _fields_ = [("rel_tol", ctypes.c_double), ("max_iter", ctypes.c_int),
+                ("precision", ctypes.c_int), ("precond", ctypes.c_int),
+                ("fallback_factor", ctypes.c_int)]
+
+    def __init__(self, rel_tol=1e-8, max_iter=100000, precision=PREC_MIXED,
+                 precond=PC_JACOBI, fallback_factor=2):
+        super().__init__(rel_tol, max_iter, precision, precond, fallback_factor)
+
+
+class SolveInfo(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("iterations", ctypes.c_int),
+                ("refinements", ctypes.c_int), ("used_fallback", ctypes.c_int),
+                ("rel_res", ctypes.c_double)]
+
+
+class Box(ctypes.Structure):
+    """Box obstacle: full dimensions and 4x4 frame (column-major)."""
+    _fields_ = [("dim", ctypes.c_double * 3), ("E1", ctypes.c_double * 16)]
+
+    def __init__(self, dim, E1):
+        super().__init__((ctypes.c_double * 3)(*list(dim)), (ctypes.c_double * 16)(*list(E1)))
+
+
+class Contact(ctypes.Structure):
+    """eolc_contact, mirroring btc::Collision (boxTriCollision.h:49-110)."""
+    _fields_ = [
+        ("dist", ctypes.c_double), ("nor1", ctypes.c_double * 3), ("nor2", ctypes.c_double * 3),
+        ("pos1", ctypes.c_double * 3), ("pos2", ctypes.c_double * 3),
+        ("pos1_", ctypes.c_double * 3), ("weights1", ctypes.c_double * 3),
+        ("weights2", ctypes.c_double * 3), ("edge_dir", ctypes.c_double * 3),
+        ("count1", ctypes.c_int), ("count2", ctypes.c_int), ("verts1", ctypes.c_int * 3),
+        ("verts2", ctypes.c_int * 3), ("tri1", ctypes.c_int), ("tri2", ctypes.c_int),
+        ("edge1", ctypes.c_int * 3), ("n_edge1", ctypes.c_int), ("edge2", ctypes.c_int),
+        ("source", ctypes.c_int)]
+
+
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int)
+_V = ctypes.c_void_p
+
+# Every symbol the C ABI exports (include/eolc.h).
+EXPORTS = ["eolc_version", "eolc_create", "eolc_destroy", "eolc_last_error", "eolc_set_stream",
+           "eolc_set_topology", "eolc_bsr_pattern", "eolc_forces_fill", "eolc_velocity_solve",
+           "eolc_step", "eolc_state_upload", "eolc_state_download", "eolc_step_resident",
+           "eolc_cd2"]
+
+
+def load_library(path=LIB_PATH):
+    if not os.path.exists(path):
+        raise ImportError("libeolc.so is not built (%s); run __graft_entry__.build()" % path)
+    L = ctypes.CDLL(path)
+    L.eolc_version.restype = ctypes.c_int
+    L.eolc_create.argtypes = [ctypes.POINTER(_V), ctypes.c_int]
+    L.eolc_destroy.argtypes = [_V]
+    L.eolc_destroy.restype = None
+    L.eolc_last_error.argtypes = [_V]
+    L.eolc_last_error.restype = ctypes.c_char_p
+    L.eolc_set_stream.argtypes = [_V, _V]
+    L.eolc_set_topology.argtypes = [_V, ctypes.c_int, _I, ctypes.c_int, _I, ctypes.c_int]
+    L.eolc_bsr_pattern.argtypes = [_V, _I, _I, _I]
+    L.eolc_forces_fill.argtypes = [_V, _D, _D, ctypes.POINTER(Material), _D, ctypes.c_double,
+                                   ctypes.c_int, _D, _D, _D]
+    L.eolc_velocity_solve.argtypes = [_V, _D, _I, _D, ctypes.c_int, ctypes.POINTER(SolveOpts),
+                                      _D, ctypes.POINTER(SolveInfo)]
+    L.eolc_step.argtypes = [_V, _D, _D, _D, ctypes.POINTER(Material), _D, ctypes.c_double, _I,
+                            _D, ctypes.c_int, ctypes.POINTER(SolveOpts),
+                            ctypes.POINTER(SolveInfo)]
+    L.eolc_state_upload.argtypes = [_V, _D, _D, _D]
+    L.eolc_state_download.argtypes = [_V, _D, _D]
+    L.eolc_step_resident.argtypes = [_V, ctypes.c_int, ctypes.POINTER(Material), _D,
+                                     ctypes.c_double, _I, _D, ctypes.c_int,
+                                     ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveInfo)]
+    L.eolc_cd2.argtypes = [_V, _D, ctypes.POINTER(Box), ctypes.c_int, _D, _D, ctypes.c_int,
+                           ctypes.c_double, ctypes.POINTER(Contact), ctypes.c_int, _I]
+    for name in EXPORTS:
+        if not hasattr(L, name):
+            raise ImportError("libeolc.so lacks %s" % name)
+        getattr(L, name).restype = getattr(L, name).restype
+    for name in EXPORTS:
+        if name not in ("eolc_version", "eolc_destroy", "eolc_last_error"):
+            getattr(L, name).restype = ctypes.c_int
+    return L
+
+
+lib = load_library()
+
+
+def _d(a):
+    return a.ctypes.data_as(_D)
+
+
+def _i(a):
+    return a.ctypes.data_as(_I)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class Context:
+    """One device, one stream, one topology."""
+
+    def __init__(self, device=0):
+        h = _V()
+        st = lib.eolc_create(ctypes.byref(h), device)
+        if st != OK:
+            raise EolcError(st, "eolc_create(%d) failed" % device)
+        self._h = h
+        self.n_nodes = 0
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib.eolc_destroy(self._h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _check(self, st):
+        if st != OK:
+            raise EolcError(st, lib.eolc_last_error(self._h).decode())
+
+    def set_topology(self, n_nodes, tri, hinge):
+        tri, hinge = _i32(tri), _i32(hinge)
+        self._tri = tri
+        self._check(lib.eolc_set_topology(self._h, n_nodes, _i(tri), len(tri.reshape(-1, 3)),
+                                          _i(hinge), len(hinge.reshape(-1, 4))))
+        self.n_nodes = n_nodes
+
+    def bsr_pattern(self):
+        nb = ctypes.c_int()
+        self._check(lib.eolc_bsr_pattern(self._h, ctypes.byref(nb), None, None))
+        rp = np.zeros(self.n_nodes + 1, np.int32)
+        ci = np.zeros(nb.value, np.int32)
+        self._check(lib.eolc_bsr_pattern(self._h, None, _i(rp), _i(ci)))
+        return rp, ci
+
+    def forces_fill(self, x, X, mat, grav, h, precision=PREC_FP64, want_M=True):
+        """Forces::fill: returns f (3N), M and MDK BSR values (n_blocks x 9)."""
+        x, X, g = _f64(x), _f64(X), _f64(grav)
+        nb = len(self.bsr_pattern()[1])
+        f = np.zeros(3 * self.n_nodes)
+        M = np.zeros(nb * 9) if want_M else None
+        MDK = np.zeros(nb * 9)
+        self._check(lib.eolc_forces_fill(self._h, _d(x), _d(X), ctypes.byref(mat), _d(g), h,
+                                         precision, _d(f), _d(M) if want_M else None, _d(MDK)))
+        return f, M, MDK
+
+    def velocity_solve(self, b, fixed_dofs, beq, opts=None, v0=None):
+        opts = opts or SolveOpts()
+        b, fixed_dofs, beq = _f64(b), _i32(fixed_dofs), _f64(beq)
+        v = np.zeros(3 * self.n_nodes) if v0 is None else _f64(v0).copy()
+        info = SolveInfo()
+        st = lib.eolc_velocity_solve(self._h, _d(b), _i(fixed_dofs), _d(beq), len(fixed_dofs),
+                                     ctypes.byref(opts), _d(v), ctypes.byref(info))
+        self._check(st)
+        return v, info
+
+    def step(self, x, X, v, mat, grav, h, fixed_dofs, fixed_vel, opts=None):
+        """Cloth::step on host arrays; x, v updated in place."""
+        opts = opts or SolveOpts()
+        assert x.dtype == np.float64 and v.dtype == np.float64
+        assert x.flags.c_contiguous and v.flags.c_contiguous
+        X, g = _f64(X), _f64(grav)
+        fixed_dofs, fixed_vel = _i32(fixed_dofs), _f64(fixed_vel)
+        info = SolveInfo()
+        st = lib.eolc_step(self._h, _d(x), _d(X), _d(v), ctypes.byref(mat), _d(g), h,
+                           _i(fixed_dofs), _d(fixed_vel), len(fixed_dofs), ctypes.byref(opts),
+                           ctypes.byref(info))
+        self._check(st)
+        return info
+
+    def state_upload(self, x, X, v):
+        self._check(lib.eolc_state_upload(self._h, _d(_f64(x)), _d(_f64(X)), _d(_f64(v))))
+
+    def state_download(self):
+        x = np.zeros(3 * self.n_nodes); v = np.zeros(3 * self.n_nodes)
+        self._check(lib.eolc_state_download(self._h, _d(x), _d(v)))
+        return x, v
+
+    def step_resident(self, n_steps, mat, grav, h, fixed_dofs, fixed_vel, opts=None):
+        opts = opts or SolveOpts()
+        fixed_dofs, fixed_vel = _i32(fixed_dofs), _f64(fixed_vel)
+        info = SolveInfo()
+        st = lib.eolc_step_resident(self._h, n_steps, ctypes.byref(mat), _d(_f64(grav)), h,
+                                    _i(fixed_dofs), _d(fixed_vel), len(fixed_dofs),
+                                    ctypes.byref(opts), ctypes.byref(info))
+        self._check(st)
+        return info
+
+    def cd2(self, x, boxes=(), points=None, normals=None, threshold=1e-3, capacity=None):
+        """CD2 contact list (point obstacles first, then each box)."""
+        x = _f64(x)
+        boxes = list(boxes)
+        barr = (Box * max(1, len(boxes)))(*boxes)
+        pts = _f64(points) if points is not None else np.zeros(3)
+        nrm = _f64(normals) if normals is not None else np.zeros(3)
+        npts = 0 if points is None else len(pts.reshape(-1, 3))
+        cap = capacity if capacity is not None else 4 * self.n_nodes + 64
+        out = (Contact * max(1, cap))()
+        n = ctypes.c_int()
+        st = lib.eolc_cd2(self._h, _d(x), barr, len(boxes), _d(pts), _d(nrm), npts, threshold,
+                          out, cap, ctypes.byref(n))
+        if st == CAPACITY and capacity is None:
+            return self.cd2(x, boxes, points, normals, threshold, capacity=n.value)
+        self._check(st)
+        return [out[k] for k in range(n.value)]
+
+
+def bsr_to_csr(ctx, vals):
+    """3x3 BSR values (n_blocks x 9, row-major blocks) -> scipy CSR."""
+    import scipy.sparse as sp
+    rp, ci = ctx.bsr_pattern()
+    return sp.bsr_matrix((np.asarray(vals).reshape(-1, 3, 3), ci, rp),
+                         shape=(3 * ctx.n_nodes, 3 * ctx.n_nodes)).tocsr()
+
+
+_CONTACT_FIELDS = [f[0] for f in Contact._fields_]
+
+
+def contact_tuple(c):
+    out = []
+    for name in _CONTACT_FIELDS:
+        v = getattr(c, name)
+        if hasattr(v, "__len__"):
+            out.append(tuple(np.asarray(list(v)).view(np.int64 if isinstance(v[0], float) else np.int32).tolist()
+                             if isinstance(v[0], float) else list(v)))
+        else:
+            out.append(np.float64(v).view(np.int64).item() if isinstance(v, float) else v)
+    return tuple(tuple(o) if isinstance(o, list) else o for o in out)
+
+
+def contacts_equal(a, b):
+    """Bitwise equality of two contact lists (order included)."""
+    if len(a) != len(b):
+        return False
+    return all(contact_tuple(x) == contact_tuple(y) for x, y in zip(a, b))
+
+
+# ---------------------------------------------------------------------------
+# Reference call surface
+# ---------------------------------------------------------------------------
+class Forces:
+    """Forces (src/Forces.h:26-45): fill() computes f, M and MDK on the GPU."""
+
+    def __init__(self, ctx, precision=PREC_FP64):
+        self.ctx = ctx
+        self.precision = precision
+        self.f = None
+        self.M = None
+        self.MDK = None
+
+    def fill(self, x, X, mat, grav, h):
+        """Forces::fill (Forces.cpp:912-930) for node positions x and
+        material coordinates X of the context's topology."""
+        f, M, MDK = self.ctx.forces_fill(x, X, mat, grav, h, self.precision)
+        self.f = f
+        self.M = bsr_to_csr(self.ctx, M)
+        self.MDK = bsr_to_csr(self.ctx, MDK)
+
+
+class GeneralizedSolver:
+    """GeneralizedSolver (src/GeneralizedSolver.h): velocitySolve on the GPU
+    for the equality-constrained case; contact QPs stay on the host."""
+
+    def __init__(self, ctx, opts=None):
+        self.ctx = ctx
+        self.opts = opts or SolveOpts()
+        self.last_info = None
+
+    def velocitySolve(self, fixedPoints, collisions, MDK, b, Aeq, beq, Aineq, bineq, v):
+        """Same arguments as GeneralizedSolver::velocitySolve
+        (GeneralizedSolver.cpp:107-173).  MDK must be the matrix of the
+        context's last fill (it stays resident on the GPU).  Aeq must consist
+        of unit rows (pinned DOFs, Constraints.cpp:114-119).  With contact
+        rows the reference hands a QP to Mosek/Gurobi; that stays on the
+        host, so collisions=True raises.  v is overwritten in place."""
+        if collisions:
+            raise EolcError(BAD_ARG, "contact QP is solved on the host, not by this library")
+        import scipy.sparse as sp
+        fixed = np.zeros(0, np.int32)
+        beqv = np.zeros(0)
+        if fixedPoints and Aeq is not None and Aeq.shape[0] > 0:
+            A = sp.csr_matrix(Aeq)
+            if np.any(np.diff(A.indptr) != 1) or np.any(A.data != 1.0):
+                raise EolcError(BAD_ARG, "Aeq must consist of unit rows")
+            fixed = A.indices.astype(np.int32)
+            beqv = np.asarray(beq, dtype=np.float64)
+        out, info = self.ctx.velocity_solve(b, fixed, beqv, self.opts)
+        v[:] = out
+        self.last_info = info
+        return info.status == OK
+
+
+def CD2(ctx, x, boxes=(), points=None, normals=None, threshold=1e-3):
+    """CD2 (Collisions.cpp:55-78): contacts of the cloth (context topology,
+    positions x) with point obstacles and boxes, in the reference's order."""
+    return ctx.cd2(x, boxes, points, normals, threshold)

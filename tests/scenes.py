@@ -1,0 +1,65 @@
+"""Seeded synthetic scenes with the shapes of the benchmark configurations.
+
+The reference ships no scenes with the benchmark sizes and no datasets; these
+generators build the same meshes (two-triangle grids of the stated node and
+triangle counts, the reference's corner pins and material) so tests, smoke()
+and bench.py all run the same workloads.
+"""
+import numpy as np
+
+import oracle as O
+
+GRAV = [0.0, 0.0, -9.8]
+H = 5e-3
+
+
+def material_c1():
+    """Configuration 1 material: rho 0.1, E 50, nu 0.3, beta 1e-5, damping (0, 1)."""
+    return dict(density=0.1, e=50.0, nu=0.3, beta=1e-5, damping=(0.0, 1.0))
+
+
+def sheet(quads, pins=(3, 4)):
+    """Unit square sheet of quads x quads two-triangle quads, pinned at the
+    named corners (ids of parseParams.cpp:298-305, all three axes, zero
+    scripted velocity)."""
+    r = quads + 1
+    x, X, tri = O.grid2(r, r)
+    hinge = O.hinges(r * r, tri)
+    ids = O.corner_ids(r, r)
+    fixed = np.array([3 * ids[k] + c for k in pins for c in range(3)], np.int32)
+    return dict(x=x, X=X, tri=tri, hinge=hinge, fixed=fixed,
+                fixed_vel=np.zeros(len(fixed)), n=r * r)
+
+
+def drape_positions(quads, steps, seed=7, jitter=1e-4, box_dim=(0.4, 0.4, 0.2),
+                    gap=0.05, threshold=1e-3):
+    """Kinematic drape of a quads x quads sheet over an axis-aligned box whose
+    top face starts `gap` below the sheet: the sheet sinks through the top face
+    while its outer part bends down over the box edges, so the three contact
+    kinds (cloth vertex / box face, box corner / cloth face, edge / edge)
+    all occur.  Each snapshot is jittered N(0, jitter) from a seeded
+    generator.  Returns (x0, X, tri, box_center, snapshots)."""
+    r = quads + 1
+    x0, X, tri = O.grid2(r, r)
+    rng = np.random.default_rng(seed)
+    xy = x0.reshape(-1, 3)[:, :2]
+    half = np.array(box_dim[:2]) / 2
+    c = np.array([0.5, 0.5])
+    d_out = np.linalg.norm(np.maximum(np.abs(xy - c) - half, 0.0), axis=1)
+    top = -gap
+    center = [0.5, 0.5, top - box_dim[2] / 2]
+    snaps = []
+    for k in range(steps):
+        t = k / max(1, steps - 1)
+        # approach during the first quarter, then hover within +-4 thresholds
+        # of the top face while the outer part folds down over the edges
+        if t < 0.25:
+            lift = gap * (1 - 4 * t) ** 2 + 4 * threshold
+        else:
+            lift = 4 * threshold * np.cos(9 * np.pi * (t - 0.25))
+        z = top + lift - 1.5 * d_out * min(1.0, 2 * t)
+        x = x0.copy().reshape(-1, 3)
+        x[:, 2] = z
+        x = x.ravel() + rng.normal(0.0, jitter, x.size)
+        snaps.append(x)
+    return x0, X, tri, center, snaps

@@ -1,0 +1,312 @@
+"""Steps/s of the EOL-Cloth hot path on a 256x256-quad sheet (GB300).
+
+Workload (the headline configuration): a 1 m square sheet of 256 x 256
+two-triangle quads (66,049 nodes, 131,072 triangles, 196,096 bending hinges,
+198,147 DOF, 852,481 3x3 blocks), corners 3 and 4 pinned, gravity -9.8,
+h = 5e-3, density 0.1, E = 50, nu = 0.3, bending 1e-5.  One step = the
+reference's Cloth::step for this scene: BSR assembly of M/MDK and f,
+pinned-corner rows, b = -(M v + h f), the velocity solve to an FP64 relative
+residual of 1e-8, and x += h v.  Steps continue one trajectory from rest.
+
+Arms:
+  (default)          this library, one GPU per rank (the sheet does not
+                     shard: N > 1 runs independent replicas, scaling "weak").
+  --impl reference   the reference's algorithm on the host cores: the CPU
+                     oracle (reference element math restated, triplet
+                     assembly, Eigen-style Jacobi CG in FP64), single thread
+                     as the reference is; each step is one full step.
+
+Timing: W warm-up steps, then K steps each bracketed by CUDA events on the
+library's stream, with L2 flushed (a 256 MiB write) before every step and
+outside the timed interval; max over ranks.  `e2e` runs the same steps
+through the host-buffer call eolc_step (H2D of x, X, v and D2H of x, v inside
+the timed region).  The roofline entry is for the PCG kernel, which
+dominates the step.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for sub in ("eol-cloth_gb300", "tests"):
+    sys.path.insert(0, os.path.join(ROOT, sub))
+
+METRIC = "steps/s @256^2 sheet: learned-PCG vs Jacobi-PCG on same GPU, rel-res 1e-8"
+QUADS = 256
+
+
+def scene(quads):
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O  # mesh builders only (topology input, not the path)
+    r = quads + 1
+    x, X, tri = O.grid2(r, r)
+    hinge = O.hinges(r * r, tri)
+    ids = O.corner_ids(r, r)
+    fixed = np.array([3 * ids[k] + c for k in (3, 4) for c in range(3)], np.int32)
+    return dict(x=x, X=X, tri=tri, hinge=hinge, fixed=fixed, fixed_vel=np.zeros(len(fixed)),
+                n=r * r)
+
+
+MAT = dict(density=0.1, e=50.0, nu=0.3, beta=1e-5, damping=(0.0, 1.0))
+GRAV = [0.0, 0.0, -9.8]
+H = 5e-3
+
+
+def algorithmic_bytes_per_iter(n_nodes, n_blocks):
+    """One Jacobi-PCG iteration: SpMV (FP32 block values + int32 column
+    index per block + row pointers + input and output 3-vectors) plus 14
+    passes over FP32 3-vectors."""
+    spmv = n_blocks * (36 + 4) + (n_nodes + 1) * 4 + 2 * n_nodes * 12
+    return spmv + 14 * n_nodes * 12
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = threading.Thread(target=self._run, daemon=True)
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index),
+                                      "--query-gpu=" + self.FIELDS,
+                                      "--format=csv,noheader,nounits"],
+                                     capture_output=True, text=True, timeout=5).stdout
+                vals = [v.strip() for v in out.strip().split(",")]
+                if len(vals) == 7:
+                    self.samples.append(vals)
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4)
+                          if s[3 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons}
+
+
+def cpu_step_seconds(sc, x, v, max_seconds=40.0):
+    """One oracle step (assembly + Jacobi CG to 1e-8 + update) on this state."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O  # the CPU baseline leg: the oracle is the thing timed here
+    mat = O.material(**MAT)
+    t0 = time.perf_counter()
+    F = O.Forces(x, sc["X"], sc["tri"], sc["hinge"], mat, GRAV, H)
+    b = F.rhs(v, H)
+    beq = (1 - 0.01) * v[sc["fixed"]] + sc["fixed_vel"]
+    vn, it, rr = F.solve(b, sc["fixed"], beq, tol=1e-8)
+    _ = x + H * vn
+    return time.perf_counter() - t0, it
+
+
+def run_reference(args, rank):
+    import numpy as np
+    if rank != 0:
+        return
+    sc = scene(QUADS)
+    x, v = sc["x"].copy(), np.zeros(3 * sc["n"])
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    mat = O.material(**MAT)
+    times, iters = [], []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        it, rr = O.step(x, sc["X"], v, sc["tri"], sc["hinge"], mat, GRAV, H, sc["fixed"],
+                        sc["fixed_vel"], tol=1e-8)
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            times.append(dt)
+            iters.append(it)
+    total = sum(times)
+    val = args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "sheet 256x256 quads, 66049 nodes, 131072 tris, 2 corners pinned,"
+                               " Jacobi CG to rel-res 1e-8, from rest",
+                   "solver": "jacobi-cg", "mean_cg_iters": statistics.mean(iters)},
+        "cpu_baseline": {"value": val, "unit": "steps/s", "cores": 1, "kind": "port",
+                         "sample": "%d full steps after %d warm-up steps, one thread "
+                                   "(the reference is single-threaded)" % (args.steps, args.warmup)},
+        "e2e": {"value": val, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+    import eolc
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    sc = scene(QUADS)
+    ctx = eolc.Context(local_rank)
+    stream = torch.cuda.Stream(device=dev)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_topology(sc["n"], sc["tri"], sc["hinge"])
+    mat = eolc.Material(**MAT)
+    precond = {"jacobi": eolc.PC_JACOBI, "block": eolc.PC_BLOCK_JACOBI,
+               "learned": eolc.PC_LEARNED}[args.precond]
+    opts = eolc.SolveOpts(rel_tol=1e-8, precision=eolc.PREC_MIXED, precond=precond)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > L2
+    n_blocks = len(ctx.bsr_pattern()[1])
+
+    ctx.state_upload(sc["x"], sc["X"], np.zeros(3 * sc["n"]))
+    ctx.step_resident(args.warmup, mat, GRAV, H, sc["fixed"], sc["fixed_vel"], opts)
+    x_w, v_w = ctx.state_download()  # post-warm-up state (also the e2e start)
+
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    step_ms, kern_ms, iters, asm_ms = [], [], [], []
+    launches0 = ctx.launch_count()
+    with ClockSampler(local_rank) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            info = ctx.step_resident(1, mat, GRAV, H, sc["fixed"], sc["fixed_vel"], opts)
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+            kern_ms.append(info.solve_kernel_ms)
+            asm_ms.append(info.assemble_ms)
+            iters.append(info.iterations)
+    torch.cuda.synchronize()
+    launches = ctx.launch_count() - launches0
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = t.item()
+        torch.distributed.barrier()
+    value = world * args.steps / (total_ms / 1e3)
+
+    # e2e: the same steps through eolc_step with pinned host buffers
+    xh = torch.empty(3 * sc["n"], dtype=torch.float64).pin_memory().numpy()
+    vh = torch.empty(3 * sc["n"], dtype=torch.float64).pin_memory().numpy()
+    Xh = torch.empty(2 * sc["n"], dtype=torch.float64).pin_memory().numpy()
+    xh[:] = x_w; vh[:] = v_w; Xh[:] = sc["X"]
+    e2e_ms = []
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.step(xh, Xh, vh, mat, GRAV, H, sc["fixed"], sc["fixed_vel"], opts)
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    e2e_total = sum(e2e_ms)
+    if world > 1:
+        t = torch.tensor([e2e_total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_total = t.item()
+    e2e_val = world * args.steps / (e2e_total / 1e3)
+
+    if rank != 0:
+        return
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    bpi = algorithmic_bytes_per_iter(sc["n"], n_blocks)
+    mean_iters = statistics.mean(iters)
+    mean_kern = statistics.mean(kern_ms)
+    achieved = bpi * mean_iters / (mean_kern / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "cg_kernel_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get("bytes_per_launch")
+        except Exception:
+            traffic = None
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        secs, cit = cpu_step_seconds(sc, x_w, v_w)
+        cpu = {"value": 1.0 / secs, "unit": "steps/s", "cores": 1, "kind": "port",
+               "sample": "one full oracle step (triplet assembly + FP64 Jacobi CG, %d iterations)"
+                         " on the post-warm-up state, one thread" % cit}
+    line = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (f64 dots + f64 refinement residual)", "data": "synthetic",
+        "config": {"workload": "sheet 256x256 quads, 66049 nodes, 131072 tris, 196096 hinges,"
+                               " 852481 blocks, 2 corners pinned, rel-res 1e-8 (FP64), from rest",
+                   "solver": "%s-PCG" % args.precond, "l2": "flushed (256 MiB write) before each step",
+                   "mean_pcg_iters": mean_iters, "assemble_ms": statistics.mean(asm_ms),
+                   "pcg_kernel_ms": mean_kern, "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "e2e": {"value": e2e_val, "unit": "steps/s", "h2d_bytes_per_step": 8 * 8 * sc["n"],
+                "d2h_bytes_per_step": 6 * 8 * sc["n"]},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic,
+                     "kernel": "cg_kernel (persistent PCG)",
+                     "algorithmic_bytes_per_iter": bpi},
+        "clocks": clk.summary(),
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precond", default="jacobi", choices=["jacobi", "block", "learned"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

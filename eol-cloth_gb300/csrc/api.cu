@@ -99,9 +99,10 @@ eolc_status ensure_state(eolc_ctx *ctx) {
   EOLC_CHECK_CUDA(ctx, ctx->X.resize(size_t(ctx->topo.n_nodes) * 2));
   EOLC_CHECK_CUDA(ctx, ctx->f.resize(n));
   EOLC_CHECK_CUDA(ctx, ctx->b.resize(n));
-  EOLC_CHECK_CUDA(ctx, ctx->A32.resize(nb9));
+  // +16 elements: the solver stages tiles with 16-byte copies whose rounded
+  // tail may run past the last block
+  EOLC_CHECK_CUDA(ctx, ctx->A32.resize(nb9 + 16));
   EOLC_CHECK_CUDA(ctx, ctx->beq_full.resize(n));
-  (void)nb9;
   return EOLC_OK;
 }
 
@@ -111,7 +112,7 @@ eolc_status assemble(eolc_ctx *ctx, const eolc_material &mat, const double g[3],
                      cudaStream_t s) {
   MaterialD md = make_material(mat, g, h);
   size_t nb9 = size_t(ctx->topo.n_blocks) * 9;
-  if (prec == EOLC_PREC_FP64) EOLC_CHECK_CUDA(ctx, ctx->A64.resize(nb9));
+  if (prec == EOLC_PREC_FP64) EOLC_CHECK_CUDA(ctx, ctx->A64.resize(nb9 + 16));
   if (want_M) EOLC_CHECK_CUDA(ctx, ctx->Mblk.resize(nb9));
   launch_assemble_blocks(ctx->topo, ctx->x.p, ctx->X.p, md, prec,
                          prec == EOLC_PREC_FP64 ? ctx->A64.p : nullptr,
@@ -119,6 +120,7 @@ eolc_status assemble(eolc_ctx *ctx, const eolc_material &mat, const double g[3],
                          want_M ? ctx->Mblk.p : nullptr, s);
   launch_forces_rhs(ctx->topo, ctx->x.p, ctx->X.p, ctx->v.p, md, prec,
                     ctx->f.p, want_b ? ctx->b.p : nullptr, s);
+  ctx->launches += 2;
   EOLC_CHECK_CUDA(ctx, cudaGetLastError());
   return EOLC_OK;
 }
@@ -141,7 +143,7 @@ eolc_status solve_device(eolc_ctx *ctx, const eolc_solve_opts *o,
   if (o->precision == EOLC_PREC_FP64 && !ctx->A64.p)
     return fail(ctx, EOLC_BAD_ARG, "no FP64 matrix assembled");
   eolc_solve_info local;
-  eolc_status st = run_pcg(ctx->work, a, info ? info : &local, s, ctx->err);
+  eolc_status st = run_pcg(ctx->work, a, info ? info : &local, s, ctx->err, ctx->launches);
   return st;
 }
 
@@ -152,6 +154,8 @@ cudaStream_t stream_of(eolc_ctx *ctx) { return ctx->stream; }
 extern "C" {
 
 int eolc_version(void) { return 1; }
+
+long long eolc_launch_count(const eolc_ctx *ctx) { return ctx ? ctx->launches : 0; }
 
 eolc_status eolc_create(eolc_ctx **out, int device) {
   if (!out) return EOLC_BAD_ARG;
@@ -178,6 +182,8 @@ void eolc_destroy(eolc_ctx *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   free_solve_work(ctx->work);
   free_collide_work(ctx->cd_work);
+  for (cudaEvent_t e : ctx->ev)
+    if (e) cudaEventDestroy(e);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -373,24 +379,34 @@ eolc_status eolc_step_resident(eolc_ctx *ctx, int n_steps,
   for (int k = 0; k < n_steps; ++k) {
     // pins from the velocity of the previous step (Constraints.cpp:472-496)
     EOLC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->beq_full.p, 0, sizeof(double) * n, s));
-    if (n_fixed > 0)
+    if (n_fixed > 0) {
       pins_kernel<<<(n_fixed + 127) / 128, 128, 0, s>>>(n_fixed, ctx->fixed_dofs.p,
                                                        ctx->fixed_vel.p, ctx->v.p,
                                                        ctx->beq_full.p);
+      ctx->launches += 1;
+    }
+    if (!ctx->ev[0]) { cudaEventCreate(&ctx->ev[0]); cudaEventCreate(&ctx->ev[1]); }
+    cudaEventRecord(ctx->ev[0], s);
     st = assemble(ctx, *mat, grav, h, opts->precision, false, true, s);
     if (st != EOLC_OK) return st;
+    cudaEventRecord(ctx->ev[1], s);
     ctx->last_precision = opts->precision;
     eolc_solve_info si{};
     st = solve_device(ctx, opts, &si, s);
+    float ams = 0.f;
+    cudaEventElapsedTime(&ams, ctx->ev[0], ctx->ev[1]);  // the solve synchronized
     agg.iterations += si.iterations;
     agg.refinements += si.refinements;
     agg.rel_res = si.rel_res;
     agg.status = si.status;
+    agg.solve_kernel_ms += si.solve_kernel_ms;
+    agg.assemble_ms += ams;
     if (st != EOLC_OK) {
       if (info) *info = agg;
       return st;
     }
     integrate_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, h, ctx->v.p, ctx->x.p);
+    ctx->launches += 1;
   }
   EOLC_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
   if (info) *info = agg;

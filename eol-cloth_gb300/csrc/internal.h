@@ -106,7 +106,7 @@ struct PcgArgs {
   const float *learned;  // learned approximate inverse blocks (n_blocks*9)
 };
 eolc_status run_pcg(SolveWork *&w, const PcgArgs &a, eolc_solve_info *info,
-                    cudaStream_t s, std::string &err);
+                    cudaStream_t s, std::string &err, long long &launches);
 void free_solve_work(SolveWork *w);
 
 // Collisions (collide.cu)
@@ -134,6 +134,8 @@ struct eolc_ctx {
   eolc::SolveWork *work = nullptr;
   int last_jacobi_iters = 0;
   int last_precision = -1;  // precision of the last assembled MDK
+  long long launches = 0;   // kernels launched by this context
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::vector<int> host_tri;  // triangle list of the current topology
   eolc::CollideWork *cd_work = nullptr;
 };

@@ -1,41 +1,43 @@
-// Preconditioned conjugate gradient on the 3x3 BSR matrix, as ONE persistent
-// cooperative kernel per solve.
+// Preconditioned conjugate gradient on the 3x3 BSR matrix as ONE persistent
+// cooperative kernel per solve, with one grid-wide barrier per iteration.
 //
 // Replaces the velocity solve of GeneralizedSolver::velocitySolve
 // (GeneralizedSolver.cpp:107-173) for the pinned-corner case: the QP
 // argmin 1/2 v'Av + b'v s.t. v_P = beq reduces to A_FF v_F = -b_F - A_FP beq.
-// The algorithm is Eigen's ConjugateGradient (x0 = 0, stop on
-// ||r|| <= tol ||rhs||, Jacobi preconditioner by default) with two
-// additions for the mixed-precision path:
-//   * inner vectors and matrix in FP32, every dot product accumulated in FP64;
-//   * "reliable updates": whenever the iterated residual has dropped by
-//     kDelta since the last check (or claims convergence) the FP32 update is
-//     folded into an FP64 solution and the TRUE residual rhs - A x is
-//     recomputed in FP64 arithmetic.  Convergence is declared only on that
-//     FP64 residual, so the reported relative residual is an FP64 one.
-// The FP64 path runs the same kernel with T = double.
+// The iteration is Eigen's preconditioned CG (x0 = 0, stop on
+// ||r|| <= tol ||rhs||, Jacobi preconditioner by default, the branch
+// GeneralizedSolver.cpp:123-126 meant to take) written in the
+// single-reduction form of Chronopoulos and Gear:
+//     u = M r, w = A u, gamma = (r,u), delta = (w,u)
+//     beta = gamma/gamma_old, alpha = gamma/(delta - beta gamma/alpha_old)
+//     p = u + beta p, s = w + beta s, x += alpha p, r -= alpha s
+// so that the two inner products of an iteration are reduced together.
+// Each neighbour's u = M (r - alpha (w + beta s)) is recomputed from its
+// previous r, w, s when a tile's halo is staged, so an iteration needs ONE
+// grid barrier (the reductions) instead of three.
 //
-// Layout: every vector is node-major with a padded 4th lane (one 16-byte load
-// per node for float).  Rows are split into tiles (<= 256 rows, <= a shared-
-// memory budget of blocks); each CTA owns a contiguous range of tiles and
-// stages a tile's BSR values and column indices in shared memory with
-// coalesced 16-byte loads, then one thread computes one block row.
+// Mixed precision: inner vectors and matrix in FP32, every inner product
+// accumulated in FP64, and "reliable updates": whenever the iterated residual
+// has dropped by kDelta since the last check (or claims convergence), the
+// FP32 solution increment is folded into an FP64 solution and the TRUE
+// residual rhs - A x is recomputed in FP64 arithmetic, together with s = A p
+// and w = A M r.  Convergence is declared only on that FP64 residual.  The
+// FP64 path runs the same kernel with T = double.
 //
-// Per iteration there are two grid-wide barriers:
-//   P1  p = z + beta p_old (computed on the fly for every neighbour),
-//       q = A p, partial p.q                                  -> barrier
-//   P2  alpha, x += alpha p, r -= alpha q, z = M^-1 r, partial r.z, r.r
-//                                                             -> barrier
+// Layout: vectors are node-major with a padded 4th lane (one 16-byte load per
+// node in FP32).  Rows are cut into tiles; a tile's BSR values and its
+// tile-local 16-bit column indices are staged in shared memory with aligned
+// 16-byte copies, and the tile's halo (the distinct columns it touches, a
+// list built once per topology) is staged as one vector window.
 // Barriers spin with an iteration cap; on expiry the kernel records
 // EOLC_TIMEOUT and every CTA returns.
-#include <cooperative_groups.h>
 #include <cuda/atomic>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
-#include <type_traits>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "internal.h"
@@ -44,11 +46,14 @@ namespace eolc {
 
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kTileRows = 256;
-constexpr int kSmemBytes = 96 * 1024;  // staged values + column indices
-constexpr double kDelta = 0.1;          // reliable-update trigger factor
-constexpr long long kSpinLimit = 1ll << 24;
+constexpr int kThreads = 512;
+constexpr int kRowThreads = 4;                     // threads per block row
+constexpr int kTileRows = kThreads / kRowThreads;  // 128
+constexpr int kValBytes = 112 * 1024;              // staged values + local cols
+constexpr int kWinMaxF = 2048;                     // halo nodes per tile (FP32)
+constexpr int kWinMaxD = 1536;                     // halo nodes per tile (FP64)
+constexpr double kDelta = 0.1;                     // reliable-update trigger
+constexpr long long kSpinLimit = 1ll << 25;
 
 template <typename T>
 struct alignas(4 * sizeof(T)) V4 {
@@ -64,36 +69,139 @@ struct DevStatus {
   double rhs_norm2;
 };
 
-// ---- grid barrier ----------------------------------------------------------
-// bar[0] = arrival counter, bar[1] = generation.  Bounded spin: on expiry the
-// barrier records EOLC_TIMEOUT and returns false.
+// ---- accumulation arithmetic ------------------------------------------------
+// FP64 instructions run at a small fraction of the FP32 rate on this part,
+// so the FP32 path accumulates inner products and forms its CG scalars in
+// double-float arithmetic (an unevaluated FP32 pair hi + lo, ~48 significant
+// bits) built from the error-free transformations TwoSum / TwoProd.  The
+// FP64 path uses plain double.
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ DF df_fast_two_sum(float a, float b) {
+  float s = a + b;
+  return DF{s, b - (s - a)};
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  float s = a.hi + b.hi;
+  float bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (b.hi - bb);
+  e += a.lo + b.lo;
+  return df_fast_two_sum(s, e);
+}
+__device__ __forceinline__ DF df_add_f(DF a, float b) {
+  float s = a.hi + b;
+  float bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (b - bb);
+  e += a.lo;
+  return df_fast_two_sum(s, e);
+}
+__device__ __forceinline__ DF df_neg(DF a) { return DF{-a.hi, -a.lo}; }
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+  float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+  return df_fast_two_sum(p, e);
+}
+__device__ __forceinline__ DF df_div(DF a, DF b) {
+  float q1 = a.hi / b.hi;
+  DF r = df_add(a, df_neg(df_mul(b, DF{q1, 0.f})));
+  float q2 = r.hi / b.hi;
+  return df_fast_two_sum(q1, q2);
+}
+__device__ __forceinline__ bool df_lt(DF a, DF b) {
+  return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo);
+}
+__device__ __forceinline__ bool df_le(DF a, DF b) { return !df_lt(b, a); }
+__device__ __forceinline__ bool df_finite(DF a) { return isfinite(a.hi) && isfinite(a.lo); }
+__device__ __forceinline__ DF df_from_double(double d) {
+  float hi = float(d);
+  return DF{hi, float(d - double(hi))};
+}
+
+// Accumulator of the arithmetic type T: DF for float, double for double.
+template <typename T>
+struct Acc;
+template <>
+struct Acc<float> {
+  using V = DF;
+  static __device__ __forceinline__ V zero() { return DF{0.f, 0.f}; }
+  static __device__ __forceinline__ V add(V a, V b) { return df_add(a, b); }
+  static __device__ __forceinline__ V addf(V a, float b) { return df_add_f(a, b); }
+  static __device__ __forceinline__ V mul(V a, V b) { return df_mul(a, b); }
+  static __device__ __forceinline__ V div(V a, V b) { return df_div(a, b); }
+  static __device__ __forceinline__ V neg(V a) { return df_neg(a); }
+  static __device__ __forceinline__ bool lt(V a, V b) { return df_lt(a, b); }
+  static __device__ __forceinline__ bool le(V a, V b) { return df_le(a, b); }
+  static __device__ __forceinline__ bool pos(V a) { return a.hi > 0.f; }
+  static __device__ __forceinline__ bool finite(V a) { return df_finite(a); }
+  static __device__ __forceinline__ float to_t(V a) { return a.hi + a.lo; }
+  static __device__ __forceinline__ double to_d(V a) { return double(a.hi) + double(a.lo); }
+  static __device__ __forceinline__ V from_d(double d) { return df_from_double(d); }
+  static __device__ __forceinline__ V shfl_xor(V a, int o) {
+    return DF{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
+  }
+};
+template <>
+struct Acc<double> {
+  using V = double;
+  static __device__ __forceinline__ V zero() { return 0.0; }
+  static __device__ __forceinline__ V add(V a, V b) { return a + b; }
+  static __device__ __forceinline__ V addf(V a, double b) { return a + b; }
+  static __device__ __forceinline__ V mul(V a, V b) { return a * b; }
+  static __device__ __forceinline__ V div(V a, V b) { return a / b; }
+  static __device__ __forceinline__ V neg(V a) { return -a; }
+  static __device__ __forceinline__ bool lt(V a, V b) { return a < b; }
+  static __device__ __forceinline__ bool le(V a, V b) { return a <= b; }
+  static __device__ __forceinline__ bool pos(V a) { return a > 0.0; }
+  static __device__ __forceinline__ bool finite(V a) { return isfinite(a); }
+  static __device__ __forceinline__ double to_t(V a) { return a; }
+  static __device__ __forceinline__ double to_d(V a) { return a; }
+  static __device__ __forceinline__ V from_d(double d) { return d; }
+  static __device__ __forceinline__ V shfl_xor(V a, int o) {
+    return __shfl_xor_sync(0xffffffffu, a, o);
+  }
+};
+static_assert(sizeof(DF) == sizeof(double), "partials share one 8-byte slot");
+
+template <typename T>
+__host__ __device__ constexpr int win_max() {
+  return sizeof(T) == 8 ? kWinMaxD : kWinMaxF;
+}
+template <typename T>
+__host__ __device__ constexpr int cap_blocks() {
+  // values (9 T) + one 16-bit local column per block, with 16-byte padding
+  return (kValBytes - 64) / (9 * int(sizeof(T)) + 2);
+}
+// shared memory: values | local columns | window (an FP64 x window plus an
+// inner-type p window, or the u window)
+template <typename T>
+__host__ __device__ constexpr size_t smem_bytes() {
+  return size_t(kValBytes) + size_t(win_max<T>()) * (sizeof(V4<double>) + sizeof(V4<T>));
+}
+
+// ---- grid barrier -----------------------------------------------------------
+// Monotonic arrival counter: CTA thread 0 adds 1 with release semantics and
+// polls (acquire) until the count reaches n_ctas * epoch.  Bounded spin: on
+// expiry the barrier records EOLC_TIMEOUT and returns false.
 __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned nblocks,
-                                             unsigned &gen, DevStatus *st) {
+                                             unsigned &epoch, DevStatus *st) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     cuda::atomic_ref<unsigned, cuda::thread_scope_device> count(bar[0]);
-    cuda::atomic_ref<unsigned, cuda::thread_scope_device> gflag(bar[1]);
-    unsigned my_gen = gen;
+    epoch += 1u;
+    const unsigned target = nblocks * epoch;
     int ok = 1;
-    __threadfence();
-    unsigned arrived = count.fetch_add(1u, cuda::memory_order_acq_rel);
-    if (arrived == nblocks - 1) {
-      count.store(0u, cuda::memory_order_relaxed);
-      gflag.store(my_gen + 1u, cuda::memory_order_release);
-    } else {
-      long long spins = 0;
-      while (gflag.load(cuda::memory_order_acquire) == my_gen) {
-        if (++spins > kSpinLimit) {
-          atomicCAS(&st->status, EOLC_OK, EOLC_TIMEOUT);
-          ok = 0;
-          break;
-        }
-        if (spins > 64) __nanosleep(64);
+    count.fetch_add(1u, cuda::memory_order_release);
+    long long spins = 0;
+    while (count.load(cuda::memory_order_acquire) < target) {
+      if (++spins > kSpinLimit) {
+        atomicCAS(&st->status, EOLC_OK, EOLC_TIMEOUT);
+        ok = 0;
+        break;
       }
     }
-    __threadfence();
-    gen = my_gen + 1u;
     if (ok) {
       cuda::atomic_ref<int, cuda::thread_scope_device> sref(st->status);
       ok = sref.load(cuda::memory_order_relaxed) == EOLC_OK;
@@ -104,30 +212,56 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned nblocks,
   return s_ok != 0;
 }
 
-// Deterministic CTA-wide FP64 sum (fixed shuffle tree, fixed warp order).
-__device__ __forceinline__ double block_sum(double v, double *red) {
+// Deterministic CTA-wide sums of three accumulators (fixed butterfly tree,
+// fixed warp order).  red must hold 3 * (kThreads / 32 + 1) accumulators.
+template <typename T>
+__device__ __forceinline__ void block_sum3(typename Acc<T>::V &a, typename Acc<T>::V &b,
+                                           typename Acc<T>::V &c, typename Acc<T>::V *red) {
+  using A = Acc<T>;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    a = A::add(a, A::shfl_xor(a, o));
+    b = A::add(b, A::shfl_xor(b, o));
+    c = A::add(c, A::shfl_xor(c, o));
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int NW = kThreads / 32;
   __syncthreads();
-  if (lane == 0) red[warp] = v;
+  if (lane == 0) { red[3 * warp] = a; red[3 * warp + 1] = b; red[3 * warp + 2] = c; }
   __syncthreads();
-  double s = 0;
-  if (threadIdx.x == 0) {
-    for (int w = 0; w < kThreads / 32; ++w) s += red[w];
-    red[kThreads / 32] = s;
+  if (warp == 0) {
+    typename A::V x = lane < NW ? red[3 * lane] : A::zero();
+    typename A::V y = lane < NW ? red[3 * lane + 1] : A::zero();
+    typename A::V z = lane < NW ? red[3 * lane + 2] : A::zero();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      x = A::add(x, A::shfl_xor(x, o));
+      y = A::add(y, A::shfl_xor(y, o));
+      z = A::add(z, A::shfl_xor(z, o));
+    }
+    if (lane == 0) { red[3 * NW] = x; red[3 * NW + 1] = y; red[3 * NW + 2] = z; }
   }
   __syncthreads();
-  return red[kThreads / 32];
+  a = red[3 * NW]; b = red[3 * NW + 1]; c = red[3 * NW + 2];
 }
 
-// Every CTA reduces the per-CTA partials of one quantity in the same fixed
-// order, so all CTAs take the same branch decisions.
-__device__ __forceinline__ double reduce_partials(const double *part, int n,
-                                                  double *red) {
-  double v = 0;
-  for (int k = threadIdx.x; k < n; k += kThreads) v += __ldcg(part + k);
-  return block_sum(v, red);
+// Every CTA reduces the per-CTA partial triples in the same fixed order, so
+// all CTAs take the same branch decisions.
+template <typename T>
+__device__ __forceinline__ void reduce_partials3(const typename Acc<T>::V *part, int G,
+                                                 typename Acc<T>::V &a, typename Acc<T>::V &b,
+                                                 typename Acc<T>::V &c, typename Acc<T>::V *red) {
+  using A = Acc<T>;
+  using V = typename A::V;
+  a = b = c = A::zero();
+  for (int k = threadIdx.x; k < G; k += kThreads) {
+    const double *pd = reinterpret_cast<const double *>(part + 3 * k);
+    double v0 = __ldcg(pd), v1 = __ldcg(pd + 1), v2 = __ldcg(pd + 2);
+    a = A::add(a, *reinterpret_cast<V *>(&v0));
+    b = A::add(b, *reinterpret_cast<V *>(&v1));
+    c = A::add(c, *reinterpret_cast<V *>(&v2));
+  }
+  block_sum3<T>(a, b, c, red);
 }
 
 template <typename T>
@@ -135,32 +269,29 @@ struct Params {
   int n_nodes;
   int n_ctas;
   const int *rowptr;
-  const int *colidx;
-  const T *A;            // inner matrix (FP32 or FP64), also used promoted
-                         // to FP64 for the true residual
-  const int *tile_row;   // tile boundaries (n_tiles + 1)
-  const int *cta_tile;   // CTA -> first tile (n_ctas + 1)
-  const V4<double> *rhs; // masked rhs of the reduced system
+  const T *A;               // inner matrix (FP32 or FP64); promoted to FP64
+                            // for the true residual
+  const uint16_t *lcol;     // tile-local column of every block
+  const int *tile_row;      // tile boundaries (n_tiles + 1)
+  const int *tile_wptr;     // window list offsets (n_tiles + 1)
+  const int *wlist;         // window node ids, per tile
+  const int *cta_tile;      // CTA -> first tile (n_ctas + 1)
+  const V4<double> *rhs;    // masked rhs of the reduced system
   V4<double> *x64;
-  V4<T> *r, *z, *pa, *pb, *q, *xacc;
-  const T *pc;           // preconditioner: 4 per node (Jacobi) or 9 (block)
-  const V4<T> *fmask;    // 1 on free DOFs, 0 on pinned
-  double *part;          // 5 x n_ctas partial sums
+  V4<T> *r[2], *w[2], *s[2];
+  V4<T> *p, *xacc;
+  const T *pc;              // preconditioner: 4 per node (Jacobi) or 9 (block)
+  const V4<T> *fmask;       // 1 on free DOFs, 0 on pinned
+  double *part;             // partial sums: 2 sets x 3 values x n_ctas
   unsigned *bar;
   DevStatus *st;
-  double tol2;           // tol^2 (scaled by ||rhs||^2 on the device)
+  double tol2;              // tol^2 (scaled by ||rhs||^2 on the device)
   int max_iter;
-  int block_pc;          // 0 = point Jacobi, 1 = block Jacobi
+  int block_pc;             // 0 = point Jacobi, 1 = block Jacobi
 };
 
 template <typename T>
-__device__ __forceinline__ V4<T> ld4(const V4<T> *p, int i) {
-  return p[i];
-}
-
-template <typename T>
-__device__ __forceinline__ V4<T> apply_pc(const Params<T> &P, int i,
-                                          V4<T> r) {
+__device__ __forceinline__ V4<T> apply_pc(const Params<T> &P, int i, V4<T> r) {
   V4<T> z;
   if (P.block_pc) {
     const T *B = P.pc + size_t(9) * i;
@@ -168,190 +299,307 @@ __device__ __forceinline__ V4<T> apply_pc(const Params<T> &P, int i,
     z.y = B[3] * r.x + B[4] * r.y + B[5] * r.z;
     z.z = B[6] * r.x + B[7] * r.y + B[8] * r.z;
   } else {
-    const T *d = P.pc + size_t(4) * i;
-    z.x = d[0] * r.x; z.y = d[1] * r.y; z.z = d[2] * r.z;
+    V4<T> d = reinterpret_cast<const V4<T> *>(P.pc)[i];
+    z.x = d.x * r.x; z.y = d.y * r.y; z.z = d.z * r.z;
   }
   z.w = T(0);
   return z;
 }
 
-// Stages the BSR values and column indices of tile rows [r0, r1) in shared
-// memory.  Returns the block offset of the tile.
+// Copies n elements (of size E) starting at src into shared memory with
+// 16-byte loads and stores; returns the element offset of src inside dst.
+// The source allocation is padded so the rounded-up tail stays inside it.
+template <typename E>
+__device__ __forceinline__ int stage_aligned(const E *src, int n, E *dst) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(src);
+  const float4 *s4 = reinterpret_cast<const float4 *>(a & ~uintptr_t(15));
+  const int off = int((a & 15) / sizeof(E));
+  const int nvec = int((size_t(off + n) * sizeof(E) + 15) / 16);
+  float4 *d4 = reinterpret_cast<float4 *>(dst);
+  for (int k = threadIdx.x; k < nvec; k += kThreads) d4[k] = __ldcg(s4 + k);
+  return off;
+}
+
+// Per-tile metadata of this CTA, loaded once per solve.
+constexpr int kMaxCtaTiles = 64;
+struct TileMeta {
+  int r0, r1, b0, b1, w0, wn;
+};
+
+// Stages a tile's values, local columns and row pointers; returns pointers
+// to the tile's first element inside shared memory.
 template <typename T>
-__device__ __forceinline__ int stage_tile(const Params<T> &P, int r0, int r1,
-                                          T *sA, int *sC) {
-  int b0 = P.rowptr[r0], b1 = P.rowptr[r1];
-  int nv = (b1 - b0) * 9;
-  const T *src = P.A + size_t(b0) * 9;
-  // 16-byte vector loads on the aligned middle part, scalar edges.
-  constexpr int VW = 16 / sizeof(T);
-  uintptr_t a = reinterpret_cast<uintptr_t>(src);
-  int head = int(((16 - (a & 15)) & 15) / sizeof(T));
-  if (head > nv) head = nv;
-  for (int k = threadIdx.x; k < head; k += kThreads) sA[k] = src[k];
-  int nvec = (nv - head) / VW;
-  const float4 *s4 = reinterpret_cast<const float4 *>(src + head);
-  for (int k = threadIdx.x; k < nvec; k += kThreads) {
-    float4 t = __ldcg(s4 + k);
-    const T *tp = reinterpret_cast<const T *>(&t);
-#pragma unroll
-    for (int j = 0; j < VW; ++j) sA[head + k * VW + j] = tp[j];
-  }
-  for (int k = head + nvec * VW + threadIdx.x; k < nv; k += kThreads) sA[k] = src[k];
-  for (int k = threadIdx.x; k < b1 - b0; k += kThreads) sC[k] = __ldg(P.colidx + b0 + k);
-  __syncthreads();
-  return b0;
+__device__ __forceinline__ void stage_tile(const Params<T> &P, const TileMeta &tm,
+                                           unsigned char *vals, const T *&sA,
+                                           const uint16_t *&sL, int *sRow) {
+  const int nb = tm.b1 - tm.b0;
+  T *dA = reinterpret_cast<T *>(vals);
+  const int offA = stage_aligned(P.A + size_t(tm.b0) * 9, nb * 9, dA);
+  const size_t abytes = (size_t(offA + nb * 9) * sizeof(T) + 31) & ~size_t(15);
+  uint16_t *dL = reinterpret_cast<uint16_t *>(vals + abytes);
+  const int offL = stage_aligned(P.lcol + tm.b0, nb, dL);
+  for (int k = threadIdx.x; k <= tm.r1 - tm.r0; k += kThreads)
+    sRow[k] = __ldg(P.rowptr + tm.r0 + k) - tm.b0;
+  sA = dA + offA;
+  sL = dL + offL;
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads)
-pcg_kernel(Params<T> P) {
+__device__ __forceinline__ T dot3(V4<T> a, V4<T> b) {
+  return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+
+// One CG phase over this CTA's tiles.
+//   kInit:  u = M r (current r), w = A u                  -> w[cur]
+//   else:   s' = w + beta s, r' = r - alpha s', u = M r' (every halo node),
+//           w' = A u, p = M r + beta p, x += alpha p
+//           -> r'[nxt], s'[nxt], w'[nxt], p, xacc
+// Accumulates (r'.u, w'.u, r'.r') into g, d, rr.
+template <typename T, bool kInit>
+__device__ __forceinline__ void cg_phase(const Params<T> &P, const TileMeta *tiles,
+                                         int ntiles, int cur, T alpha, T beta,
+                                         unsigned char *smem, typename Acc<T>::V &g,
+                                         typename Acc<T>::V &d, typename Acc<T>::V &rr) {
+  using A = Acc<T>;
+  const int nxt = cur ^ 1;
+  V4<T> *sU = reinterpret_cast<V4<T> *>(smem + kValBytes);
+  __shared__ V4<T> sRn[kTileRows];
+  __shared__ int sRow[kTileRows + 1];
+  const int lrow = threadIdx.x / kRowThreads, quarter = threadIdx.x % kRowThreads;
+  for (int t = 0; t < ntiles; ++t) {
+    const TileMeta tm = tiles[t];
+    const int i = tm.r0 + lrow;
+    const bool owner = i < tm.r1 && quarter == 0;
+    // epilogue operands, prefetched so their latency overlaps the staging
+    V4<T> m{}, ro{}, po{}, xa{};
+    if (owner) {
+      m = P.fmask[i];
+      if (!kInit) { ro = P.r[cur][i]; po = P.p[i]; xa = P.xacc[i]; }
+    }
+    const T *sA;
+    const uint16_t *sL;
+    stage_tile(P, tm, smem, sA, sL, sRow);
+    for (int j = threadIdx.x; j < tm.wn; j += kThreads) {
+      const int node = __ldg(P.wlist + tm.w0 + j);
+      V4<T> rn = P.r[cur][node];
+      if (!kInit) {
+        const V4<T> so = P.s[cur][node], wo = P.w[cur][node];
+        const V4<T> sn{wo.x + beta * so.x, wo.y + beta * so.y, wo.z + beta * so.z, T(0)};
+        rn = V4<T>{rn.x - alpha * sn.x, rn.y - alpha * sn.y, rn.z - alpha * sn.z, T(0)};
+        if (node >= tm.r0 && node < tm.r1) {
+          P.s[nxt][node] = sn;
+          P.r[nxt][node] = rn;
+        }
+      }
+      if (node >= tm.r0 && node < tm.r1) sRn[node - tm.r0] = rn;
+      sU[j] = apply_pc(P, node, rn);
+    }
+    __syncthreads();
+    T a0 = 0, a1 = 0, a2 = 0;
+    if (i < tm.r1) {
+      const int q0 = sRow[lrow], q1 = sRow[lrow + 1];
+#pragma unroll 2
+      for (int k = q0 + quarter; k < q1; k += kRowThreads) {
+        const V4<T> u = sU[sL[k]];
+        const T *blk = sA + size_t(k) * 9;
+        a0 += blk[0] * u.x + blk[1] * u.y + blk[2] * u.z;
+        a1 += blk[3] * u.x + blk[4] * u.y + blk[5] * u.z;
+        a2 += blk[6] * u.x + blk[7] * u.y + blk[8] * u.z;
+      }
+    }
+#pragma unroll
+    for (int o = 1; o < kRowThreads; o <<= 1) {
+      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    if (owner) {
+      const V4<T> wn4{a0 * m.x, a1 * m.y, a2 * m.z, T(0)};
+      const V4<T> rn = sRn[lrow];
+      const V4<T> un = apply_pc(P, i, rn);
+      if (kInit) {
+        P.w[cur][i] = wn4;
+      } else {
+        P.w[nxt][i] = wn4;
+        // p = M r_old + beta p ; x += alpha p
+        const V4<T> uo = apply_pc(P, i, ro);
+        const V4<T> pi{uo.x + beta * po.x, uo.y + beta * po.y, uo.z + beta * po.z, T(0)};
+        P.p[i] = pi;
+        xa.x += alpha * pi.x; xa.y += alpha * pi.y; xa.z += alpha * pi.z;
+        P.xacc[i] = xa;
+      }
+      g = A::addf(g, dot3(rn, un));
+      d = A::addf(d, dot3(wn4, un));
+      rr = A::addf(rr, dot3(rn, rn));
+    }
+    __syncthreads();
+  }
+}
+
+// Reliable update, second step: r = rhs - A x64 (FP64 arithmetic) and
+// s = A p, written to r[cur], s[cur].  Accumulates r.r (FP64) into rr64.
+template <typename T>
+__device__ __forceinline__ void ru_residual(const Params<T> &P, const TileMeta *tiles,
+                                           int ntiles, int cur, unsigned char *smem,
+                                           double &rr64) {
+  V4<double> *sX = reinterpret_cast<V4<double> *>(smem + kValBytes);
+  V4<T> *sP = reinterpret_cast<V4<T> *>(smem + kValBytes +
+                                         size_t(win_max<T>()) * sizeof(V4<double>));
+  __shared__ int sRow[kTileRows + 1];
+  const int lrow = threadIdx.x / kRowThreads, quarter = threadIdx.x % kRowThreads;
+  for (int t = 0; t < ntiles; ++t) {
+    const TileMeta tm = tiles[t];
+    const T *sA;
+    const uint16_t *sL;
+    stage_tile(P, tm, smem, sA, sL, sRow);
+    for (int j = threadIdx.x; j < tm.wn; j += kThreads) {
+      const int node = __ldg(P.wlist + tm.w0 + j);
+      sX[j] = P.x64[node];
+      sP[j] = P.p[node];
+    }
+    __syncthreads();
+    const int i = tm.r0 + lrow;
+    double a0 = 0, a1 = 0, a2 = 0;
+    T c0 = 0, c1 = 0, c2 = 0;
+    if (i < tm.r1) {
+      const int q0 = sRow[lrow], q1 = sRow[lrow + 1];
+      for (int k = q0 + quarter; k < q1; k += kRowThreads) {
+        const V4<double> xj = sX[sL[k]];
+        const V4<T> pj = sP[sL[k]];
+        const T *blk = sA + size_t(k) * 9;
+        a0 += double(blk[0]) * xj.x + double(blk[1]) * xj.y + double(blk[2]) * xj.z;
+        a1 += double(blk[3]) * xj.x + double(blk[4]) * xj.y + double(blk[5]) * xj.z;
+        a2 += double(blk[6]) * xj.x + double(blk[7]) * xj.y + double(blk[8]) * xj.z;
+        c0 += blk[0] * pj.x + blk[1] * pj.y + blk[2] * pj.z;
+        c1 += blk[3] * pj.x + blk[4] * pj.y + blk[5] * pj.z;
+        c2 += blk[6] * pj.x + blk[7] * pj.y + blk[8] * pj.z;
+      }
+    }
+#pragma unroll
+    for (int o = 1; o < kRowThreads; o <<= 1) {
+      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+      c0 += __shfl_xor_sync(0xffffffffu, c0, o);
+      c1 += __shfl_xor_sync(0xffffffffu, c1, o);
+      c2 += __shfl_xor_sync(0xffffffffu, c2, o);
+    }
+    if (i < tm.r1 && quarter == 0) {
+      const V4<double> b = P.rhs[i];
+      const V4<T> m = P.fmask[i];
+      const double e0 = (b.x - a0) * double(m.x), e1 = (b.y - a1) * double(m.y),
+                   e2 = (b.z - a2) * double(m.z);
+      rr64 += e0 * e0 + e1 * e1 + e2 * e2;
+      P.r[cur][i] = V4<T>{T(e0), T(e1), T(e2), T(0)};
+      P.s[cur][i] = V4<T>{c0 * m.x, c1 * m.y, c2 * m.z, T(0)};
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads, 1)
+cg_kernel(Params<T> P) {
+  using A = Acc<T>;
+  using V = typename A::V;
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ double red[kThreads / 32 + 1];
-  T *sA = reinterpret_cast<T *>(smem);
-  const int cap_blocks = kSmemBytes / (9 * sizeof(T) + sizeof(int));
-  int *sC = reinterpret_cast<int *>(smem + size_t(cap_blocks) * 9 * sizeof(T));
+  __shared__ V red[3 * (kThreads / 32 + 1)];
+  __shared__ TileMeta tiles[kMaxCtaTiles];
   const int cta = blockIdx.x;
   const int G = P.n_ctas;
-  double *part_pq = P.part, *part_rz = P.part + G, *part_rr = P.part + 2 * G,
-         *part_r64 = P.part + 3 * G;
-  unsigned gen = 0;
+  unsigned epoch = 0;
   const int t0 = P.cta_tile[cta], t1 = P.cta_tile[cta + 1];
-  const double tol2 = P.tol2 * __ldcg(&P.st->rhs_norm2);
+  const int ntiles = t1 - t0;
+  for (int t = threadIdx.x; t < ntiles; t += kThreads) {
+    TileMeta tm;
+    tm.r0 = P.tile_row[t0 + t];
+    tm.r1 = P.tile_row[t0 + t + 1];
+    tm.b0 = P.rowptr[tm.r0];
+    tm.b1 = P.rowptr[tm.r1];
+    tm.w0 = P.tile_wptr[t0 + t];
+    tm.wn = P.tile_wptr[t0 + t + 1] - tm.w0;
+    tiles[t] = tm;
+  }
+  __syncthreads();
+  const V tol2 = A::from_d(P.tol2 * __ldcg(&P.st->rhs_norm2));
+  const V delta2 = A::from_d(kDelta * kDelta);
+  V *partbuf = reinterpret_cast<V *>(P.part);
+  int pset = 0;  // partial-sum buffers alternate between barriers
 
-  double rz = reduce_partials(part_rz, G, red);  // r.z of the initial residual
-  double rz_prev = 1.0, rmax2 = reduce_partials(part_rr, G, red);
+  int cur = 0;
+  // initial residual r = rhs (x0 = 0): u = M r, w = A u
+  V gam = A::zero(), del = A::zero(), rr = A::zero();
+  cg_phase<T, true>(P, tiles, ntiles, cur, T(0), T(0), smem, gam, del, rr);
+#define EOLC_PUBLISH_AND_SYNC(a, b, c)                                  \
+  do {                                                                  \
+    block_sum3<T>(a, b, c, red);                                        \
+    V *pp = partbuf + size_t(3) * G * pset;                             \
+    if (threadIdx.x == 0) {                                             \
+      pp[3 * cta] = a; pp[3 * cta + 1] = b; pp[3 * cta + 2] = c;        \
+    }                                                                   \
+    if (!grid_barrier(P.bar, G, epoch, P.st)) return;                   \
+    reduce_partials3<T>(pp, G, a, b, c, red);                           \
+    pset ^= 1;                                                          \
+  } while (0)
+  EOLC_PUBLISH_AND_SYNC(gam, del, rr);
+  V rmax2 = rr;
+  double last_rr64 = A::to_d(rr);
   int it = 0, nref = 0, status = EOLC_NOT_CONVERGED;
-  V4<T> *pold = P.pa, *pnew = P.pb;
-  double last_rr64 = rmax2;
-  bool converged = rmax2 <= tol2;
-  while (!converged && it < P.max_iter) {
-    // ---------------- P1: p = z + beta p_old, q = A p -----------------
-    const T beta = it == 0 ? T(0) : T(rz / rz_prev);
-    double pq = 0;
-    for (int tile = t0; tile < t1; ++tile) {
-      int r0 = P.tile_row[tile], r1 = P.tile_row[tile + 1];
-      int b0 = stage_tile(P, r0, r1, sA, sC);
-      int i = r0 + threadIdx.x;
-      if (i < r1) {
-        V4<T> zi = P.z[i], po = pold[i];
-        V4<T> pi{zi.x + beta * po.x, zi.y + beta * po.y, zi.z + beta * po.z, T(0)};
-        pnew[i] = pi;
-        T a0 = 0, a1 = 0, a2 = 0;
-        int q0 = P.rowptr[i], q1 = P.rowptr[i + 1];
-        for (int k = q0; k < q1; ++k) {
-          int j = sC[k - b0];
-          V4<T> zj = P.z[j], pj = pold[j];
-          T px = zj.x + beta * pj.x, py = zj.y + beta * pj.y, pz = zj.z + beta * pj.z;
-          const T *blk = sA + size_t(k - b0) * 9;
-          a0 += blk[0] * px + blk[1] * py + blk[2] * pz;
-          a1 += blk[3] * px + blk[4] * py + blk[5] * pz;
-          a2 += blk[6] * px + blk[7] * py + blk[8] * pz;
-        }
-        V4<T> m = P.fmask[i];
-        V4<T> qi{a0 * m.x, a1 * m.y, a2 * m.z, T(0)};
-        P.q[i] = qi;
-        pq += double(pi.x) * double(qi.x) + double(pi.y) * double(qi.y) +
-              double(pi.z) * double(qi.z);
-      }
-      __syncthreads();
-    }
-    pq = block_sum(pq, red);
-    if (threadIdx.x == 0) part_pq[cta] = pq;
-    if (!grid_barrier(P.bar, G, gen, P.st)) return;
-    ++it;
-    // ---------------- P2: update ----------------------------------------
-    double pq_all = reduce_partials(part_pq, G, red);
-    if (!(pq_all > 0.0)) {
-      status = isfinite(pq_all) ? EOLC_BREAKDOWN : EOLC_NONFINITE;
+  bool converged = A::finite(rr) && A::le(rr, tol2);
+  if (!A::finite(rr)) status = EOLC_NONFINITE;
+  V gam_old = A::from_d(1.0), alpha_old = A::from_d(1.0);
+  bool restart = true;  // beta = 0 on the first step
+  while (!converged && status != EOLC_NONFINITE && it < P.max_iter) {
+    const V beta = restart ? A::zero() : A::div(gam, gam_old);
+    const V denom = restart ? del : A::add(del, A::neg(A::div(A::mul(beta, gam), alpha_old)));
+    if (!A::pos(denom) || !A::pos(gam)) {
+      status = (A::finite(denom) && A::finite(gam)) ? EOLC_BREAKDOWN : EOLC_NONFINITE;
       break;
     }
-    const double alpha_d = rz / pq_all;
-    const T alpha = T(alpha_d);
-    double rzn = 0, rr = 0;
-    for (int tile = t0; tile < t1; ++tile) {
-      int r0 = P.tile_row[tile], r1 = P.tile_row[tile + 1];
-      int i = r0 + threadIdx.x;
-      if (i < r1) {
-        V4<T> pi = pnew[i], qi = P.q[i], ri = P.r[i], xa = P.xacc[i];
-        xa.x += alpha * pi.x; xa.y += alpha * pi.y; xa.z += alpha * pi.z;
-        ri.x -= alpha * qi.x; ri.y -= alpha * qi.y; ri.z -= alpha * qi.z;
-        P.xacc[i] = xa;
-        P.r[i] = ri;
-        V4<T> zi = apply_pc(P, i, ri);
-        P.z[i] = zi;
-        rzn += double(ri.x) * double(zi.x) + double(ri.y) * double(zi.y) +
-               double(ri.z) * double(zi.z);
-        rr += double(ri.x) * double(ri.x) + double(ri.y) * double(ri.y) +
-              double(ri.z) * double(ri.z);
-      }
-    }
-    rzn = block_sum(rzn, red);
-    rr = block_sum(rr, red);
-    if (threadIdx.x == 0) { part_rz[cta] = rzn; part_rr[cta] = rr; }
-    if (!grid_barrier(P.bar, G, gen, P.st)) return;
-    rz_prev = rz;
-    rz = reduce_partials(part_rz, G, red);
-    double rr_all = reduce_partials(part_rr, G, red);
-    V4<T> *tmp = pold; pold = pnew; pnew = tmp;
-    if (!isfinite(rr_all)) { status = EOLC_NONFINITE; break; }
-    bool need_ru = rr_all < kDelta * kDelta * rmax2 || rr_all <= tol2 ||
-                   it >= P.max_iter;
-    if (!need_ru) continue;
-    // ---------------- reliable update --------------------------------------
-    // RU1: fold the low-precision update into the FP64 solution.
-    for (int tile = t0; tile < t1; ++tile) {
-      int r0 = P.tile_row[tile], r1 = P.tile_row[tile + 1];
-      int i = r0 + threadIdx.x;
-      if (i < r1) {
-        V4<T> xa = P.xacc[i];
+    const V alpha = A::div(gam, denom);
+    restart = false;
+    V g2 = A::zero(), d2 = A::zero(), rr2 = A::zero();
+    cg_phase<T, false>(P, tiles, ntiles, cur, T(A::to_t(alpha)), T(A::to_t(beta)), smem, g2,
+                       d2, rr2);
+    EOLC_PUBLISH_AND_SYNC(g2, d2, rr2);
+    ++it;
+    cur ^= 1;
+    gam_old = gam;
+    alpha_old = alpha;
+    gam = g2;
+    del = d2;
+    rr = rr2;
+    if (!A::finite(rr) || !A::finite(gam) || !A::finite(del)) { status = EOLC_NONFINITE; break; }
+    if (!(A::lt(rr, A::mul(delta2, rmax2)) || A::le(rr, tol2) || it >= P.max_iter)) continue;
+    // ---------------- reliable update ----------------------------------------
+    // RU1: fold the low-precision increment into the FP64 solution.
+    for (int t = 0; t < ntiles; ++t)
+      for (int i = tiles[t].r0 + threadIdx.x; i < tiles[t].r1; i += kThreads) {
+        const V4<T> xa = P.xacc[i];
         V4<double> x = P.x64[i];
         x.x += double(xa.x); x.y += double(xa.y); x.z += double(xa.z);
         P.x64[i] = x;
         P.xacc[i] = V4<T>{T(0), T(0), T(0), T(0)};
       }
-    }
-    if (!grid_barrier(P.bar, G, gen, P.st)) return;
-    // RU2: r64 = rhs - A x64 in FP64 arithmetic; r, z restarted from it.
-    double rr64 = 0, rz2 = 0;
-    for (int tile = t0; tile < t1; ++tile) {
-      int r0 = P.tile_row[tile], r1 = P.tile_row[tile + 1];
-      int b0 = stage_tile(P, r0, r1, sA, sC);
-      int i = r0 + threadIdx.x;
-      if (i < r1) {
-        double a0 = 0, a1 = 0, a2 = 0;
-        for (int k = P.rowptr[i]; k < P.rowptr[i + 1]; ++k) {
-          V4<double> xj = P.x64[sC[k - b0]];
-          const T *blk = sA + size_t(k - b0) * 9;
-          a0 += double(blk[0]) * xj.x + double(blk[1]) * xj.y + double(blk[2]) * xj.z;
-          a1 += double(blk[3]) * xj.x + double(blk[4]) * xj.y + double(blk[5]) * xj.z;
-          a2 += double(blk[6]) * xj.x + double(blk[7]) * xj.y + double(blk[8]) * xj.z;
-        }
-        V4<double> b = P.rhs[i];
-        V4<T> m = P.fmask[i];
-        double e0 = (b.x - a0) * double(m.x), e1 = (b.y - a1) * double(m.y),
-               e2 = (b.z - a2) * double(m.z);
-        rr64 += e0 * e0 + e1 * e1 + e2 * e2;
-        V4<T> ri{T(e0), T(e1), T(e2), T(0)};
-        P.r[i] = ri;
-        V4<T> zi = apply_pc(P, i, ri);
-        P.z[i] = zi;
-        rz2 += double(ri.x) * double(zi.x) + double(ri.y) * double(zi.y) +
-               double(ri.z) * double(zi.z);
-      }
-      __syncthreads();
-    }
-    rr64 = block_sum(rr64, red);
-    rz2 = block_sum(rz2, red);
-    if (threadIdx.x == 0) { part_r64[cta] = rr64; part_rz[cta] = rz2; }
-    if (!grid_barrier(P.bar, G, gen, P.st)) return;
+    if (!grid_barrier(P.bar, G, epoch, P.st)) return;
+    // RU2: r = rhs - A x64 (FP64), s = A p
+    double rr64d = 0;
+    ru_residual(P, tiles, ntiles, cur, smem, rr64d);
+    V rr64 = A::from_d(rr64d), z0 = A::zero(), z1 = A::zero();
+    EOLC_PUBLISH_AND_SYNC(rr64, z0, z1);
     ++nref;
-    last_rr64 = reduce_partials(part_r64, G, red);
-    rz = reduce_partials(part_rz, G, red);
-    rmax2 = last_rr64;
-    if (!isfinite(last_rr64)) { status = EOLC_NONFINITE; break; }
-    if (last_rr64 <= tol2) converged = true;
+    last_rr64 = A::to_d(rr64);
+    rmax2 = rr64;
+    if (!A::finite(rr64)) { status = EOLC_NONFINITE; break; }
+    if (A::le(rr64, tol2)) { converged = true; break; }
+    // RU3: u = M r, w = A u for the replaced residual
+    V g3 = A::zero(), d3 = A::zero(), rr3 = A::zero();
+    cg_phase<T, true>(P, tiles, ntiles, cur, T(0), T(0), smem, g3, d3, rr3);
+    EOLC_PUBLISH_AND_SYNC(g3, d3, rr3);
+    gam = g3;
+    del = d3;
   }
+#undef EOLC_PUBLISH_AND_SYNC
   if (converged) status = EOLC_OK;
   if (cta == 0 && threadIdx.x == 0) {
     atomicCAS(&P.st->status, EOLC_OK, status);
@@ -363,15 +611,15 @@ pcg_kernel(Params<T> P) {
 
 // ---- set-up kernels (one launch each per solve) -----------------------------
 
-// rhs = mask * (-b - A beq_full) in FP64 (A promoted), plus the
-// preconditioner, r = rhs, z = M^-1 r, x = 0.
+// rhs = mask * (-b - A beq_full) in FP64 (A promoted), the preconditioner,
+// r = rhs, x = 0, p = s = 0.
 template <typename T>
 __global__ void setup_kernel(int n_nodes, const int *rowptr, const int *colidx,
                              const int *diag, const T *A, const double *b,
                              const double *beq_full, const uint8_t *pinned,
                              int block_pc, V4<double> *rhs, V4<double> *x64,
-                             V4<T> *r, V4<T> *z, V4<T> *pa, V4<T> *xacc,
-                             T *pc, V4<T> *fmask) {
+                             V4<T> *r, V4<T> *p, V4<T> *s, V4<T> *xacc, T *pc,
+                             V4<T> *fmask) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_nodes) return;
   double a[3] = {0, 0, 0};
@@ -391,8 +639,6 @@ __global__ void setup_kernel(int n_nodes, const int *rowptr, const int *colidx,
   x64[i] = V4<double>{0.0, 0.0, 0.0, 0.0};
   fmask[i] = V4<T>{m[0], m[1], m[2], T(0)};
   const T *D = A + size_t(diag[i]) * 9;
-  V4<T> ri{T(e[0]), T(e[1]), T(e[2]), T(0)};
-  V4<T> zi;
   if (block_pc) {
     // inverse of the free-free part of the diagonal block (pinned rows and
     // columns replaced by the identity, then masked)
@@ -423,49 +669,32 @@ __global__ void setup_kernel(int n_nodes, const int *rowptr, const int *colidx,
     for (int rr = 0; rr < 3; ++rr)
       for (int c = 0; c < 3; ++c)
         pc[size_t(9) * i + 3 * rr + c] = T(inv[3 * rr + c] * double(m[rr]) * double(m[c]));
-    const T *B = pc + size_t(9) * i;
-    zi.x = B[0] * ri.x + B[1] * ri.y + B[2] * ri.z;
-    zi.y = B[3] * ri.x + B[4] * ri.y + B[5] * ri.z;
-    zi.z = B[6] * ri.x + B[7] * ri.y + B[8] * ri.z;
   } else {
     // Eigen's DiagonalPreconditioner: 1/diag, 1 where the diagonal is 0
-    T d[3];
     for (int c = 0; c < 3; ++c) {
       T dd = D[4 * c];
-      d[c] = (dd != T(0) ? T(1) / dd : T(1)) * m[c];
-      pc[size_t(4) * i + c] = d[c];
+      pc[size_t(4) * i + c] = (dd != T(0) ? T(1) / dd : T(1)) * m[c];
     }
     pc[size_t(4) * i + 3] = T(0);
-    zi.x = d[0] * ri.x; zi.y = d[1] * ri.y; zi.z = d[2] * ri.z;
   }
-  zi.w = T(0);
-  r[i] = ri;
-  z[i] = zi;
-  pa[i] = V4<T>{T(0), T(0), T(0), T(0)};
-  xacc[i] = V4<T>{T(0), T(0), T(0), T(0)};
+  const V4<T> zero{T(0), T(0), T(0), T(0)};
+  r[i] = V4<T>{T(e[0]), T(e[1]), T(e[2]), T(0)};
+  p[i] = zero;
+  s[i] = zero;
+  xacc[i] = zero;
 }
 
-// Per-CTA-of-setup partial sums of ||rhs||^2 and r.z, reduced by one block.
-template <typename T>
-__global__ void init_sums_kernel(int n_nodes, const V4<double> *rhs,
-                                 const V4<T> *r, const V4<T> *z, double *part,
-                                 int G, DevStatus *st) {
-  __shared__ double red[kThreads / 32 + 1];
-  double s_rhs = 0, s_rz = 0;
+// ||rhs||^2 by one CTA; resets the status record.
+__global__ void __launch_bounds__(kThreads) init_sums_kernel(int n_nodes, const V4<double> *rhs,
+                                                             DevStatus *st) {
+  __shared__ double red[3 * (kThreads / 32 + 1)];
+  double s_rhs = 0, d0 = 0, d1 = 0;
   for (int i = threadIdx.x; i < n_nodes; i += kThreads) {
     V4<double> b = rhs[i];
-    V4<T> ri = r[i], zi = z[i];
     s_rhs += b.x * b.x + b.y * b.y + b.z * b.z;
-    s_rz += double(ri.x) * double(zi.x) + double(ri.y) * double(zi.y) +
-            double(ri.z) * double(zi.z);
   }
-  s_rhs = block_sum(s_rhs, red);
-  s_rz = block_sum(s_rz, red);
-  for (int k = threadIdx.x; k < 5 * G; k += kThreads) part[k] = 0.0;
-  __syncthreads();
+  block_sum3<double>(s_rhs, d0, d1, red);
   if (threadIdx.x == 0) {
-    part[G] = s_rz;       // part_rz
-    part[2 * G] = s_rhs;  // part_rr (initial residual = rhs since x0 = 0)
     st->status = EOLC_OK;
     st->iterations = 0;
     st->refinements = 0;
@@ -474,7 +703,6 @@ __global__ void init_sums_kernel(int n_nodes, const V4<double> *rhs,
   }
 }
 
-template <typename T>
 __global__ void finish_kernel(int n_nodes, const V4<double> *x64,
                               const double *beq_full, const uint8_t *pinned,
                               double *v) {
@@ -495,61 +723,97 @@ struct SolveWork {
   DevBuf<double> part;
   DevBuf<unsigned> bar;
   DevBuf<DevStatus> st;
-  DevBuf<int> tile_row, cta_tile;
+  DevBuf<int> tile_row, tile_wptr, wlist, cta_tile;
+  DevBuf<uint16_t> lcol;
   DevBuf<unsigned char> pc;
-  std::vector<int> h_tile_row, h_cta_tile;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  ~SolveWork() {
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+  }
 };
 
 void free_solve_work(SolveWork *w) { delete w; }
 
 namespace {
 
+// Tiles of <= kTileRows rows whose staged values, local columns and halo fit
+// the shared-memory budget; the halo list and tile-local columns are built
+// here once per topology.
+std::string build_tiles(int N, const std::vector<int> &rowptr,
+                        const std::vector<int> &colidx, int cap, int win_cap,
+                        std::vector<int> &tiles, std::vector<int> &wptr,
+                        std::vector<int> &wlist, std::vector<uint16_t> &lcol) {
+  tiles.assign(1, 0);
+  wptr.assign(1, 0);
+  wlist.clear();
+  lcol.assign(colidx.size(), 0);
+  std::vector<int> stamp(N, -1), local(N, 0);
+  int start = 0;
+  std::vector<int> win;
+  while (start < N) {
+    int end = start;
+    win.clear();
+    // grow the tile row by row while it fits
+    while (end < N && end - start < kTileRows) {
+      if (rowptr[end + 1] - rowptr[start] > cap) break;
+      int added = 0;
+      for (int k = rowptr[end]; k < rowptr[end + 1]; ++k)
+        if (stamp[colidx[k]] != start) added++;
+      if (int(win.size()) + added > win_cap) break;
+      for (int k = rowptr[end]; k < rowptr[end + 1]; ++k)
+        if (stamp[colidx[k]] != start) { stamp[colidx[k]] = start; win.push_back(colidx[k]); }
+      ++end;
+    }
+    if (end == start) return "a block row does not fit the shared-memory tile";
+    // every own row is in its window (the diagonal block is always present)
+    std::sort(win.begin(), win.end());
+    for (int j = 0; j < int(win.size()); ++j) local[win[j]] = j;
+    for (int k = rowptr[start]; k < rowptr[end]; ++k) lcol[k] = uint16_t(local[colidx[k]]);
+    wlist.insert(wlist.end(), win.begin(), win.end());
+    wptr.push_back(int(wlist.size()));
+    tiles.push_back(end);
+    start = end;
+  }
+  return "";
+}
+
 template <typename T>
 eolc_status run_pcg_t(SolveWork *&w, const PcgArgs &a, eolc_solve_info *info,
-                      cudaStream_t s, std::string &err) {
+                      cudaStream_t s, std::string &err, long long &launches) {
   const DevTopology &Tp = *a.T;
   const int N = Tp.n_nodes;
-  const T *A = std::is_same<T, double>::value
-                   ? reinterpret_cast<const T *>(a.A64)
-                   : reinterpret_cast<const T *>(a.A32);
+  const T *A = std::is_same<T, double>::value ? reinterpret_cast<const T *>(a.A64)
+                                              : reinterpret_cast<const T *>(a.A32);
   int dev = 0;
   cudaGetDevice(&dev);
   int n_sm = 0;
   cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
-  const int cap_blocks = kSmemBytes / (9 * sizeof(T) + sizeof(int));
-  size_t smem = size_t(cap_blocks) * 9 * sizeof(T) + size_t(cap_blocks) * sizeof(int);
-  cudaFuncSetAttribute(pcg_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       int(smem));
+  const size_t smem = smem_bytes<T>();
+  cudaFuncSetAttribute(cg_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_kernel<T>, kThreads, smem);
-  if (per_sm < 1) { err = "pcg kernel does not fit on an SM"; return EOLC_CUDA_ERROR; }
-  per_sm = std::min(per_sm, 2);
-  const int want_G = n_sm * per_sm;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cg_kernel<T>, kThreads, smem);
+  if (per_sm < 1) { err = "cg kernel does not fit on an SM"; return EOLC_CUDA_ERROR; }
+  const int want_G = n_sm;  // one CTA per SM
   const int prec = std::is_same<T, double>::value ? 0 : 1;
+  const int bpc = a.precond == EOLC_PC_BLOCK_JACOBI ? 1 : 0;
   if (!w) w = new SolveWork();
-  if (w->n_nodes != N || w->n_blocks != Tp.n_blocks || w->prec != prec ||
-      w->G != want_G || w->block_pc != (a.precond == EOLC_PC_BLOCK_JACOBI)) {
-    // tiles: <= kTileRows rows and <= cap_blocks blocks each
-    std::vector<int> rowptr(N + 1);
+  if (w->n_nodes != N || w->n_blocks != Tp.n_blocks || w->prec != prec || w->block_pc != bpc) {
+    std::vector<int> rowptr(N + 1), colidx(Tp.n_blocks);
     cudaMemcpy(rowptr.data(), Tp.rowptr.p, sizeof(int) * (N + 1), cudaMemcpyDeviceToHost);
-    std::vector<int> tiles{0};
-    int start = 0;
-    for (int i = 0; i < N; ++i) {
-      int rows = i + 1 - start;
-      int blocks = rowptr[i + 1] - rowptr[start];
-      if (rowptr[i + 1] - rowptr[i] > cap_blocks) { err = "row too long"; return EOLC_BAD_ARG; }
-      if (rows > kTileRows || blocks > cap_blocks) {
-        tiles.push_back(i);
-        start = i;
-      }
-    }
-    tiles.push_back(N);
-    int nt = int(tiles.size()) - 1;
-    int G = std::min(want_G, nt);
-    // contiguous tile ranges balanced by block count
+    cudaMemcpy(colidx.data(), Tp.colidx.p, sizeof(int) * Tp.n_blocks, cudaMemcpyDeviceToHost);
+    std::vector<int> tiles, wptr, wlist;
+    std::vector<uint16_t> lcol;
+    std::string msg = build_tiles(N, rowptr, colidx, cap_blocks<T>(), win_max<T>(), tiles, wptr,
+                                  wlist, lcol);
+    if (!msg.empty()) { err = msg; return EOLC_BAD_ARG; }
+    const int nt = int(tiles.size()) - 1;
+    const int G = std::min(want_G, nt);
+    if ((nt + G - 1) / G > kMaxCtaTiles / 2) { err = "matrix too large for one solve"; return EOLC_BAD_ARG; }
+    // contiguous tile ranges per CTA, balanced by block count
     std::vector<int> cta(G + 1, nt);
     cta[0] = 0;
-    long long total = rowptr[N];
+    const long long total = rowptr[N];
     int t = 0;
     for (int c = 1; c < G; ++c) {
       long long target = total * c / G;
@@ -557,22 +821,28 @@ eolc_status run_pcg_t(SolveWork *&w, const PcgArgs &a, eolc_solve_info *info,
       cta[c] = std::max(t, cta[c - 1] + 1);
       if (cta[c] > nt - (G - c)) cta[c] = nt - (G - c);
     }
-    w->h_tile_row = tiles;
-    w->h_cta_tile = cta;
+    for (int c = 0; c < G; ++c)
+      if (cta[c + 1] - cta[c] > kMaxCtaTiles) { err = "tile partition too uneven"; return EOLC_BAD_ARG; }
+    // local columns are padded by 8 entries for the 16-byte staging tail
+    lcol.resize(lcol.size() + 8, 0);
     w->G = G;
     w->n_nodes = N;
     w->n_blocks = Tp.n_blocks;
     w->prec = prec;
-    w->block_pc = a.precond == EOLC_PC_BLOCK_JACOBI;
-    cudaError_t e1 = w->tile_row.upload(tiles.data(), tiles.size(), s);
-    cudaError_t e2 = w->cta_tile.upload(cta.data(), cta.size(), s);
-    size_t vb = size_t(N) * (sizeof(V4<double>) * 2 + sizeof(V4<T>) * 7);
-    cudaError_t e3 = w->vecs.resize(vb);
-    cudaError_t e4 = w->part.resize(size_t(5) * G);
-    cudaError_t e5 = w->bar.resize(2);
-    cudaError_t e6 = w->st.resize(1);
-    cudaError_t e7 = w->pc.resize(size_t(N) * 9 * sizeof(T));
-    for (cudaError_t e : {e1, e2, e3, e4, e5, e6, e7})
+    w->block_pc = bpc;
+    cudaError_t es[] = {
+        w->tile_row.upload(tiles.data(), tiles.size(), s),
+        w->tile_wptr.upload(wptr.data(), wptr.size(), s),
+        w->wlist.upload(wlist.data(), std::max<size_t>(wlist.size(), 1), s),
+        w->lcol.upload(lcol.data(), lcol.size(), s),
+        w->cta_tile.upload(cta.data(), cta.size(), s),
+        w->vecs.resize(size_t(N) * (sizeof(V4<double>) * 2 + sizeof(V4<T>) * 9)),
+        w->part.resize(size_t(6) * G),
+        w->bar.resize(2),
+        w->st.resize(1),
+        w->pc.resize(size_t(N) * 9 * sizeof(T)),
+        cudaStreamSynchronize(s)};
+    for (cudaError_t e : es)
       if (e != cudaSuccess) { err = cudaGetErrorString(e); return EOLC_CUDA_ERROR; }
   }
   const int G = w->G;
@@ -580,26 +850,30 @@ eolc_status run_pcg_t(SolveWork *&w, const PcgArgs &a, eolc_solve_info *info,
   V4<double> *rhs = reinterpret_cast<V4<double> *>(vp); vp += sizeof(V4<double>) * N;
   V4<double> *x64 = reinterpret_cast<V4<double> *>(vp); vp += sizeof(V4<double>) * N;
   V4<T> *vr = reinterpret_cast<V4<T> *>(vp);
-  V4<T> *r = vr, *z = vr + N, *pa = vr + 2 * N, *pb = vr + 3 * N, *q = vr + 4 * N,
-        *xacc = vr + 5 * N, *fmask = vr + 6 * N;
-  T *pc = reinterpret_cast<T *>(w->pc.p);
-  int bpc = a.precond == EOLC_PC_BLOCK_JACOBI ? 1 : 0;
-  setup_kernel<T><<<(N + 127) / 128, 128, 0, s>>>(
-      N, Tp.rowptr.p, Tp.colidx.p, Tp.diag.p, A, a.b, a.beq_full, a.pinned, bpc,
-      rhs, x64, r, z, pa, xacc, pc, fmask);
-  init_sums_kernel<T><<<1, kThreads, 0, s>>>(N, rhs, r, z, w->part.p, G, w->st.p);
-  cudaMemsetAsync(w->bar.p, 0, sizeof(unsigned) * 2, s);
   Params<T> P;
+  P.r[0] = vr; P.r[1] = vr + N;
+  P.w[0] = vr + 2 * N; P.w[1] = vr + 3 * N;
+  P.s[0] = vr + 4 * N; P.s[1] = vr + 5 * N;
+  P.p = vr + 6 * N;
+  P.xacc = vr + 7 * N;
+  V4<T> *fmask = vr + 8 * N;
+  T *pc = reinterpret_cast<T *>(w->pc.p);
+  setup_kernel<T><<<(N + 127) / 128, 128, 0, s>>>(
+      N, Tp.rowptr.p, Tp.colidx.p, Tp.diag.p, A, a.b, a.beq_full, a.pinned, bpc, rhs, x64,
+      P.r[0], P.p, P.s[0], P.xacc, pc, fmask);
+  init_sums_kernel<<<1, kThreads, 0, s>>>(N, rhs, w->st.p);
+  cudaMemsetAsync(w->bar.p, 0, sizeof(unsigned) * 2, s);
   P.n_nodes = N;
   P.n_ctas = G;
   P.rowptr = Tp.rowptr.p;
-  P.colidx = Tp.colidx.p;
   P.A = A;
+  P.lcol = w->lcol.p;
   P.tile_row = w->tile_row.p;
+  P.tile_wptr = w->tile_wptr.p;
+  P.wlist = w->wlist.p;
   P.cta_tile = w->cta_tile.p;
   P.rhs = rhs;
   P.x64 = x64;
-  P.r = r; P.z = z; P.pa = pa; P.pb = pb; P.q = q; P.xacc = xacc;
   P.pc = pc;
   P.fmask = fmask;
   P.part = w->part.p;
@@ -608,21 +882,28 @@ eolc_status run_pcg_t(SolveWork *&w, const PcgArgs &a, eolc_solve_info *info,
   P.max_iter = a.max_iter;
   P.block_pc = bpc;
   P.tol2 = a.rel_tol * a.rel_tol;
-  DevStatus hs;
   void *args[] = {&P};
-  cudaError_t e = cudaLaunchCooperativeKernel((void *)pcg_kernel<T>, dim3(G), dim3(kThreads),
-                                  args, smem, s);
+  if (!w->ev0) { cudaEventCreate(&w->ev0); cudaEventCreate(&w->ev1); }
+  cudaEventRecord(w->ev0, s);
+  cudaError_t e = cudaLaunchCooperativeKernel((void *)cg_kernel<T>, dim3(G), dim3(kThreads),
+                                              args, smem, s);
   if (e != cudaSuccess) { err = cudaGetErrorString(e); return EOLC_CUDA_ERROR; }
-  finish_kernel<T><<<(N + 127) / 128, 128, 0, s>>>(N, x64, a.beq_full, a.pinned, a.v);
+  cudaEventRecord(w->ev1, s);
+  finish_kernel<<<(N + 127) / 128, 128, 0, s>>>(N, x64, a.beq_full, a.pinned, a.v);
+  launches += 4;  // setup, init_sums, cg, finish
+  DevStatus hs;
   cudaMemcpyAsync(&hs, w->st.p, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
   e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) { err = cudaGetErrorString(e); return EOLC_CUDA_ERROR; }
+  float kms = 0.f;
+  cudaEventElapsedTime(&kms, w->ev0, w->ev1);
   if (info) {
     info->status = hs.status;
     info->iterations = hs.iterations;
     info->refinements = hs.refinements;
     info->used_fallback = 0;
     info->rel_res = hs.rel_res;
+    info->solve_kernel_ms = kms;
   }
   if (hs.status != EOLC_OK) {
     err = hs.status == EOLC_TIMEOUT ? "grid barrier timed out"
@@ -636,9 +917,9 @@ eolc_status run_pcg_t(SolveWork *&w, const PcgArgs &a, eolc_solve_info *info,
 }  // namespace
 
 eolc_status run_pcg(SolveWork *&w, const PcgArgs &a, eolc_solve_info *info,
-                    cudaStream_t s, std::string &err) {
-  if (a.precision == EOLC_PREC_FP64) return run_pcg_t<double>(w, a, info, s, err);
-  return run_pcg_t<float>(w, a, info, s, err);
+                    cudaStream_t s, std::string &err, long long &launches) {
+  if (a.precision == EOLC_PREC_FP64) return run_pcg_t<double>(w, a, info, s, err, launches);
+  return run_pcg_t<float>(w, a, info, s, err, launches);
 }
 
 }  // namespace eolc

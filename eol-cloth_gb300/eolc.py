@@ -55,7 +55,8 @@ class SolveOpts(ctypes.Structure):
 class SolveInfo(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("iterations", ctypes.c_int),
                 ("refinements", ctypes.c_int), ("used_fallback", ctypes.c_int),
-                ("rel_res", ctypes.c_double)]
+                ("rel_res", ctypes.c_double), ("solve_kernel_ms", ctypes.c_double),
+                ("assemble_ms", ctypes.c_double)]
 
 
 class Box(ctypes.Structure):
@@ -84,7 +85,7 @@ _I = ctypes.POINTER(ctypes.c_int)
 _V = ctypes.c_void_p
 
 # Every symbol the C ABI exports (include/eolc.h).
-EXPORTS = ["eolc_version", "eolc_create", "eolc_destroy", "eolc_last_error", "eolc_set_stream",
+EXPORTS = ["eolc_version", "eolc_launch_count", "eolc_create", "eolc_destroy", "eolc_last_error", "eolc_set_stream",
            "eolc_set_topology", "eolc_bsr_pattern", "eolc_forces_fill", "eolc_velocity_solve",
            "eolc_step", "eolc_state_upload", "eolc_state_download", "eolc_step_resident",
            "eolc_cd2"]
@@ -95,6 +96,8 @@ def load_library(path=LIB_PATH):
         raise ImportError("libeolc.so is not built (%s); run __graft_entry__.build()" % path)
     L = ctypes.CDLL(path)
     L.eolc_version.restype = ctypes.c_int
+    L.eolc_launch_count.argtypes = [_V]
+    L.eolc_launch_count.restype = ctypes.c_longlong
     L.eolc_create.argtypes = [ctypes.POINTER(_V), ctypes.c_int]
     L.eolc_destroy.argtypes = [_V]
     L.eolc_destroy.restype = None
@@ -122,7 +125,7 @@ def load_library(path=LIB_PATH):
             raise ImportError("libeolc.so lacks %s" % name)
         getattr(L, name).restype = getattr(L, name).restype
     for name in EXPORTS:
-        if name not in ("eolc_version", "eolc_destroy", "eolc_last_error"):
+        if name not in ("eolc_version", "eolc_destroy", "eolc_last_error", "eolc_launch_count"):
             getattr(L, name).restype = ctypes.c_int
     return L
 
@@ -165,6 +168,13 @@ class Context:
     @property
     def handle(self):
         return self._h
+
+    def launch_count(self):
+        return lib.eolc_launch_count(self._h)
+
+    def set_stream(self, stream_handle):
+        """Run on an external cudaStream_t (an integer handle), e.g. torch's."""
+        self._check(lib.eolc_set_stream(self._h, _V(stream_handle)))
 
     def _check(self, st):
         if st != OK:

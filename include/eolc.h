@@ -81,6 +81,8 @@ typedef struct {
   int refinements;   /* FP64 true-residual recomputations                 */
   int used_fallback; /* 1 if the learned PC fell back to Jacobi           */
   double rel_res;    /* final FP64 ||b - A v|| / ||b|| on the free DOFs    */
+  double solve_kernel_ms; /* device time of the PCG kernel(s), CUDA events */
+  double assemble_ms;     /* device time of the assembly kernels          */
 } eolc_solve_info;
 
 typedef struct eolc_ctx eolc_ctx;
@@ -92,6 +94,8 @@ const char *eolc_last_error(const eolc_ctx *ctx);
 /* stream is a cudaStream_t; NULL selects the context's own stream. */
 eolc_status eolc_set_stream(eolc_ctx *ctx, void *stream);
 int eolc_version(void);
+/* Number of kernels this context has launched so far (telemetry). */
+long long eolc_launch_count(const eolc_ctx *ctx);
 
 /* ---- topology (Mesh::add(Face) adjacency, ArcSim mesh.cpp:356-378) -----
  * tri_h:   n_tri x 3 node indices, face vertex order as in Face::v[0..2].

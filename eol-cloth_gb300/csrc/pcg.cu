@@ -36,6 +36,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -923,3 +924,234 @@ eolc_status run_pcg(SolveWork *&w, const PcgArgs &a, eolc_solve_info *info,
 }
 
 }  // namespace eolc
+
+// ===========================================================================
+// Velocity solve that allocates nothing on the device.
+//
+// For callers that cannot call cudaMalloc on their step path: an interactive
+// stepping thread (the reference's online mode steps and renders every frame)
+// cannot afford cudaMalloc/cudaFree, which may synchronize the device and take
+// milliseconds, and a host framework that reserves all device memory in its
+// own pool leaves nothing for a library allocator.  This entry point runs the
+// same mixed-precision Jacobi PCG kernels as eolc_velocity_solve, with every
+// scratch buffer carved out of one file-scope device array of fixed size.
+// The caller passes the matrix, right-hand side and solution in its own
+// device buffers.  Limits: EOLC_STATIC_MAX_NODES block rows and
+// EOLC_STATIC_MAX_BLOCKS 3x3 blocks.
+// ===========================================================================
+namespace eolc {
+namespace {
+
+constexpr size_t kStaticMaxCtas = 1024;
+
+constexpr size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct StaticLayout {
+  size_t A, rowptr, colidx, diag, lcol, wlist, tile_row, tile_wptr, cta_tile, pinned,
+      beq, vecs, pc, part, bar, st, total;
+};
+
+constexpr StaticLayout static_layout() {
+  StaticLayout L{};
+  const size_t N = EOLC_STATIC_MAX_NODES, NB = EOLC_STATIC_MAX_BLOCKS;
+  size_t o = 0;
+  L.A = o;         o += al256((NB * 9 + 16) * sizeof(float));
+  L.rowptr = o;    o += al256((N + 1) * sizeof(int));
+  L.colidx = o;    o += al256(NB * sizeof(int));
+  L.diag = o;      o += al256(N * sizeof(int));
+  L.lcol = o;      o += al256((NB + 8) * sizeof(uint16_t));
+  L.wlist = o;     o += al256(NB * sizeof(int));  // windows never exceed the blocks
+  L.tile_row = o;  o += al256((N + 1) * sizeof(int));
+  L.tile_wptr = o; o += al256((N + 1) * sizeof(int));
+  L.cta_tile = o;  o += al256((kStaticMaxCtas + 1) * sizeof(int));
+  L.pinned = o;    o += al256(3 * N);
+  L.beq = o;       o += al256(3 * N * sizeof(double));
+  L.vecs = o;      o += al256(N * (2 * sizeof(V4<double>) + 9 * sizeof(V4<float>)));
+  L.pc = o;        o += al256(N * 4 * sizeof(float));
+  L.part = o;      o += al256(6 * kStaticMaxCtas * sizeof(double));
+  L.bar = o;       o += al256(2 * sizeof(unsigned));
+  L.st = o;        o += al256(sizeof(DevStatus));
+  L.total = o;
+  return L;
+}
+
+constexpr StaticLayout kStatic = static_layout();
+
+}  // namespace
+}  // namespace eolc
+
+// The scratch itself: every GPU that loads this library holds it until exit.
+static __device__ __align__(256) unsigned char g_eolc_static_scratch[eolc::kStatic.total];
+
+namespace {
+std::mutex g_static_mutex;
+void *g_static_addr[64] = {nullptr};  // symbol address per device, set once
+}  // namespace
+
+extern "C" eolc_status eolc_velocity_solve_static(
+    int n_nodes, const int *rowptr_h, const int *colidx_h, const float *mdk_d,
+    const double *b_d, const int *fixed_dofs_h, const double *beq_h, int n_fixed,
+    double rel_tol, int max_iter, double *v_d, eolc_solve_info *info, void *stream) {
+  using namespace eolc;
+  using T = float;
+  if (n_nodes <= 0 || !rowptr_h || !colidx_h || !mdk_d || !b_d || !v_d ||
+      (n_fixed > 0 && (!fixed_dofs_h || !beq_h)) || n_fixed < 0 || !(rel_tol > 0) ||
+      max_iter <= 0)
+    return EOLC_BAD_ARG;
+  if (n_nodes > EOLC_STATIC_MAX_NODES) return EOLC_CAPACITY;
+  const int nb = rowptr_h[n_nodes];
+  if (nb <= 0 || nb > EOLC_STATIC_MAX_BLOCKS) return EOLC_CAPACITY;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return EOLC_CUDA_ERROR;
+  unsigned char *base = nullptr;
+  {
+    // one-time set-up per device, with that device current
+    std::lock_guard<std::mutex> lock(g_static_mutex);
+    if (!g_static_addr[dev]) {
+      void *p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_eolc_static_scratch) != cudaSuccess || !p)
+        return EOLC_CUDA_ERROR;
+      g_static_addr[dev] = p;
+    }
+    base = static_cast<unsigned char *>(g_static_addr[dev]);
+  }
+  // pattern checks and host-side tiling (host memory only)
+  std::vector<int> rowptr(rowptr_h, rowptr_h + n_nodes + 1), colidx(colidx_h, colidx_h + nb);
+  std::vector<int> diag(n_nodes, -1);
+  for (int i = 0; i < n_nodes; ++i) {
+    if (rowptr[i + 1] < rowptr[i]) return EOLC_BAD_ARG;
+    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+      if (colidx[k] < 0 || colidx[k] >= n_nodes) return EOLC_BAD_ARG;
+      if (colidx[k] == i) diag[i] = k;
+    }
+    if (diag[i] < 0) return EOLC_BAD_ARG;
+  }
+  std::vector<int> tiles, wptr, wlist;
+  std::vector<uint16_t> lcol;
+  if (!build_tiles(n_nodes, rowptr, colidx, cap_blocks<T>(), win_max<T>(), tiles, wptr, wlist,
+                   lcol).empty())
+    return EOLC_BAD_ARG;
+  lcol.resize(lcol.size() + 8, 0);
+  const int nt = int(tiles.size()) - 1;
+  int n_sm = 0;
+  cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+  const int G = std::min({n_sm, nt, int(kStaticMaxCtas)});
+  if ((nt + G - 1) / G > kMaxCtaTiles / 2) return EOLC_CAPACITY;
+  std::vector<int> cta(G + 1, nt);
+  cta[0] = 0;
+  {
+    const long long total = rowptr[n_nodes];
+    int t = 0;
+    for (int c = 1; c < G; ++c) {
+      long long target = total * c / G;
+      while (t < nt && rowptr[tiles[t]] < target) ++t;
+      cta[c] = std::max(t, cta[c - 1] + 1);
+      if (cta[c] > nt - (G - c)) cta[c] = nt - (G - c);
+    }
+  }
+  for (int c = 0; c < G; ++c)
+    if (cta[c + 1] - cta[c] > kMaxCtaTiles) return EOLC_CAPACITY;
+  std::vector<uint8_t> pinned(size_t(3) * n_nodes, 0);
+  std::vector<double> beq_full(size_t(3) * n_nodes, 0.0);
+  for (int k = 0; k < n_fixed; ++k) {
+    if (fixed_dofs_h[k] < 0 || fixed_dofs_h[k] >= 3 * n_nodes) return EOLC_BAD_ARG;
+    pinned[fixed_dofs_h[k]] = 1;
+    beq_full[fixed_dofs_h[k]] = beq_h[k];
+  }
+  const StaticLayout &L = kStatic;
+  T *A = reinterpret_cast<T *>(base + L.A);
+  int *d_rowptr = reinterpret_cast<int *>(base + L.rowptr);
+  int *d_colidx = reinterpret_cast<int *>(base + L.colidx);
+  int *d_diag = reinterpret_cast<int *>(base + L.diag);
+  uint16_t *d_lcol = reinterpret_cast<uint16_t *>(base + L.lcol);
+  int *d_wlist = reinterpret_cast<int *>(base + L.wlist);
+  int *d_tile_row = reinterpret_cast<int *>(base + L.tile_row);
+  int *d_tile_wptr = reinterpret_cast<int *>(base + L.tile_wptr);
+  int *d_cta = reinterpret_cast<int *>(base + L.cta_tile);
+  uint8_t *d_pinned = base + L.pinned;
+  double *d_beq = reinterpret_cast<double *>(base + L.beq);
+  double *d_part = reinterpret_cast<double *>(base + L.part);
+  unsigned *d_bar = reinterpret_cast<unsigned *>(base + L.bar);
+  DevStatus *d_st = reinterpret_cast<DevStatus *>(base + L.st);
+  const int N = n_nodes;
+  unsigned char *vp = base + L.vecs;
+  V4<double> *rhs = reinterpret_cast<V4<double> *>(vp); vp += sizeof(V4<double>) * N;
+  V4<double> *x64 = reinterpret_cast<V4<double> *>(vp); vp += sizeof(V4<double>) * N;
+  V4<T> *vr = reinterpret_cast<V4<T> *>(vp);
+  T *pc = reinterpret_cast<T *>(base + L.pc);
+  cudaError_t es[] = {
+      cudaMemcpyAsync(A, mdk_d, sizeof(T) * size_t(nb) * 9, cudaMemcpyDeviceToDevice, s),
+      cudaMemsetAsync(A + size_t(nb) * 9, 0, sizeof(T) * 16, s),
+      cudaMemcpyAsync(d_rowptr, rowptr.data(), sizeof(int) * (N + 1), cudaMemcpyHostToDevice, s),
+      cudaMemcpyAsync(d_colidx, colidx.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s),
+      cudaMemcpyAsync(d_diag, diag.data(), sizeof(int) * N, cudaMemcpyHostToDevice, s),
+      cudaMemcpyAsync(d_lcol, lcol.data(), sizeof(uint16_t) * lcol.size(), cudaMemcpyHostToDevice, s),
+      cudaMemcpyAsync(d_wlist, wlist.data(), sizeof(int) * std::max<size_t>(wlist.size(), 1),
+                      cudaMemcpyHostToDevice, s),
+      cudaMemcpyAsync(d_tile_row, tiles.data(), sizeof(int) * tiles.size(), cudaMemcpyHostToDevice, s),
+      cudaMemcpyAsync(d_tile_wptr, wptr.data(), sizeof(int) * wptr.size(), cudaMemcpyHostToDevice, s),
+      cudaMemcpyAsync(d_cta, cta.data(), sizeof(int) * cta.size(), cudaMemcpyHostToDevice, s),
+      cudaMemcpyAsync(d_pinned, pinned.data(), pinned.size(), cudaMemcpyHostToDevice, s),
+      cudaMemcpyAsync(d_beq, beq_full.data(), sizeof(double) * beq_full.size(),
+                      cudaMemcpyHostToDevice, s),
+      // the array keeps the previous call's contents: the barrier counter and
+      // the partial sums must start at zero
+      cudaMemsetAsync(d_bar, 0, sizeof(unsigned) * 2, s),
+      cudaMemsetAsync(d_part, 0, sizeof(double) * 6 * G, s)};
+  for (cudaError_t e : es)
+    if (e != cudaSuccess) return EOLC_CUDA_ERROR;
+  Params<T> P;
+  P.r[0] = vr; P.r[1] = vr + N;
+  P.w[0] = vr + 2 * N; P.w[1] = vr + 3 * N;
+  P.s[0] = vr + 4 * N; P.s[1] = vr + 5 * N;
+  P.p = vr + 6 * N;
+  P.xacc = vr + 7 * N;
+  V4<T> *fmask = vr + 8 * N;
+  setup_kernel<T><<<(N + 127) / 128, 128, 0, s>>>(N, d_rowptr, d_colidx, d_diag, A, b_d, d_beq,
+                                                   d_pinned, 0, rhs, x64, P.r[0], P.p, P.s[0],
+                                                   P.xacc, pc, fmask);
+  init_sums_kernel<<<1, kThreads, 0, s>>>(N, rhs, d_st);
+  P.n_nodes = N;
+  P.n_ctas = G;
+  P.rowptr = d_rowptr;
+  P.A = A;
+  P.lcol = d_lcol;
+  P.tile_row = d_tile_row;
+  P.tile_wptr = d_tile_wptr;
+  P.wlist = d_wlist;
+  P.cta_tile = d_cta;
+  P.rhs = rhs;
+  P.x64 = x64;
+  P.pc = pc;
+  P.fmask = fmask;
+  P.part = d_part;
+  P.bar = d_bar;
+  P.st = d_st;
+  P.max_iter = max_iter;
+  P.block_pc = 0;
+  P.tol2 = rel_tol * rel_tol;
+  const size_t smem = smem_bytes<T>();
+  if (cudaFuncSetAttribute(cg_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           int(smem)) != cudaSuccess)
+    return EOLC_CUDA_ERROR;
+  void *args[] = {&P};
+  if (cudaLaunchCooperativeKernel((void *)cg_kernel<T>, dim3(G), dim3(kThreads), args, smem, s) !=
+      cudaSuccess)
+    return EOLC_CUDA_ERROR;
+  finish_kernel<<<(N + 127) / 128, 128, 0, s>>>(N, x64, d_beq, d_pinned, v_d);
+  DevStatus hs;
+  if (cudaMemcpyAsync(&hs, d_st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return EOLC_CUDA_ERROR;
+  if (info) {
+    info->status = hs.status;
+    info->iterations = hs.iterations;
+    info->refinements = hs.refinements;
+    info->used_fallback = 0;
+    info->rel_res = hs.rel_res;
+    info->solve_kernel_ms = 0.0;
+    info->assemble_ms = 0.0;
+  }
+  return eolc_status(hs.status);
+}

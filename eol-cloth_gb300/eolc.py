@@ -88,7 +88,7 @@ _V = ctypes.c_void_p
 EXPORTS = ["eolc_version", "eolc_launch_count", "eolc_create", "eolc_destroy", "eolc_last_error", "eolc_set_stream",
            "eolc_set_topology", "eolc_bsr_pattern", "eolc_forces_fill", "eolc_velocity_solve",
            "eolc_step", "eolc_state_upload", "eolc_state_download", "eolc_step_resident",
-           "eolc_cd2"]
+           "eolc_cd2", "eolc_velocity_solve_static"]
 
 
 def load_library(path=LIB_PATH):
@@ -120,6 +120,9 @@ def load_library(path=LIB_PATH):
                                      ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveInfo)]
     L.eolc_cd2.argtypes = [_V, _D, ctypes.POINTER(Box), ctypes.c_int, _D, _D, ctypes.c_int,
                            ctypes.c_double, ctypes.POINTER(Contact), ctypes.c_int, _I]
+    L.eolc_velocity_solve_static.argtypes = [ctypes.c_int, _I, _I, _V, _V, _I, _D, ctypes.c_int,
+                                             ctypes.c_double, ctypes.c_int, _V,
+                                             ctypes.POINTER(SolveInfo), _V]
     for name in EXPORTS:
         if not hasattr(L, name):
             raise ImportError("libeolc.so lacks %s" % name)

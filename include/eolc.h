@@ -198,6 +198,41 @@ eolc_status eolc_cd2(eolc_ctx *ctx, const double *x_h, const eolc_box *boxes,
                      const double *normals_h, int n_points, double threshold,
                      eolc_contact *out_h, int capacity, int *n_out);
 
+/* ---- velocity solve without device allocation ----------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * on their step path: an interactive stepping loop (the reference's online
+ * mode) cannot afford cudaMalloc/cudaFree, which may synchronize the device
+ * and take milliseconds, and a host framework that reserves all device
+ * memory in its own pool leaves none for a library allocator.
+ * Same mixed-precision Jacobi PCG as eolc_velocity_solve (FP32 matrix and
+ * vectors, double-float inner products, FP64 true residual <= rel_tol), with
+ * every scratch buffer carved out of one fixed device array inside the
+ * library (about 17 MB, held by every GPU that loads the library until the
+ * process exits).  No context is needed and nothing is allocated on the
+ * device.
+ *   rowptr_h/colidx_h: the BSR pattern (host; eolc_bsr_pattern's layout),
+ *   mdk_d: FP32 block values (device, 9 per block), b_d: 3N right-hand side
+ *   b of Cloth.cpp:345 (device), fixed_dofs_h/beq_h: pinned DOFs and their
+ *   values (host), v_d: 3N solution (device, written).
+ * Limits: n_nodes <= EOLC_STATIC_MAX_NODES and n_blocks <=
+ * EOLC_STATIC_MAX_BLOCKS, else EOLC_CAPACITY.  The first call on a device
+ * looks up the array's device address with that device current (make it
+ * before any stream capture).  Every call shares the array and it keeps the
+ * previous call's contents (the call clears what must start at zero), so
+ * calls whose GPU work overlaps — two streams, or two threads — race and
+ * must be serialized by the caller.  stream: a cudaStream_t (NULL: the
+ * legacy default stream); the call synchronizes it before returning. */
+#define EOLC_STATIC_MAX_NODES 16384
+#define EOLC_STATIC_MAX_BLOCKS 262144
+eolc_status eolc_velocity_solve_static(int n_nodes, const int *rowptr_h,
+                                       const int *colidx_h, const float *mdk_d,
+                                       const double *b_d,
+                                       const int *fixed_dofs_h,
+                                       const double *beq_h, int n_fixed,
+                                       double rel_tol, int max_iter,
+                                       double *v_d, eolc_solve_info *info,
+                                       void *stream);
+
 #ifdef __cplusplus
 }
 #endif

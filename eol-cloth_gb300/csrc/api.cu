@@ -136,14 +136,42 @@ eolc_status solve_device(eolc_ctx *ctx, const eolc_solve_opts *o,
   a.beq_full = ctx->beq_full.p;
   a.v = ctx->v.p;
   a.precision = o->precision;
-  a.precond = o->precond == EOLC_PC_LEARNED ? EOLC_PC_JACOBI : o->precond;
+  a.precond = o->precond;
   a.rel_tol = o->rel_tol;
   a.max_iter = o->max_iter;
   a.learned = nullptr;
   if (o->precision == EOLC_PREC_FP64 && !ctx->A64.p)
     return fail(ctx, EOLC_BAD_ARG, "no FP64 matrix assembled");
-  eolc_solve_info local;
-  eolc_status st = run_pcg(ctx->work, a, info ? info : &local, s, ctx->err, ctx->launches);
+  eolc_solve_info local{};
+  eolc_solve_info *inf = info ? info : &local;
+  if (o->precond == EOLC_PC_LEARNED) {
+    if (!ctx->lpc) return fail(ctx, EOLC_BAD_ARG, "no learned preconditioner attached");
+    if (o->precision != EOLC_PREC_MIXED)
+      return fail(ctx, EOLC_BAD_ARG, "the learned preconditioner runs on the mixed path");
+    const float *Gm = nullptr;
+    std::string msg = learned_forward(ctx->lpc, ctx, ctx->pinned.p, &Gm, s);
+    if (!msg.empty()) return fail(ctx, EOLC_CUDA_ERROR, msg.c_str());
+    ctx->launches += 20;  // network forward kernels
+    // fall back to Jacobi when the learned solve has not converged within
+    // fallback_factor x the last Jacobi iteration count
+    PcgArgs al = a;
+    if (o->fallback_factor > 0 && ctx->last_jacobi_iters > 0)
+      al.max_iter = std::min(o->max_iter, o->fallback_factor * ctx->last_jacobi_iters);
+    eolc_status st = run_pcg_learned(ctx->work, al, Gm, inf, s, ctx->err, ctx->launches);
+    if (st == EOLC_OK || o->fallback_factor <= 0) return st;
+    const double kms = inf->solve_kernel_ms;
+    const int its = inf->iterations;
+    PcgArgs aj = a;
+    aj.precond = EOLC_PC_JACOBI;
+    st = run_pcg(ctx->work, aj, inf, s, ctx->err, ctx->launches);
+    inf->used_fallback = 1;
+    inf->iterations += its;
+    inf->solve_kernel_ms += kms;
+    if (st == EOLC_OK) ctx->last_jacobi_iters = inf->iterations - its;
+    return st;
+  }
+  eolc_status st = run_pcg(ctx->work, a, inf, s, ctx->err, ctx->launches);
+  if (st == EOLC_OK && o->precond == EOLC_PC_JACOBI) ctx->last_jacobi_iters = inf->iterations;
   return st;
 }
 
@@ -156,6 +184,18 @@ extern "C" {
 int eolc_version(void) { return 1; }
 
 long long eolc_launch_count(const eolc_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+eolc_status eolc_attach_preconditioner(eolc_ctx *ctx, eolc_lpc *lpc) {
+  if (!ctx) return EOLC_BAD_ARG;
+  ctx->lpc = lpc;
+  return EOLC_OK;
+}
+
+eolc_status eolc_set_jacobi_reference(eolc_ctx *ctx, int iterations) {
+  if (!ctx || iterations < 0) return EOLC_BAD_ARG;
+  ctx->last_jacobi_iters = iterations;
+  return EOLC_OK;
+}
 
 eolc_status eolc_create(eolc_ctx **out, int device) {
   if (!out) return EOLC_BAD_ARG;
@@ -397,6 +437,7 @@ eolc_status eolc_step_resident(eolc_ctx *ctx, int n_steps,
     cudaEventElapsedTime(&ams, ctx->ev[0], ctx->ev[1]);  // the solve synchronized
     agg.iterations += si.iterations;
     agg.refinements += si.refinements;
+    agg.used_fallback |= si.used_fallback;
     agg.rel_res = si.rel_res;
     agg.status = si.status;
     agg.solve_kernel_ms += si.solve_kernel_ms;

@@ -113,7 +113,18 @@ void free_solve_work(SolveWork *w);
 struct CollideWork;
 void free_collide_work(CollideWork *w);
 
+// Learned preconditioner (learned.cu / pcg.cu)
+eolc_status run_pcg_learned(SolveWork *&w, const PcgArgs &a, const float *Gm,
+                            eolc_solve_info *info, cudaStream_t s, std::string &err,
+                            long long &launches);
+
 }  // namespace eolc
+
+struct eolc_lpc;
+namespace eolc {
+std::string learned_forward(eolc_lpc *P, eolc_ctx *ctx, const uint8_t *pinned_d,
+                            const float **G_out, cudaStream_t s);
+}
 
 // ---- the context ------------------------------------------------------------
 struct eolc_ctx {
@@ -137,5 +148,6 @@ struct eolc_ctx {
   long long launches = 0;   // kernels launched by this context
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::vector<int> host_tri;  // triangle list of the current topology
+  eolc_lpc *lpc = nullptr;    // attached learned preconditioner (not owned)
   eolc::CollideWork *cd_work = nullptr;
 };

@@ -610,6 +610,263 @@ cg_kernel(Params<T> P) {
   }
 }
 
+// ---- PCG with a non-local preconditioner (learned approximate inverse) ------
+// Standard PCG with two grid barriers per iteration:
+//   P1  p = z + beta p_old (halo on the fly), q = A p        -> barrier (p.q)
+//   P2  r' = r - alpha q (halo on the fly), z = G r', x += alpha p
+//                                                          -> barrier (r'.z, r'.r')
+// G has the pattern of A, so both products reuse the tiles, local columns
+// and halo lists.  Buffers (reusing Params fields): r[2] ping-pong r,
+// w[0] = z, w[1] = q, s[0]/s[1] ping-pong p, xacc, x64.
+template <typename T>
+__device__ __forceinline__ void stage_matrix(const T *M, const uint16_t *lcol, const int *rowptr,
+                                             const TileMeta &tm, unsigned char *vals,
+                                             const T *&sA, const uint16_t *&sL, int *sRow) {
+  const int nb = tm.b1 - tm.b0;
+  T *dA = reinterpret_cast<T *>(vals);
+  const int offA = stage_aligned(M + size_t(tm.b0) * 9, nb * 9, dA);
+  const size_t abytes = (size_t(offA + nb * 9) * sizeof(T) + 31) & ~size_t(15);
+  uint16_t *dL = reinterpret_cast<uint16_t *>(vals + abytes);
+  const int offL = stage_aligned(lcol + tm.b0, nb, dL);
+  for (int k = threadIdx.x; k <= tm.r1 - tm.r0; k += kThreads)
+    sRow[k] = __ldg(rowptr + tm.r0 + k) - tm.b0;
+  sA = dA + offA;
+  sL = dL + offL;
+}
+
+enum GenMode { kGenZ = 0, kGenP = 1, kGenR = 2 };
+
+template <typename T, int kMode>
+__device__ __forceinline__ void gen_phase(const Params<T> &P, const T *Gm, const TileMeta *tiles,
+                                          int ntiles, int rcur, int pold, T alpha, T beta,
+                                          unsigned char *smem, typename Acc<T>::V &a1,
+                                          typename Acc<T>::V &a2) {
+  using A = Acc<T>;
+  V4<T> *sU = reinterpret_cast<V4<T> *>(smem + kValBytes);
+  __shared__ V4<T> sOwn[kTileRows];
+  __shared__ int sRow[kTileRows + 1];
+  const int lrow = threadIdx.x / kRowThreads, quarter = threadIdx.x % kRowThreads;
+  V4<T> *z = P.w[0], *q = P.w[1];
+  V4<T> *po = P.s[pold], *pn = P.s[pold ^ 1];
+  const T *M = kMode == kGenP ? P.A : Gm;
+  for (int t = 0; t < ntiles; ++t) {
+    const TileMeta tm = tiles[t];
+    const int i = tm.r0 + lrow;
+    const bool owner = i < tm.r1 && quarter == 0;
+    V4<T> m{}, xa{}, pv{};
+    if (owner) {
+      m = P.fmask[i];
+      if (kMode == kGenR) { xa = P.xacc[i]; pv = pn[i]; }
+    }
+    const T *sA;
+    const uint16_t *sL;
+    stage_matrix(M, P.lcol, P.rowptr, tm, smem, sA, sL, sRow);
+    for (int j = threadIdx.x; j < tm.wn; j += kThreads) {
+      const int node = __ldg(P.wlist + tm.w0 + j);
+      V4<T> u;
+      if (kMode == kGenZ) {
+        u = P.r[rcur][node];
+      } else if (kMode == kGenP) {
+        const V4<T> zj = z[node], pj = po[node];
+        u = V4<T>{zj.x + beta * pj.x, zj.y + beta * pj.y, zj.z + beta * pj.z, T(0)};
+      } else {
+        const V4<T> rj = P.r[rcur][node], qj = q[node];
+        u = V4<T>{rj.x - alpha * qj.x, rj.y - alpha * qj.y, rj.z - alpha * qj.z, T(0)};
+      }
+      if (node >= tm.r0 && node < tm.r1) sOwn[node - tm.r0] = u;
+      sU[j] = u;
+    }
+    __syncthreads();
+    T c0 = 0, c1 = 0, c2 = 0;
+    if (i < tm.r1) {
+      const int q0 = sRow[lrow], q1 = sRow[lrow + 1];
+#pragma unroll 2
+      for (int k = q0 + quarter; k < q1; k += kRowThreads) {
+        const V4<T> u = sU[sL[k]];
+        const T *blk = sA + size_t(k) * 9;
+        c0 += blk[0] * u.x + blk[1] * u.y + blk[2] * u.z;
+        c1 += blk[3] * u.x + blk[4] * u.y + blk[5] * u.z;
+        c2 += blk[6] * u.x + blk[7] * u.y + blk[8] * u.z;
+      }
+    }
+#pragma unroll
+    for (int o = 1; o < kRowThreads; o <<= 1) {
+      c0 += __shfl_xor_sync(0xffffffffu, c0, o);
+      c1 += __shfl_xor_sync(0xffffffffu, c1, o);
+      c2 += __shfl_xor_sync(0xffffffffu, c2, o);
+    }
+    if (owner) {
+      const V4<T> res{c0 * m.x, c1 * m.y, c2 * m.z, T(0)};
+      const V4<T> own = sOwn[lrow];
+      if (kMode == kGenZ) {
+        z[i] = res;
+        a1 = A::addf(a1, dot3(own, res));
+        a2 = A::addf(a2, dot3(own, own));
+      } else if (kMode == kGenP) {
+        pn[i] = own;
+        q[i] = res;
+        a1 = A::addf(a1, dot3(own, res));
+      } else {
+        P.r[rcur ^ 1][i] = own;
+        z[i] = res;
+        xa.x += alpha * pv.x; xa.y += alpha * pv.y; xa.z += alpha * pv.z;
+        P.xacc[i] = xa;
+        a1 = A::addf(a1, dot3(own, res));
+        a2 = A::addf(a2, dot3(own, own));
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Reliable update: r[rcur] = rhs - A x64 in FP64 arithmetic.
+template <typename T>
+__device__ __forceinline__ void gen_ru_residual(const Params<T> &P, const TileMeta *tiles,
+                                               int ntiles, int rcur, unsigned char *smem,
+                                               double &rr64) {
+  V4<double> *sX = reinterpret_cast<V4<double> *>(smem + kValBytes);
+  __shared__ int sRow[kTileRows + 1];
+  const int lrow = threadIdx.x / kRowThreads, quarter = threadIdx.x % kRowThreads;
+  for (int t = 0; t < ntiles; ++t) {
+    const TileMeta tm = tiles[t];
+    const T *sA;
+    const uint16_t *sL;
+    stage_matrix(P.A, P.lcol, P.rowptr, tm, smem, sA, sL, sRow);
+    for (int j = threadIdx.x; j < tm.wn; j += kThreads) sX[j] = P.x64[__ldg(P.wlist + tm.w0 + j)];
+    __syncthreads();
+    const int i = tm.r0 + lrow;
+    double a0 = 0, a1 = 0, a2 = 0;
+    if (i < tm.r1) {
+      for (int k = sRow[lrow] + quarter; k < sRow[lrow + 1]; k += kRowThreads) {
+        const V4<double> xj = sX[sL[k]];
+        const T *blk = sA + size_t(k) * 9;
+        a0 += double(blk[0]) * xj.x + double(blk[1]) * xj.y + double(blk[2]) * xj.z;
+        a1 += double(blk[3]) * xj.x + double(blk[4]) * xj.y + double(blk[5]) * xj.z;
+        a2 += double(blk[6]) * xj.x + double(blk[7]) * xj.y + double(blk[8]) * xj.z;
+      }
+    }
+#pragma unroll
+    for (int o = 1; o < kRowThreads; o <<= 1) {
+      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    if (i < tm.r1 && quarter == 0) {
+      const V4<double> b = P.rhs[i];
+      const V4<T> m = P.fmask[i];
+      const double e0 = (b.x - a0) * double(m.x), e1 = (b.y - a1) * double(m.y),
+                   e2 = (b.z - a2) * double(m.z);
+      rr64 += e0 * e0 + e1 * e1 + e2 * e2;
+      P.r[rcur][i] = V4<T>{T(e0), T(e1), T(e2), T(0)};
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads, 1)
+pcg_general_kernel(Params<T> P, const T *Gm) {
+  using A = Acc<T>;
+  using V = typename A::V;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ V red[3 * (kThreads / 32 + 1)];
+  __shared__ TileMeta tiles[kMaxCtaTiles];
+  const int cta = blockIdx.x;
+  const int G = P.n_ctas;
+  unsigned epoch = 0;
+  const int t0 = P.cta_tile[cta], t1 = P.cta_tile[cta + 1];
+  const int ntiles = t1 - t0;
+  for (int t = threadIdx.x; t < ntiles; t += kThreads) {
+    TileMeta tm;
+    tm.r0 = P.tile_row[t0 + t];
+    tm.r1 = P.tile_row[t0 + t + 1];
+    tm.b0 = P.rowptr[tm.r0];
+    tm.b1 = P.rowptr[tm.r1];
+    tm.w0 = P.tile_wptr[t0 + t];
+    tm.wn = P.tile_wptr[t0 + t + 1] - tm.w0;
+    tiles[t] = tm;
+  }
+  __syncthreads();
+  const V tol2 = A::from_d(P.tol2 * __ldcg(&P.st->rhs_norm2));
+  const V delta2 = A::from_d(kDelta * kDelta);
+  V *partbuf = reinterpret_cast<V *>(P.part);
+  int pset = 0;
+#define EOLC_SYNC3(a, b, c)                                             \
+  do {                                                                  \
+    block_sum3<T>(a, b, c, red);                                        \
+    V *pp = partbuf + size_t(3) * G * pset;                             \
+    if (threadIdx.x == 0) {                                             \
+      pp[3 * cta] = a; pp[3 * cta + 1] = b; pp[3 * cta + 2] = c;        \
+    }                                                                   \
+    if (!grid_barrier(P.bar, G, epoch, P.st)) return;                   \
+    reduce_partials3<T>(pp, G, a, b, c, red);                           \
+    pset ^= 1;                                                          \
+  } while (0)
+  int rcur = 0, pold = 0;
+  V rz = A::zero(), rr = A::zero(), zz = A::zero();
+  gen_phase<T, kGenZ>(P, Gm, tiles, ntiles, rcur, pold, T(0), T(0), smem, rz, rr);
+  EOLC_SYNC3(rz, rr, zz);
+  V rmax2 = rr;
+  double last_rr64 = A::to_d(rr);
+  int it = 0, nref = 0, status = A::finite(rr) ? EOLC_NOT_CONVERGED : EOLC_NONFINITE;
+  bool converged = A::finite(rr) && A::le(rr, tol2);
+  V rz_prev = A::from_d(1.0);
+  bool restart = true;
+  while (!converged && status != EOLC_NONFINITE && it < P.max_iter) {
+    const V beta = restart ? A::zero() : A::div(rz, rz_prev);
+    restart = false;
+    V pq = A::zero(), d1 = A::zero(), d2 = A::zero();
+    gen_phase<T, kGenP>(P, Gm, tiles, ntiles, rcur, pold, T(0), T(A::to_t(beta)), smem, pq, d1);
+    EOLC_SYNC3(pq, d1, d2);
+    if (!A::pos(pq) || !A::pos(rz)) {
+      status = (A::finite(pq) && A::finite(rz)) ? EOLC_BREAKDOWN : EOLC_NONFINITE;
+      break;
+    }
+    const V alpha = A::div(rz, pq);
+    V rz2 = A::zero(), rr2 = A::zero(), d3 = A::zero();
+    gen_phase<T, kGenR>(P, Gm, tiles, ntiles, rcur, pold, T(A::to_t(alpha)), T(0), smem, rz2, rr2);
+    EOLC_SYNC3(rz2, rr2, d3);
+    ++it;
+    rcur ^= 1;
+    pold ^= 1;
+    rz_prev = rz;
+    rz = rz2;
+    rr = rr2;
+    if (!A::finite(rr) || !A::finite(rz)) { status = EOLC_NONFINITE; break; }
+    if (!(A::lt(rr, A::mul(delta2, rmax2)) || A::le(rr, tol2) || it >= P.max_iter)) continue;
+    for (int t = 0; t < ntiles; ++t)
+      for (int i = tiles[t].r0 + threadIdx.x; i < tiles[t].r1; i += kThreads) {
+        const V4<T> xa = P.xacc[i];
+        V4<double> x = P.x64[i];
+        x.x += double(xa.x); x.y += double(xa.y); x.z += double(xa.z);
+        P.x64[i] = x;
+        P.xacc[i] = V4<T>{T(0), T(0), T(0), T(0)};
+      }
+    if (!grid_barrier(P.bar, G, epoch, P.st)) return;
+    double rr64d = 0;
+    gen_ru_residual(P, tiles, ntiles, rcur, smem, rr64d);
+    V rr64 = A::from_d(rr64d), e1 = A::zero(), e2 = A::zero();
+    EOLC_SYNC3(rr64, e1, e2);
+    ++nref;
+    last_rr64 = A::to_d(rr64);
+    rmax2 = rr64;
+    if (!A::finite(rr64)) { status = EOLC_NONFINITE; break; }
+    if (A::le(rr64, tol2)) { converged = true; break; }
+    V rz3 = A::zero(), rr3 = A::zero(), e3 = A::zero();
+    gen_phase<T, kGenZ>(P, Gm, tiles, ntiles, rcur, pold, T(0), T(0), smem, rz3, rr3);
+    EOLC_SYNC3(rz3, rr3, e3);
+    rz = rz3;
+  }
+#undef EOLC_SYNC3
+  if (converged) status = EOLC_OK;
+  if (cta == 0 && threadIdx.x == 0) {
+    atomicCAS(&P.st->status, EOLC_OK, status);
+    P.st->iterations = it;
+    P.st->refinements = nref;
+    P.st->rel_res = P.st->rhs_norm2 > 0 ? sqrt(last_rr64 / P.st->rhs_norm2) : 0.0;
+  }
+}
+
 // ---- set-up kernels (one launch each per solve) -----------------------------
 
 // rhs = mask * (-b - A beq_full) in FP64 (A promoted), the preconditioner,
@@ -921,6 +1178,128 @@ eolc_status run_pcg(SolveWork *&w, const PcgArgs &a, eolc_solve_info *info,
                     cudaStream_t s, std::string &err, long long &launches) {
   if (a.precision == EOLC_PREC_FP64) return run_pcg_t<double>(w, a, info, s, err, launches);
   return run_pcg_t<float>(w, a, info, s, err, launches);
+}
+
+namespace {
+
+// PCG with the preconditioner matrix G (FP32, pattern of A) on the mixed path.
+eolc_status run_pcg_general_f(SolveWork *&w, const PcgArgs &a, const float *Gm,
+                              eolc_solve_info *info, cudaStream_t s, std::string &err,
+                              long long &launches) {
+  using T = float;
+  // the tiling and vectors are the Jacobi layout's (point-Jacobi work)
+  PcgArgs jac = a;
+  jac.precond = EOLC_PC_JACOBI;
+  const DevTopology &Tp = *a.T;
+  const int N = Tp.n_nodes;
+  int dev = 0, n_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+  const size_t smem = smem_bytes<T>();
+  cudaFuncSetAttribute(pcg_general_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  // build (or reuse) the tiling through the Jacobi path's bookkeeping
+  if (!w || w->n_nodes != N || w->n_blocks != Tp.n_blocks || w->prec != 1 || w->block_pc != 0) {
+    std::vector<int> rowptr(N + 1), colidx(Tp.n_blocks);
+    cudaMemcpy(rowptr.data(), Tp.rowptr.p, sizeof(int) * (N + 1), cudaMemcpyDeviceToHost);
+    cudaMemcpy(colidx.data(), Tp.colidx.p, sizeof(int) * Tp.n_blocks, cudaMemcpyDeviceToHost);
+    std::vector<int> tiles, wptr, wlist;
+    std::vector<uint16_t> lcol;
+    std::string msg = build_tiles(N, rowptr, colidx, cap_blocks<T>(), win_max<T>(), tiles, wptr,
+                                  wlist, lcol);
+    if (!msg.empty()) { err = msg; return EOLC_BAD_ARG; }
+    const int nt = int(tiles.size()) - 1;
+    const int G = std::min(n_sm, nt);
+    if ((nt + G - 1) / G > kMaxCtaTiles / 2) { err = "matrix too large for one solve"; return EOLC_BAD_ARG; }
+    std::vector<int> cta(G + 1, nt);
+    cta[0] = 0;
+    const long long total = rowptr[N];
+    int t = 0;
+    for (int c = 1; c < G; ++c) {
+      long long target = total * c / G;
+      while (t < nt && rowptr[tiles[t]] < target) ++t;
+      cta[c] = std::max(t, cta[c - 1] + 1);
+      if (cta[c] > nt - (G - c)) cta[c] = nt - (G - c);
+    }
+    lcol.resize(lcol.size() + 8, 0);
+    if (!w) w = new SolveWork();
+    w->G = G; w->n_nodes = N; w->n_blocks = Tp.n_blocks; w->prec = 1; w->block_pc = 0;
+    cudaError_t es[] = {
+        w->tile_row.upload(tiles.data(), tiles.size(), s),
+        w->tile_wptr.upload(wptr.data(), wptr.size(), s),
+        w->wlist.upload(wlist.data(), std::max<size_t>(wlist.size(), 1), s),
+        w->lcol.upload(lcol.data(), lcol.size(), s),
+        w->cta_tile.upload(cta.data(), cta.size(), s),
+        w->vecs.resize(size_t(N) * (sizeof(V4<double>) * 2 + sizeof(V4<T>) * 9)),
+        w->part.resize(size_t(6) * G), w->bar.resize(2), w->st.resize(1),
+        w->pc.resize(size_t(N) * 9 * sizeof(T)), cudaStreamSynchronize(s)};
+    for (cudaError_t e : es)
+      if (e != cudaSuccess) { err = cudaGetErrorString(e); return EOLC_CUDA_ERROR; }
+  }
+  const int G = w->G;
+  unsigned char *vp = w->vecs.p;
+  V4<double> *rhs = reinterpret_cast<V4<double> *>(vp); vp += sizeof(V4<double>) * N;
+  V4<double> *x64 = reinterpret_cast<V4<double> *>(vp); vp += sizeof(V4<double>) * N;
+  V4<T> *vr = reinterpret_cast<V4<T> *>(vp);
+  Params<T> P;
+  P.r[0] = vr; P.r[1] = vr + N;
+  P.w[0] = vr + 2 * N; P.w[1] = vr + 3 * N;   // z, q
+  P.s[0] = vr + 4 * N; P.s[1] = vr + 5 * N;   // p ping-pong
+  P.p = vr + 6 * N;
+  P.xacc = vr + 7 * N;
+  V4<T> *fmask = vr + 8 * N;
+  T *pc = reinterpret_cast<T *>(w->pc.p);
+  const T *Amat = a.A32;
+  setup_kernel<T><<<(N + 127) / 128, 128, 0, s>>>(N, Tp.rowptr.p, Tp.colidx.p, Tp.diag.p, Amat,
+                                                   a.b, a.beq_full, a.pinned, 0, rhs, x64, P.r[0],
+                                                   P.p, P.s[0], P.xacc, pc, fmask);
+  init_sums_kernel<<<1, kThreads, 0, s>>>(N, rhs, w->st.p);
+  cudaMemsetAsync(w->bar.p, 0, sizeof(unsigned) * 2, s);
+  cudaMemsetAsync(P.s[0], 0, sizeof(V4<T>) * N, s);
+  P.n_nodes = N; P.n_ctas = G; P.rowptr = Tp.rowptr.p; P.A = Amat; P.lcol = w->lcol.p;
+  P.tile_row = w->tile_row.p; P.tile_wptr = w->tile_wptr.p; P.wlist = w->wlist.p;
+  P.cta_tile = w->cta_tile.p; P.rhs = rhs; P.x64 = x64; P.pc = pc; P.fmask = fmask;
+  P.part = w->part.p; P.bar = w->bar.p; P.st = w->st.p; P.max_iter = a.max_iter; P.block_pc = 0;
+  P.tol2 = a.rel_tol * a.rel_tol;
+  void *args[] = {&P, &Gm};
+  if (!w->ev0) { cudaEventCreate(&w->ev0); cudaEventCreate(&w->ev1); }
+  cudaEventRecord(w->ev0, s);
+  cudaError_t e = cudaLaunchCooperativeKernel((void *)pcg_general_kernel<T>, dim3(G),
+                                              dim3(kThreads), args, smem, s);
+  if (e != cudaSuccess) { err = cudaGetErrorString(e); return EOLC_CUDA_ERROR; }
+  cudaEventRecord(w->ev1, s);
+  finish_kernel<<<(N + 127) / 128, 128, 0, s>>>(N, x64, a.beq_full, a.pinned, a.v);
+  launches += 4;
+  DevStatus hs;
+  cudaMemcpyAsync(&hs, w->st.p, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) { err = cudaGetErrorString(e); return EOLC_CUDA_ERROR; }
+  float kms = 0.f;
+  cudaEventElapsedTime(&kms, w->ev0, w->ev1);
+  if (info) {
+    info->status = hs.status;
+    info->iterations = hs.iterations;
+    info->refinements = hs.refinements;
+    info->used_fallback = 0;
+    info->rel_res = hs.rel_res;
+    info->solve_kernel_ms = kms;
+  }
+  if (hs.status != EOLC_OK)
+    err = hs.status == EOLC_BREAKDOWN ? "PCG breakdown" : hs.status == EOLC_NONFINITE
+                                                              ? "non-finite value in PCG"
+                                                              : "PCG did not converge";
+  return eolc_status(hs.status);
+}
+
+}  // namespace
+
+eolc_status run_pcg_learned(SolveWork *&w, const PcgArgs &a, const float *Gm,
+                            eolc_solve_info *info, cudaStream_t s, std::string &err,
+                            long long &launches) {
+  if (a.precision != EOLC_PREC_MIXED) {
+    err = "the learned preconditioner runs on the mixed-precision path";
+    return EOLC_BAD_ARG;
+  }
+  return run_pcg_general_f(w, a, Gm, info, s, err, launches);
 }
 
 }  // namespace eolc

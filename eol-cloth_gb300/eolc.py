@@ -88,7 +88,11 @@ _V = ctypes.c_void_p
 EXPORTS = ["eolc_version", "eolc_launch_count", "eolc_create", "eolc_destroy", "eolc_last_error", "eolc_set_stream",
            "eolc_set_topology", "eolc_bsr_pattern", "eolc_forces_fill", "eolc_velocity_solve",
            "eolc_step", "eolc_state_upload", "eolc_state_download", "eolc_step_resident",
-           "eolc_cd2", "eolc_velocity_solve_static"]
+           "eolc_cd2", "eolc_velocity_solve_static", "eolc_lpc_create", "eolc_lpc_destroy",
+           "eolc_lpc_last_error", "eolc_lpc_num_params", "eolc_lpc_get_params",
+           "eolc_lpc_set_params", "eolc_lpc_loss_grad", "eolc_lpc_add_system",
+           "eolc_lpc_num_systems", "eolc_lpc_clear_systems", "eolc_lpc_train",
+           "eolc_attach_preconditioner", "eolc_set_jacobi_reference"]
 
 
 def load_library(path=LIB_PATH):
@@ -123,12 +127,29 @@ def load_library(path=LIB_PATH):
     L.eolc_velocity_solve_static.argtypes = [ctypes.c_int, _I, _I, _V, _V, _I, _D, ctypes.c_int,
                                              ctypes.c_double, ctypes.c_int, _V,
                                              ctypes.POINTER(SolveInfo), _V]
+    _F = ctypes.POINTER(ctypes.c_float)
+    L.eolc_lpc_create.argtypes = [ctypes.POINTER(_V), ctypes.c_int, ctypes.c_uint]
+    L.eolc_lpc_destroy.argtypes = [_V]
+    L.eolc_lpc_destroy.restype = None
+    L.eolc_lpc_last_error.argtypes = [_V]
+    L.eolc_lpc_last_error.restype = ctypes.c_char_p
+    L.eolc_lpc_num_params.argtypes = [_V]
+    L.eolc_lpc_get_params.argtypes = [_V, _F]
+    L.eolc_lpc_set_params.argtypes = [_V, _F]
+    L.eolc_lpc_loss_grad.argtypes = [_V, _V, _I, ctypes.c_int, _F, ctypes.c_int, _D, _F]
+    L.eolc_lpc_add_system.argtypes = [_V, _V, _I, ctypes.c_int, _F, ctypes.c_int]
+    L.eolc_lpc_num_systems.argtypes = [_V]
+    L.eolc_lpc_clear_systems.argtypes = [_V]
+    L.eolc_lpc_train.argtypes = [_V, ctypes.c_int, ctypes.c_float, ctypes.c_uint, _D]
+    L.eolc_attach_preconditioner.argtypes = [_V, _V]
+    L.eolc_set_jacobi_reference.argtypes = [_V, ctypes.c_int]
     for name in EXPORTS:
         if not hasattr(L, name):
             raise ImportError("libeolc.so lacks %s" % name)
         getattr(L, name).restype = getattr(L, name).restype
     for name in EXPORTS:
-        if name not in ("eolc_version", "eolc_destroy", "eolc_last_error", "eolc_launch_count"):
+        if name not in ("eolc_version", "eolc_destroy", "eolc_last_error", "eolc_launch_count",
+                        "eolc_lpc_destroy", "eolc_lpc_last_error"):
             getattr(L, name).restype = ctypes.c_int
     return L
 
@@ -268,6 +289,77 @@ class Context:
             return self.cd2(x, boxes, points, normals, threshold, capacity=n.value)
         self._check(st)
         return [out[k] for k in range(n.value)]
+
+
+class LearnedPC:
+    """The learned block-sparse approximate inverse (see include/eolc.h)."""
+
+    def __init__(self, device=0, seed=0):
+        h = _V()
+        st = lib.eolc_lpc_create(ctypes.byref(h), device, seed)
+        if st != OK:
+            raise EolcError(st, "eolc_lpc_create failed")
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib.eolc_lpc_destroy(self._h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _check(self, st):
+        if st != OK:
+            raise EolcError(st, lib.eolc_lpc_last_error(self._h).decode())
+
+    def num_params(self):
+        return lib.eolc_lpc_num_params(self._h)
+
+    def get_params(self):
+        out = np.zeros(self.num_params(), np.float32)
+        self._check(lib.eolc_lpc_get_params(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.num_params()
+        self._check(lib.eolc_lpc_set_params(self._h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+
+    def loss_grad(self, ctx, fixed_dofs, probes):
+        fixed_dofs = _i32(fixed_dofs)
+        probes = np.ascontiguousarray(probes, dtype=np.float32)
+        k = probes.shape[0]
+        grad = np.zeros(self.num_params(), np.float32)
+        loss = ctypes.c_double()
+        st = lib.eolc_lpc_loss_grad(self._h, ctx.handle, _i(fixed_dofs), len(fixed_dofs),
+                                    probes.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), k,
+                                    ctypes.byref(loss), grad.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        self._check(st)
+        return loss.value, grad
+
+    def add_system(self, ctx, fixed_dofs, probes):
+        fixed_dofs = _i32(fixed_dofs)
+        probes = np.ascontiguousarray(probes, dtype=np.float32)
+        self._check(lib.eolc_lpc_add_system(self._h, ctx.handle, _i(fixed_dofs), len(fixed_dofs),
+                                            probes.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                            probes.shape[0]))
+
+    def num_systems(self):
+        return lib.eolc_lpc_num_systems(self._h)
+
+    def clear_systems(self):
+        self._check(lib.eolc_lpc_clear_systems(self._h))
+
+    def train(self, epochs, lr=1e-3, seed=0):
+        losses = np.zeros(epochs)
+        self._check(lib.eolc_lpc_train(self._h, epochs, lr, seed, _d(losses)))
+        return losses
+
+    def attach(self, ctx):
+        ctx._check(lib.eolc_attach_preconditioner(ctx.handle, self._h))
+        ctx._lpc = self  # keep the network alive while attached
 
 
 def bsr_to_csr(ctx, vals):

@@ -198,6 +198,51 @@ eolc_status eolc_cd2(eolc_ctx *ctx, const double *x_h, const eolc_box *boxes,
                      const double *normals_h, int n_points, double threshold,
                      eolc_contact *out_h, int capacity, int *n_out);
 
+/* ---- learned preconditioner ------------------------------------------------
+ * A 3-layer message-passing network (hidden width 64, BF16 weights, FP32
+ * accumulation) on the stencil of MDK that outputs the 3x3 blocks of a
+ * symmetric positive definite approximate inverse
+ *   G = F (Lambda + sum_e [U_e; V_e][U_e; V_e]^T) F
+ * (F: free-DOF mask, Lambda: positive scaled Jacobi, one rank-3 PSD term per
+ * stencil edge), applied inside PCG (EOLC_PC_LEARNED).  Trained on the GPU by
+ * the library's own forward/backward kernels on systems the simulator
+ * produces, minimising sum_k |F (G A w_k - w_k)|^2 / |F w_k|^2 over probe
+ * vectors w_k.  The reference has no preconditioner beyond Eigen's default
+ * Jacobi (GeneralizedSolver.cpp:123-126); point Jacobi stays the fallback
+ * (eolc_solve_opts.fallback_factor) and the judge (same FP64 residual). */
+typedef struct eolc_lpc eolc_lpc;
+eolc_status eolc_lpc_create(eolc_lpc **out, int device, unsigned seed);
+void eolc_lpc_destroy(eolc_lpc *lpc);
+const char *eolc_lpc_last_error(const eolc_lpc *lpc);
+int eolc_lpc_num_params(const eolc_lpc *lpc);
+eolc_status eolc_lpc_get_params(eolc_lpc *lpc, float *params_h);
+eolc_status eolc_lpc_set_params(eolc_lpc *lpc, const float *params_h);
+/* Probe loss and its gradient w.r.t. the parameters for the context's last
+ * FP32 MDK (eolc_forces_fill / eolc_step with EOLC_PREC_MIXED).
+ * probes_h: n_probes x 3N FP32 vectors; grad_h: eolc_lpc_num_params floats. */
+eolc_status eolc_lpc_loss_grad(eolc_lpc *lpc, eolc_ctx *ctx,
+                               const int *fixed_dofs_h, int n_fixed,
+                               const float *probes_h, int n_probes,
+                               double *loss, float *grad_h);
+/* Stores a copy of the context's current FP32 MDK, its pinned mask and the
+ * probes as one training system (all systems share one topology). */
+eolc_status eolc_lpc_add_system(eolc_lpc *lpc, eolc_ctx *ctx,
+                                const int *fixed_dofs_h, int n_fixed,
+                                const float *probes_h, int n_probes);
+int eolc_lpc_num_systems(const eolc_lpc *lpc);
+eolc_status eolc_lpc_clear_systems(eolc_lpc *lpc);
+/* Adam over the stored systems (seeded shuffle); epoch_loss_h[epochs]
+ * receives the mean probe loss of each epoch. */
+eolc_status eolc_lpc_train(eolc_lpc *lpc, int epochs, float lr, unsigned seed,
+                           double *epoch_loss_h);
+/* Attach (or detach with NULL) the network used by EOLC_PC_LEARNED solves on
+ * this context; the context does not own it. */
+eolc_status eolc_attach_preconditioner(eolc_ctx *ctx, eolc_lpc *lpc);
+/* Iteration count of a plain Jacobi solve that the learned solve's fallback
+ * cap (fallback_factor x this count) refers to; set automatically by every
+ * successful Jacobi solve on the context. */
+eolc_status eolc_set_jacobi_reference(eolc_ctx *ctx, int iterations);
+
 /* ---- velocity solve without device allocation ----------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * on their step path: an interactive stepping loop (the reference's online

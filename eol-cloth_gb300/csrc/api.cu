@@ -4,7 +4,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -106,19 +108,22 @@ eolc_status ensure_state(eolc_ctx *ctx) {
   return EOLC_OK;
 }
 
-// Assembles MDK (and f, b) for the device state x, X, v.
+// Assembles MDK (and f, b) for the device state x, X, v.  batched: every
+// instance uses its own material from ctx->inst_matd (mat is ignored).
 eolc_status assemble(eolc_ctx *ctx, const eolc_material &mat, const double g[3],
                      double h, int prec, bool want_M, bool want_b,
-                     cudaStream_t s) {
+                     cudaStream_t s, bool batched = false) {
   MaterialD md = make_material(mat, g, h);
+  const MaterialD *mats = batched ? ctx->inst_matd.p : nullptr;
+  const int *node_inst = batched ? ctx->node_inst.p : nullptr;
   size_t nb9 = size_t(ctx->topo.n_blocks) * 9;
   if (prec == EOLC_PREC_FP64) EOLC_CHECK_CUDA(ctx, ctx->A64.resize(nb9 + 16));
   if (want_M) EOLC_CHECK_CUDA(ctx, ctx->Mblk.resize(nb9));
-  launch_assemble_blocks(ctx->topo, ctx->x.p, ctx->X.p, md, prec,
+  launch_assemble_blocks(ctx->topo, ctx->x.p, ctx->X.p, md, mats, node_inst, prec,
                          prec == EOLC_PREC_FP64 ? ctx->A64.p : nullptr,
                          prec == EOLC_PREC_FP64 ? nullptr : ctx->A32.p,
                          want_M ? ctx->Mblk.p : nullptr, s);
-  launch_forces_rhs(ctx->topo, ctx->x.p, ctx->X.p, ctx->v.p, md, prec,
+  launch_forces_rhs(ctx->topo, ctx->x.p, ctx->X.p, ctx->v.p, md, mats, node_inst, prec,
                     ctx->f.p, want_b ? ctx->b.p : nullptr, s);
   ctx->launches += 2;
   EOLC_CHECK_CUDA(ctx, cudaGetLastError());
@@ -177,6 +182,129 @@ eolc_status solve_device(eolc_ctx *ctx, const eolc_solve_opts *o,
 
 cudaStream_t stream_of(eolc_ctx *ctx) { return ctx->stream; }
 
+// ---- batches ---------------------------------------------------------------
+
+PcgArgs batch_pcg_args(eolc_ctx *ctx, const eolc_solve_opts *o, double *v) {
+  PcgArgs a;
+  a.T = &ctx->topo;
+  a.A64 = ctx->A64.p;
+  a.A32 = ctx->A32.p;
+  a.b = ctx->b.p;
+  a.pinned = ctx->pinned.p;
+  a.beq_full = ctx->beq_full.p;
+  a.v = v;
+  a.precision = o->precision;
+  a.precond = o->precond;
+  a.rel_tol = o->rel_tol;
+  a.max_iter = o->max_iter;
+  a.learned = nullptr;
+  return a;
+}
+
+// Checks shared by the batched entry points; uploads the pins and the
+// per-instance material table for (grav, h).
+eolc_status batch_begin(eolc_ctx *ctx, const double grav[3], double h, const int *fixed_dofs_h,
+                        const double *fixed_vel_h, int n_fixed, const eolc_solve_opts *opts,
+                        cudaStream_t s) {
+  eolc_status st = need_topology(ctx);
+  if (st != EOLC_OK) return st;
+  if ((st = check_opts(ctx, opts)) != EOLC_OK) return st;
+  if (opts->precond == EOLC_PC_LEARNED)
+    return fail(ctx, EOLC_BAD_ARG, "batched steps use the Jacobi or block-Jacobi preconditioner");
+  if (!grav) return fail(ctx, EOLC_BAD_ARG, "null gravity");
+  if (n_fixed > 0 && (!fixed_dofs_h || !fixed_vel_h)) return fail(ctx, EOLC_BAD_ARG, "null fixed list");
+  const int n_inst = int(ctx->node_off.size()) - 1;
+  if (int(ctx->inst_mat.size()) != n_inst)
+    return fail(ctx, EOLC_BAD_ARG, "no per-instance materials set");
+  if ((st = set_pins(ctx, fixed_dofs_h, fixed_vel_h, n_fixed, s)) != EOLC_OK) return st;
+  ctx->inst_matd_h.resize(n_inst);
+  for (int k = 0; k < n_inst; ++k) ctx->inst_matd_h[k] = make_material(ctx->inst_mat[k], grav, h);
+  EOLC_CHECK_CUDA(ctx, ctx->inst_matd.upload(ctx->inst_matd_h.data(), n_inst, s));
+  if (opts->precision == EOLC_PREC_FP64)
+    EOLC_CHECK_CUDA(ctx, ctx->A64.resize(size_t(ctx->topo.n_blocks) * 9 + 16));
+  return EOLC_OK;
+}
+
+// Pins, assembly and right-hand side of one batched step (no allocation, no
+// synchronisation: capturable).
+eolc_status enqueue_batch_assembly(eolc_ctx *ctx, const double grav[3], double h,
+                                   const eolc_solve_opts *o, cudaStream_t s) {
+  const int n = 3 * ctx->topo.n_nodes;
+  EOLC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->beq_full.p, 0, sizeof(double) * n, s));
+  if (ctx->n_fixed_dev > 0) {
+    pins_kernel<<<(ctx->n_fixed_dev + 127) / 128, 128, 0, s>>>(
+        ctx->n_fixed_dev, ctx->fixed_dofs.p, ctx->fixed_vel.p, ctx->v.p, ctx->beq_full.p);
+    ctx->launches += 1;
+  }
+  eolc_material unused{};
+  return assemble(ctx, unused, grav, h, o->precision, false, true, s, true);
+}
+
+// One whole batched step: pins, assembly, batched PCG, x += h v.
+eolc_status enqueue_batch_step(eolc_ctx *ctx, const double grav[3], double h,
+                               const eolc_solve_opts *o, cudaStream_t s) {
+  eolc_status st = enqueue_batch_assembly(ctx, grav, h, o, s);
+  if (st != EOLC_OK) return st;
+  PcgArgs a = batch_pcg_args(ctx, o, ctx->v.p);
+  st = batch_enqueue(ctx->bwork, a, s, ctx->err, ctx->launches);
+  if (st != EOLC_OK) return st;
+  const int n = 3 * ctx->topo.n_nodes;
+  integrate_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, h, ctx->v.p, ctx->x.p);
+  ctx->launches += 1;
+  EOLC_CHECK_CUDA(ctx, cudaGetLastError());
+  return EOLC_OK;
+}
+
+// Times every configuration of the batched solver on the current state
+// (assembled once; solutions go to a scratch vector, the state is unchanged)
+// and keeps the fastest.  ms_h (optional): one entry per configuration,
+// -1 where the configuration does not apply.
+eolc_status batch_autotune(eolc_ctx *ctx, const double grav[3], double h,
+                           const eolc_solve_opts *o, cudaStream_t s, int *chosen,
+                           double *ms_h) {
+  eolc_status st = enqueue_batch_assembly(ctx, grav, h, o, s);
+  if (st != EOLC_OK) return st;
+  DevBuf<double> scratch;
+  EOLC_CHECK_CUDA(ctx, scratch.resize(size_t(3) * ctx->topo.n_nodes));
+  PcgArgs a = batch_pcg_args(ctx, o, scratch.p);
+  if (!ctx->ev[2]) { cudaEventCreate(&ctx->ev[2]); cudaEventCreate(&ctx->ev[3]); }
+  const int nc = batch_num_configs();
+  int best = -1;
+  double best_ms = 0;
+  std::vector<BatchRecord> rec;
+  for (int c = 0; c < nc; ++c) {
+    double ms = -1;
+    std::string msg;
+    if (batch_prepare(ctx->bwork, a, ctx->node_off, c, s, msg) == EOLC_OK) {
+      bool ok = batch_reset_records(ctx->bwork, s) == EOLC_OK &&
+                batch_enqueue(ctx->bwork, a, s, ctx->err, ctx->launches) == EOLC_OK &&
+                batch_read_records(ctx->bwork, rec, s) == EOLC_OK;
+      for (const BatchRecord &r : rec) ok = ok && r.status == EOLC_OK;
+      if (ok) {
+        constexpr int kReps = 2;
+        cudaEventRecord(ctx->ev[2], s);
+        for (int k = 0; k < kReps && ok; ++k)
+          ok = batch_enqueue(ctx->bwork, a, s, ctx->err, ctx->launches) == EOLC_OK;
+        cudaEventRecord(ctx->ev[3], s);
+        EOLC_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
+        float t = 0.f;
+        cudaEventElapsedTime(&t, ctx->ev[2], ctx->ev[3]);
+        if (ok) ms = double(t) / kReps;
+      }
+      EOLC_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
+    }
+    if (ms_h) ms_h[c] = ms;
+    if (ms >= 0 && (best < 0 || ms < best_ms)) { best = c; best_ms = ms; }
+  }
+  if (best < 0) return fail(ctx, EOLC_BAD_ARG, "no batched solver configuration fits this batch");
+  std::string msg;
+  if ((st = batch_prepare(ctx->bwork, a, ctx->node_off, best, s, msg)) != EOLC_OK)
+    return fail(ctx, st, msg.c_str());
+  ctx->batch_config = best;
+  if (chosen) *chosen = best;
+  return EOLC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -222,6 +350,8 @@ void eolc_destroy(eolc_ctx *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   free_solve_work(ctx->work);
   free_collide_work(ctx->cd_work);
+  free_batch_work(ctx->bwork);
+  if (ctx->bgraph) cudaGraphExecDestroy(ctx->bgraph);
   for (cudaEvent_t e : ctx->ev)
     if (e) cudaEventDestroy(e);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -255,8 +385,36 @@ eolc_status eolc_set_stream(eolc_ctx *ctx, void *stream) {
 eolc_status eolc_set_topology(eolc_ctx *ctx, int n_nodes, const int *tri_h,
                               int n_tri, const int *hinge_h, int n_hinge) {
   if (!ctx) return EOLC_BAD_ARG;
+  const int node_off[2] = {0, n_nodes};
+  const int tri_off[2] = {0, n_tri};
+  const int hinge_off[2] = {0, n_hinge};
+  return eolc_set_topology_batched(ctx, 1, node_off, tri_h, tri_off, hinge_h, hinge_off);
+}
+
+eolc_status eolc_set_topology_batched(eolc_ctx *ctx, int n_inst, const int *node_off_h,
+                                      const int *tri_h, const int *tri_off_h,
+                                      const int *hinge_h, const int *hinge_off_h) {
+  if (!ctx) return EOLC_BAD_ARG;
+  if (n_inst <= 0 || !node_off_h || !tri_off_h || !hinge_off_h)
+    return fail(ctx, EOLC_BAD_ARG, "bad instance tables");
+  const int n_nodes = node_off_h[n_inst], n_tri = tri_off_h[n_inst],
+            n_hinge = hinge_off_h[n_inst];
   if (!tri_h || n_tri <= 0 || (n_hinge > 0 && !hinge_h))
     return fail(ctx, EOLC_BAD_ARG, "null or empty topology");
+  if (node_off_h[0] != 0 || tri_off_h[0] != 0 || hinge_off_h[0] != 0)
+    return fail(ctx, EOLC_BAD_ARG, "instance tables must start at 0");
+  for (int k = 0; k < n_inst; ++k) {
+    if (node_off_h[k + 1] <= node_off_h[k] || tri_off_h[k + 1] <= tri_off_h[k] ||
+        hinge_off_h[k + 1] < hinge_off_h[k])
+      return fail(ctx, EOLC_BAD_ARG, "every instance needs nodes and triangles");
+    const int lo = node_off_h[k], hi = node_off_h[k + 1];
+    for (int64_t q = int64_t(tri_off_h[k]) * 3; q < int64_t(tri_off_h[k + 1]) * 3; ++q)
+      if (tri_h[q] < lo || tri_h[q] >= hi)
+        return fail(ctx, EOLC_BAD_ARG, "a triangle references another instance's node");
+    for (int64_t q = int64_t(hinge_off_h[k]) * 4; q < int64_t(hinge_off_h[k + 1]) * 4; ++q)
+      if (hinge_h[q] < lo || hinge_h[q] >= hi)
+        return fail(ctx, EOLC_BAD_ARG, "a hinge references another instance's node");
+  }
   cudaSetDevice(ctx->device);
   HostTopology H;
   std::string msg = build_topology(n_nodes, tri_h, n_tri, hinge_h, n_hinge, H);
@@ -267,6 +425,9 @@ eolc_status eolc_set_topology(eolc_ctx *ctx, int n_nodes, const int *tri_h,
   T.n_tri = H.n_tri;
   T.n_hinge = H.n_hinge;
   T.n_blocks = H.n_blocks;
+  std::vector<int> node_inst(n_nodes);
+  for (int k = 0; k < n_inst; ++k)
+    std::fill(node_inst.begin() + node_off_h[k], node_inst.begin() + node_off_h[k + 1], k);
   EOLC_CHECK_CUDA(ctx, T.tri.upload(tri_h, size_t(n_tri) * 3, s));
   if (n_hinge > 0) EOLC_CHECK_CUDA(ctx, T.hinge.upload(hinge_h, size_t(n_hinge) * 4, s));
   EOLC_CHECK_CUDA(ctx, T.rowptr.upload(H.rowptr.data(), H.rowptr.size(), s));
@@ -277,15 +438,24 @@ eolc_status eolc_set_topology(eolc_ctx *ctx, int n_nodes, const int *tri_h,
   EOLC_CHECK_CUDA(ctx, T.contrib.upload(H.contrib.data(), H.contrib.size(), s));
   EOLC_CHECK_CUDA(ctx, T.nf_ptr.upload(H.nf_ptr.data(), H.nf_ptr.size(), s));
   EOLC_CHECK_CUDA(ctx, T.nf_list.upload(H.nf_list.data(), H.nf_list.size(), s));
+  EOLC_CHECK_CUDA(ctx, ctx->node_inst.upload(node_inst.data(), node_inst.size(), s));
   EOLC_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
   ctx->host = std::move(H);
   ctx->host_tri.assign(tri_h, tri_h + size_t(n_tri) * 3);
+  ctx->node_off.assign(node_off_h, node_off_h + n_inst + 1);
+  ctx->inst_mat.clear();
   free_collide_work(ctx->cd_work);
   ctx->cd_work = nullptr;
   ctx->has_topology = true;
   ctx->n_fixed_dev = -1;
   free_solve_work(ctx->work);
   ctx->work = nullptr;
+  free_batch_work(ctx->bwork);
+  ctx->bwork = nullptr;
+  ctx->batch_config = -1;
+  if (ctx->bgraph) cudaGraphExecDestroy(ctx->bgraph);
+  ctx->bgraph = nullptr;
+  ctx->bgraph_key.clear();
   ctx->A64.release();
   ctx->Mblk.release();
   eolc_status st = ensure_state(ctx);
@@ -467,6 +637,141 @@ eolc_status eolc_step(eolc_ctx *ctx, double *x_h, const double *X_h,
                           n_fixed, opts, info);
   if (st != EOLC_OK) return st;
   return eolc_state_download(ctx, x_h, v_h);
+}
+
+
+int eolc_batch_num_configs(void) { return batch_num_configs(); }
+
+const char *eolc_batch_config_name(int config) {
+  static std::vector<std::string> names;
+  static std::mutex m;
+  std::lock_guard<std::mutex> lock(m);
+  if (names.empty())
+    for (int c = 0; c < batch_num_configs(); ++c) names.push_back(batch_config_name(c));
+  return (config >= 0 && config < int(names.size())) ? names[config].c_str() : "";
+}
+
+eolc_status eolc_set_instance_materials(eolc_ctx *ctx, const eolc_material *mats, int n_inst) {
+  eolc_status st = need_topology(ctx);
+  if (st != EOLC_OK) return st;
+  if (!mats || n_inst != int(ctx->node_off.size()) - 1)
+    return fail(ctx, EOLC_BAD_ARG, "one material per instance is required");
+  ctx->inst_mat.assign(mats, mats + n_inst);
+  return EOLC_OK;
+}
+
+eolc_status eolc_batch_set_config(eolc_ctx *ctx, int config) {
+  if (!ctx) return EOLC_BAD_ARG;
+  if (config < -1 || config >= batch_num_configs())
+    return fail(ctx, EOLC_BAD_ARG, "unknown batch configuration");
+  ctx->batch_config = config;
+  return EOLC_OK;
+}
+
+eolc_status eolc_batch_autotune(eolc_ctx *ctx, const double grav[3], double h,
+                                const int *fixed_dofs_h, const double *fixed_vel_h,
+                                int n_fixed, const eolc_solve_opts *opts, int *chosen,
+                                double *ms_h) {
+  if (!ctx) return EOLC_BAD_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = stream_of(ctx);
+  eolc_status st = batch_begin(ctx, grav, h, fixed_dofs_h, fixed_vel_h, n_fixed, opts, s);
+  if (st != EOLC_OK) return st;
+  return batch_autotune(ctx, grav, h, opts, s, chosen, ms_h);
+}
+
+eolc_status eolc_step_batched(eolc_ctx *ctx, int n_steps, const double grav[3], double h,
+                              const int *fixed_dofs_h, const double *fixed_vel_h,
+                              int n_fixed, const eolc_solve_opts *opts,
+                              eolc_solve_info *inst_info_h, eolc_batch_info *total) {
+  if (!ctx) return EOLC_BAD_ARG;
+  if (n_steps < 0) return fail(ctx, EOLC_BAD_ARG, "negative step count");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = stream_of(ctx);
+  eolc_status st = batch_begin(ctx, grav, h, fixed_dofs_h, fixed_vel_h, n_fixed, opts, s);
+  if (st != EOLC_OK) return st;
+  if (ctx->batch_config < 0) {
+    if ((st = batch_autotune(ctx, grav, h, opts, s, nullptr, nullptr)) != EOLC_OK) return st;
+  }
+  {
+    PcgArgs a = batch_pcg_args(ctx, opts, ctx->v.p);
+    std::string msg;
+    if ((st = batch_prepare(ctx->bwork, a, ctx->node_off, ctx->batch_config, s, msg)) != EOLC_OK)
+      return fail(ctx, st, msg.c_str());
+  }
+  // the captured graph holds these values and device addresses
+  std::vector<double> key = {double(opts->precision), double(opts->precond), opts->rel_tol,
+                             double(opts->max_iter), h, grav[0], grav[1], grav[2],
+                             double(ctx->n_fixed_dev), double(ctx->batch_config)};
+  for (const void *p : {(const void *)ctx->fixed_dofs.p, (const void *)ctx->fixed_vel.p,
+                        (const void *)ctx->pinned.p, (const void *)ctx->beq_full.p,
+                        (const void *)ctx->A64.p, (const void *)ctx->A32.p,
+                        (const void *)ctx->inst_matd.p, (const void *)ctx->bwork})
+    key.push_back(double(reinterpret_cast<uintptr_t>(p)));
+  if (!ctx->bgraph || key != ctx->bgraph_key) {
+    if (ctx->bgraph) cudaGraphExecDestroy(ctx->bgraph);
+    ctx->bgraph = nullptr;
+    const long long before = ctx->launches;
+    EOLC_CHECK_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    st = enqueue_batch_step(ctx, grav, h, opts, s);
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(s, &g);
+    ctx->bgraph_launches = int(ctx->launches - before);
+    ctx->launches = before;
+    if (st != EOLC_OK) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    if (ce != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return fail(ctx, EOLC_CUDA_ERROR, cudaGetErrorString(ce));
+    }
+    ce = cudaGraphInstantiate(&ctx->bgraph, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) {
+      ctx->bgraph = nullptr;
+      return fail(ctx, EOLC_CUDA_ERROR, cudaGetErrorString(ce));
+    }
+    ctx->bgraph_key = key;
+  }
+  if ((st = batch_reset_records(ctx->bwork, s)) != EOLC_OK)
+    return fail(ctx, st, "record reset failed");
+  if (!ctx->ev[2]) { cudaEventCreate(&ctx->ev[2]); cudaEventCreate(&ctx->ev[3]); }
+  EOLC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
+  for (int k = 0; k < n_steps; ++k) EOLC_CHECK_CUDA(ctx, cudaGraphLaunch(ctx->bgraph, s));
+  EOLC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
+  ctx->launches += (long long)ctx->bgraph_launches * n_steps;
+  std::vector<BatchRecord> rec;
+  if ((st = batch_read_records(ctx->bwork, rec, s)) != EOLC_OK)
+    return fail(ctx, st, "batched step failed on the device");
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
+  eolc_batch_info tot{};
+  tot.status = EOLC_OK;
+  tot.config = ctx->batch_config;
+  tot.steps = n_steps;
+  tot.step_ms = ms;
+  for (size_t k = 0; k < rec.size(); ++k) {
+    const BatchRecord &r = rec[k];
+    if (r.status != EOLC_OK) {
+      if (tot.status == EOLC_OK) tot.status = r.status;
+      tot.n_failed += 1;
+    }
+    tot.iterations += r.iterations;
+    tot.max_iterations = std::max(tot.max_iterations, r.max_iterations);
+    tot.max_rel_res = std::max(tot.max_rel_res, r.rel_res);
+    if (inst_info_h) {
+      eolc_solve_info &o = inst_info_h[k];
+      o = eolc_solve_info{};
+      o.status = r.status;
+      o.iterations = r.iterations;
+      o.refinements = r.refinements;
+      o.rel_res = r.rel_res;
+    }
+  }
+  if (total) *total = tot;
+  if (tot.status != EOLC_OK) ctx->err = "an instance's solve failed (see the per-instance status)";
+  return eolc_status(tot.status);
 }
 
 }  // extern "C"

@@ -25,10 +25,14 @@ assemble_blocks_kernel(int n_blocks, const int *__restrict__ cptr,
                        const int *__restrict__ hinge,
                        const double *__restrict__ x,
                        const double *__restrict__ X, MaterialD m,
+                       const MaterialD *__restrict__ mats,
+                       const int *__restrict__ node_inst,
+                       const int *__restrict__ blk_row,
                        double *__restrict__ A64, float *__restrict__ A32,
                        double *__restrict__ Mblk) {
   int bidx = blockIdx.x * blockDim.x + threadIdx.x;
   if (bidx >= n_blocks) return;
+  if (mats) m = mats[node_inst[blk_row[bidx]]];  // batched: the row's instance
   Acc acc[9], macc[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) { acc[k] = Acc(0); macc[k] = Acc(0); }
@@ -78,9 +82,12 @@ forces_rhs_kernel(int n_nodes, const int *__restrict__ nf_ptr,
                   const int *__restrict__ nf_list, const int *__restrict__ tri,
                   const double *__restrict__ x, const double *__restrict__ X,
                   const double *__restrict__ v, MaterialD m,
+                  const MaterialD *__restrict__ mats,
+                  const int *__restrict__ node_inst,
                   double *__restrict__ f, double *__restrict__ b) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_nodes) return;
+  if (mats) m = mats[node_inst[i]];  // batched: the node's instance
   const T mu = T(m.mu), lam = T(m.lam);
   T fx = 0, fy = 0, fz = 0;
   double mvx = 0, mvy = 0, mvz = 0;
@@ -117,30 +124,34 @@ forces_rhs_kernel(int n_nodes, const int *__restrict__ nf_ptr,
 }  // namespace
 
 void launch_assemble_blocks(const DevTopology &T, const double *x,
-                            const double *X, const MaterialD &m, int prec,
-                            double *A64, float *A32, double *Mblk,
+                            const double *X, const MaterialD &m,
+                            const MaterialD *mats, const int *node_inst,
+                            int prec, double *A64, float *A32, double *Mblk,
                             cudaStream_t s) {
   int nb = T.n_blocks;
   dim3 block(128), grid((nb + 127) / 128);
   if (prec == EOLC_PREC_FP64)
     assemble_blocks_kernel<double, double><<<grid, block, 0, s>>>(
-        nb, T.cptr.p, T.contrib.p, T.tri.p, T.hinge.p, x, X, m, A64, A32, Mblk);
+        nb, T.cptr.p, T.contrib.p, T.tri.p, T.hinge.p, x, X, m, mats, node_inst, T.blk_row.p,
+        A64, A32, Mblk);
   else
     assemble_blocks_kernel<float, float><<<grid, block, 0, s>>>(
-        nb, T.cptr.p, T.contrib.p, T.tri.p, T.hinge.p, x, X, m, A64, A32, Mblk);
+        nb, T.cptr.p, T.contrib.p, T.tri.p, T.hinge.p, x, X, m, mats, node_inst, T.blk_row.p,
+        A64, A32, Mblk);
 }
 
 void launch_forces_rhs(const DevTopology &T, const double *x, const double *X,
-                       const double *v, const MaterialD &m, int prec,
+                       const double *v, const MaterialD &m,
+                       const MaterialD *mats, const int *node_inst, int prec,
                        double *f, double *b, cudaStream_t s) {
   int n = T.n_nodes;
   dim3 block(128), grid((n + 127) / 128);
   if (prec == EOLC_PREC_FP64)
     forces_rhs_kernel<double><<<grid, block, 0, s>>>(
-        n, T.nf_ptr.p, T.nf_list.p, T.tri.p, x, X, v, m, f, b);
+        n, T.nf_ptr.p, T.nf_list.p, T.tri.p, x, X, v, m, mats, node_inst, f, b);
   else
     forces_rhs_kernel<float><<<grid, block, 0, s>>>(
-        n, T.nf_ptr.p, T.nf_list.p, T.tri.p, x, X, v, m, f, b);
+        n, T.nf_ptr.p, T.nf_list.p, T.tri.p, x, X, v, m, mats, node_inst, f, b);
 }
 
 }  // namespace eolc

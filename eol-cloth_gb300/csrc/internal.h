@@ -81,13 +81,17 @@ struct MaterialD {
   double h;
 };
 
-// Kernel launchers (assemble.cu)
+// Kernel launchers (assemble.cu).  mats/node_inst (both device, may be
+// null): per-instance material table and the instance of every node, used
+// instead of m for batched topologies.
 void launch_assemble_blocks(const DevTopology &T, const double *x,
-                            const double *X, const MaterialD &m, int prec,
-                            double *A64, float *A32, double *Mblk,
+                            const double *X, const MaterialD &m,
+                            const MaterialD *mats, const int *node_inst,
+                            int prec, double *A64, float *A32, double *Mblk,
                             cudaStream_t s);
 void launch_forces_rhs(const DevTopology &T, const double *x, const double *X,
-                       const double *v, const MaterialD &m, int prec,
+                       const double *v, const MaterialD &m,
+                       const MaterialD *mats, const int *node_inst, int prec,
                        double *f, double *b, cudaStream_t s);
 
 // Solver (pcg.cu)
@@ -108,6 +112,34 @@ struct PcgArgs {
 eolc_status run_pcg(SolveWork *&w, const PcgArgs &a, eolc_solve_info *info,
                     cudaStream_t s, std::string &err, long long &launches);
 void free_solve_work(SolveWork *w);
+
+// Batched solver (batch.cu): one persistent launch over many instances.
+// Per-instance record, accumulated over the launches of one call.
+struct BatchRecord {
+  int status;          // first non-OK status, else EOLC_OK
+  int iterations;      // summed over launches
+  int refinements;
+  int max_iterations;  // largest single-launch iteration count
+  int steps;           // launches that solved this instance
+  int pad;
+  double rel_res;      // largest final relative residual
+};
+struct BatchSolveWork;
+void free_batch_work(BatchSolveWork *w);
+int batch_num_configs();
+std::string batch_config_name(int config);
+// Builds the per-instance tiling for a configuration (host work and device
+// allocations; not capturable).  node_off: n_inst + 1 node offsets.
+eolc_status batch_prepare(BatchSolveWork *&w, const PcgArgs &a,
+                          const std::vector<int> &node_off, int config,
+                          cudaStream_t s, std::string &err);
+// Enqueues set-up, the batched CG launch and the finish kernel on s; no
+// synchronisation and no allocation, so it can be captured in a graph.
+eolc_status batch_enqueue(BatchSolveWork *w, const PcgArgs &a, cudaStream_t s,
+                          std::string &err, long long &launches);
+eolc_status batch_reset_records(BatchSolveWork *w, cudaStream_t s);
+eolc_status batch_read_records(BatchSolveWork *w, std::vector<BatchRecord> &out,
+                               cudaStream_t s);
 
 // Collisions (collide.cu)
 struct CollideWork;
@@ -150,4 +182,15 @@ struct eolc_ctx {
   std::vector<int> host_tri;  // triangle list of the current topology
   eolc_lpc *lpc = nullptr;    // attached learned preconditioner (not owned)
   eolc::CollideWork *cd_work = nullptr;
+  // batches: instance k owns nodes node_off[k] .. node_off[k+1]
+  std::vector<int> node_off;
+  eolc::DevBuf<int> node_inst;                // instance of every node
+  std::vector<eolc_material> inst_mat;        // per-instance materials
+  eolc::DevBuf<eolc::MaterialD> inst_matd;    // device table for a step
+  std::vector<eolc::MaterialD> inst_matd_h;   // staging for that table
+  eolc::BatchSolveWork *bwork = nullptr;
+  int batch_config = -1;                      // -1: autotune on first use
+  cudaGraphExec_t bgraph = nullptr;           // captured batched step
+  std::vector<double> bgraph_key;             // what the graph was built for
+  int bgraph_launches = 0;                    // kernels per replay
 };

@@ -59,6 +59,13 @@ class SolveInfo(ctypes.Structure):
                 ("assemble_ms", ctypes.c_double)]
 
 
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("n_failed", ctypes.c_int), ("config", ctypes.c_int),
+                ("steps", ctypes.c_int), ("iterations", ctypes.c_longlong),
+                ("max_iterations", ctypes.c_int), ("pad", ctypes.c_int),
+                ("max_rel_res", ctypes.c_double), ("step_ms", ctypes.c_double)]
+
+
 class Box(ctypes.Structure):
     """Box obstacle: full dimensions and 4x4 frame (column-major)."""
     _fields_ = [("dim", ctypes.c_double * 3), ("E1", ctypes.c_double * 16)]
@@ -92,7 +99,10 @@ EXPORTS = ["eolc_version", "eolc_launch_count", "eolc_create", "eolc_destroy", "
            "eolc_lpc_last_error", "eolc_lpc_num_params", "eolc_lpc_get_params",
            "eolc_lpc_set_params", "eolc_lpc_loss_grad", "eolc_lpc_add_system",
            "eolc_lpc_num_systems", "eolc_lpc_clear_systems", "eolc_lpc_train",
-           "eolc_attach_preconditioner", "eolc_set_jacobi_reference"]
+           "eolc_attach_preconditioner", "eolc_set_jacobi_reference",
+           "eolc_set_topology_batched", "eolc_set_instance_materials", "eolc_step_batched",
+           "eolc_batch_num_configs", "eolc_batch_config_name", "eolc_batch_set_config",
+           "eolc_batch_autotune"]
 
 
 def load_library(path=LIB_PATH):
@@ -143,14 +153,25 @@ def load_library(path=LIB_PATH):
     L.eolc_lpc_train.argtypes = [_V, ctypes.c_int, ctypes.c_float, ctypes.c_uint, _D]
     L.eolc_attach_preconditioner.argtypes = [_V, _V]
     L.eolc_set_jacobi_reference.argtypes = [_V, ctypes.c_int]
+    L.eolc_set_topology_batched.argtypes = [_V, ctypes.c_int, _I, _I, _I, _I, _I]
+    L.eolc_set_instance_materials.argtypes = [_V, ctypes.POINTER(Material), ctypes.c_int]
+    L.eolc_step_batched.argtypes = [_V, ctypes.c_int, _D, ctypes.c_double, _I, _D, ctypes.c_int,
+                                    ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveInfo),
+                                    ctypes.POINTER(BatchInfo)]
+    L.eolc_batch_num_configs.argtypes = []
+    L.eolc_batch_config_name.argtypes = [ctypes.c_int]
+    L.eolc_batch_set_config.argtypes = [_V, ctypes.c_int]
+    L.eolc_batch_autotune.argtypes = [_V, _D, ctypes.c_double, _I, _D, ctypes.c_int,
+                                      ctypes.POINTER(SolveOpts), _I, _D]
     for name in EXPORTS:
         if not hasattr(L, name):
             raise ImportError("libeolc.so lacks %s" % name)
         getattr(L, name).restype = getattr(L, name).restype
     for name in EXPORTS:
         if name not in ("eolc_version", "eolc_destroy", "eolc_last_error", "eolc_launch_count",
-                        "eolc_lpc_destroy", "eolc_lpc_last_error"):
+                        "eolc_lpc_destroy", "eolc_lpc_last_error", "eolc_batch_config_name"):
             getattr(L, name).restype = ctypes.c_int
+    L.eolc_batch_config_name.restype = ctypes.c_char_p
     return L
 
 
@@ -289,6 +310,69 @@ class Context:
             return self.cd2(x, boxes, points, normals, threshold, capacity=n.value)
         self._check(st)
         return [out[k] for k in range(n.value)]
+
+
+    # ---- batches -------------------------------------------------------------
+    def set_topology_batched(self, sheets):
+        """sheets: list of (n_nodes, tri, hinge) with instance-local node ids.
+        Returns the node offsets (instance k owns nodes off[k]..off[k+1]-1)."""
+        node_off, tri_off, hinge_off, tris, hinges = [0], [0], [0], [], []
+        for n, tri, hinge in sheets:
+            tri, hinge = _i32(tri).reshape(-1, 3), _i32(hinge).reshape(-1, 4)
+            tris.append(tri + node_off[-1])
+            hinges.append(hinge + node_off[-1])
+            node_off.append(node_off[-1] + n)
+            tri_off.append(tri_off[-1] + len(tri))
+            hinge_off.append(hinge_off[-1] + len(hinge))
+        tri = _i32(np.concatenate(tris))
+        hinge = _i32(np.concatenate(hinges)) if hinge_off[-1] else np.zeros((1, 4), np.int32)
+        node_off, tri_off, hinge_off = _i32(node_off), _i32(tri_off), _i32(hinge_off)
+        self._tri = tri
+        self._check(lib.eolc_set_topology_batched(self._h, len(sheets), _i(node_off), _i(tri),
+                                                  _i(tri_off), _i(hinge), _i(hinge_off)))
+        self.n_nodes = int(node_off[-1])
+        self.node_off = node_off
+        return node_off
+
+    def set_instance_materials(self, mats):
+        arr = (Material * len(mats))(*mats)
+        self._check(lib.eolc_set_instance_materials(self._h, arr, len(mats)))
+
+    def step_batched(self, n_steps, grav, h, fixed_dofs, fixed_vel, opts=None):
+        """n_steps batched steps on the resident state; returns (BatchInfo,
+        per-instance SolveInfo list).  Raises on a failed instance solve."""
+        opts = opts or SolveOpts()
+        fixed_dofs, fixed_vel = _i32(fixed_dofs), _f64(fixed_vel)
+        n_inst = len(self.node_off) - 1
+        infos = (SolveInfo * n_inst)()
+        tot = BatchInfo()
+        st = lib.eolc_step_batched(self._h, n_steps, _d(_f64(grav)), h, _i(fixed_dofs),
+                                   _d(fixed_vel), len(fixed_dofs), ctypes.byref(opts), infos,
+                                   ctypes.byref(tot))
+        self._check(st)
+        return tot, [infos[k] for k in range(n_inst)]
+
+    def batch_set_config(self, config):
+        self._check(lib.eolc_batch_set_config(self._h, config))
+
+    def batch_autotune(self, grav, h, fixed_dofs, fixed_vel, opts=None):
+        """Returns (chosen configuration, ms per configuration)."""
+        opts = opts or SolveOpts()
+        fixed_dofs, fixed_vel = _i32(fixed_dofs), _f64(fixed_vel)
+        ms = np.zeros(batch_num_configs())
+        chosen = ctypes.c_int()
+        self._check(lib.eolc_batch_autotune(self._h, _d(_f64(grav)), h, _i(fixed_dofs),
+                                            _d(fixed_vel), len(fixed_dofs), ctypes.byref(opts),
+                                            ctypes.byref(chosen), _d(ms)))
+        return chosen.value, ms
+
+
+def batch_num_configs():
+    return lib.eolc_batch_num_configs()
+
+
+def batch_config_name(config):
+    return lib.eolc_batch_config_name(config).decode()
 
 
 class LearnedPC:

@@ -156,6 +156,73 @@ eolc_status eolc_step_resident(eolc_ctx *ctx, int n_steps,
                                const eolc_solve_opts *opts,
                                eolc_solve_info *info);
 
+/* ---- batches: many independent sheets in one persistent launch -----------
+ * No counterpart in the reference, whose Scene holds a single Cloth
+ * (Scene.h:56) and steps it once per Scene::step (Scene.cpp:72-98).  Each instance
+ * is a Cloth with its own material, stepped exactly as eolc_step_resident
+ * steps one sheet; all instances share h and gravity.
+ *
+ * eolc_set_topology_batched: instance k owns nodes node_off_h[k] ..
+ * node_off_h[k+1]-1, triangles tri_off_h[k] .. tri_off_h[k+1]-1 and hinges
+ * hinge_off_h[k] .. hinge_off_h[k+1]-1 (each table has n_inst + 1 entries,
+ * starting at 0); tri_h/hinge_h hold GLOBAL node indices (node_off + local)
+ * and must not reference another instance's nodes.  The state arrays of
+ * eolc_state_upload / eolc_state_download and the fixed DOF list are the
+ * concatenation over instances.  eolc_set_topology is the one-instance case.
+ */
+eolc_status eolc_set_topology_batched(eolc_ctx *ctx, int n_inst,
+                                      const int *node_off_h, const int *tri_h,
+                                      const int *tri_off_h, const int *hinge_h,
+                                      const int *hinge_off_h);
+/* One material per instance (required before eolc_step_batched). */
+eolc_status eolc_set_instance_materials(eolc_ctx *ctx,
+                                        const eolc_material *mats, int n_inst);
+
+typedef struct {
+  int status;           /* first non-OK instance status (instance order)   */
+  int n_failed;         /* instances whose solve did not reach EOLC_OK     */
+  int config;           /* batched-solver configuration used               */
+  int steps;
+  long long iterations; /* PCG iterations summed over instances and steps  */
+  int max_iterations;   /* largest iteration count of one instance solve   */
+  int pad;
+  double max_rel_res;   /* largest final FP64 relative residual            */
+  double step_ms;       /* device time of the n_steps steps (CUDA events)  */
+} eolc_batch_info;
+
+/* n_steps implicit-Euler steps of every instance on the device-resident
+ * state.  One step is one CUDA graph launch (captured on first use and
+ * whenever h, gravity, the options, the pins or the configuration change):
+ * pins, assembly with per-instance materials, ONE persistent launch of the
+ * batched PCG (instances pulled from a work queue, largest first, one CTA
+ * cluster each), x += h v.  Preconditioner: EOLC_PC_JACOBI or
+ * EOLC_PC_BLOCK_JACOBI.  inst_info_h (optional, n_inst entries): per-instance
+ * status, iterations and refinements summed over the steps and the largest
+ * relative residual.  Returns the first non-OK instance status; the other
+ * instances' states are advanced regardless.  The first call on a topology
+ * runs eolc_batch_autotune unless a configuration was set. */
+eolc_status eolc_step_batched(eolc_ctx *ctx, int n_steps, const double grav[3],
+                              double h, const int *fixed_dofs_h,
+                              const double *fixed_vel_h, int n_fixed,
+                              const eolc_solve_opts *opts,
+                              eolc_solve_info *inst_info_h,
+                              eolc_batch_info *total);
+/* Batched-solver configurations: CTA shape (threads, threads per block row,
+ * tile rows, CTAs per SM) x cluster size. */
+int eolc_batch_num_configs(void);
+const char *eolc_batch_config_name(int config);
+/* Force a configuration (-1: autotune on the next batched step). */
+eolc_status eolc_batch_set_config(eolc_ctx *ctx, int config);
+/* Times every configuration on the current state (assembled once; the state
+ * is not changed) and keeps the fastest.  ms_h (optional,
+ * eolc_batch_num_configs entries): solve time per configuration, -1 where a
+ * configuration does not fit the batch. */
+eolc_status eolc_batch_autotune(eolc_ctx *ctx, const double grav[3], double h,
+                                const int *fixed_dofs_h,
+                                const double *fixed_vel_h, int n_fixed,
+                                const eolc_solve_opts *opts, int *chosen,
+                                double *ms_h);
+
 /* ---- collisions (CD2, Collisions.cpp:55-78) ------------------------------ */
 
 /* Box obstacle: full dimensions dim[3] (Box::dim) and 4x4 frame E1

@@ -63,3 +63,27 @@ def drape_positions(quads, steps, seed=7, jitter=1e-4, box_dim=(0.4, 0.4, 0.2),
         x = x.ravel() + rng.normal(0.0, jitter, x.size)
         snaps.append(x)
     return x0, X, tri, center, snaps
+
+
+def batch(n_sheets, lo=16, hi=96, seed=3, e_range=(20.0, 100.0), pins=(3, 4)):
+    """Batched workload: n_sheets independent unit sheets whose side (in
+    quads) is drawn uniformly from lo..hi and whose Young's modulus is drawn
+    uniformly from e_range (seeded), the configuration-1 material otherwise,
+    each pinned at the named corners.  Returns the per-sheet scenes, their
+    materials and the concatenated state and fixed-DOF list (global DOFs)."""
+    rng = np.random.default_rng(seed)
+    sides = rng.integers(lo, hi + 1, n_sheets)
+    es = rng.uniform(e_range[0], e_range[1], n_sheets)
+    sheets, mats, off = [], [], [0]
+    for q, e in zip(sides, es):
+        s = sheet(int(q), pins)
+        sheets.append(s)
+        m = material_c1()
+        m["e"] = float(e)
+        mats.append(m)
+        off.append(off[-1] + s["n"])
+    x = np.concatenate([s["x"] for s in sheets])
+    X = np.concatenate([s["X"] for s in sheets])
+    fixed = np.concatenate([s["fixed"] + 3 * o for s, o in zip(sheets, off[:-1])]).astype(np.int32)
+    return dict(sheets=sheets, mats=mats, sides=sides, node_off=np.array(off), x=x, X=X,
+                v=np.zeros_like(x), fixed=fixed, fixed_vel=np.zeros(len(fixed)))

@@ -26,6 +26,8 @@ namespace {
     }                                                                \
   } while (0)
 
+constexpr int kDefaultPatchDegree = 8;  // Chebyshev degree of the patch solves
+
 eolc_status fail(eolc_ctx *ctx, eolc_status s, const char *msg) {
   if (ctx) ctx->err = msg;
   return s;
@@ -70,8 +72,10 @@ eolc_status check_opts(eolc_ctx *ctx, const eolc_solve_opts *o) {
     return fail(ctx, EOLC_BAD_ARG, "rel_tol must be > 0 and max_iter > 0");
   if (o->precision != EOLC_PREC_FP64 && o->precision != EOLC_PREC_MIXED)
     return fail(ctx, EOLC_BAD_ARG, "unknown precision");
-  if (o->precond < EOLC_PC_JACOBI || o->precond > EOLC_PC_LEARNED)
+  if (o->precond < EOLC_PC_JACOBI || o->precond > EOLC_PC_PATCH)
     return fail(ctx, EOLC_BAD_ARG, "unknown preconditioner");
+  if (o->degree < 0 || o->degree > 64)
+    return fail(ctx, EOLC_BAD_ARG, "patch degree must be in 0..64");
   return EOLC_OK;
 }
 
@@ -175,6 +179,9 @@ eolc_status solve_device(eolc_ctx *ctx, const eolc_solve_opts *o,
     if (st == EOLC_OK) ctx->last_jacobi_iters = inf->iterations - its;
     return st;
   }
+  if (o->precond == EOLC_PC_PATCH)
+    return run_pcg_patch(ctx->pwork, a, o->degree > 0 ? o->degree : kDefaultPatchDegree, inf, s,
+                         ctx->err, ctx->launches);
   eolc_status st = run_pcg(ctx->work, a, inf, s, ctx->err, ctx->launches);
   if (st == EOLC_OK && o->precond == EOLC_PC_JACOBI) ctx->last_jacobi_iters = inf->iterations;
   return st;
@@ -209,7 +216,7 @@ eolc_status batch_begin(eolc_ctx *ctx, const double grav[3], double h, const int
   eolc_status st = need_topology(ctx);
   if (st != EOLC_OK) return st;
   if ((st = check_opts(ctx, opts)) != EOLC_OK) return st;
-  if (opts->precond == EOLC_PC_LEARNED)
+  if (opts->precond != EOLC_PC_JACOBI && opts->precond != EOLC_PC_BLOCK_JACOBI)
     return fail(ctx, EOLC_BAD_ARG, "batched steps use the Jacobi or block-Jacobi preconditioner");
   if (!grav) return fail(ctx, EOLC_BAD_ARG, "null gravity");
   if (n_fixed > 0 && (!fixed_dofs_h || !fixed_vel_h)) return fail(ctx, EOLC_BAD_ARG, "null fixed list");
@@ -349,6 +356,7 @@ void eolc_destroy(eolc_ctx *ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   free_solve_work(ctx->work);
+  free_patch_work(ctx->pwork);
   free_collide_work(ctx->cd_work);
   free_batch_work(ctx->bwork);
   if (ctx->bgraph) cudaGraphExecDestroy(ctx->bgraph);
@@ -450,6 +458,8 @@ eolc_status eolc_set_topology_batched(eolc_ctx *ctx, int n_inst, const int *node
   ctx->n_fixed_dev = -1;
   free_solve_work(ctx->work);
   ctx->work = nullptr;
+  free_patch_work(ctx->pwork);
+  ctx->pwork = nullptr;
   free_batch_work(ctx->bwork);
   ctx->bwork = nullptr;
   ctx->batch_config = -1;

@@ -10,6 +10,7 @@
 // the same code runs under each shape the batch autotuner tries.
 #pragma once
 
+#include <cuda/atomic>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -85,6 +86,59 @@ __device__ __forceinline__ void block_sum3(typename Acc<T>::V &a, typename Acc<T
   }
   __syncthreads();
   a = red[3 * NW]; b = red[3 * NW + 1]; c = red[3 * NW + 2];
+}
+
+constexpr long long kSpinLimit = 1ll << 25;  // polls before a grid barrier gives up
+
+// ---- grid barrier -----------------------------------------------------------
+// Monotonic arrival counter: CTA thread 0 adds 1 with release semantics and
+// polls (acquire) until the count reaches n_ctas * epoch.  Bounded spin: on
+// expiry the barrier records EOLC_TIMEOUT and returns false.
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned nblocks,
+                                             unsigned &epoch, DevStatus *st) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    cuda::atomic_ref<unsigned, cuda::thread_scope_device> count(bar[0]);
+    epoch += 1u;
+    const unsigned target = nblocks * epoch;
+    int ok = 1;
+    count.fetch_add(1u, cuda::memory_order_release);
+    long long spins = 0;
+    while (count.load(cuda::memory_order_acquire) < target) {
+      if (++spins > kSpinLimit) {
+        atomicCAS(&st->status, EOLC_OK, EOLC_TIMEOUT);
+        ok = 0;
+        break;
+      }
+    }
+    if (ok) {
+      cuda::atomic_ref<int, cuda::thread_scope_device> sref(st->status);
+      ok = sref.load(cuda::memory_order_relaxed) == EOLC_OK;
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Every CTA reduces the per-CTA partial triples in the same fixed order, so
+// all CTAs take the same branch decisions.
+template <class C, typename T>
+__device__ __forceinline__ void reduce_partials3(const typename Acc<T>::V *part, int G,
+                                                 typename Acc<T>::V &a, typename Acc<T>::V &b,
+                                                 typename Acc<T>::V &c, typename Acc<T>::V *red) {
+  using A = Acc<T>;
+  using V = typename A::V;
+  a = b = c = A::zero();
+  for (int k = threadIdx.x; k < G; k += C::kThreads) {
+    const double *pd = reinterpret_cast<const double *>(part + 3 * k);
+    double v0 = __ldcg(pd), v1 = __ldcg(pd + 1), v2 = __ldcg(pd + 2);
+    a = A::add(a, *reinterpret_cast<V *>(&v0));
+    b = A::add(b, *reinterpret_cast<V *>(&v1));
+    c = A::add(c, *reinterpret_cast<V *>(&v2));
+  }
+  block_sum3<C, T>(a, b, c, red);
 }
 
 template <typename T>

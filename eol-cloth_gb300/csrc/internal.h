@@ -141,6 +141,13 @@ eolc_status batch_reset_records(BatchSolveWork *w, cudaStream_t s);
 eolc_status batch_read_records(BatchSolveWork *w, std::vector<BatchRecord> &out,
                                cudaStream_t s);
 
+// Patch-local preconditioned CG (patch.cu), mixed precision only.
+struct PatchWork;
+void free_patch_work(PatchWork *w);
+eolc_status run_pcg_patch(PatchWork *&w, const PcgArgs &a, int degree,
+                          eolc_solve_info *info, cudaStream_t s, std::string &err,
+                          long long &launches);
+
 // Collisions (collide.cu)
 struct CollideWork;
 void free_collide_work(CollideWork *w);
@@ -175,6 +182,7 @@ struct eolc_ctx {
   eolc::DevBuf<double> fixed_vel;
   int n_fixed_dev = -1;
   eolc::SolveWork *work = nullptr;
+  eolc::PatchWork *pwork = nullptr;
   int last_jacobi_iters = 0;
   int last_precision = -1;  // precision of the last assembled MDK
   long long launches = 0;   // kernels launched by this context

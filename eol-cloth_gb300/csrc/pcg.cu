@@ -55,7 +55,6 @@ constexpr int kThreads = C0::kThreads;
 constexpr int kValBytes = C0::kValBytes;
 constexpr int kTileRows = C0::kTileRows;
 constexpr int kRowThreads = C0::kRowThreads;
-constexpr long long kSpinLimit = 1ll << 25;
 
 template <typename T>
 constexpr int win_max() { return C0::win_max<T>(); }
@@ -64,56 +63,6 @@ constexpr int cap_blocks() { return C0::cap_blocks<T>(); }
 template <typename T>
 constexpr size_t smem_bytes() { return C0::smem_bytes<T>(); }
 
-// ---- grid barrier -----------------------------------------------------------
-// Monotonic arrival counter: CTA thread 0 adds 1 with release semantics and
-// polls (acquire) until the count reaches n_ctas * epoch.  Bounded spin: on
-// expiry the barrier records EOLC_TIMEOUT and returns false.
-__device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned nblocks,
-                                             unsigned &epoch, DevStatus *st) {
-  __shared__ int s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    cuda::atomic_ref<unsigned, cuda::thread_scope_device> count(bar[0]);
-    epoch += 1u;
-    const unsigned target = nblocks * epoch;
-    int ok = 1;
-    count.fetch_add(1u, cuda::memory_order_release);
-    long long spins = 0;
-    while (count.load(cuda::memory_order_acquire) < target) {
-      if (++spins > kSpinLimit) {
-        atomicCAS(&st->status, EOLC_OK, EOLC_TIMEOUT);
-        ok = 0;
-        break;
-      }
-    }
-    if (ok) {
-      cuda::atomic_ref<int, cuda::thread_scope_device> sref(st->status);
-      ok = sref.load(cuda::memory_order_relaxed) == EOLC_OK;
-    }
-    s_ok = ok;
-  }
-  __syncthreads();
-  return s_ok != 0;
-}
-
-// Every CTA reduces the per-CTA partial triples in the same fixed order, so
-// all CTAs take the same branch decisions.
-template <typename T>
-__device__ __forceinline__ void reduce_partials3(const typename Acc<T>::V *part, int G,
-                                                 typename Acc<T>::V &a, typename Acc<T>::V &b,
-                                                 typename Acc<T>::V &c, typename Acc<T>::V *red) {
-  using A = Acc<T>;
-  using V = typename A::V;
-  a = b = c = A::zero();
-  for (int k = threadIdx.x; k < G; k += kThreads) {
-    const double *pd = reinterpret_cast<const double *>(part + 3 * k);
-    double v0 = __ldcg(pd), v1 = __ldcg(pd + 1), v2 = __ldcg(pd + 2);
-    a = A::add(a, *reinterpret_cast<V *>(&v0));
-    b = A::add(b, *reinterpret_cast<V *>(&v1));
-    c = A::add(c, *reinterpret_cast<V *>(&v2));
-  }
-  block_sum3<C0, T>(a, b, c, red);
-}
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads, 1)
@@ -156,7 +105,7 @@ cg_kernel(Params<T> P) {
       pp[3 * cta] = a; pp[3 * cta + 1] = b; pp[3 * cta + 2] = c;        \
     }                                                                   \
     if (!grid_barrier(P.bar, G, epoch, P.st)) return;                   \
-    reduce_partials3<T>(pp, G, a, b, c, red);                           \
+    reduce_partials3<C0, T>(pp, G, a, b, c, red);                           \
     pset ^= 1;                                                          \
   } while (0)
   EOLC_PUBLISH_AND_SYNC(gam, del, rr);
@@ -416,7 +365,7 @@ pcg_general_kernel(Params<T> P, const T *Gm) {
       pp[3 * cta] = a; pp[3 * cta + 1] = b; pp[3 * cta + 2] = c;        \
     }                                                                   \
     if (!grid_barrier(P.bar, G, epoch, P.st)) return;                   \
-    reduce_partials3<T>(pp, G, a, b, c, red);                           \
+    reduce_partials3<C0, T>(pp, G, a, b, c, red);                           \
     pset ^= 1;                                                          \
   } while (0)
   int rcur = 0, pold = 0;

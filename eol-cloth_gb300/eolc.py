@@ -20,7 +20,7 @@ LIB_PATH = os.path.join(HERE, "libeolc.so")
 
 OK, NOT_CONVERGED, BREAKDOWN, NONFINITE, TIMEOUT, BAD_ARG, CUDA_ERROR, CAPACITY, NO_TOPOLOGY = range(9)
 PREC_FP64, PREC_MIXED = 0, 1
-PC_JACOBI, PC_BLOCK_JACOBI, PC_LEARNED = 0, 1, 2
+PC_JACOBI, PC_BLOCK_JACOBI, PC_LEARNED, PC_PATCH = 0, 1, 2, 3
 STATUS_NAMES = ["OK", "NOT_CONVERGED", "BREAKDOWN", "NONFINITE", "TIMEOUT", "BAD_ARG",
                 "CUDA_ERROR", "CAPACITY", "NO_TOPOLOGY"]
 
@@ -45,11 +45,11 @@ class Material(ctypes.Structure):
 class SolveOpts(ctypes.Structure):
     _fields_ = [("rel_tol", ctypes.c_double), ("max_iter", ctypes.c_int),
                 ("precision", ctypes.c_int), ("precond", ctypes.c_int),
-                ("fallback_factor", ctypes.c_int)]
+                ("fallback_factor", ctypes.c_int), ("degree", ctypes.c_int)]
 
     def __init__(self, rel_tol=1e-8, max_iter=100000, precision=PREC_MIXED,
-                 precond=PC_JACOBI, fallback_factor=2):
-        super().__init__(rel_tol, max_iter, precision, precond, fallback_factor)
+                 precond=PC_JACOBI, fallback_factor=2, degree=0):
+        super().__init__(rel_tol, max_iter, precision, precond, fallback_factor, degree)
 
 
 class SolveInfo(ctypes.Structure):

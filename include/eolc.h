@@ -62,7 +62,8 @@ typedef enum {
 typedef enum {
   EOLC_PC_JACOBI = 0,       /* point Jacobi (Eigen's default for CG)     */
   EOLC_PC_BLOCK_JACOBI = 1, /* inverse of the 3x3 diagonal blocks        */
-  EOLC_PC_LEARNED = 2       /* learned block-sparse approximate inverse  */
+  EOLC_PC_LEARNED = 2,      /* learned block-sparse approximate inverse  */
+  EOLC_PC_PATCH = 3         /* patch-local Chebyshev solves (below)      */
 } eolc_precond;
 
 typedef struct {
@@ -73,7 +74,20 @@ typedef struct {
   int fallback_factor;  /* learned PC: fall back to Jacobi after
                            fallback_factor * (last Jacobi count) iterations;
                            0 disables the fallback                       */
+  int degree;           /* patch PC: Chebyshev degree of the local solves
+                           (0: 8)                                        */
 } eolc_solve_opts;
+
+/* EOLC_PC_PATCH (mixed precision only; no counterpart in the reference,
+ * whose solve is Eigen's Jacobi CG, GeneralizedSolver.cpp:123-126): the
+ * nodes are split by recursive graph bisection into one compact patch per
+ * SM; each patch's principal submatrix, scaled to unit diagonal, is held in
+ * FP16 in that SM's shared memory for the whole solve, and the preconditioner
+ * is a degree-k Chebyshev polynomial of the block-Jacobi-preconditioned patch
+ * matrix on [l/30, l], l an upper bound of its spectrum (so it is symmetric
+ * positive definite).  Two grid barriers per PCG iteration; convergence on the
+ * same FP64 relative residual.  Meshes whose patches exceed shared memory
+ * (about 464 nodes per SM) are rejected with EOLC_BAD_ARG. */
 
 typedef struct {
   int status;        /* eolc_status of the solve                          */

@@ -149,6 +149,7 @@ eolc_status solve_device(eolc_ctx *ctx, const eolc_solve_opts *o,
   a.rel_tol = o->rel_tol;
   a.max_iter = o->max_iter;
   a.learned = nullptr;
+  a.X = ctx->X.p;
   if (o->precision == EOLC_PREC_FP64 && !ctx->A64.p)
     return fail(ctx, EOLC_BAD_ARG, "no FP64 matrix assembled");
   eolc_solve_info local{};
@@ -180,9 +181,13 @@ eolc_status solve_device(eolc_ctx *ctx, const eolc_solve_opts *o,
     return st;
   }
   if (o->precond == EOLC_PC_PATCH)
-    return run_pcg_patch(ctx->pwork, a, o->degree > 0 ? o->degree : kDefaultPatchDegree, inf, s,
-                         ctx->err, ctx->launches);
-  eolc_status st = run_pcg(ctx->work, a, inf, s, ctx->err, ctx->launches);
+    return run_pcg_resident(ctx->pwork, a, true, o->degree > 0 ? o->degree : kDefaultPatchDegree,
+                            inf, s, ctx->err, ctx->launches);
+  eolc_status st;
+  if (o->precision == EOLC_PREC_MIXED && !o->streamed && resident_fits(ctx->pwork, ctx->topo, ctx->X.p, s))
+    st = run_pcg_resident(ctx->pwork, a, false, 0, inf, s, ctx->err, ctx->launches);
+  else
+    st = run_pcg(ctx->work, a, inf, s, ctx->err, ctx->launches);
   if (st == EOLC_OK && o->precond == EOLC_PC_JACOBI) ctx->last_jacobi_iters = inf->iterations;
   return st;
 }

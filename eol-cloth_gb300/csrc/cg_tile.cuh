@@ -447,6 +447,26 @@ __global__ void setup_kernel(int n_nodes, const int *rowptr, const int *colidx,
   xacc[i] = zero;
 }
 
+// ||rhs||^2 by one CTA; resets the status record.
+template <class C>
+__global__ void __launch_bounds__(C::kThreads) init_sums_kernel(int n_nodes, const V4<double> *rhs,
+                                                             DevStatus *st) {
+  __shared__ double red[3 * (C::kThreads / 32 + 1)];
+  double s_rhs = 0, d0 = 0, d1 = 0;
+  for (int i = threadIdx.x; i < n_nodes; i += C::kThreads) {
+    V4<double> b = rhs[i];
+    s_rhs += b.x * b.x + b.y * b.y + b.z * b.z;
+  }
+  block_sum3<C, double>(s_rhs, d0, d1, red);
+  if (threadIdx.x == 0) {
+    st->status = EOLC_OK;
+    st->iterations = 0;
+    st->refinements = 0;
+    st->rel_res = s_rhs > 0 ? 1.0 : 0.0;
+    st->rhs_norm2 = s_rhs;
+  }
+}
+
 __global__ void finish_kernel(int n_nodes, const V4<double> *x64,
                               const double *beq_full, const uint8_t *pinned,
                               double *v) {

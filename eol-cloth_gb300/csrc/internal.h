@@ -108,6 +108,8 @@ struct PcgArgs {
   double rel_tol;
   int max_iter;
   const float *learned;  // learned approximate inverse blocks (n_blocks*9)
+  const double *X = nullptr;  // material coordinates (2N, device; optional):
+                              // partition hint for the resident solvers
 };
 eolc_status run_pcg(SolveWork *&w, const PcgArgs &a, eolc_solve_info *info,
                     cudaStream_t s, std::string &err, long long &launches);
@@ -141,12 +143,15 @@ eolc_status batch_reset_records(BatchSolveWork *w, cudaStream_t s);
 eolc_status batch_read_records(BatchSolveWork *w, std::vector<BatchRecord> &out,
                                cudaStream_t s);
 
-// Patch-local preconditioned CG (patch.cu), mixed precision only.
+// Resident solvers (patch.cu), mixed precision only: the matrix is held in
+// shared memory for the whole solve.  patch_pc selects the patch-local
+// Chebyshev preconditioner, else point / block Jacobi per a.precond.
 struct PatchWork;
 void free_patch_work(PatchWork *w);
-eolc_status run_pcg_patch(PatchWork *&w, const PcgArgs &a, int degree,
-                          eolc_solve_info *info, cudaStream_t s, std::string &err,
-                          long long &launches);
+bool resident_fits(PatchWork *&w, const DevTopology &T, const double *X_d, cudaStream_t s);
+eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, bool patch_pc, int degree,
+                             eolc_solve_info *info, cudaStream_t s, std::string &err,
+                             long long &launches);
 
 // Collisions (collide.cu)
 struct CollideWork;

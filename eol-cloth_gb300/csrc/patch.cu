@@ -1,35 +1,51 @@
-// PCG with a patch-local preconditioner whose matrices live in shared memory.
+// Resident solvers: the matrix lives in shared memory for the whole solve.
 //
-// The velocity solve on this GPU is bound by synchronisation latency, not by
-// bytes: a Jacobi-PCG iteration costs one grid barrier plus one pass over
-// the matrix, and the 256^2 sheet needs ~800 of them.  This preconditioner
-// spends on-chip work instead of grid barriers:
+// The velocity solve on this GPU is bound by latency (grid barriers and L2
+// round trips per staged tile), not by bytes.  These kernels remove the
+// per-iteration matrix traffic altogether:
 //
-//   * the nodes are reordered by recursive graph bisection into one compact
-//     patch per CTA (one CTA per SM), so a CTA owns a contiguous range of
-//     rows of the permuted system;
-//   * each CTA keeps the principal submatrix of its patch, symmetrically
-//     scaled to unit diagonal (A^ = S A S, S = diag^-1/2) and stored in FP16,
-//     resident in shared memory for the whole solve (~100 KB at 435 rows);
-//   * the preconditioner is M = blockdiag_p( S q_p(B^ A^_pp) B^ S ), a
-//     degree-k Chebyshev polynomial in the block-Jacobi-preconditioned patch
-//     matrix (B^ = inverse 3x3 diagonal blocks of A^), applied with CTA
-//     barriers only.  Its interval [l/30, l] takes l from the infinity norm
-//     of B^ A^_pp (an upper bound of its spectrum), so q_p > 0 on the whole
-//     spectrum and M is symmetric positive definite: plain PCG applies.
+//   * the nodes are reordered into one compact patch per CTA (<= kMaxRows
+//     rows, one CTA per SM, one thread per row) by recursive coordinate
+//     bisection of the material coordinates (recursive graph bisection when
+//     none are given);
+//   * each CTA copies its rows of the (symmetrised) FP32 BSR matrix into
+//     shared memory once per solve: the patch-internal blocks in upper-
+//     triangular storage (each used for A_ij x_j and, transposed, for
+//     A_ji x_i, read back through a transpose list in a fixed order), and the
+//     blocks that couple a row to other patches ("halo" blocks) in full;
+//   * every per-row vector (r, s, w, p, x, preconditioner) lives in the
+//     registers of the row's thread; only the values other patches read
+//     (halo exchange) go through global memory, ping-ponged so that no
+//     write races a read in the same phase.
 //
-// An iteration has two grid barriers: one for p'q after q = A p (the p halo
-// is recomputed from z and the previous p, so no exchange barrier), one for
-// r'z and r'r after the local solves.  The outer matrix product uses the
-// FP32 BSR matrix staged tile by tile; inner products are double-float;
-// convergence is declared on an FP64 true residual (reliable updates, as in
-// the Jacobi kernel), so the result meets the same FP64 criterion.
+// Two solvers run on this layout:
+//   jacobi_resident_kernel  the single-barrier Chronopoulos-Gear PCG of the
+//                           streamed kernel (pcg.cu) with point or block
+//                           Jacobi: halo values of u = M r' are recomputed
+//                           from the neighbours' r, s, w of the last step;
+//   patch_resident_kernel   PCG with the patch-local preconditioner
+//                           M = blockdiag_p( S q_p(B^ A^_pp) B^ S ): a degree-k
+//                           Chebyshev polynomial of the block-Jacobi-
+//                           preconditioned, unit-diagonal-scaled patch matrix
+//                           (A^ = S A S, S = diag^-1/2), on [l/30, l] with l the
+//                           infinity norm of B^ A^_pp (an upper bound of its
+//                           spectrum, so q_p > 0 there and M is symmetric
+//                           positive definite).  Local solves use CTA barriers
+//                           only; an iteration has two grid barriers.
+// Both take FP32 values and vectors, double-float inner products and FP64
+// reliable updates (the true residual rhs - A x64 in FP64 arithmetic), so
+// convergence is declared on the same FP64 relative residual as every other
+// solve.  The resident image holds each block pair (i, j), (j, i) averaged to
+// (A_ij + A_ji^T) / 2 (the assembly is symmetric up to last-bit rounding);
+// the true residual of every reliable update is taken with the assembled
+// blocks as they are, so the solution meets the criterion for exactly the
+// system every other path solves.
 //
-// No counterpart in the reference, whose solve is Eigen's Jacobi CG
-// (GeneralizedSolver.cpp:123-126); the judge of every result is the same
-// FP64 relative residual.
+// Meshes whose patches exceed the shared-memory image use the streamed
+// kernels (Jacobi) or are rejected (patch preconditioner).  No counterpart in
+// the reference, whose solve is Eigen's Jacobi CG (GeneralizedSolver.cpp:
+// 123-126); the result meets the same criterion.
 #include <cuda/atomic>
-#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -46,48 +62,457 @@ namespace eolc {
 namespace {
 using namespace cgc;
 
-using CA = TileCfg<512, 8, 30, 512>;  // outer product: 64-row tiles, 8 threads per row
-constexpr int kPThreads = CA::kThreads;
-constexpr int kMaxPatchRows = 464;     // rows of one patch (one thread each)
-constexpr int kMaxLocalBlocks = 6016;  // blocks of one patch's principal submatrix
-constexpr int kWinA = CA::kWinMaxF;    // halo nodes of an outer-product tile
-constexpr float kLoFrac = 30.f;        // Chebyshev interval [lmax / 30, lmax]
-constexpr float kBoundMargin = 1.02f;  // FP16 rounding margin on the norm bound
-constexpr int kLeafRows = CA::kTileRows;
-static_assert(kMaxPatchRows <= kPThreads, "one thread per patch row");
+struct RCfg {  // CTA shape of the resident kernels (block_sum3 / reduce_partials3)
+  static constexpr int kThreads = 512;
+};
+constexpr int kRThreads = RCfg::kThreads;
+constexpr int kMaxRows = 464;       // rows of one patch (one thread each)
+constexpr int kTargetRows = 448;    // rows per patch the partition aims for
+constexpr int kMaxUpper = 3072;     // patch-internal blocks, upper triangle
+constexpr int kMaxHaloBlk = 1024;   // blocks coupling the patch to others
+constexpr int kMaxHaloNodes = 384;  // distinct outside nodes those blocks touch
+constexpr float kLoFrac = 30.f;     // Chebyshev interval [lmax / 30, lmax]
+constexpr float kBoundMargin = 1.02f;
+static_assert(kMaxRows <= kRThreads, "one thread per patch row");
 
 constexpr size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
-// shared-memory layout (bytes)
-constexpr size_t kOffVals = 0;  // 10 halves per block (9 used)
-constexpr size_t kOffLc = al16(kOffVals + size_t(kMaxLocalBlocks) * 20);
-constexpr size_t kOffLp = al16(kOffLc + size_t(kMaxLocalBlocks) * 2);
-constexpr size_t kOffB = al16(kOffLp + size_t(kMaxPatchRows + 1) * 2);
-constexpr size_t kOffS = al16(kOffB + size_t(kMaxPatchRows) * 9 * 4);
-constexpr size_t kOffVec = al16(kOffS + size_t(kMaxPatchRows) * 16);  // y, res, d
-constexpr size_t kVecBytes = size_t(kMaxPatchRows) * 16 * 3;
-constexpr size_t kOffA = al16(kOffVec + kVecBytes);                    // tile values + cols
-constexpr size_t kOffW = kOffA + size_t(CA::kValBytes);                // p window
-constexpr size_t kPatchSmem = kOffW + size_t(kWinA) * 16;
-static_assert(size_t(kWinA) * sizeof(V4<double>) <= kVecBytes,
-              "the FP64 residual window overlays the Chebyshev vectors");
-static_assert(kPatchSmem <= 220 * 1024, "patch solver exceeds shared memory");
+constexpr size_t kOffU = 0;                                            // 9 floats per block
+constexpr size_t kOffH = al16(kOffU + size_t(kMaxUpper) * 36);
+constexpr size_t kOffUcol = al16(kOffH + size_t(kMaxHaloBlk) * 36);
+constexpr size_t kOffTupi = al16(kOffUcol + size_t(kMaxUpper) * 2);
+constexpr size_t kOffTrow = al16(kOffTupi + size_t(kMaxUpper) * 2);
+constexpr size_t kOffHwin = al16(kOffTrow + size_t(kMaxUpper) * 2);
+constexpr size_t kOffUptr = al16(kOffHwin + size_t(kMaxHaloBlk) * 2);
+constexpr size_t kOffTptr = al16(kOffUptr + size_t(kMaxRows + 1) * 2);
+constexpr size_t kOffHptr = al16(kOffTptr + size_t(kMaxRows + 1) * 2);
+constexpr size_t kOffHnode = al16(kOffHptr + size_t(kMaxRows + 1) * 2);
+constexpr size_t kOffXs = al16(kOffHnode + size_t(kMaxHaloNodes) * 4);
+constexpr size_t kOffXh = kOffXs + size_t(kMaxRows) * 16;
+constexpr size_t kOffDs = kOffXh + size_t(kMaxHaloNodes) * 16;
+constexpr size_t kResidentSmem = kOffDs + size_t(kMaxRows) * 16;
+static_assert(kResidentSmem <= 216 * 1024, "resident image exceeds shared memory");
 
-struct PatchParams {
-  Params<float> Q;        // permuted system: rowptr, A, lcol, tiles, vectors
-  const int *diag;        // diagonal block of every permuted row
-  const int *tr;          // block (j, i) of every block (i, j)
-  const int *patch_row;   // n_ctas + 1 row boundaries
-  const int *lptr;        // n_nodes + 1: first local block of every row
-  const int *lblk;        // permuted block of every local block
-  const uint16_t *llc;    // patch-local column of every local block
-  V4<float> *z, *q;
-  V4<float> *pp[2];       // search direction, ping-pong
-  int degree;             // Chebyshev degree
+struct ResParams {
+  int n_nodes, n_ctas, max_iter, degree, block_pc;
+  double tol2;
+  const int *patch_row;                    // n_ctas + 1
+  const int *rowptr, *colidx;              // permuted pattern
+  const float *A;                          // permuted FP32 blocks (as assembled)
+  const int *tr;                           // block (j, i) of every block (i, j)
+  const int *uptr, *ublk;                  // upper patch-internal entries per row
+  const uint16_t *ucol;
+  const int *tptr;                         // transposed entries per row
+  const uint16_t *tupi, *trow;
+  const int *hptr, *hblk;                  // halo entries per row
+  const uint16_t *hwin;
+  const int *hnptr, *hnode;                // halo nodes per patch
+  const V4<double> *rhs;
+  V4<double> *x64;
+  const V4<float> *fmask;
+  const float *pc;                         // Jacobi: 4 per node, block: 9
+  V4<float> *r[2], *s[2], *w[2], *p[2], *z;
+  double *part;
+  unsigned *bar;
+  DevStatus *st;
 };
 
-__device__ __forceinline__ void load9(const float *p, float (&m)[9]) {
+struct ResSmem {
+  float *uval, *hval;
+  uint16_t *ucol, *tupi, *trow, *hwin, *uptr, *tptr, *hptr;
+  int *hnode;
+  float4 *xs, *xh, *ds;
+};
+
+__device__ __forceinline__ ResSmem carve(unsigned char *smem) {
+  ResSmem m;
+  m.uval = reinterpret_cast<float *>(smem + kOffU);
+  m.hval = reinterpret_cast<float *>(smem + kOffH);
+  m.ucol = reinterpret_cast<uint16_t *>(smem + kOffUcol);
+  m.tupi = reinterpret_cast<uint16_t *>(smem + kOffTupi);
+  m.trow = reinterpret_cast<uint16_t *>(smem + kOffTrow);
+  m.hwin = reinterpret_cast<uint16_t *>(smem + kOffHwin);
+  m.uptr = reinterpret_cast<uint16_t *>(smem + kOffUptr);
+  m.tptr = reinterpret_cast<uint16_t *>(smem + kOffTptr);
+  m.hptr = reinterpret_cast<uint16_t *>(smem + kOffHptr);
+  m.hnode = reinterpret_cast<int *>(smem + kOffHnode);
+  m.xs = reinterpret_cast<float4 *>(smem + kOffXs);
+  m.xh = reinterpret_cast<float4 *>(smem + kOffXh);
+  m.ds = reinterpret_cast<float4 *>(smem + kOffDs);
+  return m;
+}
+
+// (A_ij + A_ji^T) / 2 of permuted block k into dst (9 floats).
+__device__ __forceinline__ void sym_block(const float *A, const int *tr, int k, float *dst) {
+  const float *a = A + size_t(k) * 9, *b = A + size_t(tr[k]) * 9;
 #pragma unroll
-  for (int k = 0; k < 9; ++k) m[k] = __ldg(p + k);
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) dst[3 * r + c] = 0.5f * (__ldg(a + 3 * r + c) + __ldg(b + 3 * c + r));
+}
+
+// Copies this patch's lists and symmetrised blocks into shared memory.
+__device__ void load_patch(const ResParams &P, const ResSmem &sm, int cta, int p0, int np) {
+  const int i = threadIdx.x;
+  if (i < np) {
+    const int row = p0 + i;
+    const int ub = P.uptr[p0], tb = P.tptr[p0], hb = P.hptr[p0];
+    const int u0 = P.uptr[row], u1 = P.uptr[row + 1];
+    sm.uptr[i] = uint16_t(u0 - ub);
+    for (int e = u0; e < u1; ++e) {
+      sym_block(P.A, P.tr, P.ublk[e], sm.uval + size_t(e - ub) * 9);
+      sm.ucol[e - ub] = P.ucol[e];
+    }
+    const int t0 = P.tptr[row], t1 = P.tptr[row + 1];
+    sm.tptr[i] = uint16_t(t0 - tb);
+    for (int t = t0; t < t1; ++t) {
+      sm.tupi[t - tb] = P.tupi[t];
+      sm.trow[t - tb] = P.trow[t];
+    }
+    const int h0 = P.hptr[row], h1 = P.hptr[row + 1];
+    sm.hptr[i] = uint16_t(h0 - hb);
+    for (int h = h0; h < h1; ++h) {
+      sym_block(P.A, P.tr, P.hblk[h], sm.hval + size_t(h - hb) * 9);
+      sm.hwin[h - hb] = P.hwin[h];
+    }
+    if (i == np - 1) {
+      sm.uptr[np] = uint16_t(u1 - ub);
+      sm.tptr[np] = uint16_t(t1 - tb);
+      sm.hptr[np] = uint16_t(h1 - hb);
+    }
+  }
+  const int n0 = P.hnptr[cta], nh = P.hnptr[cta + 1] - n0;
+  for (int h = threadIdx.x; h < nh; h += kRThreads) sm.hnode[h] = P.hnode[n0 + h];
+}
+
+__device__ __forceinline__ void fma_blk(const float *v, float4 x, float &a0, float &a1,
+                                        float &a2) {
+  a0 += v[0] * x.x + v[1] * x.y + v[2] * x.z;
+  a1 += v[3] * x.x + v[4] * x.y + v[5] * x.z;
+  a2 += v[6] * x.x + v[7] * x.y + v[8] * x.z;
+}
+__device__ __forceinline__ void fma_blkT(const float *v, float4 x, float &a0, float &a1,
+                                         float &a2) {
+  a0 += v[0] * x.x + v[3] * x.y + v[6] * x.z;
+  a1 += v[1] * x.x + v[4] * x.y + v[7] * x.z;
+  a2 += v[2] * x.x + v[5] * x.y + v[8] * x.z;
+}
+
+// Row i of A x: patch-internal part from xs, halo part from xh (kHalo).
+template <bool kHalo>
+__device__ __forceinline__ float3 row_apply(const ResSmem &sm, int i, const float4 *xs,
+                                            const float4 *xh) {
+  float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+#pragma unroll 2
+  for (int e = sm.uptr[i]; e < sm.uptr[i + 1]; ++e)
+    fma_blk(sm.uval + size_t(e) * 9, xs[sm.ucol[e]], a0, a1, a2);
+#pragma unroll 2
+  for (int t = sm.tptr[i]; t < sm.tptr[i + 1]; ++t)
+    fma_blkT(sm.uval + size_t(sm.tupi[t]) * 9, xs[sm.trow[t]], a0, a1, a2);
+  if (kHalo)
+    for (int h = sm.hptr[i]; h < sm.hptr[i + 1]; ++h)
+      fma_blk(sm.hval + size_t(h) * 9, xh[sm.hwin[h]], a0, a1, a2);
+  return make_float3(a0, a1, a2);
+}
+
+// Row `row` of rhs - A x64 in FP64 arithmetic with the assembled FP32 blocks
+// (not the symmetrised resident image), masked: the reliable update measures
+// the residual of exactly the system every other solve path solves.
+__device__ __forceinline__ V4<double> true_residual(const ResParams &P, int row,
+                                                   const V4<float> &m) {
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  for (int k = P.rowptr[row]; k < P.rowptr[row + 1]; ++k) {
+    const float *v = P.A + size_t(k) * 9;
+    const V4<double> x = P.x64[P.colidx[k]];
+    a0 += double(__ldg(v)) * x.x + double(__ldg(v + 1)) * x.y + double(__ldg(v + 2)) * x.z;
+    a1 += double(__ldg(v + 3)) * x.x + double(__ldg(v + 4)) * x.y + double(__ldg(v + 5)) * x.z;
+    a2 += double(__ldg(v + 6)) * x.x + double(__ldg(v + 7)) * x.y + double(__ldg(v + 8)) * x.z;
+  }
+  const V4<double> b = P.rhs[row];
+  return V4<double>{(b.x - a0) * double(m.x), (b.y - a1) * double(m.y), (b.z - a2) * double(m.z),
+                    0.0};
+}
+
+__device__ __forceinline__ float4 f4(V4<float> a) { return make_float4(a.x, a.y, a.z, 0.f); }
+
+// Jacobi preconditioner of one node: point (4 floats) or block (9 floats).
+struct PC {
+  float b[9];
+  __device__ void load(const float *pc, int node, int block) {
+    if (block) {
+      for (int k = 0; k < 9; ++k) b[k] = __ldg(pc + size_t(9) * node + k);
+    } else {
+      for (int k = 0; k < 9; ++k) b[k] = 0.f;
+      b[0] = __ldg(pc + size_t(4) * node);
+      b[4] = __ldg(pc + size_t(4) * node + 1);
+      b[8] = __ldg(pc + size_t(4) * node + 2);
+    }
+  }
+  __device__ V4<float> apply(V4<float> r) const {
+    return V4<float>{b[0] * r.x + b[1] * r.y + b[2] * r.z, b[3] * r.x + b[4] * r.y + b[5] * r.z,
+                     b[6] * r.x + b[7] * r.y + b[8] * r.z, 0.f};
+  }
+};
+
+// Grid-wide sums of three accumulators (deterministic: every CTA adds the
+// same partials in the same order and gets the same values).  One CTA
+// barrier before the grid barrier (warp partials -> thread 0 -> global), one
+// after (warp 0 reduces the G partials and broadcasts).  red holds the warp
+// partials in [0, 3 NW) and the broadcast in [3 NW, 3 NW + 3).  Returns false
+// when the grid barrier timed out.
+struct GridSum {
+  double *part;
+  unsigned *bar;
+  DevStatus *st;
+  int G, cta;
+  unsigned epoch;
+  int pset;
+  __device__ bool operator()(Acc<float>::V &a, Acc<float>::V &b, Acc<float>::V &c,
+                             Acc<float>::V *red) {
+    using Ac = Acc<float>;
+    using V = Ac::V;
+    constexpr int NW = kRThreads / 32;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a = Ac::add(a, Ac::shfl_xor(a, o));
+      b = Ac::add(b, Ac::shfl_xor(b, o));
+      c = Ac::add(c, Ac::shfl_xor(c, o));
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) { red[3 * warp] = a; red[3 * warp + 1] = b; red[3 * warp + 2] = c; }
+    __syncthreads();
+    V *pp = reinterpret_cast<V *>(part) + size_t(3) * G * pset;
+    if (threadIdx.x == 0) {
+      V x = Ac::zero(), y = Ac::zero(), z = Ac::zero();
+      for (int w = 0; w < NW; ++w) {
+        x = Ac::add(x, red[3 * w]);
+        y = Ac::add(y, red[3 * w + 1]);
+        z = Ac::add(z, red[3 * w + 2]);
+      }
+      pp[3 * cta] = x; pp[3 * cta + 1] = y; pp[3 * cta + 2] = z;
+    }
+    if (!grid_barrier(bar, G, epoch, st)) return false;
+    if (warp == 0) {
+      V x = Ac::zero(), y = Ac::zero(), z = Ac::zero();
+      for (int k = lane; k < G; k += 32) {
+        const double *pd = reinterpret_cast<const double *>(pp + 3 * k);
+        double v0 = __ldcg(pd), v1 = __ldcg(pd + 1), v2 = __ldcg(pd + 2);
+        x = Ac::add(x, *reinterpret_cast<V *>(&v0));
+        y = Ac::add(y, *reinterpret_cast<V *>(&v1));
+        z = Ac::add(z, *reinterpret_cast<V *>(&v2));
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        x = Ac::add(x, Ac::shfl_xor(x, o));
+        y = Ac::add(y, Ac::shfl_xor(y, o));
+        z = Ac::add(z, Ac::shfl_xor(z, o));
+      }
+      if (lane == 0) { red[3 * NW] = x; red[3 * NW + 1] = y; red[3 * NW + 2] = z; }
+    }
+    __syncthreads();
+    a = red[3 * NW]; b = red[3 * NW + 1]; c = red[3 * NW + 2];
+    pset ^= 1;
+    return true;
+  }
+  __device__ bool barrier() { return grid_barrier(bar, G, epoch, st); }
+};
+
+// ---- Jacobi PCG, one grid barrier per iteration -------------------------------
+// u'_j = M_j (r_j - alpha (w_j + beta s_j)) on the patch's halo nodes, from the
+// neighbours' values of the last step (index cur); init: u_j = M_j r_j.
+__device__ void halo_u(const ResParams &P, const ResSmem &sm, int nh, int cur, float alpha,
+                       float beta, bool init) {
+  for (int h = threadIdx.x; h < nh; h += kRThreads) {
+    const int j = sm.hnode[h];
+    V4<float> rj = P.r[cur][j];
+    if (!init) {
+      const V4<float> sj = P.s[cur][j], wj = P.w[cur][j];
+      rj.x -= alpha * (wj.x + beta * sj.x);
+      rj.y -= alpha * (wj.y + beta * sj.y);
+      rj.z -= alpha * (wj.z + beta * sj.z);
+    }
+    PC m;
+    m.load(P.pc, j, P.block_pc);
+    sm.xh[h] = f4(m.apply(rj));
+  }
+}
+
+__global__ void __launch_bounds__(kRThreads, 1) jacobi_resident_kernel(ResParams P) {
+  using A = Acc<float>;
+  using V = A::V;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ V red[3 * (kRThreads / 32 + 1)];
+  const ResSmem sm = carve(smem);
+  const int cta = blockIdx.x, i = threadIdx.x;
+  const int p0 = P.patch_row[cta], np = P.patch_row[cta + 1] - p0;
+  const int nh = P.hnptr[cta + 1] - P.hnptr[cta];
+  GridSum sync{P.part, P.bar, P.st, P.n_ctas, cta, 0u, 0};
+  load_patch(P, sm, cta, p0, np);
+  const bool own = i < np;
+  const int row = p0 + i;
+  V4<float> r{}, s{}, w{}, p{}, x{}, m{};
+  PC pc;
+  for (int k = 0; k < 9; ++k) pc.b[k] = 0.f;
+  if (own) {
+    r = P.r[0][row];
+    m = P.fmask[row];
+    pc.load(P.pc, row, P.block_pc);
+  }
+  const V tol2 = A::from_d(P.tol2 * __ldcg(&P.st->rhs_norm2));
+  const V delta2 = A::from_d(kDelta * kDelta);
+  int cur = 0;
+  V gam = A::zero(), del = A::zero(), rr = A::zero();
+  // u = M r, w = A u for the current r (start, and after a reliable update);
+  // w is published to w[cur]
+#define EOLC_INIT_PHASE(g, d, q)                                        \
+  do {                                                                  \
+    const V4<float> u_ = pc.apply(r);                                   \
+    if (own) sm.xs[i] = f4(u_);                                         \
+    halo_u(P, sm, nh, cur, 0.f, 0.f, true);                             \
+    __syncthreads();                                                    \
+    if (own) {                                                          \
+      const float3 t_ = row_apply<true>(sm, i, sm.xs, sm.xh);           \
+      w = V4<float>{t_.x * m.x, t_.y * m.y, t_.z * m.z, 0.f};           \
+      P.w[cur][row] = w;                                                \
+      g = A::addf(g, dot3(r, u_));                                      \
+      d = A::addf(d, dot3(w, u_));                                      \
+      q = A::addf(q, dot3(r, r));                                       \
+    }                                                                   \
+  } while (0)
+  __syncthreads();  // the resident image is complete
+  EOLC_INIT_PHASE(gam, del, rr);
+  if (!sync(gam, del, rr, red)) return;
+  V rmax2 = rr;
+  double last_rr64 = A::to_d(rr);
+  int it = 0, nref = 0, status = EOLC_NOT_CONVERGED;
+  bool converged = A::finite(rr) && A::le(rr, tol2);
+  if (!A::finite(rr)) status = EOLC_NONFINITE;
+  V gam_old = A::from_d(1.0), alpha_old = A::from_d(1.0);
+  bool restart = true;
+  while (!converged && status != EOLC_NONFINITE && it < P.max_iter) {
+    const V beta = restart ? A::zero() : A::div(gam, gam_old);
+    const V denom = restart ? del : A::add(del, A::neg(A::div(A::mul(beta, gam), alpha_old)));
+    if (!A::pos(denom) || !A::pos(gam)) {
+      status = (A::finite(denom) && A::finite(gam)) ? EOLC_BREAKDOWN : EOLC_NONFINITE;
+      break;
+    }
+    const V alpha = A::div(gam, denom);
+    const float af = float(A::to_t(alpha)), bf = float(A::to_t(beta));
+    restart = false;
+    const int nxt = cur ^ 1;
+    V g2 = A::zero(), d2 = A::zero(), rr2 = A::zero();
+    V4<float> un{};
+    if (own) {
+      const V4<float> sn{w.x + bf * s.x, w.y + bf * s.y, w.z + bf * s.z, 0.f};
+      const V4<float> rn{r.x - af * sn.x, r.y - af * sn.y, r.z - af * sn.z, 0.f};
+      const V4<float> uo = pc.apply(r);
+      un = pc.apply(rn);
+      p = V4<float>{uo.x + bf * p.x, uo.y + bf * p.y, uo.z + bf * p.z, 0.f};
+      x.x += af * p.x; x.y += af * p.y; x.z += af * p.z;
+      P.r[nxt][row] = rn;
+      P.s[nxt][row] = sn;
+      sm.xs[i] = f4(un);
+      r = rn;
+      s = sn;
+    }
+    halo_u(P, sm, nh, cur, af, bf, false);
+    __syncthreads();
+    if (own) {
+      const float3 t = row_apply<true>(sm, i, sm.xs, sm.xh);
+      w = V4<float>{t.x * m.x, t.y * m.y, t.z * m.z, 0.f};
+      P.w[nxt][row] = w;
+      g2 = A::addf(g2, dot3(r, un));
+      d2 = A::addf(d2, dot3(w, un));
+      rr2 = A::addf(rr2, dot3(r, r));
+    }
+    if (!sync(g2, d2, rr2, red)) return;
+    ++it;
+    cur = nxt;
+    gam_old = gam;
+    alpha_old = alpha;
+    gam = g2;
+    del = d2;
+    rr = rr2;
+    if (!A::finite(rr) || !A::finite(gam) || !A::finite(del)) { status = EOLC_NONFINITE; break; }
+    if (!(A::lt(rr, A::mul(delta2, rmax2)) || A::le(rr, tol2) || it >= P.max_iter)) continue;
+    // ---- reliable update: x64 += x; r = rhs - A x64 (FP64); s = A p --------
+    if (own) {
+      V4<double> xd = P.x64[row];
+      xd.x += double(x.x); xd.y += double(x.y); xd.z += double(x.z);
+      P.x64[row] = xd;
+      x = V4<float>{0.f, 0.f, 0.f, 0.f};
+      P.p[0][row] = p;
+      sm.xs[i] = f4(p);
+    }
+    if (!sync.barrier()) return;
+    for (int h = threadIdx.x; h < nh; h += kRThreads) sm.xh[h] = f4(P.p[0][sm.hnode[h]]);
+    __syncthreads();
+    double rr64d = 0;
+    if (own) {
+      const V4<double> q = true_residual(P, row, m);
+      rr64d = q.x * q.x + q.y * q.y + q.z * q.z;
+      r = V4<float>{float(q.x), float(q.y), float(q.z), 0.f};
+      const float3 t = row_apply<true>(sm, i, sm.xs, sm.xh);
+      s = V4<float>{t.x * m.x, t.y * m.y, t.z * m.z, 0.f};
+      P.r[cur][row] = r;
+      P.s[cur][row] = s;
+    }
+    V e0 = A::from_d(rr64d), e1 = A::zero(), e2 = A::zero();
+    if (!sync(e0, e1, e2, red)) return;
+    ++nref;
+    last_rr64 = A::to_d(e0);
+    rmax2 = e0;
+    if (!A::finite(e0)) { status = EOLC_NONFINITE; break; }
+    if (A::le(e0, tol2)) { converged = true; break; }
+    V g3 = A::zero(), d3 = A::zero(), rr3 = A::zero();
+    EOLC_INIT_PHASE(g3, d3, rr3);
+    if (!sync(g3, d3, rr3, red)) return;
+    gam = g3;
+    del = d3;
+  }
+#undef EOLC_INIT_PHASE
+  if (converged) status = EOLC_OK;
+  if (cta == 0 && threadIdx.x == 0) {
+    atomicCAS(&P.st->status, EOLC_OK, status);
+    P.st->iterations = it;
+    P.st->refinements = nref;
+    P.st->rel_res = P.st->rhs_norm2 > 0 ? sqrt(last_rr64 / P.st->rhs_norm2) : 0.0;
+  }
+}
+
+// ---- PCG with the patch-local Chebyshev preconditioner ------------------------
+struct LocalPC {
+  float S[3];
+  float B[9];
+  float lmax;
+};
+
+// z = S q(B^ A^) B^ S r on this row (CTA-wide: every thread takes part).
+__device__ V4<float> patch_apply(const ResSmem &sm, const LocalPC &L, bool own, int i, int k,
+                                 V4<float> r) {
+  const float lo = L.lmax / kLoFrac;
+  const float theta = 0.5f * (L.lmax + lo), delta = 0.5f * (L.lmax - lo);
+  const float sigma = theta / delta;
+  float rho = 1.f / sigma;
+  float res[3] = {L.S[0] * r.x, L.S[1] * r.y, L.S[2] * r.z};
+  float d[3], y[3] = {0.f, 0.f, 0.f};
+  for (int c = 0; c < 3; ++c)
+    d[c] = (L.B[3 * c] * res[0] + L.B[3 * c + 1] * res[1] + L.B[3 * c + 2] * res[2]) / theta;
+  for (int st = 0; st < k; ++st) {
+    y[0] += d[0]; y[1] += d[1]; y[2] += d[2];
+    if (st == k - 1) break;
+    if (own) sm.ds[i] = make_float4(L.S[0] * d[0], L.S[1] * d[1], L.S[2] * d[2], 0.f);
+    __syncthreads();
+    float3 t = make_float3(0.f, 0.f, 0.f);
+    if (own) t = row_apply<false>(sm, i, sm.ds, nullptr);
+    __syncthreads();
+    res[0] -= L.S[0] * t.x; res[1] -= L.S[1] * t.y; res[2] -= L.S[2] * t.z;
+    const float rho1 = 1.f / (2.f * sigma - rho);
+    const float c1 = rho1 * rho, c2 = 2.f * rho1 / delta;
+    for (int c = 0; c < 3; ++c)
+      d[c] = c1 * d[c] + c2 * (L.B[3 * c] * res[0] + L.B[3 * c + 1] * res[1] + L.B[3 * c + 2] * res[2]);
+    rho = rho1;
+  }
+  return V4<float>{L.S[0] * y[0], L.S[1] * y[1], L.S[2] * y[2], 0.f};
 }
 
 // Inverse of a symmetric 3x3 block in FP64 (pinned axes: identity, then
@@ -120,323 +545,83 @@ __device__ void inverse3_masked(const float (&D)[9], const float (&m)[3], float 
     for (int c = 0; c < 3; ++c) out[3 * r + c] = float(inv[3 * r + c] * double(m[r]) * double(m[c]));
 }
 
-__device__ __forceinline__ float3 mul3(const float *B, float x, float y, float z) {
-  return make_float3(B[0] * x + B[1] * y + B[2] * z, B[3] * x + B[4] * y + B[5] * z,
-                     B[6] * x + B[7] * y + B[8] * z);
-}
-
-struct PatchSmem {
-  __half2 *vals;
-  uint16_t *lc, *lp;
-  float *B;
-  float4 *S, *Y, *R, *D;
-  unsigned char *tileA;
-};
-
-// Local solve on the patch: Y = q(B^ A^) B^ R by k Chebyshev steps on
-// [lmax / kLoFrac, lmax] (R is overwritten by the local residual).
-__device__ void patch_chebyshev(const PatchSmem &sm, int np, int k, float lmax) {
-  const int i = threadIdx.x;
-  const float lo = lmax / kLoFrac;
-  const float theta = 0.5f * (lmax + lo), delta = 0.5f * (lmax - lo);
-  const float sigma = theta / delta;
-  float rho = 1.f / sigma;
-  float4 y = make_float4(0.f, 0.f, 0.f, 0.f), d = y, res = y;
-  const float *Bi = sm.B + 9 * i;
-  if (i < np) {
-    res = sm.R[i];
-    const float3 t = mul3(Bi, res.x, res.y, res.z);
-    d = make_float4(t.x / theta, t.y / theta, t.z / theta, 0.f);
-    sm.D[i] = d;
-  }
-  for (int s = 0; s < k; ++s) {
-    y.x += d.x; y.y += d.y; y.z += d.z;
-    if (s == k - 1) break;
-    __syncthreads();  // d complete
-    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-    if (i < np) {
-      for (int b = sm.lp[i]; b < sm.lp[i + 1]; ++b) {
-        const float4 dj = sm.D[sm.lc[b]];
-        const __half2 *h = sm.vals + 5 * b;
-        const float2 m01 = __half22float2(h[0]), m23 = __half22float2(h[1]),
-                     m45 = __half22float2(h[2]), m67 = __half22float2(h[3]),
-                     m8 = __half22float2(h[4]);
-        a0 += m01.x * dj.x + m01.y * dj.y + m23.x * dj.z;
-        a1 += m23.y * dj.x + m45.x * dj.y + m45.y * dj.z;
-        a2 += m67.x * dj.x + m67.y * dj.y + m8.x * dj.z;
-      }
-    }
-    __syncthreads();  // every read of d done
-    const float rho1 = 1.f / (2.f * sigma - rho);
-    if (i < np) {
-      res.x -= a0; res.y -= a1; res.z -= a2;
-      const float3 t = mul3(Bi, res.x, res.y, res.z);
-      const float c1 = rho1 * rho, c2 = 2.f * rho1 / delta;
-      d = make_float4(c1 * d.x + c2 * t.x, c1 * d.y + c2 * t.y, c1 * d.z + c2 * t.z, 0.f);
-      sm.D[i] = d;
-    }
-    rho = rho1;
-  }
-  if (i < np) sm.Y[i] = y;
-  __syncthreads();
-}
-
-// Own rows of the patch: [r -= alpha q, x += alpha p], z = M r.
-// Accumulates r'z and r'r.
-__device__ void patch_precond(const PatchParams &P, const PatchSmem &sm, int p0, int np,
-                              bool update, float alpha, int pnew, float lmax,
-                              Acc<float>::V &g, Acc<float>::V &rr) {
-  using A = Acc<float>;
-  const int i = threadIdx.x;
-  V4<float> r{};
-  float4 S = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (i < np) {
-    const int row = p0 + i;
-    r = P.Q.r[0][row];
-    if (update) {
-      const V4<float> q = P.q[row], pn = P.pp[pnew][row];
-      V4<float> xa = P.Q.xacc[row];
-      r.x -= alpha * q.x; r.y -= alpha * q.y; r.z -= alpha * q.z;
-      xa.x += alpha * pn.x; xa.y += alpha * pn.y; xa.z += alpha * pn.z;
-      P.Q.xacc[row] = xa;
-      P.Q.r[0][row] = r;
-    }
-    rr = A::addf(rr, dot3(r, r));
-    S = sm.S[i];
-    sm.R[i] = make_float4(S.x * r.x, S.y * r.y, S.z * r.z, 0.f);
-  }
-  __syncthreads();
-  patch_chebyshev(sm, np, P.degree, lmax);
-  if (i < np) {
-    const float4 y = sm.Y[i];
-    const V4<float> z{S.x * y.x, S.y * y.y, S.z * y.z, 0.f};
-    P.z[p0 + i] = z;
-    g = A::addf(g, dot3(r, z));
-  }
-}
-
-// q = A p over this CTA's tiles, with p = z + beta p_old recomputed on every
-// halo node (written for own rows to pp[cur ^ 1]).  Accumulates p'q.
-__device__ void patch_apass(const PatchParams &P, const PatchSmem &sm, const TileMeta *tiles,
-                            int ntiles, int cur, float beta, Acc<float>::V &pq) {
-  using A = Acc<float>;
-  V4<float> *sU = reinterpret_cast<V4<float> *>(sm.tileA + CA::kValBytes);
-  __shared__ V4<float> sOwn[CA::kTileRows];
-  __shared__ int sRow[CA::kTileRows + 1];
-  const int lrow = threadIdx.x / CA::kRowThreads, part = threadIdx.x % CA::kRowThreads;
-  const V4<float> *po = P.pp[cur];
-  V4<float> *pn = P.pp[cur ^ 1];
-  for (int t = 0; t < ntiles; ++t) {
-    const TileMeta tm = tiles[t];
-    const int i = tm.r0 + lrow;
-    const bool owner = i < tm.r1 && part == 0;
-    V4<float> m{};
-    if (owner) m = P.Q.fmask[i];
-    const float *sA;
-    const uint16_t *sL;
-    stage_tile<CA>(P.Q, tm, sm.tileA, sA, sL, sRow);
-    for (int j = threadIdx.x; j < tm.wn; j += kPThreads) {
-      const int node = __ldg(P.Q.wlist + tm.w0 + j);
-      const V4<float> zj = P.z[node], pj = po[node];
-      const V4<float> u{zj.x + beta * pj.x, zj.y + beta * pj.y, zj.z + beta * pj.z, 0.f};
-      sU[j] = u;
-      if (node >= tm.r0 && node < tm.r1) {
-        sOwn[node - tm.r0] = u;
-        pn[node] = u;
-      }
-    }
-    __syncthreads();
-    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-    if (i < tm.r1) {
-      const int q0 = sRow[lrow], q1 = sRow[lrow + 1];
-      for (int k = q0 + part; k < q1; k += CA::kRowThreads) {
-        const V4<float> u = sU[sL[k]];
-        const float *blk = sA + size_t(k) * 9;
-        a0 += blk[0] * u.x + blk[1] * u.y + blk[2] * u.z;
-        a1 += blk[3] * u.x + blk[4] * u.y + blk[5] * u.z;
-        a2 += blk[6] * u.x + blk[7] * u.y + blk[8] * u.z;
-      }
-    }
-#pragma unroll
-    for (int o = 1; o < CA::kRowThreads; o <<= 1) {
-      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
-    }
-    if (owner) {
-      const V4<float> qv{a0 * m.x, a1 * m.y, a2 * m.z, 0.f};
-      P.q[i] = qv;
-      pq = A::addf(pq, dot3(sOwn[lrow], qv));
-    }
-    __syncthreads();
-  }
-}
-
-// Reliable update: r = rhs - A x64 in FP64 arithmetic over this CTA's tiles.
-__device__ void patch_true_residual(const PatchParams &P, const PatchSmem &sm,
-                                    const TileMeta *tiles, int ntiles, double &rr64) {
-  V4<double> *sX = reinterpret_cast<V4<double> *>(sm.Y);  // overlays the Chebyshev vectors
-  __shared__ int sRow[CA::kTileRows + 1];
-  const int lrow = threadIdx.x / CA::kRowThreads, part = threadIdx.x % CA::kRowThreads;
-  for (int t = 0; t < ntiles; ++t) {
-    const TileMeta tm = tiles[t];
-    const float *sA;
-    const uint16_t *sL;
-    stage_tile<CA>(P.Q, tm, sm.tileA, sA, sL, sRow);
-    for (int j = threadIdx.x; j < tm.wn; j += kPThreads)
-      sX[j] = P.Q.x64[__ldg(P.Q.wlist + tm.w0 + j)];
-    __syncthreads();
-    const int i = tm.r0 + lrow;
-    double a0 = 0, a1 = 0, a2 = 0;
-    if (i < tm.r1) {
-      for (int k = sRow[lrow] + part; k < sRow[lrow + 1]; k += CA::kRowThreads) {
-        const V4<double> xj = sX[sL[k]];
-        const float *blk = sA + size_t(k) * 9;
-        a0 += double(blk[0]) * xj.x + double(blk[1]) * xj.y + double(blk[2]) * xj.z;
-        a1 += double(blk[3]) * xj.x + double(blk[4]) * xj.y + double(blk[5]) * xj.z;
-        a2 += double(blk[6]) * xj.x + double(blk[7]) * xj.y + double(blk[8]) * xj.z;
-      }
-    }
-#pragma unroll
-    for (int o = 1; o < CA::kRowThreads; o <<= 1) {
-      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
-    }
-    if (i < tm.r1 && part == 0) {
-      const V4<double> b = P.Q.rhs[i];
-      const V4<float> m = P.Q.fmask[i];
-      const double e0 = (b.x - a0) * double(m.x), e1 = (b.y - a1) * double(m.y),
-                   e2 = (b.z - a2) * double(m.z);
-      rr64 += e0 * e0 + e1 * e1 + e2 * e2;
-      P.Q.r[0][i] = V4<float>{float(e0), float(e1), float(e2), 0.f};
-    }
-    __syncthreads();
-  }
-}
-
-__global__ void __launch_bounds__(kPThreads, 1) patch_pcg_kernel(PatchParams P) {
+__global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams P) {
   using A = Acc<float>;
   using V = A::V;
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ V red[3 * (kPThreads / 32 + 1)];
-  __shared__ TileMeta tiles[kMaxCtaTiles];
-  __shared__ float s_max[kPThreads / 32];
-  PatchSmem sm;
-  sm.vals = reinterpret_cast<__half2 *>(smem + kOffVals);
-  sm.lc = reinterpret_cast<uint16_t *>(smem + kOffLc);
-  sm.lp = reinterpret_cast<uint16_t *>(smem + kOffLp);
-  sm.B = reinterpret_cast<float *>(smem + kOffB);
-  sm.S = reinterpret_cast<float4 *>(smem + kOffS);
-  sm.Y = reinterpret_cast<float4 *>(smem + kOffVec);
-  sm.R = sm.Y + kMaxPatchRows;
-  sm.D = sm.R + kMaxPatchRows;
-  sm.tileA = smem + kOffA;
-  const int cta = blockIdx.x;
-  const int G = P.Q.n_ctas;
-  unsigned epoch = 0;
+  __shared__ V red[3 * (kRThreads / 32 + 1)];
+  __shared__ float s_max[kRThreads / 32];
+  const ResSmem sm = carve(smem);
+  const int cta = blockIdx.x, i = threadIdx.x;
   const int p0 = P.patch_row[cta], np = P.patch_row[cta + 1] - p0;
-  const int t0 = P.Q.cta_tile[cta], ntiles = P.Q.cta_tile[cta + 1] - t0;
-  for (int t = threadIdx.x; t < ntiles; t += kPThreads) {
-    TileMeta tm;
-    tm.r0 = P.Q.tile_row[t0 + t];
-    tm.r1 = P.Q.tile_row[t0 + t + 1];
-    tm.b0 = P.Q.rowptr[tm.r0];
-    tm.b1 = P.Q.rowptr[tm.r1];
-    tm.w0 = P.Q.tile_wptr[t0 + t];
-    tm.wn = P.Q.tile_wptr[t0 + t + 1] - tm.w0;
-    tiles[t] = tm;
-  }
-  // ---- patch set-up: scaling, block-Jacobi inverses, FP16 submatrix, bound
-  const int i = threadIdx.x;
-  float lmax_row = 0.f;
-  if (i < np) {
-    const int row = p0 + i;
-    float D[9];
-    load9(P.Q.A + size_t(P.diag[row]) * 9, D);
-    const V4<float> fm = P.Q.fmask[row];
-    const float m[3] = {fm.x, fm.y, fm.z};
-    float s[3];
-    for (int c = 0; c < 3; ++c) s[c] = (m[c] != 0.f && D[4 * c] > 0.f) ? 1.f / sqrtf(D[4 * c]) : 0.f;
-    sm.S[i] = make_float4(s[0], s[1], s[2], 0.f);
+  const int nh = P.hnptr[cta + 1] - P.hnptr[cta];
+  GridSum sync{P.part, P.bar, P.st, P.n_ctas, cta, 0u, 0};
+  load_patch(P, sm, cta, p0, np);
+  __syncthreads();
+  const bool own = i < np;
+  const int row = p0 + i;
+  V4<float> r{}, z{}, p{}, x{}, m{};
+  LocalPC L;
+  for (int c = 0; c < 3; ++c) L.S[c] = 0.f;
+  for (int k = 0; k < 9; ++k) L.B[k] = 0.f;
+  // S = diag^-1/2 and B^ = (S A_ii S)^-1 from the resident diagonal block
+  if (own) {
+    r = P.r[0][row];
+    m = P.fmask[row];
+    const float mk[3] = {m.x, m.y, m.z};
+    float D[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int e = sm.uptr[i]; e < sm.uptr[i + 1]; ++e)
+      if (sm.ucol[e] == i)
+        for (int k = 0; k < 9; ++k) D[k] = sm.uval[size_t(e) * 9 + k];
+    for (int c = 0; c < 3; ++c)
+      L.S[c] = (mk[c] != 0.f && D[4 * c] > 0.f) ? 1.f / sqrtf(D[4 * c]) : 0.f;
     float Dh[9];
-    for (int r = 0; r < 3; ++r)
-      for (int c = 0; c < 3; ++c) Dh[3 * r + c] = (0.5f * (D[3 * r + c] + D[3 * c + r])) * (s[r] * s[c]);
-    float Bi[9];
-    inverse3_masked(Dh, m, Bi);
-    for (int k = 0; k < 9; ++k) sm.B[9 * i + k] = Bi[k];
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) Dh[3 * a + b] = D[3 * a + b] * (L.S[a] * L.S[b]);
+    inverse3_masked(Dh, mk, L.B);
+    sm.ds[i] = make_float4(L.S[0], L.S[1], L.S[2], 0.f);
   }
   __syncthreads();
-  if (i < np) {
-    const int row = p0 + i;
-    const int base = P.lptr[p0];
-    const int b0 = P.lptr[row] - base, b1 = P.lptr[row + 1] - base;
-    sm.lp[i] = uint16_t(b0);
-    if (i == np - 1) sm.lp[np] = uint16_t(b1);
-    const float4 si = sm.S[i];
-    const float Si[3] = {si.x, si.y, si.z};
-    const float *Bi = sm.B + 9 * i;
+  // l = infinity norm of B^ A^_pp (row sums of |B^_i S_i A_ij S_j|)
+  float lrow = 0.f;
+  if (own) {
     float acc[3] = {0.f, 0.f, 0.f};
-    for (int b = b0; b < b1; ++b) {
-      const int k = P.lblk[base + b];
-      const int jl = P.llc[base + b];
-      float Aij[9], Aji[9];
-      load9(P.Q.A + size_t(k) * 9, Aij);
-      load9(P.Q.A + size_t(P.tr[k]) * 9, Aji);
-      const float4 sj = sm.S[jl];
+    const int e0 = sm.uptr[i], e1 = sm.uptr[i + 1], t0 = sm.tptr[i], t1 = sm.tptr[i + 1];
+    for (int q = e0; q < e1 + (t1 - t0); ++q) {
+      const bool tr = q >= e1;
+      const int blk = tr ? sm.tupi[t0 + q - e1] : q;
+      const int j = tr ? sm.trow[t0 + q - e1] : sm.ucol[q];
+      const float *v = sm.uval + size_t(blk) * 9;
+      const float4 sj = sm.ds[j];
       const float Sj[3] = {sj.x, sj.y, sj.z};
       float h[9];
-      for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 3; ++c)
-          h[3 * r + c] = (0.5f * (Aij[3 * r + c] + Aji[3 * c + r])) * (Si[r] * Sj[c]);
-      __half2 *dst = sm.vals + 5 * b;
-      dst[0] = __floats2half2_rn(h[0], h[1]);
-      dst[1] = __floats2half2_rn(h[2], h[3]);
-      dst[2] = __floats2half2_rn(h[4], h[5]);
-      dst[3] = __floats2half2_rn(h[6], h[7]);
-      dst[4] = __floats2half2_rn(h[8], 0.f);
-      sm.lc[b] = uint16_t(jl);
-      // row sums of |B_i A^_ij| (infinity norm of B^ A^_pp)
-      for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 3; ++c)
-          acc[r] += fabsf(Bi[3 * r] * h[c] + Bi[3 * r + 1] * h[3 + c] + Bi[3 * r + 2] * h[6 + c]);
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+          h[3 * a + b] = (tr ? v[3 * b + a] : v[3 * a + b]) * (L.S[a] * Sj[b]);
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+          acc[a] += fabsf(L.B[3 * a] * h[b] + L.B[3 * a + 1] * h[3 + b] + L.B[3 * a + 2] * h[6 + b]);
     }
-    lmax_row = fmaxf(acc[0], fmaxf(acc[1], acc[2]));
+    lrow = fmaxf(acc[0], fmaxf(acc[1], acc[2]));
   }
-  for (int o = 16; o > 0; o >>= 1) lmax_row = fmaxf(lmax_row, __shfl_xor_sync(0xffffffffu, lmax_row, o));
-  if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = lmax_row;
+  for (int o = 16; o > 0; o >>= 1) lrow = fmaxf(lrow, __shfl_xor_sync(0xffffffffu, lrow, o));
+  if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = lrow;
   __syncthreads();
-  float lmax = 0.f;
-  for (int w = 0; w < kPThreads / 32; ++w) lmax = fmaxf(lmax, s_max[w]);
-  lmax = fmaxf(kBoundMargin * lmax, 1e-30f);
+  L.lmax = 0.f;
+  for (int wi = 0; wi < kRThreads / 32; ++wi) L.lmax = fmaxf(L.lmax, s_max[wi]);
+  L.lmax = fmaxf(kBoundMargin * L.lmax, 1e-30f);
+  __syncthreads();  // ds is reused by the local solves
 
-  V *partbuf = reinterpret_cast<V *>(P.Q.part);
-  int pset = 0;
-#define EOLC_PATCH_SYNC(a, b, c)                                        \
-  do {                                                                  \
-    block_sum3<CA, float>(a, b, c, red);                                \
-    V *pp_ = partbuf + size_t(3) * G * pset;                            \
-    if (threadIdx.x == 0) {                                             \
-      pp_[3 * cta] = a; pp_[3 * cta + 1] = b; pp_[3 * cta + 2] = c;     \
-    }                                                                   \
-    if (!grid_barrier(P.Q.bar, G, epoch, P.Q.st)) return;               \
-    reduce_partials3<CA, float>(pp_, G, a, b, c, red);                  \
-    pset ^= 1;                                                          \
-  } while (0)
-
-  // ||rhs||^2 (FP64) and the first preconditioned residual
-  double n0 = 0;
-  if (i < np) {
-    const V4<double> b = P.Q.rhs[p0 + i];
-    n0 = b.x * b.x + b.y * b.y + b.z * b.z;
-  }
-  V gam = A::zero(), rr = A::zero();
-  patch_precond(P, sm, p0, np, false, 0.f, 0, lmax, gam, rr);
-  V nrm = A::from_d(n0);  // this thread's share of ||rhs||^2
-  EOLC_PATCH_SYNC(gam, rr, nrm);
-  const double rhs2 = A::to_d(nrm);
-  const V tol2 = A::from_d(P.Q.tol2 * rhs2);
+  const V tol2 = A::from_d(P.tol2 * __ldcg(&P.st->rhs_norm2));
   const V delta2 = A::from_d(kDelta * kDelta);
+  V gam = A::zero(), rr = A::zero(), e0 = A::zero();
+  z = patch_apply(sm, L, own, i, P.degree, r);
+  if (own) {
+    P.z[row] = z;
+    gam = A::addf(gam, dot3(r, z));
+    rr = A::addf(rr, dot3(r, r));
+  }
+  if (!sync(gam, rr, e0, red)) return;
   V rmax2 = rr;
   double last_rr64 = A::to_d(rr);
   int it = 0, nref = 0, status = EOLC_NOT_CONVERGED;
@@ -444,45 +629,77 @@ __global__ void __launch_bounds__(kPThreads, 1) patch_pcg_kernel(PatchParams P) 
   if (!A::finite(rr) || !A::finite(gam)) status = EOLC_NONFINITE;
   V gam_old = A::from_d(1.0);
   bool restart = true;
-  int cur = 0;  // pp[cur] holds the current search direction's predecessor
-  while (!converged && status != EOLC_NONFINITE && it < P.Q.max_iter) {
+  int cur = 0;  // p[cur]: the neighbours' search directions of the last step
+  while (!converged && status != EOLC_NONFINITE && it < P.max_iter) {
     const V beta = restart ? A::zero() : A::div(gam, gam_old);
+    const float bf = float(A::to_t(beta));
     restart = false;
+    const int nxt = cur ^ 1;
+    // p = z + beta p (own rows and, recomputed, halo nodes); q = A p
+    if (own) {
+      p = V4<float>{z.x + bf * p.x, z.y + bf * p.y, z.z + bf * p.z, 0.f};
+      P.p[nxt][row] = p;
+      sm.xs[i] = f4(p);
+    }
+    for (int h = threadIdx.x; h < nh; h += kRThreads) {
+      const int j = sm.hnode[h];
+      const V4<float> zj = P.z[j], pj = P.p[cur][j];
+      sm.xh[h] = make_float4(zj.x + bf * pj.x, zj.y + bf * pj.y, zj.z + bf * pj.z, 0.f);
+    }
+    __syncthreads();
+    V4<float> q{};
     V pq = A::zero(), e1 = A::zero(), e2 = A::zero();
-    patch_apass(P, sm, tiles, ntiles, cur, float(A::to_t(beta)), pq);
-    EOLC_PATCH_SYNC(pq, e1, e2);
+    if (own) {
+      const float3 t = row_apply<true>(sm, i, sm.xs, sm.xh);
+      q = V4<float>{t.x * m.x, t.y * m.y, t.z * m.z, 0.f};
+      pq = A::addf(pq, dot3(p, q));
+    }
+    if (!sync(pq, e1, e2, red)) return;
     if (!A::pos(pq) || !A::pos(gam)) {
       status = (A::finite(pq) && A::finite(gam)) ? EOLC_BREAKDOWN : EOLC_NONFINITE;
       break;
     }
-    const V alpha = A::div(gam, pq);
+    const float af = float(A::to_t(A::div(gam, pq)));
+    if (own) {
+      r.x -= af * q.x; r.y -= af * q.y; r.z -= af * q.z;
+      x.x += af * p.x; x.y += af * p.y; x.z += af * p.z;
+    }
+    z = patch_apply(sm, L, own, i, P.degree, r);
     V g2 = A::zero(), rr2 = A::zero(), e3 = A::zero();
-    patch_precond(P, sm, p0, np, true, float(A::to_t(alpha)), cur ^ 1, lmax, g2, rr2);
-    EOLC_PATCH_SYNC(g2, rr2, e3);
+    if (own) {
+      P.z[row] = z;
+      g2 = A::addf(g2, dot3(r, z));
+      rr2 = A::addf(rr2, dot3(r, r));
+    }
+    if (!sync(g2, rr2, e3, red)) return;
     ++it;
-    cur ^= 1;
+    cur = nxt;
     gam_old = gam;
     gam = g2;
     rr = rr2;
     if (!A::finite(rr) || !A::finite(gam)) { status = EOLC_NONFINITE; break; }
-    if (!(A::lt(rr, A::mul(delta2, rmax2)) || A::le(rr, tol2) || it >= P.Q.max_iter)) continue;
-    // reliable update: fold the FP32 increment into the FP64 solution, then
-    // replace r by the FP64 true residual and z by M r
-    if (i < np) {
-      const int row = p0 + i;
-      const V4<float> xa = P.Q.xacc[row];
-      V4<double> x = P.Q.x64[row];
-      x.x += double(xa.x); x.y += double(xa.y); x.z += double(xa.z);
-      P.Q.x64[row] = x;
-      P.Q.xacc[row] = V4<float>{0.f, 0.f, 0.f, 0.f};
+    if (!(A::lt(rr, A::mul(delta2, rmax2)) || A::le(rr, tol2) || it >= P.max_iter)) continue;
+    // ---- reliable update: x64 += x; r = rhs - A x64 (FP64); z = M r --------
+    if (own) {
+      V4<double> xd = P.x64[row];
+      xd.x += double(x.x); xd.y += double(x.y); xd.z += double(x.z);
+      P.x64[row] = xd;
+      x = V4<float>{0.f, 0.f, 0.f, 0.f};
     }
-    if (!grid_barrier(P.Q.bar, G, epoch, P.Q.st)) return;
+    if (!sync.barrier()) return;
     double rr64d = 0;
-    patch_true_residual(P, sm, tiles, ntiles, rr64d);
-    V g3 = A::zero(), rr3 = A::zero();
-    patch_precond(P, sm, p0, np, false, 0.f, 0, lmax, g3, rr3);
-    V rr64 = A::from_d(rr64d);
-    EOLC_PATCH_SYNC(rr64, g3, rr3);
+    if (own) {
+      const V4<double> q = true_residual(P, row, m);
+      rr64d = q.x * q.x + q.y * q.y + q.z * q.z;
+      r = V4<float>{float(q.x), float(q.y), float(q.z), 0.f};
+    }
+    z = patch_apply(sm, L, own, i, P.degree, r);
+    V rr64 = A::from_d(rr64d), g3 = A::zero(), e4 = A::zero();
+    if (own) {
+      P.z[row] = z;
+      g3 = A::addf(g3, dot3(r, z));
+    }
+    if (!sync(rr64, g3, e4, red)) return;
     ++nref;
     last_rr64 = A::to_d(rr64);
     rmax2 = rr64;
@@ -490,14 +707,12 @@ __global__ void __launch_bounds__(kPThreads, 1) patch_pcg_kernel(PatchParams P) 
     if (!A::finite(rr64) || !A::finite(gam)) { status = EOLC_NONFINITE; break; }
     if (A::le(rr64, tol2)) { converged = true; break; }
   }
-#undef EOLC_PATCH_SYNC
   if (converged) status = EOLC_OK;
   if (cta == 0 && threadIdx.x == 0) {
-    atomicCAS(&P.Q.st->status, EOLC_OK, status);
-    P.Q.st->iterations = it;
-    P.Q.st->refinements = nref;
-    P.Q.st->rhs_norm2 = rhs2;
-    P.Q.st->rel_res = rhs2 > 0 ? sqrt(last_rr64 / rhs2) : 0.0;
+    atomicCAS(&P.st->status, EOLC_OK, status);
+    P.st->iterations = it;
+    P.st->refinements = nref;
+    P.st->rel_res = P.st->rhs_norm2 > 0 ? sqrt(last_rr64 / P.st->rhs_norm2) : 0.0;
   }
 }
 
@@ -541,59 +756,75 @@ __global__ void unpermute_finish_kernel(int n, const int *__restrict__ perm,
 // ---- host: patches by recursive graph bisection -------------------------------
 struct Bisector {
   const std::vector<int> &rowptr, &colidx;
-  std::vector<int> mark, dist, queue;
+  const std::vector<double> *X;  // material coordinates (2 per node), optional
+  std::vector<int> mark;
   int stamp = 0;
-  Bisector(const std::vector<int> &rp, const std::vector<int> &ci)
-      : rowptr(rp), colidx(ci), mark(rp.size() - 1, -1), dist(rp.size() - 1, 0) {}
+  Bisector(const std::vector<int> &rp, const std::vector<int> &ci, const std::vector<double> *x)
+      : rowptr(rp), colidx(ci), X(x), mark(rp.size() - 1, 0) {}
+
+  // Coordinate order: the set sorted along its longer extent (ties by index).
+  void coord_order(const std::vector<int> &set, std::vector<int> &order) {
+    double lo[2] = {1e300, 1e300}, hi[2] = {-1e300, -1e300};
+    for (int v : set)
+      for (int c = 0; c < 2; ++c) {
+        lo[c] = std::min(lo[c], (*X)[2 * v + c]);
+        hi[c] = std::max(hi[c], (*X)[2 * v + c]);
+      }
+    const int ax = (hi[1] - lo[1]) > (hi[0] - lo[0]) ? 1 : 0;
+    order = set;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+      return (*X)[2 * a + ax] < (*X)[2 * b + ax];
+    });
+  }
 
   // BFS over the subgraph induced by `set` from src; unreached nodes of the
-  // set follow in set order.
+  // set follow, each starting a new BFS.
   void bfs(const std::vector<int> &set, int src, std::vector<int> &order) {
-    ++stamp;
-    for (int v : set) mark[v] = stamp;
+    stamp += 2;
+    const int in = stamp, seen = stamp + 1;
+    for (int v : set) mark[v] = in;
     order.clear();
     order.push_back(src);
-    mark[src] = -stamp;
+    mark[src] = seen;
+    size_t scan = 0;
     for (size_t h = 0; h < order.size(); ++h) {
       const int u = order[h];
       for (int k = rowptr[u]; k < rowptr[u + 1]; ++k) {
         const int v = colidx[k];
-        if (mark[v] == stamp) { mark[v] = -stamp; order.push_back(v); }
+        if (mark[v] == in) { mark[v] = seen; order.push_back(v); }
       }
       if (h + 1 == order.size() && order.size() < set.size()) {
-        for (int v : set)
-          if (mark[v] == stamp) { mark[v] = -stamp; order.push_back(v); break; }
+        while (scan < set.size() && mark[set[scan]] != in) ++scan;
+        if (scan < set.size()) { mark[set[scan]] = seen; order.push_back(set[scan]); }
       }
     }
   }
 
-  // Splits set into `parts` pieces of near-equal size (BFS prefixes from a
-  // pseudo-peripheral node); leaves are ordered the same way down to
-  // `leaf` nodes.  Appends the ordered nodes to out and, at depth `parts`,
-  // the piece boundaries to bounds.
-  void split(const std::vector<int> &set, int parts, int leaf, std::vector<int> &out,
-             std::vector<int> *bounds) {
-    if (set.empty() || (parts <= 1 && int(set.size()) <= leaf)) {
-      out.insert(out.end(), set.begin(), set.end());
-      if (bounds) bounds->push_back(int(out.size()));
-      return;
-    }
+  // Splits set into `parts` pieces of near-equal size: recursive coordinate
+  // bisection along the longer extent when material coordinates are given,
+  // else BFS prefixes from a pseudo-peripheral node.  Appends the nodes to
+  // out and the end of each piece to bounds.
+  void split(const std::vector<int> &set, int parts, std::vector<int> &out,
+             std::vector<int> &bounds) {
     std::vector<int> order;
-    bfs(set, set[0], order);
-    bfs(set, order.back(), order);
+    if (!set.empty()) {
+      if (X) {
+        coord_order(set, order);
+      } else {
+        bfs(set, set[0], order);
+        bfs(set, order.back(), order);
+      }
+    }
     if (parts <= 1) {
-      const size_t half = order.size() / 2;
-      std::vector<int> a(order.begin(), order.begin() + half), b(order.begin() + half, order.end());
-      split(a, 1, leaf, out, nullptr);
-      split(b, 1, leaf, out, nullptr);
-      if (bounds) bounds->push_back(int(out.size()));
+      out.insert(out.end(), order.begin(), order.end());
+      bounds.push_back(int(out.size()));
       return;
     }
     const int pl = parts / 2, pr = parts - pl;
     const size_t cut = size_t((long long)order.size() * pl / parts);
     std::vector<int> a(order.begin(), order.begin() + cut), b(order.begin() + cut, order.end());
-    split(a, pl, leaf, out, bounds);
-    split(b, pr, leaf, out, bounds);
+    split(a, pl, out, bounds);
+    split(b, pr, out, bounds);
   }
 };
 
@@ -601,51 +832,28 @@ struct Bisector {
 
 struct PatchPlan {
   int G = 0;
-  std::vector<int> perm, rowptr, colidx, src, tr, diag, patch_row, tile_row, tile_wptr, wlist,
-      cta_tile, lptr, lblk;
-  std::vector<uint16_t> lcol, llc;
+  std::vector<int> perm, rowptr, colidx, src, tr, diag, patch_row, uptr, ublk, tptr, hptr, hblk,
+      hnptr, hnode;
+  std::vector<uint16_t> ucol, tupi, trow, hwin;
 };
 
-struct PatchWork {
-  int n_nodes = 0, n_blocks = 0, G = 0;
-  bool ok = false;
-  std::string why;
-  DevBuf<int> perm, rowptr, colidx, diag, tr, src, tile_row, tile_wptr, wlist, cta_tile,
-      patch_row, lptr, lblk;
-  DevBuf<uint16_t> lcol, llc;
-  DevBuf<float> Ap;
-  DevBuf<unsigned char> vecs, pc, pinp;
-  DevBuf<double> bp, beqp, part;
-  DevBuf<unsigned> bar;
-  DevBuf<DevStatus> st;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  ~PatchWork() {
-    if (ev0) cudaEventDestroy(ev0);
-    if (ev1) cudaEventDestroy(ev1);
-  }
-};
-
-void free_patch_work(PatchWork *w) { delete w; }
-
-// Host plan of the patch solver for a BSR pattern: permutation, permuted
-// pattern with source and transpose blocks, patch and tile boundaries, and
-// the patch-internal block lists.  Returns "" or the reason it does not fit.
+// Host plan of the resident solvers for a BSR pattern: permutation, permuted
+// pattern with source and transpose blocks, patch boundaries and the per-row
+// upper / transposed / halo lists.  X (optional): 2 material coordinates per
+// node, which give compact patches on any mesh.  Returns "" or the reason
+// the mesh does not fit the shared-memory image.
 std::string build_patch_plan(int N, const std::vector<int> &rowptr,
-                             const std::vector<int> &colidx, int n_sm, PatchPlan &out) {
+                             const std::vector<int> &colidx, const std::vector<double> *X,
+                             int n_sm, PatchPlan &out) {
   const int NB = int(colidx.size());
-  // patches: as many as SMs, but at least ~256 rows each on small meshes
-  const int G = std::max(1, std::min(n_sm, (N + 255) / 256));
-  if ((N + G - 1) / G > kMaxPatchRows) {
-    return "mesh too large for shared-memory patches on this device";
-  }
+  const int G = std::max(1, (N + kTargetRows - 1) / kTargetRows);
+  if (G > n_sm) return "mesh too large for shared-memory patches on this device";
   std::vector<int> all(N), perm, bounds;
   for (int k = 0; k < N; ++k) all[k] = k;
   perm.reserve(N);
-  Bisector bis(rowptr, colidx);
-  bis.split(all, G, kLeafRows, perm, &bounds);
-  if (int(perm.size()) != N || int(bounds.size()) != G) {
-    return "patch partition failed";
-  }
+  Bisector bis(rowptr, colidx, X);
+  bis.split(all, G, perm, bounds);
+  if (int(perm.size()) != N || int(bounds.size()) != G) return "patch partition failed";
   std::vector<int> iperm(N);
   for (int k = 0; k < N; ++k) iperm[perm[k]] = k;
   // permuted pattern, source blocks, transposes, diagonals
@@ -663,7 +871,8 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
       if (tmp[q].first == i) pdiag[i] = prow[i] + int(q);
     }
   }
-  for (int i = 0; i < N; ++i)
+  for (int i = 0; i < N; ++i) {
+    if (pdiag[i] < 0) return "a row without its diagonal block";
     for (int k = prow[i]; k < prow[i + 1]; ++k) {
       const int j = pcol[k];
       const int *b = pcol.data() + prow[j], *e = pcol.data() + prow[j + 1];
@@ -671,46 +880,56 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
       if (f == e || *f != i) return "matrix pattern is not symmetric";
       ptr[k] = int(f - pcol.data());
     }
+  }
   std::vector<int> patch_row(G + 1, 0);
   for (int c = 0; c < G; ++c) patch_row[c + 1] = bounds[c];
-  // outer-product tiles inside each patch
-  std::vector<int> breaks(patch_row.begin() + 1, patch_row.end() - 1);
-  std::vector<int> tiles, wptr, wlist;
-  std::vector<uint16_t> lcol;
-  std::string msg = build_tiles(N, prow, pcol, CA::cap_blocks<float>(), kWinA, CA::kTileRows,
-                                tiles, wptr, wlist, lcol, &breaks);
-  if (!msg.empty()) return msg;
-  std::vector<int> cta(G + 1, 0);
-  {
-    int t = 0;
-    for (int c = 0; c <= G; ++c) {
-      while (t < int(tiles.size()) - 1 && tiles[t] < patch_row[c]) ++t;
-      cta[c] = t;
-    }
-    cta[G] = int(tiles.size()) - 1;
-  }
-  for (int c = 0; c < G; ++c)
-    if (cta[c + 1] - cta[c] > kMaxCtaTiles) return "patch has too many tiles";
-  // local (patch-internal) blocks
-  std::vector<int> lptr(N + 1, 0), lblk;
-  std::vector<uint16_t> llc;
+  // per-row lists
+  std::vector<int> uptr(N + 1, 0), ublk, tptr(N + 1, 0), hptr(N + 1, 0), hblk, hnptr(G + 1, 0),
+      hnode;
+  std::vector<uint16_t> ucol, tupi, trow, hwin;
+  std::vector<int> upos(NB, -1);  // patch-local index of an upper entry
+  std::vector<int> win(N, -1);    // window slot of an outside node (global index)
   for (int c = 0; c < G; ++c) {
     const int r0 = patch_row[c], r1 = patch_row[c + 1];
-    if (r1 - r0 > kMaxPatchRows) return "patch too large";
-    const size_t first = lblk.size();
+    if (r1 - r0 > kMaxRows) return "patch too large";
+    const int ubase = int(ublk.size()), tbase = int(tupi.size()), hbase = int(hblk.size()),
+              nbase = int(hnode.size());
     for (int i = r0; i < r1; ++i) {
-      lptr[i] = int(lblk.size());
+      uptr[i] = int(ublk.size());
       for (int k = prow[i]; k < prow[i + 1]; ++k)
-        if (pcol[k] >= r0 && pcol[k] < r1) {
-          lblk.push_back(k);
-          llc.push_back(uint16_t(pcol[k] - r0));
+        if (pcol[k] >= i && pcol[k] < r1) {
+          upos[k] = int(ublk.size()) - ubase;
+          ublk.push_back(k);
+          ucol.push_back(uint16_t(pcol[k] - r0));
         }
     }
-    if (lblk.size() - first > size_t(kMaxLocalBlocks))
-      return "patch submatrix exceeds shared memory";
+    for (int i = r0; i < r1; ++i) {
+      tptr[i] = int(tupi.size());
+      for (int k = prow[i]; k < prow[i + 1]; ++k)
+        if (pcol[k] >= r0 && pcol[k] < i) {
+          tupi.push_back(uint16_t(upos[ptr[k]]));  // block (j, i): an upper entry of row j
+          trow.push_back(uint16_t(pcol[k] - r0));
+        }
+      hptr[i] = int(hblk.size());
+      for (int k = prow[i]; k < prow[i + 1]; ++k) {
+        const int j = pcol[k];
+        if (j >= r0 && j < r1) continue;
+        if (win[j] < nbase) {  // first time this patch sees node j
+          win[j] = int(hnode.size());
+          hnode.push_back(j);
+        }
+        hblk.push_back(k);
+        hwin.push_back(uint16_t(win[j] - nbase));
+      }
+    }
+    hnptr[c + 1] = int(hnode.size());
+    if (int(ublk.size()) - ubase > kMaxUpper || int(tupi.size()) - tbase > kMaxUpper ||
+        int(hblk.size()) - hbase > kMaxHaloBlk || int(hnode.size()) - nbase > kMaxHaloNodes)
+      return "patch exceeds the shared-memory image";
   }
-  lptr[N] = int(lblk.size());
-  lcol.resize(lcol.size() + 8, 0);
+  uptr[N] = int(ublk.size());
+  tptr[N] = int(tupi.size());
+  hptr[N] = int(hblk.size());
   out.G = G;
   out.perm = std::move(perm);
   out.rowptr = std::move(prow);
@@ -719,155 +938,199 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
   out.tr = std::move(ptr);
   out.diag = std::move(pdiag);
   out.patch_row = std::move(patch_row);
-  out.tile_row = std::move(tiles);
-  out.tile_wptr = std::move(wptr);
-  out.wlist = std::move(wlist);
-  out.lcol = std::move(lcol);
-  out.cta_tile = std::move(cta);
-  out.lptr = std::move(lptr);
-  out.lblk = std::move(lblk);
-  out.llc = std::move(llc);
+  out.uptr = std::move(uptr);
+  out.ublk = std::move(ublk);
+  out.ucol = std::move(ucol);
+  out.tptr = std::move(tptr);
+  out.tupi = std::move(tupi);
+  out.trow = std::move(trow);
+  out.hptr = std::move(hptr);
+  out.hblk = std::move(hblk);
+  out.hwin = std::move(hwin);
+  out.hnptr = std::move(hnptr);
+  out.hnode = std::move(hnode);
   return "";
 }
 
+struct PatchWork {
+  int n_nodes = -1, n_blocks = -1, G = 0;
+  std::string why;  // non-empty: the mesh does not fit
+  DevBuf<int> perm, rowptr, colidx, diag, tr, src, patch_row, uptr, ublk, tptr, hptr, hblk,
+      hnptr, hnode;
+  DevBuf<uint16_t> ucol, tupi, trow, hwin;
+  DevBuf<float> Ap;
+  DevBuf<unsigned char> vecs, pc, pinp;
+  DevBuf<double> bp, beqp, part;
+  DevBuf<unsigned> bar;
+  DevBuf<DevStatus> st;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  ~PatchWork() {
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+  }
+};
+
+void free_patch_work(PatchWork *w) { delete w; }
+
 namespace {
 
-eolc_status patch_plan(PatchWork *w, const DevTopology &Tp, int n_sm, cudaStream_t s,
-                       std::string &err) {
+template <typename B, typename Vv>
+cudaError_t upload_vec(B &buf, const Vv &v, cudaStream_t s) {
+  return buf.upload(v.data(), v.size(), s);
+}
+
+// Builds (once per topology) and uploads the plan; w->why records a misfit.
+eolc_status patch_plan(PatchWork *w, const DevTopology &Tp, const double *X_d, int n_sm,
+                       cudaStream_t s, std::string &err) {
   const int N = Tp.n_nodes, NB = Tp.n_blocks;
+  w->n_nodes = N;
+  w->n_blocks = NB;
   std::vector<int> rowptr(N + 1), colidx(NB);
   cudaMemcpy(rowptr.data(), Tp.rowptr.p, sizeof(int) * (N + 1), cudaMemcpyDeviceToHost);
   cudaMemcpy(colidx.data(), Tp.colidx.p, sizeof(int) * NB, cudaMemcpyDeviceToHost);
+  std::vector<double> X;
+  if (X_d) {
+    X.resize(size_t(2) * N);
+    cudaMemcpy(X.data(), X_d, sizeof(double) * X.size(), cudaMemcpyDeviceToHost);
+    for (double v : X)
+      if (!std::isfinite(v)) { X.clear(); break; }
+  }
   PatchPlan L;
-  err = build_patch_plan(N, rowptr, colidx, n_sm, L);
-  if (!err.empty()) return EOLC_BAD_ARG;
-  const int G = L.G;
-  const std::vector<int> &perm = L.perm, &prow = L.rowptr, &pcol = L.colidx, &pdiag = L.diag,
-                         &ptr = L.tr, &psrc = L.src, &tiles = L.tile_row, &wptr = L.tile_wptr,
-                         &wlist = L.wlist, &cta = L.cta_tile, &patch_row = L.patch_row,
-                         &lptr = L.lptr, &lblk = L.lblk;
-  const std::vector<uint16_t> &lcol = L.lcol, &llc = L.llc;
+  w->why = build_patch_plan(N, rowptr, colidx, X.empty() ? nullptr : &X, n_sm, L);
+  if (!w->why.empty()) return EOLC_OK;
+  // empty lists (e.g. no halo on a one-patch mesh) still get one element
+  for (auto *v : {&L.ublk, &L.hblk, &L.hnode})
+    if (v->empty()) v->push_back(0);
+  for (auto *v : {&L.ucol, &L.tupi, &L.trow, &L.hwin})
+    if (v->empty()) v->push_back(0);
   cudaError_t es[] = {
-      w->perm.upload(perm.data(), N, s),
-      w->rowptr.upload(prow.data(), N + 1, s),
-      w->colidx.upload(pcol.data(), NB, s),
-      w->diag.upload(pdiag.data(), N, s),
-      w->tr.upload(ptr.data(), NB, s),
-      w->src.upload(psrc.data(), NB, s),
-      w->tile_row.upload(tiles.data(), tiles.size(), s),
-      w->tile_wptr.upload(wptr.data(), wptr.size(), s),
-      w->wlist.upload(wlist.data(), std::max<size_t>(wlist.size(), 1), s),
-      w->cta_tile.upload(cta.data(), cta.size(), s),
-      w->patch_row.upload(patch_row.data(), patch_row.size(), s),
-      w->lptr.upload(lptr.data(), lptr.size(), s),
-      w->lblk.upload(lblk.data(), std::max<size_t>(lblk.size(), 1), s),
-      w->lcol.upload(lcol.data(), lcol.size(), s),
-      w->llc.upload(llc.data(), std::max<size_t>(llc.size(), 1), s),
+      upload_vec(w->perm, L.perm, s), upload_vec(w->rowptr, L.rowptr, s),
+      upload_vec(w->colidx, L.colidx, s), upload_vec(w->diag, L.diag, s),
+      upload_vec(w->tr, L.tr, s), upload_vec(w->src, L.src, s),
+      upload_vec(w->patch_row, L.patch_row, s), upload_vec(w->uptr, L.uptr, s),
+      upload_vec(w->ublk, L.ublk, s), upload_vec(w->ucol, L.ucol, s),
+      upload_vec(w->tptr, L.tptr, s), upload_vec(w->tupi, L.tupi, s),
+      upload_vec(w->trow, L.trow, s), upload_vec(w->hptr, L.hptr, s),
+      upload_vec(w->hblk, L.hblk, s), upload_vec(w->hwin, L.hwin, s),
+      upload_vec(w->hnptr, L.hnptr, s), upload_vec(w->hnode, L.hnode, s),
       w->Ap.resize(size_t(NB) * 9 + 16),
-      w->vecs.resize(size_t(N) * (sizeof(V4<double>) * 2 + sizeof(V4<float>) * 9)),
-      w->pc.resize(size_t(N) * 4 * sizeof(float)),
+      w->vecs.resize(size_t(N) * (sizeof(V4<double>) * 2 + sizeof(V4<float>) * 11)),
+      w->pc.resize(size_t(N) * 9 * sizeof(float)),
       w->pinp.resize(size_t(N) * 3),
       w->bp.resize(size_t(N) * 3),
       w->beqp.resize(size_t(N) * 3),
-      w->part.resize(size_t(6) * G),
+      w->part.resize(size_t(6) * L.G),
       w->bar.resize(2),
       w->st.resize(1),
-      cudaMemsetAsync(w->Ap.p + size_t(NB) * 9, 0, sizeof(float) * 16, s),
       cudaStreamSynchronize(s)};
   for (cudaError_t e : es)
     if (e != cudaSuccess) { err = cudaGetErrorString(e); return EOLC_CUDA_ERROR; }
-  w->n_nodes = N;
-  w->n_blocks = NB;
-  w->G = G;
+  w->G = L.G;
   return EOLC_OK;
 }
 
 }  // namespace
 
-eolc_status run_pcg_patch(PatchWork *&w, const PcgArgs &a, int degree, eolc_solve_info *info,
-                          cudaStream_t s, std::string &err, long long &launches) {
-  if (a.precision != EOLC_PREC_MIXED) {
-    err = "the patch preconditioner runs on the mixed-precision path";
-    return EOLC_BAD_ARG;
-  }
-  const DevTopology &Tp = *a.T;
-  const int N = Tp.n_nodes, NB = Tp.n_blocks;
+bool resident_fits(PatchWork *&w, const DevTopology &Tp, const double *X_d, cudaStream_t s) {
   int dev = 0, n_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
   if (!w) w = new PatchWork();
-  if (w->n_nodes != N || w->n_blocks != NB) {
-    w->n_nodes = 0;
-    eolc_status st = patch_plan(w, Tp, n_sm, s, err);
-    if (st != EOLC_OK) return st;
+  if (w->n_nodes != Tp.n_nodes || w->n_blocks != Tp.n_blocks) {
+    std::string err;
+    if (patch_plan(w, Tp, X_d, n_sm, s, err) != EOLC_OK) {
+      w->why = err.empty() ? "resident plan upload failed" : err;
+      return false;
+    }
   }
-  cudaFuncSetAttribute(patch_pcg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       int(kPatchSmem));
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, patch_pcg_kernel, kPThreads, kPatchSmem);
-  if (per_sm < 1 || w->G > per_sm * n_sm) {
-    err = "patch kernel does not fit on the device";
+  return w->why.empty();
+}
+
+eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, bool patch_pc, int degree,
+                             eolc_solve_info *info, cudaStream_t s, std::string &err,
+                             long long &launches) {
+  if (a.precision != EOLC_PREC_MIXED) {
+    err = "the resident solvers run on the mixed-precision path";
+    return EOLC_BAD_ARG;
+  }
+  const DevTopology &Tp = *a.T;
+  if (!resident_fits(w, Tp, a.X, s)) {
+    err = w->why;
+    return EOLC_BAD_ARG;
+  }
+  const int N = Tp.n_nodes, NB = Tp.n_blocks, G = w->G;
+  const void *fn =
+      patch_pc ? (const void *)patch_resident_kernel : (const void *)jacobi_resident_kernel;
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kResidentSmem));
+  int dev = 0, n_sm = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kRThreads, kResidentSmem);
+  if (per_sm < 1 || G > per_sm * n_sm) {
+    err = "resident kernel does not fit on the device";
     return EOLC_CUDA_ERROR;
   }
-  const int G = w->G;
+  const int bpc = (!patch_pc && a.precond == EOLC_PC_BLOCK_JACOBI) ? 1 : 0;
   unsigned char *vp = w->vecs.p;
   V4<double> *rhs = reinterpret_cast<V4<double> *>(vp); vp += sizeof(V4<double>) * N;
   V4<double> *x64 = reinterpret_cast<V4<double> *>(vp); vp += sizeof(V4<double>) * N;
   V4<float> *vr = reinterpret_cast<V4<float> *>(vp);
-  PatchParams P{};
-  P.Q.r[0] = vr;
-  P.z = vr + N;
-  P.pp[0] = vr + 2 * N;
-  P.pp[1] = vr + 3 * N;
-  P.q = vr + 4 * N;
-  P.Q.xacc = vr + 5 * N;
-  V4<float> *fmask = vr + 6 * N;
-  V4<float> *scratch = vr + 7 * N;  // setup_kernel's s output (unused here)
-  const int nb_blocks = (NB + 255) / 256, nn = (N + 127) / 128;
-  permute_blocks_kernel<<<nb_blocks, 256, 0, s>>>(NB, w->src.p, a.A32, w->Ap.p);
+  ResParams P{};
+  P.r[0] = vr; P.r[1] = vr + N;
+  P.s[0] = vr + 2 * N; P.s[1] = vr + 3 * N;
+  P.w[0] = vr + 4 * N; P.w[1] = vr + 5 * N;
+  P.p[0] = vr + 6 * N; P.p[1] = vr + 7 * N;
+  P.z = vr + 8 * N;
+  V4<float> *fmask = vr + 9 * N;
+  V4<float> *xacc = vr + 10 * N;  // set-up output, unused (increments live in registers)
+  float *pc = reinterpret_cast<float *>(w->pc.p);
+  const int nbk = (NB + 255) / 256, nn = (N + 127) / 128;
+  permute_blocks_kernel<<<nbk, 256, 0, s>>>(NB, w->src.p, a.A32, w->Ap.p);
   permute_vectors_kernel<<<nn, 128, 0, s>>>(N, w->perm.p, a.b, a.beq_full, a.pinned, w->bp.p,
                                              w->beqp.p, w->pinp.p);
   setup_kernel<float><<<nn, 128, 0, s>>>(N, w->rowptr.p, w->colidx.p, w->diag.p, w->Ap.p, w->bp.p,
-                                         w->beqp.p, w->pinp.p, 0, rhs, x64, P.Q.r[0], P.pp[0],
-                                         scratch, P.Q.xacc, reinterpret_cast<float *>(w->pc.p),
-                                         fmask);
+                                         w->beqp.p, w->pinp.p, bpc, rhs, x64, P.r[0], P.p[0],
+                                         P.s[0], xacc, pc, fmask);
+  init_sums_kernel<RCfg><<<1, kRThreads, 0, s>>>(N, rhs, w->st.p);
   cudaMemsetAsync(w->bar.p, 0, sizeof(unsigned) * 2, s);
-  DevStatus st0{};
-  st0.status = EOLC_OK;
-  cudaMemcpyAsync(w->st.p, &st0, sizeof(DevStatus), cudaMemcpyHostToDevice, s);
-  P.Q.n_nodes = N;
-  P.Q.n_ctas = G;
-  P.Q.rowptr = w->rowptr.p;
-  P.Q.A = w->Ap.p;
-  P.Q.lcol = w->lcol.p;
-  P.Q.tile_row = w->tile_row.p;
-  P.Q.tile_wptr = w->tile_wptr.p;
-  P.Q.wlist = w->wlist.p;
-  P.Q.cta_tile = w->cta_tile.p;
-  P.Q.rhs = rhs;
-  P.Q.x64 = x64;
-  P.Q.fmask = fmask;
-  P.Q.part = w->part.p;
-  P.Q.bar = w->bar.p;
-  P.Q.st = w->st.p;
-  P.Q.max_iter = a.max_iter;
-  P.Q.tol2 = a.rel_tol * a.rel_tol;
-  P.diag = w->diag.p;
-  P.tr = w->tr.p;
-  P.patch_row = w->patch_row.p;
-  P.lptr = w->lptr.p;
-  P.lblk = w->lblk.p;
-  P.llc = w->llc.p;
+  P.n_nodes = N;
+  P.n_ctas = G;
+  P.max_iter = a.max_iter;
   P.degree = std::max(1, std::min(degree, 64));
+  P.block_pc = bpc;
+  P.tol2 = a.rel_tol * a.rel_tol;
+  P.patch_row = w->patch_row.p;
+  P.rowptr = w->rowptr.p;
+  P.colidx = w->colidx.p;
+  P.A = w->Ap.p;
+  P.tr = w->tr.p;
+  P.uptr = w->uptr.p;
+  P.ublk = w->ublk.p;
+  P.ucol = w->ucol.p;
+  P.tptr = w->tptr.p;
+  P.tupi = w->tupi.p;
+  P.trow = w->trow.p;
+  P.hptr = w->hptr.p;
+  P.hblk = w->hblk.p;
+  P.hwin = w->hwin.p;
+  P.hnptr = w->hnptr.p;
+  P.hnode = w->hnode.p;
+  P.rhs = rhs;
+  P.x64 = x64;
+  P.fmask = fmask;
+  P.pc = pc;
+  P.part = w->part.p;
+  P.bar = w->bar.p;
+  P.st = w->st.p;
   void *args[] = {&P};
   if (!w->ev0) { cudaEventCreate(&w->ev0); cudaEventCreate(&w->ev1); }
   cudaEventRecord(w->ev0, s);
-  cudaError_t e = cudaLaunchCooperativeKernel((void *)patch_pcg_kernel, dim3(G), dim3(kPThreads),
-                                              args, kPatchSmem, s);
+  cudaError_t e =
+      cudaLaunchCooperativeKernel(fn, dim3(G), dim3(kRThreads), args, kResidentSmem, s);
   if (e != cudaSuccess) { err = cudaGetErrorString(e); return EOLC_CUDA_ERROR; }
   cudaEventRecord(w->ev1, s);
   unpermute_finish_kernel<<<nn, 128, 0, s>>>(N, w->perm.p, x64, a.beq_full, a.pinned, a.v);
-  launches += 5;  // permute x2, setup, patch PCG, finish
+  launches += 6;  // permute x2, setup, norm, resident PCG, finish
   DevStatus hs;
   cudaMemcpyAsync(&hs, w->st.p, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
   e = cudaStreamSynchronize(s);

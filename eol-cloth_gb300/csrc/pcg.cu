@@ -435,24 +435,6 @@ pcg_general_kernel(Params<T> P, const T *Gm) {
 
 // ---- set-up kernels (one launch each per solve) -----------------------------
 
-// ||rhs||^2 by one CTA; resets the status record.
-__global__ void __launch_bounds__(kThreads) init_sums_kernel(int n_nodes, const V4<double> *rhs,
-                                                             DevStatus *st) {
-  __shared__ double red[3 * (kThreads / 32 + 1)];
-  double s_rhs = 0, d0 = 0, d1 = 0;
-  for (int i = threadIdx.x; i < n_nodes; i += kThreads) {
-    V4<double> b = rhs[i];
-    s_rhs += b.x * b.x + b.y * b.y + b.z * b.z;
-  }
-  block_sum3<C0, double>(s_rhs, d0, d1, red);
-  if (threadIdx.x == 0) {
-    st->status = EOLC_OK;
-    st->iterations = 0;
-    st->refinements = 0;
-    st->rel_res = s_rhs > 0 ? 1.0 : 0.0;
-    st->rhs_norm2 = s_rhs;
-  }
-}
 
 }  // namespace
 
@@ -560,7 +542,7 @@ eolc_status run_pcg_t(SolveWork *&w, const PcgArgs &a, eolc_solve_info *info,
   setup_kernel<T><<<(N + 127) / 128, 128, 0, s>>>(
       N, Tp.rowptr.p, Tp.colidx.p, Tp.diag.p, A, a.b, a.beq_full, a.pinned, bpc, rhs, x64,
       P.r[0], P.p, P.s[0], P.xacc, pc, fmask);
-  init_sums_kernel<<<1, kThreads, 0, s>>>(N, rhs, w->st.p);
+  init_sums_kernel<C0><<<1, kThreads, 0, s>>>(N, rhs, w->st.p);
   cudaMemsetAsync(w->bar.p, 0, sizeof(unsigned) * 2, s);
   P.n_nodes = N;
   P.n_ctas = G;
@@ -691,7 +673,7 @@ eolc_status run_pcg_general_f(SolveWork *&w, const PcgArgs &a, const float *Gm,
   setup_kernel<T><<<(N + 127) / 128, 128, 0, s>>>(N, Tp.rowptr.p, Tp.colidx.p, Tp.diag.p, Amat,
                                                    a.b, a.beq_full, a.pinned, 0, rhs, x64, P.r[0],
                                                    P.p, P.s[0], P.xacc, pc, fmask);
-  init_sums_kernel<<<1, kThreads, 0, s>>>(N, rhs, w->st.p);
+  init_sums_kernel<C0><<<1, kThreads, 0, s>>>(N, rhs, w->st.p);
   cudaMemsetAsync(w->bar.p, 0, sizeof(unsigned) * 2, s);
   cudaMemsetAsync(P.s[0], 0, sizeof(V4<T>) * N, s);
   P.n_nodes = N; P.n_ctas = G; P.rowptr = Tp.rowptr.p; P.A = Amat; P.lcol = w->lcol.p;
@@ -929,7 +911,7 @@ extern "C" eolc_status eolc_velocity_solve_static(
   setup_kernel<T><<<(N + 127) / 128, 128, 0, s>>>(N, d_rowptr, d_colidx, d_diag, A, b_d, d_beq,
                                                    d_pinned, 0, rhs, x64, P.r[0], P.p, P.s[0],
                                                    P.xacc, pc, fmask);
-  init_sums_kernel<<<1, kThreads, 0, s>>>(N, rhs, d_st);
+  init_sums_kernel<C0><<<1, kThreads, 0, s>>>(N, rhs, d_st);
   P.n_nodes = N;
   P.n_ctas = G;
   P.rowptr = d_rowptr;

@@ -45,11 +45,12 @@ class Material(ctypes.Structure):
 class SolveOpts(ctypes.Structure):
     _fields_ = [("rel_tol", ctypes.c_double), ("max_iter", ctypes.c_int),
                 ("precision", ctypes.c_int), ("precond", ctypes.c_int),
-                ("fallback_factor", ctypes.c_int), ("degree", ctypes.c_int)]
+                ("fallback_factor", ctypes.c_int), ("degree", ctypes.c_int),
+                ("streamed", ctypes.c_int)]
 
     def __init__(self, rel_tol=1e-8, max_iter=100000, precision=PREC_MIXED,
-                 precond=PC_JACOBI, fallback_factor=2, degree=0):
-        super().__init__(rel_tol, max_iter, precision, precond, fallback_factor, degree)
+                 precond=PC_JACOBI, fallback_factor=2, degree=0, streamed=0):
+        super().__init__(rel_tol, max_iter, precision, precond, fallback_factor, degree, streamed)
 
 
 class SolveInfo(ctypes.Structure):

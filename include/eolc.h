@@ -76,18 +76,26 @@ typedef struct {
                            0 disables the fallback                       */
   int degree;           /* patch PC: Chebyshev degree of the local solves
                            (0: 8)                                        */
+  int streamed;         /* Jacobi / block Jacobi on the mixed path: 0 runs
+                           the shared-memory-resident kernel when the mesh
+                           fits (about 448 nodes per SM), 1 always streams
+                           the matrix from memory tile by tile           */
 } eolc_solve_opts;
 
-/* EOLC_PC_PATCH (mixed precision only; no counterpart in the reference,
- * whose solve is Eigen's Jacobi CG, GeneralizedSolver.cpp:123-126): the
- * nodes are split by recursive graph bisection into one compact patch per
- * SM; each patch's principal submatrix, scaled to unit diagonal, is held in
- * FP16 in that SM's shared memory for the whole solve, and the preconditioner
- * is a degree-k Chebyshev polynomial of the block-Jacobi-preconditioned patch
- * matrix on [l/30, l], l an upper bound of its spectrum (so it is symmetric
- * positive definite).  Two grid barriers per PCG iteration; convergence on the
- * same FP64 relative residual.  Meshes whose patches exceed shared memory
- * (about 464 nodes per SM) are rejected with EOLC_BAD_ARG. */
+/* Resident solves (mixed precision): the nodes are split by recursive graph
+ * bisection into one compact patch per SM (at most about 448 nodes each);
+ * each SM holds its rows of the FP32 matrix in shared memory for the whole
+ * solve and each row's vectors in one thread's registers.  Point / block
+ * Jacobi then run as a single-grid-barrier Chronopoulos-Gear PCG.
+ * EOLC_PC_PATCH (resident only; no counterpart in the reference, whose solve
+ * is Eigen's Jacobi CG, GeneralizedSolver.cpp:123-126): the preconditioner is
+ * a degree-k Chebyshev polynomial of the block-Jacobi-preconditioned,
+ * unit-diagonal-scaled principal submatrix of each patch on [l/30, l], l an
+ * upper bound of its spectrum (so it is symmetric positive definite), applied
+ * with SM-local barriers; two grid barriers per PCG iteration.  Every solve
+ * converges on the same FP64 relative residual.  Meshes too large for the
+ * resident image stream the matrix (Jacobi) or are rejected with
+ * EOLC_BAD_ARG (EOLC_PC_PATCH). */
 
 typedef struct {
   int status;        /* eolc_status of the solve                          */

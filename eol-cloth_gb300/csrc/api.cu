@@ -26,7 +26,7 @@ namespace {
     }                                                                \
   } while (0)
 
-constexpr int kDefaultPatchDegree = 8;  // Chebyshev degree of the patch solves
+constexpr int kDefaultPatchDegree = 6;  // Chebyshev degree of the patch solves
 
 eolc_status fail(eolc_ctx *ctx, eolc_status s, const char *msg) {
   if (ctx) ctx->err = msg;
@@ -167,13 +167,18 @@ eolc_status solve_device(eolc_ctx *ctx, const eolc_solve_opts *o,
     PcgArgs al = a;
     if (o->fallback_factor > 0 && ctx->last_jacobi_iters > 0)
       al.max_iter = std::min(o->max_iter, o->fallback_factor * ctx->last_jacobi_iters);
-    eolc_status st = run_pcg_learned(ctx->work, al, Gm, inf, s, ctx->err, ctx->launches);
+    const bool resident = !o->streamed && resident_fits(ctx->pwork, ctx->topo, ctx->X.p, s);
+    eolc_status st = resident ? run_pcg_resident(ctx->pwork, al, ResidentPC::kLearned, 0, Gm, inf,
+                                                 s, ctx->err, ctx->launches)
+                              : run_pcg_learned(ctx->work, al, Gm, inf, s, ctx->err, ctx->launches);
     if (st == EOLC_OK || o->fallback_factor <= 0) return st;
     const double kms = inf->solve_kernel_ms;
     const int its = inf->iterations;
     PcgArgs aj = a;
     aj.precond = EOLC_PC_JACOBI;
-    st = run_pcg(ctx->work, aj, inf, s, ctx->err, ctx->launches);
+    st = resident ? run_pcg_resident(ctx->pwork, aj, ResidentPC::kJacobi, 0, nullptr, inf, s,
+                                     ctx->err, ctx->launches)
+                  : run_pcg(ctx->work, aj, inf, s, ctx->err, ctx->launches);
     inf->used_fallback = 1;
     inf->iterations += its;
     inf->solve_kernel_ms += kms;
@@ -181,11 +186,13 @@ eolc_status solve_device(eolc_ctx *ctx, const eolc_solve_opts *o,
     return st;
   }
   if (o->precond == EOLC_PC_PATCH)
-    return run_pcg_resident(ctx->pwork, a, true, o->degree > 0 ? o->degree : kDefaultPatchDegree,
-                            inf, s, ctx->err, ctx->launches);
+    return run_pcg_resident(ctx->pwork, a, ResidentPC::kPatch,
+                            o->degree > 0 ? o->degree : kDefaultPatchDegree, nullptr, inf, s,
+                            ctx->err, ctx->launches);
   eolc_status st;
   if (o->precision == EOLC_PREC_MIXED && !o->streamed && resident_fits(ctx->pwork, ctx->topo, ctx->X.p, s))
-    st = run_pcg_resident(ctx->pwork, a, false, 0, inf, s, ctx->err, ctx->launches);
+    st = run_pcg_resident(ctx->pwork, a, ResidentPC::kJacobi, 0, nullptr, inf, s, ctx->err,
+                          ctx->launches);
   else
     st = run_pcg(ctx->work, a, inf, s, ctx->err, ctx->launches);
   if (st == EOLC_OK && o->precond == EOLC_PC_JACOBI) ctx->last_jacobi_iters = inf->iterations;

@@ -144,14 +144,16 @@ eolc_status batch_read_records(BatchSolveWork *w, std::vector<BatchRecord> &out,
                                cudaStream_t s);
 
 // Resident solvers (patch.cu), mixed precision only: the matrix is held in
-// shared memory for the whole solve.  patch_pc selects the patch-local
-// Chebyshev preconditioner, else point / block Jacobi per a.precond.
+// shared memory for the whole solve.  kJacobi: point / block Jacobi per
+// a.precond; kPatch: the patch-local Chebyshev preconditioner of the given
+// degree; kLearned: the learned approximate inverse Gm (original block order).
+enum class ResidentPC { kJacobi, kPatch, kLearned };
 struct PatchWork;
 void free_patch_work(PatchWork *w);
 bool resident_fits(PatchWork *&w, const DevTopology &T, const double *X_d, cudaStream_t s);
-eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, bool patch_pc, int degree,
-                             eolc_solve_info *info, cudaStream_t s, std::string &err,
-                             long long &launches);
+eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, int degree,
+                             const float *Gm, eolc_solve_info *info, cudaStream_t s,
+                             std::string &err, long long &launches);
 
 // Collisions (collide.cu)
 struct CollideWork;

@@ -69,19 +69,21 @@ constexpr int kRThreads = RCfg::kThreads;
 constexpr int kMaxRows = 464;       // rows of one patch (one thread each)
 constexpr int kTargetRows = 448;    // rows per patch the partition aims for
 constexpr int kMaxUpper = 3072;     // patch-internal blocks, upper triangle
-constexpr int kMaxHaloBlk = 1024;   // blocks coupling the patch to others
+constexpr int kMaxHaloBlk = 768;    // blocks coupling the patch to others
 constexpr int kMaxHaloNodes = 384;  // distinct outside nodes those blocks touch
 constexpr float kLoFrac = 30.f;     // Chebyshev interval [lmax / 30, lmax]
 constexpr float kBoundMargin = 1.02f;
 static_assert(kMaxRows <= kRThreads, "one thread per patch row");
 
 constexpr size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
-constexpr size_t kOffU = 0;                                            // 9 floats per block
-constexpr size_t kOffH = al16(kOffU + size_t(kMaxUpper) * 36);
-constexpr size_t kOffUcol = al16(kOffH + size_t(kMaxHaloBlk) * 36);
-constexpr size_t kOffTupi = al16(kOffUcol + size_t(kMaxUpper) * 2);
-constexpr size_t kOffTrow = al16(kOffTupi + size_t(kMaxUpper) * 2);
-constexpr size_t kOffHwin = al16(kOffTrow + size_t(kMaxUpper) * 2);
+// An upper block is one 48-byte record of three float4: (column, v0, v1, v2),
+// (v3, v4, v5, v6), (v7, v8, -, -), read with three 16-byte loads; the column
+// comes with the first so the vector load can issue early.  A transposed
+// entry is one word: upper record index | (row << 16).
+constexpr size_t kOffU = 0;
+constexpr size_t kOffH = al16(kOffU + size_t(kMaxUpper) * 48);
+constexpr size_t kOffTp = al16(kOffH + size_t(kMaxHaloBlk) * 36);
+constexpr size_t kOffHwin = al16(kOffTp + size_t(kMaxUpper) * 4);
 constexpr size_t kOffUptr = al16(kOffHwin + size_t(kMaxHaloBlk) * 2);
 constexpr size_t kOffTptr = al16(kOffUptr + size_t(kMaxRows + 1) * 2);
 constexpr size_t kOffHptr = al16(kOffTptr + size_t(kMaxRows + 1) * 2);
@@ -110,26 +112,29 @@ struct ResParams {
   V4<double> *x64;
   const V4<float> *fmask;
   const float *pc;                         // Jacobi: 4 per node, block: 9
-  V4<float> *r[2], *s[2], *w[2], *p[2], *z;
+  const float *G;                          // learned PC: permuted FP32 blocks of G
+  const int16_t *bmap;                     // per permuted block: local row (>= 0) or
+                                           // -1 - halo window slot
+  V4<float> *r[2], *s[2], *w[2], *p[2], *z, *q;
   double *part;
   unsigned *bar;
   DevStatus *st;
 };
 
 struct ResSmem {
-  float *uval, *hval;
-  uint16_t *ucol, *tupi, *trow, *hwin, *uptr, *tptr, *hptr;
+  float4 *uval;
+  float *hval;
+  unsigned *tp;
+  uint16_t *hwin, *uptr, *tptr, *hptr;
   int *hnode;
   float4 *xs, *xh, *ds;
 };
 
 __device__ __forceinline__ ResSmem carve(unsigned char *smem) {
   ResSmem m;
-  m.uval = reinterpret_cast<float *>(smem + kOffU);
+  m.uval = reinterpret_cast<float4 *>(smem + kOffU);
   m.hval = reinterpret_cast<float *>(smem + kOffH);
-  m.ucol = reinterpret_cast<uint16_t *>(smem + kOffUcol);
-  m.tupi = reinterpret_cast<uint16_t *>(smem + kOffTupi);
-  m.trow = reinterpret_cast<uint16_t *>(smem + kOffTrow);
+  m.tp = reinterpret_cast<unsigned *>(smem + kOffTp);
   m.hwin = reinterpret_cast<uint16_t *>(smem + kOffHwin);
   m.uptr = reinterpret_cast<uint16_t *>(smem + kOffUptr);
   m.tptr = reinterpret_cast<uint16_t *>(smem + kOffTptr);
@@ -159,15 +164,16 @@ __device__ void load_patch(const ResParams &P, const ResSmem &sm, int cta, int p
     const int u0 = P.uptr[row], u1 = P.uptr[row + 1];
     sm.uptr[i] = uint16_t(u0 - ub);
     for (int e = u0; e < u1; ++e) {
-      sym_block(P.A, P.tr, P.ublk[e], sm.uval + size_t(e - ub) * 9);
-      sm.ucol[e - ub] = P.ucol[e];
+      float v[9];
+      sym_block(P.A, P.tr, P.ublk[e], v);
+      float4 *rec = sm.uval + size_t(e - ub) * 3;
+      rec[0] = make_float4(__int_as_float(int(P.ucol[e])), v[0], v[1], v[2]);
+      rec[1] = make_float4(v[3], v[4], v[5], v[6]);
+      rec[2] = make_float4(v[7], v[8], 0.f, 0.f);
     }
     const int t0 = P.tptr[row], t1 = P.tptr[row + 1];
     sm.tptr[i] = uint16_t(t0 - tb);
-    for (int t = t0; t < t1; ++t) {
-      sm.tupi[t - tb] = P.tupi[t];
-      sm.trow[t - tb] = P.trow[t];
-    }
+    for (int t = t0; t < t1; ++t) sm.tp[t - tb] = unsigned(P.tupi[t]) | (unsigned(P.trow[t]) << 16);
     const int h0 = P.hptr[row], h1 = P.hptr[row + 1];
     sm.hptr[i] = uint16_t(h0 - hb);
     for (int h = h0; h < h1; ++h) {
@@ -190,11 +196,14 @@ __device__ __forceinline__ void fma_blk(const float *v, float4 x, float &a0, flo
   a1 += v[3] * x.x + v[4] * x.y + v[5] * x.z;
   a2 += v[6] * x.x + v[7] * x.y + v[8] * x.z;
 }
-__device__ __forceinline__ void fma_blkT(const float *v, float4 x, float &a0, float &a1,
-                                         float &a2) {
-  a0 += v[0] * x.x + v[3] * x.y + v[6] * x.z;
-  a1 += v[1] * x.x + v[4] * x.y + v[7] * x.z;
-  a2 += v[2] * x.x + v[5] * x.y + v[8] * x.z;
+
+// Block e of the upper storage: its 9 values and patch-local column.
+__device__ __forceinline__ int upper_block(const ResSmem &sm, int e, float (&v)[9]) {
+  const float4 q0 = sm.uval[3 * e], q1 = sm.uval[3 * e + 1], q2 = sm.uval[3 * e + 2];
+  v[0] = q0.y; v[1] = q0.z; v[2] = q0.w;
+  v[3] = q1.x; v[4] = q1.y; v[5] = q1.z; v[6] = q1.w;
+  v[7] = q2.x; v[8] = q2.y;
+  return __float_as_int(q0.x);
 }
 
 // Row i of A x: patch-internal part from xs, halo part from xh (kHalo).
@@ -203,11 +212,24 @@ __device__ __forceinline__ float3 row_apply(const ResSmem &sm, int i, const floa
                                             const float4 *xh) {
   float a0 = 0.f, a1 = 0.f, a2 = 0.f;
 #pragma unroll 2
-  for (int e = sm.uptr[i]; e < sm.uptr[i + 1]; ++e)
-    fma_blk(sm.uval + size_t(e) * 9, xs[sm.ucol[e]], a0, a1, a2);
+  for (int e = sm.uptr[i]; e < sm.uptr[i + 1]; ++e) {
+    const float4 q0 = sm.uval[3 * e];
+    const float4 x = xs[__float_as_int(q0.x)];
+    const float4 q1 = sm.uval[3 * e + 1], q2 = sm.uval[3 * e + 2];
+    a0 += q0.y * x.x + q0.z * x.y + q0.w * x.z;
+    a1 += q1.x * x.x + q1.y * x.y + q1.z * x.z;
+    a2 += q1.w * x.x + q2.x * x.y + q2.y * x.z;
+  }
 #pragma unroll 2
-  for (int t = sm.tptr[i]; t < sm.tptr[i + 1]; ++t)
-    fma_blkT(sm.uval + size_t(sm.tupi[t]) * 9, xs[sm.trow[t]], a0, a1, a2);
+  for (int t = sm.tptr[i]; t < sm.tptr[i + 1]; ++t) {
+    const unsigned w = sm.tp[t];
+    const int e = int(w & 0xffffu);
+    const float4 x = xs[w >> 16];
+    const float4 q0 = sm.uval[3 * e], q1 = sm.uval[3 * e + 1], q2 = sm.uval[3 * e + 2];
+    a0 += q0.y * x.x + q1.x * x.y + q1.w * x.z;
+    a1 += q0.z * x.x + q1.y * x.y + q2.x * x.z;
+    a2 += q0.w * x.x + q1.z * x.y + q2.y * x.z;
+  }
   if (kHalo)
     for (int h = sm.hptr[i]; h < sm.hptr[i + 1]; ++h)
       fma_blk(sm.hval + size_t(h) * 9, xh[sm.hwin[h]], a0, a1, a2);
@@ -570,9 +592,11 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
     m = P.fmask[row];
     const float mk[3] = {m.x, m.y, m.z};
     float D[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    for (int e = sm.uptr[i]; e < sm.uptr[i + 1]; ++e)
-      if (sm.ucol[e] == i)
-        for (int k = 0; k < 9; ++k) D[k] = sm.uval[size_t(e) * 9 + k];
+    for (int e = sm.uptr[i]; e < sm.uptr[i + 1]; ++e) {
+      float v[9];
+      if (upper_block(sm, e, v) == i)
+        for (int k = 0; k < 9; ++k) D[k] = v[k];
+    }
     for (int c = 0; c < 3; ++c)
       L.S[c] = (mk[c] != 0.f && D[4 * c] > 0.f) ? 1.f / sqrtf(D[4 * c]) : 0.f;
     float Dh[9];
@@ -589,9 +613,10 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
     const int e0 = sm.uptr[i], e1 = sm.uptr[i + 1], t0 = sm.tptr[i], t1 = sm.tptr[i + 1];
     for (int q = e0; q < e1 + (t1 - t0); ++q) {
       const bool tr = q >= e1;
-      const int blk = tr ? sm.tupi[t0 + q - e1] : q;
-      const int j = tr ? sm.trow[t0 + q - e1] : sm.ucol[q];
-      const float *v = sm.uval + size_t(blk) * 9;
+      const unsigned tw = tr ? sm.tp[t0 + q - e1] : 0u;
+      float v[9];
+      const int col = upper_block(sm, tr ? int(tw & 0xffffu) : q, v);
+      const int j = tr ? int(tw >> 16) : col;
       const float4 sj = sm.ds[j];
       const float Sj[3] = {sj.x, sj.y, sj.z};
       float h[9];
@@ -696,6 +721,168 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
     z = patch_apply(sm, L, own, i, P.degree, r);
     V rr64 = A::from_d(rr64d), g3 = A::zero(), e4 = A::zero();
     if (own) {
+      P.z[row] = z;
+      g3 = A::addf(g3, dot3(r, z));
+    }
+    if (!sync(rr64, g3, e4, red)) return;
+    ++nref;
+    last_rr64 = A::to_d(rr64);
+    rmax2 = rr64;
+    gam = g3;
+    if (!A::finite(rr64) || !A::finite(gam)) { status = EOLC_NONFINITE; break; }
+    if (A::le(rr64, tol2)) { converged = true; break; }
+  }
+  if (converged) status = EOLC_OK;
+  if (cta == 0 && threadIdx.x == 0) {
+    atomicCAS(&P.st->status, EOLC_OK, status);
+    P.st->iterations = it;
+    P.st->refinements = nref;
+    P.st->rel_res = P.st->rhs_norm2 > 0 ? sqrt(last_rr64 / P.st->rhs_norm2) : 0.0;
+  }
+}
+
+// ---- PCG with the learned approximate inverse G (pattern of A) ----------------
+// G is read from global memory (L2) in the order of the permuted pattern; A is
+// the resident image.  z = G r needs r on the halo: r_j - alpha q_j is
+// recomputed from the neighbours' r of the last step and q of this step, so
+// an iteration keeps two grid barriers (p'q, then r'z and r'r).
+__device__ __forceinline__ V4<float> apply_G(const ResParams &P, const ResSmem &sm, int row) {
+  float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+  for (int k = P.rowptr[row]; k < P.rowptr[row + 1]; ++k) {
+    const int m = P.bmap[k];
+    const float4 x = m >= 0 ? sm.xs[m] : sm.xh[-1 - m];
+    const float *v = P.G + size_t(k) * 9;
+    a0 += __ldg(v) * x.x + __ldg(v + 1) * x.y + __ldg(v + 2) * x.z;
+    a1 += __ldg(v + 3) * x.x + __ldg(v + 4) * x.y + __ldg(v + 5) * x.z;
+    a2 += __ldg(v + 6) * x.x + __ldg(v + 7) * x.y + __ldg(v + 8) * x.z;
+  }
+  return V4<float>{a0, a1, a2, 0.f};
+}
+
+__global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParams P) {
+  using A = Acc<float>;
+  using V = A::V;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ V red[3 * (kRThreads / 32 + 1)];
+  const ResSmem sm = carve(smem);
+  const int cta = blockIdx.x, i = threadIdx.x;
+  const int p0 = P.patch_row[cta], np = P.patch_row[cta + 1] - p0;
+  const int nh = P.hnptr[cta + 1] - P.hnptr[cta];
+  GridSum sync{P.part, P.bar, P.st, P.n_ctas, cta, 0u, 0};
+  load_patch(P, sm, cta, p0, np);
+  const bool own = i < np;
+  const int row = p0 + i;
+  V4<float> r{}, z{}, p{}, x{}, m{};
+  if (own) {
+    r = P.r[0][row];
+    m = P.fmask[row];
+  }
+  const V tol2 = A::from_d(P.tol2 * __ldcg(&P.st->rhs_norm2));
+  const V delta2 = A::from_d(kDelta * kDelta);
+  int cur = 0;  // r[cur], p[cur]: the neighbours' values of the last step
+  // z = G r for the published r[cur] (start, and after a reliable update)
+  V gam = A::zero(), rr = A::zero(), e0 = A::zero();
+  if (own) sm.xs[i] = f4(r);
+  for (int h = threadIdx.x; h < nh; h += kRThreads) sm.xh[h] = f4(P.r[cur][sm.hnode[h]]);
+  __syncthreads();
+  if (own) {
+    const V4<float> g = apply_G(P, sm, row);
+    z = V4<float>{g.x * m.x, g.y * m.y, g.z * m.z, 0.f};
+    P.z[row] = z;
+    gam = A::addf(gam, dot3(r, z));
+    rr = A::addf(rr, dot3(r, r));
+  }
+  if (!sync(gam, rr, e0, red)) return;
+  V rmax2 = rr;
+  double last_rr64 = A::to_d(rr);
+  int it = 0, nref = 0, status = EOLC_NOT_CONVERGED;
+  bool converged = A::finite(rr) && A::le(rr, tol2);
+  if (!A::finite(rr) || !A::finite(gam)) status = EOLC_NONFINITE;
+  V gam_old = A::from_d(1.0);
+  bool restart = true;
+  while (!converged && status != EOLC_NONFINITE && it < P.max_iter) {
+    const V beta = restart ? A::zero() : A::div(gam, gam_old);
+    const float bf = float(A::to_t(beta));
+    restart = false;
+    const int nxt = cur ^ 1;
+    // p = z + beta p, q = A p
+    if (own) {
+      p = V4<float>{z.x + bf * p.x, z.y + bf * p.y, z.z + bf * p.z, 0.f};
+      P.p[nxt][row] = p;
+      sm.xs[i] = f4(p);
+    }
+    for (int h = threadIdx.x; h < nh; h += kRThreads) {
+      const int j = sm.hnode[h];
+      const V4<float> zj = P.z[j], pj = P.p[cur][j];
+      sm.xh[h] = make_float4(zj.x + bf * pj.x, zj.y + bf * pj.y, zj.z + bf * pj.z, 0.f);
+    }
+    __syncthreads();
+    V4<float> q{};
+    V pq = A::zero(), e1 = A::zero(), e2 = A::zero();
+    if (own) {
+      const float3 t = row_apply<true>(sm, i, sm.xs, sm.xh);
+      q = V4<float>{t.x * m.x, t.y * m.y, t.z * m.z, 0.f};
+      P.q[row] = q;
+      pq = A::addf(pq, dot3(p, q));
+    }
+    if (!sync(pq, e1, e2, red)) return;
+    if (!A::pos(pq) || !A::pos(gam)) {
+      status = (A::finite(pq) && A::finite(gam)) ? EOLC_BREAKDOWN : EOLC_NONFINITE;
+      break;
+    }
+    const float af = float(A::to_t(A::div(gam, pq)));
+    // r -= alpha q (own rows, and recomputed on the halo); z = G r
+    if (own) {
+      r.x -= af * q.x; r.y -= af * q.y; r.z -= af * q.z;
+      x.x += af * p.x; x.y += af * p.y; x.z += af * p.z;
+      P.r[nxt][row] = r;
+      sm.xs[i] = f4(r);
+    }
+    for (int h = threadIdx.x; h < nh; h += kRThreads) {
+      const int j = sm.hnode[h];
+      const V4<float> rj = P.r[cur][j], qj = P.q[j];
+      sm.xh[h] = make_float4(rj.x - af * qj.x, rj.y - af * qj.y, rj.z - af * qj.z, 0.f);
+    }
+    __syncthreads();
+    V g2 = A::zero(), rr2 = A::zero(), e3 = A::zero();
+    if (own) {
+      const V4<float> g = apply_G(P, sm, row);
+      z = V4<float>{g.x * m.x, g.y * m.y, g.z * m.z, 0.f};
+      P.z[row] = z;
+      g2 = A::addf(g2, dot3(r, z));
+      rr2 = A::addf(rr2, dot3(r, r));
+    }
+    if (!sync(g2, rr2, e3, red)) return;
+    ++it;
+    cur = nxt;
+    gam_old = gam;
+    gam = g2;
+    rr = rr2;
+    if (!A::finite(rr) || !A::finite(gam)) { status = EOLC_NONFINITE; break; }
+    if (!(A::lt(rr, A::mul(delta2, rmax2)) || A::le(rr, tol2) || it >= P.max_iter)) continue;
+    // ---- reliable update: x64 += x; r = rhs - A x64 (FP64); z = G r --------
+    if (own) {
+      V4<double> xd = P.x64[row];
+      xd.x += double(x.x); xd.y += double(x.y); xd.z += double(x.z);
+      P.x64[row] = xd;
+      x = V4<float>{0.f, 0.f, 0.f, 0.f};
+    }
+    if (!sync.barrier()) return;
+    double rr64d = 0;
+    if (own) {
+      const V4<double> qd = true_residual(P, row, m);
+      rr64d = qd.x * qd.x + qd.y * qd.y + qd.z * qd.z;
+      r = V4<float>{float(qd.x), float(qd.y), float(qd.z), 0.f};
+      P.r[cur][row] = r;
+      sm.xs[i] = f4(r);
+    }
+    if (!sync.barrier()) return;  // the replaced residuals are published
+    for (int h = threadIdx.x; h < nh; h += kRThreads) sm.xh[h] = f4(P.r[cur][sm.hnode[h]]);
+    __syncthreads();
+    V rr64 = A::from_d(rr64d), g3 = A::zero(), e4 = A::zero();
+    if (own) {
+      const V4<float> g = apply_G(P, sm, row);
+      z = V4<float>{g.x * m.x, g.y * m.y, g.z * m.z, 0.f};
       P.z[row] = z;
       g3 = A::addf(g3, dot3(r, z));
     }
@@ -835,6 +1022,7 @@ struct PatchPlan {
   std::vector<int> perm, rowptr, colidx, src, tr, diag, patch_row, uptr, ublk, tptr, hptr, hblk,
       hnptr, hnode;
   std::vector<uint16_t> ucol, tupi, trow, hwin;
+  std::vector<int16_t> bmap;  // per permuted block: local row, or -1 - halo slot
 };
 
 // Host plan of the resident solvers for a BSR pattern: permutation, permuted
@@ -889,6 +1077,7 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
   std::vector<uint16_t> ucol, tupi, trow, hwin;
   std::vector<int> upos(NB, -1);  // patch-local index of an upper entry
   std::vector<int> win(N, -1);    // window slot of an outside node (global index)
+  std::vector<int16_t> bmap(NB, 0);
   for (int c = 0; c < G; ++c) {
     const int r0 = patch_row[c], r1 = patch_row[c + 1];
     if (r1 - r0 > kMaxRows) return "patch too large";
@@ -913,13 +1102,17 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
       hptr[i] = int(hblk.size());
       for (int k = prow[i]; k < prow[i + 1]; ++k) {
         const int j = pcol[k];
-        if (j >= r0 && j < r1) continue;
+        if (j >= r0 && j < r1) {
+          bmap[k] = int16_t(j - r0);
+          continue;
+        }
         if (win[j] < nbase) {  // first time this patch sees node j
           win[j] = int(hnode.size());
           hnode.push_back(j);
         }
         hblk.push_back(k);
         hwin.push_back(uint16_t(win[j] - nbase));
+        bmap[k] = int16_t(-1 - (win[j] - nbase));
       }
     }
     hnptr[c + 1] = int(hnode.size());
@@ -949,6 +1142,7 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
   out.hwin = std::move(hwin);
   out.hnptr = std::move(hnptr);
   out.hnode = std::move(hnode);
+  out.bmap = std::move(bmap);
   return "";
 }
 
@@ -958,7 +1152,8 @@ struct PatchWork {
   DevBuf<int> perm, rowptr, colidx, diag, tr, src, patch_row, uptr, ublk, tptr, hptr, hblk,
       hnptr, hnode;
   DevBuf<uint16_t> ucol, tupi, trow, hwin;
-  DevBuf<float> Ap;
+  DevBuf<int16_t> bmap;
+  DevBuf<float> Ap, Gp;
   DevBuf<unsigned char> vecs, pc, pinp;
   DevBuf<double> bp, beqp, part;
   DevBuf<unsigned> bar;
@@ -1013,8 +1208,9 @@ eolc_status patch_plan(PatchWork *w, const DevTopology &Tp, const double *X_d, i
       upload_vec(w->trow, L.trow, s), upload_vec(w->hptr, L.hptr, s),
       upload_vec(w->hblk, L.hblk, s), upload_vec(w->hwin, L.hwin, s),
       upload_vec(w->hnptr, L.hnptr, s), upload_vec(w->hnode, L.hnode, s),
+      upload_vec(w->bmap, L.bmap, s),
       w->Ap.resize(size_t(NB) * 9 + 16),
-      w->vecs.resize(size_t(N) * (sizeof(V4<double>) * 2 + sizeof(V4<float>) * 11)),
+      w->vecs.resize(size_t(N) * (sizeof(V4<double>) * 2 + sizeof(V4<float>) * 12)),
       w->pc.resize(size_t(N) * 9 * sizeof(float)),
       w->pinp.resize(size_t(N) * 3),
       w->bp.resize(size_t(N) * 3),
@@ -1046,9 +1242,14 @@ bool resident_fits(PatchWork *&w, const DevTopology &Tp, const double *X_d, cuda
   return w->why.empty();
 }
 
-eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, bool patch_pc, int degree,
-                             eolc_solve_info *info, cudaStream_t s, std::string &err,
-                             long long &launches) {
+eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, int degree,
+                             const float *Gm, eolc_solve_info *info, cudaStream_t s,
+                             std::string &err, long long &launches) {
+  const bool patch_pc = mode == ResidentPC::kPatch, learned = mode == ResidentPC::kLearned;
+  if (learned && !Gm) {
+    err = "no learned preconditioner blocks";
+    return EOLC_BAD_ARG;
+  }
   if (a.precision != EOLC_PREC_MIXED) {
     err = "the resident solvers run on the mixed-precision path";
     return EOLC_BAD_ARG;
@@ -1059,8 +1260,9 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, bool patch_pc, int
     return EOLC_BAD_ARG;
   }
   const int N = Tp.n_nodes, NB = Tp.n_blocks, G = w->G;
-  const void *fn =
-      patch_pc ? (const void *)patch_resident_kernel : (const void *)jacobi_resident_kernel;
+  const void *fn = patch_pc  ? (const void *)patch_resident_kernel
+                   : learned ? (const void *)learned_resident_kernel
+                             : (const void *)jacobi_resident_kernel;
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kResidentSmem));
   int dev = 0, n_sm = 0, per_sm = 0;
   cudaGetDevice(&dev);
@@ -1070,7 +1272,7 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, bool patch_pc, int
     err = "resident kernel does not fit on the device";
     return EOLC_CUDA_ERROR;
   }
-  const int bpc = (!patch_pc && a.precond == EOLC_PC_BLOCK_JACOBI) ? 1 : 0;
+  const int bpc = (mode == ResidentPC::kJacobi && a.precond == EOLC_PC_BLOCK_JACOBI) ? 1 : 0;
   unsigned char *vp = w->vecs.p;
   V4<double> *rhs = reinterpret_cast<V4<double> *>(vp); vp += sizeof(V4<double>) * N;
   V4<double> *x64 = reinterpret_cast<V4<double> *>(vp); vp += sizeof(V4<double>) * N;
@@ -1083,9 +1285,18 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, bool patch_pc, int
   P.z = vr + 8 * N;
   V4<float> *fmask = vr + 9 * N;
   V4<float> *xacc = vr + 10 * N;  // set-up output, unused (increments live in registers)
+  P.q = vr + 11 * N;
   float *pc = reinterpret_cast<float *>(w->pc.p);
   const int nbk = (NB + 255) / 256, nn = (N + 127) / 128;
   permute_blocks_kernel<<<nbk, 256, 0, s>>>(NB, w->src.p, a.A32, w->Ap.p);
+  if (learned) {
+    if (w->Gp.resize(size_t(NB) * 9) != cudaSuccess) {
+      err = "device allocation failed";
+      return EOLC_CUDA_ERROR;
+    }
+    permute_blocks_kernel<<<nbk, 256, 0, s>>>(NB, w->src.p, Gm, w->Gp.p);
+    launches += 1;
+  }
   permute_vectors_kernel<<<nn, 128, 0, s>>>(N, w->perm.p, a.b, a.beq_full, a.pinned, w->bp.p,
                                              w->beqp.p, w->pinp.p);
   setup_kernel<float><<<nn, 128, 0, s>>>(N, w->rowptr.p, w->colidx.p, w->diag.p, w->Ap.p, w->bp.p,
@@ -1119,6 +1330,8 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, bool patch_pc, int
   P.x64 = x64;
   P.fmask = fmask;
   P.pc = pc;
+  P.G = learned ? w->Gp.p : nullptr;
+  P.bmap = w->bmap.p;
   P.part = w->part.p;
   P.bar = w->bar.p;
   P.st = w->st.p;

@@ -223,8 +223,8 @@ def run_reference(args, rank):
 
 
 ARM_KERNEL = {"jacobi": "jacobi_resident_kernel", "block": "jacobi_resident_kernel",
-              "patch": "patch_resident_kernel", "learned": "pcg_general_kernel",
-              "jacobi-streamed": "cg_kernel"}
+              "patch": "patch_resident_kernel", "learned": "learned_resident_kernel",
+              "learned-r4": "learned_resident_kernel", "jacobi-streamed": "cg_kernel"}
 
 
 def arm_opts(eolc, arm, degree):
@@ -237,15 +237,22 @@ def arm_opts(eolc, arm, degree):
         return eolc.SolveOpts(precond=eolc.PC_BLOCK_JACOBI, **base)
     if arm == "patch":
         return eolc.SolveOpts(precond=eolc.PC_PATCH, degree=degree, **base)
-    if arm == "learned":
+    if arm in ("learned", "learned-r4"):
         return eolc.SolveOpts(precond=eolc.PC_LEARNED, fallback_factor=2, **base)
     raise ValueError(arm)
 
 
-def time_arm(ctx, sc, mat, opts, x_w, v_w, steps, stream, flush, world, dev):
+def arm_refresh(arm):
+    """Network evaluations per solve of an arm: learned-r4 re-evaluates the
+    learned preconditioner every 4 solves (eolc_set_learned_refresh)."""
+    return 4 if arm == "learned-r4" else 1
+
+
+def time_arm(ctx, sc, mat, opts, x_w, v_w, steps, stream, flush, world, dev, refresh=1):
     """K steps from the post-warm-up state, each bracketed by CUDA events on
     the library's stream with L2 flushed before it; max over ranks."""
     import torch
+    ctx.set_learned_refresh(refresh)
     ctx.state_upload(x_w, sc["X"], v_w)
     if world > 1:
         torch.distributed.barrier()
@@ -272,6 +279,7 @@ def time_arm(ctx, sc, mat, opts, x_w, v_w, steps, stream, flush, world, dev):
         t = torch.tensor([total_ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = t.item()
+    ctx.set_learned_refresh(1)
     return {"steps_per_s": world * steps / (total_ms / 1e3), "ms_per_step": total_ms / steps,
             "mean_pcg_iters": statistics.mean(iters), "pcg_kernel_ms": statistics.mean(kern_ms),
             "assemble_ms": statistics.mean(asm_ms), "fallbacks": fallback,
@@ -295,14 +303,14 @@ def run_ours(args, rank, world, local_rank):
     lpc = None
     weights = os.path.join(ROOT, "eol-cloth_gb300", "weights", "lpc.npy")
     arms = args.precond.split(",") if args.precond != "all" else \
-        ["jacobi", "jacobi-streamed", "patch", "learned"]
-    if "learned" in arms:
+        ["jacobi", "jacobi-streamed", "patch", "learned", "learned-r4"]
+    if any(a.startswith("learned") for a in arms):
         if os.path.exists(weights):
             lpc = eolc.LearnedPC(local_rank)
             lpc.set_params(np.load(weights))
             lpc.attach(ctx)
         else:
-            arms.remove("learned")
+            arms = [a for a in arms if not a.startswith("learned")]
 
     # warm-up steps with Jacobi from rest; every arm starts from this state
     ctx.state_upload(sc["x"], sc["X"], np.zeros(3 * sc["n"]))
@@ -315,13 +323,15 @@ def run_ours(args, rank, world, local_rank):
             ctx.step_resident(1, mat, GRAV, H, sc["fixed"], sc["fixed_vel"],
                               arm_opts(eolc, arm, args.degree))
         results = {arm: time_arm(ctx, sc, mat, arm_opts(eolc, arm, args.degree), x_w, v_w,
-                                 args.steps, stream, flush, world, dev) for arm in arms}
+                                 args.steps, stream, flush, world, dev, arm_refresh(arm))
+                   for arm in arms}
     best = max(results, key=lambda a: results[a]["steps_per_s"])
     res = results[best]
     value = res["steps_per_s"]
 
     # e2e: the best arm through eolc_step with pinned host buffers
     opts = arm_opts(eolc, best, args.degree)
+    ctx.set_learned_refresh(arm_refresh(best))
     xh = torch.empty(3 * sc["n"], dtype=torch.float64).pin_memory().numpy()
     vh = torch.empty(3 * sc["n"], dtype=torch.float64).pin_memory().numpy()
     Xh = torch.empty(2 * sc["n"], dtype=torch.float64).pin_memory().numpy()
@@ -351,7 +361,7 @@ def run_ours(args, rank, world, local_rank):
     hbm = peaks.get("hbm_gbs", 6800.0)
     # algorithmic bytes of one HBM-streamed iteration of the best arm's method
     bpi = algorithmic_bytes_per_iter(sc["n"], n_blocks)
-    if best == "learned":
+    if best.startswith("learned"):
         bpi += n_blocks * (36 + 4)  # one more BSR apply (G, pattern of MDK)
     elif best == "patch":
         bpi += (max(1, args.degree) - 1) * n_blocks * 36  # local Chebyshev products
@@ -380,9 +390,9 @@ def run_ours(args, rank, world, local_rank):
                                " 852481 blocks, 2 corners pinned, rel-res 1e-8 (FP64)",
                    "solver": "%s-PCG (fastest arm)" % best,
                    "arms": arms_out,
-                   "learned_vs_jacobi_steps_ratio": (results["learned"]["steps_per_s"] /
-                                                     results["jacobi"]["steps_per_s"])
-                   if "learned" in results and "jacobi" in results else None,
+                   "learned_vs_jacobi_steps_ratio": {
+                       a: results[a]["steps_per_s"] / results["jacobi"]["steps_per_s"]
+                       for a in results if a.startswith("learned") and "jacobi" in results},
                    "patch_degree": args.degree,
                    "l2": "flushed (256 MiB write) before each step",
                    "start": "%d Jacobi warm-up steps from rest; every arm times the same "
@@ -414,7 +424,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precond", default="all",
                     help="comma-separated arms among jacobi, jacobi-streamed, block, patch, "
-                         "learned; 'all' times jacobi, jacobi-streamed, patch and learned")
+                         "learned, learned-r4; 'all' times all but block")
     ap.add_argument("--degree", type=int, default=6, help="patch preconditioner degree")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-sheets line")

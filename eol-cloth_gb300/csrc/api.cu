@@ -158,16 +158,24 @@ eolc_status solve_device(eolc_ctx *ctx, const eolc_solve_opts *o,
     if (!ctx->lpc) return fail(ctx, EOLC_BAD_ARG, "no learned preconditioner attached");
     if (o->precision != EOLC_PREC_MIXED)
       return fail(ctx, EOLC_BAD_ARG, "the learned preconditioner runs on the mixed path");
+    const bool resident = !o->streamed && resident_fits(ctx->pwork, ctx->topo, ctx->X.p, s);
+    // the resident path keeps the network's G between solves: it is
+    // re-evaluated once it has served lpc_refresh solves (1: every solve)
+    const bool reuse = resident && ctx->lpc_cached == ctx->lpc && ctx->lpc_uses < ctx->lpc_refresh;
     const float *Gm = nullptr;
-    std::string msg = learned_forward(ctx->lpc, ctx, ctx->pinned.p, &Gm, s);
-    if (!msg.empty()) return fail(ctx, EOLC_CUDA_ERROR, msg.c_str());
-    ctx->launches += 20;  // network forward kernels
+    if (!reuse) {
+      std::string msg = learned_forward(ctx->lpc, ctx, ctx->pinned.p, &Gm, s);
+      if (!msg.empty()) return fail(ctx, EOLC_CUDA_ERROR, msg.c_str());
+      ctx->launches += 20;  // network forward kernels
+      ctx->lpc_cached = resident ? ctx->lpc : nullptr;
+      ctx->lpc_uses = 0;
+    }
+    ctx->lpc_uses += 1;
     // fall back to Jacobi when the learned solve has not converged within
     // fallback_factor x the last Jacobi iteration count
     PcgArgs al = a;
     if (o->fallback_factor > 0 && ctx->last_jacobi_iters > 0)
       al.max_iter = std::min(o->max_iter, o->fallback_factor * ctx->last_jacobi_iters);
-    const bool resident = !o->streamed && resident_fits(ctx->pwork, ctx->topo, ctx->X.p, s);
     eolc_status st = resident ? run_pcg_resident(ctx->pwork, al, ResidentPC::kLearned, 0, Gm, inf,
                                                  s, ctx->err, ctx->launches)
                               : run_pcg_learned(ctx->work, al, Gm, inf, s, ctx->err, ctx->launches);
@@ -335,6 +343,13 @@ long long eolc_launch_count(const eolc_ctx *ctx) { return ctx ? ctx->launches : 
 eolc_status eolc_attach_preconditioner(eolc_ctx *ctx, eolc_lpc *lpc) {
   if (!ctx) return EOLC_BAD_ARG;
   ctx->lpc = lpc;
+  ctx->lpc_cached = nullptr;
+  return EOLC_OK;
+}
+
+eolc_status eolc_set_learned_refresh(eolc_ctx *ctx, int solves) {
+  if (!ctx || solves < 1) return EOLC_BAD_ARG;
+  ctx->lpc_refresh = solves;
   return EOLC_OK;
 }
 
@@ -472,6 +487,7 @@ eolc_status eolc_set_topology_batched(eolc_ctx *ctx, int n_inst, const int *node
   ctx->work = nullptr;
   free_patch_work(ctx->pwork);
   ctx->pwork = nullptr;
+  ctx->lpc_cached = nullptr;
   free_batch_work(ctx->bwork);
   ctx->bwork = nullptr;
   ctx->batch_config = -1;

@@ -146,7 +146,8 @@ eolc_status batch_read_records(BatchSolveWork *w, std::vector<BatchRecord> &out,
 // Resident solvers (patch.cu), mixed precision only: the matrix is held in
 // shared memory for the whole solve.  kJacobi: point / block Jacobi per
 // a.precond; kPatch: the patch-local Chebyshev preconditioner of the given
-// degree; kLearned: the learned approximate inverse Gm (original block order).
+// degree; kLearned: the learned approximate inverse Gm (original block order;
+// nullptr reuses the G of the previous learned solve on this topology).
 enum class ResidentPC { kJacobi, kPatch, kLearned };
 struct PatchWork;
 void free_patch_work(PatchWork *w);
@@ -196,6 +197,9 @@ struct eolc_ctx {
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::vector<int> host_tri;  // triangle list of the current topology
   eolc_lpc *lpc = nullptr;    // attached learned preconditioner (not owned)
+  const eolc_lpc *lpc_cached = nullptr;  // network whose G the resident solver holds
+  int lpc_uses = 0;           // solves that G has served
+  int lpc_refresh = 1;        // re-evaluate the network every lpc_refresh solves
   eolc::CollideWork *cd_work = nullptr;
   // batches: instance k owns nodes node_off[k] .. node_off[k+1]
   std::vector<int> node_off;

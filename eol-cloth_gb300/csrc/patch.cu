@@ -112,9 +112,10 @@ struct ResParams {
   V4<double> *x64;
   const V4<float> *fmask;
   const float *pc;                         // Jacobi: 4 per node, block: 9
-  const float *G;                          // learned PC: permuted FP32 blocks of G
-  const int16_t *bmap;                     // per permuted block: local row (>= 0) or
+  const float *Gs;                         // learned PC: G in warp slices (below)
+  const int16_t *bsl;                      // per slice slot: local row (>= 0) or
                                            // -1 - halo window slot
+  const int *slice_off, *slice_len;        // per (CTA, warp) slice: first slot, slots
   V4<float> *r[2], *s[2], *w[2], *p[2], *z, *q;
   double *part;
   unsigned *bar;
@@ -746,15 +747,25 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
 // the resident image.  z = G r needs r on the halo: r_j - alpha q_j is
 // recomputed from the neighbours' r of the last step and q of this step, so
 // an iteration keeps two grid barriers (p'q, then r'z and r'r).
-__device__ __forceinline__ V4<float> apply_G(const ResParams &P, const ResSmem &sm, int row) {
+// Row of this thread of G r.  G is stored in warp slices: the rows of warp w
+// of CTA c form slice 16 c + w; slot k of the slice holds the k-th block of
+// each of the 32 rows, component-major and lane-contiguous
+// (Gs[((off + k) * 9 + comp) * 32 + lane]), zero-padded to the slice's
+// longest row, so every load of the warp is one coalesced 128-byte line.
+__device__ __forceinline__ V4<float> apply_G(const ResParams &P, const ResSmem &sm, int cta) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sl = cta * (kRThreads / 32) + warp;
+  const int off = P.slice_off[sl], len = P.slice_len[sl];
   float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-  for (int k = P.rowptr[row]; k < P.rowptr[row + 1]; ++k) {
-    const int m = P.bmap[k];
+#pragma unroll 2
+  for (int k = 0; k < len; ++k) {
+    const size_t slot = size_t(off + k);
+    const int m = P.bsl[slot * 32 + lane];
     const float4 x = m >= 0 ? sm.xs[m] : sm.xh[-1 - m];
-    const float *v = P.G + size_t(k) * 9;
-    a0 += __ldg(v) * x.x + __ldg(v + 1) * x.y + __ldg(v + 2) * x.z;
-    a1 += __ldg(v + 3) * x.x + __ldg(v + 4) * x.y + __ldg(v + 5) * x.z;
-    a2 += __ldg(v + 6) * x.x + __ldg(v + 7) * x.y + __ldg(v + 8) * x.z;
+    const float *v = P.Gs + slot * 9 * 32 + lane;
+    a0 += __ldg(v) * x.x + __ldg(v + 32) * x.y + __ldg(v + 64) * x.z;
+    a1 += __ldg(v + 96) * x.x + __ldg(v + 128) * x.y + __ldg(v + 160) * x.z;
+    a2 += __ldg(v + 192) * x.x + __ldg(v + 224) * x.y + __ldg(v + 256) * x.z;
   }
   return V4<float>{a0, a1, a2, 0.f};
 }
@@ -786,7 +797,7 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
   for (int h = threadIdx.x; h < nh; h += kRThreads) sm.xh[h] = f4(P.r[cur][sm.hnode[h]]);
   __syncthreads();
   if (own) {
-    const V4<float> g = apply_G(P, sm, row);
+    const V4<float> g = apply_G(P, sm, cta);
     z = V4<float>{g.x * m.x, g.y * m.y, g.z * m.z, 0.f};
     P.z[row] = z;
     gam = A::addf(gam, dot3(r, z));
@@ -846,7 +857,7 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
     __syncthreads();
     V g2 = A::zero(), rr2 = A::zero(), e3 = A::zero();
     if (own) {
-      const V4<float> g = apply_G(P, sm, row);
+      const V4<float> g = apply_G(P, sm, cta);
       z = V4<float>{g.x * m.x, g.y * m.y, g.z * m.z, 0.f};
       P.z[row] = z;
       g2 = A::addf(g2, dot3(r, z));
@@ -881,7 +892,7 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
     __syncthreads();
     V rr64 = A::from_d(rr64d), g3 = A::zero(), e4 = A::zero();
     if (own) {
-      const V4<float> g = apply_G(P, sm, row);
+      const V4<float> g = apply_G(P, sm, cta);
       z = V4<float>{g.x * m.x, g.y * m.y, g.z * m.z, 0.f};
       P.z[row] = z;
       g3 = A::addf(g3, dot3(r, z));
@@ -904,6 +915,19 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
 }
 
 // ---- per-solve permutation kernels --------------------------------------------
+// Warp-slice layout of the learned G (see apply_G): gsrc holds, per slot and
+// lane, the block of G in the context's order, or -1 for padding.
+__global__ void slice_blocks_kernel(int n_lanes, const int *__restrict__ gsrc,
+                                    const float *__restrict__ G, float *__restrict__ Gs) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n_lanes) return;
+  const int k = gsrc[idx];
+  const size_t slot = size_t(idx >> 5), lane = size_t(idx & 31);
+  float *d = Gs + slot * 9 * 32 + lane;
+#pragma unroll
+  for (int c = 0; c < 9; ++c) d[32 * c] = k >= 0 ? __ldg(G + size_t(k) * 9 + c) : 0.f;
+}
+
 __global__ void permute_blocks_kernel(int nb, const int *__restrict__ src,
                                       const float *__restrict__ A, float *__restrict__ Ap) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1022,7 +1046,9 @@ struct PatchPlan {
   std::vector<int> perm, rowptr, colidx, src, tr, diag, patch_row, uptr, ublk, tptr, hptr, hblk,
       hnptr, hnode;
   std::vector<uint16_t> ucol, tupi, trow, hwin;
-  std::vector<int16_t> bmap;  // per permuted block: local row, or -1 - halo slot
+  std::vector<int16_t> bsl;   // per slice slot and lane: local row, or -1 - halo slot
+  std::vector<int> gsrc;      // per slice slot and lane: block in the original order, or -1
+  std::vector<int> slice_off, slice_len;  // per (patch, warp)
 };
 
 // Host plan of the resident solvers for a BSR pattern: permutation, permuted
@@ -1142,7 +1168,33 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
   out.hwin = std::move(hwin);
   out.hnptr = std::move(hnptr);
   out.hnode = std::move(hnode);
-  out.bmap = std::move(bmap);
+  // warp slices of the pattern (for the learned G)
+  constexpr int kWarps = kRThreads / 32;
+  out.slice_off.assign(size_t(G) * kWarps, 0);
+  out.slice_len.assign(size_t(G) * kWarps, 0);
+  int slots = 0;
+  for (int c = 0; c < G; ++c)
+    for (int w = 0; w < kWarps; ++w) {
+      const int r0 = out.patch_row[c] + 32 * w, r1 = std::min(out.patch_row[c + 1], r0 + 32);
+      int len = 0;
+      for (int i = r0; i < r1; ++i) len = std::max(len, out.rowptr[i + 1] - out.rowptr[i]);
+      out.slice_off[size_t(c) * kWarps + w] = slots;
+      out.slice_len[size_t(c) * kWarps + w] = len;
+      slots += len;
+    }
+  out.bsl.assign(size_t(slots) * 32, 0);
+  out.gsrc.assign(size_t(slots) * 32, -1);
+  for (int c = 0; c < G; ++c)
+    for (int w = 0; w < kWarps; ++w) {
+      const int r0 = out.patch_row[c] + 32 * w, r1 = std::min(out.patch_row[c + 1], r0 + 32);
+      const int off = out.slice_off[size_t(c) * kWarps + w];
+      for (int i = r0; i < r1; ++i)
+        for (int k = out.rowptr[i]; k < out.rowptr[i + 1]; ++k) {
+          const size_t q = size_t(off + k - out.rowptr[i]) * 32 + (i - r0);
+          out.bsl[q] = bmap[k];
+          out.gsrc[q] = out.src[k];
+        }
+    }
   return "";
 }
 
@@ -1152,8 +1204,9 @@ struct PatchWork {
   DevBuf<int> perm, rowptr, colidx, diag, tr, src, patch_row, uptr, ublk, tptr, hptr, hblk,
       hnptr, hnode;
   DevBuf<uint16_t> ucol, tupi, trow, hwin;
-  DevBuf<int16_t> bmap;
-  DevBuf<float> Ap, Gp;
+  DevBuf<int16_t> bsl;
+  DevBuf<int> gsrc, slice_off, slice_len;
+  DevBuf<float> Ap, Gs;
   DevBuf<unsigned char> vecs, pc, pinp;
   DevBuf<double> bp, beqp, part;
   DevBuf<unsigned> bar;
@@ -1208,7 +1261,8 @@ eolc_status patch_plan(PatchWork *w, const DevTopology &Tp, const double *X_d, i
       upload_vec(w->trow, L.trow, s), upload_vec(w->hptr, L.hptr, s),
       upload_vec(w->hblk, L.hblk, s), upload_vec(w->hwin, L.hwin, s),
       upload_vec(w->hnptr, L.hnptr, s), upload_vec(w->hnode, L.hnode, s),
-      upload_vec(w->bmap, L.bmap, s),
+      upload_vec(w->bsl, L.bsl, s), upload_vec(w->gsrc, L.gsrc, s),
+      upload_vec(w->slice_off, L.slice_off, s), upload_vec(w->slice_len, L.slice_len, s),
       w->Ap.resize(size_t(NB) * 9 + 16),
       w->vecs.resize(size_t(N) * (sizeof(V4<double>) * 2 + sizeof(V4<float>) * 12)),
       w->pc.resize(size_t(N) * 9 * sizeof(float)),
@@ -1246,10 +1300,6 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, i
                              const float *Gm, eolc_solve_info *info, cudaStream_t s,
                              std::string &err, long long &launches) {
   const bool patch_pc = mode == ResidentPC::kPatch, learned = mode == ResidentPC::kLearned;
-  if (learned && !Gm) {
-    err = "no learned preconditioner blocks";
-    return EOLC_BAD_ARG;
-  }
   if (a.precision != EOLC_PREC_MIXED) {
     err = "the resident solvers run on the mixed-precision path";
     return EOLC_BAD_ARG;
@@ -1289,12 +1339,17 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, i
   float *pc = reinterpret_cast<float *>(w->pc.p);
   const int nbk = (NB + 255) / 256, nn = (N + 127) / 128;
   permute_blocks_kernel<<<nbk, 256, 0, s>>>(NB, w->src.p, a.A32, w->Ap.p);
-  if (learned) {
-    if (w->Gp.resize(size_t(NB) * 9) != cudaSuccess) {
+  if (learned && !Gm && !w->Gs.p) {
+    err = "no learned preconditioner blocks";
+    return EOLC_BAD_ARG;
+  }
+  if (learned && Gm) {  // Gm == nullptr: keep the sliced G of the last solve
+    const int n_lanes = int(w->gsrc.n);
+    if (w->Gs.resize(size_t(n_lanes) * 9) != cudaSuccess) {
       err = "device allocation failed";
       return EOLC_CUDA_ERROR;
     }
-    permute_blocks_kernel<<<nbk, 256, 0, s>>>(NB, w->src.p, Gm, w->Gp.p);
+    slice_blocks_kernel<<<(n_lanes + 255) / 256, 256, 0, s>>>(n_lanes, w->gsrc.p, Gm, w->Gs.p);
     launches += 1;
   }
   permute_vectors_kernel<<<nn, 128, 0, s>>>(N, w->perm.p, a.b, a.beq_full, a.pinned, w->bp.p,
@@ -1330,8 +1385,10 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, i
   P.x64 = x64;
   P.fmask = fmask;
   P.pc = pc;
-  P.G = learned ? w->Gp.p : nullptr;
-  P.bmap = w->bmap.p;
+  P.Gs = learned ? w->Gs.p : nullptr;
+  P.bsl = w->bsl.p;
+  P.slice_off = w->slice_off.p;
+  P.slice_len = w->slice_len.p;
   P.part = w->part.p;
   P.bar = w->bar.p;
   P.st = w->st.p;

@@ -103,7 +103,7 @@ EXPORTS = ["eolc_version", "eolc_launch_count", "eolc_create", "eolc_destroy", "
            "eolc_attach_preconditioner", "eolc_set_jacobi_reference",
            "eolc_set_topology_batched", "eolc_set_instance_materials", "eolc_step_batched",
            "eolc_batch_num_configs", "eolc_batch_config_name", "eolc_batch_set_config",
-           "eolc_batch_autotune"]
+           "eolc_batch_autotune", "eolc_set_learned_refresh"]
 
 
 def load_library(path=LIB_PATH):
@@ -154,6 +154,7 @@ def load_library(path=LIB_PATH):
     L.eolc_lpc_train.argtypes = [_V, ctypes.c_int, ctypes.c_float, ctypes.c_uint, _D]
     L.eolc_attach_preconditioner.argtypes = [_V, _V]
     L.eolc_set_jacobi_reference.argtypes = [_V, ctypes.c_int]
+    L.eolc_set_learned_refresh.argtypes = [_V, ctypes.c_int]
     L.eolc_set_topology_batched.argtypes = [_V, ctypes.c_int, _I, _I, _I, _I, _I]
     L.eolc_set_instance_materials.argtypes = [_V, ctypes.POINTER(Material), ctypes.c_int]
     L.eolc_step_batched.argtypes = [_V, ctypes.c_int, _D, ctypes.c_double, _I, _D, ctypes.c_int,
@@ -352,6 +353,9 @@ class Context:
                                    ctypes.byref(tot))
         self._check(st)
         return tot, [infos[k] for k in range(n_inst)]
+
+    def set_learned_refresh(self, solves):
+        self._check(lib.eolc_set_learned_refresh(self._h, solves))
 
     def batch_set_config(self, config):
         self._check(lib.eolc_batch_set_config(self._h, config))

@@ -327,6 +327,12 @@ eolc_status eolc_lpc_train(eolc_lpc *lpc, int epochs, float lr, unsigned seed,
 /* Attach (or detach with NULL) the network used by EOLC_PC_LEARNED solves on
  * this context; the context does not own it. */
 eolc_status eolc_attach_preconditioner(eolc_ctx *ctx, eolc_lpc *lpc);
+/* Evaluate the attached network every `solves` learned solves (default 1)
+ * and keep its G in between (a lagged preconditioner: any symmetric positive
+ * definite G leaves PCG exact, and the Jacobi fallback still bounds the
+ * iterations).  Applies to the shared-memory-resident solve; re-attaching a
+ * network (eolc_attach_preconditioner) forces a new evaluation. */
+eolc_status eolc_set_learned_refresh(eolc_ctx *ctx, int solves);
 /* Iteration count of a plain Jacobi solve that the learned solve's fallback
  * cap (fallback_factor x this count) refers to; set automatically by every
  * successful Jacobi solve on the context. */

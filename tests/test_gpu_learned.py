@@ -143,4 +143,33 @@ def test_trained_network_needs_fewer_iterations_than_jacobi(eolc):
     gain = 1.0 - np.mean(it_l) / np.mean(it_j)
     print("mean PCG iterations: Jacobi %.1f, learned %.1f (%.1f%% fewer)"
           % (np.mean(it_j), np.mean(it_l), 100 * gain))
-    assert gain >= 0.05
+    # the committed network (white-noise probes) needs ~45% fewer here
+    assert gain >= 0.30
+
+
+def test_learned_refresh_reuses_the_network_output(eolc):
+    """With a refresh interval of 3 the network runs on solves 1 and 4 only;
+    every solve still reaches the FP64 residual and Jacobi's velocities."""
+    s = scenes.sheet(32)
+    ctx = eolc.Context(0)
+    ctx.set_topology(s["n"], s["tri"], s["hinge"])
+    mat = eolc.Material(**scenes.material_c1())
+    lpc = eolc.LearnedPC(0, seed=4)
+    if os.path.exists(WEIGHTS):
+        lpc.set_params(np.load(WEIGHTS))
+    lpc.attach(ctx)
+    ctx.set_learned_refresh(3)
+    x, v = s["x"].copy(), np.zeros(3 * s["n"])
+    counts = []
+    for k in range(5):
+        xl, vl = x.copy(), v.copy()
+        ctx.step(x, s["X"], v, mat, scenes.GRAV, scenes.H, s["fixed"], s["fixed_vel"],
+                 eolc.SolveOpts(precond=eolc.PC_JACOBI))
+        c0 = ctx.launch_count()
+        info = ctx.step(xl, s["X"], vl, mat, scenes.GRAV, scenes.H, s["fixed"], s["fixed_vel"],
+                        eolc.SolveOpts(precond=eolc.PC_LEARNED, fallback_factor=0))
+        counts.append(ctx.launch_count() - c0)
+        assert info.status == eolc.OK and info.rel_res <= 1e-8
+        assert np.abs(vl - v).max() <= 1e-5 * np.abs(v).max()
+    # the network (and the re-layout of its output) runs on solves 1 and 4
+    assert counts[0] == counts[3] > counts[1] == counts[2] == counts[4], counts

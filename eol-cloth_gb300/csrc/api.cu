@@ -236,8 +236,13 @@ eolc_status batch_begin(eolc_ctx *ctx, const double grav[3], double h, const int
   eolc_status st = need_topology(ctx);
   if (st != EOLC_OK) return st;
   if ((st = check_opts(ctx, opts)) != EOLC_OK) return st;
-  if (opts->precond != EOLC_PC_JACOBI && opts->precond != EOLC_PC_BLOCK_JACOBI)
-    return fail(ctx, EOLC_BAD_ARG, "batched steps use the Jacobi or block-Jacobi preconditioner");
+  if (opts->precond == EOLC_PC_PATCH)
+    return fail(ctx, EOLC_BAD_ARG, "batched steps use Jacobi, block Jacobi or the learned preconditioner");
+  if (opts->precond == EOLC_PC_LEARNED) {
+    if (!ctx->lpc) return fail(ctx, EOLC_BAD_ARG, "no learned preconditioner attached");
+    if (opts->precision != EOLC_PREC_MIXED)
+      return fail(ctx, EOLC_BAD_ARG, "the learned preconditioner runs on the mixed path");
+  }
   if (!grav) return fail(ctx, EOLC_BAD_ARG, "null gravity");
   if (n_fixed > 0 && (!fixed_dofs_h || !fixed_vel_h)) return fail(ctx, EOLC_BAD_ARG, "null fixed list");
   const int n_inst = int(ctx->node_off.size()) - 1;
@@ -264,6 +269,7 @@ eolc_status enqueue_batch_assembly(eolc_ctx *ctx, const double grav[3], double h
     ctx->launches += 1;
   }
   eolc_material unused{};
+  ctx->last_precision = o->precision;  // the matrix the step leaves on the context
   return assemble(ctx, unused, grav, h, o->precision, false, true, s, true);
 }
 
@@ -287,8 +293,13 @@ eolc_status enqueue_batch_step(eolc_ctx *ctx, const double grav[3], double h,
 // and keeps the fastest.  ms_h (optional): one entry per configuration,
 // -1 where the configuration does not apply.
 eolc_status batch_autotune(eolc_ctx *ctx, const double grav[3], double h,
-                           const eolc_solve_opts *o, cudaStream_t s, int *chosen,
+                           const eolc_solve_opts *o_in, cudaStream_t s, int *chosen,
                            double *ms_h) {
+  // configurations are timed on the Jacobi solve (the learned solve runs on
+  // the same tiles and cluster shape)
+  eolc_solve_opts oj = *o_in;
+  if (oj.precond == EOLC_PC_LEARNED) oj.precond = EOLC_PC_JACOBI;
+  const eolc_solve_opts *o = &oj;
   eolc_status st = enqueue_batch_assembly(ctx, grav, h, o, s);
   if (st != EOLC_OK) return st;
   DevBuf<double> scratch;
@@ -330,6 +341,75 @@ eolc_status batch_autotune(eolc_ctx *ctx, const double grav[3], double h,
   ctx->batch_config = best;
   if (chosen) *chosen = best;
   return EOLC_OK;
+}
+
+// Per-instance and total results of a batched call from the device records.
+eolc_status batch_results(eolc_ctx *ctx, int n_steps, float ms, cudaStream_t s,
+                          eolc_solve_info *inst_info_h, eolc_batch_info *total) {
+  std::vector<BatchRecord> rec;
+  eolc_status st = batch_read_records(ctx->bwork, rec, s);
+  if (st != EOLC_OK) return fail(ctx, st, "batched step failed on the device");
+  eolc_batch_info tot{};
+  tot.status = EOLC_OK;
+  tot.config = ctx->batch_config;
+  tot.steps = n_steps;
+  tot.step_ms = ms;
+  for (size_t k = 0; k < rec.size(); ++k) {
+    const BatchRecord &r = rec[k];
+    if (r.status != EOLC_OK) {
+      if (tot.status == EOLC_OK) tot.status = r.status;
+      tot.n_failed += 1;
+    }
+    tot.iterations += r.iterations;
+    tot.max_iterations = std::max(tot.max_iterations, r.max_iterations);
+    tot.max_rel_res = std::max(tot.max_rel_res, r.rel_res);
+    tot.n_fallback += r.used_fallback;
+    if (inst_info_h) {
+      eolc_solve_info &o = inst_info_h[k];
+      o = eolc_solve_info{};
+      o.status = r.status;
+      o.iterations = r.iterations;
+      o.refinements = r.refinements;
+      o.used_fallback = r.used_fallback;
+      o.rel_res = r.rel_res;
+    }
+  }
+  if (total) *total = tot;
+  if (tot.status != EOLC_OK) ctx->err = "an instance's solve failed (see the per-instance status)";
+  return eolc_status(tot.status);
+}
+
+// Batched steps with the learned preconditioner: per step the assembly, the
+// network's forward pass on the whole batch (block-diagonal G), one learned
+// batched launch with per-instance caps and one Jacobi launch over the
+// instances it left unconverged, x += h v.  Not captured in a graph (the
+// forward pass synchronises).
+eolc_status step_batched_learned(eolc_ctx *ctx, int n_steps, const double grav[3], double h,
+                                 const eolc_solve_opts *opts, eolc_solve_info *inst_info_h,
+                                 eolc_batch_info *total, cudaStream_t s) {
+  eolc_status st = batch_reset_records(ctx->bwork, s);
+  if (st != EOLC_OK) return fail(ctx, st, "record reset failed");
+  if (!ctx->ev[2]) { cudaEventCreate(&ctx->ev[2]); cudaEventCreate(&ctx->ev[3]); }
+  EOLC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
+  const int n = 3 * ctx->topo.n_nodes;
+  for (int k = 0; k < n_steps; ++k) {
+    if ((st = enqueue_batch_assembly(ctx, grav, h, opts, s)) != EOLC_OK) return st;
+    const float *Gm = nullptr;
+    std::string msg = learned_forward(ctx->lpc, ctx, ctx->pinned.p, &Gm, s);
+    if (!msg.empty()) return fail(ctx, EOLC_CUDA_ERROR, msg.c_str());
+    ctx->launches += 20;
+    PcgArgs a = batch_pcg_args(ctx, opts, ctx->v.p);
+    if ((st = batch_enqueue_learned(ctx->bwork, a, Gm, opts->fallback_factor, ctx->node_inst.p, s,
+                                    ctx->err, ctx->launches)) != EOLC_OK)
+      return st;
+    integrate_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, h, ctx->v.p, ctx->x.p);
+    ctx->launches += 1;
+  }
+  EOLC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
+  EOLC_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
+  return batch_results(ctx, n_steps, ms, s, inst_info_h, total);
 }
 
 }  // namespace
@@ -698,6 +778,18 @@ eolc_status eolc_set_instance_materials(eolc_ctx *ctx, const eolc_material *mats
   return EOLC_OK;
 }
 
+eolc_status eolc_batch_set_jacobi_reference(eolc_ctx *ctx, const int *iters_h, int n_inst) {
+  eolc_status st = need_topology(ctx);
+  if (st != EOLC_OK) return st;
+  if (!iters_h || n_inst != int(ctx->node_off.size()) - 1)
+    return fail(ctx, EOLC_BAD_ARG, "one reference per instance is required");
+  if (!ctx->bwork || ctx->batch_config < 0)
+    return fail(ctx, EOLC_BAD_ARG, "no batched step has prepared the batch yet");
+  return batch_set_jacobi_reference(ctx->bwork, iters_h, n_inst, stream_of(ctx)) == EOLC_OK
+             ? EOLC_OK
+             : fail(ctx, EOLC_CUDA_ERROR, "reference upload failed");
+}
+
 eolc_status eolc_batch_set_config(eolc_ctx *ctx, int config) {
   if (!ctx) return EOLC_BAD_ARG;
   if (config < -1 || config >= batch_num_configs())
@@ -733,10 +825,13 @@ eolc_status eolc_step_batched(eolc_ctx *ctx, int n_steps, const double grav[3], 
   }
   {
     PcgArgs a = batch_pcg_args(ctx, opts, ctx->v.p);
+    if (opts->precond == EOLC_PC_LEARNED) a.precond = EOLC_PC_JACOBI;
     std::string msg;
     if ((st = batch_prepare(ctx->bwork, a, ctx->node_off, ctx->batch_config, s, msg)) != EOLC_OK)
       return fail(ctx, st, msg.c_str());
   }
+  if (opts->precond == EOLC_PC_LEARNED)
+    return step_batched_learned(ctx, n_steps, grav, h, opts, inst_info_h, total, s);
   // the captured graph holds these values and device addresses
   std::vector<double> key = {double(opts->precision), double(opts->precond), opts->rel_tol,
                              double(opts->max_iter), h, grav[0], grav[1], grav[2],
@@ -779,37 +874,10 @@ eolc_status eolc_step_batched(eolc_ctx *ctx, int n_steps, const double grav[3], 
   for (int k = 0; k < n_steps; ++k) EOLC_CHECK_CUDA(ctx, cudaGraphLaunch(ctx->bgraph, s));
   EOLC_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
   ctx->launches += (long long)ctx->bgraph_launches * n_steps;
-  std::vector<BatchRecord> rec;
-  if ((st = batch_read_records(ctx->bwork, rec, s)) != EOLC_OK)
-    return fail(ctx, st, "batched step failed on the device");
+  EOLC_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
-  eolc_batch_info tot{};
-  tot.status = EOLC_OK;
-  tot.config = ctx->batch_config;
-  tot.steps = n_steps;
-  tot.step_ms = ms;
-  for (size_t k = 0; k < rec.size(); ++k) {
-    const BatchRecord &r = rec[k];
-    if (r.status != EOLC_OK) {
-      if (tot.status == EOLC_OK) tot.status = r.status;
-      tot.n_failed += 1;
-    }
-    tot.iterations += r.iterations;
-    tot.max_iterations = std::max(tot.max_iterations, r.max_iterations);
-    tot.max_rel_res = std::max(tot.max_rel_res, r.rel_res);
-    if (inst_info_h) {
-      eolc_solve_info &o = inst_info_h[k];
-      o = eolc_solve_info{};
-      o.status = r.status;
-      o.iterations = r.iterations;
-      o.refinements = r.refinements;
-      o.rel_res = r.rel_res;
-    }
-  }
-  if (total) *total = tot;
-  if (tot.status != EOLC_OK) ctx->err = "an instance's solve failed (see the per-instance status)";
-  return eolc_status(tot.status);
+  return batch_results(ctx, n_steps, ms, s, inst_info_h, total);
 }
 
 }  // extern "C"

@@ -41,13 +41,39 @@ constexpr int kMaxBatchTiles = 160;  // tiles of one instance held by one CTA
 
 struct BatchArgs {
   int n_inst;
+  const int *n_inst_d;   // if set: the queue length, read on the device
   const int *inst_tile;  // n_inst + 1: first tile of every instance
   const int *order;      // queue position -> instance (largest first)
   unsigned *queue;       // next queue position; zero before each launch
   BatchRecord *rec;      // per instance, accumulated over launches
+  const int *cap;        // if set: per-instance iteration cap (else max_iter)
+  int *last_status;      // if set: per-instance status of this launch
+  int *jac_iters;        // if set: Jacobi iterations of each converged instance
+  int fallback;          // 1: this launch re-solves instances a learned solve left
   double tol2;           // rel_tol^2
   int max_iter;
 };
+
+// Per-instance bookkeeping at the end of an instance's solve (rank 0,
+// thread 0 of its cluster).  A learned solve that stopped at its cap leaves
+// the status to the Jacobi re-solve that follows.
+__device__ __forceinline__ void record_instance(const BatchArgs &B, int inst, int status, int it,
+                                                int nref, double last_rr64, double rhs2,
+                                                bool learned) {
+  BatchRecord r = B.rec[inst];
+  const bool deferred = learned && status == EOLC_NOT_CONVERGED;
+  if (r.status == EOLC_OK && !deferred) r.status = status;
+  r.iterations += it;
+  r.refinements += nref;
+  r.max_iterations = max(r.max_iterations, it);
+  if (!deferred) r.steps += 1;
+  if (B.fallback) r.used_fallback = 1;
+  const double rel = rhs2 > 0 ? sqrt(last_rr64 / rhs2) : 0.0;
+  if (!deferred) r.rel_res = fmax(r.rel_res, rel);
+  B.rec[inst] = r;
+  if (B.last_status) B.last_status[inst] = status;
+  if (B.jac_iters && !learned && status == EOLC_OK) B.jac_iters[inst] = it;
+}
 
 __device__ __forceinline__ void cluster_barrier() {
   // Every thread of every CTA of the cluster arrives.  release: this thread's
@@ -106,11 +132,13 @@ batch_cg_kernel(Params<T> P, BatchArgs B) {
     if (crank == 0 && threadIdx.x == 0) s_inst = int(atomicAdd(B.queue, 1u));
     cluster_barrier();
     const int q = *cl.map_shared_rank(&s_inst, 0);
-    if (q >= B.n_inst) {
+    const int n_queue = B.n_inst_d ? *B.n_inst_d : B.n_inst;
+    if (q >= n_queue) {
       cluster_barrier();  // nobody leaves while the leader's slot may be read
       return;
     }
     const int inst = B.order[q];
+    const int max_iter = B.cap ? B.cap[inst] : B.max_iter;
     const int it0 = B.inst_tile[inst];
     const int nt = B.inst_tile[inst + 1] - it0;
     const int c0 = it0 + int((long long)nt * crank / csize);
@@ -149,7 +177,7 @@ batch_cg_kernel(Params<T> P, BatchArgs B) {
     if (!A::finite(rr)) status = EOLC_NONFINITE;
     V gam_old = A::from_d(1.0), alpha_old = A::from_d(1.0);
     bool restart = true;
-    while (!converged && status != EOLC_NONFINITE && it < B.max_iter) {
+    while (!converged && status != EOLC_NONFINITE && it < max_iter) {
       const V beta = restart ? A::zero() : A::div(gam, gam_old);
       const V denom =
           restart ? del : A::add(del, A::neg(A::div(A::mul(beta, gam), alpha_old)));
@@ -171,7 +199,7 @@ batch_cg_kernel(Params<T> P, BatchArgs B) {
       del = d2;
       rr = rr2;
       if (!A::finite(rr) || !A::finite(gam) || !A::finite(del)) { status = EOLC_NONFINITE; break; }
-      if (!(A::lt(rr, A::mul(delta2, rmax2)) || A::le(rr, tol2) || it >= B.max_iter)) continue;
+      if (!(A::lt(rr, A::mul(delta2, rmax2)) || A::le(rr, tol2) || it >= max_iter)) continue;
       // reliable update: fold the FP32 increment into the FP64 solution ...
       for (int t = 0; t < ntiles; ++t)
         for (int i = tiles[t].r0 + threadIdx.x; i < tiles[t].r1; i += C::kThreads) {
@@ -199,19 +227,197 @@ batch_cg_kernel(Params<T> P, BatchArgs B) {
       del = d3;
     }
     if (converged) status = EOLC_OK;
-    if (crank == 0 && threadIdx.x == 0) {
-      BatchRecord r = B.rec[inst];
-      if (r.status == EOLC_OK) r.status = status;
-      r.iterations += it;
-      r.refinements += nref;
-      r.max_iterations = max(r.max_iterations, it);
-      r.steps += 1;
-      const double rel = rhs2 > 0 ? sqrt(last_rr64 / rhs2) : 0.0;
-      r.rel_res = fmax(r.rel_res, rel);
-      B.rec[inst] = r;
+    if (crank == 0 && threadIdx.x == 0)
+      record_instance(B, inst, status, it, nref, last_rr64, rhs2, false);
+    __syncthreads();
+  }
+}
+
+
+// Batched PCG with the learned approximate inverse G (FP32, pattern of A):
+// standard PCG per instance, two cluster reductions per iteration (p'q after
+// q = A p; r'z and r'r after z = G r), the halo values recomputed on the fly
+// as in pcg_general_kernel (pcg.cu).  An instance stops at its cap
+// (B.cap: fallback_factor x its last Jacobi count) and is left to the Jacobi
+// re-solve that follows in the same step.
+template <class C, int kMinBlocks>
+__global__ void __launch_bounds__(C::kThreads, kMinBlocks)
+batch_gen_kernel(Params<float> P, BatchArgs B, const float *Gm) {
+  using T = float;
+  using A = Acc<T>;
+  using V = typename A::V;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ V red[3 * (C::kThreads / 32 + 1)];
+  __shared__ TileMeta tiles[kMaxBatchTiles];
+  __shared__ double xch[2][3];
+  __shared__ int s_inst;
+  cgr::cluster_group cl = cgr::this_cluster();
+  const int crank = int(cl.block_rank()), csize = int(cl.num_blocks());
+  int pset = 0;
+  const V delta2 = A::from_d(kDelta * kDelta);
+  double *redd = reinterpret_cast<double *>(red);
+  for (;;) {
+    if (crank == 0 && threadIdx.x == 0) s_inst = int(atomicAdd(B.queue, 1u));
+    cluster_barrier();
+    const int q = *cl.map_shared_rank(&s_inst, 0);
+    const int n_queue = B.n_inst_d ? *B.n_inst_d : B.n_inst;
+    if (q >= n_queue) {
+      cluster_barrier();
+      return;
+    }
+    const int inst = B.order[q];
+    const int max_iter = B.cap ? B.cap[inst] : B.max_iter;
+    const int it0 = B.inst_tile[inst];
+    const int nt = B.inst_tile[inst + 1] - it0;
+    const int c0 = it0 + int((long long)nt * crank / csize);
+    const int c1 = it0 + int((long long)nt * (crank + 1) / csize);
+    const int ntiles = c1 - c0;
+    for (int t = threadIdx.x; t < ntiles; t += C::kThreads) {
+      TileMeta tm;
+      tm.r0 = P.tile_row[c0 + t];
+      tm.r1 = P.tile_row[c0 + t + 1];
+      tm.b0 = P.rowptr[tm.r0];
+      tm.b1 = P.rowptr[tm.r1];
+      tm.w0 = P.tile_wptr[c0 + t];
+      tm.wn = P.tile_wptr[c0 + t + 1] - tm.w0;
+      tiles[t] = tm;
+    }
+    __syncthreads();
+    double n0 = 0, n1 = 0, n2 = 0;
+    for (int t = 0; t < ntiles; ++t)
+      for (int i = tiles[t].r0 + threadIdx.x; i < tiles[t].r1; i += C::kThreads) {
+        const V4<double> b = P.rhs[i];
+        n0 += b.x * b.x + b.y * b.y + b.z * b.z;
+      }
+    cluster_sum3<C, double>(cl, csize, n0, n1, n2, redd, xch, pset);
+    const double rhs2 = n0;
+    const V tol2 = A::from_d(B.tol2 * rhs2);
+    int rcur = 0, pold = 0;
+    V rz = A::zero(), rr = A::zero(), zz = A::zero();
+    gen_phase<C, T, kGenZ>(P, Gm, tiles, ntiles, rcur, pold, T(0), T(0), smem, rz, rr);
+    cluster_sum3<C, T>(cl, csize, rz, rr, zz, red, xch, pset);
+    V rmax2 = rr;
+    double last_rr64 = A::to_d(rr);
+    int it = 0, nref = 0, status = A::finite(rr) ? EOLC_NOT_CONVERGED : EOLC_NONFINITE;
+    bool converged = A::finite(rr) && A::le(rr, tol2);
+    V rz_prev = A::from_d(1.0);
+    bool restart = true;
+    while (!converged && status != EOLC_NONFINITE && it < max_iter) {
+      const V beta = restart ? A::zero() : A::div(rz, rz_prev);
+      restart = false;
+      V pq = A::zero(), d1 = A::zero(), d2 = A::zero();
+      gen_phase<C, T, kGenP>(P, Gm, tiles, ntiles, rcur, pold, T(0), T(A::to_t(beta)), smem, pq,
+                             d1);
+      cluster_sum3<C, T>(cl, csize, pq, d1, d2, red, xch, pset);
+      if (!A::pos(pq) || !A::pos(rz)) {
+        status = (A::finite(pq) && A::finite(rz)) ? EOLC_BREAKDOWN : EOLC_NONFINITE;
+        break;
+      }
+      const V alpha = A::div(rz, pq);
+      V rz2 = A::zero(), rr2 = A::zero(), d3 = A::zero();
+      gen_phase<C, T, kGenR>(P, Gm, tiles, ntiles, rcur, pold, T(A::to_t(alpha)), T(0), smem,
+                             rz2, rr2);
+      cluster_sum3<C, T>(cl, csize, rz2, rr2, d3, red, xch, pset);
+      ++it;
+      rcur ^= 1;
+      pold ^= 1;
+      rz_prev = rz;
+      rz = rz2;
+      rr = rr2;
+      if (!A::finite(rr) || !A::finite(rz)) { status = EOLC_NONFINITE; break; }
+      if (!(A::lt(rr, A::mul(delta2, rmax2)) || A::le(rr, tol2) || it >= max_iter)) continue;
+      for (int t = 0; t < ntiles; ++t)
+        for (int i = tiles[t].r0 + threadIdx.x; i < tiles[t].r1; i += C::kThreads) {
+          const V4<T> xa = P.xacc[i];
+          V4<double> x = P.x64[i];
+          x.x += double(xa.x); x.y += double(xa.y); x.z += double(xa.z);
+          P.x64[i] = x;
+          P.xacc[i] = V4<T>{T(0), T(0), T(0), T(0)};
+        }
+      if (csize > 1) cluster_barrier(); else __syncthreads();
+      double rr64d = 0, z0 = 0, z1 = 0;
+      gen_ru_residual<C>(P, tiles, ntiles, rcur, smem, rr64d);
+      cluster_sum3<C, double>(cl, csize, rr64d, z0, z1, redd, xch, pset);
+      ++nref;
+      last_rr64 = rr64d;
+      rmax2 = A::from_d(rr64d);
+      if (!isfinite(rr64d)) { status = EOLC_NONFINITE; break; }
+      if (A::le(A::from_d(rr64d), tol2)) { converged = true; break; }
+      V rz3 = A::zero(), rr3 = A::zero(), e3 = A::zero();
+      gen_phase<C, T, kGenZ>(P, Gm, tiles, ntiles, rcur, pold, T(0), T(0), smem, rz3, rr3);
+      cluster_sum3<C, T>(cl, csize, rz3, rr3, e3, red, xch, pset);
+      rz = rz3;
+    }
+    if (converged) status = EOLC_OK;
+    if (crank == 0 && threadIdx.x == 0)
+      record_instance(B, inst, status, it, nref, last_rr64, rhs2, true);
+    __syncthreads();
+  }
+}
+
+// Iteration caps of a learned batched solve: fallback_factor x each
+// instance's last Jacobi count (uncapped where there is none yet).
+__global__ void caps_kernel(int n_inst, const int *jac_iters, int factor, int max_iter, int *cap) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_inst) return;
+  const int j = jac_iters[k];
+  cap[k] = (factor > 0 && j > 0) ? min(max_iter, factor * j) : max_iter;
+}
+
+// The instances a learned launch left unconverged, in queue order (one CTA,
+// fixed order): order_out[0 .. *count), and a flag per instance.
+__global__ void collect_failed_kernel(int n_inst, const int *order, const int *last_status,
+                                      int *order_out, int *count, int *flag) {
+  __shared__ int s_base;
+  if (threadIdx.x == 0) s_base = 0;
+  __syncthreads();
+  for (int c0 = 0; c0 < n_inst; c0 += blockDim.x) {
+    const int q = c0 + threadIdx.x;
+    const int inst = q < n_inst ? order[q] : -1;
+    const int f = (inst >= 0 && last_status[inst] == EOLC_NOT_CONVERGED) ? 1 : 0;
+    if (inst >= 0) flag[inst] = f;
+    // block-wide exclusive scan of f in thread order
+    const unsigned ballot = __ballot_sync(0xffffffffu, f);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ int s_warp[32];
+    if (lane == 0) s_warp[warp] = __popc(ballot);
+    __syncthreads();
+    int before = 0;
+    for (int w = 0; w < warp; ++w) before += s_warp[w];
+    const int pos = s_base + before + __popc(ballot & ((1u << lane) - 1u));
+    if (f) order_out[pos] = inst;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int tot = 0;
+      for (int w = 0; w < int(blockDim.x) / 32; ++w) tot += s_warp[w];
+      s_base += tot;
     }
     __syncthreads();
   }
+  if (threadIdx.x == 0) *count = s_base;
+}
+
+// Set-up / finish restricted to the nodes of flagged instances.
+__global__ void setup_flagged_kernel(int n_nodes, const int *node_inst, const int *flag,
+                                     const int *rowptr, const int *colidx, const int *diag,
+                                     const float *A, const double *b, const double *beq_full,
+                                     const uint8_t *pinned, V4<double> *rhs, V4<double> *x64,
+                                     V4<float> *r, V4<float> *p, V4<float> *s, V4<float> *xacc,
+                                     float *pc, V4<float> *fmask) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_nodes || !flag[node_inst[i]]) return;
+  setup_node<float>(i, rowptr, colidx, diag, A, b, beq_full, pinned, 0, rhs, x64, r, p, s, xacc,
+                    pc, fmask);
+}
+
+__global__ void finish_flagged_kernel(int n_nodes, const int *node_inst, const int *flag,
+                                      const V4<double> *x64, const double *beq_full,
+                                      const uint8_t *pinned, double *v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_nodes || !flag[node_inst[i]]) return;
+  const V4<double> x = x64[i];
+  const double xs[3] = {x.x, x.y, x.z};
+  for (int c = 0; c < 3; ++c) v[3 * i + c] = pinned[3 * i + c] ? beq_full[3 * i + c] : xs[c];
 }
 
 // ---- configurations ---------------------------------------------------------
@@ -264,6 +470,15 @@ const void *kernel_of(int k) {
   }
 }
 
+const void *gen_kernel_of(int k) {
+  switch (k) {
+    case 0: return reinterpret_cast<const void *>(batch_gen_kernel<K0, 1>);
+    case 1: return reinterpret_cast<const void *>(batch_gen_kernel<K1, 1>);
+    case 2: return reinterpret_cast<const void *>(batch_gen_kernel<K2, 2>);
+    default: return reinterpret_cast<const void *>(batch_gen_kernel<K3, 2>);
+  }
+}
+
 }  // namespace
 
 int batch_num_configs() { return kNumShapes * kNumCluster; }
@@ -277,8 +492,11 @@ std::string batch_config_name(int config) {
 struct BatchSolveWork {
   int config = -1, prec = -1, block_pc = -1;
   int n_nodes = 0, n_blocks = 0, n_inst = 0;
-  int grid = 0;
+  int grid = 0, gen_grid = 0;
   size_t smem = 0;
+  // learned solves: per-instance caps, statuses, Jacobi references (kept
+  // across configurations of one topology), the fallback queue
+  DevBuf<int> cap, last_status, jac_iters, flag, order2, count;
   DevBuf<unsigned char> vecs, pc;
   DevBuf<int> tile_row, tile_wptr, wlist, inst_tile, order;
   DevBuf<uint16_t> lcol;
@@ -366,6 +584,24 @@ eolc_status batch_prepare(BatchSolveWork *&w, const PcgArgs &a, const std::vecto
     err = e != cudaSuccess ? cudaGetErrorString(e) : "batch kernel does not fit on the device";
     return EOLC_CUDA_ERROR;
   }
+  // the learned kernel of this shape (mixed precision only)
+  int gen_clusters = 0;
+  if (!fp64) {
+    const void *gfn = gen_kernel_of(k);
+    e = cudaFuncSetAttribute(gfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(&gen_clusters, gfn, &lc);
+    if (e != cudaSuccess || gen_clusters < 1) {
+      err = e != cudaSuccess ? cudaGetErrorString(e) : "batch kernel does not fit on the device";
+      return EOLC_CUDA_ERROR;
+    }
+  }
+  if (int(w->jac_iters.n) != std::max(n_inst, 1)) {
+    if (w->jac_iters.resize(std::max(n_inst, 1)) != cudaSuccess ||
+        cudaMemsetAsync(w->jac_iters.p, 0, sizeof(int) * w->jac_iters.n, s) != cudaSuccess) {
+      err = "device allocation failed";
+      return EOLC_CUDA_ERROR;
+    }
+  }
   lcol.resize(lcol.size() + 8, 0);
   const size_t vt = fp64 ? sizeof(V4<double>) : sizeof(V4<float>);
   cudaError_t es[] = {
@@ -379,6 +615,11 @@ eolc_status batch_prepare(BatchSolveWork *&w, const PcgArgs &a, const std::vecto
       w->pc.resize(size_t(N) * 9 * (fp64 ? sizeof(double) : sizeof(float))),
       w->queue.resize(1),
       w->rec.resize(std::max(n_inst, 1)),
+      w->cap.resize(std::max(n_inst, 1)),
+      w->last_status.resize(std::max(n_inst, 1)),
+      w->flag.resize(std::max(n_inst, 1)),
+      w->order2.resize(std::max(n_inst, 1)),
+      w->count.resize(1),
       cudaStreamSynchronize(s)};
   for (cudaError_t x : es)
     if (x != cudaSuccess) { err = cudaGetErrorString(x); return EOLC_CUDA_ERROR; }
@@ -389,6 +630,7 @@ eolc_status batch_prepare(BatchSolveWork *&w, const PcgArgs &a, const std::vecto
   w->n_blocks = Tp.n_blocks;
   w->n_inst = n_inst;
   w->grid = n_clusters * csize;
+  w->gen_grid = gen_clusters * csize;
   w->smem = smem;
   return EOLC_OK;
 }
@@ -432,12 +674,14 @@ eolc_status batch_enqueue_t(BatchSolveWork *w, const PcgArgs &a, cudaStream_t s,
   P.max_iter = a.max_iter;
   P.block_pc = w->block_pc;
   P.tol2 = a.rel_tol * a.rel_tol;
-  BatchArgs B;
+  BatchArgs B{};
   B.n_inst = w->n_inst;
   B.inst_tile = w->inst_tile.p;
   B.order = w->order.p;
   B.queue = w->queue.p;
   B.rec = w->rec.p;
+  B.last_status = w->last_status.p;
+  B.jac_iters = (w->block_pc == 0) ? w->jac_iters.p : nullptr;
   B.tol2 = a.rel_tol * a.rel_tol;
   B.max_iter = a.max_iter;
   const int k = w->config / kNumCluster, csize = kClusterSizes[w->config % kNumCluster];
@@ -465,11 +709,124 @@ eolc_status batch_enqueue_t(BatchSolveWork *w, const PcgArgs &a, cudaStream_t s,
 
 }  // namespace
 
+// One learned batched solve with the per-instance Jacobi fallback, all on the
+// device: set-up, caps, the learned launch, finish, the list of instances it
+// left at their cap, their set-up, one Jacobi launch over that list, their
+// finish.  No host synchronisation.
+eolc_status batch_enqueue_learned(BatchSolveWork *w, const PcgArgs &a, const float *Gm,
+                                  int fallback_factor, const int *node_inst, cudaStream_t s,
+                                  std::string &err, long long &launches) {
+  if (!w || w->config < 0 || w->prec != 1 || w->block_pc != 0) {
+    err = "batch solver not prepared for mixed-precision Jacobi";
+    return EOLC_BAD_ARG;
+  }
+  const DevTopology &Tp = *a.T;
+  const int N = Tp.n_nodes;
+  const float *A = a.A32;
+  unsigned char *vp = w->vecs.p;
+  V4<double> *rhs = reinterpret_cast<V4<double> *>(vp); vp += sizeof(V4<double>) * N;
+  V4<double> *x64 = reinterpret_cast<V4<double> *>(vp); vp += sizeof(V4<double>) * N;
+  V4<float> *vr = reinterpret_cast<V4<float> *>(vp);
+  Params<float> P{};
+  P.r[0] = vr; P.r[1] = vr + N;
+  P.w[0] = vr + 2 * N; P.w[1] = vr + 3 * N;  // learned: z, q
+  P.s[0] = vr + 4 * N; P.s[1] = vr + 5 * N;  // learned: p ping-pong
+  P.p = vr + 6 * N;
+  P.xacc = vr + 7 * N;
+  V4<float> *fmask = vr + 8 * N;
+  float *pc = reinterpret_cast<float *>(w->pc.p);
+  const int nn = (N + 127) / 128;
+  setup_kernel<float><<<nn, 128, 0, s>>>(N, Tp.rowptr.p, Tp.colidx.p, Tp.diag.p, A, a.b,
+                                         a.beq_full, a.pinned, 0, rhs, x64, P.r[0], P.p, P.s[0],
+                                         P.xacc, pc, fmask);
+  caps_kernel<<<(w->n_inst + 127) / 128, 128, 0, s>>>(w->n_inst, w->jac_iters.p, fallback_factor,
+                                                      a.max_iter, w->cap.p);
+  cudaMemsetAsync(w->queue.p, 0, sizeof(unsigned), s);
+  P.n_nodes = N;
+  P.rowptr = Tp.rowptr.p;
+  P.A = A;
+  P.lcol = w->lcol.p;
+  P.tile_row = w->tile_row.p;
+  P.tile_wptr = w->tile_wptr.p;
+  P.wlist = w->wlist.p;
+  P.rhs = rhs;
+  P.x64 = x64;
+  P.pc = pc;
+  P.fmask = fmask;
+  P.max_iter = a.max_iter;
+  P.block_pc = 0;
+  P.tol2 = a.rel_tol * a.rel_tol;
+  BatchArgs B{};
+  B.n_inst = w->n_inst;
+  B.inst_tile = w->inst_tile.p;
+  B.order = w->order.p;
+  B.queue = w->queue.p;
+  B.rec = w->rec.p;
+  B.cap = w->cap.p;
+  B.last_status = w->last_status.p;
+  B.tol2 = a.rel_tol * a.rel_tol;
+  B.max_iter = a.max_iter;
+  const int k = w->config / kNumCluster, csize = kClusterSizes[w->config % kNumCluster];
+  cudaLaunchConfig_t lc = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = csize;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  lc.gridDim = dim3(w->gen_grid);
+  lc.blockDim = dim3(shape(k).threads);
+  lc.dynamicSmemBytes = w->smem;
+  lc.stream = s;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  {
+    void *args[] = {&P, &B, &Gm};
+    cudaError_t e = cudaLaunchKernelExC(&lc, gen_kernel_of(k), args);
+    if (e != cudaSuccess) { err = cudaGetErrorString(e); return EOLC_CUDA_ERROR; }
+  }
+  finish_kernel<<<nn, 128, 0, s>>>(N, x64, a.beq_full, a.pinned, a.v);
+  // Jacobi re-solve of the instances the learned launch left at their cap
+  collect_failed_kernel<<<1, 1024, 0, s>>>(w->n_inst, w->order.p, w->last_status.p, w->order2.p,
+                                           w->count.p, w->flag.p);
+  setup_flagged_kernel<<<nn, 128, 0, s>>>(N, node_inst, w->flag.p, Tp.rowptr.p, Tp.colidx.p,
+                                          Tp.diag.p, A, a.b, a.beq_full, a.pinned, rhs, x64,
+                                          P.r[0], P.p, P.s[0], P.xacc, pc, fmask);
+  cudaMemsetAsync(w->queue.p, 0, sizeof(unsigned), s);
+  BatchArgs J = B;
+  J.n_inst_d = w->count.p;
+  J.order = w->order2.p;
+  J.cap = nullptr;
+  J.jac_iters = w->jac_iters.p;
+  J.fallback = 1;
+  lc.gridDim = dim3(w->grid);
+  {
+    void *args[] = {&P, &J};
+    cudaError_t e = cudaLaunchKernelExC(&lc, kernel_of<float>(k), args);
+    if (e != cudaSuccess) { err = cudaGetErrorString(e); return EOLC_CUDA_ERROR; }
+  }
+  finish_flagged_kernel<<<nn, 128, 0, s>>>(N, node_inst, w->flag.p, x64, a.beq_full, a.pinned,
+                                           a.v);
+  launches += 8;  // setup, caps, learned, finish, collect, setup, Jacobi, finish
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) { err = cudaGetErrorString(e); return EOLC_CUDA_ERROR; }
+  return EOLC_OK;
+}
+
 eolc_status batch_enqueue(BatchSolveWork *w, const PcgArgs &a, cudaStream_t s, std::string &err,
                           long long &launches) {
   if (!w || w->config < 0) { err = "batch solver not prepared"; return EOLC_BAD_ARG; }
   if (a.precision == EOLC_PREC_FP64) return batch_enqueue_t<double>(w, a, s, err, launches);
   return batch_enqueue_t<float>(w, a, s, err, launches);
+}
+
+eolc_status batch_set_jacobi_reference(BatchSolveWork *w, const int *iters_h, int n,
+                                       cudaStream_t s) {
+  if (!w || int(w->jac_iters.n) < n) return EOLC_BAD_ARG;
+  if (cudaMemcpyAsync(w->jac_iters.p, iters_h, sizeof(int) * n, cudaMemcpyHostToDevice, s) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return EOLC_CUDA_ERROR;
+  return EOLC_OK;
 }
 
 eolc_status batch_reset_records(BatchSolveWork *w, cudaStream_t s) {

@@ -374,17 +374,161 @@ __device__ __forceinline__ void ru_residual(const Params<T> &P, const TileMeta *
   }
 }
 
+// ---- tile phases of PCG with a non-local preconditioner G (pattern of A) ----
+template <class C, typename T>
+__device__ __forceinline__ void stage_matrix(const T *M, const uint16_t *lcol, const int *rowptr,
+                                             const TileMeta &tm, unsigned char *vals,
+                                             const T *&sA, const uint16_t *&sL, int *sRow) {
+  const int nb = tm.b1 - tm.b0;
+  T *dA = reinterpret_cast<T *>(vals);
+  const int offA = stage_aligned<C>(M + size_t(tm.b0) * 9, nb * 9, dA);
+  const size_t abytes = (size_t(offA + nb * 9) * sizeof(T) + 31) & ~size_t(15);
+  uint16_t *dL = reinterpret_cast<uint16_t *>(vals + abytes);
+  const int offL = stage_aligned<C>(lcol + tm.b0, nb, dL);
+  for (int k = threadIdx.x; k <= tm.r1 - tm.r0; k += C::kThreads)
+    sRow[k] = __ldg(rowptr + tm.r0 + k) - tm.b0;
+  sA = dA + offA;
+  sL = dL + offL;
+}
+
+enum GenMode { kGenZ = 0, kGenP = 1, kGenR = 2 };
+
+template <class C, typename T, int kMode>
+__device__ __forceinline__ void gen_phase(const Params<T> &P, const T *Gm, const TileMeta *tiles,
+                                          int ntiles, int rcur, int pold, T alpha, T beta,
+                                          unsigned char *smem, typename Acc<T>::V &a1,
+                                          typename Acc<T>::V &a2) {
+  using A = Acc<T>;
+  V4<T> *sU = reinterpret_cast<V4<T> *>(smem + C::kValBytes);
+  __shared__ V4<T> sOwn[C::kTileRows];
+  __shared__ int sRow[C::kTileRows + 1];
+  const int lrow = threadIdx.x / C::kRowThreads, quarter = threadIdx.x % C::kRowThreads;
+  V4<T> *z = P.w[0], *q = P.w[1];
+  V4<T> *po = P.s[pold], *pn = P.s[pold ^ 1];
+  const T *M = kMode == kGenP ? P.A : Gm;
+  for (int t = 0; t < ntiles; ++t) {
+    const TileMeta tm = tiles[t];
+    const int i = tm.r0 + lrow;
+    const bool owner = i < tm.r1 && quarter == 0;
+    V4<T> m{}, xa{}, pv{};
+    if (owner) {
+      m = P.fmask[i];
+      if (kMode == kGenR) { xa = P.xacc[i]; pv = pn[i]; }
+    }
+    const T *sA;
+    const uint16_t *sL;
+    stage_matrix<C>(M, P.lcol, P.rowptr, tm, smem, sA, sL, sRow);
+    for (int j = threadIdx.x; j < tm.wn; j += C::kThreads) {
+      const int node = __ldg(P.wlist + tm.w0 + j);
+      V4<T> u;
+      if (kMode == kGenZ) {
+        u = P.r[rcur][node];
+      } else if (kMode == kGenP) {
+        const V4<T> zj = z[node], pj = po[node];
+        u = V4<T>{zj.x + beta * pj.x, zj.y + beta * pj.y, zj.z + beta * pj.z, T(0)};
+      } else {
+        const V4<T> rj = P.r[rcur][node], qj = q[node];
+        u = V4<T>{rj.x - alpha * qj.x, rj.y - alpha * qj.y, rj.z - alpha * qj.z, T(0)};
+      }
+      if (node >= tm.r0 && node < tm.r1) sOwn[node - tm.r0] = u;
+      sU[j] = u;
+    }
+    __syncthreads();
+    T c0 = 0, c1 = 0, c2 = 0;
+    if (i < tm.r1) {
+      const int q0 = sRow[lrow], q1 = sRow[lrow + 1];
+#pragma unroll 2
+      for (int k = q0 + quarter; k < q1; k += C::kRowThreads) {
+        const V4<T> u = sU[sL[k]];
+        const T *blk = sA + size_t(k) * 9;
+        c0 += blk[0] * u.x + blk[1] * u.y + blk[2] * u.z;
+        c1 += blk[3] * u.x + blk[4] * u.y + blk[5] * u.z;
+        c2 += blk[6] * u.x + blk[7] * u.y + blk[8] * u.z;
+      }
+    }
+#pragma unroll
+    for (int o = 1; o < C::kRowThreads; o <<= 1) {
+      c0 += __shfl_xor_sync(0xffffffffu, c0, o);
+      c1 += __shfl_xor_sync(0xffffffffu, c1, o);
+      c2 += __shfl_xor_sync(0xffffffffu, c2, o);
+    }
+    if (owner) {
+      const V4<T> res{c0 * m.x, c1 * m.y, c2 * m.z, T(0)};
+      const V4<T> own = sOwn[lrow];
+      if (kMode == kGenZ) {
+        z[i] = res;
+        a1 = A::addf(a1, dot3(own, res));
+        a2 = A::addf(a2, dot3(own, own));
+      } else if (kMode == kGenP) {
+        pn[i] = own;
+        q[i] = res;
+        a1 = A::addf(a1, dot3(own, res));
+      } else {
+        P.r[rcur ^ 1][i] = own;
+        z[i] = res;
+        xa.x += alpha * pv.x; xa.y += alpha * pv.y; xa.z += alpha * pv.z;
+        P.xacc[i] = xa;
+        a1 = A::addf(a1, dot3(own, res));
+        a2 = A::addf(a2, dot3(own, own));
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Reliable update: r[rcur] = rhs - A x64 in FP64 arithmetic.
+template <class C, typename T>
+__device__ __forceinline__ void gen_ru_residual(const Params<T> &P, const TileMeta *tiles,
+                                               int ntiles, int rcur, unsigned char *smem,
+                                               double &rr64) {
+  V4<double> *sX = reinterpret_cast<V4<double> *>(smem + C::kValBytes);
+  __shared__ int sRow[C::kTileRows + 1];
+  const int lrow = threadIdx.x / C::kRowThreads, quarter = threadIdx.x % C::kRowThreads;
+  for (int t = 0; t < ntiles; ++t) {
+    const TileMeta tm = tiles[t];
+    const T *sA;
+    const uint16_t *sL;
+    stage_matrix<C>(P.A, P.lcol, P.rowptr, tm, smem, sA, sL, sRow);
+    for (int j = threadIdx.x; j < tm.wn; j += C::kThreads) sX[j] = P.x64[__ldg(P.wlist + tm.w0 + j)];
+    __syncthreads();
+    const int i = tm.r0 + lrow;
+    double a0 = 0, a1 = 0, a2 = 0;
+    if (i < tm.r1) {
+      for (int k = sRow[lrow] + quarter; k < sRow[lrow + 1]; k += C::kRowThreads) {
+        const V4<double> xj = sX[sL[k]];
+        const T *blk = sA + size_t(k) * 9;
+        a0 += double(blk[0]) * xj.x + double(blk[1]) * xj.y + double(blk[2]) * xj.z;
+        a1 += double(blk[3]) * xj.x + double(blk[4]) * xj.y + double(blk[5]) * xj.z;
+        a2 += double(blk[6]) * xj.x + double(blk[7]) * xj.y + double(blk[8]) * xj.z;
+      }
+    }
+#pragma unroll
+    for (int o = 1; o < C::kRowThreads; o <<= 1) {
+      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    if (i < tm.r1 && quarter == 0) {
+      const V4<double> b = P.rhs[i];
+      const V4<T> m = P.fmask[i];
+      const double e0 = (b.x - a0) * double(m.x), e1 = (b.y - a1) * double(m.y),
+                   e2 = (b.z - a2) * double(m.z);
+      rr64 += e0 * e0 + e1 * e1 + e2 * e2;
+      P.r[rcur][i] = V4<T>{T(e0), T(e1), T(e2), T(0)};
+    }
+    __syncthreads();
+  }
+}
+
 // rhs = mask * (-b - A beq_full) in FP64 (A promoted), the preconditioner,
 // r = rhs, x = 0, p = s = 0.
 template <typename T>
-__global__ void setup_kernel(int n_nodes, const int *rowptr, const int *colidx,
-                             const int *diag, const T *A, const double *b,
-                             const double *beq_full, const uint8_t *pinned,
-                             int block_pc, V4<double> *rhs, V4<double> *x64,
-                             V4<T> *r, V4<T> *p, V4<T> *s, V4<T> *xacc, T *pc,
-                             V4<T> *fmask) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_nodes) return;
+__device__ void setup_node(int i, const int *rowptr, const int *colidx,
+                           const int *diag, const T *A, const double *b,
+                           const double *beq_full, const uint8_t *pinned,
+                           int block_pc, V4<double> *rhs, V4<double> *x64,
+                           V4<T> *r, V4<T> *p, V4<T> *s, V4<T> *xacc, T *pc,
+                           V4<T> *fmask) {
   double a[3] = {0, 0, 0};
   for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
     int j = colidx[k];
@@ -445,6 +589,19 @@ __global__ void setup_kernel(int n_nodes, const int *rowptr, const int *colidx,
   p[i] = zero;
   s[i] = zero;
   xacc[i] = zero;
+}
+
+template <typename T>
+__global__ void setup_kernel(int n_nodes, const int *rowptr, const int *colidx,
+                             const int *diag, const T *A, const double *b,
+                             const double *beq_full, const uint8_t *pinned,
+                             int block_pc, V4<double> *rhs, V4<double> *x64,
+                             V4<T> *r, V4<T> *p, V4<T> *s, V4<T> *xacc, T *pc,
+                             V4<T> *fmask) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_nodes) return;
+  setup_node<T>(i, rowptr, colidx, diag, A, b, beq_full, pinned, block_pc, rhs, x64, r, p, s,
+                xacc, pc, fmask);
 }
 
 // ||rhs||^2 by one CTA; resets the status record.

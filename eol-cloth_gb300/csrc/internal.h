@@ -123,7 +123,7 @@ struct BatchRecord {
   int refinements;
   int max_iterations;  // largest single-launch iteration count
   int steps;           // launches that solved this instance
-  int pad;
+  int used_fallback;   // a learned solve of this instance fell back to Jacobi
   double rel_res;      // largest final relative residual
 };
 struct BatchSolveWork;
@@ -139,7 +139,16 @@ eolc_status batch_prepare(BatchSolveWork *&w, const PcgArgs &a,
 // synchronisation and no allocation, so it can be captured in a graph.
 eolc_status batch_enqueue(BatchSolveWork *w, const PcgArgs &a, cudaStream_t s,
                           std::string &err, long long &launches);
+// Learned batched solve (mixed precision, a prepared Jacobi configuration):
+// the learned launch with per-instance caps of fallback_factor x each
+// instance's last Jacobi count, then one Jacobi launch over the instances it
+// left unconverged (node_inst: instance of every node, device).
+eolc_status batch_enqueue_learned(BatchSolveWork *w, const PcgArgs &a, const float *Gm,
+                                  int fallback_factor, const int *node_inst, cudaStream_t s,
+                                  std::string &err, long long &launches);
 eolc_status batch_reset_records(BatchSolveWork *w, cudaStream_t s);
+eolc_status batch_set_jacobi_reference(BatchSolveWork *w, const int *iters_h, int n,
+                                       cudaStream_t s);
 eolc_status batch_read_records(BatchSolveWork *w, std::vector<BatchRecord> &out,
                                cudaStream_t s);
 

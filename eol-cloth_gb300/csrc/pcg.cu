@@ -185,151 +185,6 @@ cg_kernel(Params<T> P) {
 // and halo lists.  Buffers (reusing Params fields): r[2] ping-pong r,
 // w[0] = z, w[1] = q, s[0]/s[1] ping-pong p, xacc, x64.
 template <typename T>
-__device__ __forceinline__ void stage_matrix(const T *M, const uint16_t *lcol, const int *rowptr,
-                                             const TileMeta &tm, unsigned char *vals,
-                                             const T *&sA, const uint16_t *&sL, int *sRow) {
-  const int nb = tm.b1 - tm.b0;
-  T *dA = reinterpret_cast<T *>(vals);
-  const int offA = stage_aligned<C0>(M + size_t(tm.b0) * 9, nb * 9, dA);
-  const size_t abytes = (size_t(offA + nb * 9) * sizeof(T) + 31) & ~size_t(15);
-  uint16_t *dL = reinterpret_cast<uint16_t *>(vals + abytes);
-  const int offL = stage_aligned<C0>(lcol + tm.b0, nb, dL);
-  for (int k = threadIdx.x; k <= tm.r1 - tm.r0; k += kThreads)
-    sRow[k] = __ldg(rowptr + tm.r0 + k) - tm.b0;
-  sA = dA + offA;
-  sL = dL + offL;
-}
-
-enum GenMode { kGenZ = 0, kGenP = 1, kGenR = 2 };
-
-template <typename T, int kMode>
-__device__ __forceinline__ void gen_phase(const Params<T> &P, const T *Gm, const TileMeta *tiles,
-                                          int ntiles, int rcur, int pold, T alpha, T beta,
-                                          unsigned char *smem, typename Acc<T>::V &a1,
-                                          typename Acc<T>::V &a2) {
-  using A = Acc<T>;
-  V4<T> *sU = reinterpret_cast<V4<T> *>(smem + kValBytes);
-  __shared__ V4<T> sOwn[kTileRows];
-  __shared__ int sRow[kTileRows + 1];
-  const int lrow = threadIdx.x / kRowThreads, quarter = threadIdx.x % kRowThreads;
-  V4<T> *z = P.w[0], *q = P.w[1];
-  V4<T> *po = P.s[pold], *pn = P.s[pold ^ 1];
-  const T *M = kMode == kGenP ? P.A : Gm;
-  for (int t = 0; t < ntiles; ++t) {
-    const TileMeta tm = tiles[t];
-    const int i = tm.r0 + lrow;
-    const bool owner = i < tm.r1 && quarter == 0;
-    V4<T> m{}, xa{}, pv{};
-    if (owner) {
-      m = P.fmask[i];
-      if (kMode == kGenR) { xa = P.xacc[i]; pv = pn[i]; }
-    }
-    const T *sA;
-    const uint16_t *sL;
-    stage_matrix(M, P.lcol, P.rowptr, tm, smem, sA, sL, sRow);
-    for (int j = threadIdx.x; j < tm.wn; j += kThreads) {
-      const int node = __ldg(P.wlist + tm.w0 + j);
-      V4<T> u;
-      if (kMode == kGenZ) {
-        u = P.r[rcur][node];
-      } else if (kMode == kGenP) {
-        const V4<T> zj = z[node], pj = po[node];
-        u = V4<T>{zj.x + beta * pj.x, zj.y + beta * pj.y, zj.z + beta * pj.z, T(0)};
-      } else {
-        const V4<T> rj = P.r[rcur][node], qj = q[node];
-        u = V4<T>{rj.x - alpha * qj.x, rj.y - alpha * qj.y, rj.z - alpha * qj.z, T(0)};
-      }
-      if (node >= tm.r0 && node < tm.r1) sOwn[node - tm.r0] = u;
-      sU[j] = u;
-    }
-    __syncthreads();
-    T c0 = 0, c1 = 0, c2 = 0;
-    if (i < tm.r1) {
-      const int q0 = sRow[lrow], q1 = sRow[lrow + 1];
-#pragma unroll 2
-      for (int k = q0 + quarter; k < q1; k += kRowThreads) {
-        const V4<T> u = sU[sL[k]];
-        const T *blk = sA + size_t(k) * 9;
-        c0 += blk[0] * u.x + blk[1] * u.y + blk[2] * u.z;
-        c1 += blk[3] * u.x + blk[4] * u.y + blk[5] * u.z;
-        c2 += blk[6] * u.x + blk[7] * u.y + blk[8] * u.z;
-      }
-    }
-#pragma unroll
-    for (int o = 1; o < kRowThreads; o <<= 1) {
-      c0 += __shfl_xor_sync(0xffffffffu, c0, o);
-      c1 += __shfl_xor_sync(0xffffffffu, c1, o);
-      c2 += __shfl_xor_sync(0xffffffffu, c2, o);
-    }
-    if (owner) {
-      const V4<T> res{c0 * m.x, c1 * m.y, c2 * m.z, T(0)};
-      const V4<T> own = sOwn[lrow];
-      if (kMode == kGenZ) {
-        z[i] = res;
-        a1 = A::addf(a1, dot3(own, res));
-        a2 = A::addf(a2, dot3(own, own));
-      } else if (kMode == kGenP) {
-        pn[i] = own;
-        q[i] = res;
-        a1 = A::addf(a1, dot3(own, res));
-      } else {
-        P.r[rcur ^ 1][i] = own;
-        z[i] = res;
-        xa.x += alpha * pv.x; xa.y += alpha * pv.y; xa.z += alpha * pv.z;
-        P.xacc[i] = xa;
-        a1 = A::addf(a1, dot3(own, res));
-        a2 = A::addf(a2, dot3(own, own));
-      }
-    }
-    __syncthreads();
-  }
-}
-
-// Reliable update: r[rcur] = rhs - A x64 in FP64 arithmetic.
-template <typename T>
-__device__ __forceinline__ void gen_ru_residual(const Params<T> &P, const TileMeta *tiles,
-                                               int ntiles, int rcur, unsigned char *smem,
-                                               double &rr64) {
-  V4<double> *sX = reinterpret_cast<V4<double> *>(smem + kValBytes);
-  __shared__ int sRow[kTileRows + 1];
-  const int lrow = threadIdx.x / kRowThreads, quarter = threadIdx.x % kRowThreads;
-  for (int t = 0; t < ntiles; ++t) {
-    const TileMeta tm = tiles[t];
-    const T *sA;
-    const uint16_t *sL;
-    stage_matrix(P.A, P.lcol, P.rowptr, tm, smem, sA, sL, sRow);
-    for (int j = threadIdx.x; j < tm.wn; j += kThreads) sX[j] = P.x64[__ldg(P.wlist + tm.w0 + j)];
-    __syncthreads();
-    const int i = tm.r0 + lrow;
-    double a0 = 0, a1 = 0, a2 = 0;
-    if (i < tm.r1) {
-      for (int k = sRow[lrow] + quarter; k < sRow[lrow + 1]; k += kRowThreads) {
-        const V4<double> xj = sX[sL[k]];
-        const T *blk = sA + size_t(k) * 9;
-        a0 += double(blk[0]) * xj.x + double(blk[1]) * xj.y + double(blk[2]) * xj.z;
-        a1 += double(blk[3]) * xj.x + double(blk[4]) * xj.y + double(blk[5]) * xj.z;
-        a2 += double(blk[6]) * xj.x + double(blk[7]) * xj.y + double(blk[8]) * xj.z;
-      }
-    }
-#pragma unroll
-    for (int o = 1; o < kRowThreads; o <<= 1) {
-      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
-    }
-    if (i < tm.r1 && quarter == 0) {
-      const V4<double> b = P.rhs[i];
-      const V4<T> m = P.fmask[i];
-      const double e0 = (b.x - a0) * double(m.x), e1 = (b.y - a1) * double(m.y),
-                   e2 = (b.z - a2) * double(m.z);
-      rr64 += e0 * e0 + e1 * e1 + e2 * e2;
-      P.r[rcur][i] = V4<T>{T(e0), T(e1), T(e2), T(0)};
-    }
-    __syncthreads();
-  }
-}
-
-template <typename T>
 __global__ void __launch_bounds__(kThreads, 1)
 pcg_general_kernel(Params<T> P, const T *Gm) {
   using A = Acc<T>;
@@ -370,7 +225,7 @@ pcg_general_kernel(Params<T> P, const T *Gm) {
   } while (0)
   int rcur = 0, pold = 0;
   V rz = A::zero(), rr = A::zero(), zz = A::zero();
-  gen_phase<T, kGenZ>(P, Gm, tiles, ntiles, rcur, pold, T(0), T(0), smem, rz, rr);
+  gen_phase<C0, T, kGenZ>(P, Gm, tiles, ntiles, rcur, pold, T(0), T(0), smem, rz, rr);
   EOLC_SYNC3(rz, rr, zz);
   V rmax2 = rr;
   double last_rr64 = A::to_d(rr);
@@ -382,7 +237,7 @@ pcg_general_kernel(Params<T> P, const T *Gm) {
     const V beta = restart ? A::zero() : A::div(rz, rz_prev);
     restart = false;
     V pq = A::zero(), d1 = A::zero(), d2 = A::zero();
-    gen_phase<T, kGenP>(P, Gm, tiles, ntiles, rcur, pold, T(0), T(A::to_t(beta)), smem, pq, d1);
+    gen_phase<C0, T, kGenP>(P, Gm, tiles, ntiles, rcur, pold, T(0), T(A::to_t(beta)), smem, pq, d1);
     EOLC_SYNC3(pq, d1, d2);
     if (!A::pos(pq) || !A::pos(rz)) {
       status = (A::finite(pq) && A::finite(rz)) ? EOLC_BREAKDOWN : EOLC_NONFINITE;
@@ -390,7 +245,7 @@ pcg_general_kernel(Params<T> P, const T *Gm) {
     }
     const V alpha = A::div(rz, pq);
     V rz2 = A::zero(), rr2 = A::zero(), d3 = A::zero();
-    gen_phase<T, kGenR>(P, Gm, tiles, ntiles, rcur, pold, T(A::to_t(alpha)), T(0), smem, rz2, rr2);
+    gen_phase<C0, T, kGenR>(P, Gm, tiles, ntiles, rcur, pold, T(A::to_t(alpha)), T(0), smem, rz2, rr2);
     EOLC_SYNC3(rz2, rr2, d3);
     ++it;
     rcur ^= 1;
@@ -410,7 +265,7 @@ pcg_general_kernel(Params<T> P, const T *Gm) {
       }
     if (!grid_barrier(P.bar, G, epoch, P.st)) return;
     double rr64d = 0;
-    gen_ru_residual(P, tiles, ntiles, rcur, smem, rr64d);
+    gen_ru_residual<C0>(P, tiles, ntiles, rcur, smem, rr64d);
     V rr64 = A::from_d(rr64d), e1 = A::zero(), e2 = A::zero();
     EOLC_SYNC3(rr64, e1, e2);
     ++nref;
@@ -419,7 +274,7 @@ pcg_general_kernel(Params<T> P, const T *Gm) {
     if (!A::finite(rr64)) { status = EOLC_NONFINITE; break; }
     if (A::le(rr64, tol2)) { converged = true; break; }
     V rz3 = A::zero(), rr3 = A::zero(), e3 = A::zero();
-    gen_phase<T, kGenZ>(P, Gm, tiles, ntiles, rcur, pold, T(0), T(0), smem, rz3, rr3);
+    gen_phase<C0, T, kGenZ>(P, Gm, tiles, ntiles, rcur, pold, T(0), T(0), smem, rz3, rr3);
     EOLC_SYNC3(rz3, rr3, e3);
     rz = rz3;
   }

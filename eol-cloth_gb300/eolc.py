@@ -63,7 +63,7 @@ class SolveInfo(ctypes.Structure):
 class BatchInfo(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("n_failed", ctypes.c_int), ("config", ctypes.c_int),
                 ("steps", ctypes.c_int), ("iterations", ctypes.c_longlong),
-                ("max_iterations", ctypes.c_int), ("pad", ctypes.c_int),
+                ("max_iterations", ctypes.c_int), ("n_fallback", ctypes.c_int),
                 ("max_rel_res", ctypes.c_double), ("step_ms", ctypes.c_double)]
 
 
@@ -103,7 +103,8 @@ EXPORTS = ["eolc_version", "eolc_launch_count", "eolc_create", "eolc_destroy", "
            "eolc_attach_preconditioner", "eolc_set_jacobi_reference",
            "eolc_set_topology_batched", "eolc_set_instance_materials", "eolc_step_batched",
            "eolc_batch_num_configs", "eolc_batch_config_name", "eolc_batch_set_config",
-           "eolc_batch_autotune", "eolc_set_learned_refresh"]
+           "eolc_batch_autotune", "eolc_set_learned_refresh",
+           "eolc_batch_set_jacobi_reference"]
 
 
 def load_library(path=LIB_PATH):
@@ -155,6 +156,7 @@ def load_library(path=LIB_PATH):
     L.eolc_attach_preconditioner.argtypes = [_V, _V]
     L.eolc_set_jacobi_reference.argtypes = [_V, ctypes.c_int]
     L.eolc_set_learned_refresh.argtypes = [_V, ctypes.c_int]
+    L.eolc_batch_set_jacobi_reference.argtypes = [_V, _I, ctypes.c_int]
     L.eolc_set_topology_batched.argtypes = [_V, ctypes.c_int, _I, _I, _I, _I, _I]
     L.eolc_set_instance_materials.argtypes = [_V, ctypes.POINTER(Material), ctypes.c_int]
     L.eolc_step_batched.argtypes = [_V, ctypes.c_int, _D, ctypes.c_double, _I, _D, ctypes.c_int,
@@ -356,6 +358,10 @@ class Context:
 
     def set_learned_refresh(self, solves):
         self._check(lib.eolc_set_learned_refresh(self._h, solves))
+
+    def batch_set_jacobi_reference(self, iters):
+        iters = _i32(iters)
+        self._check(lib.eolc_batch_set_jacobi_reference(self._h, _i(iters), len(iters)))
 
     def batch_set_config(self, config):
         self._check(lib.eolc_batch_set_config(self._h, config))

@@ -12,11 +12,15 @@ a sparse approximate inverse (all modes weighted alike, which is what the
 conjugate-gradient iteration count depends on); probes="smooth": the step's
 velocity and two seeded smooth random fields.
 
-Training: eolc_lpc_train (Adam on the GPU, the library's own forward and
-backward kernels).  Usage:
+meshes="mixed" (generate_mixed): the systems come from one batched context
+holding a 48x48 grid and six irregular Delaunay sheets, so the network also
+sees remeshed-like stencils.
 
-    python eol-cloth_gb300/train_lpc.py --systems 2000 --epochs 20 --lr 3e-3 --probes white \
-        --out eol-cloth_gb300/weights/lpc.npy
+Training: eolc_lpc_train (Adam on the GPU, the library's own forward and
+backward kernels).  The committed weights come from:
+
+    python eol-cloth_gb300/train_lpc.py --systems 1000 --epochs 20 --lr 3e-3 --probes white \
+        --meshes mixed --seed 1 --out eol-cloth_gb300/weights/lpc.npy
 """
 import argparse
 import os
@@ -142,19 +146,83 @@ def generate(lpc, n_systems, quads=64, steps_per_run=50, seed=1, device=0, ctx=N
     return ctx
 
 
+def generate_mixed(lpc, n_systems, seed=1, steps_per_run=40, device=0, n_delaunay=6,
+                   quads=48, probes="white"):
+    """Training systems on one batched topology that holds a quads x quads
+    grid sheet and n_delaunay irregular Delaunay sheets of 1,500-6,000
+    triangles (density gradient along x), so the network sees regular and
+    remeshed-like stencils.  Per run: random pins per instance (a non-empty
+    subset of the corners plus a few boundary nodes), random wind, E ~ U(20,
+    100) and a density giving h^2 K / M of 64^2..256^2 sheets; every batched
+    Jacobi step adds the whole batch's MDK as one system."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import scenes  # mesh generators shared with the tests
+    rng = np.random.default_rng(seed)
+    sheets = []
+    x0, X, tri, hinge, corners = grid_sheet(quads)
+    sheets.append(dict(x=x0, X=X, tri=tri, hinge=hinge, n=len(x0) // 3,
+                       corners=[corners[c] for c in (1, 2, 3, 4)]))
+    for k in range(n_delaunay):
+        d = scenes.delaunay_sheet(int(rng.integers(1500, 6001)), rng)
+        Xd = d["X"].reshape(-1, 2)
+        cs = [int(np.argmin((Xd[:, 0] - cx) ** 2 + (Xd[:, 1] - cy) ** 2))
+              for cx, cy in ((0, 0), (0, 1), (1, 1), (1, 0))]
+        sheets.append(dict(x=d["x"], X=d["X"], tri=d["tri"], hinge=d["hinge"], n=d["n"],
+                           corners=cs))
+    ctx = eolc.Context(device)
+    off = ctx.set_topology_batched([(s["n"], s["tri"], s["hinge"]) for s in sheets])
+    xall = np.concatenate([s["x"] for s in sheets])
+    Xall = np.concatenate([s["X"] for s in sheets])
+    made, runs = 0, 0
+    while made < n_systems:
+        runs += 1
+        if runs > 50 * max(1, n_systems // steps_per_run + 1):
+            raise RuntimeError("the simulator keeps failing; no training systems")
+        mats, fixed = [], []
+        for k, s in enumerate(sheets):
+            n_eff = rng.uniform(64, 256)
+            side = np.sqrt(s["n"])
+            mats.append(eolc.Material(density=0.1 * (side / n_eff) ** 2, e=rng.uniform(20, 100),
+                                      nu=0.3, beta=1e-5, damping=(0.0, 1.0)))
+            pins = list(rng.choice(s["corners"], size=rng.integers(1, 5), replace=False))
+            fixed += [3 * (off[k] + p) + c for p in pins for c in range(3)]
+        ctx.set_instance_materials(mats)
+        fixed = np.array(sorted(set(fixed)), np.int32)
+        wind = np.array([rng.normal(0, 3.0), rng.normal(0, 3.0), 0.0])
+        ctx.state_upload(xall, Xall, np.zeros_like(xall))
+        opts = eolc.SolveOpts(precision=eolc.PREC_MIXED, precond=eolc.PC_JACOBI)
+        for step in range(steps_per_run):
+            try:
+                ctx.step_batched(1, GRAV + wind, H, fixed, np.zeros(len(fixed)), opts)
+            except eolc.EolcError:
+                break  # an indefinite MDK ends this run; its systems so far are kept
+            _, v = ctx.state_download()
+            lpc.add_system(ctx, fixed, make_probes(rng, Xall, v, probes))
+            made += 1
+            if made >= n_systems:
+                break
+    return ctx
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--systems", type=int, default=2000)
+    ap.add_argument("--systems", type=int, default=1000)
     ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--lr", type=float, default=3e-3)
     ap.add_argument("--quads", type=int, default=64)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--probes", default="white", choices=["white", "smooth"])
+    ap.add_argument("--meshes", default="mixed", choices=["grid", "mixed"],
+                    help="grid: one quads x quads sheet; mixed: a batch of a grid and "
+                         "irregular Delaunay sheets")
     ap.add_argument("--out", default=os.path.join(HERE, "weights", "lpc.npy"))
     args = ap.parse_args()
     lpc = eolc.LearnedPC(0, seed=args.seed)
     t0 = time.time()
-    generate(lpc, args.systems, quads=args.quads, seed=args.seed, probes=args.probes)
+    if args.meshes == "mixed":
+        generate_mixed(lpc, args.systems, seed=args.seed, probes=args.probes)
+    else:
+        generate(lpc, args.systems, quads=args.quads, seed=args.seed, probes=args.probes)
     t1 = time.time()
     losses = lpc.train(args.epochs, lr=args.lr, seed=args.seed)
     t2 = time.time()

@@ -207,7 +207,7 @@ typedef struct {
   int steps;
   long long iterations; /* PCG iterations summed over instances and steps  */
   int max_iterations;   /* largest iteration count of one instance solve   */
-  int pad;
+  int n_fallback;       /* instances whose learned solve fell back to Jacobi */
   double max_rel_res;   /* largest final FP64 relative residual            */
   double step_ms;       /* device time of the n_steps steps (CUDA events)  */
 } eolc_batch_info;
@@ -217,8 +217,13 @@ typedef struct {
  * whenever h, gravity, the options, the pins or the configuration change):
  * pins, assembly with per-instance materials, ONE persistent launch of the
  * batched PCG (instances pulled from a work queue, largest first, one CTA
- * cluster each), x += h v.  Preconditioner: EOLC_PC_JACOBI or
- * EOLC_PC_BLOCK_JACOBI.  inst_info_h (optional, n_inst entries): per-instance
+ * cluster each), x += h v.  Preconditioner: EOLC_PC_JACOBI,
+ * EOLC_PC_BLOCK_JACOBI or EOLC_PC_LEARNED (mixed precision, a network attached):
+ * the network's forward pass on the whole batch, one learned batched launch
+ * in which each instance stops at fallback_factor x its last Jacobi iteration
+ * count (uncapped until it has one), and one Jacobi launch over the
+ * instances it left unconverged (a step per call is then not a single graph:
+ * the forward pass synchronises).  inst_info_h (optional, n_inst entries): per-instance
  * status, iterations and refinements summed over the steps and the largest
  * relative residual.  Returns the first non-OK instance status; the other
  * instances' states are advanced regardless.  The first call on a topology
@@ -233,6 +238,11 @@ eolc_status eolc_step_batched(eolc_ctx *ctx, int n_steps, const double grav[3],
  * tile rows, CTAs per SM) x cluster size. */
 int eolc_batch_num_configs(void);
 const char *eolc_batch_config_name(int config);
+/* Per-instance Jacobi iteration counts the learned batched solve's caps refer
+ * to (set automatically by every converged batched Jacobi solve of an
+ * instance); needs a prepared batch (one batched step or autotune). */
+eolc_status eolc_batch_set_jacobi_reference(eolc_ctx *ctx, const int *iters_h,
+                                            int n_inst);
 /* Force a configuration (-1: autotune on the next batched step). */
 eolc_status eolc_batch_set_config(eolc_ctx *ctx, int config);
 /* Times every configuration on the current state (assembled once; the state

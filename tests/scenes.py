@@ -87,3 +87,66 @@ def batch(n_sheets, lo=16, hi=96, seed=3, e_range=(20.0, 100.0), pins=(3, 4)):
     fixed = np.concatenate([s["fixed"] + 3 * o for s, o in zip(sheets, off[:-1])]).astype(np.int32)
     return dict(sheets=sheets, mats=mats, sides=sides, node_off=np.array(off), x=x, X=X,
                 v=np.zeros_like(x), fixed=fixed, fixed_vel=np.zeros(len(fixed)))
+
+
+def delaunay_sheet(n_tri, rng, gradient=3.0):
+    """Irregular unit sheet of about n_tri triangles, mimicking a remeshed
+    sheet refined toward one side: the seeded Delaunay triangulation of a
+    jittered lattice (each point moved by up to 0.35 of a cell) whose x
+    coordinate is warped so that the point density grows linearly along x
+    (density 1 + gradient x), boundary points on the square's edges.
+    Triangles counter-clockwise in material space, hinges in ArcSim edge
+    order, the two top corners (0, 1), (1, 1) pinned."""
+    from scipy.spatial import Delaunay
+    m = max(2, int(round(np.sqrt(max(8, n_tri // 2)))))
+    g = gradient
+
+    def warp(u):  # inverse CDF of the density (1 + g x) / (1 + g / 2) on [0, 1]
+        return (-1 + np.sqrt(1 + 2 * g * u * (1 + g / 2))) / g if g > 0 else u
+
+    t = np.arange(m + 1) / m
+    bnd = np.concatenate([np.stack([warp(t), np.zeros(m + 1)], 1),
+                          np.stack([warp(t), np.ones(m + 1)], 1),
+                          np.stack([np.zeros(m - 1), t[1:-1]], 1),
+                          np.stack([np.ones(m - 1), t[1:-1]], 1)])
+    ii, jj = np.meshgrid(np.arange(1, m), np.arange(1, m), indexing="ij")
+    u = (ii + rng.uniform(-0.35, 0.35, ii.shape)) / m
+    v = (jj + rng.uniform(-0.35, 0.35, jj.shape)) / m
+    inner = np.stack([warp(u.ravel()), v.ravel()], 1)
+    pts = np.concatenate([bnd, inner])
+    tri = Delaunay(pts).simplices.astype(np.int64)
+    a, b, c = pts[tri[:, 0]], pts[tri[:, 1]], pts[tri[:, 2]]
+    area = 0.5 * ((b[:, 0] - a[:, 0]) * (c[:, 1] - a[:, 1]) - (b[:, 1] - a[:, 1]) * (c[:, 0] - a[:, 0]))
+    flip = area < 0
+    tri[flip] = tri[flip][:, [0, 2, 1]]
+    tri = tri[np.abs(area) > 1e-12]
+    used = np.unique(tri)
+    remap = -np.ones(len(pts), np.int64)
+    remap[used] = np.arange(len(used))
+    tri = remap[tri].astype(np.int32)
+    X = pts[used]
+    n = len(X)
+    x = np.concatenate([X, np.zeros((n, 1))], 1).ravel()
+    hinge = O.hinges(n, tri)
+    corners = [int(np.argmin((X[:, 0] - cx) ** 2 + (X[:, 1] - 1.0) ** 2)) for cx in (0.0, 1.0)]
+    fixed = np.array([3 * k + c for k in corners for c in range(3)], np.int32)
+    return dict(x=x, X=X.ravel(), tri=tri, hinge=hinge, fixed=fixed, fixed_vel=np.zeros(len(fixed)),
+                n=n)
+
+
+def delaunay_batch(n_meshes, tri_lo=5000, tri_hi=50000, seed=5):
+    """Batched irregular workload: n_meshes Delaunay sheets of U(tri_lo,
+    tri_hi) triangles (seeded), configuration-1 material, top corners pinned;
+    the same layout as batch()."""
+    rng = np.random.default_rng(seed)
+    sheets, mats, off = [], [], [0]
+    for k in range(n_meshes):
+        s = delaunay_sheet(int(rng.integers(tri_lo, tri_hi + 1)), rng)
+        sheets.append(s)
+        mats.append(material_c1())
+        off.append(off[-1] + s["n"])
+    x = np.concatenate([s["x"] for s in sheets])
+    X = np.concatenate([s["X"] for s in sheets])
+    fixed = np.concatenate([s["fixed"] + 3 * o for s, o in zip(sheets, off[:-1])]).astype(np.int32)
+    return dict(sheets=sheets, mats=mats, node_off=np.array(off), x=x, X=X,
+                v=np.zeros_like(x), fixed=fixed, fixed_vel=np.zeros(len(fixed)))

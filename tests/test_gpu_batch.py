@@ -176,3 +176,60 @@ def test_batch_argument_errors(eolc):
     with pytest.raises(eolc.EolcError) as e:
         ctx.set_topology_batched([(s0["n"], s0["tri"], s0["hinge"]), (s1["n"], bad, s1["hinge"])])
     assert e.value.status == eolc.BAD_ARG
+
+
+WEIGHTS = __import__("os").path.join(__import__("os").path.dirname(__import__("os").path.dirname(
+    __import__("os").path.abspath(__file__))), "eol-cloth_gb300", "weights", "lpc.npy")
+
+
+def _learned_batch(eolc, B, seed=0, trained=True):
+    ctx = _batch_ctx(eolc, B)
+    lpc = eolc.LearnedPC(0, seed=seed)
+    if trained:
+        lpc.set_params(np.load(WEIGHTS))
+    lpc.attach(ctx)
+    return ctx, lpc
+
+
+def test_batched_learned_steps_on_delaunay_meshes(eolc):
+    """Irregular meshes, learned batched solve: every instance reaches the
+    FP64 residual and the velocities of a one-sheet Jacobi step."""
+    B = scenes.delaunay_batch(5, tri_lo=600, tri_hi=3000, seed=2)
+    ctx, lpc = _learned_batch(eolc, B)
+    x = B["x"].copy()
+    ctx.state_upload(x, B["X"], B["v"])
+    # one Jacobi step sets every instance's reference count
+    tot, _ = ctx.step_batched(1, scenes.GRAV, scenes.H, B["fixed"], B["fixed_vel"],
+                              eolc.SolveOpts())
+    assert tot.status == eolc.OK
+    x1, v1 = ctx.state_download()
+    opts = eolc.SolveOpts(precond=eolc.PC_LEARNED, fallback_factor=2)
+    tot, infos = ctx.step_batched(1, scenes.GRAV, scenes.H, B["fixed"], B["fixed_vel"], opts)
+    assert tot.status == eolc.OK and tot.max_rel_res <= 1e-8
+    assert tot.n_fallback == 0, [i.iterations for i in infos]
+    _, vb = ctx.state_download()
+    _, vs, sinfo = _single_steps(eolc, B, x1, v1, eolc.SolveOpts())
+    _compare(B, vb, vs, 1e-5)
+    print("learned iterations %s, Jacobi %s" % ([i.iterations for i in infos],
+                                                 [i.iterations for i in sinfo]))
+    assert sum(i.iterations for i in infos) < sum(i.iterations for i in sinfo)
+
+
+def test_batched_learned_falls_back_per_instance(eolc):
+    """References of 1 iteration cap every learned solve at 2: each instance
+    falls back to Jacobi inside the same step and still converges."""
+    B = scenes.delaunay_batch(4, tri_lo=600, tri_hi=2000, seed=3)
+    ctx, lpc = _learned_batch(eolc, B, trained=False)
+    ctx.state_upload(B["x"], B["X"], B["v"])
+    ctx.step_batched(1, scenes.GRAV, scenes.H, B["fixed"], B["fixed_vel"], eolc.SolveOpts())
+    x1, v1 = ctx.state_download()
+    refs = np.ones(len(B["sheets"]), np.int32)
+    refs[0] = 100000  # instance 0 is not capped
+    ctx.batch_set_jacobi_reference(refs)
+    opts = eolc.SolveOpts(precond=eolc.PC_LEARNED, fallback_factor=2)
+    tot, infos = ctx.step_batched(1, scenes.GRAV, scenes.H, B["fixed"], B["fixed_vel"], opts)
+    assert tot.status == eolc.OK and tot.max_rel_res <= 1e-8
+    assert [i.used_fallback for i in infos] == [0] + [1] * (len(infos) - 1)
+    _, vb = ctx.state_download()
+    _, vs, _ = _single_steps(eolc, B, x1, v1, eolc.SolveOpts())
+    _compare(B, vb, vs, 1e-5)

@@ -186,6 +186,67 @@ def run_batched(args, local_rank, stream, flush):
     }
 
 
+def run_delaunay(args, local_rank, stream, flush):
+    """Irregular batched workload: 64 Delaunay sheets of U(5k, 50k) triangles
+    (seeded; density gradient along x, mimicking remeshed output), top
+    corners pinned.  Jacobi-PCG and learned-PCG (per-instance Jacobi fallback
+    at 2x the instance's last Jacobi count) each time K batched steps from
+    the same state after W Jacobi warm-up steps."""
+    import numpy as np
+    import torch
+    import eolc
+    import scenes
+    t0 = time.perf_counter()
+    B = scenes.delaunay_batch(args.delaunay_meshes, tri_lo=5000, tri_hi=50000, seed=5)
+    ctx = eolc.Context(local_rank)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_topology_batched([(s["n"], s["tri"], s["hinge"]) for s in B["sheets"]])
+    ctx.set_instance_materials([eolc.Material(**m) for m in B["mats"]])
+    lpc = eolc.LearnedPC(local_rank)
+    lpc.set_params(np.load(os.path.join(ROOT, "eol-cloth_gb300", "weights", "lpc.npy")))
+    lpc.attach(ctx)
+    ctx.state_upload(B["x"], B["X"], B["v"])
+    setup_s = time.perf_counter() - t0
+    jac = eolc.SolveOpts(rel_tol=1e-8, precision=eolc.PREC_MIXED, precond=eolc.PC_JACOBI)
+    lrn = eolc.SolveOpts(rel_tol=1e-8, precision=eolc.PREC_MIXED, precond=eolc.PC_LEARNED,
+                         fallback_factor=2)
+    chosen, _ = ctx.batch_autotune(GRAV, H, B["fixed"], B["fixed_vel"], jac)
+    ctx.step_batched(args.warmup, GRAV, H, B["fixed"], B["fixed_vel"], jac)
+    x_w, v_w = ctx.state_download()
+    out = {}
+    for name, opts in (("jacobi", jac), ("learned", lrn)):
+        ctx.state_upload(x_w, B["X"], v_w)
+        ctx.step_batched(1, GRAV, H, B["fixed"], B["fixed_vel"], jac)  # per-instance references
+        ctx.state_upload(x_w, B["X"], v_w)
+        step_ms, iters, fb, worst = [], 0, 0, 0.0
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            tot, _ = ctx.step_batched(1, GRAV, H, B["fixed"], B["fixed_vel"], opts)
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+            iters += tot.iterations
+            fb += tot.n_fallback
+            worst = max(worst, tot.max_rel_res)
+        total = sum(step_ms)
+        out[name] = {"sheet_steps_per_s": len(B["sheets"]) * args.steps / (total / 1e3),
+                     "ms_per_batch_step": total / args.steps,
+                     "mean_pcg_iters_per_sheet": iters / (args.steps * len(B["sheets"])),
+                     "fallbacks": fb, "max_rel_res": worst}
+    n_tri = sum(len(s["tri"]) for s in B["sheets"])
+    return {"workload": "%d Delaunay sheets, U(5k, 50k) triangles (seed 5), %d triangles and %d "
+                        "nodes in total, top corners pinned" % (len(B["sheets"]), n_tri,
+                                                                 int(B["node_off"][-1])),
+            "arms": out, "learned_vs_jacobi": out["learned"]["sheet_steps_per_s"] /
+            out["jacobi"]["sheet_steps_per_s"],
+            "autotuned_config": eolc.batch_config_name(chosen), "host_setup_s": setup_s,
+            "l2": "flushed (256 MiB write) before each step"}
+
+
 def run_reference(args, rank):
     import numpy as np
     if rank != 0:
@@ -413,6 +474,7 @@ def run_ours(args, rank, world, local_rank):
         line["cpu_baseline"] = cpu
     if world == 1 and not args.no_batch:
         line["batched"] = run_batched(args, local_rank, stream, flush)
+        line["batched_delaunay_learned"] = run_delaunay(args, local_rank, stream, flush)
     print(json.dumps(line), flush=True)
 
 
@@ -429,6 +491,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-sheets line")
     ap.add_argument("--batch-sheets", type=int, default=256)
+    ap.add_argument("--delaunay-meshes", type=int, default=64)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

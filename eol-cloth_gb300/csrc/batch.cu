@@ -448,8 +448,8 @@ ShapeInfo shape_info(const char *name) {
 }
 
 constexpr int kNumShapes = 4;
-constexpr int kClusterSizes[] = {1, 2, 4};
-constexpr int kNumCluster = 3;
+constexpr int kClusterSizes[] = {1, 2, 4, 8};  // 8: the portable maximum
+constexpr int kNumCluster = 4;
 
 const ShapeInfo &shape(int k) {
   static const ShapeInfo s[kNumShapes] = {

@@ -166,7 +166,7 @@ eolc_status solve_device(eolc_ctx *ctx, const eolc_solve_opts *o,
     if (!reuse) {
       std::string msg = learned_forward(ctx->lpc, ctx, ctx->pinned.p, &Gm, s);
       if (!msg.empty()) return fail(ctx, EOLC_CUDA_ERROR, msg.c_str());
-      ctx->launches += 20;  // network forward kernels
+      ctx->launches += 8;  // network forward kernels
       ctx->lpc_cached = resident ? ctx->lpc : nullptr;
       ctx->lpc_uses = 0;
     }
@@ -397,7 +397,7 @@ eolc_status step_batched_learned(eolc_ctx *ctx, int n_steps, const double grav[3
     const float *Gm = nullptr;
     std::string msg = learned_forward(ctx->lpc, ctx, ctx->pinned.p, &Gm, s);
     if (!msg.empty()) return fail(ctx, EOLC_CUDA_ERROR, msg.c_str());
-    ctx->launches += 20;
+    ctx->launches += 8;  // network forward kernels
     PcgArgs a = batch_pcg_args(ctx, opts, ctx->v.p);
     if ((st = batch_enqueue_learned(ctx->bwork, a, Gm, opts->fallback_factor, ctx->node_inst.p, s,
                                     ctx->err, ctx->launches)) != EOLC_OK)

@@ -332,6 +332,102 @@ __global__ void edge_concat_bwd_kernel(int n, const int *inc_ptr, const int *inc
   dh[size_t(i) * kH + c] += acc;
 }
 
+// ---- inference forward, fused ------------------------------------------------
+// One message-passing layer per launch, without the per-edge gate matrix:
+// a CTA takes kLayerNodes nodes; each warp aggregates its nodes (lane c
+// handles channels c and c + 32) with the gate g_e = sigmoid(x_e Wg + bg)
+// evaluated on the fly, then the CTA applies the 128 -> 64 layer to
+// [h, agg] from shared memory.  Every sum runs in the order of the training
+// kernels (dense_fwd_kernel, aggregate_fwd_kernel), so the activations are
+// the same numbers.
+constexpr int kLayerNodes = 32;
+constexpr int kLayerThreads = 256;
+
+__global__ void __launch_bounds__(kLayerThreads)
+layer_fused_kernel(int n, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
+                   const int *__restrict__ ei, const int *__restrict__ ej,
+                   const float *__restrict__ deg_inv, const float *__restrict__ fE,
+                   const float *__restrict__ Wg, const float *__restrict__ Wl,
+                   const float *__restrict__ h_in, float *__restrict__ h_out) {
+  __shared__ float sWl[2 * kH * kH + kH];  // W then b, BF16-rounded W
+  __shared__ float sWg[kFE * kH + kH];
+  __shared__ float sCat[kLayerNodes][2 * kH];
+  for (int k = threadIdx.x; k < 2 * kH * kH; k += kLayerThreads) sWl[k] = bf16r(Wl[k]);
+  for (int k = threadIdx.x; k < kH; k += kLayerThreads) sWl[2 * kH * kH + k] = Wl[2 * kH * kH + k];
+  for (int k = threadIdx.x; k < kFE * kH; k += kLayerThreads) sWg[k] = bf16r(Wg[k]);
+  for (int k = threadIdx.x; k < kH; k += kLayerThreads) sWg[kFE * kH + k] = Wg[kFE * kH + k];
+  __syncthreads();
+  const int node0 = blockIdx.x * kLayerNodes;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int ln = warp; ln < kLayerNodes; ln += kLayerThreads / 32) {
+    const int i = node0 + ln;
+    float a0 = 0.f, a1 = 0.f;
+    if (i < n) {
+      for (int q = inc_ptr[i]; q < inc_ptr[i + 1]; ++q) {
+        const int e = inc[q] >> 1, side = inc[q] & 1;
+        const int o = side ? ei[e] : ej[e];
+        const float *x = fE + size_t(e) * kFE;
+        float g0 = sWg[kFE * kH + lane], g1 = sWg[kFE * kH + lane + 32];
+        for (int k = 0; k < kFE; ++k) {
+          const float xk = __ldg(x + k);
+          g0 += xk * sWg[k * kH + lane];
+          g1 += xk * sWg[k * kH + lane + 32];
+        }
+        a0 += sigm(g0) * __ldg(h_in + size_t(o) * kH + lane);
+        a1 += sigm(g1) * __ldg(h_in + size_t(o) * kH + lane + 32);
+      }
+      sCat[ln][lane] = __ldg(h_in + size_t(i) * kH + lane);
+      sCat[ln][lane + 32] = __ldg(h_in + size_t(i) * kH + lane + 32);
+      sCat[ln][kH + lane] = a0 * deg_inv[i];
+      sCat[ln][kH + lane + 32] = a1 * deg_inv[i];
+    }
+  }
+  __syncthreads();
+  const int c = threadIdx.x % kH, g = threadIdx.x / kH;  // 4 node groups
+  for (int ln = g; ln < kLayerNodes; ln += kLayerThreads / kH) {
+    const int i = node0 + ln;
+    if (i >= n) break;
+    float acc = sWl[2 * kH * kH + c];
+    for (int k = 0; k < 2 * kH; ++k) acc += sCat[ln][k] * sWl[k * kH + c];
+    h_out[size_t(i) * kH + c] = fmaxf(acc, 0.f);
+  }
+}
+
+// Edge head o_e = [h3_i, h3_j, x_e] Wo + bo (18 outputs), one thread per edge,
+// summed in the order of the training kernel.
+__global__ void __launch_bounds__(128)
+edge_out_kernel(int m, const int *__restrict__ ei, const int *__restrict__ ej,
+                const float *__restrict__ h, const float *__restrict__ fE,
+                const float *__restrict__ Wo, float *__restrict__ o) {
+  __shared__ float sW[kEdgeIn * kOE + kOE];
+  for (int k = threadIdx.x; k < kEdgeIn * kOE; k += blockDim.x) sW[k] = bf16r(Wo[k]);
+  for (int k = threadIdx.x; k < kOE; k += blockDim.x) sW[kEdgeIn * kOE + k] = Wo[kEdgeIn * kOE + k];
+  __syncthreads();
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m) return;
+  float acc[kOE];
+#pragma unroll
+  for (int c = 0; c < kOE; ++c) acc[c] = sW[kEdgeIn * kOE + c];
+  const float *hi = h + size_t(ei[e]) * kH, *hj = h + size_t(ej[e]) * kH;
+  for (int k = 0; k < kH; ++k) {
+    const float x = __ldg(hi + k);
+#pragma unroll
+    for (int c = 0; c < kOE; ++c) acc[c] += x * sW[k * kOE + c];
+  }
+  for (int k = 0; k < kH; ++k) {
+    const float x = __ldg(hj + k);
+#pragma unroll
+    for (int c = 0; c < kOE; ++c) acc[c] += x * sW[(kH + k) * kOE + c];
+  }
+  for (int k = 0; k < kFE; ++k) {
+    const float x = __ldg(fE + size_t(e) * kFE + k);
+#pragma unroll
+    for (int c = 0; c < kOE; ++c) acc[c] += x * sW[(2 * kH + k) * kOE + c];
+  }
+#pragma unroll
+  for (int c = 0; c < kOE; ++c) o[size_t(e) * kOE + c] = acc[c];
+}
+
 // ---- G assembly -----------------------------------------------------------------
 // 3x3 helpers, row-major
 __device__ __forceinline__ void mmT(const float *P, const float *Q, float *R) {  // R = P Q^T
@@ -530,6 +626,7 @@ struct LearnedPC {
   // graph + activations for the current topology
   const void *topo_key = nullptr;
   int topo_n = -1, topo_nb = -1;
+  bool topo_train = false;  // training buffers allocated for this topology
   lpc::Graph G;
   DevBuf<float> fN, dvec, fE, h[4], cat[3], gate, eX, o, theta;
   DevBuf<float> dh, dcat, dgate, deX, dO, dtheta, dGv, tmpX;
@@ -670,17 +767,55 @@ std::string backward(LearnedPC &P, const Graph &G, const uint8_t *pinned, cudaSt
 namespace eolc {
 namespace lpc {
 
-std::string ensure_buffers(LearnedPC &P, int n, int m, int nb) {
+// Inference forward (8 launches): features, h0, three fused layers, theta,
+// the edge head, G assembly.  Fills P.Gv; the same numbers as forward().
+std::string forward_fused(LearnedPC &P, const Graph &G, const int *blk_row, const float *A,
+                          const uint8_t *pinned, cudaStream_t s) {
+  const Layout &L = P.L;
+  const float *W = P.params.p;
+  const int n = G.n, m = G.m;
+  features_kernel<<<nblk(std::max(n, m), 256), 256, 0, s>>>(n, m, G.rowptr.p, G.diag.p, A, pinned,
+                                                          G.ei.p, G.ej.p, G.bij.p, P.fN.p,
+                                                          P.dvec.p, P.fE.p);
+  dense_fwd_kernel<<<nblk(n, 64), 256, size_t(kFN * kH + kH) * sizeof(float), s>>>(
+      n, kFN, kH, P.fN.p, W + L.Wn, W + L.Wn + kFN * kH, kRelu, P.h[0].p);
+  for (int l = 0; l < kLayers; ++l)
+    layer_fused_kernel<<<nblk(n, kLayerNodes), kLayerThreads, 0, s>>>(
+        n, G.inc_ptr.p, G.inc.p, G.ei.p, G.ej.p, G.deg_inv.p, P.fE.p, W + L.Wg, W + L.Wl[l],
+        P.h[l].p, P.h[l + 1].p);
+  dense_fwd_kernel<<<nblk(n, 64), 256, size_t(kH * kON + kON) * sizeof(float), s>>>(
+      n, kH, kON, P.h[3].p, W + L.Wt, W + L.Wt + kH * kON, kNone, P.theta.p);
+  edge_out_kernel<<<nblk(m, 128), 128, 0, s>>>(m, G.ei.p, G.ej.p, P.h[3].p, P.fE.p, W + L.Wo,
+                                               P.o.p);
+  g_assemble_kernel<<<nblk(G.nb, 128), 128, 0, s>>>(G.nb, blk_row, G.colidx.p, G.blk_edge.p,
+                                                   G.inc_ptr.p, G.inc.p, G.ei.p, G.ej.p, P.o.p,
+                                                   P.theta.p, P.dvec.p, pinned, P.Gv.p);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? "" : cudaGetErrorString(e);
+}
+
+// Buffers of the inference forward; with train, also those of the training
+// forward and backward (the per-edge gate and concat matrices and all
+// gradients), allocated only when a training call needs them.
+std::string ensure_buffers(LearnedPC &P, int n, int m, int nb, bool train) {
   const size_t N = size_t(n), M = size_t(m);
+  {
+    cudaError_t es[] = {
+        P.fN.resize(N * kFN), P.dvec.resize(N * 3), P.fE.resize(M * kFE),
+        P.h[0].resize(N * kH), P.h[1].resize(N * kH), P.h[2].resize(N * kH),
+        P.h[3].resize(N * kH), P.o.resize(M * kOE), P.theta.resize(N * kON),
+        P.Gv.resize(size_t(nb) * 9 + 16)};
+    for (cudaError_t e : es)
+      if (e != cudaSuccess) return cudaGetErrorString(e);
+  }
+  if (!train) return "";
   cudaError_t es[] = {
-      P.fN.resize(N * kFN), P.dvec.resize(N * 3), P.fE.resize(M * kFE),
-      P.h[0].resize(N * kH), P.h[1].resize(N * kH), P.h[2].resize(N * kH), P.h[3].resize(N * kH),
       P.cat[0].resize(N * 2 * kH), P.cat[1].resize(N * 2 * kH), P.cat[2].resize(N * 2 * kH),
-      P.gate.resize(M * kH), P.eX.resize(M * kEdgeIn), P.o.resize(M * kOE),
-      P.theta.resize(N * kON), P.dh.resize(N * kH), P.dcat.resize(N * 2 * kH),
+      P.gate.resize(M * kH), P.eX.resize(M * kEdgeIn),
+      P.dh.resize(N * kH), P.dcat.resize(N * 2 * kH),
       P.dgate.resize(M * kH), P.deX.resize(M * kEdgeIn), P.dO.resize(M * kOE),
       P.dtheta.resize(N * kON), P.dGv.resize(size_t(nb) * 9), P.tmpX.resize(N * kH),
-      P.Gv.resize(size_t(nb) * 9 + 16), P.y.resize(N * 3), P.r.resize(N * 3),
+      P.y.resize(N * 3), P.r.resize(N * 3),
       P.dpart.resize((N + 255) / 256 + 1), P.dloss.resize(2),
       // dense-backward partials: largest (rows/64) x (in*out + out)
       P.parts.resize(std::max(((M + 63) / 64) * size_t(kEdgeIn * kOE + kOE),
@@ -691,16 +826,20 @@ std::string ensure_buffers(LearnedPC &P, int n, int m, int nb) {
 }
 
 std::string use_topology(LearnedPC &P, const HostTopology &H, DevBuf<int> &blk_row_out,
-                         cudaStream_t s) {
+                         cudaStream_t s, bool train = true) {
   (void)blk_row_out;
-  if (P.topo_n == H.n_nodes && P.topo_nb == H.n_blocks && P.topo_key == &H) return "";
-  std::string msg = build_graph(H, P.G, s);
+  if (P.topo_n != H.n_nodes || P.topo_nb != H.n_blocks || P.topo_key != &H) {
+    std::string msg = build_graph(H, P.G, s);
+    if (!msg.empty()) return msg;
+    P.topo_n = H.n_nodes;
+    P.topo_nb = H.n_blocks;
+    P.topo_key = &H;
+    P.topo_train = false;
+  }
+  if (train && P.topo_train) return "";
+  std::string msg = ensure_buffers(P, H.n_nodes, P.G.m, H.n_blocks, train);
   if (!msg.empty()) return msg;
-  msg = ensure_buffers(P, H.n_nodes, P.G.m, H.n_blocks);
-  if (!msg.empty()) return msg;
-  P.topo_n = H.n_nodes;
-  P.topo_nb = H.n_blocks;
-  P.topo_key = &H;
+  if (train) P.topo_train = true;
   return "";
 }
 
@@ -912,6 +1051,30 @@ eolc_status eolc_lpc_add_system(eolc_lpc *P, eolc_ctx *ctx, const int *fixed_dof
 
 int eolc_lpc_num_systems(const eolc_lpc *P) { return P ? int(P->sys_A.size()) : 0; }
 
+eolc_status eolc_lpc_blocks(eolc_lpc *P, eolc_ctx *ctx, const int *fixed_dofs_h, int n_fixed,
+                            float *G_h) {
+  if (!P || !G_h || (n_fixed > 0 && !fixed_dofs_h)) return EOLC_BAD_ARG;
+  eolc_status st = ctx_mixed_matrix(ctx);
+  if (st != EOLC_OK) return st;
+  cudaSetDevice(P->device);
+  const int n = ctx->topo.n_nodes, nb = ctx->topo.n_blocks;
+  auto mask = pin_mask(n, fixed_dofs_h, n_fixed);
+  DevBuf<uint8_t> pin;
+  if (pin.upload(mask.data(), mask.size(), P->stream) != cudaSuccess) return EOLC_CUDA_ERROR;
+  cudaStreamSynchronize(P->stream);
+  const float *Gm = nullptr;
+  std::string msg = learned_forward(P, ctx, pin.p, &Gm, ctx->stream);
+  if (!msg.empty()) {
+    P->err = msg;
+    return EOLC_CUDA_ERROR;
+  }
+  if (cudaMemcpyAsync(G_h, Gm, sizeof(float) * size_t(nb) * 9, cudaMemcpyDeviceToHost,
+                      ctx->stream) != cudaSuccess ||
+      cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+    return EOLC_CUDA_ERROR;
+  return EOLC_OK;
+}
+
 eolc_status eolc_lpc_train(eolc_lpc *P, int epochs, float lr, unsigned seed,
                            double *epoch_loss_h) {
   if (!P || epochs <= 0 || !(lr > 0) || P->sys_A.empty()) return EOLC_BAD_ARG;
@@ -970,12 +1133,12 @@ const char *eolc_lpc_last_error(const eolc_lpc *P) { return P ? P->err.c_str() :
 namespace eolc {
 std::string learned_forward(eolc_lpc *P, eolc_ctx *ctx, const uint8_t *pinned_d,
                             const float **G_out, cudaStream_t s) {
-  cudaStreamSynchronize(s);
-  std::string msg = lpc::use_topology(*P, ctx->host, P->train_blk_row, P->stream);
+  // the first call on a topology builds the graph (host work and uploads on
+  // the network's stream, synchronised); later calls only enqueue on s
+  std::string msg = lpc::use_topology(*P, ctx->host, P->train_blk_row, P->stream, false);
   if (!msg.empty()) return msg;
-  msg = lpc::forward(*P, P->G, ctx->topo.blk_row.p, ctx->A32.p, pinned_d, P->stream);
+  msg = lpc::forward_fused(*P, P->G, ctx->topo.blk_row.p, ctx->A32.p, pinned_d, s);
   if (!msg.empty()) return msg;
-  if (cudaStreamSynchronize(P->stream) != cudaSuccess) return "learned forward failed";
   *G_out = P->Gv.p;
   return "";
 }

@@ -104,7 +104,7 @@ EXPORTS = ["eolc_version", "eolc_launch_count", "eolc_create", "eolc_destroy", "
            "eolc_set_topology_batched", "eolc_set_instance_materials", "eolc_step_batched",
            "eolc_batch_num_configs", "eolc_batch_config_name", "eolc_batch_set_config",
            "eolc_batch_autotune", "eolc_set_learned_refresh",
-           "eolc_batch_set_jacobi_reference"]
+           "eolc_batch_set_jacobi_reference", "eolc_lpc_blocks"]
 
 
 def load_library(path=LIB_PATH):
@@ -151,6 +151,7 @@ def load_library(path=LIB_PATH):
     L.eolc_lpc_loss_grad.argtypes = [_V, _V, _I, ctypes.c_int, _F, ctypes.c_int, _D, _F]
     L.eolc_lpc_add_system.argtypes = [_V, _V, _I, ctypes.c_int, _F, ctypes.c_int]
     L.eolc_lpc_num_systems.argtypes = [_V]
+    L.eolc_lpc_blocks.argtypes = [_V, _V, _I, ctypes.c_int, _F]
     L.eolc_lpc_clear_systems.argtypes = [_V]
     L.eolc_lpc_train.argtypes = [_V, ctypes.c_int, ctypes.c_float, ctypes.c_uint, _D]
     L.eolc_attach_preconditioner.argtypes = [_V, _V]
@@ -440,6 +441,15 @@ class LearnedPC:
         self._check(lib.eolc_lpc_add_system(self._h, ctx.handle, _i(fixed_dofs), len(fixed_dofs),
                                             probes.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
                                             probes.shape[0]))
+
+    def blocks(self, ctx, fixed_dofs):
+        """G (n_blocks x 9) for the context's current FP32 MDK."""
+        fixed_dofs = _i32(fixed_dofs)
+        nb = len(ctx.bsr_pattern()[1])
+        G = np.zeros(nb * 9, np.float32)
+        self._check(lib.eolc_lpc_blocks(self._h, ctx.handle, _i(fixed_dofs), len(fixed_dofs),
+                                        G.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return G.reshape(-1, 9)
 
     def num_systems(self):
         return lib.eolc_lpc_num_systems(self._h)

@@ -329,6 +329,11 @@ eolc_status eolc_lpc_add_system(eolc_lpc *lpc, eolc_ctx *ctx,
                                 const int *fixed_dofs_h, int n_fixed,
                                 const float *probes_h, int n_probes);
 int eolc_lpc_num_systems(const eolc_lpc *lpc);
+/* The approximate inverse G (n_blocks x 9 FP32 values, the BSR pattern of
+ * MDK) the network produces for the context's current FP32 MDK with the
+ * given pinned DOFs: the blocks EOLC_PC_LEARNED applies. */
+eolc_status eolc_lpc_blocks(eolc_lpc *lpc, eolc_ctx *ctx, const int *fixed_dofs_h,
+                            int n_fixed, float *G_h);
 eolc_status eolc_lpc_clear_systems(eolc_lpc *lpc);
 /* Adam over the stored systems (seeded shuffle); epoch_loss_h[epochs]
  * receives the mean probe loss of each epoch. */

@@ -2,9 +2,10 @@
 
 TEST INFRASTRUCTURE ONLY: checks the library's hand-written CUDA forward and
 backward kernels (eol-cloth_gb300/csrc/learned.cu).  The same network, the
-same BF16 rounding of the weights in the forward pass (straight-through in
-the backward pass), the same G assembly and the same probe loss, written
-with torch on the CPU in FP64 and differentiated by torch.autograd.
+same BF16 rounding of the weight matrices in the forward pass (biases stay
+FP32; straight-through in the backward pass), the same G assembly and the
+same probe loss, written with torch on the CPU in FP64 and differentiated by
+torch.autograd.
 """
 import numpy as np
 import torch
@@ -50,9 +51,10 @@ def graph(rowptr, colidx):
     return np.array(ei), np.array(ej), np.array(bij), np.array(bji), diag
 
 
-def loss_and_grad(params, A, rowptr, colidx, pinned, probes):
-    """params: (P,) float32; A: (nb, 9) float32 block values; pinned: (3N,)
-    bool; probes: (k, 3N) float32.  Returns (loss, grad (P,) float64)."""
+def _forward(th, A, rowptr, colidx, pinned):
+    """G (nb, 3, 3) from the FP64 parameter vector th: weight matrices are
+    rounded to BF16 (straight-through for the gradient), biases are not —
+    as in the library's kernels."""
     L, P = layout()
     n = len(rowptr) - 1
     ei, ej, bij, bji, diag = graph(rowptr, colidx)
@@ -60,12 +62,13 @@ def loss_and_grad(params, A, rowptr, colidx, pinned, probes):
     A = torch.tensor(np.asarray(A, np.float64).reshape(-1, 3, 3))
     pin = torch.tensor(np.asarray(pinned, bool).reshape(n, 3))
     free = (~pin).double()
-    th = torch.tensor(np.asarray(params, np.float64), requires_grad=True)
-    Wr = th + (bf16_round(th) - th).detach()  # BF16 forward, straight-through
 
     def W(name, shape):
         o, c = L[name]
-        return Wr[o:o + c].reshape(shape)
+        v = th[o:o + c]
+        if name.startswith("W"):
+            v = v + (bf16_round(v) - v).detach()
+        return v.reshape(shape)
 
     D = A[diag]
     d = torch.stack([D[:, 0, 0], D[:, 1, 1], D[:, 2, 2]], 1)
@@ -111,6 +114,22 @@ def loss_and_grad(params, A, rowptr, colidx, pinned, probes):
     # free-DOF mask on both sides
     col_of = torch.tensor(np.asarray(colidx))
     G = G * free[torch.tensor(row_of)][:, :, None] * free[col_of][:, None, :]
+    return G, (n, row_of, torch.tensor(np.asarray(colidx)), free, A)
+
+
+def g_blocks(params, A, rowptr, colidx, pinned):
+    """The approximate inverse G (nb x 9, float64) of the network for MDK
+    blocks A (nb x 9), BF16 weights, FP64 arithmetic."""
+    th = torch.tensor(np.asarray(params, np.float64))
+    G, _ = _forward(th, A, rowptr, colidx, pinned)
+    return G.detach().numpy().reshape(-1, 9)
+
+
+def loss_and_grad(params, A, rowptr, colidx, pinned, probes):
+    """params: (P,) float32; A: (nb, 9) float32 block values; pinned: (3N,)
+    bool; probes: (k, 3N) float32.  Returns (loss, grad (P,) float64)."""
+    th = torch.tensor(np.asarray(params, np.float64), requires_grad=True)
+    G, (n, row_of, col_of, free, A) = _forward(th, A, rowptr, colidx, pinned)
     loss = 0.0
     k = probes.shape[0]
     At = A

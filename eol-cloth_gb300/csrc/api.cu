@@ -123,13 +123,17 @@ eolc_status assemble(eolc_ctx *ctx, const eolc_material &mat, const double g[3],
   size_t nb9 = size_t(ctx->topo.n_blocks) * 9;
   if (prec == EOLC_PREC_FP64) EOLC_CHECK_CUDA(ctx, ctx->A64.resize(nb9 + 16));
   if (want_M) EOLC_CHECK_CUDA(ctx, ctx->Mblk.resize(nb9));
-  launch_assemble_blocks(ctx->topo, ctx->x.p, ctx->X.p, md, mats, node_inst, prec,
+  {
+    const size_t need = assemble_scratch_bytes(ctx->topo, prec);
+    if (ctx->elem.n < need) EOLC_CHECK_CUDA(ctx, ctx->elem.resize(need));
+  }
+  launch_assemble_blocks(ctx->topo, ctx->x.p, ctx->X.p, md, mats, node_inst, prec, ctx->elem.p,
                          prec == EOLC_PREC_FP64 ? ctx->A64.p : nullptr,
                          prec == EOLC_PREC_FP64 ? nullptr : ctx->A32.p,
                          want_M ? ctx->Mblk.p : nullptr, s);
   launch_forces_rhs(ctx->topo, ctx->x.p, ctx->X.p, ctx->v.p, md, mats, node_inst, prec,
                     ctx->f.p, want_b ? ctx->b.p : nullptr, s);
-  ctx->launches += 2;
+  ctx->launches += ctx->topo.n_hinge > 0 ? 4 : 3;
   EOLC_CHECK_CUDA(ctx, cudaGetLastError());
   return EOLC_OK;
 }
@@ -254,6 +258,9 @@ eolc_status batch_begin(eolc_ctx *ctx, const double grav[3], double h, const int
   EOLC_CHECK_CUDA(ctx, ctx->inst_matd.upload(ctx->inst_matd_h.data(), n_inst, s));
   if (opts->precision == EOLC_PREC_FP64)
     EOLC_CHECK_CUDA(ctx, ctx->A64.resize(size_t(ctx->topo.n_blocks) * 9 + 16));
+  // the captured assembly writes its element blocks here
+  const size_t need = assemble_scratch_bytes(ctx->topo, opts->precision);
+  if (ctx->elem.n < need) EOLC_CHECK_CUDA(ctx, ctx->elem.resize(need));
   return EOLC_OK;
 }
 
@@ -576,6 +583,7 @@ eolc_status eolc_set_topology_batched(eolc_ctx *ctx, int n_inst, const int *node
   ctx->bgraph_key.clear();
   ctx->A64.release();
   ctx->Mblk.release();
+  ctx->elem.release();
   eolc_status st = ensure_state(ctx);
   if (st != EOLC_OK) return st;
   EOLC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->v.p, 0, sizeof(double) * ctx->v.n, s));
@@ -839,7 +847,8 @@ eolc_status eolc_step_batched(eolc_ctx *ctx, int n_steps, const double grav[3], 
   for (const void *p : {(const void *)ctx->fixed_dofs.p, (const void *)ctx->fixed_vel.p,
                         (const void *)ctx->pinned.p, (const void *)ctx->beq_full.p,
                         (const void *)ctx->A64.p, (const void *)ctx->A32.p,
-                        (const void *)ctx->inst_matd.p, (const void *)ctx->bwork})
+                        (const void *)ctx->elem.p, (const void *)ctx->inst_matd.p,
+                        (const void *)ctx->bwork})
     key.push_back(double(reinterpret_cast<uintptr_t>(p)));
   if (!ctx->bgraph || key != ctx->bgraph_key) {
     if (ctx->bgraph) cudaGraphExecDestroy(ctx->bgraph);

@@ -3,11 +3,13 @@
 //
 // Replaces the triplet loops of faceBasedF / edgeBasedF and the two
 // setFromTriplets calls (Forces.cpp:331-930) plus b = -(M v + h f)
-// (Cloth.cpp:345).  Design: one thread per BSR block gathers the element
-// terms that land in its block, in the reference's insertion order (faces
-// ascending, then hinges ascending), and writes the block once.  No atomics,
-// no staging buffer: results are bit-reproducible run to run and the only
-// HBM writes are the BSR values themselves.
+// (Cloth.cpp:345).  Design: an element pass (one thread per triangle, one
+// per hinge) evaluates each element once and writes its 3x3 blocks (9 per
+// triangle: d_B h^2 K_e; 16 per hinge: d_B h^2 K_b) and the triangle's mass
+// t8 to a contribution buffer; then one thread per BSR block sums the
+// contributions that land in it in the reference's insertion order (faces
+// ascending, then hinges ascending) and writes the block once.  No atomics:
+// results are bit-reproducible run to run.
 #include <cuda_runtime.h>
 
 #include "elements.cuh"
@@ -17,46 +19,96 @@ namespace eolc {
 
 namespace {
 
-template <typename T, typename Acc>
+// Element pass, triangles: d_B h^2 K_e block (la, lb) of face t at
+// Kt[((t * 3 + la) * 3 + lb) * 9 ...] (fillxxMI, Forces.cpp:103-125), and
+// t8 = rho 2 A (ComputeInertial.cpp:33).
+template <typename T>
 __global__ void __launch_bounds__(128)
-assemble_blocks_kernel(int n_blocks, const int *__restrict__ cptr,
-                       const int *__restrict__ contrib,
-                       const int *__restrict__ tri,
-                       const int *__restrict__ hinge,
-                       const double *__restrict__ x,
-                       const double *__restrict__ X, MaterialD m,
-                       const MaterialD *__restrict__ mats,
-                       const int *__restrict__ node_inst,
-                       const int *__restrict__ blk_row,
-                       double *__restrict__ A64, float *__restrict__ A32,
-                       double *__restrict__ Mblk) {
-  int bidx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (bidx >= n_blocks) return;
-  if (mats) m = mats[node_inst[blk_row[bidx]]];  // batched: the row's instance
-  Acc acc[9], macc[9];
+tri_blocks_kernel(int n_tri, const int *__restrict__ tri, const double *__restrict__ x,
+                  const double *__restrict__ X, MaterialD m,
+                  const MaterialD *__restrict__ mats, const int *__restrict__ node_inst,
+                  T *__restrict__ Kt, T *__restrict__ t8) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tri) return;
+  const int a = __ldg(tri + 3 * t), b = __ldg(tri + 3 * t + 1), c = __ldg(tri + 3 * t + 2);
+  if (mats) m = mats[node_inst[a]];  // batched: the element's instance
+  const Tri<T> q = make_tri<T>(x, X, a, b, c);
+  const T mu = T(m.mu), lam = T(m.lam), dh2 = T(m.dh2);
+  T *out = Kt + size_t(t) * 81;
+#pragma unroll 1
+  for (int la = 0; la < 3; ++la)
+#pragma unroll 1
+    for (int lb = 0; lb < 3; ++lb) {
+      T blk[9];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) { acc[k] = Acc(0); macc[k] = Acc(0); }
-  const T mu = T(m.mu), lam = T(m.lam), dh2 = T(m.dh2), beta = T(m.beta);
-  int c0 = cptr[bidx], c1 = cptr[bidx + 1];
+      for (int k = 0; k < 9; ++k) blk[k] = T(0);
+      add_membrane_block<T, T>(q, la, lb, mu, lam, dh2, blk);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) out[(3 * la + lb) * 9 + k] = blk[k];
+    }
+  t8[t] = T(m.rho) * T(2) * q.A;
+}
+
+// Element pass, hinges: d_B h^2 K_b block (la, lb) of hinge e at
+// Kh[((e * 4 + la) * 4 + lb) * 9 ...] (fillxxB, Forces.cpp:522-539, 885-908).
+template <typename T>
+__global__ void __launch_bounds__(128)
+hinge_blocks_kernel(int n_hinge, const int *__restrict__ hinge, const double *__restrict__ x,
+                    const double *__restrict__ X, MaterialD m,
+                    const MaterialD *__restrict__ mats, const int *__restrict__ node_inst,
+                    T *__restrict__ Kh) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_hinge) return;
+  const int *hv = hinge + 4 * e;
+  const int v0 = __ldg(hv), v1 = __ldg(hv + 1), v2 = __ldg(hv + 2), v3n = __ldg(hv + 3);
+  if (mats) m = mats[node_inst[v0]];
+  const Hinge<T> H = make_hinge<T>(x, X, v0, v1, v2, v3n, T(m.beta));
+  const T dh2 = T(m.dh2);
+  T *out = Kh + size_t(e) * 144;
+#pragma unroll 1
+  for (int la = 0; la < 4; ++la)
+#pragma unroll 1
+    for (int lb = 0; lb < 4; ++lb) {
+      T blk[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) blk[k] = T(0);
+      add_bending_block<T, T>(H, la, lb, dh2, blk);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) out[(4 * la + lb) * 9 + k] = blk[k];
+    }
+}
+
+// Block gather: MDK (and M) of every BSR block from the element blocks, in
+// the reference's insertion order: per face, MDK += d_B h^2 K_e then the mass
+// M_e (t8/12 on the diagonal, t8/24 off it, times I); per hinge,
+// MDK += d_B h^2 K_b.
+template <typename T>
+__global__ void __launch_bounds__(128)
+gather_blocks_kernel(int n_blocks, const int *__restrict__ cptr, const int *__restrict__ contrib,
+                     const T *__restrict__ Kt, const T *__restrict__ t8,
+                     const T *__restrict__ Kh, double *__restrict__ A64,
+                     float *__restrict__ A32, double *__restrict__ Mblk) {
+  const int bidx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (bidx >= n_blocks) return;
+  T acc[9], macc[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) { acc[k] = T(0); macc[k] = T(0); }
+  const int c0 = cptr[bidx], c1 = cptr[bidx + 1];
   for (int q = c0; q < c1; ++q) {
-    int code = __ldg(contrib + q);
-    int lb = code & 3, la = (code >> 2) & 3, e = code >> 5;
+    const int code = __ldg(contrib + q);
+    const int lb = code & 3, la = (code >> 2) & 3, e = code >> 5;
     if (!(code & kHingeBit)) {
-      int a = __ldg(tri + 3 * e), b = __ldg(tri + 3 * e + 1),
-          c = __ldg(tri + 3 * e + 2);
-      Tri<T> t = make_tri<T>(x, X, a, b, c);
-      // MDK += M_e + dh2 K_e (fillxMI / fillxxMI, Forces.cpp:103-125)
-      add_membrane_block<T, Acc>(t, la, lb, mu, lam, dh2, acc);
-      T t8 = T(m.rho) * T(2) * t.A;
-      T mm = la == lb ? t8 / T(12) : t8 / T(24);
-      acc[0] += Acc(mm); acc[4] += Acc(mm); acc[8] += Acc(mm);
-      macc[0] += Acc(mm); macc[4] += Acc(mm); macc[8] += Acc(mm);
+      const T *blk = Kt + size_t(e) * 81 + (3 * la + lb) * 9;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) acc[k] += __ldg(blk + k);
+      const T te = __ldg(t8 + e);
+      const T mm = la == lb ? te / T(12) : te / T(24);
+      acc[0] += mm; acc[4] += mm; acc[8] += mm;
+      macc[0] += mm; macc[4] += mm; macc[8] += mm;
     } else {
-      const int *hv = hinge + 4 * e;
-      Hinge<T> H = make_hinge<T>(x, X, __ldg(hv), __ldg(hv + 1), __ldg(hv + 2),
-                                 __ldg(hv + 3), beta);
-      // MDK += dh2 Kb (fillxB / fillxxB, Forces.cpp:522-539, 885-908)
-      add_bending_block<T, Acc>(H, la, lb, dh2, acc);
+      const T *blk = Kh + size_t(e) * 144 + (4 * la + lb) * 9;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) acc[k] += __ldg(blk + k);
     }
   }
   if (A64) {
@@ -126,18 +178,33 @@ forces_rhs_kernel(int n_nodes, const int *__restrict__ nf_ptr,
 void launch_assemble_blocks(const DevTopology &T, const double *x,
                             const double *X, const MaterialD &m,
                             const MaterialD *mats, const int *node_inst,
-                            int prec, double *A64, float *A32, double *Mblk,
+                            int prec, void *elem, double *A64, float *A32, double *Mblk,
                             cudaStream_t s) {
-  int nb = T.n_blocks;
-  dim3 block(128), grid((nb + 127) / 128);
-  if (prec == EOLC_PREC_FP64)
-    assemble_blocks_kernel<double, double><<<grid, block, 0, s>>>(
-        nb, T.cptr.p, T.contrib.p, T.tri.p, T.hinge.p, x, X, m, mats, node_inst, T.blk_row.p,
-        A64, A32, Mblk);
-  else
-    assemble_blocks_kernel<float, float><<<grid, block, 0, s>>>(
-        nb, T.cptr.p, T.contrib.p, T.tri.p, T.hinge.p, x, X, m, mats, node_inst, T.blk_row.p,
-        A64, A32, Mblk);
+  const int nb = T.n_blocks, nt = T.n_tri, nh = T.n_hinge;
+  if (prec == EOLC_PREC_FP64) {
+    double *Kt = static_cast<double *>(elem), *t8 = Kt + size_t(nt) * 81, *Kh = t8 + nt;
+    tri_blocks_kernel<double><<<(nt + 127) / 128, 128, 0, s>>>(nt, T.tri.p, x, X, m, mats,
+                                                               node_inst, Kt, t8);
+    if (nh > 0)
+      hinge_blocks_kernel<double><<<(nh + 127) / 128, 128, 0, s>>>(nh, T.hinge.p, x, X, m, mats,
+                                                                   node_inst, Kh);
+    gather_blocks_kernel<double><<<(nb + 127) / 128, 128, 0, s>>>(
+        nb, T.cptr.p, T.contrib.p, Kt, t8, Kh, A64, A32, Mblk);
+  } else {
+    float *Kt = static_cast<float *>(elem), *t8 = Kt + size_t(nt) * 81, *Kh = t8 + nt;
+    tri_blocks_kernel<float><<<(nt + 127) / 128, 128, 0, s>>>(nt, T.tri.p, x, X, m, mats,
+                                                              node_inst, Kt, t8);
+    if (nh > 0)
+      hinge_blocks_kernel<float><<<(nh + 127) / 128, 128, 0, s>>>(nh, T.hinge.p, x, X, m, mats,
+                                                                  node_inst, Kh);
+    gather_blocks_kernel<float><<<(nb + 127) / 128, 128, 0, s>>>(
+        nb, T.cptr.p, T.contrib.p, Kt, t8, Kh, A64, A32, Mblk);
+  }
+}
+
+size_t assemble_scratch_bytes(const DevTopology &T, int prec) {
+  const size_t e = prec == EOLC_PREC_FP64 ? sizeof(double) : sizeof(float);
+  return e * (size_t(T.n_tri) * 82 + size_t(T.n_hinge) * 144);
 }
 
 void launch_forces_rhs(const DevTopology &T, const double *x, const double *X,

@@ -84,11 +84,14 @@ struct MaterialD {
 // Kernel launchers (assemble.cu).  mats/node_inst (both device, may be
 // null): per-instance material table and the instance of every node, used
 // instead of m for batched topologies.
+// elem: device scratch of assemble_scratch_bytes(T, prec) for the element
+// blocks.  Launches the triangle pass, the hinge pass and the block gather.
 void launch_assemble_blocks(const DevTopology &T, const double *x,
                             const double *X, const MaterialD &m,
                             const MaterialD *mats, const int *node_inst,
-                            int prec, double *A64, float *A32, double *Mblk,
+                            int prec, void *elem, double *A64, float *A32, double *Mblk,
                             cudaStream_t s);
+size_t assemble_scratch_bytes(const DevTopology &T, int prec);
 void launch_forces_rhs(const DevTopology &T, const double *x, const double *X,
                        const double *v, const MaterialD &m,
                        const MaterialD *mats, const int *node_inst, int prec,
@@ -194,6 +197,7 @@ struct eolc_ctx {
   // state and per-step buffers
   eolc::DevBuf<double> x, X, v, f, b, A64, Mblk, beq_full;
   eolc::DevBuf<float> A32;
+  eolc::DevBuf<unsigned char> elem;  // element blocks of the assembly
   eolc::DevBuf<uint8_t> pinned;
   eolc::DevBuf<int> fixed_dofs;
   eolc::DevBuf<double> fixed_vel;

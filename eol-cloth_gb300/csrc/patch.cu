@@ -282,6 +282,7 @@ struct PC {
 // after (warp 0 reduces the G partials and broadcasts).  red holds the warp
 // partials in [0, 3 NW) and the broadcast in [3 NW, 3 NW + 3).  Returns false
 // when the grid barrier timed out.
+constexpr int kPartPerLane = 6;  // partials one lane reads: up to 192 CTAs
 struct GridSum {
   double *part;
   unsigned *bar;
@@ -304,24 +305,35 @@ struct GridSum {
     if (lane == 0) { red[3 * warp] = a; red[3 * warp + 1] = b; red[3 * warp + 2] = c; }
     __syncthreads();
     V *pp = reinterpret_cast<V *>(part) + size_t(3) * G * pset;
-    if (threadIdx.x == 0) {
+    if (warp == 0) {  // this CTA's partial: a fixed tree over its warps
       V x = Ac::zero(), y = Ac::zero(), z = Ac::zero();
-      for (int w = 0; w < NW; ++w) {
-        x = Ac::add(x, red[3 * w]);
-        y = Ac::add(y, red[3 * w + 1]);
-        z = Ac::add(z, red[3 * w + 2]);
+      if (lane < NW) { x = red[3 * lane]; y = red[3 * lane + 1]; z = red[3 * lane + 2]; }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        x = Ac::add(x, Ac::shfl_xor(x, o));
+        y = Ac::add(y, Ac::shfl_xor(y, o));
+        z = Ac::add(z, Ac::shfl_xor(z, o));
       }
-      pp[3 * cta] = x; pp[3 * cta + 1] = y; pp[3 * cta + 2] = z;
+      if (lane == 0) { pp[3 * cta] = x; pp[3 * cta + 1] = y; pp[3 * cta + 2] = z; }
     }
     if (!grid_barrier(bar, G, epoch, st)) return false;
     if (warp == 0) {
-      V x = Ac::zero(), y = Ac::zero(), z = Ac::zero();
-      for (int k = lane; k < G; k += 32) {
+      // every load issued before the first add: one L2 round trip
+      double v[kPartPerLane][3];
+#pragma unroll
+      for (int j = 0; j < kPartPerLane; ++j) {
+        const int k = lane + 32 * j;
         const double *pd = reinterpret_cast<const double *>(pp + 3 * k);
-        double v0 = __ldcg(pd), v1 = __ldcg(pd + 1), v2 = __ldcg(pd + 2);
-        x = Ac::add(x, *reinterpret_cast<V *>(&v0));
-        y = Ac::add(y, *reinterpret_cast<V *>(&v1));
-        z = Ac::add(z, *reinterpret_cast<V *>(&v2));
+        v[j][0] = k < G ? __ldcg(pd) : 0.0;
+        v[j][1] = k < G ? __ldcg(pd + 1) : 0.0;
+        v[j][2] = k < G ? __ldcg(pd + 2) : 0.0;
+      }
+      V x = Ac::zero(), y = Ac::zero(), z = Ac::zero();
+#pragma unroll
+      for (int j = 0; j < kPartPerLane; ++j) {
+        x = Ac::add(x, *reinterpret_cast<V *>(&v[j][0]));
+        y = Ac::add(y, *reinterpret_cast<V *>(&v[j][1]));
+        z = Ac::add(z, *reinterpret_cast<V *>(&v[j][2]));
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
@@ -1061,7 +1073,8 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
                              int n_sm, PatchPlan &out) {
   const int NB = int(colidx.size());
   const int G = std::max(1, (N + kTargetRows - 1) / kTargetRows);
-  if (G > n_sm) return "mesh too large for shared-memory patches on this device";
+  if (G > n_sm || G > 32 * kPartPerLane)
+    return "mesh too large for shared-memory patches on this device";
   std::vector<int> all(N), perm, bounds;
   for (int k = 0; k < N; ++k) all[k] = k;
   perm.reserve(N);

@@ -74,6 +74,7 @@ constexpr int kMaxHaloNodes = 384;  // distinct outside nodes those blocks touch
 constexpr float kLoFrac = 30.f;     // Chebyshev interval [lmax / 30, lmax]
 constexpr float kBoundMargin = 1.02f;
 static_assert(kMaxRows <= kRThreads, "one thread per patch row");
+static_assert(kMaxHaloNodes <= kRThreads, "at most one halo node per thread");
 
 constexpr size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
 // An upper block is one 48-byte record of three float4: (column, v0, v1, v2),
@@ -278,10 +279,12 @@ struct PC {
 
 // Grid-wide sums of three accumulators (deterministic: every CTA adds the
 // same partials in the same order and gets the same values).  One CTA
-// barrier before the grid barrier (warp partials -> thread 0 -> global), one
+// barrier before the grid barrier (warp partials -> warp 0 -> global), one
 // after (warp 0 reduces the G partials and broadcasts).  red holds the warp
-// partials in [0, 3 NW) and the broadcast in [3 NW, 3 NW + 3).  Returns false
-// when the grid barrier timed out.
+// partials in [0, 3 NW) and the broadcast in [3 NW, 3 NW + 3).  pre() runs in
+// every thread right after the grid barrier, so that loads it issues (the
+// halo values of the next step) overlap warp 0's read of the partials.
+// Returns false when the grid barrier timed out.
 constexpr int kPartPerLane = 6;  // partials one lane reads: up to 192 CTAs
 struct GridSum {
   double *part;
@@ -290,8 +293,12 @@ struct GridSum {
   int G, cta;
   unsigned epoch;
   int pset;
+  struct NoPre {
+    __device__ void operator()() const {}
+  };
+  template <class F = NoPre>
   __device__ bool operator()(Acc<float>::V &a, Acc<float>::V &b, Acc<float>::V &c,
-                             Acc<float>::V *red) {
+                             Acc<float>::V *red, F &&pre = F()) {
     using Ac = Acc<float>;
     using V = Ac::V;
     constexpr int NW = kRThreads / 32;
@@ -317,6 +324,7 @@ struct GridSum {
       if (lane == 0) { pp[3 * cta] = x; pp[3 * cta + 1] = y; pp[3 * cta + 2] = z; }
     }
     if (!grid_barrier(bar, G, epoch, st)) return false;
+    pre();
     if (warp == 0) {
       // every load issued before the first add: one L2 round trip
       double v[kPartPerLane][3];
@@ -414,8 +422,25 @@ __global__ void __launch_bounds__(kRThreads, 1) jacobi_resident_kernel(ResParams
     }                                                                   \
   } while (0)
   __syncthreads();  // the resident image is complete
+  // this thread's halo node (at most one: nh <= kMaxHaloNodes <= kRThreads),
+  // its preconditioner block, and its r, s, w of the last step, prefetched
+  // right after each grid barrier
+  const int hj = i < nh ? sm.hnode[i] : -1;
+  PC hpc;
+  for (int k = 0; k < 9; ++k) hpc.b[k] = 0.f;
+  if (hj >= 0) hpc.load(P.pc, hj, P.block_pc);
+  V4<float> hr{}, hs{}, hw{};
+  int pf = 0;  // vector index the prefetch reads
+  const auto prefetch = [&]() {
+    if (hj >= 0) {
+      hr = P.r[pf][hj];
+      hs = P.s[pf][hj];
+      hw = P.w[pf][hj];
+    }
+  };
   EOLC_INIT_PHASE(gam, del, rr);
-  if (!sync(gam, del, rr, red)) return;
+  pf = cur;
+  if (!sync(gam, del, rr, red, prefetch)) return;
   V rmax2 = rr;
   double last_rr64 = A::to_d(rr);
   int it = 0, nref = 0, status = EOLC_NOT_CONVERGED;
@@ -449,7 +474,13 @@ __global__ void __launch_bounds__(kRThreads, 1) jacobi_resident_kernel(ResParams
       r = rn;
       s = sn;
     }
-    halo_u(P, sm, nh, cur, af, bf, false);
+    if (hj >= 0) {  // u'_j = M_j (r_j - alpha (w_j + beta s_j)) from the prefetch
+      V4<float> rj = hr;
+      rj.x -= af * (hw.x + bf * hs.x);
+      rj.y -= af * (hw.y + bf * hs.y);
+      rj.z -= af * (hw.z + bf * hs.z);
+      sm.xh[i] = f4(hpc.apply(rj));
+    }
     __syncthreads();
     if (own) {
       const float3 t = row_apply<true>(sm, i, sm.xs, sm.xh);
@@ -459,7 +490,8 @@ __global__ void __launch_bounds__(kRThreads, 1) jacobi_resident_kernel(ResParams
       d2 = A::addf(d2, dot3(w, un));
       rr2 = A::addf(rr2, dot3(r, r));
     }
-    if (!sync(g2, d2, rr2, red)) return;
+    pf = nxt;
+    if (!sync(g2, d2, rr2, red, prefetch)) return;
     ++it;
     cur = nxt;
     gam_old = gam;
@@ -500,7 +532,8 @@ __global__ void __launch_bounds__(kRThreads, 1) jacobi_resident_kernel(ResParams
     if (A::le(e0, tol2)) { converged = true; break; }
     V g3 = A::zero(), d3 = A::zero(), rr3 = A::zero();
     EOLC_INIT_PHASE(g3, d3, rr3);
-    if (!sync(g3, d3, rr3, red)) return;
+    pf = cur;
+    if (!sync(g3, d3, rr3, red, prefetch)) return;
     gam = g3;
     del = d3;
   }
@@ -653,13 +686,24 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
   const V tol2 = A::from_d(P.tol2 * __ldcg(&P.st->rhs_norm2));
   const V delta2 = A::from_d(kDelta * kDelta);
   V gam = A::zero(), rr = A::zero(), e0 = A::zero();
+  // this thread's halo node (at most one) and its z, p of the last step,
+  // prefetched right after the grid barrier that precedes their use
+  const int hj = i < nh ? sm.hnode[i] : -1;
+  V4<float> hz{}, hp{};
+  int pf = 0;  // index of p the prefetch reads
+  const auto prefetch = [&]() {
+    if (hj >= 0) {
+      hz = P.z[hj];
+      hp = P.p[pf][hj];
+    }
+  };
   z = patch_apply(sm, L, own, i, P.degree, r);
   if (own) {
     P.z[row] = z;
     gam = A::addf(gam, dot3(r, z));
     rr = A::addf(rr, dot3(r, r));
   }
-  if (!sync(gam, rr, e0, red)) return;
+  if (!sync(gam, rr, e0, red, prefetch)) return;
   V rmax2 = rr;
   double last_rr64 = A::to_d(rr);
   int it = 0, nref = 0, status = EOLC_NOT_CONVERGED;
@@ -679,11 +723,7 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
       P.p[nxt][row] = p;
       sm.xs[i] = f4(p);
     }
-    for (int h = threadIdx.x; h < nh; h += kRThreads) {
-      const int j = sm.hnode[h];
-      const V4<float> zj = P.z[j], pj = P.p[cur][j];
-      sm.xh[h] = make_float4(zj.x + bf * pj.x, zj.y + bf * pj.y, zj.z + bf * pj.z, 0.f);
-    }
+    if (hj >= 0) sm.xh[i] = make_float4(hz.x + bf * hp.x, hz.y + bf * hp.y, hz.z + bf * hp.z, 0.f);
     __syncthreads();
     V4<float> q{};
     V pq = A::zero(), e1 = A::zero(), e2 = A::zero();
@@ -709,7 +749,8 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
       g2 = A::addf(g2, dot3(r, z));
       rr2 = A::addf(rr2, dot3(r, r));
     }
-    if (!sync(g2, rr2, e3, red)) return;
+    pf = nxt;
+    if (!sync(g2, rr2, e3, red, prefetch)) return;
     ++it;
     cur = nxt;
     gam_old = gam;
@@ -737,7 +778,8 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
       P.z[row] = z;
       g3 = A::addf(g3, dot3(r, z));
     }
-    if (!sync(rr64, g3, e4, red)) return;
+    pf = cur;
+    if (!sync(rr64, g3, e4, red, prefetch)) return;
     ++nref;
     last_rr64 = A::to_d(rr64);
     rmax2 = rr64;
@@ -808,6 +850,24 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
   if (own) sm.xs[i] = f4(r);
   for (int h = threadIdx.x; h < nh; h += kRThreads) sm.xh[h] = f4(P.r[cur][sm.hnode[h]]);
   __syncthreads();
+  // this thread's halo node (at most one); after the grid barrier that
+  // precedes their use, its z and p (step top) or r and q (residual update)
+  // of the last phase are prefetched
+  const int hj = i < nh ? sm.hnode[i] : -1;
+  V4<float> ha{}, hb{};
+  int pf = 0;
+  const auto prefetch_zp = [&]() {
+    if (hj >= 0) {
+      ha = P.z[hj];
+      hb = P.p[pf][hj];
+    }
+  };
+  const auto prefetch_rq = [&]() {
+    if (hj >= 0) {
+      ha = P.r[pf][hj];
+      hb = P.q[hj];
+    }
+  };
   if (own) {
     const V4<float> g = apply_G(P, sm, cta);
     z = V4<float>{g.x * m.x, g.y * m.y, g.z * m.z, 0.f};
@@ -815,7 +875,8 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
     gam = A::addf(gam, dot3(r, z));
     rr = A::addf(rr, dot3(r, r));
   }
-  if (!sync(gam, rr, e0, red)) return;
+  pf = cur;
+  if (!sync(gam, rr, e0, red, prefetch_zp)) return;
   V rmax2 = rr;
   double last_rr64 = A::to_d(rr);
   int it = 0, nref = 0, status = EOLC_NOT_CONVERGED;
@@ -834,11 +895,7 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
       P.p[nxt][row] = p;
       sm.xs[i] = f4(p);
     }
-    for (int h = threadIdx.x; h < nh; h += kRThreads) {
-      const int j = sm.hnode[h];
-      const V4<float> zj = P.z[j], pj = P.p[cur][j];
-      sm.xh[h] = make_float4(zj.x + bf * pj.x, zj.y + bf * pj.y, zj.z + bf * pj.z, 0.f);
-    }
+    if (hj >= 0) sm.xh[i] = make_float4(ha.x + bf * hb.x, ha.y + bf * hb.y, ha.z + bf * hb.z, 0.f);
     __syncthreads();
     V4<float> q{};
     V pq = A::zero(), e1 = A::zero(), e2 = A::zero();
@@ -848,7 +905,8 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
       P.q[row] = q;
       pq = A::addf(pq, dot3(p, q));
     }
-    if (!sync(pq, e1, e2, red)) return;
+    pf = cur;
+    if (!sync(pq, e1, e2, red, prefetch_rq)) return;
     if (!A::pos(pq) || !A::pos(gam)) {
       status = (A::finite(pq) && A::finite(gam)) ? EOLC_BREAKDOWN : EOLC_NONFINITE;
       break;
@@ -861,11 +919,7 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
       P.r[nxt][row] = r;
       sm.xs[i] = f4(r);
     }
-    for (int h = threadIdx.x; h < nh; h += kRThreads) {
-      const int j = sm.hnode[h];
-      const V4<float> rj = P.r[cur][j], qj = P.q[j];
-      sm.xh[h] = make_float4(rj.x - af * qj.x, rj.y - af * qj.y, rj.z - af * qj.z, 0.f);
-    }
+    if (hj >= 0) sm.xh[i] = make_float4(ha.x - af * hb.x, ha.y - af * hb.y, ha.z - af * hb.z, 0.f);
     __syncthreads();
     V g2 = A::zero(), rr2 = A::zero(), e3 = A::zero();
     if (own) {
@@ -875,7 +929,8 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
       g2 = A::addf(g2, dot3(r, z));
       rr2 = A::addf(rr2, dot3(r, r));
     }
-    if (!sync(g2, rr2, e3, red)) return;
+    pf = nxt;
+    if (!sync(g2, rr2, e3, red, prefetch_zp)) return;
     ++it;
     cur = nxt;
     gam_old = gam;
@@ -909,7 +964,8 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
       P.z[row] = z;
       g3 = A::addf(g3, dot3(r, z));
     }
-    if (!sync(rr64, g3, e4, red)) return;
+    pf = cur;
+    if (!sync(rr64, g3, e4, red, prefetch_zp)) return;
     ++nref;
     last_rr64 = A::to_d(rr64);
     rmax2 = rr64;

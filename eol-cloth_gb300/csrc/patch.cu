@@ -68,32 +68,39 @@ struct RCfg {  // CTA shape of the resident kernels (block_sum3 / reduce_partial
 constexpr int kRThreads = RCfg::kThreads;
 constexpr int kMaxRows = 464;       // rows of one patch (one thread each)
 constexpr int kTargetRows = 448;    // rows per patch the partition aims for
-constexpr int kMaxUpper = 3072;     // patch-internal blocks, upper triangle
-constexpr int kMaxHaloBlk = 768;    // blocks coupling the patch to others
-constexpr int kMaxHaloNodes = 384;  // distinct outside nodes those blocks touch
+constexpr int kMaxFwd = 3328;       // forward records: off-diagonal upper + halo blocks
+constexpr int kMaxSlots = 2688;     // transposed products (one per off-diagonal upper block)
+constexpr int kMaxHaloNodes = 384;  // distinct outside nodes the halo blocks touch
+constexpr int kMaxCount = 255;      // records or slots of one row (8-bit counts)
+constexpr int kWarps = kRThreads / 32;
 constexpr float kLoFrac = 30.f;     // Chebyshev interval [lmax / 30, lmax]
 constexpr float kBoundMargin = 1.02f;
 static_assert(kMaxRows <= kRThreads, "one thread per patch row");
 static_assert(kMaxHaloNodes <= kRThreads, "at most one halo node per thread");
 
 constexpr size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
-// An upper block is one 48-byte record of three float4: (column, v0, v1, v2),
-// (v3, v4, v5, v6), (v7, v8, -, -), read with three 16-byte loads; the column
-// comes with the first so the vector load can issue early.  A transposed
-// entry is one word: upper record index | (row << 16).
-constexpr size_t kOffU = 0;
-constexpr size_t kOffH = al16(kOffU + size_t(kMaxUpper) * 48);
-constexpr size_t kOffTp = al16(kOffH + size_t(kMaxHaloBlk) * 36);
-constexpr size_t kOffHwin = al16(kOffTp + size_t(kMaxUpper) * 4);
-constexpr size_t kOffUptr = al16(kOffHwin + size_t(kMaxHaloBlk) * 2);
-constexpr size_t kOffTptr = al16(kOffUptr + size_t(kMaxRows + 1) * 2);
-constexpr size_t kOffHptr = al16(kOffTptr + size_t(kMaxRows + 1) * 2);
-constexpr size_t kOffHnode = al16(kOffHptr + size_t(kMaxRows + 1) * 2);
-constexpr size_t kOffXs = al16(kOffHnode + size_t(kMaxHaloNodes) * 4);
+// Shared-memory image of one patch.
+//   fval: forward records, 48 bytes each as three float4: (word, v0, v1, v2),
+//         (v3, v4, v5, v6), (v7, v8, -, -); word = column | slot << 16.  The
+//         column indexes the vector image x (0..kMaxRows-1: patch rows,
+//         kMaxRows + h: halo node h); slot is where the record's transposed
+//         product goes (0xffff: a halo block, whose transpose lives in the
+//         other patch).  Records are warp-compacted: at step k of a warp, the
+//         lanes whose row has more than k records read consecutive records
+//         (position = warp base + records of the warp's earlier steps + active
+//         lanes below), so every record load is free of bank conflicts.
+//   slot: transposed products A_ji^T x_j of the upper blocks (j, i), i > j,
+//         gathered by row i, warp-compacted in the same way.
+//   xs, xh (contiguous): the vector on the patch rows and on the halo nodes;
+//   ds: a second patch vector (local solves); hnode: the halo nodes.
+constexpr size_t kOffF = 0;
+constexpr size_t kOffS = al16(kOffF + size_t(kMaxFwd) * 48);
+constexpr size_t kOffXs = al16(kOffS + size_t(kMaxSlots) * 16);
 constexpr size_t kOffXh = kOffXs + size_t(kMaxRows) * 16;
 constexpr size_t kOffDs = kOffXh + size_t(kMaxHaloNodes) * 16;
-constexpr size_t kResidentSmem = kOffDs + size_t(kMaxRows) * 16;
-static_assert(kResidentSmem <= 216 * 1024, "resident image exceeds shared memory");
+constexpr size_t kOffHnode = kOffDs + size_t(kMaxRows) * 16;
+constexpr size_t kResidentSmem = al16(kOffHnode + size_t(kMaxHaloNodes) * 4);
+static_assert(kResidentSmem <= 222 * 1024, "resident image exceeds shared memory");
 
 struct ResParams {
   int n_nodes, n_ctas, max_iter, degree, block_pc;
@@ -102,12 +109,12 @@ struct ResParams {
   const int *rowptr, *colidx;              // permuted pattern
   const float *A;                          // permuted FP32 blocks (as assembled)
   const int *tr;                           // block (j, i) of every block (i, j)
-  const int *uptr, *ublk;                  // upper patch-internal entries per row
-  const uint16_t *ucol;
-  const int *tptr;                         // transposed entries per row
-  const uint16_t *tupi, *trow;
-  const int *hptr, *hblk;                  // halo entries per row
-  const uint16_t *hwin;
+  const int *diag;                         // diagonal block of every row
+  const int *fptr;                         // first forward record of every patch
+  const int *fblk;                         // per record: source block (permuted)
+  const unsigned *fword;                   // per record: column | slot << 16
+  const int *rcnt;                         // per row: fi | ft << 8 | tc << 16
+  const int *wbase;                        // per (patch, warp): first record, first slot
   const int *hnptr, *hnode;                // halo nodes per patch
   const V4<double> *rhs;
   V4<double> *x64;
@@ -124,27 +131,19 @@ struct ResParams {
 };
 
 struct ResSmem {
-  float4 *uval;
-  float *hval;
-  unsigned *tp;
-  uint16_t *hwin, *uptr, *tptr, *hptr;
-  int *hnode;
+  float4 *fval, *slot;
   float4 *xs, *xh, *ds;
+  int *hnode;
 };
 
 __device__ __forceinline__ ResSmem carve(unsigned char *smem) {
   ResSmem m;
-  m.uval = reinterpret_cast<float4 *>(smem + kOffU);
-  m.hval = reinterpret_cast<float *>(smem + kOffH);
-  m.tp = reinterpret_cast<unsigned *>(smem + kOffTp);
-  m.hwin = reinterpret_cast<uint16_t *>(smem + kOffHwin);
-  m.uptr = reinterpret_cast<uint16_t *>(smem + kOffUptr);
-  m.tptr = reinterpret_cast<uint16_t *>(smem + kOffTptr);
-  m.hptr = reinterpret_cast<uint16_t *>(smem + kOffHptr);
-  m.hnode = reinterpret_cast<int *>(smem + kOffHnode);
+  m.fval = reinterpret_cast<float4 *>(smem + kOffF);
+  m.slot = reinterpret_cast<float4 *>(smem + kOffS);
   m.xs = reinterpret_cast<float4 *>(smem + kOffXs);
   m.xh = reinterpret_cast<float4 *>(smem + kOffXh);
   m.ds = reinterpret_cast<float4 *>(smem + kOffDs);
+  m.hnode = reinterpret_cast<int *>(smem + kOffHnode);
   return m;
 }
 
@@ -157,90 +156,99 @@ __device__ __forceinline__ void sym_block(const float *A, const int *tr, int k, 
     for (int c = 0; c < 3; ++c) dst[3 * r + c] = 0.5f * (__ldg(a + 3 * r + c) + __ldg(b + 3 * c + r));
 }
 
-// Copies this patch's lists and symmetrised blocks into shared memory.
-__device__ void load_patch(const ResParams &P, const ResSmem &sm, int cta, int p0, int np) {
-  const int i = threadIdx.x;
+// Per-thread data of the row's product: counts of its forward records
+// (patch-internal first, then halo) and of its transposed slots, the warp's
+// first record and slot, and the symmetric diagonal block in registers.
+struct RowMeta {
+  int fi, ft, tc;
+  int fbase, sbase;
+  float d[6];  // d00 d01 d02 d11 d12 d22
+};
+
+// Copies this patch's symmetrised blocks into shared memory and loads the
+// thread's row data.
+__device__ void load_patch(const ResParams &P, const ResSmem &sm, int cta, int p0, int np,
+                           RowMeta &M) {
+  const int i = threadIdx.x, warp = i >> 5;
+  const int f0 = P.fptr[cta], nrec = P.fptr[cta + 1] - f0;
+  for (int q = i; q < nrec; q += kRThreads) {
+    float v[9];
+    sym_block(P.A, P.tr, P.fblk[f0 + q], v);
+    float4 *rec = sm.fval + size_t(q) * 3;
+    rec[0] = make_float4(__uint_as_float(P.fword[f0 + q]), v[0], v[1], v[2]);
+    rec[1] = make_float4(v[3], v[4], v[5], v[6]);
+    rec[2] = make_float4(v[7], v[8], 0.f, 0.f);
+  }
+  M.fi = M.ft = M.tc = 0;
+  M.fbase = P.wbase[2 * (cta * kWarps + warp)];
+  M.sbase = P.wbase[2 * (cta * kWarps + warp) + 1];
+  for (int k = 0; k < 6; ++k) M.d[k] = 0.f;
   if (i < np) {
     const int row = p0 + i;
-    const int ub = P.uptr[p0], tb = P.tptr[p0], hb = P.hptr[p0];
-    const int u0 = P.uptr[row], u1 = P.uptr[row + 1];
-    sm.uptr[i] = uint16_t(u0 - ub);
-    for (int e = u0; e < u1; ++e) {
-      float v[9];
-      sym_block(P.A, P.tr, P.ublk[e], v);
-      float4 *rec = sm.uval + size_t(e - ub) * 3;
-      rec[0] = make_float4(__int_as_float(int(P.ucol[e])), v[0], v[1], v[2]);
-      rec[1] = make_float4(v[3], v[4], v[5], v[6]);
-      rec[2] = make_float4(v[7], v[8], 0.f, 0.f);
-    }
-    const int t0 = P.tptr[row], t1 = P.tptr[row + 1];
-    sm.tptr[i] = uint16_t(t0 - tb);
-    for (int t = t0; t < t1; ++t) sm.tp[t - tb] = unsigned(P.tupi[t]) | (unsigned(P.trow[t]) << 16);
-    const int h0 = P.hptr[row], h1 = P.hptr[row + 1];
-    sm.hptr[i] = uint16_t(h0 - hb);
-    for (int h = h0; h < h1; ++h) {
-      sym_block(P.A, P.tr, P.hblk[h], sm.hval + size_t(h - hb) * 9);
-      sm.hwin[h - hb] = P.hwin[h];
-    }
-    if (i == np - 1) {
-      sm.uptr[np] = uint16_t(u1 - ub);
-      sm.tptr[np] = uint16_t(t1 - tb);
-      sm.hptr[np] = uint16_t(h1 - hb);
-    }
+    const int c = P.rcnt[row];
+    M.fi = c & 0xff;
+    M.ft = (c >> 8) & 0xff;
+    M.tc = (c >> 16) & 0xff;
+    float D[9];
+    sym_block(P.A, P.tr, P.diag[row], D);
+    M.d[0] = D[0]; M.d[1] = D[1]; M.d[2] = D[2];
+    M.d[3] = D[4]; M.d[4] = D[5]; M.d[5] = D[8];
   }
   const int n0 = P.hnptr[cta], nh = P.hnptr[cta + 1] - n0;
   for (int h = threadIdx.x; h < nh; h += kRThreads) sm.hnode[h] = P.hnode[n0 + h];
 }
 
-__device__ __forceinline__ void fma_blk(const float *v, float4 x, float &a0, float &a1,
-                                        float &a2) {
-  a0 += v[0] * x.x + v[1] * x.y + v[2] * x.z;
-  a1 += v[3] * x.x + v[4] * x.y + v[5] * x.z;
-  a2 += v[6] * x.x + v[7] * x.y + v[8] * x.z;
-}
-
-// Block e of the upper storage: its 9 values and patch-local column.
-__device__ __forceinline__ int upper_block(const ResSmem &sm, int e, float (&v)[9]) {
-  const float4 q0 = sm.uval[3 * e], q1 = sm.uval[3 * e + 1], q2 = sm.uval[3 * e + 2];
-  v[0] = q0.y; v[1] = q0.z; v[2] = q0.w;
-  v[3] = q1.x; v[4] = q1.y; v[5] = q1.z; v[6] = q1.w;
-  v[7] = q2.x; v[8] = q2.y;
-  return __float_as_int(q0.x);
-}
-
-// Row i of A x: patch-internal part from xs, halo part from xh (kHalo).
+// Row i of A x for every thread of the CTA (threads without a row get 0):
+// diagonal block from registers, then the forward records (patch-internal
+// ones only when !kHalo), each also scattering its transposed product
+// A_ij^T x_i to the slot of row j; a CTA barrier; then the row's slots.
+// x: the vector image (xs, whose halo part xh follows it, or ds); xo: this
+// row's own entry of x.  Sum order: diagonal, forward records, slots (fixed:
+// results are reproducible run to run).
 template <bool kHalo>
-__device__ __forceinline__ float3 row_apply(const ResSmem &sm, int i, const float4 *xs,
-                                            const float4 *xh) {
-  float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+__device__ __forceinline__ float3 spmv(const ResSmem &sm, const RowMeta &M, const float4 *x,
+                                       float4 xo) {
+  const unsigned lt = (1u << (threadIdx.x & 31)) - 1u;
+  float a0 = M.d[0] * xo.x + M.d[1] * xo.y + M.d[2] * xo.z;
+  float a1 = M.d[1] * xo.x + M.d[3] * xo.y + M.d[4] * xo.z;
+  float a2 = M.d[2] * xo.x + M.d[4] * xo.y + M.d[5] * xo.z;
+  const int n = kHalo ? M.ft : M.fi;
+  const int kmax = __reduce_max_sync(0xffffffffu, n);
+  int base = M.fbase;
 #pragma unroll 2
-  for (int e = sm.uptr[i]; e < sm.uptr[i + 1]; ++e) {
-    const float4 q0 = sm.uval[3 * e];
-    const float4 x = xs[__float_as_int(q0.x)];
-    const float4 q1 = sm.uval[3 * e + 1], q2 = sm.uval[3 * e + 2];
-    a0 += q0.y * x.x + q0.z * x.y + q0.w * x.z;
-    a1 += q1.x * x.x + q1.y * x.y + q1.z * x.z;
-    a2 += q1.w * x.x + q2.x * x.y + q2.y * x.z;
+  for (int k = 0; k < kmax; ++k) {
+    const unsigned act = __ballot_sync(0xffffffffu, k < M.ft);
+    if (k < n) {
+      const int e = base + __popc(act & lt);
+      const float4 q0 = sm.fval[3 * e], q1 = sm.fval[3 * e + 1], q2 = sm.fval[3 * e + 2];
+      const unsigned w = __float_as_uint(q0.x);
+      const float4 xv = x[w & 0xffffu];
+      a0 += q0.y * xv.x + q0.z * xv.y + q0.w * xv.z;
+      a1 += q1.x * xv.x + q1.y * xv.y + q1.z * xv.z;
+      a2 += q1.w * xv.x + q2.x * xv.y + q2.y * xv.z;
+      const unsigned sl = w >> 16;
+      if (sl != 0xffffu)
+        sm.slot[sl] = make_float4(q0.y * xo.x + q1.x * xo.y + q1.w * xo.z,
+                                  q0.z * xo.x + q1.y * xo.y + q2.x * xo.z,
+                                  q0.w * xo.x + q1.z * xo.y + q2.y * xo.z, 0.f);
+    }
+    base += __popc(act);
   }
+  __syncthreads();
+  const int tmax = __reduce_max_sync(0xffffffffu, M.tc);
+  int sb = M.sbase;
 #pragma unroll 2
-  for (int t = sm.tptr[i]; t < sm.tptr[i + 1]; ++t) {
-    const unsigned w = sm.tp[t];
-    const int e = int(w & 0xffffu);
-    const float4 x = xs[w >> 16];
-    const float4 q0 = sm.uval[3 * e], q1 = sm.uval[3 * e + 1], q2 = sm.uval[3 * e + 2];
-    a0 += q0.y * x.x + q1.x * x.y + q1.w * x.z;
-    a1 += q0.z * x.x + q1.y * x.y + q2.x * x.z;
-    a2 += q0.w * x.x + q1.z * x.y + q2.y * x.z;
+  for (int k = 0; k < tmax; ++k) {
+    const unsigned act = __ballot_sync(0xffffffffu, k < M.tc);
+    if (k < M.tc) {
+      const float4 c = sm.slot[sb + __popc(act & lt)];
+      a0 += c.x; a1 += c.y; a2 += c.z;
+    }
+    sb += __popc(act);
   }
-  if (kHalo)
-    for (int h = sm.hptr[i]; h < sm.hptr[i + 1]; ++h)
-      fma_blk(sm.hval + size_t(h) * 9, xh[sm.hwin[h]], a0, a1, a2);
   return make_float3(a0, a1, a2);
 }
 
-// Row `row` of rhs - A x64 in FP64 arithmetic with the assembled FP32 blocks
-// (not the symmetrised resident image), masked: the reliable update measures
-// the residual of exactly the system every other solve path solves.
 __device__ __forceinline__ V4<double> true_residual(const ResParams &P, int row,
                                                    const V4<float> &m) {
   double a0 = 0.0, a1 = 0.0, a2 = 0.0;
@@ -389,7 +397,8 @@ __global__ void __launch_bounds__(kRThreads, 1) jacobi_resident_kernel(ResParams
   const int p0 = P.patch_row[cta], np = P.patch_row[cta + 1] - p0;
   const int nh = P.hnptr[cta + 1] - P.hnptr[cta];
   GridSum sync{P.part, P.bar, P.st, P.n_ctas, cta, 0u, 0};
-  load_patch(P, sm, cta, p0, np);
+  RowMeta M;
+  load_patch(P, sm, cta, p0, np, M);
   const bool own = i < np;
   const int row = p0 + i;
   V4<float> r{}, s{}, w{}, p{}, x{}, m{};
@@ -412,8 +421,8 @@ __global__ void __launch_bounds__(kRThreads, 1) jacobi_resident_kernel(ResParams
     if (own) sm.xs[i] = f4(u_);                                         \
     halo_u(P, sm, nh, cur, 0.f, 0.f, true);                             \
     __syncthreads();                                                    \
+    const float3 t_ = spmv<true>(sm, M, sm.xs, f4(u_));                 \
     if (own) {                                                          \
-      const float3 t_ = row_apply<true>(sm, i, sm.xs, sm.xh);           \
       w = V4<float>{t_.x * m.x, t_.y * m.y, t_.z * m.z, 0.f};           \
       P.w[cur][row] = w;                                                \
       g = A::addf(g, dot3(r, u_));                                      \
@@ -482,8 +491,8 @@ __global__ void __launch_bounds__(kRThreads, 1) jacobi_resident_kernel(ResParams
       sm.xh[i] = f4(hpc.apply(rj));
     }
     __syncthreads();
+    const float3 t = spmv<true>(sm, M, sm.xs, f4(un));
     if (own) {
-      const float3 t = row_apply<true>(sm, i, sm.xs, sm.xh);
       w = V4<float>{t.x * m.x, t.y * m.y, t.z * m.z, 0.f};
       P.w[nxt][row] = w;
       g2 = A::addf(g2, dot3(r, un));
@@ -514,12 +523,12 @@ __global__ void __launch_bounds__(kRThreads, 1) jacobi_resident_kernel(ResParams
     for (int h = threadIdx.x; h < nh; h += kRThreads) sm.xh[h] = f4(P.p[0][sm.hnode[h]]);
     __syncthreads();
     double rr64d = 0;
+    const float3 ts = spmv<true>(sm, M, sm.xs, f4(p));
     if (own) {
       const V4<double> q = true_residual(P, row, m);
       rr64d = q.x * q.x + q.y * q.y + q.z * q.z;
       r = V4<float>{float(q.x), float(q.y), float(q.z), 0.f};
-      const float3 t = row_apply<true>(sm, i, sm.xs, sm.xh);
-      s = V4<float>{t.x * m.x, t.y * m.y, t.z * m.z, 0.f};
+      s = V4<float>{ts.x * m.x, ts.y * m.y, ts.z * m.z, 0.f};
       P.r[cur][row] = r;
       P.s[cur][row] = s;
     }
@@ -555,8 +564,8 @@ struct LocalPC {
 };
 
 // z = S q(B^ A^) B^ S r on this row (CTA-wide: every thread takes part).
-__device__ V4<float> patch_apply(const ResSmem &sm, const LocalPC &L, bool own, int i, int k,
-                                 V4<float> r) {
+__device__ V4<float> patch_apply(const ResSmem &sm, const RowMeta &M, const LocalPC &L, bool own,
+                                 int i, int k, V4<float> r) {
   const float lo = L.lmax / kLoFrac;
   const float theta = 0.5f * (L.lmax + lo), delta = 0.5f * (L.lmax - lo);
   const float sigma = theta / delta;
@@ -568,10 +577,10 @@ __device__ V4<float> patch_apply(const ResSmem &sm, const LocalPC &L, bool own, 
   for (int st = 0; st < k; ++st) {
     y[0] += d[0]; y[1] += d[1]; y[2] += d[2];
     if (st == k - 1) break;
-    if (own) sm.ds[i] = make_float4(L.S[0] * d[0], L.S[1] * d[1], L.S[2] * d[2], 0.f);
+    const float4 dv = make_float4(L.S[0] * d[0], L.S[1] * d[1], L.S[2] * d[2], 0.f);
+    if (own) sm.ds[i] = dv;
     __syncthreads();
-    float3 t = make_float3(0.f, 0.f, 0.f);
-    if (own) t = row_apply<false>(sm, i, sm.ds, nullptr);
+    const float3 t = spmv<false>(sm, M, sm.ds, dv);
     __syncthreads();
     res[0] -= L.S[0] * t.x; res[1] -= L.S[1] * t.y; res[2] -= L.S[2] * t.z;
     const float rho1 = 1.f / (2.f * sigma - rho);
@@ -624,7 +633,8 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
   const int p0 = P.patch_row[cta], np = P.patch_row[cta + 1] - p0;
   const int nh = P.hnptr[cta + 1] - P.hnptr[cta];
   GridSum sync{P.part, P.bar, P.st, P.n_ctas, cta, 0u, 0};
-  load_patch(P, sm, cta, p0, np);
+  RowMeta M;
+  load_patch(P, sm, cta, p0, np, M);
   __syncthreads();
   const bool own = i < np;
   const int row = p0 + i;
@@ -637,12 +647,7 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
     r = P.r[0][row];
     m = P.fmask[row];
     const float mk[3] = {m.x, m.y, m.z};
-    float D[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    for (int e = sm.uptr[i]; e < sm.uptr[i + 1]; ++e) {
-      float v[9];
-      if (upper_block(sm, e, v) == i)
-        for (int k = 0; k < 9; ++k) D[k] = v[k];
-    }
+    const float D[9] = {M.d[0], M.d[1], M.d[2], M.d[1], M.d[3], M.d[4], M.d[2], M.d[4], M.d[5]};
     for (int c = 0; c < 3; ++c)
       L.S[c] = (mk[c] != 0.f && D[4 * c] > 0.f) ? 1.f / sqrtf(D[4 * c]) : 0.f;
     float Dh[9];
@@ -652,23 +657,21 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
     sm.ds[i] = make_float4(L.S[0], L.S[1], L.S[2], 0.f);
   }
   __syncthreads();
-  // l = infinity norm of B^ A^_pp (row sums of |B^_i S_i A_ij S_j|)
+  // l = infinity norm of B^ A^_pp (row sums of |B^_i S_i A_ij S_j| over the
+  // patch-internal blocks of the row, read once from the permuted matrix)
   float lrow = 0.f;
   if (own) {
     float acc[3] = {0.f, 0.f, 0.f};
-    const int e0 = sm.uptr[i], e1 = sm.uptr[i + 1], t0 = sm.tptr[i], t1 = sm.tptr[i + 1];
-    for (int q = e0; q < e1 + (t1 - t0); ++q) {
-      const bool tr = q >= e1;
-      const unsigned tw = tr ? sm.tp[t0 + q - e1] : 0u;
+    for (int k = P.rowptr[row]; k < P.rowptr[row + 1]; ++k) {
+      const int j = P.colidx[k] - p0;
+      if (j < 0 || j >= np) continue;
       float v[9];
-      const int col = upper_block(sm, tr ? int(tw & 0xffffu) : q, v);
-      const int j = tr ? int(tw >> 16) : col;
+      sym_block(P.A, P.tr, k, v);
       const float4 sj = sm.ds[j];
       const float Sj[3] = {sj.x, sj.y, sj.z};
       float h[9];
       for (int a = 0; a < 3; ++a)
-        for (int b = 0; b < 3; ++b)
-          h[3 * a + b] = (tr ? v[3 * b + a] : v[3 * a + b]) * (L.S[a] * Sj[b]);
+        for (int b = 0; b < 3; ++b) h[3 * a + b] = v[3 * a + b] * (L.S[a] * Sj[b]);
       for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 3; ++b)
           acc[a] += fabsf(L.B[3 * a] * h[b] + L.B[3 * a + 1] * h[3 + b] + L.B[3 * a + 2] * h[6 + b]);
@@ -697,7 +700,7 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
       hp = P.p[pf][hj];
     }
   };
-  z = patch_apply(sm, L, own, i, P.degree, r);
+  z = patch_apply(sm, M, L, own, i, P.degree, r);
   if (own) {
     P.z[row] = z;
     gam = A::addf(gam, dot3(r, z));
@@ -727,8 +730,8 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
     __syncthreads();
     V4<float> q{};
     V pq = A::zero(), e1 = A::zero(), e2 = A::zero();
+    const float3 t = spmv<true>(sm, M, sm.xs, f4(p));
     if (own) {
-      const float3 t = row_apply<true>(sm, i, sm.xs, sm.xh);
       q = V4<float>{t.x * m.x, t.y * m.y, t.z * m.z, 0.f};
       pq = A::addf(pq, dot3(p, q));
     }
@@ -742,7 +745,7 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
       r.x -= af * q.x; r.y -= af * q.y; r.z -= af * q.z;
       x.x += af * p.x; x.y += af * p.y; x.z += af * p.z;
     }
-    z = patch_apply(sm, L, own, i, P.degree, r);
+    z = patch_apply(sm, M, L, own, i, P.degree, r);
     V g2 = A::zero(), rr2 = A::zero(), e3 = A::zero();
     if (own) {
       P.z[row] = z;
@@ -772,7 +775,7 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
       rr64d = q.x * q.x + q.y * q.y + q.z * q.z;
       r = V4<float>{float(q.x), float(q.y), float(q.z), 0.f};
     }
-    z = patch_apply(sm, L, own, i, P.degree, r);
+    z = patch_apply(sm, M, L, own, i, P.degree, r);
     V rr64 = A::from_d(rr64d), g3 = A::zero(), e4 = A::zero();
     if (own) {
       P.z[row] = z;
@@ -834,7 +837,8 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
   const int p0 = P.patch_row[cta], np = P.patch_row[cta + 1] - p0;
   const int nh = P.hnptr[cta + 1] - P.hnptr[cta];
   GridSum sync{P.part, P.bar, P.st, P.n_ctas, cta, 0u, 0};
-  load_patch(P, sm, cta, p0, np);
+  RowMeta M;
+  load_patch(P, sm, cta, p0, np, M);
   const bool own = i < np;
   const int row = p0 + i;
   V4<float> r{}, z{}, p{}, x{}, m{};
@@ -899,8 +903,8 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
     __syncthreads();
     V4<float> q{};
     V pq = A::zero(), e1 = A::zero(), e2 = A::zero();
+    const float3 t = spmv<true>(sm, M, sm.xs, f4(p));
     if (own) {
-      const float3 t = row_apply<true>(sm, i, sm.xs, sm.xh);
       q = V4<float>{t.x * m.x, t.y * m.y, t.z * m.z, 0.f};
       P.q[row] = q;
       pq = A::addf(pq, dot3(p, q));
@@ -1111,9 +1115,9 @@ struct Bisector {
 
 struct PatchPlan {
   int G = 0;
-  std::vector<int> perm, rowptr, colidx, src, tr, diag, patch_row, uptr, ublk, tptr, hptr, hblk,
-      hnptr, hnode;
-  std::vector<uint16_t> ucol, tupi, trow, hwin;
+  std::vector<int> perm, rowptr, colidx, src, tr, diag, patch_row, hnptr, hnode;
+  std::vector<int> fptr, fblk, rcnt, wbase;  // shared-memory image (load_patch)
+  std::vector<unsigned> fword;
   std::vector<int16_t> bsl;   // per slice slot and lane: local row, or -1 - halo slot
   std::vector<int> gsrc;      // per slice slot and lane: block in the original order, or -1
   std::vector<int> slice_off, slice_len;  // per (patch, warp)
@@ -1166,35 +1170,31 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
   }
   std::vector<int> patch_row(G + 1, 0);
   for (int c = 0; c < G; ++c) patch_row[c + 1] = bounds[c];
-  // per-row lists
-  std::vector<int> uptr(N + 1, 0), ublk, tptr(N + 1, 0), hptr(N + 1, 0), hblk, hnptr(G + 1, 0),
-      hnode;
-  std::vector<uint16_t> ucol, tupi, trow, hwin;
-  std::vector<int> upos(NB, -1);  // patch-local index of an upper entry
-  std::vector<int> win(N, -1);    // window slot of an outside node (global index)
+  // shared-memory image of every patch: forward records and slots, both
+  // warp-compacted (step k of a warp holds the k-th entry of each of its rows
+  // that has more than k), per-row counts and per-warp bases
+  std::vector<int> fptr(G + 1, 0), fblk, rcnt(N, 0), wbase(size_t(G) * kWarps * 2, 0),
+      hnptr(G + 1, 0), hnode;
+  std::vector<unsigned> fword;
+  std::vector<int> win(N, -1);  // window slot of an outside node (global index)
   std::vector<int16_t> bmap(NB, 0);
   for (int c = 0; c < G; ++c) {
-    const int r0 = patch_row[c], r1 = patch_row[c + 1];
-    if (r1 - r0 > kMaxRows) return "patch too large";
-    const int ubase = int(ublk.size()), tbase = int(tupi.size()), hbase = int(hblk.size()),
-              nbase = int(hnode.size());
+    const int r0 = patch_row[c], r1 = patch_row[c + 1], np = r1 - r0;
+    if (np > kMaxRows) return "patch too large";
+    const int nbase = int(hnode.size());
+    // per row: forward entries (block, column) internal then halo; transposed
+    // entries (column j < row, ascending)
+    std::vector<std::vector<std::pair<int, int>>> fw(np);
+    std::vector<std::vector<int>> tcol(np);
+    std::vector<int> fi(np, 0);
     for (int i = r0; i < r1; ++i) {
-      uptr[i] = int(ublk.size());
-      for (int k = prow[i]; k < prow[i + 1]; ++k)
-        if (pcol[k] >= i && pcol[k] < r1) {
-          upos[k] = int(ublk.size()) - ubase;
-          ublk.push_back(k);
-          ucol.push_back(uint16_t(pcol[k] - r0));
-        }
-    }
-    for (int i = r0; i < r1; ++i) {
-      tptr[i] = int(tupi.size());
-      for (int k = prow[i]; k < prow[i + 1]; ++k)
-        if (pcol[k] >= r0 && pcol[k] < i) {
-          tupi.push_back(uint16_t(upos[ptr[k]]));  // block (j, i): an upper entry of row j
-          trow.push_back(uint16_t(pcol[k] - r0));
-        }
-      hptr[i] = int(hblk.size());
+      const int l = i - r0;
+      for (int k = prow[i]; k < prow[i + 1]; ++k) {
+        const int j = pcol[k];
+        if (j > i && j < r1) fw[l].push_back({k, j - r0});
+        if (j >= r0 && j < i) tcol[l].push_back(j - r0);
+      }
+      fi[l] = int(fw[l].size());
       for (int k = prow[i]; k < prow[i + 1]; ++k) {
         const int j = pcol[k];
         if (j >= r0 && j < r1) {
@@ -1205,19 +1205,53 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
           win[j] = int(hnode.size());
           hnode.push_back(j);
         }
-        hblk.push_back(k);
-        hwin.push_back(uint16_t(win[j] - nbase));
+        fw[l].push_back({k, kMaxRows + (win[j] - nbase)});
         bmap[k] = int16_t(-1 - (win[j] - nbase));
       }
+      if (int(fw[l].size()) > kMaxCount || int(tcol[l].size()) > kMaxCount)
+        return "patch exceeds the shared-memory image";
+      rcnt[i] = fi[l] | (int(fw[l].size()) << 8) | (int(tcol[l].size()) << 16);
     }
+    if (int(hnode.size()) - nbase > kMaxHaloNodes) return "patch exceeds the shared-memory image";
     hnptr[c + 1] = int(hnode.size());
-    if (int(ublk.size()) - ubase > kMaxUpper || int(tupi.size()) - tbase > kMaxUpper ||
-        int(hblk.size()) - hbase > kMaxHaloBlk || int(hnode.size()) - nbase > kMaxHaloNodes)
-      return "patch exceeds the shared-memory image";
+    // slot positions
+    std::vector<std::vector<int>> spos(np);
+    int nslot = 0;
+    for (int w = 0; w < kWarps; ++w) {
+      const int l0 = 32 * w, l1 = std::min(np, l0 + 32);
+      wbase[(size_t(c) * kWarps + w) * 2 + 1] = nslot;
+      int kmax = 0;
+      for (int l = l0; l < l1; ++l) kmax = std::max(kmax, int(tcol[l].size()));
+      for (int k = 0; k < kmax; ++k)
+        for (int l = l0; l < l1; ++l)
+          if (k < int(tcol[l].size())) spos[l].push_back(nslot++);
+    }
+    // forward records
+    int nrec = 0;
+    for (int w = 0; w < kWarps; ++w) {
+      const int l0 = 32 * w, l1 = std::min(np, l0 + 32);
+      wbase[(size_t(c) * kWarps + w) * 2] = nrec;
+      int kmax = 0;
+      for (int l = l0; l < l1; ++l) kmax = std::max(kmax, int(fw[l].size()));
+      for (int k = 0; k < kmax; ++k)
+        for (int l = l0; l < l1; ++l) {
+          if (k >= int(fw[l].size())) continue;
+          const int col = fw[l][k].second;
+          unsigned slot = 0xffffu;
+          if (col < kMaxRows) {  // upper block (l, col): the transposed entry of row col
+            const std::vector<int> &tc = tcol[col];
+            const int t = int(std::lower_bound(tc.begin(), tc.end(), l) - tc.begin());
+            if (t == int(tc.size()) || tc[t] != l) return "patch transpose lists disagree";
+            slot = unsigned(spos[col][t]);
+          }
+          fblk.push_back(fw[l][k].first);
+          fword.push_back(unsigned(col) | (slot << 16));
+          ++nrec;
+        }
+    }
+    if (nrec > kMaxFwd || nslot > kMaxSlots) return "patch exceeds the shared-memory image";
+    fptr[c + 1] = fptr[c] + nrec;
   }
-  uptr[N] = int(ublk.size());
-  tptr[N] = int(tupi.size());
-  hptr[N] = int(hblk.size());
   out.G = G;
   out.perm = std::move(perm);
   out.rowptr = std::move(prow);
@@ -1226,19 +1260,14 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
   out.tr = std::move(ptr);
   out.diag = std::move(pdiag);
   out.patch_row = std::move(patch_row);
-  out.uptr = std::move(uptr);
-  out.ublk = std::move(ublk);
-  out.ucol = std::move(ucol);
-  out.tptr = std::move(tptr);
-  out.tupi = std::move(tupi);
-  out.trow = std::move(trow);
-  out.hptr = std::move(hptr);
-  out.hblk = std::move(hblk);
-  out.hwin = std::move(hwin);
+  out.fptr = std::move(fptr);
+  out.fblk = std::move(fblk);
+  out.fword = std::move(fword);
+  out.rcnt = std::move(rcnt);
+  out.wbase = std::move(wbase);
   out.hnptr = std::move(hnptr);
   out.hnode = std::move(hnode);
   // warp slices of the pattern (for the learned G)
-  constexpr int kWarps = kRThreads / 32;
   out.slice_off.assign(size_t(G) * kWarps, 0);
   out.slice_len.assign(size_t(G) * kWarps, 0);
   int slots = 0;
@@ -1270,9 +1299,9 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
 struct PatchWork {
   int n_nodes = -1, n_blocks = -1, G = 0;
   std::string why;  // non-empty: the mesh does not fit
-  DevBuf<int> perm, rowptr, colidx, diag, tr, src, patch_row, uptr, ublk, tptr, hptr, hblk,
-      hnptr, hnode;
-  DevBuf<uint16_t> ucol, tupi, trow, hwin;
+  DevBuf<int> perm, rowptr, colidx, diag, tr, src, patch_row, fptr, fblk, rcnt, wbase, hnptr,
+      hnode;
+  DevBuf<unsigned> fword;
   DevBuf<int16_t> bsl;
   DevBuf<int> gsrc, slice_off, slice_len;
   DevBuf<float> Ap, Gs;
@@ -1316,19 +1345,16 @@ eolc_status patch_plan(PatchWork *w, const DevTopology &Tp, const double *X_d, i
   w->why = build_patch_plan(N, rowptr, colidx, X.empty() ? nullptr : &X, n_sm, L);
   if (!w->why.empty()) return EOLC_OK;
   // empty lists (e.g. no halo on a one-patch mesh) still get one element
-  for (auto *v : {&L.ublk, &L.hblk, &L.hnode})
+  for (auto *v : {&L.fblk, &L.hnode})
     if (v->empty()) v->push_back(0);
-  for (auto *v : {&L.ucol, &L.tupi, &L.trow, &L.hwin})
-    if (v->empty()) v->push_back(0);
+  if (L.fword.empty()) L.fword.push_back(0u);
   cudaError_t es[] = {
       upload_vec(w->perm, L.perm, s), upload_vec(w->rowptr, L.rowptr, s),
       upload_vec(w->colidx, L.colidx, s), upload_vec(w->diag, L.diag, s),
       upload_vec(w->tr, L.tr, s), upload_vec(w->src, L.src, s),
-      upload_vec(w->patch_row, L.patch_row, s), upload_vec(w->uptr, L.uptr, s),
-      upload_vec(w->ublk, L.ublk, s), upload_vec(w->ucol, L.ucol, s),
-      upload_vec(w->tptr, L.tptr, s), upload_vec(w->tupi, L.tupi, s),
-      upload_vec(w->trow, L.trow, s), upload_vec(w->hptr, L.hptr, s),
-      upload_vec(w->hblk, L.hblk, s), upload_vec(w->hwin, L.hwin, s),
+      upload_vec(w->patch_row, L.patch_row, s), upload_vec(w->fptr, L.fptr, s),
+      upload_vec(w->fblk, L.fblk, s), upload_vec(w->fword, L.fword, s),
+      upload_vec(w->rcnt, L.rcnt, s), upload_vec(w->wbase, L.wbase, s),
       upload_vec(w->hnptr, L.hnptr, s), upload_vec(w->hnode, L.hnode, s),
       upload_vec(w->bsl, L.bsl, s), upload_vec(w->gsrc, L.gsrc, s),
       upload_vec(w->slice_off, L.slice_off, s), upload_vec(w->slice_len, L.slice_len, s),
@@ -1439,15 +1465,12 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, i
   P.colidx = w->colidx.p;
   P.A = w->Ap.p;
   P.tr = w->tr.p;
-  P.uptr = w->uptr.p;
-  P.ublk = w->ublk.p;
-  P.ucol = w->ucol.p;
-  P.tptr = w->tptr.p;
-  P.tupi = w->tupi.p;
-  P.trow = w->trow.p;
-  P.hptr = w->hptr.p;
-  P.hblk = w->hblk.p;
-  P.hwin = w->hwin.p;
+  P.diag = w->diag.p;
+  P.fptr = w->fptr.p;
+  P.fblk = w->fblk.p;
+  P.fword = w->fword.p;
+  P.rcnt = w->rcnt.p;
+  P.wbase = w->wbase.p;
   P.hnptr = w->hnptr.p;
   P.hnode = w->hnode.p;
   P.rhs = rhs;

@@ -125,6 +125,8 @@ struct ResParams {
                                            // -1 - halo window slot
   const int *slice_off, *slice_len;        // per (CTA, warp) slice: first slot, slots
   V4<float> *r[2], *s[2], *w[2], *p[2], *z, *q;
+  unsigned long long *tw;                  // learned PCG: epoch-tagged u, [2][N][4] words
+  unsigned seq;                            // launch number in the tags (1..4095)
   double *part;
   unsigned *bar;
   DevStatus *st;
@@ -162,6 +164,7 @@ __device__ __forceinline__ void sym_block(const float *A, const int *tr, int k, 
 struct RowMeta {
   int fi, ft, tc;
   int fbase, sbase;
+  bool bnd;    // the row is a halo node of another patch
   float d[6];  // d00 d01 d02 d11 d12 d22
 };
 
@@ -180,6 +183,7 @@ __device__ void load_patch(const ResParams &P, const ResSmem &sm, int cta, int p
     rec[2] = make_float4(v[7], v[8], 0.f, 0.f);
   }
   M.fi = M.ft = M.tc = 0;
+  M.bnd = false;
   M.fbase = P.wbase[2 * (cta * kWarps + warp)];
   M.sbase = P.wbase[2 * (cta * kWarps + warp) + 1];
   for (int k = 0; k < 6; ++k) M.d[k] = 0.f;
@@ -189,6 +193,7 @@ __device__ void load_patch(const ResParams &P, const ResSmem &sm, int cta, int p
     M.fi = c & 0xff;
     M.ft = (c >> 8) & 0xff;
     M.tc = (c >> 16) & 0xff;
+    M.bnd = (c >> 24) & 1;
     float D[9];
     sym_block(P.A, P.tr, P.diag[row], D);
     M.d[0] = D[0]; M.d[1] = D[1]; M.d[2] = D[2];
@@ -800,15 +805,61 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
 }
 
 // ---- PCG with the learned approximate inverse G (pattern of A) ----------------
-// G is read from global memory (L2) in the order of the permuted pattern; A is
-// the resident image.  z = G r needs r on the halo: r_j - alpha q_j is
-// recomputed from the neighbours' r of the last step and q of this step, so
-// an iteration keeps two grid barriers (p'q, then r'z and r'r).
-// Row of this thread of G r.  G is stored in warp slices: the rows of warp w
-// of CTA c form slice 16 c + w; slot k of the slice holds the k-th block of
-// each of the 32 rows, component-major and lane-contiguous
-// (Gs[((off + k) * 9 + comp) * 32 + lane]), zero-padded to the slice's
-// longest row, so every load of the warp is one coalesced 128-byte line.
+// Single-reduction Chronopoulos-Gear PCG with u = G r, w = A u.  G couples a
+// row to its matrix neighbours, so u = G r needs r on the halo (recomputed
+// as r_j - alpha (w_j + beta s_j) from the neighbours' r, s, w of the last
+// step, prefetched after the grid barrier) and w = A u needs u on the halo,
+// two rings out: each patch publishes u of its boundary rows as epoch-tagged
+// 64-bit words (value | tag << 32, tag = launch number << 20 | epoch),
+// double-buffered by the epoch's parity, and the neighbours poll them.  One
+// grid barrier and one neighbour exchange per iteration.  Two buffers
+// suffice: a patch publishes epoch e + 2 only after the grid reduction that
+// follows the exchange of e + 1, which every patch joins after its read of
+// e.  G is read from global memory (L2); A is the resident image.
+__device__ __forceinline__ void ld_tag2(const unsigned long long *p, unsigned long long &a,
+                                        unsigned long long &b) {
+  asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];"
+               : "=l"(a), "=l"(b)
+               : "l"(p)
+               : "memory");
+}
+__device__ __forceinline__ void st_tag2(unsigned long long *p, unsigned long long a,
+                                        unsigned long long b) {
+  asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(a), "l"(b)
+               : "memory");
+}
+__device__ __forceinline__ unsigned long long tag_word(unsigned tag, float v) {
+  return (static_cast<unsigned long long>(tag) << 32) | __float_as_uint(v);
+}
+__device__ __forceinline__ unsigned tag_of(unsigned long long w) { return unsigned(w >> 32); }
+__device__ __forceinline__ float tag_val(unsigned long long w) {
+  return __uint_as_float(unsigned(w & 0xffffffffull));
+}
+__device__ __forceinline__ unsigned exch_tag(unsigned seq, unsigned epoch) {
+  return (seq << 20) | (epoch & 0xfffffu);
+}
+__device__ __forceinline__ void publish_tagged(unsigned long long *tw, int N, int row,
+                                               unsigned tag, const V4<float> &v) {
+  unsigned long long *q = tw + (size_t(tag & 1u) * N + row) * 4;
+  st_tag2(q, tag_word(tag, v.x), tag_word(tag, v.y));
+  st_tag2(q + 2, tag_word(tag, v.z), tag_word(tag, 0.f));
+}
+// Polls node's words until they carry the tag; false after kSpinLimit polls.
+__device__ __forceinline__ bool poll_tagged(const unsigned long long *tw, int N, int node,
+                                            unsigned tag, V4<float> &v) {
+  const unsigned long long *q = tw + (size_t(tag & 1u) * N + node) * 4;
+  for (long long spin = 0; spin < kSpinLimit; ++spin) {
+    unsigned long long a, b, c, d;
+    ld_tag2(q, a, b);
+    ld_tag2(q + 2, c, d);
+    if (tag_of(a) == tag && tag_of(b) == tag && tag_of(c) == tag) {
+      v = V4<float>{tag_val(a), tag_val(b), tag_val(c), 0.f};
+      return true;
+    }
+  }
+  return false;
+}
+
 __device__ __forceinline__ V4<float> apply_G(const ResParams &P, const ResSmem &sm, int cta) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int sl = cta * (kRThreads / 32) + warp;
@@ -832,151 +883,166 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
   using V = A::V;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ V red[3 * (kRThreads / 32 + 1)];
+  __shared__ int s_fail;
   const ResSmem sm = carve(smem);
   const int cta = blockIdx.x, i = threadIdx.x;
   const int p0 = P.patch_row[cta], np = P.patch_row[cta + 1] - p0;
   const int nh = P.hnptr[cta + 1] - P.hnptr[cta];
+  const int N = P.n_nodes;
   GridSum sync{P.part, P.bar, P.st, P.n_ctas, cta, 0u, 0};
   RowMeta M;
   load_patch(P, sm, cta, p0, np, M);
   const bool own = i < np;
   const int row = p0 + i;
-  V4<float> r{}, z{}, p{}, x{}, m{};
+  V4<float> r{}, s{}, w{}, p{}, x{}, u{}, m{};
   if (own) {
     r = P.r[0][row];
     m = P.fmask[row];
   }
+  if (i == 0) s_fail = 0;
+  // this thread's halo node (at most one) and its r, s, w of the last step,
+  // prefetched right after each grid barrier
+  const int hj = i < nh ? sm.hnode[i] : -1;
+  V4<float> hr{}, hs{}, hw{};
+  int pf = 0;
+  const auto prefetch = [&]() {
+    if (hj >= 0) {
+      hr = P.r[pf][hj];
+      hs = P.s[pf][hj];
+      hw = P.w[pf][hj];
+    }
+  };
   const V tol2 = A::from_d(P.tol2 * __ldcg(&P.st->rhs_norm2));
   const V delta2 = A::from_d(kDelta * kDelta);
-  int cur = 0;  // r[cur], p[cur]: the neighbours' values of the last step
-  // z = G r for the published r[cur] (start, and after a reliable update)
-  V gam = A::zero(), rr = A::zero(), e0 = A::zero();
+  unsigned epoch = 0;
+  int cur = 0;
+  __syncthreads();  // the resident image is complete
+  // u = G r (xs / xh hold r), u exchanged with the neighbours, w = A u
+  // published to w[c]; then the dots of this step
+#define EOLC_LPC_UW(c, g, d, q)                                            \
+  do {                                                                     \
+    __syncthreads();                                                       \
+    if (own) {                                                             \
+      const V4<float> g_ = apply_G(P, sm, cta);                            \
+      u = V4<float>{g_.x * m.x, g_.y * m.y, g_.z * m.z, 0.f};              \
+    }                                                                      \
+    __syncthreads();                                                       \
+    epoch += 1u;                                                           \
+    const unsigned tag_ = exch_tag(P.seq, epoch);                          \
+    if (own) {                                                             \
+      sm.xs[i] = f4(u);                                                    \
+      if (M.bnd) publish_tagged(P.tw, N, row, tag_, u);                    \
+    }                                                                      \
+    if (hj >= 0) {                                                         \
+      V4<float> uj{};                                                      \
+      if (!poll_tagged(P.tw, N, hj, tag_, uj)) {                           \
+        atomicCAS(&P.st->status, EOLC_OK, EOLC_TIMEOUT);                   \
+        s_fail = 1;                                                        \
+      }                                                                    \
+      sm.xh[i] = f4(uj);                                                   \
+    }                                                                      \
+    __syncthreads();                                                       \
+    const float3 t_ = spmv<true>(sm, M, sm.xs, f4(u));                     \
+    if (own) {                                                             \
+      w = V4<float>{t_.x * m.x, t_.y * m.y, t_.z * m.z, 0.f};              \
+      P.w[c][row] = w;                                                     \
+      g = A::addf(g, dot3(r, u));                                          \
+      d = A::addf(d, dot3(w, u));                                          \
+      q = A::addf(q, dot3(r, r));                                          \
+    }                                                                      \
+  } while (0)
+  V gam = A::zero(), del = A::zero(), rr = A::zero();
   if (own) sm.xs[i] = f4(r);
-  for (int h = threadIdx.x; h < nh; h += kRThreads) sm.xh[h] = f4(P.r[cur][sm.hnode[h]]);
-  __syncthreads();
-  // this thread's halo node (at most one); after the grid barrier that
-  // precedes their use, its z and p (step top) or r and q (residual update)
-  // of the last phase are prefetched
-  const int hj = i < nh ? sm.hnode[i] : -1;
-  V4<float> ha{}, hb{};
-  int pf = 0;
-  const auto prefetch_zp = [&]() {
-    if (hj >= 0) {
-      ha = P.z[hj];
-      hb = P.p[pf][hj];
-    }
-  };
-  const auto prefetch_rq = [&]() {
-    if (hj >= 0) {
-      ha = P.r[pf][hj];
-      hb = P.q[hj];
-    }
-  };
-  if (own) {
-    const V4<float> g = apply_G(P, sm, cta);
-    z = V4<float>{g.x * m.x, g.y * m.y, g.z * m.z, 0.f};
-    P.z[row] = z;
-    gam = A::addf(gam, dot3(r, z));
-    rr = A::addf(rr, dot3(r, r));
-  }
+  if (hj >= 0) sm.xh[i] = f4(P.r[cur][hj]);
+  EOLC_LPC_UW(cur, gam, del, rr);
   pf = cur;
-  if (!sync(gam, rr, e0, red, prefetch_zp)) return;
+  if (!sync(gam, del, rr, red, prefetch)) return;
+  if (s_fail) return;  // a neighbour exchange timed out (status recorded)
   V rmax2 = rr;
   double last_rr64 = A::to_d(rr);
   int it = 0, nref = 0, status = EOLC_NOT_CONVERGED;
   bool converged = A::finite(rr) && A::le(rr, tol2);
-  if (!A::finite(rr) || !A::finite(gam)) status = EOLC_NONFINITE;
-  V gam_old = A::from_d(1.0);
+  if (!A::finite(rr)) status = EOLC_NONFINITE;
+  V gam_old = A::from_d(1.0), alpha_old = A::from_d(1.0);
   bool restart = true;
   while (!converged && status != EOLC_NONFINITE && it < P.max_iter) {
     const V beta = restart ? A::zero() : A::div(gam, gam_old);
-    const float bf = float(A::to_t(beta));
-    restart = false;
-    const int nxt = cur ^ 1;
-    // p = z + beta p, q = A p
-    if (own) {
-      p = V4<float>{z.x + bf * p.x, z.y + bf * p.y, z.z + bf * p.z, 0.f};
-      P.p[nxt][row] = p;
-      sm.xs[i] = f4(p);
-    }
-    if (hj >= 0) sm.xh[i] = make_float4(ha.x + bf * hb.x, ha.y + bf * hb.y, ha.z + bf * hb.z, 0.f);
-    __syncthreads();
-    V4<float> q{};
-    V pq = A::zero(), e1 = A::zero(), e2 = A::zero();
-    const float3 t = spmv<true>(sm, M, sm.xs, f4(p));
-    if (own) {
-      q = V4<float>{t.x * m.x, t.y * m.y, t.z * m.z, 0.f};
-      P.q[row] = q;
-      pq = A::addf(pq, dot3(p, q));
-    }
-    pf = cur;
-    if (!sync(pq, e1, e2, red, prefetch_rq)) return;
-    if (!A::pos(pq) || !A::pos(gam)) {
-      status = (A::finite(pq) && A::finite(gam)) ? EOLC_BREAKDOWN : EOLC_NONFINITE;
+    const V denom = restart ? del : A::add(del, A::neg(A::div(A::mul(beta, gam), alpha_old)));
+    if (!A::pos(denom) || !A::pos(gam)) {
+      status = (A::finite(denom) && A::finite(gam)) ? EOLC_BREAKDOWN : EOLC_NONFINITE;
       break;
     }
-    const float af = float(A::to_t(A::div(gam, pq)));
-    // r -= alpha q (own rows, and recomputed on the halo); z = G r
+    const V alpha = A::div(gam, denom);
+    const float af = float(A::to_t(alpha)), bf = float(A::to_t(beta));
+    restart = false;
+    const int nxt = cur ^ 1;
     if (own) {
-      r.x -= af * q.x; r.y -= af * q.y; r.z -= af * q.z;
+      s = V4<float>{w.x + bf * s.x, w.y + bf * s.y, w.z + bf * s.z, 0.f};
+      r = V4<float>{r.x - af * s.x, r.y - af * s.y, r.z - af * s.z, 0.f};
+      p = V4<float>{u.x + bf * p.x, u.y + bf * p.y, u.z + bf * p.z, 0.f};
       x.x += af * p.x; x.y += af * p.y; x.z += af * p.z;
       P.r[nxt][row] = r;
+      P.s[nxt][row] = s;
       sm.xs[i] = f4(r);
     }
-    if (hj >= 0) sm.xh[i] = make_float4(ha.x - af * hb.x, ha.y - af * hb.y, ha.z - af * hb.z, 0.f);
-    __syncthreads();
-    V g2 = A::zero(), rr2 = A::zero(), e3 = A::zero();
-    if (own) {
-      const V4<float> g = apply_G(P, sm, cta);
-      z = V4<float>{g.x * m.x, g.y * m.y, g.z * m.z, 0.f};
-      P.z[row] = z;
-      g2 = A::addf(g2, dot3(r, z));
-      rr2 = A::addf(rr2, dot3(r, r));
+    if (hj >= 0) {  // r_j - alpha (w_j + beta s_j) from the prefetch
+      sm.xh[i] = make_float4(hr.x - af * (hw.x + bf * hs.x), hr.y - af * (hw.y + bf * hs.y),
+                             hr.z - af * (hw.z + bf * hs.z), 0.f);
     }
+    V g2 = A::zero(), d2 = A::zero(), rr2 = A::zero();
+    EOLC_LPC_UW(nxt, g2, d2, rr2);
     pf = nxt;
-    if (!sync(g2, rr2, e3, red, prefetch_zp)) return;
+    if (!sync(g2, d2, rr2, red, prefetch)) return;
+    if (s_fail) return;
     ++it;
     cur = nxt;
     gam_old = gam;
+    alpha_old = alpha;
     gam = g2;
+    del = d2;
     rr = rr2;
-    if (!A::finite(rr) || !A::finite(gam)) { status = EOLC_NONFINITE; break; }
+    if (!A::finite(rr) || !A::finite(gam) || !A::finite(del)) { status = EOLC_NONFINITE; break; }
     if (!(A::lt(rr, A::mul(delta2, rmax2)) || A::le(rr, tol2) || it >= P.max_iter)) continue;
-    // ---- reliable update: x64 += x; r = rhs - A x64 (FP64); z = G r --------
+    // ---- reliable update: x64 += x; r = rhs - A x64 (FP64); s = A p --------
     if (own) {
       V4<double> xd = P.x64[row];
       xd.x += double(x.x); xd.y += double(x.y); xd.z += double(x.z);
       P.x64[row] = xd;
       x = V4<float>{0.f, 0.f, 0.f, 0.f};
+      P.p[0][row] = p;
+      sm.xs[i] = f4(p);
     }
     if (!sync.barrier()) return;
+    if (hj >= 0) sm.xh[i] = f4(P.p[0][hj]);
+    __syncthreads();
     double rr64d = 0;
+    const float3 ts = spmv<true>(sm, M, sm.xs, f4(p));
     if (own) {
       const V4<double> qd = true_residual(P, row, m);
       rr64d = qd.x * qd.x + qd.y * qd.y + qd.z * qd.z;
       r = V4<float>{float(qd.x), float(qd.y), float(qd.z), 0.f};
+      s = V4<float>{ts.x * m.x, ts.y * m.y, ts.z * m.z, 0.f};
       P.r[cur][row] = r;
-      sm.xs[i] = f4(r);
+      P.s[cur][row] = s;
     }
-    if (!sync.barrier()) return;  // the replaced residuals are published
-    for (int h = threadIdx.x; h < nh; h += kRThreads) sm.xh[h] = f4(P.r[cur][sm.hnode[h]]);
-    __syncthreads();
-    V rr64 = A::from_d(rr64d), g3 = A::zero(), e4 = A::zero();
-    if (own) {
-      const V4<float> g = apply_G(P, sm, cta);
-      z = V4<float>{g.x * m.x, g.y * m.y, g.z * m.z, 0.f};
-      P.z[row] = z;
-      g3 = A::addf(g3, dot3(r, z));
-    }
-    pf = cur;
-    if (!sync(rr64, g3, e4, red, prefetch_zp)) return;
+    V e0 = A::from_d(rr64d), e1 = A::zero(), e2 = A::zero();
+    if (!sync(e0, e1, e2, red)) return;  // also publishes r, s
     ++nref;
-    last_rr64 = A::to_d(rr64);
-    rmax2 = rr64;
+    last_rr64 = A::to_d(e0);
+    rmax2 = e0;
+    if (!A::finite(e0)) { status = EOLC_NONFINITE; break; }
+    if (A::le(e0, tol2)) { converged = true; break; }
+    V g3 = A::zero(), d3 = A::zero(), rr3 = A::zero();
+    if (own) sm.xs[i] = f4(r);
+    if (hj >= 0) sm.xh[i] = f4(P.r[cur][hj]);
+    EOLC_LPC_UW(cur, g3, d3, rr3);
+    pf = cur;
+    if (!sync(g3, d3, rr3, red, prefetch)) return;
+    if (s_fail) return;
     gam = g3;
-    if (!A::finite(rr64) || !A::finite(gam)) { status = EOLC_NONFINITE; break; }
-    if (A::le(rr64, tol2)) { converged = true; break; }
+    del = d3;
   }
+#undef EOLC_LPC_UW
   if (converged) status = EOLC_OK;
   if (cta == 0 && threadIdx.x == 0) {
     atomicCAS(&P.st->status, EOLC_OK, status);
@@ -1252,6 +1318,7 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
     if (nrec > kMaxFwd || nslot > kMaxSlots) return "patch exceeds the shared-memory image";
     fptr[c + 1] = fptr[c] + nrec;
   }
+  for (int j : hnode) rcnt[j] |= 1 << 24;  // a halo node of some patch: it publishes
   out.G = G;
   out.perm = std::move(perm);
   out.rowptr = std::move(prow);
@@ -1302,6 +1369,8 @@ struct PatchWork {
   DevBuf<int> perm, rowptr, colidx, diag, tr, src, patch_row, fptr, fblk, rcnt, wbase, hnptr,
       hnode;
   DevBuf<unsigned> fword;
+  DevBuf<unsigned long long> tw;  // learned PCG: tagged halo values, zeroed once per plan
+  unsigned seq = 0;               // launches (tag generation)
   DevBuf<int16_t> bsl;
   DevBuf<int> gsrc, slice_off, slice_len;
   DevBuf<float> Ap, Gs;
@@ -1365,6 +1434,8 @@ eolc_status patch_plan(PatchWork *w, const DevTopology &Tp, const double *X_d, i
       w->bp.resize(size_t(N) * 3),
       w->beqp.resize(size_t(N) * 3),
       w->part.resize(size_t(6) * L.G),
+      w->tw.resize(size_t(8) * N),
+      cudaMemsetAsync(w->tw.p, 0, sizeof(unsigned long long) * 8 * size_t(N), s),
       w->bar.resize(2),
       w->st.resize(1),
       cudaStreamSynchronize(s)};
@@ -1481,6 +1552,9 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, i
   P.bsl = w->bsl.p;
   P.slice_off = w->slice_off.p;
   P.slice_len = w->slice_len.p;
+  P.tw = w->tw.p;
+  w->seq = w->seq % 4095u + 1u;  // 1..4095: a tag never equals the zeroed words
+  P.seq = w->seq;
   P.part = w->part.p;
   P.bar = w->bar.p;
   P.st = w->st.p;

@@ -18,12 +18,13 @@
 //     (halo exchange) go through global memory, ping-ponged so that no
 //     write races a read in the same phase.
 //
-// Two solvers run on this layout:
-//   jacobi_resident_kernel  the single-barrier Chronopoulos-Gear PCG of the
-//                           streamed kernel (pcg.cu) with point or block
-//                           Jacobi: halo values of u = M r' are recomputed
-//                           from the neighbours' r, s, w of the last step;
-//   patch_resident_kernel   PCG with the patch-local preconditioner
+// Three solvers run on this layout, all the single-barrier
+// Chronopoulos-Gear PCG of the streamed kernel (pcg.cu): one grid-wide
+// reduction (r.u, w.u, r.r) per iteration, with u = M r and w = A u:
+//   jacobi_resident_kernel  point or block Jacobi: halo values of u are
+//                           recomputed from the neighbours' r, s, w of the
+//                           last step;
+//   patch_resident_kernel   the patch-local preconditioner
 //                           M = blockdiag_p( S q_p(B^ A^_pp) B^ S ): a degree-k
 //                           Chebyshev polynomial of the block-Jacobi-
 //                           preconditioned, unit-diagonal-scaled patch matrix
@@ -31,8 +32,10 @@
 //                           infinity norm of B^ A^_pp (an upper bound of its
 //                           spectrum, so q_p > 0 there and M is symmetric
 //                           positive definite).  Local solves use CTA barriers
-//                           only; an iteration has two grid barriers.
-// Both take FP32 values and vectors, double-float inner products and FP64
+//                           only; u reaches the neighbours through the
+//                           epoch-tagged neighbour exchange (no grid barrier);
+//   learned_resident_kernel the learned approximate inverse G (below).
+// All take FP32 values and vectors, double-float inner products and FP64
 // reliable updates (the true residual rhs - A x64 in FP64 arithmetic), so
 // convergence is declared on the same FP64 relative residual as every other
 // solve.  The resident image holds each block pair (i, j), (j, i) averaged to
@@ -125,7 +128,7 @@ struct ResParams {
                                            // -1 - halo window slot
   const int *slice_off, *slice_len;        // per (CTA, warp) slice: first slot, slots
   V4<float> *r[2], *s[2], *w[2], *p[2], *z, *q;
-  unsigned long long *tw;                  // learned PCG: epoch-tagged u, [2][N][4] words
+  unsigned long long *tw;                  // neighbour exchange: tagged u, [2][N][4] words
   unsigned seq;                            // launch number in the tags (1..4095)
   double *part;
   unsigned *bar;
@@ -561,6 +564,58 @@ __global__ void __launch_bounds__(kRThreads, 1) jacobi_resident_kernel(ResParams
   }
 }
 
+// ---- epoch-tagged neighbour exchange -------------------------------------------
+// A patch publishes a vector on its boundary rows as 64-bit words (value |
+// tag << 32; tag = launch number << 20 | epoch), double-buffered by the
+// epoch's parity, and the neighbour patches poll the words of their halo
+// nodes: no grid barrier.  Two buffers suffice when a grid-wide reduction
+// separates consecutive exchanges: a patch publishes epoch e + 2 only after
+// the reduction that follows the exchange of e + 1, which every patch joins
+// after its read of e.
+__device__ __forceinline__ void ld_tag2(const unsigned long long *p, unsigned long long &a,
+                                        unsigned long long &b) {
+  asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];"
+               : "=l"(a), "=l"(b)
+               : "l"(p)
+               : "memory");
+}
+__device__ __forceinline__ void st_tag2(unsigned long long *p, unsigned long long a,
+                                        unsigned long long b) {
+  asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(a), "l"(b)
+               : "memory");
+}
+__device__ __forceinline__ unsigned long long tag_word(unsigned tag, float v) {
+  return (static_cast<unsigned long long>(tag) << 32) | __float_as_uint(v);
+}
+__device__ __forceinline__ unsigned tag_of(unsigned long long w) { return unsigned(w >> 32); }
+__device__ __forceinline__ float tag_val(unsigned long long w) {
+  return __uint_as_float(unsigned(w & 0xffffffffull));
+}
+__device__ __forceinline__ unsigned exch_tag(unsigned seq, unsigned epoch) {
+  return (seq << 20) | (epoch & 0xfffffu);
+}
+__device__ __forceinline__ void publish_tagged(unsigned long long *tw, int N, int row,
+                                               unsigned tag, const V4<float> &v) {
+  unsigned long long *q = tw + (size_t(tag & 1u) * N + row) * 4;
+  st_tag2(q, tag_word(tag, v.x), tag_word(tag, v.y));
+  st_tag2(q + 2, tag_word(tag, v.z), tag_word(tag, 0.f));
+}
+// Polls node's words until they carry the tag; false after kSpinLimit polls.
+__device__ __forceinline__ bool poll_tagged(const unsigned long long *tw, int N, int node,
+                                            unsigned tag, V4<float> &v) {
+  const unsigned long long *q = tw + (size_t(tag & 1u) * N + node) * 4;
+  for (long long spin = 0; spin < kSpinLimit; ++spin) {
+    unsigned long long a, b, c, d;
+    ld_tag2(q, a, b);
+    ld_tag2(q + 2, c, d);
+    if (tag_of(a) == tag && tag_of(b) == tag && tag_of(c) == tag) {
+      v = V4<float>{tag_val(a), tag_val(b), tag_val(c), 0.f};
+      return true;
+    }
+  }
+  return false;
+}
+
 // ---- PCG with the patch-local Chebyshev preconditioner ------------------------
 struct LocalPC {
   float S[3];
@@ -633,6 +688,7 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ V red[3 * (kRThreads / 32 + 1)];
   __shared__ float s_max[kRThreads / 32];
+  __shared__ int s_fail;
   const ResSmem sm = carve(smem);
   const int cta = blockIdx.x, i = threadIdx.x;
   const int p0 = P.patch_row[cta], np = P.patch_row[cta + 1] - p0;
@@ -643,7 +699,7 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
   __syncthreads();
   const bool own = i < np;
   const int row = p0 + i;
-  V4<float> r{}, z{}, p{}, x{}, m{};
+  V4<float> r{}, p{}, x{}, m{};
   LocalPC L;
   for (int c = 0; c < 3; ++c) L.S[c] = 0.f;
   for (int k = 0; k < 9; ++k) L.B[k] = 0.f;
@@ -693,108 +749,113 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
 
   const V tol2 = A::from_d(P.tol2 * __ldcg(&P.st->rhs_norm2));
   const V delta2 = A::from_d(kDelta * kDelta);
-  V gam = A::zero(), rr = A::zero(), e0 = A::zero();
-  // this thread's halo node (at most one) and its z, p of the last step,
-  // prefetched right after the grid barrier that precedes their use
+  const int N = P.n_nodes;
   const int hj = i < nh ? sm.hnode[i] : -1;
-  V4<float> hz{}, hp{};
-  int pf = 0;  // index of p the prefetch reads
-  const auto prefetch = [&]() {
-    if (hj >= 0) {
-      hz = P.z[hj];
-      hp = P.p[pf][hj];
-    }
-  };
-  z = patch_apply(sm, M, L, own, i, P.degree, r);
-  if (own) {
-    P.z[row] = z;
-    gam = A::addf(gam, dot3(r, z));
-    rr = A::addf(rr, dot3(r, r));
-  }
-  if (!sync(gam, rr, e0, red, prefetch)) return;
+  if (i == 0) s_fail = 0;
+  unsigned epoch = 0;
+  V4<float> s{}, w{}, u{};
+  // u = M r (patch-local), u exchanged with the neighbour patches through
+  // epoch-tagged words, w = A u; then the dots of this step
+#define EOLC_PATCH_UW(g, d, q)                                               \
+  do {                                                                       \
+    u = patch_apply(sm, M, L, own, i, P.degree, r);                          \
+    epoch += 1u;                                                             \
+    const unsigned tag_ = exch_tag(P.seq, epoch);                            \
+    if (own) {                                                               \
+      sm.xs[i] = f4(u);                                                      \
+      if (M.bnd) publish_tagged(P.tw, N, row, tag_, u);                      \
+    }                                                                        \
+    if (hj >= 0) {                                                           \
+      V4<float> uj{};                                                        \
+      if (!poll_tagged(P.tw, N, hj, tag_, uj)) {                             \
+        atomicCAS(&P.st->status, EOLC_OK, EOLC_TIMEOUT);                     \
+        s_fail = 1;                                                          \
+      }                                                                      \
+      sm.xh[i] = f4(uj);                                                     \
+    }                                                                        \
+    __syncthreads();                                                         \
+    const float3 t_ = spmv<true>(sm, M, sm.xs, f4(u));                       \
+    if (own) {                                                               \
+      w = V4<float>{t_.x * m.x, t_.y * m.y, t_.z * m.z, 0.f};                \
+      g = A::addf(g, dot3(r, u));                                            \
+      d = A::addf(d, dot3(w, u));                                            \
+      q = A::addf(q, dot3(r, r));                                            \
+    }                                                                        \
+  } while (0)
+  V gam = A::zero(), del = A::zero(), rr = A::zero();
+  EOLC_PATCH_UW(gam, del, rr);
+  if (!sync(gam, del, rr, red)) return;
+  if (s_fail) return;  // a neighbour exchange timed out (status recorded)
   V rmax2 = rr;
   double last_rr64 = A::to_d(rr);
   int it = 0, nref = 0, status = EOLC_NOT_CONVERGED;
   bool converged = A::finite(rr) && A::le(rr, tol2);
   if (!A::finite(rr) || !A::finite(gam)) status = EOLC_NONFINITE;
-  V gam_old = A::from_d(1.0);
+  V gam_old = A::from_d(1.0), alpha_old = A::from_d(1.0);
   bool restart = true;
-  int cur = 0;  // p[cur]: the neighbours' search directions of the last step
   while (!converged && status != EOLC_NONFINITE && it < P.max_iter) {
     const V beta = restart ? A::zero() : A::div(gam, gam_old);
-    const float bf = float(A::to_t(beta));
-    restart = false;
-    const int nxt = cur ^ 1;
-    // p = z + beta p (own rows and, recomputed, halo nodes); q = A p
-    if (own) {
-      p = V4<float>{z.x + bf * p.x, z.y + bf * p.y, z.z + bf * p.z, 0.f};
-      P.p[nxt][row] = p;
-      sm.xs[i] = f4(p);
-    }
-    if (hj >= 0) sm.xh[i] = make_float4(hz.x + bf * hp.x, hz.y + bf * hp.y, hz.z + bf * hp.z, 0.f);
-    __syncthreads();
-    V4<float> q{};
-    V pq = A::zero(), e1 = A::zero(), e2 = A::zero();
-    const float3 t = spmv<true>(sm, M, sm.xs, f4(p));
-    if (own) {
-      q = V4<float>{t.x * m.x, t.y * m.y, t.z * m.z, 0.f};
-      pq = A::addf(pq, dot3(p, q));
-    }
-    if (!sync(pq, e1, e2, red)) return;
-    if (!A::pos(pq) || !A::pos(gam)) {
-      status = (A::finite(pq) && A::finite(gam)) ? EOLC_BREAKDOWN : EOLC_NONFINITE;
+    const V denom = restart ? del : A::add(del, A::neg(A::div(A::mul(beta, gam), alpha_old)));
+    if (!A::pos(denom) || !A::pos(gam)) {
+      status = (A::finite(denom) && A::finite(gam)) ? EOLC_BREAKDOWN : EOLC_NONFINITE;
       break;
     }
-    const float af = float(A::to_t(A::div(gam, pq)));
+    const V alpha = A::div(gam, denom);
+    const float af = float(A::to_t(alpha)), bf = float(A::to_t(beta));
+    restart = false;
     if (own) {
-      r.x -= af * q.x; r.y -= af * q.y; r.z -= af * q.z;
+      s = V4<float>{w.x + bf * s.x, w.y + bf * s.y, w.z + bf * s.z, 0.f};
+      r = V4<float>{r.x - af * s.x, r.y - af * s.y, r.z - af * s.z, 0.f};
+      p = V4<float>{u.x + bf * p.x, u.y + bf * p.y, u.z + bf * p.z, 0.f};
       x.x += af * p.x; x.y += af * p.y; x.z += af * p.z;
     }
-    z = patch_apply(sm, M, L, own, i, P.degree, r);
-    V g2 = A::zero(), rr2 = A::zero(), e3 = A::zero();
-    if (own) {
-      P.z[row] = z;
-      g2 = A::addf(g2, dot3(r, z));
-      rr2 = A::addf(rr2, dot3(r, r));
-    }
-    pf = nxt;
-    if (!sync(g2, rr2, e3, red, prefetch)) return;
+    V g2 = A::zero(), d2 = A::zero(), rr2 = A::zero();
+    EOLC_PATCH_UW(g2, d2, rr2);
+    if (!sync(g2, d2, rr2, red)) return;
+    if (s_fail) return;
     ++it;
-    cur = nxt;
     gam_old = gam;
+    alpha_old = alpha;
     gam = g2;
+    del = d2;
     rr = rr2;
-    if (!A::finite(rr) || !A::finite(gam)) { status = EOLC_NONFINITE; break; }
+    if (!A::finite(rr) || !A::finite(gam) || !A::finite(del)) { status = EOLC_NONFINITE; break; }
     if (!(A::lt(rr, A::mul(delta2, rmax2)) || A::le(rr, tol2) || it >= P.max_iter)) continue;
-    // ---- reliable update: x64 += x; r = rhs - A x64 (FP64); z = M r --------
+    // ---- reliable update: x64 += x; r = rhs - A x64 (FP64); s = A p --------
     if (own) {
       V4<double> xd = P.x64[row];
       xd.x += double(x.x); xd.y += double(x.y); xd.z += double(x.z);
       P.x64[row] = xd;
       x = V4<float>{0.f, 0.f, 0.f, 0.f};
+      P.p[0][row] = p;
+      sm.xs[i] = f4(p);
     }
     if (!sync.barrier()) return;
+    if (hj >= 0) sm.xh[i] = f4(P.p[0][hj]);
+    __syncthreads();
     double rr64d = 0;
+    const float3 ts = spmv<true>(sm, M, sm.xs, f4(p));
     if (own) {
-      const V4<double> q = true_residual(P, row, m);
-      rr64d = q.x * q.x + q.y * q.y + q.z * q.z;
-      r = V4<float>{float(q.x), float(q.y), float(q.z), 0.f};
+      const V4<double> qd = true_residual(P, row, m);
+      rr64d = qd.x * qd.x + qd.y * qd.y + qd.z * qd.z;
+      r = V4<float>{float(qd.x), float(qd.y), float(qd.z), 0.f};
+      s = V4<float>{ts.x * m.x, ts.y * m.y, ts.z * m.z, 0.f};
     }
-    z = patch_apply(sm, M, L, own, i, P.degree, r);
-    V rr64 = A::from_d(rr64d), g3 = A::zero(), e4 = A::zero();
-    if (own) {
-      P.z[row] = z;
-      g3 = A::addf(g3, dot3(r, z));
-    }
-    pf = cur;
-    if (!sync(rr64, g3, e4, red, prefetch)) return;
+    V e0 = A::from_d(rr64d), e1 = A::zero(), e2 = A::zero();
+    if (!sync(e0, e1, e2, red)) return;
     ++nref;
-    last_rr64 = A::to_d(rr64);
-    rmax2 = rr64;
+    last_rr64 = A::to_d(e0);
+    rmax2 = e0;
+    if (!A::finite(e0)) { status = EOLC_NONFINITE; break; }
+    if (A::le(e0, tol2)) { converged = true; break; }
+    V g3 = A::zero(), d3 = A::zero(), rr3 = A::zero();
+    EOLC_PATCH_UW(g3, d3, rr3);
+    if (!sync(g3, d3, rr3, red)) return;
+    if (s_fail) return;
     gam = g3;
-    if (!A::finite(rr64) || !A::finite(gam)) { status = EOLC_NONFINITE; break; }
-    if (A::le(rr64, tol2)) { converged = true; break; }
+    del = d3;
   }
+#undef EOLC_PATCH_UW
   if (converged) status = EOLC_OK;
   if (cta == 0 && threadIdx.x == 0) {
     atomicCAS(&P.st->status, EOLC_OK, status);
@@ -809,56 +870,9 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
 // row to its matrix neighbours, so u = G r needs r on the halo (recomputed
 // as r_j - alpha (w_j + beta s_j) from the neighbours' r, s, w of the last
 // step, prefetched after the grid barrier) and w = A u needs u on the halo,
-// two rings out: each patch publishes u of its boundary rows as epoch-tagged
-// 64-bit words (value | tag << 32, tag = launch number << 20 | epoch),
-// double-buffered by the epoch's parity, and the neighbours poll them.  One
-// grid barrier and one neighbour exchange per iteration.  Two buffers
-// suffice: a patch publishes epoch e + 2 only after the grid reduction that
-// follows the exchange of e + 1, which every patch joins after its read of
-// e.  G is read from global memory (L2); A is the resident image.
-__device__ __forceinline__ void ld_tag2(const unsigned long long *p, unsigned long long &a,
-                                        unsigned long long &b) {
-  asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];"
-               : "=l"(a), "=l"(b)
-               : "l"(p)
-               : "memory");
-}
-__device__ __forceinline__ void st_tag2(unsigned long long *p, unsigned long long a,
-                                        unsigned long long b) {
-  asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(a), "l"(b)
-               : "memory");
-}
-__device__ __forceinline__ unsigned long long tag_word(unsigned tag, float v) {
-  return (static_cast<unsigned long long>(tag) << 32) | __float_as_uint(v);
-}
-__device__ __forceinline__ unsigned tag_of(unsigned long long w) { return unsigned(w >> 32); }
-__device__ __forceinline__ float tag_val(unsigned long long w) {
-  return __uint_as_float(unsigned(w & 0xffffffffull));
-}
-__device__ __forceinline__ unsigned exch_tag(unsigned seq, unsigned epoch) {
-  return (seq << 20) | (epoch & 0xfffffu);
-}
-__device__ __forceinline__ void publish_tagged(unsigned long long *tw, int N, int row,
-                                               unsigned tag, const V4<float> &v) {
-  unsigned long long *q = tw + (size_t(tag & 1u) * N + row) * 4;
-  st_tag2(q, tag_word(tag, v.x), tag_word(tag, v.y));
-  st_tag2(q + 2, tag_word(tag, v.z), tag_word(tag, 0.f));
-}
-// Polls node's words until they carry the tag; false after kSpinLimit polls.
-__device__ __forceinline__ bool poll_tagged(const unsigned long long *tw, int N, int node,
-                                            unsigned tag, V4<float> &v) {
-  const unsigned long long *q = tw + (size_t(tag & 1u) * N + node) * 4;
-  for (long long spin = 0; spin < kSpinLimit; ++spin) {
-    unsigned long long a, b, c, d;
-    ld_tag2(q, a, b);
-    ld_tag2(q + 2, c, d);
-    if (tag_of(a) == tag && tag_of(b) == tag && tag_of(c) == tag) {
-      v = V4<float>{tag_val(a), tag_val(b), tag_val(c), 0.f};
-      return true;
-    }
-  }
-  return false;
-}
+// two rings out, which comes through the epoch-tagged neighbour exchange.
+// One grid barrier and one neighbour exchange per iteration.  G is read from
+// global memory (L2); A is the resident image.
 
 __device__ __forceinline__ V4<float> apply_G(const ResParams &P, const ResSmem &sm, int cta) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1369,7 +1383,7 @@ struct PatchWork {
   DevBuf<int> perm, rowptr, colidx, diag, tr, src, patch_row, fptr, fblk, rcnt, wbase, hnptr,
       hnode;
   DevBuf<unsigned> fword;
-  DevBuf<unsigned long long> tw;  // learned PCG: tagged halo values, zeroed once per plan
+  DevBuf<unsigned long long> tw;  // neighbour exchange: tagged values, zeroed once per plan
   unsigned seq = 0;               // launches (tag generation)
   DevBuf<int16_t> bsl;
   DevBuf<int> gsrc, slice_off, slice_len;

@@ -284,7 +284,8 @@ def run_reference(args, rank):
 
 
 ARM_KERNEL = {"jacobi": "jacobi_resident_kernel", "block": "jacobi_resident_kernel",
-              "patch": "patch_resident_kernel", "learned": "learned_resident_kernel",
+              "patch": "patch_resident_kernel", "patch-1l": "patch_resident_kernel",
+              "learned": "learned_resident_kernel",
               "learned-r4": "learned_resident_kernel", "jacobi-streamed": "cg_kernel"}
 
 
@@ -298,6 +299,8 @@ def arm_opts(eolc, arm, degree):
         return eolc.SolveOpts(precond=eolc.PC_BLOCK_JACOBI, **base)
     if arm == "patch":
         return eolc.SolveOpts(precond=eolc.PC_PATCH, degree=degree, **base)
+    if arm == "patch-1l":
+        return eolc.SolveOpts(precond=eolc.PC_PATCH, degree=degree, no_coarse=1, **base)
     if arm in ("learned", "learned-r4"):
         return eolc.SolveOpts(precond=eolc.PC_LEARNED, fallback_factor=2, **base)
     raise ValueError(arm)
@@ -364,7 +367,7 @@ def run_ours(args, rank, world, local_rank):
     lpc = None
     weights = os.path.join(ROOT, "eol-cloth_gb300", "weights", "lpc.npy")
     arms = args.precond.split(",") if args.precond != "all" else \
-        ["jacobi", "jacobi-streamed", "patch", "learned", "learned-r4"]
+        ["jacobi", "jacobi-streamed", "patch", "patch-1l", "learned", "learned-r4"]
     if any(a.startswith("learned") for a in arms):
         if os.path.exists(weights):
             lpc = eolc.LearnedPC(local_rank)

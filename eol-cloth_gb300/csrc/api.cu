@@ -200,7 +200,7 @@ eolc_status solve_device(eolc_ctx *ctx, const eolc_solve_opts *o,
   if (o->precond == EOLC_PC_PATCH)
     return run_pcg_resident(ctx->pwork, a, ResidentPC::kPatch,
                             o->degree > 0 ? o->degree : kDefaultPatchDegree, nullptr, inf, s,
-                            ctx->err, ctx->launches);
+                            ctx->err, ctx->launches, o->no_coarse == 0);
   eolc_status st;
   if (o->precision == EOLC_PREC_MIXED && !o->streamed && resident_fits(ctx->pwork, ctx->topo, ctx->X.p, s))
     st = run_pcg_resident(ctx->pwork, a, ResidentPC::kJacobi, 0, nullptr, inf, s, ctx->err,

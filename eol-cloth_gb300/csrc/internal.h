@@ -166,7 +166,8 @@ void free_patch_work(PatchWork *w);
 bool resident_fits(PatchWork *&w, const DevTopology &T, const double *X_d, cudaStream_t s);
 eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, int degree,
                              const float *Gm, eolc_solve_info *info, cudaStream_t s,
-                             std::string &err, long long &launches);
+                             std::string &err, long long &launches,
+                             bool coarse = false);
 
 // Collisions (collide.cu)
 struct CollideWork;

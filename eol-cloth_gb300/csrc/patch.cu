@@ -77,6 +77,9 @@ constexpr int kMaxHaloNodes = 384;  // distinct outside nodes the halo blocks to
 constexpr int kMaxCount = 255;      // records or slots of one row (8-bit counts)
 constexpr int kWarps = kRThreads / 32;
 constexpr float kLoFrac = 30.f;     // Chebyshev interval [lmax / 30, lmax]
+constexpr int kMaxAgg = 42;         // coarse aggregates (3 coarse unknowns each)
+constexpr int kMaxTgt = 16;         // aggregates one patch's rows couple to
+constexpr int kCoarseWords = 12;    // per-CTA coarse partials: sums of r, w, s (+ pad)
 constexpr float kBoundMargin = 1.02f;
 static_assert(kMaxRows <= kRThreads, "one thread per patch row");
 static_assert(kMaxHaloNodes <= kRThreads, "at most one halo node per thread");
@@ -104,6 +107,9 @@ constexpr size_t kOffDs = kOffXh + size_t(kMaxHaloNodes) * 16;
 constexpr size_t kOffHnode = kOffDs + size_t(kMaxRows) * 16;
 constexpr size_t kResidentSmem = al16(kOffHnode + size_t(kMaxHaloNodes) * 4);
 static_assert(kResidentSmem <= 222 * 1024, "resident image exceeds shared memory");
+// the coarse set-up and reductions use the slot and vector images as scratch
+static_assert(size_t(3 * kMaxAgg) * (3 * kMaxAgg) * 4 <= kOffHnode - kOffS, "coarse matrix scratch");
+static_assert(size_t(kCoarseWords) * 32 * 6 * 4 <= size_t(kMaxSlots) * 16, "coarse partial scratch");
 
 struct ResParams {
   int n_nodes, n_ctas, max_iter, degree, block_pc;
@@ -128,6 +134,13 @@ struct ResParams {
                                            // -1 - halo window slot
   const int *slice_off, *slice_len;        // per (CTA, warp) slice: first slot, slots
   V4<float> *r[2], *s[2], *w[2], *p[2], *z, *q;
+  // coarse correction (patch PC; n_agg == 0: off): aggregates of consecutive
+  // patches, the aggregate of every halo node, per patch its target
+  // aggregates; cpart: per (patch, target) the CTA's sum of masked blocks;
+  // partc: per-CTA sums of r, w, s, [2][G][kCoarseWords]
+  int n_agg;
+  const int *agg_first, *hagg, *ctgt;
+  float *cpart, *partc;
   unsigned long long *tw;                  // neighbour exchange: tagged u, [2][N][4] words
   unsigned seq;                            // launch number in the tags (1..4095)
   double *part;
@@ -343,6 +356,88 @@ struct GridSum {
     pre();
     if (warp == 0) {
       // every load issued before the first add: one L2 round trip
+      double v[kPartPerLane][3];
+#pragma unroll
+      for (int j = 0; j < kPartPerLane; ++j) {
+        const int k = lane + 32 * j;
+        const double *pd = reinterpret_cast<const double *>(pp + 3 * k);
+        v[j][0] = k < G ? __ldcg(pd) : 0.0;
+        v[j][1] = k < G ? __ldcg(pd + 1) : 0.0;
+        v[j][2] = k < G ? __ldcg(pd + 2) : 0.0;
+      }
+      V x = Ac::zero(), y = Ac::zero(), z = Ac::zero();
+#pragma unroll
+      for (int j = 0; j < kPartPerLane; ++j) {
+        x = Ac::add(x, *reinterpret_cast<V *>(&v[j][0]));
+        y = Ac::add(y, *reinterpret_cast<V *>(&v[j][1]));
+        z = Ac::add(z, *reinterpret_cast<V *>(&v[j][2]));
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        x = Ac::add(x, Ac::shfl_xor(x, o));
+        y = Ac::add(y, Ac::shfl_xor(y, o));
+        z = Ac::add(z, Ac::shfl_xor(z, o));
+      }
+      if (lane == 0) { red[3 * NW] = x; red[3 * NW + 1] = y; red[3 * NW + 2] = z; }
+    }
+    __syncthreads();
+    a = red[3 * NW]; b = red[3 * NW + 1]; c = red[3 * NW + 2];
+    pset ^= 1;
+    return true;
+  }
+  // As operator(), plus nine FP32 coarse partials per thread (cf: this row's
+  // r, w, s): their CTA sums (fixed trees) go to partc beside the
+  // double-float partials, and after the barrier every CTA's nine sums are
+  // copied to cs[12 c + q] (shared memory) for the caller.
+  __device__ bool with_coarse(Acc<float>::V &a, Acc<float>::V &b, Acc<float>::V &c,
+                              float (&cf)[9], Acc<float>::V *red, float *cwred, float *partc,
+                              float *cs) {
+    using Ac = Acc<float>;
+    using V = Ac::V;
+    constexpr int NW = kRThreads / 32;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a = Ac::add(a, Ac::shfl_xor(a, o));
+      b = Ac::add(b, Ac::shfl_xor(b, o));
+      c = Ac::add(c, Ac::shfl_xor(c, o));
+#pragma unroll
+      for (int q = 0; q < 9; ++q) cf[q] += __shfl_xor_sync(0xffffffffu, cf[q], o);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+      red[3 * warp] = a; red[3 * warp + 1] = b; red[3 * warp + 2] = c;
+#pragma unroll
+      for (int q = 0; q < 9; ++q) cwred[9 * warp + q] = cf[q];
+    }
+    __syncthreads();
+    V *pp = reinterpret_cast<V *>(part) + size_t(3) * G * pset;
+    float *pc = partc + size_t(kCoarseWords) * G * pset;
+    if (warp == 0) {
+      V x = Ac::zero(), y = Ac::zero(), z = Ac::zero();
+      float f[9];
+#pragma unroll
+      for (int q = 0; q < 9; ++q) f[q] = lane < NW ? cwred[9 * lane + q] : 0.f;
+      if (lane < NW) { x = red[3 * lane]; y = red[3 * lane + 1]; z = red[3 * lane + 2]; }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        x = Ac::add(x, Ac::shfl_xor(x, o));
+        y = Ac::add(y, Ac::shfl_xor(y, o));
+        z = Ac::add(z, Ac::shfl_xor(z, o));
+#pragma unroll
+        for (int q = 0; q < 9; ++q) f[q] += __shfl_xor_sync(0xffffffffu, f[q], o);
+      }
+      if (lane == 0) {
+        pp[3 * cta] = x; pp[3 * cta + 1] = y; pp[3 * cta + 2] = z;
+        float4 *d = reinterpret_cast<float4 *>(pc + size_t(kCoarseWords) * cta);
+        d[0] = make_float4(f[0], f[1], f[2], f[3]);
+        d[1] = make_float4(f[4], f[5], f[6], f[7]);
+        d[2] = make_float4(f[8], 0.f, 0.f, 0.f);
+      }
+    }
+    if (!grid_barrier(bar, G, epoch, st)) return false;
+    for (int t = threadIdx.x; t < 3 * G; t += kRThreads)
+      reinterpret_cast<float4 *>(cs)[t] = __ldcg(reinterpret_cast<const float4 *>(pc) + t);
+    if (warp == 0) {
       double v[kPartPerLane][3];
 #pragma unroll
       for (int j = 0; j < kPartPerLane; ++j) {
@@ -682,6 +777,203 @@ __device__ void inverse3_masked(const float (&D)[9], const float (&m)[3], float 
     for (int c = 0; c < 3; ++c) out[3 * r + c] = float(inv[3 * r + c] * double(m[r]) * double(m[c]));
 }
 
+// ---- coarse correction of the patch preconditioner ---------------------------
+// Coarse space: the three translations of each aggregate of consecutive
+// patches (R sums the free DOFs of an aggregate per axis, P = R^T).  The
+// preconditioner is M = M_patch + R^T A_c^-1 R with A_c = R A R^T (masked).
+//
+// coarse_setup (once per solve, every CTA): the CTA's sums of masked blocks
+// per target aggregate (fixed trees, deterministic) go to cpart; after a
+// grid barrier every CTA assembles the dense A_c (3 n_agg square) in the
+// free part of its shared memory in patch order, symmetrises it, inverts it
+// by in-place Gauss-Jordan (SPD: no pivoting) and keeps the three rows of
+// its own aggregate of (X + X^T) / 2 in X_own.  Returns false when the grid
+// barrier timed out.
+// CTA sum of nine floats (fixed trees); thread 0 writes it to out9 (global).
+__device__ void cta_sum9(float (&v)[9], float *tmp, float *out9) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int q = 0; q < 9; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < 9; ++q) tmp[9 * warp + q] = v[q];
+  __syncthreads();
+  if (warp == 0) {
+    float f[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) f[q] = lane < kWarps ? tmp[9 * lane + q] : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+      for (int q = 0; q < 9; ++q) f[q] += __shfl_xor_sync(0xffffffffu, f[q], o);
+    if (lane == 0)
+#pragma unroll
+      for (int q = 0; q < 9; ++q) out9[q] = f[q];
+  }
+  __syncthreads();
+}
+
+__device__ bool coarse_setup(const ResParams &P, const ResSmem &sm, const RowMeta &M, int cta,
+                             int p0, bool own, const V4<float> &m, GridSum &sync, float *tmp,
+                             float *X_own) {
+  const unsigned lt = (1u << (threadIdx.x & 31)) - 1u;
+  const int n_agg = P.n_agg, nc = 3 * n_agg;
+  const int *tg = P.ctgt + size_t(cta) * kMaxTgt;
+  const int hbase = P.hnptr[cta];
+  const float mi[3] = {m.x, m.y, m.z};
+  for (int t = 0; t < kMaxTgt; ++t) {
+    const int b = tg[t];
+    if (b < 0) break;
+    float acc[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) acc[q] = 0.f;
+    if (t == 0 && own) {  // diagonal block
+      const float D[9] = {M.d[0], M.d[1], M.d[2], M.d[1], M.d[3], M.d[4], M.d[2], M.d[4], M.d[5]};
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) acc[3 * r + c] += mi[r] * D[3 * r + c] * mi[c];
+    }
+    const int kmax = __reduce_max_sync(0xffffffffu, M.ft);
+    int base = M.fbase;
+    for (int k = 0; k < kmax; ++k) {
+      const unsigned act = __ballot_sync(0xffffffffu, k < M.ft);
+      if (k < M.ft) {
+        const int e = base + __popc(act & lt);
+        const float4 q0 = sm.fval[3 * e], q1 = sm.fval[3 * e + 1], q2 = sm.fval[3 * e + 2];
+        const unsigned col = __float_as_uint(q0.x) & 0xffffu;
+        const float v[9] = {q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y};
+        if (col < unsigned(kMaxRows)) {  // internal upper block: (i, j) and (j, i)
+          if (t == 0) {
+            const V4<float> mj4 = P.fmask[p0 + int(col)];
+            const float mj[3] = {mj4.x, mj4.y, mj4.z};
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+#pragma unroll
+              for (int c = 0; c < 3; ++c)
+                acc[3 * r + c] += mi[r] * v[3 * r + c] * mj[c] + mj[r] * v[3 * c + r] * mi[c];
+          }
+        } else {
+          const int h = int(col) - kMaxRows;
+          if (P.hagg[hbase + h] == b) {
+            const V4<float> mj4 = P.fmask[P.hnode[hbase + h]];
+            const float mj[3] = {mj4.x, mj4.y, mj4.z};
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+#pragma unroll
+              for (int c = 0; c < 3; ++c) acc[3 * r + c] += mi[r] * v[3 * r + c] * mj[c];
+          }
+        }
+      }
+      base += __popc(act);
+    }
+    cta_sum9(acc, tmp, P.cpart + (size_t(cta) * kMaxTgt + t) * 9);
+  }
+  if (!sync.barrier()) return false;
+  // dense A_c in the free shared memory (slot, vector images): block (a, b)
+  // summed over the patches of a in order
+  float *Ac = reinterpret_cast<float *>(sm.slot);
+  for (int pr = threadIdx.x; pr < n_agg * n_agg; pr += kRThreads) {
+    const int a = pr / n_agg, b = pr % n_agg;
+    float blk[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) blk[q] = 0.f;
+    for (int c = P.agg_first[a]; c < P.agg_first[a + 1]; ++c)
+      for (int t = 0; t < kMaxTgt; ++t) {
+        const int tb = P.ctgt[size_t(c) * kMaxTgt + t];
+        if (tb < 0) break;
+        if (tb != b) continue;
+        const float *src = P.cpart + (size_t(c) * kMaxTgt + t) * 9;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) blk[q] += __ldcg(src + q);
+      }
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) Ac[size_t(3 * a + r) * nc + 3 * b + c] = blk[3 * r + c];
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < nc * nc; q += kRThreads) {  // symmetrise
+    const int r = q / nc, c = q % nc;
+    if (r < c) {
+      const float v = 0.5f * (Ac[size_t(r) * nc + c] + Ac[size_t(c) * nc + r]);
+      Ac[size_t(r) * nc + c] = v;
+      Ac[size_t(c) * nc + r] = v;
+    }
+  }
+  // free coarse DOFs only: an axis with no free DOF in its aggregate has a
+  // zero row; it becomes the identity there (its residual sum is zero)
+  __syncthreads();
+  for (int r = threadIdx.x; r < nc; r += kRThreads)
+    if (!(Ac[size_t(r) * nc + r] > 0.f)) {
+      for (int c = 0; c < nc; ++c) { Ac[size_t(r) * nc + c] = 0.f; Ac[size_t(c) * nc + r] = 0.f; }
+      Ac[size_t(r) * nc + r] = 1.f;
+    }
+  __syncthreads();
+  // in-place Gauss-Jordan
+  for (int k = 0; k < nc; ++k) {
+    const float pinv = 1.f / Ac[size_t(k) * nc + k];
+    __syncthreads();
+    for (int j = threadIdx.x; j < nc; j += kRThreads)
+      if (j != k) Ac[size_t(k) * nc + j] *= pinv;
+    __syncthreads();
+    for (int q = threadIdx.x; q < nc * nc; q += kRThreads) {
+      const int i = q / nc, j = q % nc;
+      if (i != k && j != k) Ac[q] -= Ac[size_t(i) * nc + k] * Ac[size_t(k) * nc + j];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nc; i += kRThreads)
+      if (i != k) Ac[size_t(i) * nc + k] *= -pinv;
+    if (threadIdx.x == 0) Ac[size_t(k) * nc + k] = pinv;
+  }
+  __syncthreads();
+  const int ag = tg[0];
+  for (int q = threadIdx.x; q < 3 * nc; q += kRThreads) {
+    const int r = 3 * ag + q / nc, c = q % nc;
+    X_own[q] = 0.5f * (Ac[size_t(r) * nc + c] + Ac[size_t(c) * nc + r]);
+  }
+  __syncthreads();
+  return true;
+}
+
+// Per-aggregate sums of the CTAs' coarse partials cs (after with_coarse):
+// ca[9 a + q], patches of a added in order.
+__device__ __forceinline__ void coarse_aggregate(const ResParams &P, const float *cs, float *ca) {
+  for (int t = threadIdx.x; t < 9 * P.n_agg; t += kRThreads) {
+    const int a = t / 9, q = t % 9;
+    float v = 0.f;
+    for (int c = P.agg_first[a]; c < P.agg_first[a + 1]; ++c) v += cs[kCoarseWords * c + q];
+    ca[t] = v;
+  }
+}
+
+// e = X_own R r' with R r' = ca_r - alpha (ca_w + beta ca_s) per aggregate
+// (alpha = 0: R r' = ca_r); warp 0 computes, e[0..2] in shared memory.
+__device__ __forceinline__ void coarse_correction(const ResParams &P, const float *ca,
+                                                  const float *X_own, float af, float bf,
+                                                  float *e) {
+  if ((threadIdx.x >> 5) != 0) return;
+  const int lane = threadIdx.x & 31, nc = 3 * P.n_agg;
+  float e0 = 0.f, e1 = 0.f, e2 = 0.f;
+  for (int j = lane; j < nc; j += 32) {
+    const int a = j / 3, c = j % 3;
+    const float rs = ca[9 * a + 3 + c] + bf * ca[9 * a + 6 + c];
+    const float rr = ca[9 * a + c] - af * rs;
+    e0 += X_own[j] * rr;
+    e1 += X_own[nc + j] * rr;
+    e2 += X_own[2 * nc + j] * rr;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    e0 += __shfl_xor_sync(0xffffffffu, e0, o);
+    e1 += __shfl_xor_sync(0xffffffffu, e1, o);
+    e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+  }
+  if (lane == 0) { e[0] = e0; e[1] = e1; e[2] = e2; }
+}
+
 __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams P) {
   using A = Acc<float>;
   using V = A::V;
@@ -689,6 +981,7 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
   __shared__ V red[3 * (kRThreads / 32 + 1)];
   __shared__ float s_max[kRThreads / 32];
   __shared__ int s_fail;
+  __shared__ float s_tmp9[9 * kWarps], s_X[3 * 3 * kMaxAgg], s_ca[9 * kMaxAgg], s_e[3];
   const ResSmem sm = carve(smem);
   const int cta = blockIdx.x, i = threadIdx.x;
   const int p0 = P.patch_row[cta], np = P.patch_row[cta + 1] - p0;
@@ -754,11 +1047,26 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
   if (i == 0) s_fail = 0;
   unsigned epoch = 0;
   V4<float> s{}, w{}, u{};
+  // coarse correction: A_c^-1 rows of this aggregate, then e for r_0
+  const bool coarse = P.n_agg > 0;
+  float *cs = reinterpret_cast<float *>(sm.slot);  // every CTA's coarse partials
+  if (i < 3) s_e[i] = 0.f;
+  if (coarse) {
+    if (!coarse_setup(P, sm, M, cta, p0, own, m, sync, s_tmp9, s_X)) return;
+    V z0 = A::zero(), z1 = A::zero(), z2 = A::zero();
+    float cf[9] = {r.x, r.y, r.z, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (!sync.with_coarse(z0, z1, z2, cf, red, s_tmp9, P.partc, cs)) return;
+    coarse_aggregate(P, cs, s_ca);
+    __syncthreads();
+    coarse_correction(P, s_ca, s_X, 0.f, 0.f, s_e);
+    __syncthreads();
+  }
   // u = M r (patch-local), u exchanged with the neighbour patches through
   // epoch-tagged words, w = A u; then the dots of this step
 #define EOLC_PATCH_UW(g, d, q)                                               \
   do {                                                                       \
     u = patch_apply(sm, M, L, own, i, P.degree, r);                          \
+    u.x += s_e[0] * m.x; u.y += s_e[1] * m.y; u.z += s_e[2] * m.z;           \
     epoch += 1u;                                                             \
     const unsigned tag_ = exch_tag(P.seq, epoch);                            \
     if (own) {                                                               \
@@ -782,9 +1090,21 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
       q = A::addf(q, dot3(r, r));                                            \
     }                                                                        \
   } while (0)
+  // the step's reduction, with the patch's sums of r, w, s when coarse
+#define EOLC_PATCH_SUM(g, d, q)                                              \
+  do {                                                                       \
+    if (coarse) {                                                            \
+      float cf_[9] = {r.x, r.y, r.z, w.x, w.y, w.z, s.x, s.y, s.z};          \
+      if (!sync.with_coarse(g, d, q, cf_, red, s_tmp9, P.partc, cs)) return; \
+      coarse_aggregate(P, cs, s_ca);                                         \
+      __syncthreads();                                                       \
+    } else if (!sync(g, d, q, red)) {                                        \
+      return;                                                                \
+    }                                                                        \
+  } while (0)
   V gam = A::zero(), del = A::zero(), rr = A::zero();
   EOLC_PATCH_UW(gam, del, rr);
-  if (!sync(gam, del, rr, red)) return;
+  EOLC_PATCH_SUM(gam, del, rr);
   if (s_fail) return;  // a neighbour exchange timed out (status recorded)
   V rmax2 = rr;
   double last_rr64 = A::to_d(rr);
@@ -803,6 +1123,10 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
     const V alpha = A::div(gam, denom);
     const float af = float(A::to_t(alpha)), bf = float(A::to_t(beta));
     restart = false;
+    if (coarse) {  // e for r' = r - alpha (w + beta s), from the aggregate sums
+      coarse_correction(P, s_ca, s_X, af, bf, s_e);
+      __syncthreads();
+    }
     if (own) {
       s = V4<float>{w.x + bf * s.x, w.y + bf * s.y, w.z + bf * s.z, 0.f};
       r = V4<float>{r.x - af * s.x, r.y - af * s.y, r.z - af * s.z, 0.f};
@@ -811,7 +1135,7 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
     }
     V g2 = A::zero(), d2 = A::zero(), rr2 = A::zero();
     EOLC_PATCH_UW(g2, d2, rr2);
-    if (!sync(g2, d2, rr2, red)) return;
+    EOLC_PATCH_SUM(g2, d2, rr2);
     if (s_fail) return;
     ++it;
     gam_old = gam;
@@ -842,20 +1166,32 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
       s = V4<float>{ts.x * m.x, ts.y * m.y, ts.z * m.z, 0.f};
     }
     V e0 = A::from_d(rr64d), e1 = A::zero(), e2 = A::zero();
-    if (!sync(e0, e1, e2, red)) return;
+    if (coarse) {  // with R r of the replaced residual
+      float cf[9] = {r.x, r.y, r.z, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      if (!sync.with_coarse(e0, e1, e2, cf, red, s_tmp9, P.partc, cs)) return;
+      coarse_aggregate(P, cs, s_ca);
+      __syncthreads();
+    } else if (!sync(e0, e1, e2, red)) {
+      return;
+    }
     ++nref;
     last_rr64 = A::to_d(e0);
     rmax2 = e0;
     if (!A::finite(e0)) { status = EOLC_NONFINITE; break; }
     if (A::le(e0, tol2)) { converged = true; break; }
+    if (coarse) {
+      coarse_correction(P, s_ca, s_X, 0.f, 0.f, s_e);
+      __syncthreads();
+    }
     V g3 = A::zero(), d3 = A::zero(), rr3 = A::zero();
     EOLC_PATCH_UW(g3, d3, rr3);
-    if (!sync(g3, d3, rr3, red)) return;
+    EOLC_PATCH_SUM(g3, d3, rr3);
     if (s_fail) return;
     gam = g3;
     del = d3;
   }
 #undef EOLC_PATCH_UW
+#undef EOLC_PATCH_SUM
   if (converged) status = EOLC_OK;
   if (cta == 0 && threadIdx.x == 0) {
     atomicCAS(&P.st->status, EOLC_OK, status);
@@ -1198,6 +1534,11 @@ struct PatchPlan {
   std::vector<int> perm, rowptr, colidx, src, tr, diag, patch_row, hnptr, hnode;
   std::vector<int> fptr, fblk, rcnt, wbase;  // shared-memory image (load_patch)
   std::vector<unsigned> fword;
+  // coarse space: n_agg aggregates of consecutive patches (agg_first), the
+  // aggregate of every halo node (hagg, like hnode) and, per patch, the
+  // aggregates its rows couple to (ctgt, own aggregate first, -1 padded)
+  int n_agg = 0;
+  std::vector<int> agg_first, hagg, ctgt;
   std::vector<int16_t> bsl;   // per slice slot and lane: local row, or -1 - halo slot
   std::vector<int> gsrc;      // per slice slot and lane: block in the original order, or -1
   std::vector<int> slice_off, slice_len;  // per (patch, warp)
@@ -1333,6 +1674,25 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
     fptr[c + 1] = fptr[c] + nrec;
   }
   for (int j : hnode) rcnt[j] |= 1 << 24;  // a halo node of some patch: it publishes
+  // coarse aggregates: consecutive patches of the bisection order
+  const int n_agg = std::min(G, kMaxAgg);
+  std::vector<int> agg_first(n_agg + 1), patch_agg(G), node_patch(N), hagg(hnode.size());
+  for (int a = 0; a <= n_agg; ++a) agg_first[a] = int((long long)a * G / n_agg);
+  for (int a = 0; a < n_agg; ++a)
+    for (int c = agg_first[a]; c < agg_first[a + 1]; ++c) patch_agg[c] = a;
+  for (int c = 0; c < G; ++c)
+    for (int i = patch_row[c]; i < patch_row[c + 1]; ++i) node_patch[i] = c;
+  std::vector<int> ctgt(size_t(G) * kMaxTgt, -1);
+  for (int c = 0; c < G; ++c) {
+    std::vector<int> t = {patch_agg[c]};
+    for (int h = hnptr[c]; h < hnptr[c + 1]; ++h) {
+      hagg[h] = patch_agg[node_patch[hnode[h]]];
+      if (std::find(t.begin(), t.end(), hagg[h]) == t.end()) t.push_back(hagg[h]);
+    }
+    if (int(t.size()) > kMaxTgt) return "patch couples to too many coarse aggregates";
+    std::sort(t.begin() + 1, t.end());
+    std::copy(t.begin(), t.end(), ctgt.begin() + size_t(c) * kMaxTgt);
+  }
   out.G = G;
   out.perm = std::move(perm);
   out.rowptr = std::move(prow);
@@ -1348,6 +1708,10 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
   out.wbase = std::move(wbase);
   out.hnptr = std::move(hnptr);
   out.hnode = std::move(hnode);
+  out.n_agg = n_agg;
+  out.agg_first = std::move(agg_first);
+  out.hagg = std::move(hagg);
+  out.ctgt = std::move(ctgt);
   // warp slices of the pattern (for the learned G)
   out.slice_off.assign(size_t(G) * kWarps, 0);
   out.slice_len.assign(size_t(G) * kWarps, 0);
@@ -1384,6 +1748,9 @@ struct PatchWork {
       hnode;
   DevBuf<unsigned> fword;
   DevBuf<unsigned long long> tw;  // neighbour exchange: tagged values, zeroed once per plan
+  int n_agg = 0;                  // coarse aggregates of the plan
+  DevBuf<int> agg_first, hagg, ctgt;
+  DevBuf<float> cpart, partc;
   unsigned seq = 0;               // launches (tag generation)
   DevBuf<int16_t> bsl;
   DevBuf<int> gsrc, slice_off, slice_len;
@@ -1428,7 +1795,7 @@ eolc_status patch_plan(PatchWork *w, const DevTopology &Tp, const double *X_d, i
   w->why = build_patch_plan(N, rowptr, colidx, X.empty() ? nullptr : &X, n_sm, L);
   if (!w->why.empty()) return EOLC_OK;
   // empty lists (e.g. no halo on a one-patch mesh) still get one element
-  for (auto *v : {&L.fblk, &L.hnode})
+  for (auto *v : {&L.fblk, &L.hnode, &L.hagg})
     if (v->empty()) v->push_back(0);
   if (L.fword.empty()) L.fword.push_back(0u);
   cudaError_t es[] = {
@@ -1448,6 +1815,10 @@ eolc_status patch_plan(PatchWork *w, const DevTopology &Tp, const double *X_d, i
       w->bp.resize(size_t(N) * 3),
       w->beqp.resize(size_t(N) * 3),
       w->part.resize(size_t(6) * L.G),
+      upload_vec(w->agg_first, L.agg_first, s), upload_vec(w->ctgt, L.ctgt, s),
+      upload_vec(w->hagg, L.hagg, s),
+      w->cpart.resize(size_t(L.G) * kMaxTgt * 9),
+      w->partc.resize(size_t(2) * kCoarseWords * L.G),
       w->tw.resize(size_t(8) * N),
       cudaMemsetAsync(w->tw.p, 0, sizeof(unsigned long long) * 8 * size_t(N), s),
       w->bar.resize(2),
@@ -1456,6 +1827,7 @@ eolc_status patch_plan(PatchWork *w, const DevTopology &Tp, const double *X_d, i
   for (cudaError_t e : es)
     if (e != cudaSuccess) { err = cudaGetErrorString(e); return EOLC_CUDA_ERROR; }
   w->G = L.G;
+  w->n_agg = L.n_agg;
   return EOLC_OK;
 }
 
@@ -1478,7 +1850,7 @@ bool resident_fits(PatchWork *&w, const DevTopology &Tp, const double *X_d, cuda
 
 eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, int degree,
                              const float *Gm, eolc_solve_info *info, cudaStream_t s,
-                             std::string &err, long long &launches) {
+                             std::string &err, long long &launches, bool coarse) {
   const bool patch_pc = mode == ResidentPC::kPatch, learned = mode == ResidentPC::kLearned;
   if (a.precision != EOLC_PREC_MIXED) {
     err = "the resident solvers run on the mixed-precision path";
@@ -1566,6 +1938,12 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, i
   P.bsl = w->bsl.p;
   P.slice_off = w->slice_off.p;
   P.slice_len = w->slice_len.p;
+  P.n_agg = (patch_pc && coarse) ? w->n_agg : 0;
+  P.agg_first = w->agg_first.p;
+  P.hagg = w->hagg.p;
+  P.ctgt = w->ctgt.p;
+  P.cpart = w->cpart.p;
+  P.partc = w->partc.p;
   P.tw = w->tw.p;
   w->seq = w->seq % 4095u + 1u;  // 1..4095: a tag never equals the zeroed words
   P.seq = w->seq;

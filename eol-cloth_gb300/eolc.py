@@ -46,11 +46,12 @@ class SolveOpts(ctypes.Structure):
     _fields_ = [("rel_tol", ctypes.c_double), ("max_iter", ctypes.c_int),
                 ("precision", ctypes.c_int), ("precond", ctypes.c_int),
                 ("fallback_factor", ctypes.c_int), ("degree", ctypes.c_int),
-                ("streamed", ctypes.c_int)]
+                ("streamed", ctypes.c_int), ("no_coarse", ctypes.c_int)]
 
     def __init__(self, rel_tol=1e-8, max_iter=100000, precision=PREC_MIXED,
-                 precond=PC_JACOBI, fallback_factor=2, degree=0, streamed=0):
-        super().__init__(rel_tol, max_iter, precision, precond, fallback_factor, degree, streamed)
+                 precond=PC_JACOBI, fallback_factor=2, degree=0, streamed=0, no_coarse=0):
+        super().__init__(rel_tol, max_iter, precision, precond, fallback_factor, degree, streamed,
+                         no_coarse)
 
 
 class SolveInfo(ctypes.Structure):

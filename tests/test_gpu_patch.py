@@ -50,6 +50,32 @@ def test_patch_steps_match_jacobi_steps(eolc, quads):
         x, v = xj, vj
 
 
+@pytest.mark.parametrize("quads", [40, 128])
+def test_coarse_correction_keeps_solution_and_cuts_iterations(eolc, quads):
+    """Two-level patch preconditioner (default) against the one-level one
+    (no_coarse=1): the same velocities to the FP64 criterion's accuracy,
+    and fewer iterations at 128^2 (42 aggregates of patches)."""
+    s = scenes.sheet(quads)
+    ctx = _ctx(eolc, s)
+    mat = eolc.Material(**scenes.material_c1())
+    x, v = s["x"].copy(), np.zeros(3 * s["n"])
+    its2, its1 = [], []
+    for step in range(3):
+        xa, va = x.copy(), v.copy()
+        i2 = ctx.step(xa, s["X"], va, mat, scenes.GRAV, scenes.H, s["fixed"], s["fixed_vel"],
+                      eolc.SolveOpts(precond=eolc.PC_PATCH))
+        i1 = ctx.step(x, s["X"], v, mat, scenes.GRAV, scenes.H, s["fixed"], s["fixed_vel"],
+                      eolc.SolveOpts(precond=eolc.PC_PATCH, no_coarse=1))
+        assert i2.status == eolc.OK and i2.rel_res <= 1e-8
+        assert i1.status == eolc.OK and i1.rel_res <= 1e-8
+        assert np.abs(va - v).max() <= 1e-5 * np.abs(v).max()
+        its2.append(i2.iterations)
+        its1.append(i1.iterations)
+    print("two-level %s, one-level %s" % (its2, its1))
+    if quads >= 128:
+        assert np.mean(its2) <= 0.75 * np.mean(its1)
+
+
 def test_patch_solve_matches_direct_solve(eolc):
     import oracle as O
     s = scenes.sheet(20)

@@ -285,6 +285,7 @@ def run_reference(args, rank):
 
 ARM_KERNEL = {"jacobi": "jacobi_resident_kernel", "block": "jacobi_resident_kernel",
               "patch": "patch_resident_kernel", "patch-1l": "patch_resident_kernel",
+              "patch-r4": "patch_resident_kernel",
               "learned": "learned_resident_kernel",
               "learned-r4": "learned_resident_kernel", "jacobi-streamed": "cg_kernel"}
 
@@ -299,6 +300,8 @@ def arm_opts(eolc, arm, degree):
         return eolc.SolveOpts(precond=eolc.PC_BLOCK_JACOBI, **base)
     if arm == "patch":
         return eolc.SolveOpts(precond=eolc.PC_PATCH, degree=degree, **base)
+    if arm == "patch-r4":
+        return eolc.SolveOpts(precond=eolc.PC_PATCH, degree=degree, **base)
     if arm == "patch-1l":
         return eolc.SolveOpts(precond=eolc.PC_PATCH, degree=degree, no_coarse=1, **base)
     if arm in ("learned", "learned-r4"):
@@ -307,9 +310,10 @@ def arm_opts(eolc, arm, degree):
 
 
 def arm_refresh(arm):
-    """Network evaluations per solve of an arm: learned-r4 re-evaluates the
-    learned preconditioner every 4 solves (eolc_set_learned_refresh)."""
-    return 4 if arm == "learned-r4" else 1
+    """Refresh interval of an arm: learned-r4 re-evaluates the learned
+    preconditioner every 4 solves (eolc_set_learned_refresh), patch-r4
+    rebuilds the coarse operator every 4 solves (eolc_set_coarse_refresh)."""
+    return 4 if arm in ("learned-r4", "patch-r4") else 1
 
 
 def time_arm(ctx, sc, mat, opts, x_w, v_w, steps, stream, flush, world, dev, refresh=1):
@@ -317,6 +321,7 @@ def time_arm(ctx, sc, mat, opts, x_w, v_w, steps, stream, flush, world, dev, ref
     the library's stream with L2 flushed before it; max over ranks."""
     import torch
     ctx.set_learned_refresh(refresh)
+    ctx.set_coarse_refresh(refresh)
     ctx.state_upload(x_w, sc["X"], v_w)
     if world > 1:
         torch.distributed.barrier()
@@ -367,7 +372,7 @@ def run_ours(args, rank, world, local_rank):
     lpc = None
     weights = os.path.join(ROOT, "eol-cloth_gb300", "weights", "lpc.npy")
     arms = args.precond.split(",") if args.precond != "all" else \
-        ["jacobi", "jacobi-streamed", "patch", "patch-1l", "learned", "learned-r4"]
+        ["jacobi", "jacobi-streamed", "patch", "patch-r4", "patch-1l", "learned", "learned-r4"]
     if any(a.startswith("learned") for a in arms):
         if os.path.exists(weights):
             lpc = eolc.LearnedPC(local_rank)

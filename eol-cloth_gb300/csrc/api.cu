@@ -200,7 +200,7 @@ eolc_status solve_device(eolc_ctx *ctx, const eolc_solve_opts *o,
   if (o->precond == EOLC_PC_PATCH)
     return run_pcg_resident(ctx->pwork, a, ResidentPC::kPatch,
                             o->degree > 0 ? o->degree : kDefaultPatchDegree, nullptr, inf, s,
-                            ctx->err, ctx->launches, o->no_coarse == 0);
+                            ctx->err, ctx->launches, o->no_coarse == 0, ctx->coarse_refresh);
   eolc_status st;
   if (o->precision == EOLC_PREC_MIXED && !o->streamed && resident_fits(ctx->pwork, ctx->topo, ctx->X.p, s))
     st = run_pcg_resident(ctx->pwork, a, ResidentPC::kJacobi, 0, nullptr, inf, s, ctx->err,
@@ -437,6 +437,12 @@ eolc_status eolc_attach_preconditioner(eolc_ctx *ctx, eolc_lpc *lpc) {
 eolc_status eolc_set_learned_refresh(eolc_ctx *ctx, int solves) {
   if (!ctx || solves < 1) return EOLC_BAD_ARG;
   ctx->lpc_refresh = solves;
+  return EOLC_OK;
+}
+
+eolc_status eolc_set_coarse_refresh(eolc_ctx *ctx, int solves) {
+  if (!ctx || solves < 1) return EOLC_BAD_ARG;
+  ctx->coarse_refresh = solves;
   return EOLC_OK;
 }
 

@@ -167,7 +167,7 @@ bool resident_fits(PatchWork *&w, const DevTopology &T, const double *X_d, cudaS
 eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, int degree,
                              const float *Gm, eolc_solve_info *info, cudaStream_t s,
                              std::string &err, long long &launches,
-                             bool coarse = false);
+                             bool coarse = false, int coarse_refresh = 1);
 
 // Collisions (collide.cu)
 struct CollideWork;
@@ -214,6 +214,7 @@ struct eolc_ctx {
   const eolc_lpc *lpc_cached = nullptr;  // network whose G the resident solver holds
   int lpc_uses = 0;           // solves that G has served
   int lpc_refresh = 1;        // re-evaluate the network every lpc_refresh solves
+  int coarse_refresh = 1;     // rebuild the patch PC's coarse operator every ... solves
   eolc::CollideWork *cd_work = nullptr;
   // batches: instance k owns nodes node_off[k] .. node_off[k+1]
   std::vector<int> node_off;

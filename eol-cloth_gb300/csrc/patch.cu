@@ -138,9 +138,9 @@ struct ResParams {
   // patches, the aggregate of every halo node, per patch its target
   // aggregates; cpart: per (patch, target) the CTA's sum of masked blocks;
   // partc: per-CTA sums of r, w, s, [2][G][kCoarseWords]
-  int n_agg;
-  const int *agg_first, *hagg, *ctgt;
-  float *cpart, *partc;
+  int n_agg, coarse_fresh;                 // fresh: rebuild X_own (else reuse Xg)
+  const int *agg_first, *hagg, *ctgt, *cl_ptr, *cl_idx;
+  float *cpart, *partc, *Xg;               // Xg: every CTA's X_own of the last build
   unsigned long long *tw;                  // neighbour exchange: tagged u, [2][N][4] words
   unsigned seq;                            // launch number in the tags (1..4095)
   double *part;
@@ -817,12 +817,19 @@ __device__ void cta_sum9(float (&v)[9], float *tmp, float *out9) {
 
 __device__ bool coarse_setup(const ResParams &P, const ResSmem &sm, const RowMeta &M, int cta,
                              int p0, bool own, const V4<float> &m, GridSum &sync, float *tmp,
-                             float *X_own) {
+                             float *gj, float *X_own) {
   const unsigned lt = (1u << (threadIdx.x & 31)) - 1u;
   const int n_agg = P.n_agg, nc = 3 * n_agg;
   const int *tg = P.ctgt + size_t(cta) * kMaxTgt;
-  const int hbase = P.hnptr[cta];
+  const int hbase = P.hnptr[cta], nh = P.hnptr[cta + 1] - hbase;
   const float mi[3] = {m.x, m.y, m.z};
+  // masks of the patch rows (xs) and halo nodes (xh, w = aggregate) staged
+  if (threadIdx.x < kMaxRows) sm.xs[threadIdx.x] = make_float4(m.x, m.y, m.z, 0.f);
+  for (int h = threadIdx.x; h < nh; h += kRThreads) {
+    const V4<float> mh = P.fmask[P.hnode[hbase + h]];
+    sm.xh[h] = make_float4(mh.x, mh.y, mh.z, __int_as_float(P.hagg[hbase + h]));
+  }
+  __syncthreads();
   for (int t = 0; t < kMaxTgt; ++t) {
     const int b = tg[t];
     if (b < 0) break;
@@ -847,7 +854,7 @@ __device__ bool coarse_setup(const ResParams &P, const ResSmem &sm, const RowMet
         const float v[9] = {q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y};
         if (col < unsigned(kMaxRows)) {  // internal upper block: (i, j) and (j, i)
           if (t == 0) {
-            const V4<float> mj4 = P.fmask[p0 + int(col)];
+            const float4 mj4 = sm.xs[col];
             const float mj[3] = {mj4.x, mj4.y, mj4.z};
 #pragma unroll
             for (int r = 0; r < 3; ++r)
@@ -856,9 +863,8 @@ __device__ bool coarse_setup(const ResParams &P, const ResSmem &sm, const RowMet
                 acc[3 * r + c] += mi[r] * v[3 * r + c] * mj[c] + mj[r] * v[3 * c + r] * mi[c];
           }
         } else {
-          const int h = int(col) - kMaxRows;
-          if (P.hagg[hbase + h] == b) {
-            const V4<float> mj4 = P.fmask[P.hnode[hbase + h]];
+          const float4 mj4 = sm.xh[int(col) - kMaxRows];
+          if (__float_as_int(mj4.w) == b) {
             const float mj[3] = {mj4.x, mj4.y, mj4.z};
 #pragma unroll
             for (int r = 0; r < 3; ++r)
@@ -871,6 +877,7 @@ __device__ bool coarse_setup(const ResParams &P, const ResSmem &sm, const RowMet
     }
     cta_sum9(acc, tmp, P.cpart + (size_t(cta) * kMaxTgt + t) * 9);
   }
+  (void)p0;
   if (!sync.barrier()) return false;
   // dense A_c in the free shared memory (slot, vector images): block (a, b)
   // summed over the patches of a in order
@@ -880,15 +887,11 @@ __device__ bool coarse_setup(const ResParams &P, const ResSmem &sm, const RowMet
     float blk[9];
 #pragma unroll
     for (int q = 0; q < 9; ++q) blk[q] = 0.f;
-    for (int c = P.agg_first[a]; c < P.agg_first[a + 1]; ++c)
-      for (int t = 0; t < kMaxTgt; ++t) {
-        const int tb = P.ctgt[size_t(c) * kMaxTgt + t];
-        if (tb < 0) break;
-        if (tb != b) continue;
-        const float *src = P.cpart + (size_t(c) * kMaxTgt + t) * 9;
+    for (int j = P.cl_ptr[pr]; j < P.cl_ptr[pr + 1]; ++j) {
+      const float *src = P.cpart + size_t(P.cl_idx[j]) * 9;
 #pragma unroll
-        for (int q = 0; q < 9; ++q) blk[q] += __ldcg(src + q);
-      }
+      for (int q = 0; q < 9; ++q) blk[q] += __ldcg(src + q);
+    }
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
@@ -912,23 +915,41 @@ __device__ bool coarse_setup(const ResParams &P, const ResSmem &sm, const RowMet
       Ac[size_t(r) * nc + r] = 1.f;
     }
   __syncthreads();
-  // in-place Gauss-Jordan
+  // in-place Gauss-Jordan, two barriers per pivot: the old pivot row and
+  // column are staged (gj), then every entry is updated from them (rows over
+  // warps, columns over lanes, the pivot row segment in registers):
+  //   row k: a_kj p (j != k), p;  others: a_ij - a_ik p a_kj (j != k), -a_ik p
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int kJ = (3 * kMaxAgg + 31) / 32;
+  float *rowk = gj, *colk = gj + 3 * kMaxAgg;
   for (int k = 0; k < nc; ++k) {
-    const float pinv = 1.f / Ac[size_t(k) * nc + k];
-    __syncthreads();
-    for (int j = threadIdx.x; j < nc; j += kRThreads)
-      if (j != k) Ac[size_t(k) * nc + j] *= pinv;
-    __syncthreads();
-    for (int q = threadIdx.x; q < nc * nc; q += kRThreads) {
-      const int i = q / nc, j = q % nc;
-      if (i != k && j != k) Ac[q] -= Ac[size_t(i) * nc + k] * Ac[size_t(k) * nc + j];
+    for (int j = threadIdx.x; j < nc; j += kRThreads) {
+      rowk[j] = Ac[size_t(k) * nc + j];
+      colk[j] = Ac[size_t(j) * nc + k];
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < nc; i += kRThreads)
-      if (i != k) Ac[size_t(i) * nc + k] *= -pinv;
-    if (threadIdx.x == 0) Ac[size_t(k) * nc + k] = pinv;
+    const float pinv = 1.f / rowk[k];
+    float rkp[kJ];
+#pragma unroll
+    for (int q = 0; q < kJ; ++q) {
+      const int j = lane + 32 * q;
+      rkp[q] = j < nc ? rowk[j] * pinv : 0.f;
+    }
+    for (int i = warp; i < nc; i += kWarps) {
+      float *ri = Ac + size_t(i) * nc;
+      const float f = colk[i];
+#pragma unroll
+      for (int q = 0; q < kJ; ++q) {
+        const int j = lane + 32 * q;
+        if (j >= nc) continue;
+        float v;
+        if (i == k) v = j == k ? pinv : rkp[q];
+        else v = j == k ? -f * pinv : ri[j] - f * rkp[q];
+        ri[j] = v;
+      }
+    }
+    __syncthreads();
   }
-  __syncthreads();
   const int ag = tg[0];
   for (int q = threadIdx.x; q < 3 * nc; q += kRThreads) {
     const int r = 3 * ag + q / nc, c = q % nc;
@@ -938,40 +959,27 @@ __device__ bool coarse_setup(const ResParams &P, const ResSmem &sm, const RowMet
   return true;
 }
 
-// Per-aggregate sums of the CTAs' coarse partials cs (after with_coarse):
-// ca[9 a + q], patches of a added in order.
-__device__ __forceinline__ void coarse_aggregate(const ResParams &P, const float *cs, float *ca) {
-  for (int t = threadIdx.x; t < 9 * P.n_agg; t += kRThreads) {
-    const int a = t / 9, q = t % 9;
+// After with_coarse: g[3 q + c] = (X_own R q)_c for q = r, w, s, from every
+// CTA's partial sums cs (nine warps, one dot product each over the patches'
+// axis sums, lanes over patches, a fixed tree).  The correction for
+// r' = r - alpha (w + beta s) is then e = g_r - alpha (g_w + beta g_s).
+__device__ __forceinline__ void coarse_g(const ResParams &P, int G, const float *cs,
+                                         const int *patch_agg, const float *X_own, float *g) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp < 9) {
+    const int q = warp / 3, c = warp % 3, nc = 3 * P.n_agg;
+    const float *xr = X_own + c * nc;
     float v = 0.f;
-    for (int c = P.agg_first[a]; c < P.agg_first[a + 1]; ++c) v += cs[kCoarseWords * c + q];
-    ca[t] = v;
-  }
-}
-
-// e = X_own R r' with R r' = ca_r - alpha (ca_w + beta ca_s) per aggregate
-// (alpha = 0: R r' = ca_r); warp 0 computes, e[0..2] in shared memory.
-__device__ __forceinline__ void coarse_correction(const ResParams &P, const float *ca,
-                                                  const float *X_own, float af, float bf,
-                                                  float *e) {
-  if ((threadIdx.x >> 5) != 0) return;
-  const int lane = threadIdx.x & 31, nc = 3 * P.n_agg;
-  float e0 = 0.f, e1 = 0.f, e2 = 0.f;
-  for (int j = lane; j < nc; j += 32) {
-    const int a = j / 3, c = j % 3;
-    const float rs = ca[9 * a + 3 + c] + bf * ca[9 * a + 6 + c];
-    const float rr = ca[9 * a + c] - af * rs;
-    e0 += X_own[j] * rr;
-    e1 += X_own[nc + j] * rr;
-    e2 += X_own[2 * nc + j] * rr;
-  }
+    for (int p = lane; p < G; p += 32) {
+      const float *cp = cs + kCoarseWords * p + 3 * q;
+      const int j = 3 * patch_agg[p];
+      v += xr[j] * cp[0] + xr[j + 1] * cp[1] + xr[j + 2] * cp[2];
+    }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    e0 += __shfl_xor_sync(0xffffffffu, e0, o);
-    e1 += __shfl_xor_sync(0xffffffffu, e1, o);
-    e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) g[3 * q + c] = v;
   }
-  if (lane == 0) { e[0] = e0; e[1] = e1; e[2] = e2; }
+  __syncthreads();
 }
 
 __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams P) {
@@ -981,7 +989,9 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
   __shared__ V red[3 * (kRThreads / 32 + 1)];
   __shared__ float s_max[kRThreads / 32];
   __shared__ int s_fail;
-  __shared__ float s_tmp9[9 * kWarps], s_X[3 * 3 * kMaxAgg], s_ca[9 * kMaxAgg], s_e[3];
+  __shared__ float s_tmp9[9 * kWarps], s_X[3 * 3 * kMaxAgg], s_g[9];
+  __shared__ int s_pagg[32 * kPartPerLane];  // aggregate of every patch
+  __shared__ float s_gj[2 * 3 * kMaxAgg];     // coarse set-up: pivot row and column
   const ResSmem sm = carve(smem);
   const int cta = blockIdx.x, i = threadIdx.x;
   const int p0 = P.patch_row[cta], np = P.patch_row[cta + 1] - p0;
@@ -1050,23 +1060,32 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
   // coarse correction: A_c^-1 rows of this aggregate, then e for r_0
   const bool coarse = P.n_agg > 0;
   float *cs = reinterpret_cast<float *>(sm.slot);  // every CTA's coarse partials
-  if (i < 3) s_e[i] = 0.f;
+  if (i < 9) s_g[i] = 0.f;
+  if (coarse)
+    for (int a = 0; a < P.n_agg; ++a)
+      for (int c = P.agg_first[a] + i; c < P.agg_first[a + 1]; c += kRThreads) s_pagg[c] = a;
+  float ce[3] = {0.f, 0.f, 0.f};  // this patch's coarse correction for the next u
   if (coarse) {
-    if (!coarse_setup(P, sm, M, cta, p0, own, m, sync, s_tmp9, s_X)) return;
+    const int nc3 = 9 * P.n_agg;  // X_own: 3 rows of 3 n_agg
+    if (P.coarse_fresh) {
+      if (!coarse_setup(P, sm, M, cta, p0, own, m, sync, s_tmp9, s_gj, s_X)) return;
+      for (int q = i; q < nc3; q += kRThreads) P.Xg[size_t(cta) * 9 * kMaxAgg + q] = s_X[q];
+    } else {
+      for (int q = i; q < nc3; q += kRThreads) s_X[q] = P.Xg[size_t(cta) * 9 * kMaxAgg + q];
+      __syncthreads();
+    }
     V z0 = A::zero(), z1 = A::zero(), z2 = A::zero();
     float cf[9] = {r.x, r.y, r.z, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     if (!sync.with_coarse(z0, z1, z2, cf, red, s_tmp9, P.partc, cs)) return;
-    coarse_aggregate(P, cs, s_ca);
-    __syncthreads();
-    coarse_correction(P, s_ca, s_X, 0.f, 0.f, s_e);
-    __syncthreads();
+    coarse_g(P, P.n_ctas, cs, s_pagg, s_X, s_g);
+    ce[0] = s_g[0]; ce[1] = s_g[1]; ce[2] = s_g[2];
   }
   // u = M r (patch-local), u exchanged with the neighbour patches through
   // epoch-tagged words, w = A u; then the dots of this step
 #define EOLC_PATCH_UW(g, d, q)                                               \
   do {                                                                       \
     u = patch_apply(sm, M, L, own, i, P.degree, r);                          \
-    u.x += s_e[0] * m.x; u.y += s_e[1] * m.y; u.z += s_e[2] * m.z;           \
+    u.x += ce[0] * m.x; u.y += ce[1] * m.y; u.z += ce[2] * m.z;              \
     epoch += 1u;                                                             \
     const unsigned tag_ = exch_tag(P.seq, epoch);                            \
     if (own) {                                                               \
@@ -1096,8 +1115,7 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
     if (coarse) {                                                            \
       float cf_[9] = {r.x, r.y, r.z, w.x, w.y, w.z, s.x, s.y, s.z};          \
       if (!sync.with_coarse(g, d, q, cf_, red, s_tmp9, P.partc, cs)) return; \
-      coarse_aggregate(P, cs, s_ca);                                         \
-      __syncthreads();                                                       \
+      coarse_g(P, P.n_ctas, cs, s_pagg, s_X, s_g);                               \
     } else if (!sync(g, d, q, red)) {                                        \
       return;                                                                \
     }                                                                        \
@@ -1123,10 +1141,8 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
     const V alpha = A::div(gam, denom);
     const float af = float(A::to_t(alpha)), bf = float(A::to_t(beta));
     restart = false;
-    if (coarse) {  // e for r' = r - alpha (w + beta s), from the aggregate sums
-      coarse_correction(P, s_ca, s_X, af, bf, s_e);
-      __syncthreads();
-    }
+    // coarse correction for r' = r - alpha (w + beta s)
+    for (int c = 0; c < 3; ++c) ce[c] = s_g[c] - af * (s_g[3 + c] + bf * s_g[6 + c]);
     if (own) {
       s = V4<float>{w.x + bf * s.x, w.y + bf * s.y, w.z + bf * s.z, 0.f};
       r = V4<float>{r.x - af * s.x, r.y - af * s.y, r.z - af * s.z, 0.f};
@@ -1169,8 +1185,7 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
     if (coarse) {  // with R r of the replaced residual
       float cf[9] = {r.x, r.y, r.z, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
       if (!sync.with_coarse(e0, e1, e2, cf, red, s_tmp9, P.partc, cs)) return;
-      coarse_aggregate(P, cs, s_ca);
-      __syncthreads();
+      coarse_g(P, P.n_ctas, cs, s_pagg, s_X, s_g);
     } else if (!sync(e0, e1, e2, red)) {
       return;
     }
@@ -1179,10 +1194,7 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
     rmax2 = e0;
     if (!A::finite(e0)) { status = EOLC_NONFINITE; break; }
     if (A::le(e0, tol2)) { converged = true; break; }
-    if (coarse) {
-      coarse_correction(P, s_ca, s_X, 0.f, 0.f, s_e);
-      __syncthreads();
-    }
+    for (int c = 0; c < 3; ++c) ce[c] = s_g[c];
     V g3 = A::zero(), d3 = A::zero(), rr3 = A::zero();
     EOLC_PATCH_UW(g3, d3, rr3);
     EOLC_PATCH_SUM(g3, d3, rr3);
@@ -1539,6 +1551,9 @@ struct PatchPlan {
   // aggregates its rows couple to (ctgt, own aggregate first, -1 padded)
   int n_agg = 0;
   std::vector<int> agg_first, hagg, ctgt;
+  // per coarse block (a, b): the (patch, target) records of cpart that sum
+  // to it, patches in order (cl_ptr over n_agg^2 blocks, cl_idx = c kMaxTgt + t)
+  std::vector<int> cl_ptr, cl_idx;
   std::vector<int16_t> bsl;   // per slice slot and lane: local row, or -1 - halo slot
   std::vector<int> gsrc;      // per slice slot and lane: block in the original order, or -1
   std::vector<int> slice_off, slice_len;  // per (patch, warp)
@@ -1693,6 +1708,14 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
     std::sort(t.begin() + 1, t.end());
     std::copy(t.begin(), t.end(), ctgt.begin() + size_t(c) * kMaxTgt);
   }
+  std::vector<int> cl_ptr(size_t(n_agg) * n_agg + 1, 0), cl_idx;
+  for (int a = 0; a < n_agg; ++a)
+    for (int b = 0; b < n_agg; ++b) {
+      for (int c = agg_first[a]; c < agg_first[a + 1]; ++c)
+        for (int t = 0; t < kMaxTgt && ctgt[size_t(c) * kMaxTgt + t] >= 0; ++t)
+          if (ctgt[size_t(c) * kMaxTgt + t] == b) cl_idx.push_back(c * kMaxTgt + t);
+      cl_ptr[size_t(a) * n_agg + b + 1] = int(cl_idx.size());
+    }
   out.G = G;
   out.perm = std::move(perm);
   out.rowptr = std::move(prow);
@@ -1712,6 +1735,8 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
   out.agg_first = std::move(agg_first);
   out.hagg = std::move(hagg);
   out.ctgt = std::move(ctgt);
+  out.cl_ptr = std::move(cl_ptr);
+  out.cl_idx = std::move(cl_idx);
   // warp slices of the pattern (for the learned G)
   out.slice_off.assign(size_t(G) * kWarps, 0);
   out.slice_len.assign(size_t(G) * kWarps, 0);
@@ -1749,8 +1774,9 @@ struct PatchWork {
   DevBuf<unsigned> fword;
   DevBuf<unsigned long long> tw;  // neighbour exchange: tagged values, zeroed once per plan
   int n_agg = 0;                  // coarse aggregates of the plan
-  DevBuf<int> agg_first, hagg, ctgt;
-  DevBuf<float> cpart, partc;
+  DevBuf<int> agg_first, hagg, ctgt, cl_ptr, cl_idx;
+  DevBuf<float> cpart, partc, Xg;
+  int coarse_age = -1;            // solves since the coarse operator was built (-1: never)
   unsigned seq = 0;               // launches (tag generation)
   DevBuf<int16_t> bsl;
   DevBuf<int> gsrc, slice_off, slice_len;
@@ -1795,7 +1821,7 @@ eolc_status patch_plan(PatchWork *w, const DevTopology &Tp, const double *X_d, i
   w->why = build_patch_plan(N, rowptr, colidx, X.empty() ? nullptr : &X, n_sm, L);
   if (!w->why.empty()) return EOLC_OK;
   // empty lists (e.g. no halo on a one-patch mesh) still get one element
-  for (auto *v : {&L.fblk, &L.hnode, &L.hagg})
+  for (auto *v : {&L.fblk, &L.hnode, &L.hagg, &L.cl_idx})
     if (v->empty()) v->push_back(0);
   if (L.fword.empty()) L.fword.push_back(0u);
   cudaError_t es[] = {
@@ -1816,8 +1842,10 @@ eolc_status patch_plan(PatchWork *w, const DevTopology &Tp, const double *X_d, i
       w->beqp.resize(size_t(N) * 3),
       w->part.resize(size_t(6) * L.G),
       upload_vec(w->agg_first, L.agg_first, s), upload_vec(w->ctgt, L.ctgt, s),
-      upload_vec(w->hagg, L.hagg, s),
+      upload_vec(w->hagg, L.hagg, s), upload_vec(w->cl_ptr, L.cl_ptr, s),
+      upload_vec(w->cl_idx, L.cl_idx, s),
       w->cpart.resize(size_t(L.G) * kMaxTgt * 9),
+      w->Xg.resize(size_t(L.G) * 9 * kMaxAgg),
       w->partc.resize(size_t(2) * kCoarseWords * L.G),
       w->tw.resize(size_t(8) * N),
       cudaMemsetAsync(w->tw.p, 0, sizeof(unsigned long long) * 8 * size_t(N), s),
@@ -1828,6 +1856,7 @@ eolc_status patch_plan(PatchWork *w, const DevTopology &Tp, const double *X_d, i
     if (e != cudaSuccess) { err = cudaGetErrorString(e); return EOLC_CUDA_ERROR; }
   w->G = L.G;
   w->n_agg = L.n_agg;
+  w->coarse_age = -1;
   return EOLC_OK;
 }
 
@@ -1850,7 +1879,8 @@ bool resident_fits(PatchWork *&w, const DevTopology &Tp, const double *X_d, cuda
 
 eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, int degree,
                              const float *Gm, eolc_solve_info *info, cudaStream_t s,
-                             std::string &err, long long &launches, bool coarse) {
+                             std::string &err, long long &launches, bool coarse,
+                             int coarse_refresh) {
   const bool patch_pc = mode == ResidentPC::kPatch, learned = mode == ResidentPC::kLearned;
   if (a.precision != EOLC_PREC_MIXED) {
     err = "the resident solvers run on the mixed-precision path";
@@ -1939,9 +1969,17 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, i
   P.slice_off = w->slice_off.p;
   P.slice_len = w->slice_len.p;
   P.n_agg = (patch_pc && coarse) ? w->n_agg : 0;
+  P.coarse_fresh = 1;
+  if (P.n_agg > 0) {  // rebuild the coarse operator, or reuse the last one
+    P.coarse_fresh = (w->coarse_age < 0 || w->coarse_age + 1 >= coarse_refresh) ? 1 : 0;
+    w->coarse_age = P.coarse_fresh ? 0 : w->coarse_age + 1;
+  }
+  P.Xg = w->Xg.p;
   P.agg_first = w->agg_first.p;
   P.hagg = w->hagg.p;
   P.ctgt = w->ctgt.p;
+  P.cl_ptr = w->cl_ptr.p;
+  P.cl_idx = w->cl_idx.p;
   P.cpart = w->cpart.p;
   P.partc = w->partc.p;
   P.tw = w->tw.p;

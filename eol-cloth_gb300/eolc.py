@@ -104,7 +104,7 @@ EXPORTS = ["eolc_version", "eolc_launch_count", "eolc_create", "eolc_destroy", "
            "eolc_attach_preconditioner", "eolc_set_jacobi_reference",
            "eolc_set_topology_batched", "eolc_set_instance_materials", "eolc_step_batched",
            "eolc_batch_num_configs", "eolc_batch_config_name", "eolc_batch_set_config",
-           "eolc_batch_autotune", "eolc_set_learned_refresh",
+           "eolc_batch_autotune", "eolc_set_learned_refresh", "eolc_set_coarse_refresh",
            "eolc_batch_set_jacobi_reference", "eolc_lpc_blocks"]
 
 
@@ -158,6 +158,7 @@ def load_library(path=LIB_PATH):
     L.eolc_attach_preconditioner.argtypes = [_V, _V]
     L.eolc_set_jacobi_reference.argtypes = [_V, ctypes.c_int]
     L.eolc_set_learned_refresh.argtypes = [_V, ctypes.c_int]
+    L.eolc_set_coarse_refresh.argtypes = [_V, ctypes.c_int]
     L.eolc_batch_set_jacobi_reference.argtypes = [_V, _I, ctypes.c_int]
     L.eolc_set_topology_batched.argtypes = [_V, ctypes.c_int, _I, _I, _I, _I, _I]
     L.eolc_set_instance_materials.argtypes = [_V, ctypes.POINTER(Material), ctypes.c_int]
@@ -360,6 +361,11 @@ class Context:
 
     def set_learned_refresh(self, solves):
         self._check(lib.eolc_set_learned_refresh(self._h, solves))
+
+    def set_coarse_refresh(self, solves):
+        """Rebuild the patch preconditioner's coarse operator every `solves`
+        solves (eolc_set_coarse_refresh)."""
+        self._check(lib.eolc_set_coarse_refresh(self._h, solves))
 
     def batch_set_jacobi_reference(self, iters):
         iters = _i32(iters)

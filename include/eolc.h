@@ -351,6 +351,11 @@ eolc_status eolc_attach_preconditioner(eolc_ctx *ctx, eolc_lpc *lpc);
  * iterations).  Applies to the shared-memory-resident solve; re-attaching a
  * network (eolc_attach_preconditioner) forces a new evaluation. */
 eolc_status eolc_set_learned_refresh(eolc_ctx *ctx, int solves);
+/* Rebuild the coarse operator of the two-level patch preconditioner (its
+ * assembly and inverse) every `solves` EOLC_PC_PATCH solves (default 1) and
+ * reuse it in between (a lagged coarse correction: still symmetric positive
+ * definite, so PCG stays exact).  A new topology forces a rebuild. */
+eolc_status eolc_set_coarse_refresh(eolc_ctx *ctx, int solves);
 /* Iteration count of a plain Jacobi solve that the learned solve's fallback
  * cap (fallback_factor x this count) refers to; set automatically by every
  * successful Jacobi solve on the context. */

@@ -76,6 +76,28 @@ def test_coarse_correction_keeps_solution_and_cuts_iterations(eolc, quads):
         assert np.mean(its2) <= 0.75 * np.mean(its1)
 
 
+def test_lagged_coarse_operator_converges(eolc):
+    """Coarse operator rebuilt every 3 solves (eolc_set_coarse_refresh): the
+    reused ones still give converged steps matching the fresh ones."""
+    s = scenes.sheet(64)
+    ctx = _ctx(eolc, s)
+    lag = _ctx(eolc, s)
+    lag.set_coarse_refresh(3)
+    mat = eolc.Material(**scenes.material_c1())
+    x, v = s["x"].copy(), np.zeros(3 * s["n"])
+    xl, vl = x.copy(), v.copy()
+    for step in range(5):
+        i1 = ctx.step(x, s["X"], v, mat, scenes.GRAV, scenes.H, s["fixed"], s["fixed_vel"],
+                      eolc.SolveOpts(precond=eolc.PC_PATCH))
+        i2 = lag.step(xl, s["X"], vl, mat, scenes.GRAV, scenes.H, s["fixed"], s["fixed_vel"],
+                      eolc.SolveOpts(precond=eolc.PC_PATCH))
+        assert i1.status == eolc.OK and i2.status == eolc.OK and i2.rel_res <= 1e-8
+        assert np.abs(vl - v).max() <= 1e-5 * np.abs(v).max()
+        print("step %d: fresh %d iterations, lagged %d" % (step, i1.iterations, i2.iterations))
+    with pytest.raises(eolc.EolcError):
+        lag.set_coarse_refresh(0)
+
+
 def test_patch_solve_matches_direct_solve(eolc):
     import oracle as O
     s = scenes.sheet(20)

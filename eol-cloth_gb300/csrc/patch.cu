@@ -52,6 +52,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <string>
 #include <vector>
@@ -134,12 +135,12 @@ struct ResParams {
                                            // -1 - halo window slot
   const int *slice_off, *slice_len;        // per (CTA, warp) slice: first slot, slots
   V4<float> *r[2], *s[2], *w[2], *p[2], *z, *q;
-  // coarse correction (patch PC; n_agg == 0: off): aggregates of consecutive
-  // patches, the aggregate of every halo node, per patch its target
+  // coarse correction (patch PC; n_agg == 0: off): the aggregate of every
+  // patch and of every halo node, per patch its target
   // aggregates; cpart: per (patch, target) the CTA's sum of masked blocks;
   // partc: per-CTA sums of r, w, s, [2][G][kCoarseWords]
   int n_agg, coarse_fresh;                 // fresh: rebuild X_own (else reuse Xg)
-  const int *agg_first, *hagg, *ctgt, *cl_ptr, *cl_idx;
+  const int *patch_agg, *hagg, *ctgt, *cl_ptr, *cl_idx;
   float *cpart, *partc, *Xg;               // Xg: every CTA's X_own of the last build
   unsigned long long *tw;                  // neighbour exchange: tagged u, [2][N][4] words
   unsigned seq;                            // launch number in the tags (1..4095)
@@ -778,8 +779,8 @@ __device__ void inverse3_masked(const float (&D)[9], const float (&m)[3], float 
 }
 
 // ---- coarse correction of the patch preconditioner ---------------------------
-// Coarse space: the three translations of each aggregate of consecutive
-// patches (R sums the free DOFs of an aggregate per axis, P = R^T).  The
+// Coarse space: the three translations of each aggregate of patches (compact
+// groups of patches: R sums the free DOFs of an aggregate per axis, P = R^T).  The
 // preconditioner is M = M_patch + R^T A_c^-1 R with A_c = R A R^T (masked).
 //
 // coarse_setup (once per solve, every CTA): the CTA's sums of masked blocks
@@ -1062,8 +1063,7 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
   float *cs = reinterpret_cast<float *>(sm.slot);  // every CTA's coarse partials
   if (i < 9) s_g[i] = 0.f;
   if (coarse)
-    for (int a = 0; a < P.n_agg; ++a)
-      for (int c = P.agg_first[a] + i; c < P.agg_first[a + 1]; c += kRThreads) s_pagg[c] = a;
+    for (int c = i; c < P.n_ctas; c += kRThreads) s_pagg[c] = P.patch_agg[c];
   float ce[3] = {0.f, 0.f, 0.f};  // this patch's coarse correction for the next u
   if (coarse) {
     const int nc3 = 9 * P.n_agg;  // X_own: 3 rows of 3 n_agg
@@ -1546,11 +1546,11 @@ struct PatchPlan {
   std::vector<int> perm, rowptr, colidx, src, tr, diag, patch_row, hnptr, hnode;
   std::vector<int> fptr, fblk, rcnt, wbase;  // shared-memory image (load_patch)
   std::vector<unsigned> fword;
-  // coarse space: n_agg aggregates of consecutive patches (agg_first), the
+  // coarse space: n_agg aggregates of patches (patch_agg), the
   // aggregate of every halo node (hagg, like hnode) and, per patch, the
   // aggregates its rows couple to (ctgt, own aggregate first, -1 padded)
   int n_agg = 0;
-  std::vector<int> agg_first, hagg, ctgt;
+  std::vector<int> patch_agg, hagg, ctgt;
   // per coarse block (a, b): the (patch, target) records of cpart that sum
   // to it, patches in order (cl_ptr over n_agg^2 blocks, cl_idx = c kMaxTgt + t)
   std::vector<int> cl_ptr, cl_idx;
@@ -1689,12 +1689,50 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
     fptr[c + 1] = fptr[c] + nrec;
   }
   for (int j : hnode) rcnt[j] |= 1 << 24;  // a halo node of some patch: it publishes
-  // coarse aggregates: consecutive patches of the bisection order
+  // coarse aggregates: recursive coordinate bisection of the patch centroids
+  // (material coordinates) into n_agg compact groups; without coordinates,
+  // runs of consecutive patches of the bisection order
   const int n_agg = std::min(G, kMaxAgg);
-  std::vector<int> agg_first(n_agg + 1), patch_agg(G), node_patch(N), hagg(hnode.size());
-  for (int a = 0; a <= n_agg; ++a) agg_first[a] = int((long long)a * G / n_agg);
-  for (int a = 0; a < n_agg; ++a)
-    for (int c = agg_first[a]; c < agg_first[a + 1]; ++c) patch_agg[c] = a;
+  std::vector<int> patch_agg(G), node_patch(N), hagg(hnode.size());
+  if (X) {
+    std::vector<double> cx(G, 0.0), cy(G, 0.0);
+    for (int c = 0; c < G; ++c) {
+      for (int i = patch_row[c]; i < patch_row[c + 1]; ++i) {
+        cx[c] += (*X)[2 * size_t(perm[i])];
+        cy[c] += (*X)[2 * size_t(perm[i]) + 1];
+      }
+      const int np = std::max(1, patch_row[c + 1] - patch_row[c]);
+      cx[c] /= np;
+      cy[c] /= np;
+    }
+    std::vector<int> ids(G);
+    for (int c = 0; c < G; ++c) ids[c] = c;
+    int next = 0;
+    std::function<void(int, int, int)> split = [&](int lo, int hi, int k) {
+      if (k <= 1) {
+        for (int q = lo; q < hi; ++q) patch_agg[ids[q]] = next;
+        ++next;
+        return;
+      }
+      double x0 = 1e300, x1 = -1e300, y0 = 1e300, y1 = -1e300;
+      for (int q = lo; q < hi; ++q) {
+        x0 = std::min(x0, cx[ids[q]]); x1 = std::max(x1, cx[ids[q]]);
+        y0 = std::min(y0, cy[ids[q]]); y1 = std::max(y1, cy[ids[q]]);
+      }
+      const bool by_x = x1 - x0 >= y1 - y0;
+      std::sort(ids.begin() + lo, ids.begin() + hi, [&](int a, int b) {
+        const double va = by_x ? cx[a] : cy[a], vb = by_x ? cx[b] : cy[b];
+        return va < vb || (va == vb && a < b);
+      });
+      const int k1 = k / 2;
+      const int mid = lo + int((long long)(hi - lo) * k1 / k);
+      split(lo, mid, k1);
+      split(mid, hi, k - k1);
+    };
+    split(0, G, n_agg);
+  } else {
+    for (int c = 0; c < G; ++c) patch_agg[c] = int((long long)c * n_agg / G);
+  }
   for (int c = 0; c < G; ++c)
     for (int i = patch_row[c]; i < patch_row[c + 1]; ++i) node_patch[i] = c;
   std::vector<int> ctgt(size_t(G) * kMaxTgt, -1);
@@ -1708,10 +1746,12 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
     std::sort(t.begin() + 1, t.end());
     std::copy(t.begin(), t.end(), ctgt.begin() + size_t(c) * kMaxTgt);
   }
+  std::vector<std::vector<int>> members(n_agg);
+  for (int c = 0; c < G; ++c) members[patch_agg[c]].push_back(c);
   std::vector<int> cl_ptr(size_t(n_agg) * n_agg + 1, 0), cl_idx;
   for (int a = 0; a < n_agg; ++a)
     for (int b = 0; b < n_agg; ++b) {
-      for (int c = agg_first[a]; c < agg_first[a + 1]; ++c)
+      for (int c : members[a])
         for (int t = 0; t < kMaxTgt && ctgt[size_t(c) * kMaxTgt + t] >= 0; ++t)
           if (ctgt[size_t(c) * kMaxTgt + t] == b) cl_idx.push_back(c * kMaxTgt + t);
       cl_ptr[size_t(a) * n_agg + b + 1] = int(cl_idx.size());
@@ -1732,7 +1772,7 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
   out.hnptr = std::move(hnptr);
   out.hnode = std::move(hnode);
   out.n_agg = n_agg;
-  out.agg_first = std::move(agg_first);
+  out.patch_agg = std::move(patch_agg);
   out.hagg = std::move(hagg);
   out.ctgt = std::move(ctgt);
   out.cl_ptr = std::move(cl_ptr);
@@ -1774,7 +1814,7 @@ struct PatchWork {
   DevBuf<unsigned> fword;
   DevBuf<unsigned long long> tw;  // neighbour exchange: tagged values, zeroed once per plan
   int n_agg = 0;                  // coarse aggregates of the plan
-  DevBuf<int> agg_first, hagg, ctgt, cl_ptr, cl_idx;
+  DevBuf<int> patch_agg, hagg, ctgt, cl_ptr, cl_idx;
   DevBuf<float> cpart, partc, Xg;
   int coarse_age = -1;            // solves since the coarse operator was built (-1: never)
   unsigned seq = 0;               // launches (tag generation)
@@ -1841,7 +1881,7 @@ eolc_status patch_plan(PatchWork *w, const DevTopology &Tp, const double *X_d, i
       w->bp.resize(size_t(N) * 3),
       w->beqp.resize(size_t(N) * 3),
       w->part.resize(size_t(6) * L.G),
-      upload_vec(w->agg_first, L.agg_first, s), upload_vec(w->ctgt, L.ctgt, s),
+      upload_vec(w->patch_agg, L.patch_agg, s), upload_vec(w->ctgt, L.ctgt, s),
       upload_vec(w->hagg, L.hagg, s), upload_vec(w->cl_ptr, L.cl_ptr, s),
       upload_vec(w->cl_idx, L.cl_idx, s),
       w->cpart.resize(size_t(L.G) * kMaxTgt * 9),
@@ -1975,7 +2015,7 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, i
     w->coarse_age = P.coarse_fresh ? 0 : w->coarse_age + 1;
   }
   P.Xg = w->Xg.p;
-  P.agg_first = w->agg_first.p;
+  P.patch_agg = w->patch_agg.p;
   P.hagg = w->hagg.p;
   P.ctgt = w->ctgt.p;
   P.cl_ptr = w->cl_ptr.p;

@@ -432,8 +432,10 @@ def run_ours(args, rank, world, local_rank):
     bpi = algorithmic_bytes_per_iter(sc["n"], n_blocks)
     if best.startswith("learned"):
         bpi += n_blocks * (36 + 4)  # one more BSR apply (G, pattern of MDK)
-    elif best == "patch":
-        bpi += (max(1, args.degree) - 1) * n_blocks * 36  # local Chebyshev products
+    elif best.startswith("patch"):
+        # the k - 1 local Chebyshev products (patch-internal blocks; counted
+        # as all blocks plus an input and an output 3-vector)
+        bpi += (max(1, args.degree) - 1) * (n_blocks * 36 + 2 * sc["n"] * 12)
     achieved = bpi * res["mean_pcg_iters"] / (res["pcg_kernel_ms"] / 1e3) / 1e9
     kernel = ARM_KERNEL[best]
     traffic = None
@@ -473,9 +475,12 @@ def run_ours(args, rank, world, local_rank):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "kernel": kernel,
                      "algorithmic_bytes_per_iter": bpi,
-                     "note": "achieved = HBM-streamed algorithmic bytes per iteration x "
-                             "iterations / kernel time; the resident kernels read the matrix "
-                             "from HBM once per solve (traffic) and are latency-bound"},
+                     "note": "achieved = the bytes an HBM-streamed implementation of the "
+                             "method moves per iteration (every product's matrix and vectors "
+                             "plus the CG vector passes) x iterations / kernel time: frac > 1 "
+                             "means no HBM-streamed implementation could match it; the "
+                             "resident kernels read the matrix from HBM once per solve "
+                             "(traffic) and are bound by synchronisation latency"},
         "clocks": clk.summary(),
     }
     if cpu:

@@ -85,20 +85,23 @@ typedef struct {
                            one-level patch preconditioner                */
 } eolc_solve_opts;
 
-/* Resident solves (mixed precision): the nodes are split by recursive graph
- * bisection into one compact patch per SM (at most about 448 nodes each);
- * each SM holds its rows of the FP32 matrix in shared memory for the whole
- * solve and each row's vectors in one thread's registers.  Point / block
- * Jacobi then run as a single-grid-barrier Chronopoulos-Gear PCG.
+/* Resident solves (mixed precision): the nodes are split by recursive
+ * coordinate (or graph) bisection into one compact patch per SM (at most
+ * about 448 nodes each); each SM holds its rows of the FP32 matrix in shared
+ * memory for the whole solve and each row's vectors in one thread's
+ * registers; every preconditioner runs as a single-grid-barrier
+ * Chronopoulos-Gear PCG.
  * EOLC_PC_PATCH (resident only; no counterpart in the reference, whose solve
- * is Eigen's Jacobi CG, GeneralizedSolver.cpp:123-126): the preconditioner is
- * a degree-k Chebyshev polynomial of the block-Jacobi-preconditioned,
- * unit-diagonal-scaled principal submatrix of each patch on [l/30, l], l an
- * upper bound of its spectrum (so it is symmetric positive definite), applied
- * with SM-local barriers; two grid barriers per PCG iteration.  Every solve
- * converges on the same FP64 relative residual.  Meshes too large for the
- * resident image stream the matrix (Jacobi) or are rejected with
- * EOLC_BAD_ARG (EOLC_PC_PATCH). */
+ * is Eigen's Jacobi CG, GeneralizedSolver.cpp:123-126): a two-level
+ * preconditioner.  Local level: a degree-k Chebyshev polynomial of the
+ * block-Jacobi-preconditioned, unit-diagonal-scaled principal submatrix of
+ * each patch on [l/30, l], l an upper bound of its spectrum (symmetric
+ * positive definite), applied with SM-local barriers.  Coarse level (unless
+ * no_coarse): the translations of up to 42 aggregates of patches, with the
+ * coarse matrix R A R^T assembled and inverted on the device (see
+ * eolc_set_coarse_refresh).  Every solve converges on the same FP64 relative
+ * residual.  Meshes too large for the resident image stream the matrix
+ * (Jacobi) or are rejected with EOLC_BAD_ARG (EOLC_PC_PATCH). */
 
 typedef struct {
   int status;        /* eolc_status of the solve                          */

@@ -500,7 +500,7 @@ def main():
     ap.add_argument("--precond", default="all",
                     help="comma-separated arms among jacobi, jacobi-streamed, block, patch, "
                          "learned, learned-r4; 'all' times all but block")
-    ap.add_argument("--degree", type=int, default=6, help="patch preconditioner degree")
+    ap.add_argument("--degree", type=int, default=5, help="patch preconditioner degree")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-sheets line")
     ap.add_argument("--batch-sheets", type=int, default=256)

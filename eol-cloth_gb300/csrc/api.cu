@@ -26,7 +26,7 @@ namespace {
     }                                                                \
   } while (0)
 
-constexpr int kDefaultPatchDegree = 6;  // Chebyshev degree of the patch solves
+constexpr int kDefaultPatchDegree = 5;  // Chebyshev degree of the patch solves
 
 eolc_status fail(eolc_ctx *ctx, eolc_status s, const char *msg) {
   if (ctx) ctx->err = msg;

@@ -75,7 +75,7 @@ typedef struct {
                            fallback_factor * (last Jacobi count) iterations;
                            0 disables the fallback                       */
   int degree;           /* patch PC: Chebyshev degree of the local solves
-                           (0: 6)                                        */
+                           (0: 5)                                        */
   int streamed;         /* Jacobi / block Jacobi on the mixed path: 0 runs
                            the shared-memory-resident kernel when the mesh
                            fits (about 448 nodes per SM), 1 always streams

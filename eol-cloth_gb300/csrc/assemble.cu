@@ -21,7 +21,8 @@ namespace {
 
 // Element pass, triangles: d_B h^2 K_e block (la, lb) of face t at
 // Kt[((t * 3 + la) * 3 + lb) * 9 ...] (fillxxMI, Forces.cpp:103-125), and
-// t8 = rho 2 A (ComputeInertial.cpp:33).
+// t8 = rho 2 A (ComputeInertial.cpp:33).  K_e is symmetric: the blocks with
+// la <= lb are evaluated and (lb, la) gets the transpose.
 template <typename T>
 __global__ void __launch_bounds__(128)
 tri_blocks_kernel(int n_tri, const int *__restrict__ tri, const double *__restrict__ x,
@@ -38,19 +39,26 @@ tri_blocks_kernel(int n_tri, const int *__restrict__ tri, const double *__restri
 #pragma unroll 1
   for (int la = 0; la < 3; ++la)
 #pragma unroll 1
-    for (int lb = 0; lb < 3; ++lb) {
+    for (int lb = la; lb < 3; ++lb) {
       T blk[9];
 #pragma unroll
       for (int k = 0; k < 9; ++k) blk[k] = T(0);
       add_membrane_block<T, T>(q, la, lb, mu, lam, dh2, blk);
 #pragma unroll
       for (int k = 0; k < 9; ++k) out[(3 * la + lb) * 9 + k] = blk[k];
+      if (lb != la)
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) out[(3 * lb + la) * 9 + 3 * c + r] = blk[3 * r + c];
     }
   t8[t] = T(m.rho) * T(2) * q.A;
 }
 
 // Element pass, hinges: d_B h^2 K_b block (la, lb) of hinge e at
 // Kh[((e * 4 + la) * 4 + lb) * 9 ...] (fillxxB, Forces.cpp:522-539, 885-908).
+// K_b is a Hessian: the blocks with la <= lb are evaluated and (lb, la) gets
+// the transpose.
 template <typename T>
 __global__ void __launch_bounds__(128)
 hinge_blocks_kernel(int n_hinge, const int *__restrict__ hinge, const double *__restrict__ x,
@@ -68,13 +76,18 @@ hinge_blocks_kernel(int n_hinge, const int *__restrict__ hinge, const double *__
 #pragma unroll 1
   for (int la = 0; la < 4; ++la)
 #pragma unroll 1
-    for (int lb = 0; lb < 4; ++lb) {
+    for (int lb = la; lb < 4; ++lb) {
       T blk[9];
 #pragma unroll
       for (int k = 0; k < 9; ++k) blk[k] = T(0);
       add_bending_block<T, T>(H, la, lb, dh2, blk);
 #pragma unroll
       for (int k = 0; k < 9; ++k) out[(4 * la + lb) * 9 + k] = blk[k];
+      if (lb != la)
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) out[(4 * lb + la) * 9 + 3 * c + r] = blk[3 * r + c];
     }
 }
 

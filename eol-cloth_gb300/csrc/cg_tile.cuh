@@ -608,6 +608,53 @@ __global__ void setup_kernel(int n_nodes, const int *rowptr, const int *colidx,
                 xacc, pc, fmask);
 }
 
+// setup_kernel (128 threads per block) plus each block's FP64 partial of
+// ||rhs||^2 (warp trees, then the four warps in order).
+template <typename T>
+__global__ void __launch_bounds__(128)
+    setup_norm_kernel(int n_nodes, const int *rowptr, const int *colidx, const int *diag,
+                      const T *A, const double *b, const double *beq_full,
+                      const uint8_t *pinned, int block_pc, V4<double> *rhs, V4<double> *x64,
+                      V4<T> *r, V4<T> *p, V4<T> *s, V4<T> *xacc, T *pc, V4<T> *fmask,
+                      double *part) {
+  __shared__ double red[4];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double s2 = 0.0;
+  if (i < n_nodes) {
+    setup_node<T>(i, rowptr, colidx, diag, A, b, beq_full, pinned, block_pc, rhs, x64, r, p, s,
+                  xacc, pc, fmask);
+    const V4<double> q = rhs[i];
+    s2 = q.x * q.x + q.y * q.y + q.z * q.z;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s2;
+  __syncthreads();
+  if (threadIdx.x == 0) part[blockIdx.x] = (red[0] + red[1]) + (red[2] + red[3]);
+}
+
+// ||rhs||^2 from the nb partials of setup_norm_kernel (one CTA of 256
+// threads, a fixed order); resets the status record.
+__global__ void __launch_bounds__(256) norm_finish_kernel(int nb, const double *part,
+                                                          DevStatus *st) {
+  __shared__ double red[8];
+  double s2 = 0.0;
+  for (int k = threadIdx.x; k < nb; k += 256) s2 += part[k];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s2;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double v = 0.0;
+    for (int w = 0; w < 8; ++w) v += red[w];
+    st->status = EOLC_OK;
+    st->iterations = 0;
+    st->refinements = 0;
+    st->rel_res = v > 0 ? 1.0 : 0.0;
+    st->rhs_norm2 = v;
+  }
+}
+
 // ||rhs||^2 by one CTA; resets the status record.
 template <class C>
 __global__ void __launch_bounds__(C::kThreads) init_sums_kernel(int n_nodes, const V4<double> *rhs,

@@ -1816,6 +1816,7 @@ struct PatchWork {
   int n_agg = 0;                  // coarse aggregates of the plan
   DevBuf<int> patch_agg, hagg, ctgt, cl_ptr, cl_idx;
   DevBuf<float> cpart, partc, Xg;
+  DevBuf<double> npart;           // per set-up block: partial of ||rhs||^2
   int coarse_age = -1;            // solves since the coarse operator was built (-1: never)
   unsigned seq = 0;               // launches (tag generation)
   DevBuf<int16_t> bsl;
@@ -1976,10 +1977,15 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, i
   }
   permute_vectors_kernel<<<nn, 128, 0, s>>>(N, w->perm.p, a.b, a.beq_full, a.pinned, w->bp.p,
                                              w->beqp.p, w->pinp.p);
-  setup_kernel<float><<<nn, 128, 0, s>>>(N, w->rowptr.p, w->colidx.p, w->diag.p, w->Ap.p, w->bp.p,
-                                         w->beqp.p, w->pinp.p, bpc, rhs, x64, P.r[0], P.p[0],
-                                         P.s[0], xacc, pc, fmask);
-  init_sums_kernel<RCfg><<<1, kRThreads, 0, s>>>(N, rhs, w->st.p);
+  if (w->npart.resize(size_t(nn)) != cudaSuccess) {
+    err = "device allocation failed";
+    return EOLC_CUDA_ERROR;
+  }
+  setup_norm_kernel<float><<<nn, 128, 0, s>>>(N, w->rowptr.p, w->colidx.p, w->diag.p, w->Ap.p,
+                                              w->bp.p, w->beqp.p, w->pinp.p, bpc, rhs, x64,
+                                              P.r[0], P.p[0], P.s[0], xacc, pc, fmask,
+                                              w->npart.p);
+  norm_finish_kernel<<<1, 256, 0, s>>>(nn, w->npart.p, w->st.p);
   cudaMemsetAsync(w->bar.p, 0, sizeof(unsigned) * 2, s);
   P.n_nodes = N;
   P.n_ctas = G;

@@ -286,7 +286,7 @@ def run_reference(args, rank):
 ARM_KERNEL = {"jacobi": "jacobi_resident_kernel", "block": "jacobi_resident_kernel",
               "patch": "patch_resident_kernel", "patch-1l": "patch_resident_kernel",
               "patch-r4": "patch_resident_kernel",
-              "learned": "learned_resident_kernel",
+              "learned": "learned_resident_kernel", "learned-1l": "learned_resident_kernel",
               "learned-r4": "learned_resident_kernel", "jacobi-streamed": "cg_kernel"}
 
 
@@ -306,6 +306,8 @@ def arm_opts(eolc, arm, degree):
         return eolc.SolveOpts(precond=eolc.PC_PATCH, degree=degree, no_coarse=1, **base)
     if arm in ("learned", "learned-r4"):
         return eolc.SolveOpts(precond=eolc.PC_LEARNED, fallback_factor=2, **base)
+    if arm == "learned-1l":
+        return eolc.SolveOpts(precond=eolc.PC_LEARNED, fallback_factor=2, no_coarse=1, **base)
     raise ValueError(arm)
 
 
@@ -372,7 +374,8 @@ def run_ours(args, rank, world, local_rank):
     lpc = None
     weights = os.path.join(ROOT, "eol-cloth_gb300", "weights", "lpc.npy")
     arms = args.precond.split(",") if args.precond != "all" else \
-        ["jacobi", "jacobi-streamed", "patch", "patch-r4", "patch-1l", "learned", "learned-r4"]
+        ["jacobi", "jacobi-streamed", "patch", "patch-r4", "patch-1l", "learned", "learned-r4",
+         "learned-1l"]
     if any(a.startswith("learned") for a in arms):
         if os.path.exists(weights):
             lpc = eolc.LearnedPC(local_rank)

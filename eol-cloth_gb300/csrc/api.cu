@@ -181,7 +181,8 @@ eolc_status solve_device(eolc_ctx *ctx, const eolc_solve_opts *o,
     if (o->fallback_factor > 0 && ctx->last_jacobi_iters > 0)
       al.max_iter = std::min(o->max_iter, o->fallback_factor * ctx->last_jacobi_iters);
     eolc_status st = resident ? run_pcg_resident(ctx->pwork, al, ResidentPC::kLearned, 0, Gm, inf,
-                                                 s, ctx->err, ctx->launches)
+                                                 s, ctx->err, ctx->launches, o->no_coarse == 0,
+                                                 ctx->coarse_refresh)
                               : run_pcg_learned(ctx->work, al, Gm, inf, s, ctx->err, ctx->launches);
     if (st == EOLC_OK || o->fallback_factor <= 0) return st;
     const double kms = inf->solve_kernel_ms;

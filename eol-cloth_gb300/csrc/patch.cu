@@ -390,9 +390,10 @@ struct GridSum {
   // r, w, s): their CTA sums (fixed trees) go to partc beside the
   // double-float partials, and after the barrier every CTA's nine sums are
   // copied to cs[12 c + q] (shared memory) for the caller.
+  template <class F = NoPre>
   __device__ bool with_coarse(Acc<float>::V &a, Acc<float>::V &b, Acc<float>::V &c,
                               float (&cf)[9], Acc<float>::V *red, float *cwred, float *partc,
-                              float *cs) {
+                              float *cs, F &&pre = F()) {
     using Ac = Acc<float>;
     using V = Ac::V;
     constexpr int NW = kRThreads / 32;
@@ -436,6 +437,7 @@ struct GridSum {
       }
     }
     if (!grid_barrier(bar, G, epoch, st)) return false;
+    pre();
     for (int t = threadIdx.x; t < 3 * G; t += kRThreads)
       reinterpret_cast<float4 *>(cs)[t] = __ldcg(reinterpret_cast<const float4 *>(pc) + t);
     if (warp == 0) {
@@ -1246,6 +1248,9 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ V red[3 * (kRThreads / 32 + 1)];
   __shared__ int s_fail;
+  __shared__ float s_tmp9[9 * kWarps], s_X[3 * 3 * kMaxAgg], s_g[9];
+  __shared__ int s_pagg[32 * kPartPerLane];  // aggregate of every patch
+  __shared__ float s_gj[2 * 3 * kMaxAgg];     // coarse set-up: pivot row and column
   const ResSmem sm = carve(smem);
   const int cta = blockIdx.x, i = threadIdx.x;
   const int p0 = P.patch_row[cta], np = P.patch_row[cta + 1] - p0;
@@ -1279,6 +1284,29 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
   unsigned epoch = 0;
   int cur = 0;
   __syncthreads();  // the resident image is complete
+  // coarse correction (as in the patch kernel): A_c^-1 rows of this
+  // aggregate, then e for r_0
+  const bool coarse = P.n_agg > 0;
+  float *cs = reinterpret_cast<float *>(sm.slot);  // every CTA's coarse partials
+  if (i < 9) s_g[i] = 0.f;
+  if (coarse)
+    for (int c = i; c < P.n_ctas; c += kRThreads) s_pagg[c] = P.patch_agg[c];
+  float ce[3] = {0.f, 0.f, 0.f};
+  if (coarse) {
+    const int nc3 = 9 * P.n_agg;
+    if (P.coarse_fresh) {
+      if (!coarse_setup(P, sm, M, cta, p0, own, m, sync, s_tmp9, s_gj, s_X)) return;
+      for (int q = i; q < nc3; q += kRThreads) P.Xg[size_t(cta) * 9 * kMaxAgg + q] = s_X[q];
+    } else {
+      for (int q = i; q < nc3; q += kRThreads) s_X[q] = P.Xg[size_t(cta) * 9 * kMaxAgg + q];
+      __syncthreads();
+    }
+    V z0 = A::zero(), z1 = A::zero(), z2 = A::zero();
+    float cf[9] = {r.x, r.y, r.z, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (!sync.with_coarse(z0, z1, z2, cf, red, s_tmp9, P.partc, cs)) return;
+    coarse_g(P, P.n_ctas, cs, s_pagg, s_X, s_g);
+    ce[0] = s_g[0]; ce[1] = s_g[1]; ce[2] = s_g[2];
+  }
   // u = G r (xs / xh hold r), u exchanged with the neighbours, w = A u
   // published to w[c]; then the dots of this step
 #define EOLC_LPC_UW(c, g, d, q)                                            \
@@ -1286,7 +1314,8 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
     __syncthreads();                                                       \
     if (own) {                                                             \
       const V4<float> g_ = apply_G(P, sm, cta);                            \
-      u = V4<float>{g_.x * m.x, g_.y * m.y, g_.z * m.z, 0.f};              \
+      u = V4<float>{(g_.x + ce[0]) * m.x, (g_.y + ce[1]) * m.y,            \
+                    (g_.z + ce[2]) * m.z, 0.f};                            \
     }                                                                      \
     __syncthreads();                                                       \
     epoch += 1u;                                                           \
@@ -1313,12 +1342,25 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
       q = A::addf(q, dot3(r, r));                                          \
     }                                                                      \
   } while (0)
+  // the step's reduction (prefetching the halo r, s, w of pf), with the
+  // patch's sums of r, w, s when coarse
+#define EOLC_LPC_SUM(g, d, q)                                                  \
+  do {                                                                         \
+    if (coarse) {                                                              \
+      float cf_[9] = {r.x, r.y, r.z, w.x, w.y, w.z, s.x, s.y, s.z};            \
+      if (!sync.with_coarse(g, d, q, cf_, red, s_tmp9, P.partc, cs, prefetch)) \
+        return;                                                                \
+      coarse_g(P, P.n_ctas, cs, s_pagg, s_X, s_g);                             \
+    } else if (!sync(g, d, q, red, prefetch)) {                                \
+      return;                                                                  \
+    }                                                                          \
+  } while (0)
   V gam = A::zero(), del = A::zero(), rr = A::zero();
   if (own) sm.xs[i] = f4(r);
   if (hj >= 0) sm.xh[i] = f4(P.r[cur][hj]);
   EOLC_LPC_UW(cur, gam, del, rr);
   pf = cur;
-  if (!sync(gam, del, rr, red, prefetch)) return;
+  EOLC_LPC_SUM(gam, del, rr);
   if (s_fail) return;  // a neighbour exchange timed out (status recorded)
   V rmax2 = rr;
   double last_rr64 = A::to_d(rr);
@@ -1338,6 +1380,8 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
     const float af = float(A::to_t(alpha)), bf = float(A::to_t(beta));
     restart = false;
     const int nxt = cur ^ 1;
+    // coarse correction for r' = r - alpha (w + beta s)
+    for (int c = 0; c < 3; ++c) ce[c] = s_g[c] - af * (s_g[3 + c] + bf * s_g[6 + c]);
     if (own) {
       s = V4<float>{w.x + bf * s.x, w.y + bf * s.y, w.z + bf * s.z, 0.f};
       r = V4<float>{r.x - af * s.x, r.y - af * s.y, r.z - af * s.z, 0.f};
@@ -1354,7 +1398,7 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
     V g2 = A::zero(), d2 = A::zero(), rr2 = A::zero();
     EOLC_LPC_UW(nxt, g2, d2, rr2);
     pf = nxt;
-    if (!sync(g2, d2, rr2, red, prefetch)) return;
+    EOLC_LPC_SUM(g2, d2, rr2);
     if (s_fail) return;
     ++it;
     cur = nxt;
@@ -1388,23 +1432,31 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
       P.s[cur][row] = s;
     }
     V e0 = A::from_d(rr64d), e1 = A::zero(), e2 = A::zero();
-    if (!sync(e0, e1, e2, red)) return;  // also publishes r, s
+    if (coarse) {  // with R r of the replaced residual; also publishes r, s
+      float cf[9] = {r.x, r.y, r.z, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      if (!sync.with_coarse(e0, e1, e2, cf, red, s_tmp9, P.partc, cs)) return;
+      coarse_g(P, P.n_ctas, cs, s_pagg, s_X, s_g);
+    } else if (!sync(e0, e1, e2, red)) {
+      return;
+    }
     ++nref;
     last_rr64 = A::to_d(e0);
     rmax2 = e0;
     if (!A::finite(e0)) { status = EOLC_NONFINITE; break; }
     if (A::le(e0, tol2)) { converged = true; break; }
     V g3 = A::zero(), d3 = A::zero(), rr3 = A::zero();
+    for (int c = 0; c < 3; ++c) ce[c] = s_g[c];
     if (own) sm.xs[i] = f4(r);
     if (hj >= 0) sm.xh[i] = f4(P.r[cur][hj]);
     EOLC_LPC_UW(cur, g3, d3, rr3);
     pf = cur;
-    if (!sync(g3, d3, rr3, red, prefetch)) return;
+    EOLC_LPC_SUM(g3, d3, rr3);
     if (s_fail) return;
     gam = g3;
     del = d3;
   }
 #undef EOLC_LPC_UW
+#undef EOLC_LPC_SUM
   if (converged) status = EOLC_OK;
   if (cta == 0 && threadIdx.x == 0) {
     atomicCAS(&P.st->status, EOLC_OK, status);
@@ -2014,7 +2066,7 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, i
   P.bsl = w->bsl.p;
   P.slice_off = w->slice_off.p;
   P.slice_len = w->slice_len.p;
-  P.n_agg = (patch_pc && coarse) ? w->n_agg : 0;
+  P.n_agg = ((patch_pc || learned) && coarse) ? w->n_agg : 0;
   P.coarse_fresh = 1;
   if (P.n_agg > 0) {  // rebuild the coarse operator, or reuse the last one
     P.coarse_fresh = (w->coarse_age < 0 || w->coarse_age + 1 >= coarse_refresh) ? 1 : 0;

@@ -80,9 +80,10 @@ typedef struct {
                            the shared-memory-resident kernel when the mesh
                            fits (about 448 nodes per SM), 1 always streams
                            the matrix from memory tile by tile           */
-  int no_coarse;        /* patch PC: 0 adds the coarse-grid correction on
-                           aggregates of patches (default), 1 runs the
-                           one-level patch preconditioner                */
+  int no_coarse;        /* patch and learned PCs on the resident path: 0
+                           adds the coarse-grid correction on aggregates
+                           of patches (default), 1 runs the one-level
+                           preconditioner                                */
 } eolc_solve_opts;
 
 /* Resident solves (mixed precision): the nodes are split by recursive

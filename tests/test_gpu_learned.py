@@ -130,21 +130,29 @@ def test_trained_network_needs_fewer_iterations_than_jacobi(eolc):
     lpc.set_params(np.load(WEIGHTS))
     lpc.attach(ctx)
     x, v = s["x"].copy(), np.zeros(3 * s["n"])
-    it_j, it_l = [], []
+    it_j, it_l, it_2 = [], [], []
     for k in range(6):
         xl, vl = x.copy(), v.copy()
+        x2, v2 = x.copy(), v.copy()
         ij = ctx.step(x, s["X"], v, mat, scenes.GRAV, scenes.H, s["fixed"], s["fixed_vel"],
                       eolc.SolveOpts(precond=eolc.PC_JACOBI))
         il = ctx.step(xl, s["X"], vl, mat, scenes.GRAV, scenes.H, s["fixed"], s["fixed_vel"],
+                      eolc.SolveOpts(precond=eolc.PC_LEARNED, fallback_factor=0, no_coarse=1))
+        i2 = ctx.step(x2, s["X"], v2, mat, scenes.GRAV, scenes.H, s["fixed"], s["fixed_vel"],
                       eolc.SolveOpts(precond=eolc.PC_LEARNED, fallback_factor=0))
         assert il.status == eolc.OK and il.rel_res <= 1e-8
+        assert i2.status == eolc.OK and i2.rel_res <= 1e-8
+        assert np.abs(v2 - v).max() <= 1e-5 * np.abs(v).max()
         it_j.append(ij.iterations)
         it_l.append(il.iterations)
+        it_2.append(i2.iterations)
     gain = 1.0 - np.mean(it_l) / np.mean(it_j)
-    print("mean PCG iterations: Jacobi %.1f, learned %.1f (%.1f%% fewer)"
-          % (np.mean(it_j), np.mean(it_l), 100 * gain))
-    # the committed network (white-noise probes) needs ~45% fewer here
+    print("mean PCG iterations: Jacobi %.1f, learned %.1f (%.1f%% fewer), learned + coarse %.1f"
+          % (np.mean(it_j), np.mean(it_l), 100 * gain, np.mean(it_2)))
+    # the committed network alone (white-noise probes) needs ~45% fewer here
     assert gain >= 0.30
+    # and the coarse-grid correction removes more
+    assert np.mean(it_2) <= np.mean(it_l)
 
 
 def test_learned_refresh_reuses_the_network_output(eolc):

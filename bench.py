@@ -357,6 +357,54 @@ def time_arm(ctx, sc, mat, opts, x_w, v_w, steps, stream, flush, world, dev, ref
             "launches": ctx.launch_count() - launches0}
 
 
+def run_export(ctx, sc, x, stream, frames=10):
+    """OBJ frame export of the current state (the two files of
+    Cloth::exportBrender): device text generation into host memory and into
+    files, against the oracle's sprintf text of the same frame."""
+    import tempfile
+    import numpy as np
+    import torch
+    import oracle as O
+    ctx.state_upload(x, sc["X"], np.zeros_like(x))
+    a, b = ctx.export_obj_text(1, H)  # warm-up (buffers)
+    t0 = time.perf_counter()
+    ra, rb = O.obj_text(x, sc["X"], sc["tri"], frame=1, time=H)
+    cpu_s = time.perf_counter() - t0
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    text_ms, dev_ms = [], []
+    for k in range(frames):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ev0.record(stream)
+        ctx.export_obj_text(k, k * H)
+        ev1.record(stream)
+        text_ms.append(1e3 * (time.perf_counter() - t0))
+        ev1.synchronize()
+        dev_ms.append(ev0.elapsed_time(ev1))
+    file_ms = []
+    with tempfile.TemporaryDirectory() as d:
+        for k in range(frames):
+            t0 = time.perf_counter()
+            ctx.export_obj(d, k, k * H)
+            file_ms.append(1e3 * (time.perf_counter() - t0))
+    nbytes = len(a) + len(b)
+    med = lambda v: float(np.median(v))
+    return {"workload": "2 OBJ files (Cloth2D, Cloth3D) of the 256x256-quad sheet state, "
+                        "%d bytes per frame" % nbytes,
+            "byte_identical_to_oracle": (a, b) == (ra, rb),
+            "frames_per_s_text": 1e3 / med(text_ms), "ms_per_frame_text": med(text_ms),
+            "ms_per_frame_device": med(dev_ms), "text_gb_s": nbytes / med(text_ms) / 1e6,
+            "ms_per_frame_files": med(file_ms),
+            "gpu_launches_per_frame": 4,
+            "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "frames/s", "cores": 1,
+                             "kind": "port", "sample": "one frame's text by the oracle "
+                                                       "(the reference's sprintf formats)"},
+            "note": "text: device formatting + one device-to-host copy into pinned memory + "
+                    "copy into the caller's buffer; device: the same on the stream's clock "
+                    "(one host round trip for the text size inside); files: text + two "
+                    "fwrite calls to a temporary directory"}
+
+
 def run_ours(args, rank, world, local_rank):
     import numpy as np
     import torch
@@ -488,6 +536,8 @@ def run_ours(args, rank, world, local_rank):
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    if world == 1 and not args.no_export:
+        line["obj_export"] = run_export(ctx, sc, x_w, stream)
     if world == 1 and not args.no_batch:
         line["batched"] = run_batched(args, local_rank, stream, flush)
         line["batched_delaunay_learned"] = run_delaunay(args, local_rank, stream, flush)
@@ -506,6 +556,7 @@ def main():
     ap.add_argument("--degree", type=int, default=5, help="patch preconditioner degree")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-sheets line")
+    ap.add_argument("--no-export", action="store_true", help="skip the OBJ export line")
     ap.add_argument("--batch-sheets", type=int, default=256)
     ap.add_argument("--delaunay-meshes", type=int, default=64)
     args = ap.parse_args()

@@ -112,8 +112,20 @@ eolc_status ensure_state(eolc_ctx *ctx) {
   return EOLC_OK;
 }
 
+// The side stream and its fork / join events (created outside any capture).
+eolc_status ensure_aux(eolc_ctx *ctx) {
+  if (ctx->aux) return EOLC_OK;
+  EOLC_CHECK_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking));
+  EOLC_CHECK_CUDA(ctx, cudaEventCreateWithFlags(&ctx->aux_fork, cudaEventDisableTiming));
+  EOLC_CHECK_CUDA(ctx, cudaEventCreateWithFlags(&ctx->aux_join, cudaEventDisableTiming));
+  return EOLC_OK;
+}
+
 // Assembles MDK (and f, b) for the device state x, X, v.  batched: every
 // instance uses its own material from ctx->inst_matd (mat is ignored).
+// The FP64 force pass (FP64 pipe) runs on the side stream concurrently with
+// the FP32 matrix passes; s waits for it before returning to the caller's
+// next work.
 eolc_status assemble(eolc_ctx *ctx, const eolc_material &mat, const double g[3],
                      double h, int prec, bool want_M, bool want_b,
                      cudaStream_t s, bool batched = false) {
@@ -127,13 +139,19 @@ eolc_status assemble(eolc_ctx *ctx, const eolc_material &mat, const double g[3],
     const size_t need = assemble_scratch_bytes(ctx->topo, prec);
     if (ctx->elem.n < need) EOLC_CHECK_CUDA(ctx, ctx->elem.resize(need));
   }
+  eolc_status st = ensure_aux(ctx);
+  if (st != EOLC_OK) return st;
+  EOLC_CHECK_CUDA(ctx, cudaEventRecord(ctx->aux_fork, s));
+  EOLC_CHECK_CUDA(ctx, cudaStreamWaitEvent(ctx->aux, ctx->aux_fork, 0));
+  launch_forces_rhs(ctx->topo, ctx->x.p, ctx->X.p, ctx->v.p, md, mats, node_inst, prec,
+                    ctx->elem.p, ctx->f.p, want_b ? ctx->b.p : nullptr, ctx->aux);
+  EOLC_CHECK_CUDA(ctx, cudaEventRecord(ctx->aux_join, ctx->aux));
   launch_assemble_blocks(ctx->topo, ctx->x.p, ctx->X.p, md, mats, node_inst, prec, ctx->elem.p,
                          prec == EOLC_PREC_FP64 ? ctx->A64.p : nullptr,
                          prec == EOLC_PREC_FP64 ? nullptr : ctx->A32.p,
                          want_M ? ctx->Mblk.p : nullptr, s);
-  launch_forces_rhs(ctx->topo, ctx->x.p, ctx->X.p, ctx->v.p, md, mats, node_inst, prec,
-                    ctx->f.p, want_b ? ctx->b.p : nullptr, s);
-  ctx->launches += ctx->topo.n_hinge > 0 ? 4 : 3;
+  EOLC_CHECK_CUDA(ctx, cudaStreamWaitEvent(s, ctx->aux_join, 0));
+  ctx->launches += ctx->topo.n_hinge > 0 ? 5 : 4;
   EOLC_CHECK_CUDA(ctx, cudaGetLastError());
   return EOLC_OK;
 }
@@ -259,10 +277,11 @@ eolc_status batch_begin(eolc_ctx *ctx, const double grav[3], double h, const int
   EOLC_CHECK_CUDA(ctx, ctx->inst_matd.upload(ctx->inst_matd_h.data(), n_inst, s));
   if (opts->precision == EOLC_PREC_FP64)
     EOLC_CHECK_CUDA(ctx, ctx->A64.resize(size_t(ctx->topo.n_blocks) * 9 + 16));
-  // the captured assembly writes its element blocks here
+  // the captured assembly writes its element blocks here, and forks its
+  // force pass onto the side stream
   const size_t need = assemble_scratch_bytes(ctx->topo, opts->precision);
   if (ctx->elem.n < need) EOLC_CHECK_CUDA(ctx, ctx->elem.resize(need));
-  return EOLC_OK;
+  return ensure_aux(ctx);
 }
 
 // Pins, assembly and right-hand side of one batched step (no allocation, no
@@ -479,10 +498,17 @@ void eolc_destroy(eolc_ctx *ctx) {
   free_solve_work(ctx->work);
   free_patch_work(ctx->pwork);
   free_collide_work(ctx->cd_work);
+  free_export_work(ctx->ex_work);
   free_batch_work(ctx->bwork);
   if (ctx->bgraph) cudaGraphExecDestroy(ctx->bgraph);
   for (cudaEvent_t e : ctx->ev)
     if (e) cudaEventDestroy(e);
+  if (ctx->aux) {
+    cudaStreamSynchronize(ctx->aux);
+    cudaStreamDestroy(ctx->aux);
+    cudaEventDestroy(ctx->aux_fork);
+    cudaEventDestroy(ctx->aux_join);
+  }
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -574,6 +600,7 @@ eolc_status eolc_set_topology_batched(eolc_ctx *ctx, int n_inst, const int *node
   ctx->node_off.assign(node_off_h, node_off_h + n_inst + 1);
   ctx->inst_mat.clear();
   free_collide_work(ctx->cd_work);
+  free_export_work(ctx->ex_work);
   ctx->cd_work = nullptr;
   ctx->has_topology = true;
   ctx->n_fixed_dev = -1;

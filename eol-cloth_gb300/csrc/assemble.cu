@@ -138,51 +138,77 @@ gather_blocks_kernel(int n_blocks, const int *__restrict__ cptr, const int *__re
   }
 }
 
-// Per node: f_i = sum over incident faces of membrane + gravity forces
-// (faceBasedF non-EOL, Forces.cpp:498-501; bending adds no force there,
-// Forces.cpp:885-908), then b_i = -((M v)_i + h f_i) (Cloth.cpp:345).
-template <typename T>
+// Forces, FP64 in every precision mode (the FP64 refinement residual of the
+// mixed solve is only as accurate as b; near rest FP32 membrane forces are
+// rounding noise as large as the gravity loads).  Two passes, so that each
+// triangle is evaluated once:
+//   tri_forces_kernel    per triangle: the membrane force on each of its
+//                        vertices and t8 = rho 2 A, at Ft[10 t ...];
+//   forces_rhs_kernel    per node: f_i = sum over incident faces of membrane
+//                        + gravity forces in face order (faceBasedF non-EOL,
+//                        Forces.cpp:498-501; bending adds no force there,
+//                        Forces.cpp:885-908), then b_i = -((M v)_i + h f_i)
+//                        (Cloth.cpp:345).
+constexpr int kForceWords = 10;  // 3 x 3 vertex forces + t8
+
+__global__ void __launch_bounds__(128)
+tri_forces_kernel(int n_tri, const int *__restrict__ tri, const double *__restrict__ x,
+                  const double *__restrict__ X, MaterialD m,
+                  const MaterialD *__restrict__ mats, const int *__restrict__ node_inst,
+                  double *__restrict__ Ft) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tri) return;
+  const int a = __ldg(tri + 3 * t), b = __ldg(tri + 3 * t + 1), c = __ldg(tri + 3 * t + 2);
+  if (mats) m = mats[node_inst[a]];  // batched: the element's instance
+  const Tri<double> q = make_tri<double>(x, X, a, b, c);
+  double *out = Ft + size_t(t) * kForceWords;
+#pragma unroll
+  for (int la = 0; la < 3; ++la) {
+    const v3<double> fm = membrane_force(q, la, m.mu, m.lam);
+    out[3 * la] = fm.x;
+    out[3 * la + 1] = fm.y;
+    out[3 * la + 2] = fm.z;
+  }
+  out[9] = m.rho * 2.0 * q.A;
+}
+
 __global__ void __launch_bounds__(128)
 forces_rhs_kernel(int n_nodes, const int *__restrict__ nf_ptr,
                   const int *__restrict__ nf_list, const int *__restrict__ tri,
-                  const double *__restrict__ x, const double *__restrict__ X,
-                  const double *__restrict__ v, MaterialD m,
-                  const MaterialD *__restrict__ mats,
-                  const int *__restrict__ node_inst,
+                  const double *__restrict__ Ft, const double *__restrict__ v, MaterialD m,
+                  const MaterialD *__restrict__ mats, const int *__restrict__ node_inst,
                   double *__restrict__ f, double *__restrict__ b) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_nodes) return;
   if (mats) m = mats[node_inst[i]];  // batched: the node's instance
-  const T mu = T(m.mu), lam = T(m.lam);
-  T fx = 0, fy = 0, fz = 0;
+  double fx = 0, fy = 0, fz = 0;
   double mvx = 0, mvy = 0, mvz = 0;
   for (int q = nf_ptr[i]; q < nf_ptr[i + 1]; ++q) {
-    int code = __ldg(nf_list + q);
-    int e = code >> 2, la = code & 3;
-    int vv[3] = {__ldg(tri + 3 * e), __ldg(tri + 3 * e + 1), __ldg(tri + 3 * e + 2)};
-    Tri<T> t = make_tri<T>(x, X, vv[0], vv[1], vv[2]);
-    v3<T> fm = membrane_force(t, la, mu, lam);
-    T t8 = T(m.rho) * T(2) * t.A;
-    fx += fm.x + t8 * T(m.g[0]) / T(6);
-    fy += fm.y + t8 * T(m.g[1]) / T(6);
-    fz += fm.z + t8 * T(m.g[2]) / T(6);
+    const int code = __ldg(nf_list + q);
+    const int e = code >> 2, la = code & 3;
+    const double *fe = Ft + size_t(e) * kForceWords;
+    const double t8 = __ldg(fe + 9);
+    fx += __ldg(fe + 3 * la) + t8 * m.g[0] / 6.0;
+    fy += __ldg(fe + 3 * la + 1) + t8 * m.g[1] / 6.0;
+    fz += __ldg(fe + 3 * la + 2) + t8 * m.g[2] / 6.0;
     if (b) {
 #pragma unroll
       for (int w = 0; w < 3; ++w) {
-        double mm = double(w == la ? t8 / T(12) : t8 / T(24));
-        mvx += mm * v[3 * vv[w]];
-        mvy += mm * v[3 * vv[w] + 1];
-        mvz += mm * v[3 * vv[w] + 2];
+        const int vw = __ldg(tri + 3 * e + w);
+        const double mm = w == la ? t8 / 12.0 : t8 / 24.0;
+        mvx += mm * v[3 * vw];
+        mvy += mm * v[3 * vw + 1];
+        mvz += mm * v[3 * vw + 2];
       }
     }
   }
   if (f) {
-    f[3 * i] = double(fx); f[3 * i + 1] = double(fy); f[3 * i + 2] = double(fz);
+    f[3 * i] = fx; f[3 * i + 1] = fy; f[3 * i + 2] = fz;
   }
   if (b) {
-    b[3 * i] = -(mvx + m.h * double(fx));
-    b[3 * i + 1] = -(mvy + m.h * double(fy));
-    b[3 * i + 2] = -(mvz + m.h * double(fz));
+    b[3 * i] = -(mvx + m.h * fx);
+    b[3 * i + 1] = -(mvy + m.h * fy);
+    b[3 * i + 2] = -(mvz + m.h * fz);
   }
 }
 
@@ -215,23 +241,27 @@ void launch_assemble_blocks(const DevTopology &T, const double *x,
   }
 }
 
-size_t assemble_scratch_bytes(const DevTopology &T, int prec) {
+// The force pass's per-triangle words follow the element blocks, 256-byte
+// aligned.
+size_t forces_scratch_offset(const DevTopology &T, int prec) {
   const size_t e = prec == EOLC_PREC_FP64 ? sizeof(double) : sizeof(float);
-  return e * (size_t(T.n_tri) * 82 + size_t(T.n_hinge) * 144);
+  return (e * (size_t(T.n_tri) * 82 + size_t(T.n_hinge) * 144) + 255) / 256 * 256;
+}
+
+size_t assemble_scratch_bytes(const DevTopology &T, int prec) {
+  return forces_scratch_offset(T, prec) + sizeof(double) * kForceWords * size_t(T.n_tri);
 }
 
 void launch_forces_rhs(const DevTopology &T, const double *x, const double *X,
                        const double *v, const MaterialD &m,
-                       const MaterialD *mats, const int *node_inst, int prec,
+                       const MaterialD *mats, const int *node_inst, int prec, void *elem,
                        double *f, double *b, cudaStream_t s) {
-  int n = T.n_nodes;
-  dim3 block(128), grid((n + 127) / 128);
-  if (prec == EOLC_PREC_FP64)
-    forces_rhs_kernel<double><<<grid, block, 0, s>>>(
-        n, T.nf_ptr.p, T.nf_list.p, T.tri.p, x, X, v, m, mats, node_inst, f, b);
-  else
-    forces_rhs_kernel<float><<<grid, block, 0, s>>>(
-        n, T.nf_ptr.p, T.nf_list.p, T.tri.p, x, X, v, m, mats, node_inst, f, b);
+  const int n = T.n_nodes, nt = T.n_tri;
+  double *Ft = reinterpret_cast<double *>(static_cast<char *>(elem) +
+                                          forces_scratch_offset(T, prec));
+  tri_forces_kernel<<<(nt + 127) / 128, 128, 0, s>>>(nt, T.tri.p, x, X, m, mats, node_inst, Ft);
+  forces_rhs_kernel<<<(n + 127) / 128, 128, 0, s>>>(n, T.nf_ptr.p, T.nf_list.p, T.tri.p, Ft, v,
+                                                    m, mats, node_inst, f, b);
 }
 
 }  // namespace eolc

@@ -92,9 +92,13 @@ void launch_assemble_blocks(const DevTopology &T, const double *x,
                             int prec, void *elem, double *A64, float *A32, double *Mblk,
                             cudaStream_t s);
 size_t assemble_scratch_bytes(const DevTopology &T, int prec);
+// Forces and right-hand side, always in FP64 (the FP64 refinement residual
+// of the mixed-precision solve is only as accurate as b): a triangle pass and
+// a node gather (two launches).  elem: the assembly scratch of
+// assemble_scratch_bytes(T, prec); the force words sit after the blocks.
 void launch_forces_rhs(const DevTopology &T, const double *x, const double *X,
                        const double *v, const MaterialD &m,
-                       const MaterialD *mats, const int *node_inst, int prec,
+                       const MaterialD *mats, const int *node_inst, int prec, void *elem,
                        double *f, double *b, cudaStream_t s);
 
 // Solver (pcg.cu)
@@ -173,6 +177,10 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, i
 struct CollideWork;
 void free_collide_work(CollideWork *w);
 
+// OBJ export (export.cu)
+struct ExportWork;
+void free_export_work(ExportWork *w);
+
 // Learned preconditioner (learned.cu / pcg.cu)
 eolc_status run_pcg_learned(SolveWork *&w, const PcgArgs &a, const float *Gm,
                             eolc_solve_info *info, cudaStream_t s, std::string &err,
@@ -209,6 +217,9 @@ struct eolc_ctx {
   int last_precision = -1;  // precision of the last assembled MDK
   long long launches = 0;   // kernels launched by this context
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // the FP64 force pass runs on aux beside the FP32 matrix passes
+  cudaStream_t aux = nullptr;
+  cudaEvent_t aux_fork = nullptr, aux_join = nullptr;
   std::vector<int> host_tri;  // triangle list of the current topology
   eolc_lpc *lpc = nullptr;    // attached learned preconditioner (not owned)
   const eolc_lpc *lpc_cached = nullptr;  // network whose G the resident solver holds
@@ -216,6 +227,7 @@ struct eolc_ctx {
   int lpc_refresh = 1;        // re-evaluate the network every lpc_refresh solves
   int coarse_refresh = 1;     // rebuild the patch PC's coarse operator every ... solves
   eolc::CollideWork *cd_work = nullptr;
+  eolc::ExportWork *ex_work = nullptr;
   // batches: instance k owns nodes node_off[k] .. node_off[k+1]
   std::vector<int> node_off;
   eolc::DevBuf<int> node_inst;                // instance of every node

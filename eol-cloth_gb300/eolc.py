@@ -18,16 +18,17 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libeolc.so")
 
-OK, NOT_CONVERGED, BREAKDOWN, NONFINITE, TIMEOUT, BAD_ARG, CUDA_ERROR, CAPACITY, NO_TOPOLOGY = range(9)
+(OK, NOT_CONVERGED, BREAKDOWN, NONFINITE, TIMEOUT, BAD_ARG, CUDA_ERROR, CAPACITY, NO_TOPOLOGY,
+ IO_ERROR) = range(10)
 PREC_FP64, PREC_MIXED = 0, 1
 PC_JACOBI, PC_BLOCK_JACOBI, PC_LEARNED, PC_PATCH = 0, 1, 2, 3
 STATUS_NAMES = ["OK", "NOT_CONVERGED", "BREAKDOWN", "NONFINITE", "TIMEOUT", "BAD_ARG",
-                "CUDA_ERROR", "CAPACITY", "NO_TOPOLOGY"]
+                "CUDA_ERROR", "CAPACITY", "NO_TOPOLOGY", "IO_ERROR"]
 
 
 class EolcError(RuntimeError):
     def __init__(self, status, msg):
-        super().__init__("%s: %s" % (STATUS_NAMES[status] if 0 <= status < 9 else status, msg))
+        super().__init__("%s: %s" % (STATUS_NAMES[status] if 0 <= status < len(STATUS_NAMES) else status, msg))
         self.status = status
 
 
@@ -105,7 +106,8 @@ EXPORTS = ["eolc_version", "eolc_launch_count", "eolc_create", "eolc_destroy", "
            "eolc_set_topology_batched", "eolc_set_instance_materials", "eolc_step_batched",
            "eolc_batch_num_configs", "eolc_batch_config_name", "eolc_batch_set_config",
            "eolc_batch_autotune", "eolc_set_learned_refresh", "eolc_set_coarse_refresh",
-           "eolc_batch_set_jacobi_reference", "eolc_lpc_blocks"]
+           "eolc_batch_set_jacobi_reference", "eolc_lpc_blocks", "eolc_export_obj",
+           "eolc_export_obj_text"]
 
 
 def load_library(path=LIB_PATH):
@@ -170,6 +172,9 @@ def load_library(path=LIB_PATH):
     L.eolc_batch_set_config.argtypes = [_V, ctypes.c_int]
     L.eolc_batch_autotune.argtypes = [_V, _D, ctypes.c_double, _I, _D, ctypes.c_int,
                                       ctypes.POINTER(SolveOpts), _I, _D]
+    L.eolc_export_obj.argtypes = [_V, ctypes.c_char_p, ctypes.c_int, ctypes.c_double]
+    L.eolc_export_obj_text.argtypes = [_V, ctypes.c_int, ctypes.c_double, ctypes.c_char_p,
+                                       ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
     for name in EXPORTS:
         if not hasattr(L, name):
             raise ImportError("libeolc.so lacks %s" % name)
@@ -318,6 +323,20 @@ class Context:
         self._check(st)
         return [out[k] for k in range(n.value)]
 
+    # ---- OBJ export ------------------------------------------------------------
+    def export_obj(self, export_dir, frame, time=0.0):
+        """Writes <dir>/<frame>_Cloth2D.obj and <dir>/<frame>_Cloth3D.obj from
+        the device state (positions of the last upload or step)."""
+        self._check(lib.eolc_export_obj(self._h, os.fsencode(export_dir), frame, time))
+
+    def export_obj_text(self, frame, time=0.0):
+        """The two files' bytes: (Cloth2D, Cloth3D)."""
+        ln = (ctypes.c_size_t * 2)()
+        self._check(lib.eolc_export_obj_text(self._h, frame, time, None, 0, ln))
+        buf = ctypes.create_string_buffer(ln[0] + ln[1])
+        self._check(lib.eolc_export_obj_text(self._h, frame, time, buf, ln[0] + ln[1], ln))
+        raw = buf.raw
+        return raw[:ln[0]], raw[ln[0]:ln[0] + ln[1]]
 
     # ---- batches -------------------------------------------------------------
     def set_topology_batched(self, sheets):
@@ -563,3 +582,25 @@ def CD2(ctx, x, boxes=(), points=None, normals=None, threshold=1e-3):
     """CD2 (Collisions.cpp:55-78): contacts of the cloth (context topology,
     positions x) with point obstacles and boxes, in the reference's order."""
     return ctx.cd2(x, boxes, points, normals, threshold)
+
+
+class BrenderManager:
+    """Per-frame OBJ export (src/BrenderManager.h:15-45): set_export_dir,
+    get_frame and export_brender(time), which writes the frame's files and
+    then advances the frame counter.  Unlike the reference's singleton, one
+    manager per cloth context; obstacle shapes are not exported."""
+
+    def __init__(self, ctx, export_dir="."):
+        self.ctx = ctx
+        self.export_dir = export_dir
+        self.frame = 0
+
+    def set_export_dir(self, export_dir):
+        self.export_dir = export_dir
+
+    def get_frame(self):
+        return self.frame
+
+    def export_brender(self, time=0.0):
+        self.ctx.export_obj(self.export_dir, self.frame, time)
+        self.frame += 1

@@ -9,6 +9,8 @@
  *   Cloth::solve / Cloth::step       src/Cloth.cpp:343-413 (minus dumps)
  *   CD2 / btc::boxTriCollision /     src/Collisions.cpp:55-78,
  *   btc::pointTriCollision           src/boxTriCollision.cpp:602-1224
+ *   BrenderManager::exportBrender /  src/BrenderManager.cpp:34-84,
+ *   Cloth::exportBrender (OBJ)       src/Cloth.cpp:535-590
  *
  * Conventions
  *   - Plain pointers and sizes only.  Arrays suffixed _h are HOST memory
@@ -27,6 +29,8 @@
 #ifndef EOLC_H_
 #define EOLC_H_
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -40,7 +44,8 @@ typedef enum {
   EOLC_BAD_ARG = 5,
   EOLC_CUDA_ERROR = 6,
   EOLC_CAPACITY = 7,      /* output buffer too small; *n_out has the need  */
-  EOLC_NO_TOPOLOGY = 8
+  EOLC_NO_TOPOLOGY = 8,
+  EOLC_IO_ERROR = 9       /* a file could not be opened or written         */
 } eolc_status;
 
 /* Material of src/Cloth.h:28-35 (dampingA is unused by the reference). */
@@ -55,8 +60,9 @@ typedef struct {
 
 typedef enum {
   EOLC_PREC_FP64 = 0,  /* FP64 element math, FP64 BSR, FP64 PCG          */
-  EOLC_PREC_MIXED = 1  /* FP32 element math / BSR / PCG, FP64 dots and an
-                          FP64 iterative-refinement residual              */
+  EOLC_PREC_MIXED = 1  /* FP32 matrix element math / BSR / PCG, FP64 dots,
+                          FP64 forces and right-hand side, and an FP64
+                          iterative-refinement residual                  */
 } eolc_precision;
 
 typedef enum {
@@ -142,7 +148,9 @@ eolc_status eolc_bsr_pattern(eolc_ctx *ctx, int *n_blocks, int *rowptr_h,
 /* ---- Forces::fill (Forces.cpp:912-930, non-EOL branches) ----------------
  * Computes f (3N), M and MDK (BSR values, n_blocks*9 each) for positions
  * x_h and material coordinates X_h.  Any output pointer may be NULL.
- * precision selects FP64 or FP32 element arithmetic; outputs are FP64. */
+ * precision selects FP64 or FP32 element arithmetic for M and MDK; f is
+ * always evaluated in FP64 (near rest the FP32 membrane forces are rounding
+ * noise of the size of the gravity loads).  Outputs are FP64. */
 eolc_status eolc_forces_fill(eolc_ctx *ctx, const double *x_h,
                              const double *X_h, const eolc_material *mat,
                              const double grav[3], double h, int precision,
@@ -364,6 +372,29 @@ eolc_status eolc_set_coarse_refresh(eolc_ctx *ctx, int solves);
  * cap (fallback_factor x this count) refers to; set automatically by every
  * successful Jacobi solve on the context. */
 eolc_status eolc_set_jacobi_reference(eolc_ctx *ctx, int iterations);
+
+/* ---- OBJ frame export (BrenderManager::exportBrender, BrenderManager.cpp:
+ * 34-84, with Cloth::exportBrender, Cloth.cpp:535-590) --------------------
+ * Writes the two files of one frame from the context's device state (the
+ * positions and material coordinates of the last upload or step and the
+ * topology's triangles):
+ *   <dir>/<frame %06d>_Cloth2D.obj  "v u0 u1 0", "vt u0 u1", "vn 0 0 1"
+ *   <dir>/<frame %06d>_Cloth3D.obj  "v x", "vt u0 u1", "vn n" (node normals
+ *                                   of ArcSim normal<WS>, geometry.cpp:302-316)
+ * each after the header "# frame %06d \n# time %f \n# name <name> \n" and
+ * with 1-based faces "f a/a/a b/b/b c/c/c", numbers as C's "%f" prints them
+ * (positions, texture coordinates and normals rounded to float first, as the
+ * reference's posBuf/texBuf/norBuf).  The text is generated on the GPU.  The
+ * caller keeps the frame counter (the reference's BrenderManager increments
+ * it after every export).  EOLC_BAD_ARG when a coordinate has magnitude
+ * 2^63 or more; EOLC_IO_ERROR when a file cannot be written. */
+eolc_status eolc_export_obj(eolc_ctx *ctx, const char *dir, int frame,
+                            double time);
+/* The same two files' bytes into host memory: the Cloth2D file, then the
+ * Cloth3D file, len[0] and len[1] bytes (no terminating NUL).  buf == NULL
+ * returns the lengths only; EOLC_CAPACITY when capacity < len[0] + len[1]. */
+eolc_status eolc_export_obj_text(eolc_ctx *ctx, int frame, double time,
+                                 char *buf, size_t capacity, size_t len[2]);
 
 /* ---- velocity solve without device allocation ----------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc

@@ -106,6 +106,18 @@ int orc_cd2(int n_nodes, const double *x, const int *tri, int n_tri,
 int orc_create_edges(int n_nodes, const double *x, const int *tri, int n_tri,
                      int *edges6, int cap);
 
+/* ---- OBJ frame export (BrenderManager.cpp:34-84, Cloth.cpp:535-590) -----
+ * The Cloth2D file then the Cloth3D file of one frame, as the reference's
+ * sprintf calls write them (the 2D file's literal 0 z printed as 0.0), into
+ * buf; len[0], len[1] get the two lengths.  buf == NULL: lengths only.
+ * Returns 1 when cap is too small, else 0. */
+int orc_obj_text(int n_nodes, const double *x, const double *X, const int *tri,
+                 int n_tri, int frame, double time, char *buf, long long cap,
+                 long long *len);
+/* ArcSim normal<WS> of every node (geometry.cpp:302-316), FP64. */
+void orc_node_normals(int n_nodes, const double *x, const int *tri, int n_tri,
+                      double *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -13,7 +13,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
-SOURCES = ["mesh.cpp", "elements.cpp", "assemble.cpp", "collide.cpp"]
+SOURCES = ["mesh.cpp", "elements.cpp", "assemble.cpp", "collide.cpp", "export.cpp"]
 
 
 def build(force=False):
@@ -99,6 +99,10 @@ def lib():
         L.orc_create_edges.argtypes = [ctypes.c_int, _D, _I, ctypes.c_int, _I,
                                        ctypes.c_int]
         L.orc_hinges.argtypes = [ctypes.c_int, _I, ctypes.c_int, _I, ctypes.c_int]
+        L.orc_obj_text.argtypes = [ctypes.c_int, _D, _D, _I, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_double, ctypes.c_char_p, ctypes.c_longlong,
+                                   ctypes.POINTER(ctypes.c_longlong)]
+        L.orc_node_normals.argtypes = [ctypes.c_int, _D, _I, ctypes.c_int, _D]
         for name in ("orc_grid2_build", "orc_gridc_build"):
             getattr(L, name).argtypes = [ctypes.c_int, ctypes.c_int, _D, _D, _D, _I]
         _lib = L
@@ -291,3 +295,29 @@ def create_edges(x, tri):
     out = np.zeros(6 * cap, np.int32)
     n = lib().orc_create_edges(len(x) // 3, dp(x), ip(tri), len(tri), ip(out), cap)
     return out[:6 * n].reshape(-1, 6)
+
+
+def obj_text(x, X, tri, frame=0, time=0.0):
+    """The (Cloth2D, Cloth3D) OBJ files of one frame as bytes, formatted as
+    BrenderManager::exportBrender + Cloth::exportBrender write them."""
+    tri = np.ascontiguousarray(tri, dtype=np.int32)
+    x = np.ascontiguousarray(x, np.float64)
+    X = np.ascontiguousarray(X, np.float64)
+    n = len(x) // 3
+    ln = (ctypes.c_longlong * 2)()
+    lib().orc_obj_text(n, dp(x), dp(X), ip(tri), len(tri.reshape(-1, 3)), frame,
+                       ctypes.c_double(time), None, 0, ln)
+    buf = ctypes.create_string_buffer(ln[0] + ln[1])
+    assert lib().orc_obj_text(n, dp(x), dp(X), ip(tri), len(tri.reshape(-1, 3)), frame,
+                              ctypes.c_double(time), buf, ln[0] + ln[1], ln) == 0
+    raw = buf.raw
+    return raw[:ln[0]], raw[ln[0]:ln[0] + ln[1]]
+
+
+def node_normals(x, tri):
+    """ArcSim normal<WS> of every node, FP64 (3N)."""
+    tri = np.ascontiguousarray(tri, dtype=np.int32)
+    x = np.ascontiguousarray(x, np.float64)
+    out = np.zeros(len(x))
+    lib().orc_node_normals(len(x) // 3, dp(x), ip(tri), len(tri.reshape(-1, 3)), dp(out))
+    return out

@@ -4,9 +4,10 @@ Tolerances (stated per the spec contract):
   * FP64 path: f, M and MDK BSR values within 1e-10 relative (max-norm);
     velocities of an FP64 solve at tol 1e-12 within 1e-10 of the oracle's
     direct solution.
-  * mixed path (FP32 assembly / PCG, FP64 dots + FP64 refinement residual):
-    final FP64 relative residual <= 1e-8 on its own system; its error against
-    the FP64 oracle is measured and bounded (1e-4 relative on v).
+  * mixed path (FP32 matrix assembly / PCG, FP64 forces and right-hand side,
+    FP64 dots + FP64 refinement residual): final FP64 relative residual
+    <= 1e-8 on its own system; its error against the FP64 oracle is measured
+    and bounded (1e-5 relative on v).
   * collisions: contact list bit-identical, order included.
 """
 import numpy as np
@@ -130,9 +131,9 @@ def test_velocity_solve_mixed_reaches_fp64_residual(eolc, ctx, precond):
     r = (-b - A @ vf)[free]
     rhs = (-b - A[:, s["fixed"]] @ beq)[free]
     assert np.linalg.norm(r) <= 1.05e-8 * np.linalg.norm(rhs)
-    # error against the FP64 oracle solution is stated, bounded loosely
+    # error against the FP64 oracle solution (only the FP32 matrix differs)
     vd = F.solve_direct(b, s["fixed"], beq)
-    assert relmax(v, vd) <= 1e-4
+    assert relmax(v, vd) <= 1e-5
 
 
 def _oracle_step_direct(F, v, fixed, fixed_vel):
@@ -174,7 +175,8 @@ def test_config1_100_steps_fp64_per_step(eolc, ctx):
 
 def test_config1_mixed_per_step_error_vs_fp64(eolc, ctx):
     """Mixed path on the configuration-1 states: FP64 residual <= 1e-8 every
-    step; stated error against the FP64 oracle velocity <= 1e-4 relative."""
+    step; stated error against the FP64 oracle velocity <= 1e-5 relative (FP32
+    matrix, FP64 forces and right-hand side)."""
     s = scenes.sheet(20)
     ctx.set_topology(s["n"], s["tri"], s["hinge"])
     opts = eolc.SolveOpts(rel_tol=1e-8, precision=eolc.PREC_MIXED)
@@ -189,7 +191,8 @@ def test_config1_mixed_per_step_error_vs_fp64(eolc, ctx):
         vo = _oracle_step_direct(F, vo, s["fixed"], s["fixed_vel"])
         xo = xo + scenes.H * vo
         worst = max(worst, relmax(vg, vo))
-    assert worst <= 1e-4, worst
+    print("worst mixed velocity error vs FP64 oracle: %.2e" % worst)
+    assert worst <= 1e-5, worst
 
 
 def test_short_free_run_tracks_oracle(eolc, ctx):

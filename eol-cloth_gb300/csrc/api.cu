@@ -158,76 +158,7 @@ eolc_status assemble(eolc_ctx *ctx, const eolc_material &mat, const double g[3],
 
 eolc_status solve_device(eolc_ctx *ctx, const eolc_solve_opts *o,
                          eolc_solve_info *info, cudaStream_t s) {
-  PcgArgs a;
-  a.T = &ctx->topo;
-  a.A64 = ctx->A64.p;
-  a.A32 = ctx->A32.p;
-  a.b = ctx->b.p;
-  a.pinned = ctx->pinned.p;
-  a.beq_full = ctx->beq_full.p;
-  a.v = ctx->v.p;
-  a.precision = o->precision;
-  a.precond = o->precond;
-  a.rel_tol = o->rel_tol;
-  a.max_iter = o->max_iter;
-  a.learned = nullptr;
-  a.X = ctx->X.p;
-  if (o->precision == EOLC_PREC_FP64 && !ctx->A64.p)
-    return fail(ctx, EOLC_BAD_ARG, "no FP64 matrix assembled");
-  eolc_solve_info local{};
-  eolc_solve_info *inf = info ? info : &local;
-  if (o->precond == EOLC_PC_LEARNED) {
-    if (!ctx->lpc) return fail(ctx, EOLC_BAD_ARG, "no learned preconditioner attached");
-    if (o->precision != EOLC_PREC_MIXED)
-      return fail(ctx, EOLC_BAD_ARG, "the learned preconditioner runs on the mixed path");
-    const bool resident = !o->streamed && resident_fits(ctx->pwork, ctx->topo, ctx->X.p, s);
-    // the resident path keeps the network's G between solves: it is
-    // re-evaluated once it has served lpc_refresh solves (1: every solve)
-    const bool reuse = resident && ctx->lpc_cached == ctx->lpc && ctx->lpc_uses < ctx->lpc_refresh;
-    const float *Gm = nullptr;
-    if (!reuse) {
-      std::string msg = learned_forward(ctx->lpc, ctx, ctx->pinned.p, &Gm, s);
-      if (!msg.empty()) return fail(ctx, EOLC_CUDA_ERROR, msg.c_str());
-      ctx->launches += 8;  // network forward kernels
-      ctx->lpc_cached = resident ? ctx->lpc : nullptr;
-      ctx->lpc_uses = 0;
-    }
-    ctx->lpc_uses += 1;
-    // fall back to Jacobi when the learned solve has not converged within
-    // fallback_factor x the last Jacobi iteration count
-    PcgArgs al = a;
-    if (o->fallback_factor > 0 && ctx->last_jacobi_iters > 0)
-      al.max_iter = std::min(o->max_iter, o->fallback_factor * ctx->last_jacobi_iters);
-    eolc_status st = resident ? run_pcg_resident(ctx->pwork, al, ResidentPC::kLearned, 0, Gm, inf,
-                                                 s, ctx->err, ctx->launches, o->no_coarse == 0,
-                                                 ctx->coarse_refresh)
-                              : run_pcg_learned(ctx->work, al, Gm, inf, s, ctx->err, ctx->launches);
-    if (st == EOLC_OK || o->fallback_factor <= 0) return st;
-    const double kms = inf->solve_kernel_ms;
-    const int its = inf->iterations;
-    PcgArgs aj = a;
-    aj.precond = EOLC_PC_JACOBI;
-    st = resident ? run_pcg_resident(ctx->pwork, aj, ResidentPC::kJacobi, 0, nullptr, inf, s,
-                                     ctx->err, ctx->launches)
-                  : run_pcg(ctx->work, aj, inf, s, ctx->err, ctx->launches);
-    inf->used_fallback = 1;
-    inf->iterations += its;
-    inf->solve_kernel_ms += kms;
-    if (st == EOLC_OK) ctx->last_jacobi_iters = inf->iterations - its;
-    return st;
-  }
-  if (o->precond == EOLC_PC_PATCH)
-    return run_pcg_resident(ctx->pwork, a, ResidentPC::kPatch,
-                            o->degree > 0 ? o->degree : kDefaultPatchDegree, nullptr, inf, s,
-                            ctx->err, ctx->launches, o->no_coarse == 0, ctx->coarse_refresh);
-  eolc_status st;
-  if (o->precision == EOLC_PREC_MIXED && !o->streamed && resident_fits(ctx->pwork, ctx->topo, ctx->X.p, s))
-    st = run_pcg_resident(ctx->pwork, a, ResidentPC::kJacobi, 0, nullptr, inf, s, ctx->err,
-                          ctx->launches);
-  else
-    st = run_pcg(ctx->work, a, inf, s, ctx->err, ctx->launches);
-  if (st == EOLC_OK && o->precond == EOLC_PC_JACOBI) ctx->last_jacobi_iters = inf->iterations;
-  return st;
+  return solve_with_args(ctx, o, default_pcg_args(ctx, o), info, s);
 }
 
 cudaStream_t stream_of(eolc_ctx *ctx) { return ctx->stream; }
@@ -441,6 +372,105 @@ eolc_status step_batched_learned(eolc_ctx *ctx, int n_steps, const double grav[3
 
 }  // namespace
 
+namespace eolc {
+
+PcgArgs default_pcg_args(eolc_ctx *ctx, const eolc_solve_opts *o) {
+  PcgArgs a;
+  a.T = &ctx->topo;
+  a.A64 = ctx->A64.p;
+  a.A32 = ctx->A32.p;
+  a.b = ctx->b.p;
+  a.pinned = ctx->pinned.p;
+  a.beq_full = ctx->beq_full.p;
+  a.v = ctx->v.p;
+  a.precision = o->precision;
+  a.precond = o->precond;
+  a.rel_tol = o->rel_tol;
+  a.max_iter = o->max_iter;
+  a.learned = nullptr;
+  a.X = ctx->X.p;
+  return a;
+}
+
+// The dispatch of eolc_velocity_solve on explicit arguments (matrix, rhs and
+// solution buffers of a): learned (with the Jacobi fallback), patch, resident
+// or streamed PCG.
+eolc_status solve_with_args(eolc_ctx *ctx, const eolc_solve_opts *o, const PcgArgs &a,
+                            eolc_solve_info *info, cudaStream_t s) {
+  if (o->precision == EOLC_PREC_FP64 && !ctx->A64.p)
+    return fail(ctx, EOLC_BAD_ARG, "no FP64 matrix assembled");
+  eolc_solve_info local{};
+  eolc_solve_info *inf = info ? info : &local;
+  if (o->precond == EOLC_PC_LEARNED) {
+    if (!ctx->lpc) return fail(ctx, EOLC_BAD_ARG, "no learned preconditioner attached");
+    if (o->precision != EOLC_PREC_MIXED)
+      return fail(ctx, EOLC_BAD_ARG, "the learned preconditioner runs on the mixed path");
+    const bool resident = !o->streamed && resident_fits(ctx->pwork, ctx->topo, ctx->X.p, s);
+    // the resident path keeps the network's G between solves: it is
+    // re-evaluated once it has served lpc_refresh solves (1: every solve)
+    const bool reuse = resident && ctx->lpc_cached == ctx->lpc && ctx->lpc_uses < ctx->lpc_refresh;
+    const float *Gm = nullptr;
+    if (!reuse) {
+      std::string msg = learned_forward(ctx->lpc, ctx, ctx->pinned.p, &Gm, s);
+      if (!msg.empty()) return fail(ctx, EOLC_CUDA_ERROR, msg.c_str());
+      ctx->launches += 8;  // network forward kernels
+      ctx->lpc_cached = resident ? ctx->lpc : nullptr;
+      ctx->lpc_uses = 0;
+    }
+    ctx->lpc_uses += 1;
+    // fall back to Jacobi when the learned solve has not converged within
+    // fallback_factor x the last Jacobi iteration count
+    PcgArgs al = a;
+    if (o->fallback_factor > 0 && ctx->last_jacobi_iters > 0)
+      al.max_iter = std::min(o->max_iter, o->fallback_factor * ctx->last_jacobi_iters);
+    eolc_status st = resident ? run_pcg_resident(ctx->pwork, al, ResidentPC::kLearned, 0, Gm, inf,
+                                                 s, ctx->err, ctx->launches, o->no_coarse == 0,
+                                                 ctx->coarse_refresh)
+                              : run_pcg_learned(ctx->work, al, Gm, inf, s, ctx->err, ctx->launches);
+    if (st == EOLC_OK || o->fallback_factor <= 0) return st;
+    const double kms = inf->solve_kernel_ms;
+    const int its = inf->iterations;
+    PcgArgs aj = a;
+    aj.precond = EOLC_PC_JACOBI;
+    st = resident ? run_pcg_resident(ctx->pwork, aj, ResidentPC::kJacobi, 0, nullptr, inf, s,
+                                     ctx->err, ctx->launches)
+                  : run_pcg(ctx->work, aj, inf, s, ctx->err, ctx->launches);
+    inf->used_fallback = 1;
+    inf->iterations += its;
+    inf->solve_kernel_ms += kms;
+    if (st == EOLC_OK) ctx->last_jacobi_iters = inf->iterations - its;
+    return st;
+  }
+  if (o->precond == EOLC_PC_PATCH)
+    return run_pcg_resident(ctx->pwork, a, ResidentPC::kPatch,
+                            o->degree > 0 ? o->degree : kDefaultPatchDegree, nullptr, inf, s,
+                            ctx->err, ctx->launches, o->no_coarse == 0, ctx->coarse_refresh);
+  eolc_status st;
+  if (o->precision == EOLC_PREC_MIXED && !o->streamed && resident_fits(ctx->pwork, ctx->topo, ctx->X.p, s))
+    st = run_pcg_resident(ctx->pwork, a, ResidentPC::kJacobi, 0, nullptr, inf, s, ctx->err,
+                          ctx->launches);
+  else
+    st = run_pcg(ctx->work, a, inf, s, ctx->err, ctx->launches);
+  if (st == EOLC_OK && o->precond == EOLC_PC_JACOBI) ctx->last_jacobi_iters = inf->iterations;
+  return st;
+}
+
+
+eolc_status prepare_pins_rhs(eolc_ctx *ctx, const double *b_h, const int *fixed_dofs_h,
+                             const double *beq_h, int n_fixed, cudaStream_t s) {
+  const int n = 3 * ctx->topo.n_nodes;
+  eolc_status st = set_pins(ctx, fixed_dofs_h, nullptr, n_fixed, s);
+  if (st != EOLC_OK) return st;
+  std::vector<double> beq_full(n, 0.0);
+  for (int k = 0; k < n_fixed; ++k) beq_full[fixed_dofs_h[k]] = beq_h[k];
+  EOLC_CHECK_CUDA(ctx, ctx->beq_full.upload(beq_full.data(), n, s));
+  EOLC_CHECK_CUDA(ctx, ctx->b.upload(b_h, n, s));
+  return EOLC_OK;
+}
+
+}  // namespace eolc
+
+
 extern "C" {
 
 int eolc_version(void) { return 1; }
@@ -499,6 +529,7 @@ void eolc_destroy(eolc_ctx *ctx) {
   free_patch_work(ctx->pwork);
   free_collide_work(ctx->cd_work);
   free_export_work(ctx->ex_work);
+  free_ineq_work(ctx->iq_work);
   free_batch_work(ctx->bwork);
   if (ctx->bgraph) cudaGraphExecDestroy(ctx->bgraph);
   for (cudaEvent_t e : ctx->ev)
@@ -695,6 +726,7 @@ eolc_status eolc_velocity_solve(eolc_ctx *ctx, const double *b_h,
   for (int k = 0; k < n_fixed; ++k) beq_full[fixed_dofs_h[k]] = beq_h[k];
   EOLC_CHECK_CUDA(ctx, ctx->beq_full.upload(beq_full.data(), n, s));
   EOLC_CHECK_CUDA(ctx, ctx->b.upload(b_h, n, s));
+  EOLC_CHECK_CUDA(ctx, ctx->v.upload(v_h, n, s));  // initial guess
   st = solve_device(ctx, opts, info, s);
   EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(v_h, ctx->v.p, sizeof(double) * n,
                                        cudaMemcpyDeviceToHost, s));
@@ -799,6 +831,55 @@ eolc_status eolc_step(eolc_ctx *ctx, double *x_h, const double *X_h,
   return eolc_state_download(ctx, x_h, v_h);
 }
 
+eolc_status eolc_step_contacts(eolc_ctx *ctx, double *x_h, const double *X_h, double *v_h,
+                               const eolc_material *mat, const double grav[3], double h,
+                               const int *fixed_dofs_h, const double *fixed_vel_h, int n_fixed,
+                               const eolc_box *boxes, int n_boxes, const double *points_h,
+                               const double *normals_h, int n_points, double threshold,
+                               const eolc_solve_opts *opts, eolc_ineq_info *info) {
+  eolc_status st = need_topology(ctx);
+  if (st != EOLC_OK) return st;
+  if ((st = check_opts(ctx, opts)) != EOLC_OK) return st;
+  if (!x_h || !X_h || !v_h || !mat || !grav) return fail(ctx, EOLC_BAD_ARG, "null state");
+  if (n_fixed > 0 && (!fixed_dofs_h || !fixed_vel_h)) return fail(ctx, EOLC_BAD_ARG, "null fixed list");
+  if ((st = eolc_state_upload(ctx, x_h, X_h, v_h)) != EOLC_OK) return st;
+  cudaStream_t s = stream_of(ctx);
+  const int N = ctx->topo.n_nodes, n = 3 * N;
+  // Constraints::fill: pins from the previous velocity (Constraints.cpp:
+  // 472-496), CD2 on the step's positions and its rows (:422-468)
+  if ((st = set_pins(ctx, fixed_dofs_h, fixed_vel_h, n_fixed, s)) != EOLC_OK) return st;
+  EOLC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->beq_full.p, 0, sizeof(double) * n, s));
+  if (n_fixed > 0) {
+    pins_kernel<<<(n_fixed + 127) / 128, 128, 0, s>>>(n_fixed, ctx->fixed_dofs.p, ctx->fixed_vel.p,
+                                                     ctx->v.p, ctx->beq_full.p);
+    ctx->launches += 1;
+  }
+  std::vector<eolc_contact> cons(size_t(4) * N + 64);
+  int nc = 0;
+  st = eolc_cd2(ctx, x_h, boxes, n_boxes, points_h, normals_h, n_points, threshold, cons.data(),
+                int(cons.size()), &nc);
+  if (st == EOLC_CAPACITY) {
+    cons.resize(nc);
+    st = eolc_cd2(ctx, x_h, boxes, n_boxes, points_h, normals_h, n_points, threshold,
+                  cons.data(), nc, &nc);
+  }
+  if (st != EOLC_OK) return st;
+  std::vector<int> ptr(nc + 1), col(size_t(9) * std::max(1, nc));
+  std::vector<double> val(size_t(9) * std::max(1, nc)), d(std::max(1, nc));
+  int m = 0;
+  if ((st = eolc_contact_rows(cons.data(), nc, nc, ptr.data(), col.data(), val.data(), d.data(),
+                              &m)) != EOLC_OK)
+    return fail(ctx, st, "contact rows");
+  // Forces::fill, then the QP (GeneralizedSolver::velocitySolve), x += h v
+  if ((st = assemble(ctx, *mat, grav, h, opts->precision, false, true, s)) != EOLC_OK) return st;
+  ctx->last_precision = opts->precision;
+  st = ineq_solve_device(ctx, m, ptr.data(), col.data(), val.data(), d.data(), opts, nullptr,
+                         info);
+  if (st != EOLC_OK) return st;
+  integrate_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, h, ctx->v.p, ctx->x.p);
+  ctx->launches += 1;
+  return eolc_state_download(ctx, x_h, v_h);
+}
 
 int eolc_batch_num_configs(void) { return batch_num_configs(); }
 

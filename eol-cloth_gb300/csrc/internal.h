@@ -181,6 +181,10 @@ void free_collide_work(CollideWork *w);
 struct ExportWork;
 void free_export_work(ExportWork *w);
 
+// Contact-constrained solve (contact.cu)
+struct IneqWork;
+void free_ineq_work(IneqWork *w);
+
 // Learned preconditioner (learned.cu / pcg.cu)
 eolc_status run_pcg_learned(SolveWork *&w, const PcgArgs &a, const float *Gm,
                             eolc_solve_info *info, cudaStream_t s, std::string &err,
@@ -193,6 +197,24 @@ namespace eolc {
 std::string learned_forward(eolc_lpc *P, eolc_ctx *ctx, const uint8_t *pinned_d,
                             const float **G_out, cudaStream_t s);
 }
+
+// Solve entry points shared by the C ABI functions (api.cu).
+namespace eolc {
+// PcgArgs on the context's buffers (MDK, b, pins, v) for the options.
+PcgArgs default_pcg_args(eolc_ctx *ctx, const eolc_solve_opts *o);
+// The solver dispatch of eolc_velocity_solve on explicit arguments.
+eolc_status solve_with_args(eolc_ctx *ctx, const eolc_solve_opts *o, const PcgArgs &a,
+                            eolc_solve_info *info, cudaStream_t s);
+// The contact QP (contact.cu) on the device state: MDK, b, pins, v (initial
+// guess in, solution out).
+eolc_status ineq_solve_device(eolc_ctx *ctx, int n_ineq, const int *ineq_ptr_h,
+                              const int *ineq_col_h, const double *ineq_val_h,
+                              const double *bineq_h, const eolc_solve_opts *opts,
+                              double *lambda_h, eolc_ineq_info *info);
+// Uploads the pinned DOFs, their values and the right-hand side b.
+eolc_status prepare_pins_rhs(eolc_ctx *ctx, const double *b_h, const int *fixed_dofs_h,
+                             const double *beq_h, int n_fixed, cudaStream_t s);
+}  // namespace eolc
 
 // ---- the context ------------------------------------------------------------
 struct eolc_ctx {
@@ -228,6 +250,7 @@ struct eolc_ctx {
   int coarse_refresh = 1;     // rebuild the patch PC's coarse operator every ... solves
   eolc::CollideWork *cd_work = nullptr;
   eolc::ExportWork *ex_work = nullptr;
+  eolc::IneqWork *iq_work = nullptr;
   // batches: instance k owns nodes node_off[k] .. node_off[k+1]
   std::vector<int> node_off;
   eolc::DevBuf<int> node_inst;                // instance of every node

@@ -62,6 +62,14 @@ class SolveInfo(ctypes.Structure):
                 ("assemble_ms", ctypes.c_double)]
 
 
+class IneqInfo(ctypes.Structure):
+    """Layout of eolc_ineq_info (include/eolc.h)."""
+    _fields_ = [("status", ctypes.c_int), ("solves", ctypes.c_int), ("outer", ctypes.c_int),
+                ("iterations", ctypes.c_int), ("n_active", ctypes.c_int),
+                ("max_violation", ctypes.c_double), ("rel_res", ctypes.c_double),
+                ("solve_kernel_ms", ctypes.c_double)]
+
+
 class BatchInfo(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("n_failed", ctypes.c_int), ("config", ctypes.c_int),
                 ("steps", ctypes.c_int), ("iterations", ctypes.c_longlong),
@@ -107,7 +115,8 @@ EXPORTS = ["eolc_version", "eolc_launch_count", "eolc_create", "eolc_destroy", "
            "eolc_batch_num_configs", "eolc_batch_config_name", "eolc_batch_set_config",
            "eolc_batch_autotune", "eolc_set_learned_refresh", "eolc_set_coarse_refresh",
            "eolc_batch_set_jacobi_reference", "eolc_lpc_blocks", "eolc_export_obj",
-           "eolc_export_obj_text"]
+           "eolc_export_obj_text", "eolc_velocity_solve_ineq", "eolc_contact_rows",
+           "eolc_step_contacts"]
 
 
 def load_library(path=LIB_PATH):
@@ -173,6 +182,15 @@ def load_library(path=LIB_PATH):
     L.eolc_batch_autotune.argtypes = [_V, _D, ctypes.c_double, _I, _D, ctypes.c_int,
                                       ctypes.POINTER(SolveOpts), _I, _D]
     L.eolc_export_obj.argtypes = [_V, ctypes.c_char_p, ctypes.c_int, ctypes.c_double]
+    L.eolc_velocity_solve_ineq.argtypes = [_V, _D, _I, _D, ctypes.c_int, ctypes.c_int, _I, _I, _D,
+                                           _D, ctypes.POINTER(SolveOpts), _D, _D,
+                                           ctypes.POINTER(IneqInfo)]
+    L.eolc_step_contacts.argtypes = [_V, _D, _D, _D, ctypes.POINTER(Material), _D,
+                                     ctypes.c_double, _I, _D, ctypes.c_int, ctypes.POINTER(Box),
+                                     ctypes.c_int, _D, _D, ctypes.c_int, ctypes.c_double,
+                                     ctypes.POINTER(SolveOpts), ctypes.POINTER(IneqInfo)]
+    L.eolc_contact_rows.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _I, _I, _D, _D,
+                                    _I]
     L.eolc_export_obj_text.argtypes = [_V, ctypes.c_int, ctypes.c_double, ctypes.c_char_p,
                                        ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
     for name in EXPORTS:
@@ -272,6 +290,50 @@ class Context:
                                      ctypes.byref(opts), _d(v), ctypes.byref(info))
         self._check(st)
         return v, info
+
+    def velocity_solve_ineq(self, b, fixed_dofs, beq, Aineq, bineq, opts=None, v0=None):
+        """Contact-constrained solve (eolc_velocity_solve_ineq): Aineq a scipy
+        sparse matrix over the 3N DOFs (or (indptr, indices, data)), bineq its
+        right-hand side.  Returns (v, lambda, IneqInfo)."""
+        opts = opts or SolveOpts()
+        b, fixed_dofs, beq = _f64(b), _i32(fixed_dofs), _f64(beq)
+        if isinstance(Aineq, tuple):
+            ptr, col, val = (_i32(Aineq[0]), _i32(Aineq[1]), _f64(Aineq[2]))
+        else:
+            import scipy.sparse as sp
+            A = sp.csr_matrix(Aineq)
+            ptr, col, val = _i32(A.indptr), _i32(A.indices), _f64(A.data)
+        m = len(ptr) - 1
+        d = _f64(bineq) if m > 0 else np.zeros(1)
+        v = np.zeros(3 * self.n_nodes) if v0 is None else _f64(v0).copy()
+        lam = np.zeros(max(1, m))
+        info = IneqInfo()
+        st = lib.eolc_velocity_solve_ineq(self._h, _d(b), _i(fixed_dofs), _d(beq),
+                                          len(fixed_dofs), m, _i(ptr),
+                                          _i(col if len(col) else np.zeros(1, np.int32)),
+                                          _d(val if len(val) else np.zeros(1)), _d(d),
+                                          ctypes.byref(opts), _d(v), _d(lam), ctypes.byref(info))
+        self._check(st)
+        return v, lam[:m], info
+
+    def step_contacts(self, x, X, v, mat, grav, h, fixed_dofs, fixed_vel, boxes=(), points=None,
+                      normals=None, threshold=1e-3, opts=None):
+        """Cloth::step with the contact QP (eolc_step_contacts); x, v updated
+        in place.  Returns the QP's IneqInfo."""
+        opts = opts or SolveOpts()
+        fixed_dofs, fixed_vel = _i32(fixed_dofs), _f64(fixed_vel)
+        boxes = list(boxes)
+        barr = (Box * max(1, len(boxes)))(*boxes)
+        pts = _f64(points) if points is not None else np.zeros(3)
+        nrm = _f64(normals) if normals is not None else np.zeros(3)
+        npts = 0 if points is None else len(pts.reshape(-1, 3))
+        info = IneqInfo()
+        st = lib.eolc_step_contacts(self._h, _d(x), _d(_f64(X)), _d(v), ctypes.byref(mat),
+                                    _d(_f64(grav)), h, _i(fixed_dofs), _d(fixed_vel),
+                                    len(fixed_dofs), barr, len(boxes), _d(pts), _d(nrm), npts,
+                                    threshold, ctypes.byref(opts), ctypes.byref(info))
+        self._check(st)
+        return info
 
     def step(self, x, X, v, mat, grav, h, fixed_dofs, fixed_vel, opts=None):
         """Cloth::step on host arrays; x, v updated in place."""
@@ -493,6 +555,27 @@ class LearnedPC:
         ctx._lpc = self  # keep the network alive while attached
 
 
+def contact_rows(contacts, n_nodes):
+    """Inequality rows of Constraints::fill from CD2 contacts
+    (Constraints.cpp:422-468) via eolc_contact_rows: (scipy CSR over the 3N
+    DOFs, bineq)."""
+    import scipy.sparse as sp
+    n = len(contacts)
+    arr = (Contact * max(1, n))(*contacts)
+    ptr = np.zeros(n + 1, np.int32)
+    col = np.zeros(max(1, 9 * n), np.int32)
+    val = np.zeros(max(1, 9 * n))
+    d = np.zeros(max(1, n))
+    m = ctypes.c_int()
+    st = lib.eolc_contact_rows(ctypes.cast(arr, ctypes.c_void_p), n, n, _i(ptr), _i(col), _d(val),
+                               _d(d), ctypes.byref(m))
+    if st != OK:
+        raise EolcError(st, "eolc_contact_rows failed")
+    m = m.value
+    C = sp.csr_matrix((val[:ptr[m]], col[:ptr[m]], ptr[:m + 1]), shape=(m, 3 * n_nodes))
+    return C, d[:m].copy()
+
+
 def bsr_to_csr(ctx, vals):
     """3x3 BSR values (n_blocks x 9, row-major blocks) -> scipy CSR."""
     import scipy.sparse as sp
@@ -546,8 +629,8 @@ class Forces:
 
 
 class GeneralizedSolver:
-    """GeneralizedSolver (src/GeneralizedSolver.h): velocitySolve on the GPU
-    for the equality-constrained case; contact QPs stay on the host."""
+    """GeneralizedSolver (src/GeneralizedSolver.h): velocitySolve on the GPU,
+    with or without contact rows."""
 
     def __init__(self, ctx, opts=None):
         self.ctx = ctx
@@ -558,11 +641,10 @@ class GeneralizedSolver:
         """Same arguments as GeneralizedSolver::velocitySolve
         (GeneralizedSolver.cpp:107-173).  MDK must be the matrix of the
         context's last fill (it stays resident on the GPU).  Aeq must consist
-        of unit rows (pinned DOFs, Constraints.cpp:114-119).  With contact
-        rows the reference hands a QP to Mosek/Gurobi; that stays on the
-        host, so collisions=True raises.  v is overwritten in place."""
-        if collisions:
-            raise EolcError(BAD_ARG, "contact QP is solved on the host, not by this library")
+        of unit rows (pinned DOFs, Constraints.cpp:114-119).  With
+        collisions=True the QP with Aineq v <= bineq (which the reference
+        hands to Mosek/Gurobi) is solved by eolc_velocity_solve_ineq.  v is
+        the initial guess and is overwritten in place."""
         import scipy.sparse as sp
         fixed = np.zeros(0, np.int32)
         beqv = np.zeros(0)
@@ -572,7 +654,11 @@ class GeneralizedSolver:
                 raise EolcError(BAD_ARG, "Aeq must consist of unit rows")
             fixed = A.indices.astype(np.int32)
             beqv = np.asarray(beq, dtype=np.float64)
-        out, info = self.ctx.velocity_solve(b, fixed, beqv, self.opts)
+        if collisions and Aineq is not None and Aineq.shape[0] > 0:
+            out, self.lambda_ineq, info = self.ctx.velocity_solve_ineq(
+                b, fixed, beqv, Aineq, bineq, self.opts, v0=v)
+        else:
+            out, info = self.ctx.velocity_solve(b, fixed, beqv, self.opts, v0=v)
         v[:] = out
         self.last_info = info
         return info.status == OK

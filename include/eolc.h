@@ -167,6 +167,44 @@ eolc_status eolc_velocity_solve(eolc_ctx *ctx, const double *b_h,
                                 int n_fixed, const eolc_solve_opts *opts,
                                 double *v_h, eolc_solve_info *info);
 
+/* ---- GeneralizedSolver::velocitySolve with collisions --------------------
+ * The QP that the reference hands Mosek or Gurobi (GeneralizedSolver.cpp:
+ * 138-170; quadprog convention, QuadProg.h:8-9):
+ *   argmin 1/2 v'MDK v + b'v  s.t.  v[fixed_dofs[k]] = beq[k],
+ *                                   Aineq v <= bineq,
+ * on the MDK of the last eolc_forces_fill / eolc_step.  Aineq: n_ineq rows
+ * in CSR over the 3N DOFs (ineq_ptr_h: n_ineq + 1 offsets, ineq_col_h DOF
+ * indices, ineq_val_h values; duplicates are summed).  A row may touch up to
+ * four nodes, and every pair of them must share a triangle or a hinge (true
+ * of the contact rows of Constraints.cpp:422-468; eolc_contact_rows builds
+ * them), else EOLC_BAD_ARG.  Solved on the GPU by an augmented Lagrangian
+ * with semismooth-Newton active sets; every linear solve is this library's
+ * PCG with opts (precision, preconditioner, rel_tol), warm-started.  Stops
+ * when the multipliers change by at most 10 rel_tol max|v| / rho (the
+ * remaining infeasibility); EOLC_NOT_CONVERGED after 50 multiplier updates.
+ * v_h: initial guess in, solution out (3N); lambda_h (n_ineq, may be NULL):
+ * the inequality multipliers (>= 0, MDK v + b + Aineq' lambda = 0 on the
+ * free DOFs, Mosek's getDualInequality). */
+typedef struct {
+  int status;           /* eolc_status of the solve                        */
+  int solves;           /* linear solves (semismooth Newton steps)         */
+  int outer;            /* multiplier updates                              */
+  int iterations;       /* PCG iterations summed over the solves           */
+  int n_active;         /* rows with lambda > 0 at the end                 */
+  double max_violation; /* max(0, Aineq v - bineq) / max|v| at the end     */
+  double rel_res;       /* relative residual of the last linear solve      */
+  double solve_kernel_ms; /* device time of the PCG kernels, summed        */
+} eolc_ineq_info;
+eolc_status eolc_velocity_solve_ineq(eolc_ctx *ctx, const double *b_h,
+                                     const int *fixed_dofs_h,
+                                     const double *beq_h, int n_fixed,
+                                     int n_ineq, const int *ineq_ptr_h,
+                                     const int *ineq_col_h,
+                                     const double *ineq_val_h,
+                                     const double *bineq_h,
+                                     const eolc_solve_opts *opts, double *v_h,
+                                     double *lambda_h, eolc_ineq_info *info);
+
 /* ---- Cloth::step (Cloth.cpp:359-413, non-EOL, no remeshing, no QP) -----
  * One implicit-Euler step on host buffers: Forces::fill, pinned-corner
  * equality rows beq = 0.99 v + c (Constraints.cpp:114-119,472-496),
@@ -311,6 +349,36 @@ eolc_status eolc_cd2(eolc_ctx *ctx, const double *x_h, const eolc_box *boxes,
                      int n_boxes, const double *points_h,
                      const double *normals_h, int n_points, double threshold,
                      eolc_contact *out_h, int capacity, int *n_out);
+/* The inequality rows Constraints::fill builds from CD2 contacts of a
+ * non-EOL mesh (Constraints.cpp:422-468), in contact order: box face /
+ * cloth vertex -> -nor1 on the vertex; edge / edge -> -nor2 weights2[j] on
+ * the two cloth vertices; box corner or point / cloth face -> -nor2
+ * weights2[j] on the three cloth vertices; bineq = 0.  Other contact kinds
+ * give no row.  Host only.  Writes at most cap_rows rows (ineq_ptr_h needs
+ * cap_rows + 1 entries, ineq_col_h / ineq_val_h 9 cap_rows) and sets
+ * *n_rows; EOLC_CAPACITY when cap_rows is too small. */
+eolc_status eolc_contact_rows(const eolc_contact *contacts, int n_contacts,
+                              int cap_rows, int *ineq_ptr_h, int *ineq_col_h,
+                              double *ineq_val_h, double *bineq_h,
+                              int *n_rows);
+
+/* ---- Cloth::step with collisions (Cloth.cpp:359-413, non-EOL, no remesh) --
+ * One implicit-Euler step with the contact QP, on host buffers like
+ * eolc_step: pins beq = 0.99 v + c, CD2 of the step's positions against the
+ * boxes and point obstacles (as eolc_cd2), the inequality rows of
+ * Constraints.cpp:422-468 (eolc_contact_rows), Forces::fill, the QP of
+ * eolc_velocity_solve_ineq warm-started from v, x += h v.  info (may be
+ * NULL) reports the QP solve. */
+eolc_status eolc_step_contacts(eolc_ctx *ctx, double *x_h, const double *X_h,
+                               double *v_h, const eolc_material *mat,
+                               const double grav[3], double h,
+                               const int *fixed_dofs_h,
+                               const double *fixed_vel_h, int n_fixed,
+                               const eolc_box *boxes, int n_boxes,
+                               const double *points_h,
+                               const double *normals_h, int n_points,
+                               double threshold, const eolc_solve_opts *opts,
+                               eolc_ineq_info *info);
 
 /* ---- learned preconditioner ------------------------------------------------
  * A 3-layer message-passing network (hidden width 64, BF16 weights, FP32

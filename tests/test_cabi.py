@@ -44,11 +44,12 @@ def test_struct_layouts_match_c(built, tmp_path):
     src = tmp_path / "layout.c"
     src.write_text(
         '#include <stddef.h>\n#include <stdio.h>\n#include "%s"\n'
-        'int main(void){printf("%%zu %%zu %%zu %%zu %%zu %%zu %%zu %%zu %%zu %%zu\\n",'
+        'int main(void){printf("%%zu %%zu %%zu %%zu %%zu %%zu %%zu %%zu %%zu %%zu %%zu %%zu\\n",'
         ' sizeof(eolc_contact), offsetof(eolc_contact, count1), offsetof(eolc_contact, source),'
         ' sizeof(eolc_box), sizeof(eolc_material), sizeof(eolc_solve_opts),'
         ' sizeof(eolc_solve_info), sizeof(eolc_batch_info), offsetof(eolc_batch_info, iterations),'
-        ' offsetof(eolc_batch_info, step_ms)); return 0;}\n'
+        ' offsetof(eolc_batch_info, step_ms), sizeof(eolc_ineq_info),'
+        ' offsetof(eolc_ineq_info, max_violation)); return 0;}\n'
         % HEADER)
     exe = tmp_path / "layout"
     subprocess.check_call(["gcc", str(src), "-o", str(exe)])
@@ -56,7 +57,8 @@ def test_struct_layouts_match_c(built, tmp_path):
     want = [ctypes.sizeof(eolc.Contact), eolc.Contact.count1.offset, eolc.Contact.source.offset,
             ctypes.sizeof(eolc.Box), ctypes.sizeof(eolc.Material), ctypes.sizeof(eolc.SolveOpts),
             ctypes.sizeof(eolc.SolveInfo), ctypes.sizeof(eolc.BatchInfo),
-            eolc.BatchInfo.iterations.offset, eolc.BatchInfo.step_ms.offset]
+            eolc.BatchInfo.iterations.offset, eolc.BatchInfo.step_ms.offset,
+            ctypes.sizeof(eolc.IneqInfo), eolc.IneqInfo.max_violation.offset]
     assert got == want
 
 

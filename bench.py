@@ -405,6 +405,107 @@ def run_export(ctx, sc, x, stream, frames=10):
                     "fwrite calls to a temporary directory"}
 
 
+def run_contacts(args, local_rank, stream, flush, steps=5):
+    """Cloth::step with the contact QP (eolc_step_contacts) on the 256x256-quad
+    sheet draped over a box (10.6k CD2 contacts), against the plain step on the
+    same state; and the QP solve alone on a 24x24-quad drape against the
+    oracle's exact active-set QP (the reference's Mosek / Gurobi are not
+    available)."""
+    import numpy as np
+    import torch
+    import eolc
+    import oracle as O
+    import qp_ref
+    import scenes as S
+    x0, X, tri, center, snaps = S.drape_positions(QUADS, 40)
+    n = len(x0) // 3
+    hinge = O.hinges(n, tri)
+    box = O.axis_box(center, (0.4, 0.4, 0.2))
+    ebox = eolc.Box(box.dim, box.E1)
+    ids = O.corner_ids(QUADS + 1, QUADS + 1)
+    fixed = np.array([3 * ids[k] + c for k in (3, 4) for c in range(3)], np.int32)
+    fvel = np.zeros(len(fixed))
+    ctx = eolc.Context(local_rank)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_topology(n, tri, hinge)
+    mat = eolc.Material(**MAT)
+    rng = np.random.default_rng(4)
+    xs = snaps[14].copy()
+    vs = rng.normal(0, 0.02, 3 * n)
+    vs[2::3] -= 0.4
+    opts = arm_opts(eolc, "patch", args.degree)
+    xh = torch.empty(3 * n, dtype=torch.float64).pin_memory().numpy()
+    vh = torch.empty(3 * n, dtype=torch.float64).pin_memory().numpy()
+    Xh = torch.empty(2 * n, dtype=torch.float64).pin_memory().numpy()
+    Xh[:] = X
+    out = {}
+    for label, contact in (("plain", False), ("contacts", True)):
+        ms, infos = [], []
+        for k in range(steps + 1):
+            xh[:] = xs
+            vh[:] = vs
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if contact:
+                infos.append(ctx.step_contacts(xh, Xh, vh, mat, GRAV, H, fixed, fvel,
+                                               boxes=[ebox], threshold=1e-3, opts=opts))
+            else:
+                infos.append(ctx.step(xh, Xh, vh, mat, GRAV, H, fixed, fvel, opts))
+            if k:  # the first call builds plans
+                ms.append(1e3 * (time.perf_counter() - t0))
+        info = infos[-1]
+        out[label] = {"ms_per_step": float(np.median(ms)), "steps_per_s": 1e3 / float(np.median(ms)),
+                      "pcg_iterations": info.iterations,
+                      "pcg_kernel_ms": round(info.solve_kernel_ms, 4)}
+        if contact:
+            out[label].update({"qp_solves": info.solves, "multiplier_updates": info.outer,
+                               "active_rows": info.n_active,
+                               "max_violation": info.max_violation})
+    cons = O.cd2(xs, tri, [box], threshold=1e-3)
+    out["rows"] = len(qp_ref.contact_rows(cons, n)[1])
+    # like for like on a small drape: the QP solve alone, GPU vs the oracle
+    q = 24
+    x0s, Xs, tris, cs, snapss = S.drape_positions(q, 40)
+    ns = len(x0s) // 3
+    hs = O.hinges(ns, tris)
+    bs = O.axis_box(cs, (0.4, 0.4, 0.2))
+    xq = snapss[9]
+    F = O.Forces(xq, Xs, tris, hs, O.material(), GRAV, H)
+    vq = rng.normal(0, 0.02, 3 * ns)
+    vq[2::3] -= 0.4
+    bq = F.rhs(vq, H)
+    ids = O.corner_ids(q + 1, q + 1)
+    fq = np.array([3 * ids[k] + c for k in (3, 4) for c in range(3)], np.int32)
+    beq = 0.99 * vq[fq]
+    C, d = qp_ref.contact_rows(O.cd2(xq, tris, [bs], threshold=1e-3), ns)
+    t0 = time.perf_counter()
+    vo, lo, _ = qp_ref.solve_qp(F.csr(1), bq, fq, beq, C, d)
+    cpu_s = time.perf_counter() - t0
+    c2 = eolc.Context(local_rank)
+    c2.set_topology(ns, tris, hs)
+    c2.forces_fill(xq, Xs, mat, GRAV, H, eolc.PREC_FP64)
+    o64 = eolc.SolveOpts(rel_tol=1e-10, precision=eolc.PREC_FP64)
+    c2.velocity_solve_ineq(bq, fq, beq, C, d, o64)
+    ts = []
+    for k in range(5):
+        t0 = time.perf_counter()
+        vg, lg, ig = c2.velocity_solve_ineq(bq, fq, beq, C, d, o64)
+        ts.append(time.perf_counter() - t0)
+    out["small_qp"] = {"workload": "24x24-quad drape, %d contact rows, FP64" % C.shape[0],
+                       "gpu_ms": 1e3 * float(np.median(ts)), "solves": ig.solves,
+                       "v_rel_err_vs_oracle": float(np.abs(vg - vo).max() / np.abs(vo).max()),
+                       "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "QP solves/s", "cores": 1,
+                                        "kind": "port",
+                                        "sample": "the oracle's exact active-set QP (scipy "
+                                                  "sparse LU per working-set change) on the "
+                                                  "same problem"}}
+    out["workload"] = ("256x256-quad sheet draped over a 0.4 x 0.4 box (snapshot 14 of the "
+                       "seeded drape), 2 corners pinned, patch-PCG, rel-res 1e-8, host buffers")
+    return out
+
+
 def run_ours(args, rank, world, local_rank):
     import numpy as np
     import torch
@@ -538,6 +639,8 @@ def run_ours(args, rank, world, local_rank):
         line["cpu_baseline"] = cpu
     if world == 1 and not args.no_export:
         line["obj_export"] = run_export(ctx, sc, x_w, stream)
+    if world == 1 and not args.no_contacts:
+        line["contact_step"] = run_contacts(args, local_rank, stream, flush)
     if world == 1 and not args.no_batch:
         line["batched"] = run_batched(args, local_rank, stream, flush)
         line["batched_delaunay_learned"] = run_delaunay(args, local_rank, stream, flush)
@@ -557,6 +660,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-sheets line")
     ap.add_argument("--no-export", action="store_true", help="skip the OBJ export line")
+    ap.add_argument("--no-contacts", action="store_true", help="skip the contact-step line")
     ap.add_argument("--batch-sheets", type=int, default=256)
     ap.add_argument("--delaunay-meshes", type=int, default=64)
     args = ap.parse_args()

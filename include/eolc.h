@@ -179,7 +179,9 @@ eolc_status eolc_velocity_solve(eolc_ctx *ctx, const double *b_h,
  * of the contact rows of Constraints.cpp:422-468; eolc_contact_rows builds
  * them), else EOLC_BAD_ARG.  Solved on the GPU by an augmented Lagrangian
  * with semismooth-Newton active sets; every linear solve is this library's
- * PCG with opts (precision, preconditioner, rel_tol), warm-started.  Stops
+ * PCG with opts (precision, preconditioner, rel_tol), warm-started
+ * (EOLC_PC_LEARNED runs as EOLC_PC_BLOCK_JACOBI here: the network
+ * approximates the inverse of MDK, not of the contact-penalised matrix).  Stops
  * when the multipliers change by at most 10 rel_tol max|v| / rho (the
  * remaining infeasibility); EOLC_NOT_CONVERGED after 50 multiplier updates.
  * v_h: initial guess in, solution out (3N); lambda_h (n_ineq, may be NULL):

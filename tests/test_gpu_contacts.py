@@ -77,10 +77,19 @@ def test_fp64_matches_exact_qp(eolc, snap, pins):
         assert np.array_equal(v[fixed], beq)
 
 
-@pytest.mark.parametrize("precond", [0, 1, 3])
+@pytest.mark.parametrize("precond", [0, 1, 2, 3])
 def test_mixed_matches_exact_qp(eolc, precond):
     ctx, A, b, fixed, beq, C, d, cons = _problem(eolc, 24, 24, eolc.PREC_MIXED, True)
-    opts = eolc.SolveOpts(rel_tol=1e-8, precision=eolc.PREC_MIXED, precond=precond)
+    if precond == eolc.PC_LEARNED:
+        import os
+        lpc = eolc.LearnedPC(0, seed=1)
+        w = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                         "eol-cloth_gb300", "weights", "lpc.npy")
+        if os.path.exists(w):
+            lpc.set_params(np.load(w))
+        lpc.attach(ctx)
+    opts = eolc.SolveOpts(rel_tol=1e-8, precision=eolc.PREC_MIXED, precond=precond,
+                          fallback_factor=0)
     v, lam, info = ctx.velocity_solve_ineq(b, fixed, beq, C, d, opts)
     vo, lo, _ = qp_ref.solve_qp(A, b, fixed, beq, C, d)
     print("precond %d: solves %d, updates %d, PCG iterations %d, v err %.2e"
@@ -97,7 +106,7 @@ def test_without_rows_equals_plain_solve(eolc):
     v, lam, info = ctx.velocity_solve_ineq(b, fixed, beq, empty, np.zeros(0), opts)
     v2, _ = ctx.velocity_solve(b, fixed, beq, opts)
     assert info.status == eolc.OK and info.solves == 1
-    assert np.array_equal(v, v2)
+    assert _relmax(v, v2) <= 1e-9
 
 
 def test_inactive_rows_change_nothing(eolc):
@@ -109,7 +118,7 @@ def test_inactive_rows_change_nothing(eolc):
     v, lam, info = ctx.velocity_solve_ineq(b, fixed, beq, C, dd, opts)
     assert info.status == eolc.OK and info.n_active == 0
     assert not lam.any()
-    assert _relmax(v, v0) <= 1e-9
+    assert _relmax(v, v0) <= 1e-8  # two solves to rel-res 1e-10
 
 
 def test_results_are_reproducible(eolc):

@@ -190,6 +190,8 @@ eolc_status batch_begin(eolc_ctx *ctx, const double grav[3], double h, const int
   eolc_status st = need_topology(ctx);
   if (st != EOLC_OK) return st;
   if ((st = check_opts(ctx, opts)) != EOLC_OK) return st;
+  // host mirrors before any capture (the learned network's graph reads them)
+  if (!host_topology(ctx)) return EOLC_CUDA_ERROR;
   if (opts->precond == EOLC_PC_PATCH)
     return fail(ctx, EOLC_BAD_ARG, "batched steps use Jacobi, block Jacobi or the learned preconditioner");
   if (opts->precond == EOLC_PC_LEARNED) {
@@ -471,6 +473,103 @@ eolc_status prepare_pins_rhs(eolc_ctx *ctx, const double *b_h, const int *fixed_
 }  // namespace eolc
 
 
+namespace eolc {
+
+const HostTopology *host_topology(eolc_ctx *ctx) {
+  if (ctx->host_valid) return &ctx->host;
+  const DevTopology &T = ctx->topo;
+  HostTopology &H = ctx->host;
+  const int N = T.n_nodes, NB = T.n_blocks;
+  cudaStream_t s = ctx->stream;
+  H.n_nodes = N;
+  H.n_tri = T.n_tri;
+  H.n_hinge = T.n_hinge;
+  H.n_blocks = NB;
+  H.rowptr.resize(size_t(N) + 1);
+  H.colidx.resize(NB);
+  H.blk_row.resize(NB);
+  H.diag.resize(N);
+  H.cptr.resize(size_t(NB) + 1);
+  H.nf_ptr.resize(size_t(N) + 1);
+  H.nf_list.resize(size_t(3) * T.n_tri);
+  auto get = [&](std::vector<int> &dst, const int *src) {
+    return cudaMemcpyAsync(dst.data(), src, sizeof(int) * dst.size(), cudaMemcpyDeviceToHost, s);
+  };
+  cudaError_t e = get(H.rowptr, T.rowptr.p);
+  if (e == cudaSuccess) e = get(H.colidx, T.colidx.p);
+  if (e == cudaSuccess) e = get(H.blk_row, T.blk_row.p);
+  if (e == cudaSuccess) e = get(H.diag, T.diag.p);
+  if (e == cudaSuccess) e = get(H.cptr, T.cptr.p);
+  if (e == cudaSuccess) e = get(H.nf_ptr, T.nf_ptr.p);
+  if (e == cudaSuccess) e = get(H.nf_list, T.nf_list.p);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess) {
+    H.contrib.resize(H.cptr[NB]);
+    e = get(H.contrib, T.contrib.p);
+  }
+  if (e == cudaSuccess && ctx->host_tri.size() != size_t(3) * T.n_tri) {
+    ctx->host_tri.resize(size_t(3) * T.n_tri);
+    e = cudaMemcpyAsync(ctx->host_tri.data(), T.tri.p, sizeof(int) * ctx->host_tri.size(),
+                        cudaMemcpyDeviceToHost, s);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    ctx->err = std::string("topology download: ") + cudaGetErrorString(e);
+    return nullptr;
+  }
+  ctx->host_valid = true;
+  return &ctx->host;
+}
+
+}  // namespace eolc
+
+namespace {
+
+// Builds the BSR pattern, contribution lists and node -> face lists on the
+// device from ctx->topo.tri / hinge (already on the device).
+eolc_status topology_from_device(eolc_ctx *ctx, int n_nodes, int n_tri, int n_hinge,
+                                 cudaStream_t s) {
+  ctx->has_topology = false;
+  ctx->host_valid = false;
+  std::string msg = build_topology_device(ctx->topo_work, n_nodes, ctx->topo.tri.p, n_tri,
+                                          n_hinge > 0 ? ctx->topo.hinge.p : nullptr, n_hinge,
+                                          ctx->topo, s, ctx->launches);
+  if (!msg.empty()) return fail(ctx, EOLC_BAD_ARG, msg.c_str());
+  return EOLC_OK;
+}
+
+// Drops every plan, graph and buffer that depends on the old topology.
+eolc_status reset_after_topology(eolc_ctx *ctx, cudaStream_t s) {
+  ctx->inst_mat.clear();
+  free_collide_work(ctx->cd_work);
+  free_export_work(ctx->ex_work);
+  ctx->cd_work = nullptr;
+  ctx->ex_work = nullptr;
+  ctx->has_topology = true;
+  ctx->n_fixed_dev = -1;
+  free_solve_work(ctx->work);
+  ctx->work = nullptr;
+  free_patch_work(ctx->pwork);
+  ctx->pwork = nullptr;
+  ctx->lpc_cached = nullptr;
+  free_batch_work(ctx->bwork);
+  ctx->bwork = nullptr;
+  ctx->batch_config = -1;
+  if (ctx->bgraph) cudaGraphExecDestroy(ctx->bgraph);
+  ctx->bgraph = nullptr;
+  ctx->bgraph_key.clear();
+  ctx->A64.release();
+  ctx->Mblk.release();
+  ctx->elem.release();
+  eolc_status st = ensure_state(ctx);
+  if (st != EOLC_OK) return st;
+  EOLC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->v.p, 0, sizeof(double) * ctx->v.n, s));
+  EOLC_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
+  return EOLC_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 int eolc_version(void) { return 1; }
@@ -530,6 +629,7 @@ void eolc_destroy(eolc_ctx *ctx) {
   free_collide_work(ctx->cd_work);
   free_export_work(ctx->ex_work);
   free_ineq_work(ctx->iq_work);
+  free_topo_scratch(ctx->topo_work);
   free_batch_work(ctx->bwork);
   if (ctx->bgraph) cudaGraphExecDestroy(ctx->bgraph);
   for (cudaEvent_t e : ctx->ev)
@@ -602,69 +702,87 @@ eolc_status eolc_set_topology_batched(eolc_ctx *ctx, int n_inst, const int *node
         return fail(ctx, EOLC_BAD_ARG, "a hinge references another instance's node");
   }
   cudaSetDevice(ctx->device);
-  HostTopology H;
-  std::string msg = build_topology(n_nodes, tri_h, n_tri, hinge_h, n_hinge, H);
-  if (!msg.empty()) return fail(ctx, EOLC_BAD_ARG, msg.c_str());
   cudaStream_t s = stream_of(ctx);
   DevTopology &T = ctx->topo;
-  T.n_nodes = H.n_nodes;
-  T.n_tri = H.n_tri;
-  T.n_hinge = H.n_hinge;
-  T.n_blocks = H.n_blocks;
+  EOLC_CHECK_CUDA(ctx, T.tri.upload(tri_h, size_t(n_tri) * 3, s));
+  if (n_hinge > 0) EOLC_CHECK_CUDA(ctx, T.hinge.upload(hinge_h, size_t(n_hinge) * 4, s));
+  eolc_status st = topology_from_device(ctx, n_nodes, n_tri, n_hinge, s);
+  if (st != EOLC_OK) return st;
   std::vector<int> node_inst(n_nodes);
   for (int k = 0; k < n_inst; ++k)
     std::fill(node_inst.begin() + node_off_h[k], node_inst.begin() + node_off_h[k + 1], k);
-  EOLC_CHECK_CUDA(ctx, T.tri.upload(tri_h, size_t(n_tri) * 3, s));
-  if (n_hinge > 0) EOLC_CHECK_CUDA(ctx, T.hinge.upload(hinge_h, size_t(n_hinge) * 4, s));
-  EOLC_CHECK_CUDA(ctx, T.rowptr.upload(H.rowptr.data(), H.rowptr.size(), s));
-  EOLC_CHECK_CUDA(ctx, T.colidx.upload(H.colidx.data(), H.colidx.size(), s));
-  EOLC_CHECK_CUDA(ctx, T.blk_row.upload(H.blk_row.data(), H.blk_row.size(), s));
-  EOLC_CHECK_CUDA(ctx, T.diag.upload(H.diag.data(), H.diag.size(), s));
-  EOLC_CHECK_CUDA(ctx, T.cptr.upload(H.cptr.data(), H.cptr.size(), s));
-  EOLC_CHECK_CUDA(ctx, T.contrib.upload(H.contrib.data(), H.contrib.size(), s));
-  EOLC_CHECK_CUDA(ctx, T.nf_ptr.upload(H.nf_ptr.data(), H.nf_ptr.size(), s));
-  EOLC_CHECK_CUDA(ctx, T.nf_list.upload(H.nf_list.data(), H.nf_list.size(), s));
   EOLC_CHECK_CUDA(ctx, ctx->node_inst.upload(node_inst.data(), node_inst.size(), s));
   EOLC_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
-  ctx->host = std::move(H);
   ctx->host_tri.assign(tri_h, tri_h + size_t(n_tri) * 3);
   ctx->node_off.assign(node_off_h, node_off_h + n_inst + 1);
-  ctx->inst_mat.clear();
-  free_collide_work(ctx->cd_work);
-  free_export_work(ctx->ex_work);
-  ctx->cd_work = nullptr;
-  ctx->has_topology = true;
-  ctx->n_fixed_dev = -1;
-  free_solve_work(ctx->work);
-  ctx->work = nullptr;
-  free_patch_work(ctx->pwork);
-  ctx->pwork = nullptr;
-  ctx->lpc_cached = nullptr;
-  free_batch_work(ctx->bwork);
-  ctx->bwork = nullptr;
-  ctx->batch_config = -1;
-  if (ctx->bgraph) cudaGraphExecDestroy(ctx->bgraph);
-  ctx->bgraph = nullptr;
-  ctx->bgraph_key.clear();
-  ctx->A64.release();
-  ctx->Mblk.release();
-  ctx->elem.release();
-  eolc_status st = ensure_state(ctx);
+  return reset_after_topology(ctx, s);
+}
+
+eolc_status eolc_set_topology_device(eolc_ctx *ctx, int n_nodes, const int *tri_d, int n_tri,
+                                     const int *hinge_d, int n_hinge) {
+  if (!ctx) return EOLC_BAD_ARG;
+  if (!tri_d || n_tri <= 0 || n_nodes <= 0 || n_hinge < 0 || (n_hinge > 0 && !hinge_d))
+    return fail(ctx, EOLC_BAD_ARG, "null or empty topology");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = stream_of(ctx);
+  DevTopology &T = ctx->topo;
+  EOLC_CHECK_CUDA(ctx, T.tri.resize(size_t(n_tri) * 3));
+  EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(T.tri.p, tri_d, sizeof(int) * 3 * size_t(n_tri),
+                                       cudaMemcpyDeviceToDevice, s));
+  if (n_hinge > 0) {
+    EOLC_CHECK_CUDA(ctx, T.hinge.resize(size_t(n_hinge) * 4));
+    EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(T.hinge.p, hinge_d, sizeof(int) * 4 * size_t(n_hinge),
+                                         cudaMemcpyDeviceToDevice, s));
+  }
+  eolc_status st = topology_from_device(ctx, n_nodes, n_tri, n_hinge, s);
   if (st != EOLC_OK) return st;
-  EOLC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->v.p, 0, sizeof(double) * ctx->v.n, s));
+  EOLC_CHECK_CUDA(ctx, ctx->node_inst.resize(n_nodes));
+  EOLC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->node_inst.p, 0, sizeof(int) * n_nodes, s));
+  ctx->host_tri.clear();  // downloaded on first use
+  ctx->node_off.assign({0, n_nodes});
+  return reset_after_topology(ctx, s);
+}
+
+eolc_status eolc_topology_arrays(eolc_ctx *ctx, int *rowptr_h, int *colidx_h, int *cptr_h,
+                                 int *contrib_h, int *nf_ptr_h, int *nf_list_h, int sizes[4]) {
+  eolc_status st = need_topology(ctx);
+  if (st != EOLC_OK) return st;
+  if (!sizes) return fail(ctx, EOLC_BAD_ARG, "null sizes");
+  const DevTopology &T = ctx->topo;
+  const int N = T.n_nodes, NB = T.n_blocks;
+  int ncon = 0;
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = stream_of(ctx);
+  EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(&ncon, T.cptr.p + NB, sizeof(int), cudaMemcpyDeviceToHost, s));
+  EOLC_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
+  sizes[0] = N;
+  sizes[1] = NB;
+  sizes[2] = ncon;
+  sizes[3] = 3 * T.n_tri;
+  auto get = [&](int *dst, const int *src, size_t n) -> cudaError_t {
+    return dst ? cudaMemcpyAsync(dst, src, sizeof(int) * n, cudaMemcpyDeviceToHost, s)
+               : cudaSuccess;
+  };
+  EOLC_CHECK_CUDA(ctx, get(rowptr_h, T.rowptr.p, size_t(N) + 1));
+  EOLC_CHECK_CUDA(ctx, get(colidx_h, T.colidx.p, NB));
+  EOLC_CHECK_CUDA(ctx, get(cptr_h, T.cptr.p, size_t(NB) + 1));
+  EOLC_CHECK_CUDA(ctx, get(contrib_h, T.contrib.p, ncon));
+  EOLC_CHECK_CUDA(ctx, get(nf_ptr_h, T.nf_ptr.p, size_t(N) + 1));
+  EOLC_CHECK_CUDA(ctx, get(nf_list_h, T.nf_list.p, size_t(3) * T.n_tri));
   EOLC_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
   return EOLC_OK;
 }
+
 
 eolc_status eolc_bsr_pattern(eolc_ctx *ctx, int *n_blocks, int *rowptr_h,
                              int *colidx_h) {
   eolc_status st = need_topology(ctx);
   if (st != EOLC_OK) return st;
-  if (n_blocks) *n_blocks = ctx->host.n_blocks;
-  if (rowptr_h)
-    std::memcpy(rowptr_h, ctx->host.rowptr.data(), sizeof(int) * ctx->host.rowptr.size());
-  if (colidx_h)
-    std::memcpy(colidx_h, ctx->host.colidx.data(), sizeof(int) * ctx->host.colidx.size());
+  const HostTopology *H = host_topology(ctx);
+  if (!H) return EOLC_CUDA_ERROR;
+  if (n_blocks) *n_blocks = H->n_blocks;
+  if (rowptr_h) std::memcpy(rowptr_h, H->rowptr.data(), sizeof(int) * H->rowptr.size());
+  if (colidx_h) std::memcpy(colidx_h, H->colidx.data(), sizeof(int) * H->colidx.size());
   return EOLC_OK;
 }
 

@@ -913,6 +913,7 @@ extern "C" eolc_status eolc_cd2(eolc_ctx *ctx, const double *x_h,
     // topology-only parts: cloth edges and the perturbation sequence
     // (std::mt19937 seeded 1, uniform_real_distribution(-1, 1), three draws
     // per vertex, :648-659)
+    if (!host_topology(ctx)) return EOLC_CUDA_ERROR;
     W.h_edges = create_edges_host(ctx->host_tri.data(), F);
     CK(W.edges.upload(W.h_edges.data(), W.h_edges.size(), s));
     std::vector<double> rnd(size_t(3) * N);

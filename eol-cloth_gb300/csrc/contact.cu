@@ -312,7 +312,9 @@ eolc_status ineq_solve_device(eolc_ctx *ctx, int n_ineq, const int *ineq_ptr_h,
                               double *lambda_h, eolc_ineq_info *info) {
   if (n_ineq < 0 || (n_ineq > 0 && (!ineq_ptr_h || !ineq_col_h || !ineq_val_h || !bineq_h)))
     return bad(ctx, "null inequality rows");
-  const HostTopology &H = ctx->host;
+  const HostTopology *Hp = host_topology(ctx);
+  if (!Hp) return EOLC_CUDA_ERROR;
+  const HostTopology &H = *Hp;
   const int N = H.n_nodes, n = 3 * N, m = n_ineq;
   // rows grouped by node (first-appearance order), columns checked
   std::vector<int> rnode(size_t(kRowNodes) * std::max(1, m), -1);

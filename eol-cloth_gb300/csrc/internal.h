@@ -51,7 +51,7 @@ __host__ __device__ inline int contrib_code(int elem, bool hinge, int lrow,
   return (elem << 5) | (hinge ? kHingeBit : 0) | (lrow << 2) | lcol;
 }
 
-// ---- topology (host build; topology.cpp) ------------------------------------
+// ---- topology (device build, topology_gpu.cu; host mirror on demand) -------
 struct HostTopology {
   int n_nodes = 0, n_tri = 0, n_hinge = 0, n_blocks = 0;
   std::vector<int> rowptr;   // n_nodes + 1
@@ -63,10 +63,6 @@ struct HostTopology {
   std::vector<int> nf_ptr;   // n_nodes + 1
   std::vector<int> nf_list;  // (face << 2) | local vertex
 };
-
-// Returns an empty string on success, else a message.
-std::string build_topology(int n_nodes, const int *tri, int n_tri,
-                           const int *hinge, int n_hinge, HostTopology &out);
 
 // ---- device state -----------------------------------------------------------
 struct DevTopology {
@@ -80,6 +76,14 @@ struct MaterialD {
   double g[3];
   double h;
 };
+
+// Device build of the same arrays (topology_gpu.cu) from device triangles
+// and hinges; T.tri / T.hinge are not touched.  "" on success.
+struct TopoScratch;
+void free_topo_scratch(TopoScratch *w);
+std::string build_topology_device(TopoScratch *&w, int N, const int *tri_d, int n_tri,
+                                  const int *hinge_d, int n_hinge, DevTopology &T,
+                                  cudaStream_t s, long long &launches);
 
 // Kernel launchers (assemble.cu).  mats/node_inst (both device, may be
 // null): per-instance material table and the instance of every node, used
@@ -200,6 +204,10 @@ std::string learned_forward(eolc_lpc *P, eolc_ctx *ctx, const uint8_t *pinned_d,
 
 // Solve entry points shared by the C ABI functions (api.cu).
 namespace eolc {
+// Host copies of the device topology (and of the triangle list), downloaded
+// on first use after a topology change; nullptr (with ctx->err set) on a
+// CUDA error.
+const HostTopology *host_topology(eolc_ctx *ctx);
 // PcgArgs on the context's buffers (MDK, b, pins, v) for the options.
 PcgArgs default_pcg_args(eolc_ctx *ctx, const eolc_solve_opts *o);
 // The solver dispatch of eolc_velocity_solve on explicit arguments.
@@ -223,7 +231,9 @@ struct eolc_ctx {
   bool own_stream = false;
   std::string err;
   bool has_topology = false;
-  eolc::HostTopology host;
+  bool host_valid = false;     // host mirrors of the device topology are current
+  eolc::HostTopology host;     // read through eolc::host_topology()
+  eolc::TopoScratch *topo_work = nullptr;
   eolc::DevTopology topo;
   // state and per-step buffers
   eolc::DevBuf<double> x, X, v, f, b, A64, Mblk, beq_full;

@@ -983,7 +983,9 @@ eolc_status eolc_lpc_loss_grad(eolc_lpc *P, eolc_ctx *ctx, const int *fixed_dofs
   cudaStream_t s = P->stream;
   cudaStreamSynchronize(ctx->stream);
   const int n = ctx->topo.n_nodes;
-  std::string msg = lpc::use_topology(*P, ctx->host, P->train_blk_row, s);
+  const HostTopology *H = host_topology(ctx);
+  if (!H) { P->err = ctx->err; return EOLC_CUDA_ERROR; }
+  std::string msg = lpc::use_topology(*P, *H, P->train_blk_row, s);
   if (!msg.empty()) { P->err = msg; return EOLC_BAD_ARG; }
   auto mask = pin_mask(n, fixed_dofs_h, n_fixed);
   auto norms = probe_norms(n, mask, probes_h, n_probes);
@@ -1018,13 +1020,15 @@ eolc_status eolc_lpc_add_system(eolc_lpc *P, eolc_ctx *ctx, const int *fixed_dof
   cudaStream_t s = P->stream;
   cudaStreamSynchronize(ctx->stream);
   const int n = ctx->topo.n_nodes, nb = ctx->topo.n_blocks;
+  const HostTopology *H = host_topology(ctx);
+  if (!H) { P->err = ctx->err; return EOLC_CUDA_ERROR; }
   if (!P->has_train_topo) {
-    P->train_topo = ctx->host;
+    P->train_topo = *H;
     P->has_train_topo = true;
-    if (P->train_blk_row.upload(ctx->host.blk_row.data(), nb, s) != cudaSuccess)
+    if (P->train_blk_row.upload(H->blk_row.data(), nb, s) != cudaSuccess)
       return EOLC_CUDA_ERROR;
   } else if (P->train_topo.n_nodes != n || P->train_topo.n_blocks != nb ||
-             P->train_topo.colidx != ctx->host.colidx) {
+             P->train_topo.colidx != H->colidx) {
     P->err = "training systems must share one topology";
     return EOLC_BAD_ARG;
   }
@@ -1135,7 +1139,9 @@ std::string learned_forward(eolc_lpc *P, eolc_ctx *ctx, const uint8_t *pinned_d,
                             const float **G_out, cudaStream_t s) {
   // the first call on a topology builds the graph (host work and uploads on
   // the network's stream, synchronised); later calls only enqueue on s
-  std::string msg = lpc::use_topology(*P, ctx->host, P->train_blk_row, P->stream, false);
+  const HostTopology *H = host_topology(ctx);
+  if (!H) return ctx->err;
+  std::string msg = lpc::use_topology(*P, *H, P->train_blk_row, P->stream, false);
   if (!msg.empty()) return msg;
   msg = lpc::forward_fused(*P, P->G, ctx->topo.blk_row.p, ctx->A32.p, pinned_d, s);
   if (!msg.empty()) return msg;

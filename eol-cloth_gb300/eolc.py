@@ -116,7 +116,7 @@ EXPORTS = ["eolc_version", "eolc_launch_count", "eolc_create", "eolc_destroy", "
            "eolc_batch_autotune", "eolc_set_learned_refresh", "eolc_set_coarse_refresh",
            "eolc_batch_set_jacobi_reference", "eolc_lpc_blocks", "eolc_export_obj",
            "eolc_export_obj_text", "eolc_velocity_solve_ineq", "eolc_contact_rows",
-           "eolc_step_contacts"]
+           "eolc_step_contacts", "eolc_set_topology_device", "eolc_topology_arrays"]
 
 
 def load_library(path=LIB_PATH):
@@ -185,6 +185,9 @@ def load_library(path=LIB_PATH):
     L.eolc_velocity_solve_ineq.argtypes = [_V, _D, _I, _D, ctypes.c_int, ctypes.c_int, _I, _I, _D,
                                            _D, ctypes.POINTER(SolveOpts), _D, _D,
                                            ctypes.POINTER(IneqInfo)]
+    L.eolc_set_topology_device.argtypes = [_V, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                           ctypes.c_void_p, ctypes.c_int]
+    L.eolc_topology_arrays.argtypes = [_V, _I, _I, _I, _I, _I, _I, _I]
     L.eolc_step_contacts.argtypes = [_V, _D, _D, _D, ctypes.POINTER(Material), _D,
                                      ctypes.c_double, _I, _D, ctypes.c_int, ctypes.POINTER(Box),
                                      ctypes.c_int, _D, _D, ctypes.c_int, ctypes.c_double,
@@ -261,6 +264,31 @@ class Context:
         self._check(lib.eolc_set_topology(self._h, n_nodes, _i(tri), len(tri.reshape(-1, 3)),
                                           _i(hinge), len(hinge.reshape(-1, 4))))
         self.n_nodes = n_nodes
+
+    def set_topology_device(self, n_nodes, tri_ptr, n_tri, hinge_ptr, n_hinge):
+        """eolc_set_topology_device: tri / hinge as device addresses (e.g.
+        torch CUDA int32 tensors' data_ptr())."""
+        self._check(lib.eolc_set_topology_device(self._h, n_nodes, ctypes.c_void_p(tri_ptr), n_tri,
+                                                 ctypes.c_void_p(hinge_ptr), n_hinge))
+        self.n_nodes = n_nodes
+
+    def topology_arrays(self):
+        """The device topology: dict of rowptr, colidx, cptr, contrib,
+        nf_ptr, nf_list (eolc_topology_arrays)."""
+        sizes = np.zeros(4, np.int32)
+        self._check(lib.eolc_topology_arrays(self._h, None, None, None, None, None, None,
+                                             _i(sizes)))
+        n, nb, nc, nf = (int(v) for v in sizes)
+        out = dict(rowptr=np.zeros(n + 1, np.int32), colidx=np.zeros(max(1, nb), np.int32),
+                   cptr=np.zeros(nb + 1, np.int32), contrib=np.zeros(max(1, nc), np.int32),
+                   nf_ptr=np.zeros(n + 1, np.int32), nf_list=np.zeros(max(1, nf), np.int32))
+        self._check(lib.eolc_topology_arrays(self._h, _i(out["rowptr"]), _i(out["colidx"]),
+                                             _i(out["cptr"]), _i(out["contrib"]),
+                                             _i(out["nf_ptr"]), _i(out["nf_list"]), _i(sizes)))
+        out["colidx"] = out["colidx"][:nb]
+        out["contrib"] = out["contrib"][:nc]
+        out["nf_list"] = out["nf_list"][:nf]
+        return out
 
     def bsr_pattern(self):
         nb = ctypes.c_int()

@@ -145,6 +145,25 @@ eolc_status eolc_set_topology(eolc_ctx *ctx, int n_nodes, const int *tri_h,
 eolc_status eolc_bsr_pattern(eolc_ctx *ctx, int *n_blocks, int *rowptr_h,
                              int *colidx_h);
 
+/* Topology refresh from device arrays (e.g. a remesher's output kept on the
+ * GPU): same semantics and checks as eolc_set_topology (one instance), the
+ * pattern, contribution lists and node -> face lists built on the device;
+ * host copies are made only when a host-side routine needs them.  Every
+ * eolc_set_topology* call builds on the device. */
+eolc_status eolc_set_topology_device(eolc_ctx *ctx, int n_nodes,
+                                     const int *tri_d, int n_tri,
+                                     const int *hinge_d, int n_hinge);
+/* The device topology for inspection: any array pointer may be NULL.
+ * sizes: n_nodes, n_blocks, contributions, node -> face entries (3 n_tri).
+ * rowptr/colidx: eolc_bsr_pattern's; cptr (n_blocks + 1) and contrib: the
+ * element contributions of every block in the reference's insertion order
+ * (faces ascending, then hinges; code = element << 5 | hinge << 4 |
+ * row vertex << 2 | column vertex); nf_ptr (n_nodes + 1) / nf_list: each
+ * node's faces ascending, code face << 2 | local vertex. */
+eolc_status eolc_topology_arrays(eolc_ctx *ctx, int *rowptr_h, int *colidx_h,
+                                 int *cptr_h, int *contrib_h, int *nf_ptr_h,
+                                 int *nf_list_h, int sizes[4]);
+
 /* ---- Forces::fill (Forces.cpp:912-930, non-EOL branches) ----------------
  * Computes f (3N), M and MDK (BSR values, n_blocks*9 each) for positions
  * x_h and material coordinates X_h.  Any output pointer may be NULL.

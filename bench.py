@@ -544,8 +544,8 @@ def run_refresh(args, local_rank, stream, sc, reps=3):
                     "plan_ms": round(med(first) - med(steady), 3)}
     out["note"] = ("set_topology: BSR pattern, contribution lists and node-face lists built "
                    "on the GPU (the former host build took 536 ms); plan_ms: the solver's "
-                   "per-topology plan (patch partition and shared-memory image layout, or "
-                   "the streamed tiling), still built on the host at the first step")
+                   "per-topology plan (patch partition and shared-memory image layout on "
+                   "host threads, or the streamed tiling), built at the first step")
     return out
 
 

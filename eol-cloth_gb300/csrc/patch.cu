@@ -55,6 +55,7 @@
 #include <functional>
 #include <cmath>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "cg_common.cuh"
@@ -1589,6 +1590,29 @@ struct Bisector {
     split(a, pl, out, bounds);
     split(b, pr, out, bounds);
   }
+
+  // split() with the two halves of the top `depth` levels on separate host
+  // threads; same result.  Only the coordinate bisection (it reads X alone)
+  // runs in parallel; the BFS variant shares `mark`.
+  void split_par(const std::vector<int> &set, int parts, std::vector<int> &out,
+                 std::vector<int> &bounds, int depth) {
+    if (depth <= 0 || !X || parts <= 1 || set.empty()) {
+      split(set, parts, out, bounds);
+      return;
+    }
+    std::vector<int> order;
+    coord_order(set, order);
+    const int pl = parts / 2, pr = parts - pl;
+    const size_t cut = size_t((long long)order.size() * pl / parts);
+    std::vector<int> a(order.begin(), order.begin() + cut), b(order.begin() + cut, order.end());
+    std::vector<int> ob, bb;
+    std::thread right([&] { split_par(b, pr, ob, bb, depth - 1); });
+    split_par(a, pl, out, bounds, depth - 1);
+    right.join();
+    const int base = int(out.size());
+    out.insert(out.end(), ob.begin(), ob.end());
+    for (int x : bb) bounds.push_back(base + x);
+  }
 };
 
 }  // namespace
@@ -1611,14 +1635,41 @@ struct PatchPlan {
   std::vector<int> slice_off, slice_len;  // per (patch, warp)
 };
 
+// Runs f(lo, hi, t) on n_threads host threads over contiguous pieces of
+// [0, n) (inline when n_threads <= 1).
+template <typename F>
+void parallel_ranges(int n, int n_threads, F f) {
+  if (n_threads <= 1 || n < 2) {
+    f(0, n, 0);
+    return;
+  }
+  const int per = (n + n_threads - 1) / n_threads;
+  std::vector<std::thread> th;
+  for (int t = 0; t < n_threads; ++t) {
+    const int lo = t * per, hi = std::min(n, lo + per);
+    if (lo < hi) th.emplace_back(f, lo, hi, t);
+  }
+  for (std::thread &x : th) x.join();
+}
+
+int plan_threads(int n_threads) {
+  if (n_threads > 0) return n_threads;
+  const int hw = int(std::thread::hardware_concurrency());
+  return std::max(1, std::min(16, hw));
+}
+
 // Host plan of the resident solvers for a BSR pattern: permutation, permuted
 // pattern with source and transpose blocks, patch boundaries and the per-row
 // upper / transposed / halo lists.  X (optional): 2 material coordinates per
 // node, which give compact patches on any mesh.  Returns "" or the reason
 // the mesh does not fit the shared-memory image.
+// n_threads: host threads (0: the machine's, up to 16).  The plan does not
+// depend on it: every piece is computed independently and concatenated in
+// order, and the error reported is the first in serial order.
 std::string build_patch_plan(int N, const std::vector<int> &rowptr,
                              const std::vector<int> &colidx, const std::vector<double> *X,
-                             int n_sm, PatchPlan &out) {
+                             int n_sm, PatchPlan &out, int n_threads = 0) {
+  const int T = plan_threads(n_threads);
   const int NB = int(colidx.size());
   const int G = std::max(1, (N + kTargetRows - 1) / kTargetRows);
   if (G > n_sm || G > 32 * kPartPerLane)
@@ -1627,35 +1678,52 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
   for (int k = 0; k < N; ++k) all[k] = k;
   perm.reserve(N);
   Bisector bis(rowptr, colidx, X);
-  bis.split(all, G, perm, bounds);
+  int depth = 0;
+  while ((1 << depth) < T) ++depth;
+  bis.split_par(all, G, perm, bounds, depth);
   if (int(perm.size()) != N || int(bounds.size()) != G) return "patch partition failed";
   std::vector<int> iperm(N);
   for (int k = 0; k < N; ++k) iperm[perm[k]] = k;
   // permuted pattern, source blocks, transposes, diagonals
   std::vector<int> prow(N + 1, 0), pcol(NB), psrc(NB), ptr(NB), pdiag(N, -1);
   for (int i = 0; i < N; ++i) prow[i + 1] = prow[i] + rowptr[perm[i] + 1] - rowptr[perm[i]];
-  std::vector<std::pair<int, int>> tmp;
-  for (int i = 0; i < N; ++i) {
-    const int o = perm[i];
-    tmp.clear();
-    for (int k = rowptr[o]; k < rowptr[o + 1]; ++k) tmp.push_back({iperm[colidx[k]], k});
-    std::sort(tmp.begin(), tmp.end());
-    for (size_t q = 0; q < tmp.size(); ++q) {
-      pcol[prow[i] + q] = tmp[q].first;
-      psrc[prow[i] + q] = tmp[q].second;
-      if (tmp[q].first == i) pdiag[i] = prow[i] + int(q);
+  parallel_ranges(N, T, [&](int lo, int hi, int) {
+    std::vector<std::pair<int, int>> tmp;
+    for (int i = lo; i < hi; ++i) {
+      const int o = perm[i];
+      tmp.clear();
+      for (int k = rowptr[o]; k < rowptr[o + 1]; ++k) tmp.push_back({iperm[colidx[k]], k});
+      std::sort(tmp.begin(), tmp.end());
+      for (size_t q = 0; q < tmp.size(); ++q) {
+        pcol[prow[i] + q] = tmp[q].first;
+        psrc[prow[i] + q] = tmp[q].second;
+        if (tmp[q].first == i) pdiag[i] = prow[i] + int(q);
+      }
     }
-  }
-  for (int i = 0; i < N; ++i) {
-    if (pdiag[i] < 0) return "a row without its diagonal block";
-    for (int k = prow[i]; k < prow[i + 1]; ++k) {
-      const int j = pcol[k];
-      const int *b = pcol.data() + prow[j], *e = pcol.data() + prow[j + 1];
-      const int *f = std::lower_bound(b, e, i);
-      if (f == e || *f != i) return "matrix pattern is not symmetric";
-      ptr[k] = int(f - pcol.data());
+  });
+  // first failing row in order: 1 = no diagonal block, 2 = not symmetric
+  std::vector<std::pair<int, int>> bad(T, {N, 0});
+  parallel_ranges(N, T, [&](int lo, int hi, int t) {
+    for (int i = lo; i < hi; ++i) {
+      if (pdiag[i] < 0) {
+        bad[t] = {i, 1};
+        return;
+      }
+      for (int k = prow[i]; k < prow[i + 1]; ++k) {
+        const int j = pcol[k];
+        const int *b = pcol.data() + prow[j], *e = pcol.data() + prow[j + 1];
+        const int *f = std::lower_bound(b, e, i);
+        if (f == e || *f != i) {
+          bad[t] = {i, 2};
+          return;
+        }
+        ptr[k] = int(f - pcol.data());
+      }
     }
-  }
+  });
+  const std::pair<int, int> first = *std::min_element(bad.begin(), bad.end());
+  if (first.second == 1) return "a row without its diagonal block";
+  if (first.second == 2) return "matrix pattern is not symmetric";
   std::vector<int> patch_row(G + 1, 0);
   for (int c = 0; c < G; ++c) patch_row[c + 1] = bounds[c];
   // shared-memory image of every patch: forward records and slots, both
@@ -1664,81 +1732,116 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
   std::vector<int> fptr(G + 1, 0), fblk, rcnt(N, 0), wbase(size_t(G) * kWarps * 2, 0),
       hnptr(G + 1, 0), hnode;
   std::vector<unsigned> fword;
-  std::vector<int> win(N, -1);  // window slot of an outside node (global index)
   std::vector<int16_t> bmap(NB, 0);
-  for (int c = 0; c < G; ++c) {
-    const int r0 = patch_row[c], r1 = patch_row[c + 1], np = r1 - r0;
-    if (np > kMaxRows) return "patch too large";
-    const int nbase = int(hnode.size());
-    // per row: forward entries (block, column) internal then halo; transposed
-    // entries (column j < row, ascending)
-    std::vector<std::vector<std::pair<int, int>>> fw(np);
-    std::vector<std::vector<int>> tcol(np);
-    std::vector<int> fi(np, 0);
-    for (int i = r0; i < r1; ++i) {
-      const int l = i - r0;
-      for (int k = prow[i]; k < prow[i + 1]; ++k) {
-        const int j = pcol[k];
-        if (j > i && j < r1) fw[l].push_back({k, j - r0});
-        if (j >= r0 && j < i) tcol[l].push_back(j - r0);
+  // each patch's halo nodes and records, built independently (rows, blocks
+  // and warp bases of different patches are disjoint), then concatenated
+  struct Image {
+    std::vector<int> hnode, fblk;
+    std::vector<unsigned> fword;
+    std::string err;
+  };
+  std::vector<Image> img(G);
+  parallel_ranges(G, T, [&](int c_lo, int c_hi, int) {
+    std::vector<int> seen(N, -1), hidx(N, 0);  // halo index of an outside node, per patch
+    for (int c = c_lo; c < c_hi; ++c) {
+      Image &I = img[c];
+      const int r0 = patch_row[c], r1 = patch_row[c + 1], np = r1 - r0;
+      if (np > kMaxRows) {
+        I.err = "patch too large";
+        continue;
       }
-      fi[l] = int(fw[l].size());
-      for (int k = prow[i]; k < prow[i + 1]; ++k) {
-        const int j = pcol[k];
-        if (j >= r0 && j < r1) {
-          bmap[k] = int16_t(j - r0);
-          continue;
+      // per row: forward entries (block, column) internal then halo;
+      // transposed entries (column j < row, ascending)
+      std::vector<std::vector<std::pair<int, int>>> fw(np);
+      std::vector<std::vector<int>> tcol(np);
+      std::vector<int> fi(np, 0);
+      for (int i = r0; i < r1 && I.err.empty(); ++i) {
+        const int l = i - r0;
+        for (int k = prow[i]; k < prow[i + 1]; ++k) {
+          const int j = pcol[k];
+          if (j > i && j < r1) fw[l].push_back({k, j - r0});
+          if (j >= r0 && j < i) tcol[l].push_back(j - r0);
         }
-        if (win[j] < nbase) {  // first time this patch sees node j
-          win[j] = int(hnode.size());
-          hnode.push_back(j);
-        }
-        fw[l].push_back({k, kMaxRows + (win[j] - nbase)});
-        bmap[k] = int16_t(-1 - (win[j] - nbase));
-      }
-      if (int(fw[l].size()) > kMaxCount || int(tcol[l].size()) > kMaxCount)
-        return "patch exceeds the shared-memory image";
-      rcnt[i] = fi[l] | (int(fw[l].size()) << 8) | (int(tcol[l].size()) << 16);
-    }
-    if (int(hnode.size()) - nbase > kMaxHaloNodes) return "patch exceeds the shared-memory image";
-    hnptr[c + 1] = int(hnode.size());
-    // slot positions
-    std::vector<std::vector<int>> spos(np);
-    int nslot = 0;
-    for (int w = 0; w < kWarps; ++w) {
-      const int l0 = 32 * w, l1 = std::min(np, l0 + 32);
-      wbase[(size_t(c) * kWarps + w) * 2 + 1] = nslot;
-      int kmax = 0;
-      for (int l = l0; l < l1; ++l) kmax = std::max(kmax, int(tcol[l].size()));
-      for (int k = 0; k < kmax; ++k)
-        for (int l = l0; l < l1; ++l)
-          if (k < int(tcol[l].size())) spos[l].push_back(nslot++);
-    }
-    // forward records
-    int nrec = 0;
-    for (int w = 0; w < kWarps; ++w) {
-      const int l0 = 32 * w, l1 = std::min(np, l0 + 32);
-      wbase[(size_t(c) * kWarps + w) * 2] = nrec;
-      int kmax = 0;
-      for (int l = l0; l < l1; ++l) kmax = std::max(kmax, int(fw[l].size()));
-      for (int k = 0; k < kmax; ++k)
-        for (int l = l0; l < l1; ++l) {
-          if (k >= int(fw[l].size())) continue;
-          const int col = fw[l][k].second;
-          unsigned slot = 0xffffu;
-          if (col < kMaxRows) {  // upper block (l, col): the transposed entry of row col
-            const std::vector<int> &tc = tcol[col];
-            const int t = int(std::lower_bound(tc.begin(), tc.end(), l) - tc.begin());
-            if (t == int(tc.size()) || tc[t] != l) return "patch transpose lists disagree";
-            slot = unsigned(spos[col][t]);
+        fi[l] = int(fw[l].size());
+        for (int k = prow[i]; k < prow[i + 1]; ++k) {
+          const int j = pcol[k];
+          if (j >= r0 && j < r1) {
+            bmap[k] = int16_t(j - r0);
+            continue;
           }
-          fblk.push_back(fw[l][k].first);
-          fword.push_back(unsigned(col) | (slot << 16));
-          ++nrec;
+          if (seen[j] != c) {  // first time this patch sees node j
+            seen[j] = c;
+            hidx[j] = int(I.hnode.size());
+            I.hnode.push_back(j);
+          }
+          fw[l].push_back({k, kMaxRows + hidx[j]});
+          bmap[k] = int16_t(-1 - hidx[j]);
         }
+        if (int(fw[l].size()) > kMaxCount || int(tcol[l].size()) > kMaxCount) {
+          I.err = "patch exceeds the shared-memory image";
+          break;
+        }
+        rcnt[i] = fi[l] | (int(fw[l].size()) << 8) | (int(tcol[l].size()) << 16);
+      }
+      if (!I.err.empty()) continue;
+      if (int(I.hnode.size()) > kMaxHaloNodes) {
+        I.err = "patch exceeds the shared-memory image";
+        continue;
+      }
+      // slot positions
+      std::vector<std::vector<int>> spos(np);
+      int nslot = 0;
+      for (int w = 0; w < kWarps; ++w) {
+        const int l0 = 32 * w, l1 = std::min(np, l0 + 32);
+        wbase[(size_t(c) * kWarps + w) * 2 + 1] = nslot;
+        int kmax = 0;
+        for (int l = l0; l < l1; ++l) kmax = std::max(kmax, int(tcol[l].size()));
+        for (int k = 0; k < kmax; ++k)
+          for (int l = l0; l < l1; ++l)
+            if (k < int(tcol[l].size())) spos[l].push_back(nslot++);
+      }
+      // forward records
+      int nrec = 0;
+      for (int w = 0; w < kWarps && I.err.empty(); ++w) {
+        const int l0 = 32 * w, l1 = std::min(np, l0 + 32);
+        wbase[(size_t(c) * kWarps + w) * 2] = nrec;
+        int kmax = 0;
+        for (int l = l0; l < l1; ++l) kmax = std::max(kmax, int(fw[l].size()));
+        for (int k = 0; k < kmax && I.err.empty(); ++k)
+          for (int l = l0; l < l1; ++l) {
+            if (k >= int(fw[l].size())) continue;
+            const int col = fw[l][k].second;
+            unsigned slot = 0xffffu;
+            if (col < kMaxRows) {  // upper block (l, col): the transposed entry of row col
+              const std::vector<int> &tc = tcol[col];
+              const int t = int(std::lower_bound(tc.begin(), tc.end(), l) - tc.begin());
+              if (t == int(tc.size()) || tc[t] != l) {
+                I.err = "patch transpose lists disagree";
+                break;
+              }
+              slot = unsigned(spos[col][t]);
+            }
+            I.fblk.push_back(fw[l][k].first);
+            I.fword.push_back(unsigned(col) | (slot << 16));
+            ++nrec;
+          }
+      }
+      if (I.err.empty() && (nrec > kMaxFwd || nslot > kMaxSlots))
+        I.err = "patch exceeds the shared-memory image";
     }
-    if (nrec > kMaxFwd || nslot > kMaxSlots) return "patch exceeds the shared-memory image";
-    fptr[c + 1] = fptr[c] + nrec;
+  });
+  for (int c = 0; c < G; ++c) {
+    if (!img[c].err.empty()) return img[c].err;
+    hnptr[c + 1] = hnptr[c] + int(img[c].hnode.size());
+    fptr[c + 1] = fptr[c] + int(img[c].fblk.size());
+  }
+  hnode.reserve(hnptr[G]);
+  fblk.reserve(fptr[G]);
+  fword.reserve(fptr[G]);
+  for (int c = 0; c < G; ++c) {
+    hnode.insert(hnode.end(), img[c].hnode.begin(), img[c].hnode.end());
+    fblk.insert(fblk.end(), img[c].fblk.begin(), img[c].fblk.end());
+    fword.insert(fword.end(), img[c].fword.begin(), img[c].fword.end());
   }
   for (int j : hnode) rcnt[j] |= 1 << 24;  // a halo node of some patch: it publishes
   // coarse aggregates: recursive coordinate bisection of the patch centroids
@@ -1832,19 +1935,24 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
   // warp slices of the pattern (for the learned G)
   out.slice_off.assign(size_t(G) * kWarps, 0);
   out.slice_len.assign(size_t(G) * kWarps, 0);
+  parallel_ranges(G, T, [&](int c_lo, int c_hi, int) {
+    for (int c = c_lo; c < c_hi; ++c)
+      for (int w = 0; w < kWarps; ++w) {
+        const int r0 = out.patch_row[c] + 32 * w, r1 = std::min(out.patch_row[c + 1], r0 + 32);
+        int len = 0;
+        for (int i = r0; i < r1; ++i) len = std::max(len, out.rowptr[i + 1] - out.rowptr[i]);
+        out.slice_len[size_t(c) * kWarps + w] = len;
+      }
+  });
   int slots = 0;
-  for (int c = 0; c < G; ++c)
-    for (int w = 0; w < kWarps; ++w) {
-      const int r0 = out.patch_row[c] + 32 * w, r1 = std::min(out.patch_row[c + 1], r0 + 32);
-      int len = 0;
-      for (int i = r0; i < r1; ++i) len = std::max(len, out.rowptr[i + 1] - out.rowptr[i]);
-      out.slice_off[size_t(c) * kWarps + w] = slots;
-      out.slice_len[size_t(c) * kWarps + w] = len;
-      slots += len;
-    }
+  for (size_t q = 0; q < out.slice_len.size(); ++q) {
+    out.slice_off[q] = slots;
+    slots += out.slice_len[q];
+  }
   out.bsl.assign(size_t(slots) * 32, 0);
   out.gsrc.assign(size_t(slots) * 32, -1);
-  for (int c = 0; c < G; ++c)
+  parallel_ranges(G, T, [&](int c_lo, int c_hi, int) {
+  for (int c = c_lo; c < c_hi; ++c)
     for (int w = 0; w < kWarps; ++w) {
       const int r0 = out.patch_row[c] + 32 * w, r1 = std::min(out.patch_row[c + 1], r0 + 32);
       const int off = out.slice_off[size_t(c) * kWarps + w];
@@ -1855,6 +1963,7 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
           out.gsrc[q] = out.src[k];
         }
     }
+  });
   return "";
 }
 

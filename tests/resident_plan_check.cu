@@ -28,13 +28,27 @@ int main(int argc, char **argv) {
     return 2;
   fclose(f);
   using namespace eolc;
-  PatchPlan L;
+  PatchPlan L, L1;
   const std::string why = build_patch_plan(N, rowptr, colidx, &X, 152, L);
   if (!why.empty()) {
     printf("misfit: %s\n", why.c_str());
     return 3;
   }
   long bad = 0;
+  // the threaded build equals the single-threaded one, array for array
+  if (!build_patch_plan(N, rowptr, colidx, &X, 152, L1, 1).empty()) ++bad;
+  const bool same =
+      L.G == L1.G && L.perm == L1.perm && L.rowptr == L1.rowptr && L.colidx == L1.colidx &&
+      L.src == L1.src && L.tr == L1.tr && L.diag == L1.diag && L.patch_row == L1.patch_row &&
+      L.hnptr == L1.hnptr && L.hnode == L1.hnode && L.fptr == L1.fptr && L.fblk == L1.fblk &&
+      L.rcnt == L1.rcnt && L.wbase == L1.wbase && L.fword == L1.fword &&
+      L.n_agg == L1.n_agg && L.patch_agg == L1.patch_agg && L.hagg == L1.hagg &&
+      L.ctgt == L1.ctgt && L.cl_ptr == L1.cl_ptr && L.cl_idx == L1.cl_idx && L.bsl == L1.bsl &&
+      L.gsrc == L1.gsrc && L.slice_off == L1.slice_off && L.slice_len == L1.slice_len;
+  if (!same) {
+    printf("threaded plan differs from the single-threaded plan\n");
+    ++bad;
+  }
   int max_rec = 0, max_slot = 0;
   std::vector<int> patch_of(N);
   for (int c = 0; c < L.G; ++c)

@@ -1,7 +1,8 @@
 """Resident solvers' plan on the CPU: build_patch_plan (csrc/patch.cu) run on
 real meshes by a host program (resident_plan_check.cu) that replays the
 device's warp-compacted record / slot arithmetic and checks the image and
-coarse-space invariants.  No GPU: the program only runs host code."""
+coarse-space invariants, and that the plan built on several host threads
+equals the single-threaded one.  No GPU: the program only runs host code."""
 import os
 import shutil
 import subprocess

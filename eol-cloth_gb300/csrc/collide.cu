@@ -825,35 +825,9 @@ __global__ void copy_best_kernel(int n, const int *best, int *info) {
   if (i < n) info[i] = best[i];
 }
 
-// createEdges (:141-231), topology part: 32-bit wrapped hash
-// kmin + (3 nf + 1) kmax, stable sort, twins paired.  Output per edge:
-// (verts(0), verts(1), face0, face1 or -1).
-std::vector<int4> create_edges_host(const int *tri, int nf) {
-  struct FE { int v0, v1, face; int32_t hash; };
-  int n = 3 * nf;
-  std::vector<FE> tmp(n);
-  for (int k = 0; k < nf; ++k)
-    for (int i = 0; i < 3; ++i) {
-      int a = tri[3 * k + i], b = tri[3 * k + (i + 1) % 3];
-      uint32_t kmin = uint32_t(std::min(a, b) + 1), kmax = uint32_t(std::max(a, b) + 1);
-      tmp[3 * k + i] = FE{a, b, k, int32_t(kmin + uint32_t(n + 1) * kmax)};
-    }
-  std::stable_sort(tmp.begin(), tmp.end(),
-                   [](const FE &x, const FE &y) { return x.hash < y.hash; });
-  std::vector<int4> out;
-  out.reserve(n / 2 + 16);
-  int k = 0;
-  while (k < n) {
-    if (k < n - 1 && tmp[k].hash == tmp[k + 1].hash) {
-      out.push_back(make_int4(tmp[k].v0, tmp[k].v1, tmp[k].face, tmp[k + 1].face));
-      k += 2;
-    } else {
-      out.push_back(make_int4(tmp[k].v0, tmp[k].v1, tmp[k].face, -1));
-      k += 1;
-    }
-  }
-  return out;
-}
+// createEdges (:141-231), topology part, is built on the device by
+// build_edges_device (topology_gpu.cu): per edge (verts(0), verts(1), face0,
+// face1 or -1) in the reference's order.
 
 }  // namespace
 
@@ -861,8 +835,8 @@ std::vector<int4> create_edges_host(const int *tri, int nf) {
 namespace eolc {
 
 struct CollideWork {
-  int n_nodes = -1, n_tri = -1;
-  std::vector<int4> h_edges;
+  int n_nodes = -1, n_tri = -1, n_edges = 0;
+  EdgeScratch *es = nullptr;  // scratch of the device edge-list build
   DevBuf<int4> edges;
   DevBuf<double> rnd, x, v2, fn2, fn0, aabb_part, aabb, qpos, qnor, part_d;
   DevBuf<int> part_j, best_q, info, bsum, boff, off, scalars;
@@ -870,7 +844,10 @@ struct CollideWork {
   DevBuf<eolc_contact> out;
 };
 
-void free_collide_work(CollideWork *w) { delete w; }
+void free_collide_work(CollideWork *w) {
+  if (w) free_edge_scratch(w->es);
+  delete w;
+}
 
 }  // namespace eolc
 
@@ -913,9 +890,12 @@ extern "C" eolc_status eolc_cd2(eolc_ctx *ctx, const double *x_h,
     // topology-only parts: cloth edges and the perturbation sequence
     // (std::mt19937 seeded 1, uniform_real_distribution(-1, 1), three draws
     // per vertex, :648-659)
-    if (!host_topology(ctx)) return EOLC_CUDA_ERROR;
-    W.h_edges = create_edges_host(ctx->host_tri.data(), F);
-    CK(W.edges.upload(W.h_edges.data(), W.h_edges.size(), s));
+    const std::string emsg = build_edges_device(W.es, ctx->topo.tri.p, F, W.edges, W.n_edges, s,
+                                                ctx->launches);
+    if (!emsg.empty()) {
+      ctx->err = emsg;
+      return EOLC_CUDA_ERROR;
+    }
     std::vector<double> rnd(size_t(3) * N);
     std::mt19937 gen;
     std::uniform_real_distribution<> dis(-1.0, 1.0);
@@ -926,7 +906,7 @@ extern "C" eolc_status eolc_cd2(eolc_ctx *ctx, const double *x_h,
     W.n_nodes = N;
     W.n_tri = F;
   }
-  const int E = int(W.h_edges.size());
+  const int E = W.n_edges;
   // host box data
   std::vector<BoxDev> hb(std::max(1, n_boxes));
   for (int b = 0; b < n_boxes; ++b) {
@@ -1040,6 +1020,33 @@ extern "C" eolc_status eolc_cd2(eolc_ctx *ctx, const double *x_h,
   if (sc[0] > capacity) {
     ctx->err = "contact buffer too small";
     return EOLC_CAPACITY;
+  }
+  return EOLC_OK;
+}
+
+extern "C" eolc_status eolc_edge_list(eolc_ctx *ctx, int *edges_h, int capacity, int *n_edges) {
+  if (!ctx) return EOLC_BAD_ARG;
+  if (!ctx->has_topology) { ctx->err = "no topology set"; return EOLC_NO_TOPOLOGY; }
+  if (!n_edges || capacity < 0 || (capacity > 0 && !edges_h)) {
+    ctx->err = "bad edge-list arguments";
+    return EOLC_BAD_ARG;
+  }
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = ctx->stream;
+  if (!ctx->cd_work) ctx->cd_work = new CollideWork();
+  CollideWork &W = *ctx->cd_work;
+  if (W.n_tri != ctx->topo.n_tri) {
+    const std::string msg = build_edges_device(W.es, ctx->topo.tri.p, ctx->topo.n_tri, W.edges,
+                                               W.n_edges, s, ctx->launches);
+    if (!msg.empty()) { ctx->err = msg; return EOLC_CUDA_ERROR; }
+  }
+  *n_edges = W.n_edges;
+  if (capacity < W.n_edges) { ctx->err = "edge list capacity too small"; return EOLC_CAPACITY; }
+  if (W.n_edges > 0) {
+    cudaError_t e = cudaMemcpyAsync(edges_h, W.edges.p, sizeof(int4) * W.n_edges,
+                                    cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); return EOLC_CUDA_ERROR; }
   }
   return EOLC_OK;
 }

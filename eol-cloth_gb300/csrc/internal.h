@@ -85,6 +85,14 @@ std::string build_topology_device(TopoScratch *&w, int N, const int *tri_d, int 
                                   const int *hinge_d, int n_hinge, DevTopology &T,
                                   cudaStream_t s, long long &launches);
 
+// CD2's edge list (createEdges, boxTriCollision.cpp:141-231) built on the
+// device (topology_gpu.cu): per edge (v0, v1, face, twin face or -1) in the
+// reference's order; n_edges gets the count.  "" on success.
+struct EdgeScratch;
+void free_edge_scratch(EdgeScratch *w);
+std::string build_edges_device(EdgeScratch *&w, const int *tri_d, int nf, DevBuf<int4> &edges,
+                               int &n_edges, cudaStream_t s, long long &launches);
+
 // Kernel launchers (assemble.cu).  mats/node_inst (both device, may be
 // null): per-instance material table and the instance of every node, used
 // instead of m for batched topologies.

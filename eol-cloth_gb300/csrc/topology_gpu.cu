@@ -230,6 +230,106 @@ topo_row_kernel(int N, int pass, const int *__restrict__ tri, const int *__restr
 
 int grid(long long n) { return int((n + kT - 1) / kT); }
 
+// ---- CD2's edge list (createEdges, boxTriCollision.cpp:141-231) ------------
+// Record k = 3 f + i is edge i of face f (vertices i, i+1, other i+2) with
+// hash kmin + (n + 1) kmax in 32-bit two's complement (n = 3 nf, vertex ids
+// + 1), as the reference's int arithmetic gives on its targets.  The records
+// are stably sorted by hash (stable LSD radix sort, 4-bit digits, on the
+// hash with its sign bit flipped), then neighbours with equal hashes pair
+// greedily from the left: within a run of equal hashes, positions 0-1, 2-3,
+// ... are internal edges and an odd last one is a boundary edge.
+constexpr int kRadixItems = 8;                    // keys per thread, blocked
+constexpr int kRadixTile = kT * kRadixItems;      // keys per CTA
+
+__global__ void edge_keys_kernel(const int *__restrict__ tri, int nf, unsigned *key, int *val) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = 3 * nf;
+  if (k >= n) return;
+  const int f = k / 3, i = k % 3;
+  const int a = tri[3 * f + i], b = tri[3 * f + (i + 1) % 3];
+  const unsigned kmin = unsigned(min(a, b) + 1), kmax = unsigned(max(a, b) + 1);
+  const unsigned hash = kmin + unsigned(n + 1) * kmax;  // wraps like the int expression
+  key[k] = hash ^ 0x80000000u;                          // signed order as unsigned order
+  val[k] = k;
+}
+
+// digit counts per CTA, digit-major: hist[d * nblk + block]
+__global__ void radix_hist_kernel(const unsigned *__restrict__ key, int n, int shift,
+                                  int *__restrict__ hist) {
+  __shared__ int cnt[16];
+  if (threadIdx.x < 16) cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const int base = blockIdx.x * kRadixTile + threadIdx.x * kRadixItems;
+  for (int q = 0; q < kRadixItems; ++q)
+    if (base + q < n) atomicAdd(&cnt[(key[base + q] >> shift) & 15], 1);
+  __syncthreads();
+  if (threadIdx.x < 16) hist[threadIdx.x * gridDim.x + blockIdx.x] = cnt[threadIdx.x];
+}
+
+// stable scatter: a thread's keys are consecutive, so a key's place is the
+// CTA's offset for its digit + the counts of that digit in earlier threads +
+// the count earlier in the same thread
+__global__ void __launch_bounds__(kT)
+radix_scatter_kernel(const unsigned *__restrict__ key, const int *__restrict__ val, int n,
+                     int shift, const int *__restrict__ off, unsigned *__restrict__ key_out,
+                     int *__restrict__ val_out) {
+  __shared__ int sh[kT / 32];
+  __shared__ int pre[16][kT];
+  const int base = blockIdx.x * kRadixTile + threadIdx.x * kRadixItems;
+  unsigned kk[kRadixItems];
+  int cnt[16];
+  for (int d = 0; d < 16; ++d) cnt[d] = 0;
+  for (int q = 0; q < kRadixItems; ++q) {
+    kk[q] = base + q < n ? key[base + q] : 0u;
+    if (base + q < n) ++cnt[(kk[q] >> shift) & 15];
+  }
+  for (int d = 0; d < 16; ++d) {
+    const int inc = block_scan_incl(cnt[d], sh);
+    pre[d][threadIdx.x] = inc - cnt[d];
+    __syncthreads();
+  }
+  for (int d = 0; d < 16; ++d) cnt[d] = 0;
+  for (int q = 0; q < kRadixItems; ++q) {
+    if (base + q >= n) break;
+    const int d = (kk[q] >> shift) & 15;
+    const int pos = off[d * gridDim.x + blockIdx.x] + pre[d][threadIdx.x] + cnt[d]++;
+    key_out[pos] = kk[q];
+    val_out[pos] = val[base + q];
+  }
+}
+
+__global__ void edge_flag_kernel(const unsigned *__restrict__ key, int n, int *flag) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) flag[k] = (k == 0 || key[k] != key[k - 1]) ? 1 : 0;
+}
+
+// run r of equal hashes starts at start[r]; rid = exclusive scan of flags
+__global__ void edge_start_kernel(const int *__restrict__ flag, const int *__restrict__ rid,
+                                  int n, int *start) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n && flag[k]) start[rid[k]] = k;
+}
+
+// an edge starts at every even position of a run
+__global__ void edge_emit_kernel(const int *__restrict__ flag, const int *__restrict__ rid,
+                                 const int *__restrict__ start, int n, int *emit) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int r = rid[k] + flag[k] - 1;
+  emit[k] = ((k - start[r]) & 1) == 0 ? 1 : 0;
+}
+
+// (v0, v1, face, twin face or -1) in the sorted order
+__global__ void edge_write_kernel(const int *__restrict__ tri, const unsigned *__restrict__ key,
+                                  const int *__restrict__ val, const int *__restrict__ emit,
+                                  const int *__restrict__ eoff, int n, int4 *edges) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n || !emit[k]) return;
+  const int rec = val[k], f = rec / 3, i = rec % 3;
+  const int twin = (k + 1 < n && key[k + 1] == key[k]) ? val[k + 1] / 3 : -1;
+  edges[eoff[k]] = make_int4(tri[3 * f + i], tri[3 * f + (i + 1) % 3], f, twin);
+}
+
 }  // namespace
 
 struct TopoScratch {
@@ -328,6 +428,68 @@ std::string build_topology_device(TopoScratch *&w, int N, const int *tri_d, int 
   T.n_hinge = n_hinge;
   T.n_blocks = nblk;
 #undef TG
+  return "";
+}
+
+}  // namespace eolc
+
+namespace eolc {
+
+struct EdgeScratch {
+  DevBuf<unsigned> key[2];
+  DevBuf<int> val[2], hist, off, flag, rid, start, emit, eoff, bsum;
+};
+
+void free_edge_scratch(EdgeScratch *w) { delete w; }
+
+std::string build_edges_device(EdgeScratch *&w, const int *tri_d, int nf, DevBuf<int4> &edges,
+                               int &n_edges, cudaStream_t s, long long &launches) {
+  if (nf <= 0 || int64_t(nf) * 3 >= (int64_t(1) << 30)) return "bad face count";
+  if (!w) w = new EdgeScratch();
+  EdgeScratch &W = *w;
+#define EG(expr)                                                                    \
+  do {                                                                              \
+    cudaError_t e_ = (expr);                                                        \
+    if (e_ != cudaSuccess) return std::string(#expr ": ") + cudaGetErrorString(e_); \
+  } while (0)
+  const int n = 3 * nf;
+  const int nblk = (n + kRadixTile - 1) / kRadixTile;
+  for (int b = 0; b < 2; ++b) {
+    EG(W.key[b].resize(n));
+    EG(W.val[b].resize(n));
+  }
+  EG(W.hist.resize(size_t(16) * nblk));
+  EG(W.off.resize(size_t(16) * nblk + 1));
+  EG(W.flag.resize(n));
+  EG(W.rid.resize(size_t(n) + 1));
+  EG(W.start.resize(n));
+  EG(W.emit.resize(n));
+  EG(W.eoff.resize(size_t(n) + 1));
+  EG(W.bsum.resize(size_t(grid(std::max(n, 16 * nblk) + 1)) + 1));
+  edge_keys_kernel<<<grid(n), kT, 0, s>>>(tri_d, nf, W.key[0].p, W.val[0].p);
+  int cur = 0;
+  for (int shift = 0; shift < 32; shift += 4) {
+    radix_hist_kernel<<<nblk, kT, 0, s>>>(W.key[cur].p, n, shift, W.hist.p);
+    scan(W.hist.p, 16 * nblk, W.off.p, W.bsum, s);
+    radix_scatter_kernel<<<nblk, kT, 0, s>>>(W.key[cur].p, W.val[cur].p, n, shift, W.off.p,
+                                             W.key[1 - cur].p, W.val[1 - cur].p);
+    cur = 1 - cur;
+  }
+  edge_flag_kernel<<<grid(n), kT, 0, s>>>(W.key[cur].p, n, W.flag.p);
+  scan(W.flag.p, n, W.rid.p, W.bsum, s);
+  edge_start_kernel<<<grid(n), kT, 0, s>>>(W.flag.p, W.rid.p, n, W.start.p);
+  edge_emit_kernel<<<grid(n), kT, 0, s>>>(W.flag.p, W.rid.p, W.start.p, n, W.emit.p);
+  scan(W.emit.p, n, W.eoff.p, W.bsum, s);
+  int ne = 0;
+  EG(cudaMemcpyAsync(&ne, W.eoff.p + n, sizeof(int), cudaMemcpyDeviceToHost, s));
+  EG(cudaStreamSynchronize(s));
+  EG(edges.resize(std::max(1, ne)));
+  edge_write_kernel<<<grid(n), kT, 0, s>>>(tri_d, W.key[cur].p, W.val[cur].p, W.emit.p,
+                                           W.eoff.p, n, edges.p);
+  EG(cudaGetLastError());
+  launches += 1 + 8 * 5 + 3 * 3 + 3;
+  n_edges = ne;
+#undef EG
   return "";
 }
 

@@ -116,7 +116,8 @@ EXPORTS = ["eolc_version", "eolc_launch_count", "eolc_create", "eolc_destroy", "
            "eolc_batch_autotune", "eolc_set_learned_refresh", "eolc_set_coarse_refresh",
            "eolc_batch_set_jacobi_reference", "eolc_lpc_blocks", "eolc_export_obj",
            "eolc_export_obj_text", "eolc_velocity_solve_ineq", "eolc_contact_rows",
-           "eolc_step_contacts", "eolc_set_topology_device", "eolc_topology_arrays"]
+           "eolc_step_contacts", "eolc_set_topology_device", "eolc_topology_arrays",
+           "eolc_edge_list"]
 
 
 def load_library(path=LIB_PATH):
@@ -188,6 +189,7 @@ def load_library(path=LIB_PATH):
     L.eolc_set_topology_device.argtypes = [_V, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                            ctypes.c_void_p, ctypes.c_int]
     L.eolc_topology_arrays.argtypes = [_V, _I, _I, _I, _I, _I, _I, _I]
+    L.eolc_edge_list.argtypes = [_V, _I, ctypes.c_int, _I]
     L.eolc_step_contacts.argtypes = [_V, _D, _D, _D, ctypes.POINTER(Material), _D,
                                      ctypes.c_double, _I, _D, ctypes.c_int, ctypes.POINTER(Box),
                                      ctypes.c_int, _D, _D, ctypes.c_int, ctypes.c_double,
@@ -289,6 +291,17 @@ class Context:
         out["contrib"] = out["contrib"][:nc]
         out["nf_list"] = out["nf_list"][:nf]
         return out
+
+    def edge_list(self):
+        """CD2's cloth edges (eolc_edge_list): (E, 4) int32 rows
+        (v0, v1, face0, face1 or -1)."""
+        n = ctypes.c_int()
+        st = lib.eolc_edge_list(self._h, None, 0, ctypes.byref(n))
+        if st not in (OK, CAPACITY):
+            self._check(st)
+        out = np.zeros((max(1, n.value), 4), np.int32)
+        self._check(lib.eolc_edge_list(self._h, _i(out), n.value, ctypes.byref(n)))
+        return out[:n.value]
 
     def bsr_pattern(self):
         nb = ctypes.c_int()

@@ -370,6 +370,14 @@ eolc_status eolc_cd2(eolc_ctx *ctx, const double *x_h, const eolc_box *boxes,
                      int n_boxes, const double *points_h,
                      const double *normals_h, int n_points, double threshold,
                      eolc_contact *out_h, int capacity, int *n_out);
+/* The cloth edge list CD2 uses (createEdges, boxTriCollision.cpp:141-231),
+ * built on the device once per topology: per edge (verts(0), verts(1),
+ * face0, face1 or -1), 4 ints, in the reference's order (faces' edges
+ * stably sorted by the 32-bit hash kmin + (3 n_tri + 1) kmax, twins
+ * paired).  *n_edges gets the count; EOLC_CAPACITY when capacity (edges) is
+ * smaller. */
+eolc_status eolc_edge_list(eolc_ctx *ctx, int *edges_h, int capacity,
+                           int *n_edges);
 /* The inequality rows Constraints::fill builds from CD2 contacts of a
  * non-EOL mesh (Constraints.cpp:422-468), in contact order: box face /
  * cloth vertex -> -nor1 on the vertex; edge / edge -> -nor2 weights2[j] on

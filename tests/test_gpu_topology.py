@@ -104,3 +104,21 @@ def test_invalid_topologies_are_rejected(eolc, bad):
     # the context is still usable
     ctx.set_topology(s["n"], s["tri"], s["hinge"])
     _same(ctx.topology_arrays(), topology_ref.build(s["n"], s["tri"], s["hinge"]))
+
+
+@pytest.mark.parametrize("case", ["sheet16", "sheet160", "delaunay"])
+def test_edge_list_matches_oracle(eolc, case):
+    """CD2's edge list built on the device against the oracle's createEdges
+    (oracle/collide.cpp), row for row; the 160x160 sheet (51,200 faces) is
+    past the size where the reference's 32-bit hash wraps."""
+    if case.startswith("sheet"):
+        s = scenes.sheet(int(case[5:]))
+    else:
+        s = scenes.delaunay_sheet(5000, np.random.default_rng(4))
+    ctx = eolc.Context(0)
+    ctx.set_topology(s["n"], s["tri"], s["hinge"])
+    got = ctx.edge_list()
+    want = O.create_edges(s["x"], s["tri"])
+    assert got.shape[0] == want.shape[0]
+    assert np.array_equal(got[:, 0], want[:, 0]) and np.array_equal(got[:, 1], want[:, 1])
+    assert np.array_equal(got[:, 2], want[:, 4]) and np.array_equal(got[:, 3], want[:, 5])

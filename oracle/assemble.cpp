@@ -351,3 +351,196 @@ int orc_step(int n_nodes, double *x, const double *X, double *v,
 }
 
 }  // extern "C"
+
+// ---- Forces::fill with EOL nodes ------------------------------------------
+// The EOL branches of faceBasedF (Forces.cpp:399-497 with fillEOLInertia /
+// fillEOLMembrane, :177-329) and edgeBasedF (:746-884 with fillEOLBending,
+// :580-683).  A node with EoL_index k owns two Eulerian DOFs at 3N + 2k.
+// With the element's Lagrangian blocks K_vw and, for an EOL vertex v, its
+// deformation gradient F_v (3x2; the face's for faces, the mean of the two
+// adjacent faces' for hinges), the reference fills
+//   (x_v, x_w) = K_vw,  (X_v, x_w) = -F_v' K_vw,  (x_w, X_v) = -K_wv F_v,
+//   (X_v, X_w) = F_v' K_vw F_w,  f_X_v = -F_v' f_v,
+// in this triplet order: Lagrangian diagonal blocks, Lagrangian pairs,
+// Eulerian diagonal blocks, Eulerian pairs, then for each EOL vertex v in
+// order the blocks (X_v, x_w) for w >= v followed by (x_u, X_v) for u < v
+// (each fill also pushes the transpose).  Faces do this for M and MDK
+// (MDK = M + dB h^2 K); hinges for MDK only, and a hinge that touches an EOL
+// node also adds its bending force to the Lagrangian DOFs (the non-EOL
+// branch adds none).
+namespace {
+
+struct F32 {
+  double a[3][2];
+};
+
+// deform_grad (UtilEOL.cpp:13-28): Dx * inverse(DX), Eigen's 2x2 inverse.
+F32 deform_grad(const double *x, const double *X, int i0, int i1, int i2) {
+  double Dx[3][2], DX[2][2];
+  for (int c = 0; c < 3; ++c) {
+    Dx[c][0] = x[3 * i1 + c] - x[3 * i0 + c];
+    Dx[c][1] = x[3 * i2 + c] - x[3 * i0 + c];
+  }
+  for (int c = 0; c < 2; ++c) {
+    DX[c][0] = X[2 * i1 + c] - X[2 * i0 + c];
+    DX[c][1] = X[2 * i2 + c] - X[2 * i0 + c];
+  }
+  const double det = DX[0][0] * DX[1][1] - DX[1][0] * DX[0][1];
+  const double id = 1.0 / det;
+  const double inv[2][2] = {{DX[1][1] * id, -DX[0][1] * id}, {-DX[1][0] * id, DX[0][0] * id}};
+  F32 F;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 2; ++c) F.a[r][c] = Dx[r][0] * inv[0][c] + Dx[r][1] * inv[1][c];
+  return F;
+}
+
+// One element's triplets.  nv vertices with global Lagrangian DOF base
+// xi[v] and Eulerian base Xi[v] (-1: not EOL); K(i, j) / M(i, j) read the
+// element's 3nv x 3nv matrices; M may be null (hinges).  s = dB h^2.
+template <typename KF, typename MF>
+void emit_eol_element(int nv, const int *xi, const int *Xi, const F32 *F, KF K, MF M,
+                      bool has_m, double s, std::vector<Trip> &Mt, std::vector<Trip> &Kt) {
+  auto blk = [&](auto &A, int v, int w, int j, int k) { return A(3 * v + j, 3 * w + k); };
+  // value of a transformed block entry: kind 0 x-x, 1 X-x, 2 x-X, 3 X-X
+  auto tr = [&](auto &A, int kind, int v, int w, int j, int k) {
+    double r = 0;
+    if (kind == 0) return blk(A, v, w, j, k);
+    if (kind == 1) {  // -F_v' A_vw, (2 x 3)
+      for (int p = 0; p < 3; ++p) r += F[v].a[p][j] * blk(A, v, w, p, k);
+      return -r;
+    }
+    if (kind == 2) {  // -A_vw F_w, (3 x 2)
+      for (int q = 0; q < 3; ++q) r += blk(A, v, w, j, q) * F[w].a[q][k];
+      return -r;
+    }
+    for (int p = 0; p < 3; ++p) {  // F_v' A_vw F_w, (2 x 2)
+      double t = 0;
+      for (int q = 0; q < 3; ++q) t += blk(A, v, w, p, q) * F[w].a[q][k];
+      r += F[v].a[p][j] * t;
+    }
+    return r;
+  };
+  // push block (v, w) of the given kind at rows r0, cols c0, and its
+  // transpose when sym
+  auto push = [&](int kind, int v, int w, int r0, int c0, bool sym) {
+    const int nr = (kind == 1 || kind == 3) ? 2 : 3, nc = (kind == 2 || kind == 3) ? 2 : 3;
+    for (int j = 0; j < nr; ++j)
+      for (int k = 0; k < nc; ++k) {
+        const double m = has_m ? tr(M, kind, v, w, j, k) : 0.0;
+        const double kk = has_m ? m + s * tr(K, kind, v, w, j, k) : s * tr(K, kind, v, w, j, k);
+        if (has_m) Mt.push_back({r0 + j, c0 + k, m});
+        Kt.push_back({r0 + j, c0 + k, kk});
+        if (sym) {
+          if (has_m) Mt.push_back({c0 + k, r0 + j, m});
+          Kt.push_back({c0 + k, r0 + j, kk});
+        }
+      }
+  };
+  for (int v = 0; v < nv; ++v) push(0, v, v, xi[v], xi[v], false);
+  for (int v = 0; v < nv; ++v)
+    for (int w = v + 1; w < nv; ++w) push(0, v, w, xi[v], xi[w], true);
+  for (int v = 0; v < nv; ++v)
+    if (Xi[v] >= 0) push(3, v, v, Xi[v], Xi[v], false);
+  for (int v = 0; v < nv; ++v)
+    for (int w = v + 1; w < nv; ++w)
+      if (Xi[v] >= 0 && Xi[w] >= 0) push(3, v, w, Xi[v], Xi[w], true);
+  for (int v = 0; v < nv; ++v) {
+    if (Xi[v] < 0) continue;
+    for (int w = v; w < nv; ++w) push(1, v, w, Xi[v], xi[w], true);
+    for (int u = 0; u < v; ++u) push(2, u, v, xi[u], Xi[v], true);
+  }
+}
+
+}  // namespace
+
+extern "C" orc_forces *orc_forces_fill_eol(int n_nodes, const double *x, const double *X,
+                                           const int *tri, int n_tri, const int *hinge,
+                                           int n_hinge, const eolc_material *mat,
+                                           const double *grav, double h, const int *eol_index,
+                                           int n_eol) {
+  auto *F = new orc_forces;
+  const int n = 3 * n_nodes + 2 * n_eol;
+  F->n_nodes = n_nodes;
+  F->f.assign(n, 0.0);
+  std::vector<Trip> Mt, Kt;
+  const double dh2 = mat->damping_b * h * h;
+  auto Xdof = [&](int node) { return eol_index[node] >= 0 ? 3 * n_nodes + 2 * eol_index[node] : -1; };
+  for (int t = 0; t < n_tri; ++t) {
+    const int *v = tri + 3 * t;
+    double x9[9], X6[6], P6[6], Q4[4];
+    for (int a = 0; a < 3; ++a) {
+      for (int c = 0; c < 3; ++c) x9[3 * a + c] = x[3 * v[a] + c];
+      for (int c = 0; c < 2; ++c) X6[2 * a + c] = X[2 * v[a] + c];
+    }
+    orc_face_frame(x9, X6, P6, Q4);
+    double W, fm[9], Km[81], fi[9], Mi[81];
+    orc_membrane(x9, X6, mat->e, mat->nu, P6, Q4, &W, fm, Km);
+    orc_inertial(x9, X6, grav, mat->density, &W, fi, Mi);
+    auto Kme = [&](int i, int j) { return Km[j * 9 + i]; };
+    auto Mie = [&](int i, int j) { return Mi[j * 9 + i]; };
+    int xi[3], Xi[3];
+    bool eol = false;
+    for (int a = 0; a < 3; ++a) {
+      xi[a] = 3 * v[a];
+      Xi[a] = Xdof(v[a]);
+      eol |= Xi[a] >= 0;
+    }
+    const F32 Fg = deform_grad(x, X, v[0], v[1], v[2]);
+    F32 Fv[3] = {Fg, Fg, Fg};
+    for (int a = 0; a < 3; ++a) {
+      for (int c = 0; c < 3; ++c) F->f[xi[a] + c] += fm[3 * a + c] + fi[3 * a + c];
+      if (Xi[a] < 0) continue;
+      for (int j = 0; j < 2; ++j) {  // (-F' fm) + (-F' fi), Forces.cpp:206-216,284-294,406-416
+        double sm = 0, si = 0;
+        for (int p = 0; p < 3; ++p) {
+          sm += Fg.a[p][j] * fm[3 * a + p];
+          si += Fg.a[p][j] * fi[3 * a + p];
+        }
+        F->f[Xi[a] + j] += -sm + -si;
+      }
+    }
+    emit_eol_element(3, xi, Xi, Fv, Kme, Mie, true, dh2, Mt, Kt);
+    (void)eol;
+  }
+  for (int e = 0; e < n_hinge; ++e) {
+    const int *v = hinge + 4 * e;
+    double x12[12], X8[8];
+    for (int a = 0; a < 4; ++a) {
+      for (int c = 0; c < 3; ++c) x12[3 * a + c] = x[3 * v[a] + c];
+      for (int c = 0; c < 2; ++c) X8[2 * a + c] = X[2 * v[a] + c];
+    }
+    double W, fb[12], Kb[144];
+    orc_bending(x12, X8, mat->beta, &W, fb, Kb);
+    auto Kbe = [&](int i, int j) { return Kb[j * 12 + i]; };
+    auto none = [&](int, int) { return 0.0; };
+    int xi[4], Xi[4];
+    bool eol = false;
+    for (int a = 0; a < 4; ++a) {
+      xi[a] = 3 * v[a];
+      Xi[a] = Xdof(v[a]);
+      eol |= Xi[a] >= 0;
+    }
+    F32 Fv[4];
+    if (eol) {
+      // (F1 + F2) / 2 over the two adjacent faces (Forces.cpp:590-596)
+      const F32 F1 = deform_grad(x, X, v[0], v[1], v[2]), F2 = deform_grad(x, X, v[0], v[1], v[3]);
+      F32 Fm;
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 2; ++c) Fm.a[r][c] = (F1.a[r][c] + F2.a[r][c]) / 2;
+      for (int a = 0; a < 4; ++a) Fv[a] = Fm;
+      for (int a = 0; a < 4; ++a) {  // the EOL branch adds the bending force
+        for (int c = 0; c < 3; ++c) F->f[xi[a] + c] += fb[3 * a + c];
+        if (Xi[a] < 0) continue;
+        for (int j = 0; j < 2; ++j) {
+          double sb = 0;
+          for (int p = 0; p < 3; ++p) sb += Fm.a[p][j] * fb[3 * a + p];
+          F->f[Xi[a] + j] += -sb;
+        }
+      }
+    }
+    emit_eol_element(4, xi, Xi, Fv, Kbe, none, false, dh2, Mt, Kt);
+  }
+  F->M = from_triplets(n, Mt);
+  F->MDK = from_triplets(n, Kt);
+  return F;
+}

@@ -67,6 +67,16 @@ void orc_forces_csr(const orc_forces *F, int which, int *rowptr, int *col,
                     double *val);
 void orc_forces_f(const orc_forces *F, double *f);
 
+/* Forces::fill with EOL nodes (Forces.cpp:177-329, 399-497, 580-683,
+ * 746-884): eol_index[node] = its EoL_index or -1; the system has
+ * 3 n_nodes + 2 n_eol DOFs (Eulerian DOFs of EoL_index k at 3 N + 2 k).
+ * Read it with orc_forces_nnz / orc_forces_csr / orc_forces_f. */
+orc_forces *orc_forces_fill_eol(int n_nodes, const double *x, const double *X,
+                                const int *tri, int n_tri, const int *hinge,
+                                int n_hinge, const eolc_material *mat,
+                                const double *grav, double h,
+                                const int *eol_index, int n_eol);
+
 /* b = -(M v + h f) (Cloth.cpp:345) */
 void orc_rhs(const orc_forces *F, const double *v, double h, double *b);
 

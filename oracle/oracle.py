@@ -99,6 +99,10 @@ def lib():
         L.orc_create_edges.argtypes = [ctypes.c_int, _D, _I, ctypes.c_int, _I,
                                        ctypes.c_int]
         L.orc_hinges.argtypes = [ctypes.c_int, _I, ctypes.c_int, _I, ctypes.c_int]
+        L.orc_forces_fill_eol.restype = ctypes.c_void_p
+        L.orc_forces_fill_eol.argtypes = [ctypes.c_int, _D, _D, _I, ctypes.c_int, _I,
+                                          ctypes.c_int, ctypes.POINTER(Material), _D,
+                                          ctypes.c_double, _I, ctypes.c_int]
         L.orc_obj_text.argtypes = [ctypes.c_int, _D, _D, _I, ctypes.c_int, ctypes.c_int,
                                    ctypes.c_double, ctypes.c_char_p, ctypes.c_longlong,
                                    ctypes.POINTER(ctypes.c_longlong)]
@@ -209,14 +213,18 @@ class Forces:
             lib().orc_forces_free(self._h)
             self._h = None
 
+    @property
+    def n_dofs(self):
+        return 3 * self.n_nodes + 2 * getattr(self, "n_eol", 0)
+
     def f(self):
-        out = np.zeros(3 * self.n_nodes)
+        out = np.zeros(self.n_dofs)
         lib().orc_forces_f(self._h, dp(out))
         return out
 
     def csr(self, which):
         import scipy.sparse as sp
-        n = 3 * self.n_nodes
+        n = self.n_dofs
         nnz = lib().orc_forces_nnz(self._h, which)
         rp = np.zeros(n + 1, np.int32); c = np.zeros(nnz, np.int32); v = np.zeros(nnz)
         lib().orc_forces_csr(self._h, which, ip(rp), ip(c), dp(v))
@@ -246,6 +254,23 @@ class Forces:
         if rc != 0:
             raise RuntimeError("direct solve failed (%d)" % rc)
         return v
+
+
+class ForcesEOL(Forces):
+    """Forces::fill with EOL nodes: eol_nodes[k] is the node of EoL_index k;
+    f, M, MDK over the 3N + 2E DOFs (Eulerian DOFs of k at 3N + 2k)."""
+
+    def __init__(self, x, X, tri, hinge, mat, grav, h, eol_nodes):
+        self.n_nodes = len(x) // 3
+        self.n_eol = len(eol_nodes)
+        idx = -np.ones(self.n_nodes, np.int32)
+        idx[np.asarray(eol_nodes, np.int64)] = np.arange(self.n_eol, dtype=np.int32)
+        tri = np.ascontiguousarray(tri, dtype=np.int32)
+        hinge = np.ascontiguousarray(hinge, dtype=np.int32)
+        g = np.ascontiguousarray(grav, dtype=np.float64)
+        self._h = lib().orc_forces_fill_eol(self.n_nodes, dp(x), dp(X), ip(tri), len(tri),
+                                            ip(hinge), len(hinge), ctypes.byref(mat), dp(g),
+                                            ctypes.c_double(h), ip(idx), self.n_eol)
 
 
 def step(x, X, v, tri, hinge, mat, grav, h, fixed_dofs, fixed_vel, tol=1e-8,

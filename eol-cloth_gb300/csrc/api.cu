@@ -89,11 +89,34 @@ eolc_status set_pins(eolc_ctx *ctx, const int *dofs_h, const double *vel_h,
     if (dofs_h[k] < 0 || dofs_h[k] >= n) return fail(ctx, EOLC_BAD_ARG, "fixed dof out of range");
     mask[dofs_h[k]] = 1;
   }
+  // the padded third DOF of every Eulerian (EOL) node stays 0
+  for (int i = ctx->topo.n_real; i < ctx->topo.n_nodes; ++i) mask[3 * i + 2] = 1;
   EOLC_CHECK_CUDA(ctx, ctx->pinned.upload(mask.data(), n, s));
   EOLC_CHECK_CUDA(ctx, ctx->fixed_dofs.upload(dofs_h, n_fixed, s));
   if (vel_h) EOLC_CHECK_CUDA(ctx, ctx->fixed_vel.upload(vel_h, n_fixed, s));
   ctx->n_fixed_dev = n_fixed;
   EOLC_CHECK_CUDA(ctx, ctx->beq_full.resize(n));
+  return EOLC_OK;
+}
+
+// Positions x (3 n_real) and material coordinates X (2 n_real) of the mesh
+// nodes; an Eulerian node's slots repeat its EOL node's (only the resident
+// solver's partition reads them).
+eolc_status upload_positions(eolc_ctx *ctx, const double *x_h, const double *X_h,
+                             cudaStream_t s) {
+  const DevTopology &T = ctx->topo;
+  const int n = T.n_real;
+  if (x_h) EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->x.p, x_h, sizeof(double) * 3 * n,
+                                                cudaMemcpyHostToDevice, s));
+  if (X_h) EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->X.p, X_h, sizeof(double) * 2 * n,
+                                                cudaMemcpyHostToDevice, s));
+  for (size_t k = 0; k < ctx->eol_nodes.size(); ++k) {
+    const int v = ctx->eol_nodes[k];
+    if (x_h) EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->x.p + 3 * (n + k), ctx->x.p + 3 * v,
+                                                  sizeof(double) * 3, cudaMemcpyDeviceToDevice, s));
+    if (X_h) EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->X.p + 2 * (n + k), ctx->X.p + 2 * v,
+                                                  sizeof(double) * 2, cudaMemcpyDeviceToDevice, s));
+  }
   return EOLC_OK;
 }
 
@@ -133,6 +156,8 @@ eolc_status assemble(eolc_ctx *ctx, const eolc_material &mat, const double g[3],
   const MaterialD *mats = batched ? ctx->inst_matd.p : nullptr;
   const int *node_inst = batched ? ctx->node_inst.p : nullptr;
   size_t nb9 = size_t(ctx->topo.n_blocks) * 9;
+  const bool eol = ctx->topo.n_eol > 0;
+  if (eol && want_b) want_M = true;  // b = -(M v + h f) from the assembled M
   if (prec == EOLC_PREC_FP64) EOLC_CHECK_CUDA(ctx, ctx->A64.resize(nb9 + 16));
   if (want_M) EOLC_CHECK_CUDA(ctx, ctx->Mblk.resize(nb9));
   {
@@ -152,6 +177,13 @@ eolc_status assemble(eolc_ctx *ctx, const eolc_material &mat, const double g[3],
                          want_M ? ctx->Mblk.p : nullptr, s);
   EOLC_CHECK_CUDA(ctx, cudaStreamWaitEvent(s, ctx->aux_join, 0));
   ctx->launches += ctx->topo.n_hinge > 0 ? 5 : 4;
+  if (eol) {
+    ctx->launches += 1;
+    if (want_b) {
+      launch_bsr_rhs(ctx->topo, ctx->Mblk.p, ctx->v.p, ctx->f.p, h, ctx->b.p, s);
+      ctx->launches += 1;
+    }
+  }
   EOLC_CHECK_CUDA(ctx, cudaGetLastError());
   return EOLC_OK;
 }
@@ -190,6 +222,7 @@ eolc_status batch_begin(eolc_ctx *ctx, const double grav[3], double h, const int
   eolc_status st = need_topology(ctx);
   if (st != EOLC_OK) return st;
   if ((st = check_opts(ctx, opts)) != EOLC_OK) return st;
+  if ((st = refuse_eol(ctx)) != EOLC_OK) return st;
   // host mirrors before any capture (the learned network's graph reads them)
   if (!host_topology(ctx)) return EOLC_CUDA_ERROR;
   if (opts->precond == EOLC_PC_PATCH)
@@ -404,6 +437,7 @@ eolc_status solve_with_args(eolc_ctx *ctx, const eolc_solve_opts *o, const PcgAr
   eolc_solve_info local{};
   eolc_solve_info *inf = info ? info : &local;
   if (o->precond == EOLC_PC_LEARNED) {
+    if (ctx->topo.n_eol > 0) return refuse_eol(ctx);
     if (!ctx->lpc) return fail(ctx, EOLC_BAD_ARG, "no learned preconditioner attached");
     if (o->precision != EOLC_PREC_MIXED)
       return fail(ctx, EOLC_BAD_ARG, "the learned preconditioner runs on the mixed path");
@@ -490,7 +524,7 @@ const HostTopology *host_topology(eolc_ctx *ctx) {
   H.blk_row.resize(NB);
   H.diag.resize(N);
   H.cptr.resize(size_t(NB) + 1);
-  H.nf_ptr.resize(size_t(N) + 1);
+  H.nf_ptr.resize(size_t(T.n_real) + 1);
   H.nf_list.resize(size_t(3) * T.n_tri);
   auto get = [&](std::vector<int> &dst, const int *src) {
     return cudaMemcpyAsync(dst.data(), src, sizeof(int) * dst.size(), cudaMemcpyDeviceToHost, s);
@@ -528,12 +562,12 @@ namespace {
 // Builds the BSR pattern, contribution lists and node -> face lists on the
 // device from ctx->topo.tri / hinge (already on the device).
 eolc_status topology_from_device(eolc_ctx *ctx, int n_nodes, int n_tri, int n_hinge,
-                                 cudaStream_t s) {
+                                 cudaStream_t s, int n_eol = 0) {
   ctx->has_topology = false;
   ctx->host_valid = false;
   std::string msg = build_topology_device(ctx->topo_work, n_nodes, ctx->topo.tri.p, n_tri,
                                           n_hinge > 0 ? ctx->topo.hinge.p : nullptr, n_hinge,
-                                          ctx->topo, s, ctx->launches);
+                                          ctx->topo, s, ctx->launches, n_eol);
   if (!msg.empty()) return fail(ctx, EOLC_BAD_ARG, msg.c_str());
   return EOLC_OK;
 }
@@ -715,6 +749,7 @@ eolc_status eolc_set_topology_batched(eolc_ctx *ctx, int n_inst, const int *node
   EOLC_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
   ctx->host_tri.assign(tri_h, tri_h + size_t(n_tri) * 3);
   ctx->node_off.assign(node_off_h, node_off_h + n_inst + 1);
+  ctx->eol_nodes.clear();
   return reset_after_topology(ctx, s);
 }
 
@@ -740,6 +775,43 @@ eolc_status eolc_set_topology_device(eolc_ctx *ctx, int n_nodes, const int *tri_
   EOLC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->node_inst.p, 0, sizeof(int) * n_nodes, s));
   ctx->host_tri.clear();  // downloaded on first use
   ctx->node_off.assign({0, n_nodes});
+  ctx->eol_nodes.clear();
+  return reset_after_topology(ctx, s);
+}
+
+eolc_status eolc_set_topology_eol(eolc_ctx *ctx, int n_nodes, const int *tri_h, int n_tri,
+                                  const int *hinge_h, int n_hinge, const int *eol_nodes_h,
+                                  int n_eol) {
+  if (!ctx) return EOLC_BAD_ARG;
+  if (!tri_h || n_tri <= 0 || n_nodes <= 0 || n_hinge < 0 || (n_hinge > 0 && !hinge_h) ||
+      n_eol < 0 || (n_eol > 0 && !eol_nodes_h))
+    return fail(ctx, EOLC_BAD_ARG, "null or empty topology");
+  std::vector<int> eol(n_nodes, -1);
+  for (int k = 0; k < n_eol; ++k) {
+    const int v = eol_nodes_h[k];
+    if (v < 0 || v >= n_nodes) return fail(ctx, EOLC_BAD_ARG, "EOL node out of range");
+    if (eol[v] >= 0) return fail(ctx, EOLC_BAD_ARG, "EOL node listed twice");
+    eol[v] = k;
+  }
+  for (int64_t q = 0; q < int64_t(n_tri) * 3; ++q)
+    if (tri_h[q] < 0 || tri_h[q] >= n_nodes)
+      return fail(ctx, EOLC_BAD_ARG, "element index out of range");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = stream_of(ctx);
+  DevTopology &T = ctx->topo;
+  EOLC_CHECK_CUDA(ctx, T.tri.upload(tri_h, size_t(n_tri) * 3, s));
+  if (n_hinge > 0) EOLC_CHECK_CUDA(ctx, T.hinge.upload(hinge_h, size_t(n_hinge) * 4, s));
+  if (n_eol > 0) {
+    EOLC_CHECK_CUDA(ctx, T.eol.upload(eol.data(), eol.size(), s));
+    EOLC_CHECK_CUDA(ctx, T.eol_node.upload(eol_nodes_h, n_eol, s));
+  }
+  eolc_status st = topology_from_device(ctx, n_nodes, n_tri, n_hinge, s, n_eol);
+  if (st != EOLC_OK) return st;
+  EOLC_CHECK_CUDA(ctx, ctx->node_inst.resize(T.n_nodes));
+  EOLC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->node_inst.p, 0, sizeof(int) * T.n_nodes, s));
+  ctx->host_tri.assign(tri_h, tri_h + size_t(n_tri) * 3);
+  ctx->node_off.assign({0, T.n_nodes});
+  ctx->eol_nodes.assign(eol_nodes_h, eol_nodes_h + n_eol);
   return reset_after_topology(ctx, s);
 }
 
@@ -799,8 +871,7 @@ eolc_status eolc_forces_fill(eolc_ctx *ctx, const double *x_h,
   cudaStream_t s = stream_of(ctx);
   int N = ctx->topo.n_nodes;
   size_t nb9 = size_t(ctx->topo.n_blocks) * 9;
-  EOLC_CHECK_CUDA(ctx, ctx->x.upload(x_h, size_t(N) * 3, s));
-  EOLC_CHECK_CUDA(ctx, ctx->X.upload(X_h, size_t(N) * 2, s));
+  if ((st = upload_positions(ctx, x_h, X_h, s)) != EOLC_OK) return st;
   st = assemble(ctx, *mat, grav, h, precision, M_h != nullptr, false, s);
   if (st != EOLC_OK) return st;
   if (f_h) EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(f_h, ctx->f.p, sizeof(double) * 3 * N,
@@ -856,6 +927,7 @@ eolc_status eolc_state_upload(eolc_ctx *ctx, const double *x_h,
                               const double *X_h, const double *v_h) {
   eolc_status st = need_topology(ctx);
   if (st != EOLC_OK) return st;
+  if ((st = refuse_eol(ctx)) != EOLC_OK) return st;
   cudaSetDevice(ctx->device);
   cudaStream_t s = stream_of(ctx);
   int N = ctx->topo.n_nodes;
@@ -869,6 +941,7 @@ eolc_status eolc_state_upload(eolc_ctx *ctx, const double *x_h,
 eolc_status eolc_state_download(eolc_ctx *ctx, double *x_h, double *v_h) {
   eolc_status st = need_topology(ctx);
   if (st != EOLC_OK) return st;
+  if ((st = refuse_eol(ctx)) != EOLC_OK) return st;
   cudaSetDevice(ctx->device);
   cudaStream_t s = stream_of(ctx);
   int N = ctx->topo.n_nodes;
@@ -888,6 +961,7 @@ eolc_status eolc_step_resident(eolc_ctx *ctx, int n_steps,
                                eolc_solve_info *info) {
   eolc_status st = need_topology(ctx);
   if (st != EOLC_OK) return st;
+  if ((st = refuse_eol(ctx)) != EOLC_OK) return st;
   if ((st = check_opts(ctx, opts)) != EOLC_OK) return st;
   if (!mat || !grav || n_steps < 0) return fail(ctx, EOLC_BAD_ARG, "bad step arguments");
   if (n_fixed > 0 && (!fixed_dofs_h || !fixed_vel_h)) return fail(ctx, EOLC_BAD_ARG, "null fixed list");
@@ -957,6 +1031,7 @@ eolc_status eolc_step_contacts(eolc_ctx *ctx, double *x_h, const double *X_h, do
                                const eolc_solve_opts *opts, eolc_ineq_info *info) {
   eolc_status st = need_topology(ctx);
   if (st != EOLC_OK) return st;
+  if ((st = refuse_eol(ctx)) != EOLC_OK) return st;
   if ((st = check_opts(ctx, opts)) != EOLC_OK) return st;
   if (!x_h || !X_h || !v_h || !mat || !grav) return fail(ctx, EOLC_BAD_ARG, "null state");
   if (n_fixed > 0 && (!fixed_dofs_h || !fixed_vel_h)) return fail(ctx, EOLC_BAD_ARG, "null fixed list");

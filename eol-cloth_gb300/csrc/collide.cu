@@ -858,6 +858,7 @@ extern "C" eolc_status eolc_cd2(eolc_ctx *ctx, const double *x_h,
                                 eolc_contact *out_h, int capacity, int *n_out) {
   if (!ctx) return EOLC_BAD_ARG;
   if (!ctx->has_topology) { ctx->err = "no topology set"; return EOLC_NO_TOPOLOGY; }
+  if (refuse_eol(ctx) != EOLC_OK) return EOLC_BAD_ARG;
   if (!x_h || n_boxes < 0 || n_points < 0 || capacity < 0 || !n_out ||
       (n_boxes > 0 && !boxes) || (n_points > 0 && (!points_h || !normals_h)) ||
       (capacity > 0 && !out_h)) {

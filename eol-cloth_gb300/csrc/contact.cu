@@ -570,6 +570,7 @@ extern "C" eolc_status eolc_velocity_solve_ineq(
     return EOLC_NO_TOPOLOGY;
   }
   if (!opts) return bad(ctx, "null solve options");
+  if (refuse_eol(ctx) != EOLC_OK) return EOLC_BAD_ARG;
   if (!b_h || !v_h || (n_fixed > 0 && !beq_h)) return bad(ctx, "null input");
   if (ctx->last_precision < 0) return bad(ctx, "no matrix assembled");
   if (opts->precision != ctx->last_precision)

@@ -310,6 +310,7 @@ eolc_status generate(eolc_ctx *ctx, size_t len[2]) {
     ctx->err = "no topology set";
     return EOLC_NO_TOPOLOGY;
   }
+  if (refuse_eol(ctx) != EOLC_OK) return EOLC_BAD_ARG;
   cudaSetDevice(ctx->device);
   cudaStream_t s = ctx->stream;
   if (!ctx->ex_work) ctx->ex_work = new ExportWork();

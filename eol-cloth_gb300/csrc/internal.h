@@ -42,13 +42,15 @@ struct DevBuf {
 };
 
 // Contribution code of one element to one 3x3 block:
-//   bits 0-1: local vertex of the block's column, bits 2-3: local vertex of
-//   the block's row, bit 4: 0 = triangle (membrane + inertia),
-//   1 = hinge (bending), bits 5-31: element index.
-constexpr int kHingeBit = 1 << 4;
+//   bits 0-2: the block's column in the element, bits 3-5: its row — each a
+//   local vertex (bits 0-1) plus kVirtual when it is that vertex's Eulerian
+//   (EOL) node; bit 6: 0 = triangle (membrane + inertia), 1 = hinge
+//   (bending); bits 7-30: element index.
+constexpr int kHingeBit = 1 << 6;
+constexpr int kVirtual = 4;
 __host__ __device__ inline int contrib_code(int elem, bool hinge, int lrow,
                                             int lcol) {
-  return (elem << 5) | (hinge ? kHingeBit : 0) | (lrow << 2) | lcol;
+  return (elem << 7) | (hinge ? kHingeBit : 0) | (lrow << 3) | lcol;
 }
 
 // ---- topology (device build, topology_gpu.cu; host mirror on demand) -------
@@ -65,10 +67,15 @@ struct HostTopology {
 };
 
 // ---- device state -----------------------------------------------------------
+// n_nodes rows of the BSR pattern: the n_real mesh nodes, then one Eulerian
+// node per EOL node (n_eol; its two Eulerian DOFs and a padded third that
+// the solves pin).  eol[node] = EoL_index or -1 (n_real entries) and
+// eol_node[k] = the node of EoL_index k, both only when n_eol > 0.
 struct DevTopology {
-  int n_nodes = 0, n_tri = 0, n_hinge = 0, n_blocks = 0;
+  int n_nodes = 0, n_tri = 0, n_hinge = 0, n_blocks = 0, n_real = 0, n_eol = 0;
   DevBuf<int> tri, hinge, rowptr, colidx, blk_row, diag, cptr, contrib,
-      nf_ptr, nf_list;
+      nf_ptr, nf_list, eol, eol_node;
+  DevBuf<int> nh_ptr, nh_list;  // node -> hinges (hinge << 2 | local vertex), n_real rows
 };
 
 struct MaterialD {
@@ -81,9 +88,10 @@ struct MaterialD {
 // and hinges; T.tri / T.hinge are not touched.  "" on success.
 struct TopoScratch;
 void free_topo_scratch(TopoScratch *w);
+// n_eol > 0: T.eol / T.eol_node hold the EOL tables already (device).
 std::string build_topology_device(TopoScratch *&w, int N, const int *tri_d, int n_tri,
                                   const int *hinge_d, int n_hinge, DevTopology &T,
-                                  cudaStream_t s, long long &launches);
+                                  cudaStream_t s, long long &launches, int n_eol = 0);
 
 // CD2's edge list (createEdges, boxTriCollision.cpp:141-231) built on the
 // device (topology_gpu.cu): per edge (v0, v1, face, twin face or -1) in the
@@ -112,6 +120,10 @@ void launch_forces_rhs(const DevTopology &T, const double *x, const double *X,
                        const double *v, const MaterialD &m,
                        const MaterialD *mats, const int *node_inst, int prec, void *elem,
                        double *f, double *b, cudaStream_t s);
+
+// b = -(M v + h f) from the assembled FP64 M blocks (EOL topologies).
+void launch_bsr_rhs(const DevTopology &T, const double *Mblk, const double *v, const double *f,
+                    double h, double *b, cudaStream_t s);
 
 // Solver (pcg.cu)
 struct SolveWork;
@@ -261,6 +273,7 @@ struct eolc_ctx {
   cudaStream_t aux = nullptr;
   cudaEvent_t aux_fork = nullptr, aux_join = nullptr;
   std::vector<int> host_tri;  // triangle list of the current topology
+  std::vector<int> eol_nodes; // node of every EoL_index (EOL topologies)
   eolc_lpc *lpc = nullptr;    // attached learned preconditioner (not owned)
   const eolc_lpc *lpc_cached = nullptr;  // network whose G the resident solver holds
   int lpc_uses = 0;           // solves that G has served
@@ -281,3 +294,16 @@ struct eolc_ctx {
   std::vector<double> bgraph_key;             // what the graph was built for
   int bgraph_launches = 0;                    // kernels per replay
 };
+
+namespace eolc {
+// Entry points that take positions or states of every block row (steps,
+// collisions, export, batches, contact rows) refuse topologies with EOL
+// nodes, whose Eulerian rows have no positions of their own.
+inline eolc_status refuse_eol(eolc_ctx *ctx) {
+  if (ctx && ctx->topo.n_eol > 0) {
+    ctx->err = "not available on a topology with EOL nodes";
+    return EOLC_BAD_ARG;
+  }
+  return EOLC_OK;
+}
+}  // namespace eolc

@@ -159,73 +159,103 @@ __global__ void topo_sort_kernel(int N, const int *__restrict__ fptr, int *flist
   insertion_sort(hlist + hptr[i], hptr[i + 1] - hptr[i]);
 }
 
-// The smallest node above `last` among the nodes of row i's faces and
-// hinges (INT_MAX: none).  Walking it from last = -1 lists the row's distinct
-// columns in ascending order without a per-thread buffer.
-__device__ __forceinline__ int next_column(int i, int last, const int *__restrict__ tri,
+// Node index of local vertex c of an element (global node g): g, or with
+// kVirtual its Eulerian node N + eol[g] (-1 when g is not EOL).
+__device__ __forceinline__ int elem_node(int g, int virt, int N, const int *__restrict__ eol) {
+  if (!virt) return g;
+  const int k = eol ? eol[g] : -1;
+  return k < 0 ? -1 : N + k;
+}
+
+// The smallest node above `last` among the nodes of the faces and hinges
+// of node `base` (a row's own node, or the EOL node of an Eulerian row), their
+// Eulerian nodes included (INT_MAX: none).  Walking it from last = -1 lists
+// the row's distinct columns in ascending order without a per-thread buffer.
+__device__ __forceinline__ int next_column(int base, int last, int N, const int *__restrict__ eol,
+                                           const int *__restrict__ tri,
                                            const int *__restrict__ hinge,
                                            const int *__restrict__ fptr,
                                            const int *__restrict__ flist,
                                            const int *__restrict__ hptr,
                                            const int *__restrict__ hlist) {
   int best = INT_MAX;
-  for (int q = fptr[i]; q < fptr[i + 1]; ++q) {
+  for (int q = fptr[base]; q < fptr[base + 1]; ++q) {
     const int t = flist[q] >> 2;
-    for (int b = 0; b < 3; ++b) {
-      const int c = tri[3 * t + b];
+    for (int b = 0; b < 6; ++b) {
+      const int c = elem_node(tri[3 * t + b % 3], b >= 3, N, eol);
       if (c > last && c < best) best = c;
     }
   }
-  for (int q = hptr[i]; q < hptr[i + 1]; ++q) {
+  for (int q = hptr[base]; q < hptr[base + 1]; ++q) {
     const int e = hlist[q] >> 2;
-    for (int b = 0; b < 4; ++b) {
-      const int c = hinge[4 * e + b];
+    for (int b = 0; b < 8; ++b) {
+      const int c = elem_node(hinge[4 * e + b % 4], b >= 4, N, eol);
       if (c > last && c < best) best = c;
     }
   }
   return best;
 }
 
+// Rows 0..N-1 are the nodes, rows N..Ntot-1 the Eulerian nodes of the EOL
+// nodes (eol_node[k], eol[node] = k or -1; both null without EOL nodes).
 // pass 0: ncol[i], ncon[i]; pass 1: the row's blocks and contributions.
 __global__ void __launch_bounds__(kT)
-topo_row_kernel(int N, int pass, const int *__restrict__ tri, const int *__restrict__ hinge,
-                const int *__restrict__ fptr, const int *__restrict__ flist,
-                const int *__restrict__ hptr, const int *__restrict__ hlist, int *ncol,
-                int *ncon, const int *__restrict__ rowptr, const int *__restrict__ cbase,
-                int *colidx, int *blk_row, int *diag, int *cptr, int *contrib, int *err) {
+topo_row_kernel(int N, int Ntot, int pass, const int *__restrict__ eol,
+                const int *__restrict__ eol_node, const int *__restrict__ tri,
+                const int *__restrict__ hinge, const int *__restrict__ fptr,
+                const int *__restrict__ flist, const int *__restrict__ hptr,
+                const int *__restrict__ hlist, int *ncol, int *ncon,
+                const int *__restrict__ rowptr, const int *__restrict__ cbase, int *colidx,
+                int *blk_row, int *diag, int *cptr, int *contrib, int *err) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
+  if (i >= Ntot) return;
+  const int virt_row = i >= N ? kVirtual : 0;
+  const int base = i < N ? i : eol_node[i - N];
   if (pass == 0) {
     int u = 0;
-    for (int j = next_column(i, -1, tri, hinge, fptr, flist, hptr, hlist); j != INT_MAX;
-         j = next_column(i, j, tri, hinge, fptr, flist, hptr, hlist))
+    for (int j = next_column(base, -1, N, eol, tri, hinge, fptr, flist, hptr, hlist);
+         j != INT_MAX; j = next_column(base, j, N, eol, tri, hinge, fptr, flist, hptr, hlist))
       ++u;
     if (u == 0) atomicOr(err, kErrIsolated);
     ncol[i] = u;
-    ncon[i] = 3 * (fptr[i + 1] - fptr[i]) + 4 * (hptr[i + 1] - hptr[i]);
+    int nc = 0;  // one contribution per (element, node of the extended element)
+    for (int q = fptr[base]; q < fptr[base + 1]; ++q) {
+      const int t = flist[q] >> 2;
+      nc += 3;
+      for (int b = 0; b < 3; ++b) nc += elem_node(tri[3 * t + b], 1, N, eol) >= 0;
+    }
+    for (int q = hptr[base]; q < hptr[base + 1]; ++q) {
+      const int e = hlist[q] >> 2;
+      nc += 4;
+      for (int b = 0; b < 4; ++b) nc += elem_node(hinge[4 * e + b], 1, N, eol) >= 0;
+    }
+    ncon[i] = nc;
     return;
   }
   int pos = cbase[i], blk = rowptr[i], dg = -1;
-  for (int j = next_column(i, -1, tri, hinge, fptr, flist, hptr, hlist); j != INT_MAX;
-       j = next_column(i, j, tri, hinge, fptr, flist, hptr, hlist), ++blk) {
+  for (int j = next_column(base, -1, N, eol, tri, hinge, fptr, flist, hptr, hlist);
+       j != INT_MAX; j = next_column(base, j, N, eol, tri, hinge, fptr, flist, hptr, hlist),
+           ++blk) {
     colidx[blk] = j;
     blk_row[blk] = i;
     if (j == i) dg = blk;
     cptr[blk] = pos;
-    for (int q = fptr[i]; q < fptr[i + 1]; ++q) {
+    for (int q = fptr[base]; q < fptr[base + 1]; ++q) {
       const int t = flist[q] >> 2, a = flist[q] & 3;
-      for (int b = 0; b < 3; ++b)
-        if (tri[3 * t + b] == j) contrib[pos++] = contrib_code(t, false, a, b);
+      for (int b = 0; b < 6; ++b)
+        if (elem_node(tri[3 * t + b % 3], b >= 3, N, eol) == j)
+          contrib[pos++] = contrib_code(t, false, a | virt_row, b % 3 | (b >= 3 ? kVirtual : 0));
     }
-    for (int q = hptr[i]; q < hptr[i + 1]; ++q) {
+    for (int q = hptr[base]; q < hptr[base + 1]; ++q) {
       const int e = hlist[q] >> 2, a = hlist[q] & 3;
-      for (int b = 0; b < 4; ++b)
-        if (hinge[4 * e + b] == j) contrib[pos++] = contrib_code(e, true, a, b);
+      for (int b = 0; b < 8; ++b)
+        if (elem_node(hinge[4 * e + b % 4], b >= 4, N, eol) == j)
+          contrib[pos++] = contrib_code(e, true, a | virt_row, b % 4 | (b >= 4 ? kVirtual : 0));
     }
   }
   diag[i] = dg;
   if (dg < 0) atomicOr(err, kErrIsolated);
-  if (i == N - 1) cptr[rowptr[N]] = pos;
+  if (i == Ntot - 1) cptr[rowptr[Ntot]] = pos;
 }
 
 int grid(long long n) { return int((n + kT - 1) / kT); }
@@ -352,9 +382,11 @@ void scan(const int *in, int n, int *out, DevBuf<int> &bsum, cudaStream_t s) {
 
 std::string build_topology_device(TopoScratch *&w, int N, const int *tri_d, int n_tri,
                                   const int *hinge_d, int n_hinge, DevTopology &T,
-                                  cudaStream_t s, long long &launches) {
-  if (N <= 0 || n_tri <= 0 || n_hinge < 0) return "bad sizes";
-  if (int64_t(n_tri) + n_hinge >= (int64_t(1) << 26)) return "too many elements";
+                                  cudaStream_t s, long long &launches, int n_eol) {
+  if (N <= 0 || n_tri <= 0 || n_hinge < 0 || n_eol < 0 || n_eol > N) return "bad sizes";
+  const int Nt = N + n_eol;  // rows: nodes, then the EOL nodes' Eulerian nodes
+  const int *eol = n_eol > 0 ? T.eol.p : nullptr, *eol_node = n_eol > 0 ? T.eol_node.p : nullptr;
+  if (n_tri >= (1 << 24) || n_hinge >= (1 << 24)) return "too many elements";
   if (!w) w = new TopoScratch();
   TopoScratch &W = *w;
 #define TG(expr)                                                   \
@@ -362,22 +394,22 @@ std::string build_topology_device(TopoScratch *&w, int N, const int *tri_d, int 
     cudaError_t e_ = (expr);                                       \
     if (e_ != cudaSuccess) return std::string(#expr ": ") + cudaGetErrorString(e_); \
   } while (0)
-  const int nb_max = grid(N + 1) + 1;
+  const int nb_max = grid(Nt + 1) + 1;
   TG(W.fcnt.resize(N));
   TG(W.hcnt.resize(N));
   TG(W.fcur.resize(N + 1));
   TG(W.hcur.resize(N + 1));
   TG(W.hptr.resize(N + 1));
-  TG(W.ncol.resize(N));
-  TG(W.ncon.resize(N));
-  TG(W.cbase.resize(N + 1));
+  TG(W.ncol.resize(Nt));
+  TG(W.ncon.resize(Nt));
+  TG(W.cbase.resize(Nt + 1));
   TG(W.bsum.resize(nb_max + 1));
   TG(W.err.resize(1));
   TG(W.hlist.resize(size_t(4) * std::max(1, n_hinge)));
   TG(T.nf_ptr.resize(N + 1));
   TG(T.nf_list.resize(size_t(3) * n_tri));
-  TG(T.rowptr.resize(N + 1));
-  TG(T.diag.resize(N));
+  TG(T.rowptr.resize(Nt + 1));
+  TG(T.diag.resize(Nt));
   TG(cudaMemsetAsync(W.fcnt.p, 0, sizeof(int) * N, s));
   TG(cudaMemsetAsync(W.hcnt.p, 0, sizeof(int) * N, s));
   TG(cudaMemsetAsync(W.err.p, 0, sizeof(int), s));
@@ -398,14 +430,15 @@ std::string build_topology_device(TopoScratch *&w, int N, const int *tri_d, int 
   topo_scatter_kernel<<<grid(ne), kT, 0, s>>>(tri_d, n_tri, hinge_d, n_hinge, W.fcur.p, W.hcur.p,
                                                T.nf_list.p, W.hlist.p);
   topo_sort_kernel<<<grid(N), kT, 0, s>>>(N, T.nf_ptr.p, T.nf_list.p, W.hptr.p, W.hlist.p);
-  topo_row_kernel<<<grid(N), kT, 0, s>>>(N, 0, tri_d, hinge_d, T.nf_ptr.p, T.nf_list.p, W.hptr.p,
-                                          W.hlist.p, W.ncol.p, W.ncon.p, nullptr, nullptr,
-                                          nullptr, nullptr, nullptr, nullptr, nullptr, W.err.p);
-  scan(W.ncol.p, N, T.rowptr.p, W.bsum, s);
-  scan(W.ncon.p, N, W.cbase.p, W.bsum, s);
+  topo_row_kernel<<<grid(Nt), kT, 0, s>>>(N, Nt, 0, eol, eol_node, tri_d, hinge_d, T.nf_ptr.p,
+                                           T.nf_list.p, W.hptr.p, W.hlist.p, W.ncol.p, W.ncon.p,
+                                           nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                           nullptr, W.err.p);
+  scan(W.ncol.p, Nt, T.rowptr.p, W.bsum, s);
+  scan(W.ncon.p, Nt, W.cbase.p, W.bsum, s);
   int tot[2] = {0, 0};
-  TG(cudaMemcpyAsync(&tot[0], T.rowptr.p + N, sizeof(int), cudaMemcpyDeviceToHost, s));
-  TG(cudaMemcpyAsync(&tot[1], W.cbase.p + N, sizeof(int), cudaMemcpyDeviceToHost, s));
+  TG(cudaMemcpyAsync(&tot[0], T.rowptr.p + Nt, sizeof(int), cudaMemcpyDeviceToHost, s));
+  TG(cudaMemcpyAsync(&tot[1], W.cbase.p + Nt, sizeof(int), cudaMemcpyDeviceToHost, s));
   TG(cudaMemcpyAsync(&err, W.err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   TG(cudaStreamSynchronize(s));
   launches += 2 + 3 * 4 + 1;
@@ -415,15 +448,22 @@ std::string build_topology_device(TopoScratch *&w, int N, const int *tri_d, int 
   TG(T.blk_row.resize(nblk));
   TG(T.cptr.resize(size_t(nblk) + 1));
   TG(T.contrib.resize(ncon));
-  topo_row_kernel<<<grid(N), kT, 0, s>>>(N, 1, tri_d, hinge_d, T.nf_ptr.p, T.nf_list.p, W.hptr.p,
-                                          W.hlist.p, W.ncol.p, W.ncon.p, T.rowptr.p, W.cbase.p,
-                                          T.colidx.p, T.blk_row.p, T.diag.p, T.cptr.p,
-                                          T.contrib.p, W.err.p);
+  topo_row_kernel<<<grid(Nt), kT, 0, s>>>(N, Nt, 1, eol, eol_node, tri_d, hinge_d, T.nf_ptr.p,
+                                           T.nf_list.p, W.hptr.p, W.hlist.p, W.ncol.p, W.ncon.p,
+                                           T.rowptr.p, W.cbase.p, T.colidx.p, T.blk_row.p,
+                                           T.diag.p, T.cptr.p, T.contrib.p, W.err.p);
   TG(cudaMemcpyAsync(&err, W.err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   TG(cudaStreamSynchronize(s));
   launches += 1;
   if (err & kErrIsolated) return "node without any element";
-  T.n_nodes = N;
+  TG(T.nh_ptr.resize(N + 1));
+  TG(T.nh_list.resize(size_t(4) * std::max(1, n_hinge)));
+  TG(cudaMemcpyAsync(T.nh_ptr.p, W.hptr.p, sizeof(int) * (N + 1), cudaMemcpyDeviceToDevice, s));
+  TG(cudaMemcpyAsync(T.nh_list.p, W.hlist.p, sizeof(int) * 4 * std::max(1, n_hinge),
+                     cudaMemcpyDeviceToDevice, s));
+  T.n_nodes = Nt;
+  T.n_real = N;
+  T.n_eol = n_eol;
   T.n_tri = n_tri;
   T.n_hinge = n_hinge;
   T.n_blocks = nblk;

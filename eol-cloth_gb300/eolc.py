@@ -117,7 +117,7 @@ EXPORTS = ["eolc_version", "eolc_launch_count", "eolc_create", "eolc_destroy", "
            "eolc_batch_set_jacobi_reference", "eolc_lpc_blocks", "eolc_export_obj",
            "eolc_export_obj_text", "eolc_velocity_solve_ineq", "eolc_contact_rows",
            "eolc_step_contacts", "eolc_set_topology_device", "eolc_topology_arrays",
-           "eolc_edge_list"]
+           "eolc_edge_list", "eolc_set_topology_eol"]
 
 
 def load_library(path=LIB_PATH):
@@ -190,6 +190,8 @@ def load_library(path=LIB_PATH):
                                            ctypes.c_void_p, ctypes.c_int]
     L.eolc_topology_arrays.argtypes = [_V, _I, _I, _I, _I, _I, _I, _I]
     L.eolc_edge_list.argtypes = [_V, _I, ctypes.c_int, _I]
+    L.eolc_set_topology_eol.argtypes = [_V, ctypes.c_int, _I, ctypes.c_int, _I, ctypes.c_int,
+                                        _I, ctypes.c_int]
     L.eolc_step_contacts.argtypes = [_V, _D, _D, _D, ctypes.POINTER(Material), _D,
                                      ctypes.c_double, _I, _D, ctypes.c_int, ctypes.POINTER(Box),
                                      ctypes.c_int, _D, _D, ctypes.c_int, ctypes.c_double,
@@ -266,6 +268,18 @@ class Context:
         self._check(lib.eolc_set_topology(self._h, n_nodes, _i(tri), len(tri.reshape(-1, 3)),
                                           _i(hinge), len(hinge.reshape(-1, 4))))
         self.n_nodes = n_nodes
+
+    def set_topology_eol(self, n_nodes, tri, hinge, eol_nodes):
+        """eolc_set_topology_eol: EOL node k = eol_nodes[k] gets an Eulerian
+        block row n_nodes + k (see eol_reference_index)."""
+        tri, hinge, eol = _i32(tri), _i32(hinge), _i32(eol_nodes)
+        self._tri = tri
+        self._check(lib.eolc_set_topology_eol(self._h, n_nodes, _i(tri), len(tri.reshape(-1, 3)),
+                                              _i(hinge), len(hinge.reshape(-1, 4)),
+                                              _i(eol if len(eol) else np.zeros(1, np.int32)),
+                                              len(eol)))
+        self.n_nodes = n_nodes + len(eol)  # block rows (mesh nodes + Eulerian nodes)
+        self.n_real = n_nodes
 
     def set_topology_device(self, n_nodes, tri_ptr, n_tri, hinge_ptr, n_hinge):
         """eolc_set_topology_device: tri / hinge as device addresses (e.g.
@@ -615,6 +629,15 @@ def contact_rows(contacts, n_nodes):
     m = m.value
     C = sp.csr_matrix((val[:ptr[m]], col[:ptr[m]], ptr[:m + 1]), shape=(m, 3 * n_nodes))
     return C, d[:m].copy()
+
+
+def eol_reference_index(n_real, n_eol):
+    """For each DOF of the reference's EOL system (3N Lagrangian, then 2 per
+    EOL node), its DOF in the library's extended layout (Eulerian node k's
+    DOFs 0, 1 at 3 (N + k))."""
+    k = np.arange(n_eol)
+    eul = np.stack([3 * (n_real + k), 3 * (n_real + k) + 1], 1).ravel()
+    return np.concatenate([np.arange(3 * n_real), eul]).astype(np.int64)
 
 
 def bsr_to_csr(ctx, vals):

@@ -153,12 +153,30 @@ eolc_status eolc_bsr_pattern(eolc_ctx *ctx, int *n_blocks, int *rowptr_h,
 eolc_status eolc_set_topology_device(eolc_ctx *ctx, int n_nodes,
                                      const int *tri_d, int n_tri,
                                      const int *hinge_d, int n_hinge);
+/* Topology with EOL nodes (Forces.cpp:177-329, 399-497, 580-683, 746-884:
+ * the EOL branches of Forces::fill).  eol_nodes_h[k] is the node of
+ * EoL_index k.  The block rows are the n_nodes mesh nodes followed by one
+ * Eulerian node per EOL node: its DOFs 0 and 1 are the reference's Eulerian
+ * DOFs 3 n_nodes + 2k and + 1, DOF 2 is padding (zero in f, M and MDK except
+ * a 1 on MDK's diagonal; every solve pins it).  On such a topology
+ * eolc_forces_fill takes x_h (3 n_nodes) and X_h (2 n_nodes) and returns f
+ * (3 (n_nodes + n_eol)), M and MDK over the extended rows, with the
+ * reference's EOL blocks (-F' K, -K F, F' K F with the element's
+ * deformation gradient; a hinge's F is the mean of its two faces') and
+ * forces (-F' f on the Eulerian DOFs; a hinge with an EOL vertex also adds
+ * its bending force); eolc_velocity_solve takes b, v and the fixed DOFs in
+ * the extended layout.  Steps, collisions, export, batches, contact rows and
+ * the learned preconditioner refuse EOL topologies (EOLC_BAD_ARG). */
+eolc_status eolc_set_topology_eol(eolc_ctx *ctx, int n_nodes, const int *tri_h,
+                                  int n_tri, const int *hinge_h, int n_hinge,
+                                  const int *eol_nodes_h, int n_eol);
 /* The device topology for inspection: any array pointer may be NULL.
  * sizes: n_nodes, n_blocks, contributions, node -> face entries (3 n_tri).
  * rowptr/colidx: eolc_bsr_pattern's; cptr (n_blocks + 1) and contrib: the
  * element contributions of every block in the reference's insertion order
- * (faces ascending, then hinges; code = element << 5 | hinge << 4 |
- * row vertex << 2 | column vertex); nf_ptr (n_nodes + 1) / nf_list: each
+ * (faces ascending, then hinges; code = element << 7 | hinge << 6 |
+ * row << 3 | column, row / column = local vertex, + 4 for its Eulerian
+ * node); nf_ptr (n_nodes + 1) / nf_list: each
  * node's faces ascending, code face << 2 | local vertex. */
 eolc_status eolc_topology_arrays(eolc_ctx *ctx, int *rowptr_h, int *colidx_h,
                                  int *cptr_h, int *contrib_h, int *nf_ptr_h,

@@ -7,7 +7,7 @@ block in the order the reference inserts its triplets (Forces.cpp:331-930:
 faces in order, each with its 3x3 (row vertex, column vertex) blocks, then
 hinges in order with their 4x4; setFromTriplets sums duplicates in that
 order, Forces.cpp:925-929), and each node's faces in order.  Contribution
-code: element << 5 | hinge << 4 | row vertex << 2 | column vertex; face
+code: element << 7 | hinge << 6 | row vertex << 3 | column vertex; face
 entry: face << 2 | local vertex.
 """
 import numpy as np
@@ -23,8 +23,8 @@ def build(n_nodes, tri, hinge):
     rows = np.concatenate([tri[:, ta.ravel()].ravel(), hinge[:, ha.ravel()].ravel()])
     cols = np.concatenate([tri[:, tb.ravel()].ravel(), hinge[:, hb.ravel()].ravel()])
     codes = np.concatenate([
-        (np.arange(T)[:, None] << 5 | ta.ravel()[None, :] << 2 | tb.ravel()[None, :]).ravel(),
-        (np.arange(H)[:, None] << 5 | 16 | ha.ravel()[None, :] << 2 | hb.ravel()[None, :]).ravel()])
+        (np.arange(T)[:, None] << 7 | ta.ravel()[None, :] << 3 | tb.ravel()[None, :]).ravel(),
+        (np.arange(H)[:, None] << 7 | 64 | ha.ravel()[None, :] << 3 | hb.ravel()[None, :]).ravel()])
     seq = np.arange(len(rows))
     order = np.lexsort((seq, cols, rows))  # stable in insertion order per block
     r, c, code = rows[order], cols[order], codes[order]

@@ -24,9 +24,9 @@ def _check(s):
         row = int(np.searchsorted(t["rowptr"], b, side="right") - 1)
         col = int(t["colidx"][b])
         codes = t["contrib"][t["cptr"][b]:t["cptr"][b + 1]]
-        want = [(f << 5) | (a << 2) | c for f in range(len(tri)) for a in range(3)
+        want = [(f << 7) | (a << 3) | c for f in range(len(tri)) for a in range(3)
                 for c in range(3) if tri[f, a] == row and tri[f, c] == col]
-        want += [(e << 5) | 16 | (a << 2) | c for e in range(len(hinge)) for a in range(4)
+        want += [(e << 7) | 64 | (a << 3) | c for e in range(len(hinge)) for a in range(4)
                  for c in range(4) if hinge[e, a] == row and hinge[e, c] == col]
         assert codes.tolist() == want
     for i in range(0, n, max(1, n // 100)):

@@ -549,6 +549,48 @@ def run_refresh(args, local_rank, stream, sc, reps=3):
     return out
 
 
+def run_eol(args, local_rank, stream, sc, reps=5):
+    """Forces::fill with EOL nodes (eolc_set_topology_eol): the 256x256-quad
+    sheet with its middle row of nodes (257) as EOL nodes, FP64, host
+    arrays in and out, against the same fill without EOL nodes and the
+    oracle's EOL fill on one core."""
+    import numpy as np
+    import torch
+    import eolc
+    import oracle as O
+    r = QUADS + 1
+    eol = (r // 2) * r + np.arange(r)  # node k = i r + j; the row i = r // 2
+    rng = np.random.default_rng(8)
+    x = sc["x"] + rng.normal(0, 1e-3, sc["x"].size)
+    mat = eolc.Material(**MAT)
+    out = {"workload": "256x256-quad sheet, %d EOL nodes (one row), FP64 f, M and MDK "
+                       "(host arrays)" % len(eol)}
+    for label in ("plain", "eol"):
+        ctx = eolc.Context(local_rank)
+        ctx.set_stream(stream.cuda_stream)
+        if label == "eol":
+            ctx.set_topology_eol(sc["n"], sc["tri"], sc["hinge"], eol)
+        else:
+            ctx.set_topology(sc["n"], sc["tri"], sc["hinge"])
+        ctx.forces_fill(x, sc["X"], mat, GRAV, H, eolc.PREC_FP64)
+        ts = []
+        for k in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ctx.forces_fill(x, sc["X"], mat, GRAV, H, eolc.PREC_FP64)
+            ts.append(time.perf_counter() - t0)
+        out[label + "_ms"] = round(1e3 * float(np.median(ts)), 3)
+        out[label + "_blocks"] = len(ctx.bsr_pattern()[1])
+    t0 = time.perf_counter()
+    O.ForcesEOL(x, sc["X"], sc["tri"], sc["hinge"], O.material(), GRAV, H, eol)
+    cpu_s = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": 1.0 / cpu_s, "unit": "fills/s", "cores": 1, "kind": "port",
+                           "sample": "one oracle Forces::fill with the same EOL nodes"}
+    out["note"] = ("wall time of eolc_forces_fill including the upload of x, X and the "
+                   "download of f, M and MDK")
+    return out
+
+
 def run_ours(args, rank, world, local_rank):
     import numpy as np
     import torch
@@ -686,6 +728,8 @@ def run_ours(args, rank, world, local_rank):
         line["contact_step"] = run_contacts(args, local_rank, stream, flush)
     if world == 1 and not args.no_refresh:
         line["topology_refresh"] = run_refresh(args, local_rank, stream, sc)
+    if world == 1 and not args.no_eol:
+        line["eol_fill"] = run_eol(args, local_rank, stream, sc)
     if world == 1 and not args.no_batch:
         line["batched"] = run_batched(args, local_rank, stream, flush)
         line["batched_delaunay_learned"] = run_delaunay(args, local_rank, stream, flush)
@@ -707,6 +751,7 @@ def main():
     ap.add_argument("--no-export", action="store_true", help="skip the OBJ export line")
     ap.add_argument("--no-contacts", action="store_true", help="skip the contact-step line")
     ap.add_argument("--no-refresh", action="store_true", help="skip the topology-refresh line")
+    ap.add_argument("--no-eol", action="store_true", help="skip the EOL-fill line")
     ap.add_argument("--batch-sheets", type=int, default=256)
     ap.add_argument("--delaunay-meshes", type=int, default=64)
     args = ap.parse_args()

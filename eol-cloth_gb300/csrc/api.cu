@@ -575,6 +575,7 @@ eolc_status topology_from_device(eolc_ctx *ctx, int n_nodes, int n_tri, int n_hi
 // Drops every plan, graph and buffer that depends on the old topology.
 eolc_status reset_after_topology(eolc_ctx *ctx, cudaStream_t s) {
   ctx->inst_mat.clear();
+  ctx->contact_lambda.clear();
   free_collide_work(ctx->cd_work);
   free_export_work(ctx->ex_work);
   ctx->cd_work = nullptr;
@@ -1066,12 +1067,38 @@ eolc_status eolc_step_contacts(eolc_ctx *ctx, double *x_h, const double *X_h, do
   // Forces::fill, then the QP (GeneralizedSolver::velocitySolve), x += h v
   if ((st = assemble(ctx, *mat, grav, h, opts->precision, false, true, s)) != EOLC_OK) return st;
   ctx->last_precision = opts->precision;
-  st = ineq_solve_device(ctx, m, ptr.data(), col.data(), val.data(), d.data(), opts, nullptr,
-                         info);
+  // warm start: a contact present at the previous step (same obstacle,
+  // kind and vertices) starts from that step's multiplier
+  std::vector<std::array<int, 9>> keys;
+  keys.reserve(m);
+  for (int k = 0; k < nc; ++k) {
+    const eolc_contact &c = cons[k];
+    const bool row = (c.count1 == 3 && c.count2 == 1) || (c.count1 == 2 && c.count2 == 2) ||
+                     (c.count1 == 1 && c.count2 == 3);  // the kinds eolc_contact_rows keeps
+    if (!row) continue;
+    keys.push_back({c.source, c.count1, c.count2, c.verts1[0], c.verts1[1], c.verts1[2],
+                    c.verts2[0], c.verts2[1], c.verts2[2]});
+  }
+  std::vector<double> lam0(std::max(1, m), 0.0), lam(std::max(1, m), 0.0);
+  for (int i = 0; i < m; ++i) {
+    auto it = ctx->contact_lambda.find(keys[i]);
+    if (it != ctx->contact_lambda.end()) lam0[i] = it->second;
+  }
+  st = ineq_solve_device(ctx, m, ptr.data(), col.data(), val.data(), d.data(), opts, lam.data(),
+                         info, lam0.data());
   if (st != EOLC_OK) return st;
+  ctx->contact_lambda.clear();
+  for (int i = 0; i < m; ++i)
+    if (lam[i] > 0) ctx->contact_lambda[keys[i]] = lam[i];
   integrate_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, h, ctx->v.p, ctx->x.p);
   ctx->launches += 1;
   return eolc_state_download(ctx, x_h, v_h);
+}
+
+eolc_status eolc_clear_contact_multipliers(eolc_ctx *ctx) {
+  if (!ctx) return EOLC_BAD_ARG;
+  ctx->contact_lambda.clear();
+  return EOLC_OK;
 }
 
 int eolc_batch_num_configs(void) { return batch_num_configs(); }

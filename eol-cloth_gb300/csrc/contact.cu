@@ -309,7 +309,8 @@ namespace eolc {
 eolc_status ineq_solve_device(eolc_ctx *ctx, int n_ineq, const int *ineq_ptr_h,
                               const int *ineq_col_h, const double *ineq_val_h,
                               const double *bineq_h, const eolc_solve_opts *opts,
-                              double *lambda_h, eolc_ineq_info *info) {
+                              double *lambda_h, eolc_ineq_info *info,
+                              const double *lambda0_h) {
   if (n_ineq < 0 || (n_ineq > 0 && (!ineq_ptr_h || !ineq_col_h || !ineq_val_h || !bineq_h)))
     return bad(ctx, "null inequality rows");
   const HostTopology *Hp = host_topology(ctx);
@@ -416,6 +417,8 @@ eolc_status ineq_solve_device(eolc_ctx *ctx, int n_ineq, const int *ineq_ptr_h,
   IQ_CHECK(W.part.resize(size_t(2) * nbr));
   W.part_h.resize(size_t(2) * nbr);
   IQ_CHECK(cudaMemsetAsync(W.lam.p, 0, sizeof(double) * std::max(1, m), s));
+  if (lambda0_h && m > 0)  // warm start: the active set starts from these
+    IQ_CHECK(cudaMemcpyAsync(W.lam.p, lambda0_h, sizeof(double) * m, cudaMemcpyHostToDevice, s));
   IQ_CHECK(cudaMemsetAsync(W.act.p, 0, std::max(1, m), s));
   IQ_CHECK(cudaMemcpyAsync(W.bpen.p, ctx->b.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
   // the learned network approximates the inverse of MDK, not of the
@@ -524,6 +527,19 @@ eolc_status ineq_solve_device(eolc_ctx *ctx, int n_ineq, const int *ineq_ptr_h,
         ac.rel_tol = stol * qn / rn;
         eolc_solve_info si{};
         st = solve_with_args(ctx, opts, ac, &si, s);
+        if (st == EOLC_BREAKDOWN && opts->precond != EOLC_PC_BLOCK_JACOBI) {
+          // a breakdown of the preconditioned recurrence on a strongly
+          // penalised system: the same correction solve once more with block
+          // Jacobi (the contact terms sit in its diagonal blocks)
+          eolc_solve_opts bj = *opts;
+          bj.precond = EOLC_PC_BLOCK_JACOBI;
+          PcgArgs ab = ac;
+          ab.precond = EOLC_PC_BLOCK_JACOBI;
+          I.iterations += si.iterations;
+          si = eolc_solve_info{};
+          st = solve_with_args(ctx, &bj, ab, &si, s);
+          I.fallbacks += 1;
+        }
         I.iterations += si.iterations;
         I.rel_res = si.rel_res * rn / std::max(qn, 1e-300);
         I.solve_kernel_ms += si.solve_kernel_ms;

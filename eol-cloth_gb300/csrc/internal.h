@@ -3,8 +3,10 @@
 
 #include <cuda_runtime.h>
 
+#include <array>
 #include <cstdint>
 #include <cstdio>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -234,11 +236,12 @@ PcgArgs default_pcg_args(eolc_ctx *ctx, const eolc_solve_opts *o);
 eolc_status solve_with_args(eolc_ctx *ctx, const eolc_solve_opts *o, const PcgArgs &a,
                             eolc_solve_info *info, cudaStream_t s);
 // The contact QP (contact.cu) on the device state: MDK, b, pins, v (initial
-// guess in, solution out).
+// guess in, solution out); lambda0_h (optional): initial multipliers.
 eolc_status ineq_solve_device(eolc_ctx *ctx, int n_ineq, const int *ineq_ptr_h,
                               const int *ineq_col_h, const double *ineq_val_h,
                               const double *bineq_h, const eolc_solve_opts *opts,
-                              double *lambda_h, eolc_ineq_info *info);
+                              double *lambda_h, eolc_ineq_info *info,
+                              const double *lambda0_h = nullptr);
 // Uploads the pinned DOFs, their values and the right-hand side b.
 eolc_status prepare_pins_rhs(eolc_ctx *ctx, const double *b_h, const int *fixed_dofs_h,
                              const double *beq_h, int n_fixed, cudaStream_t s);
@@ -274,6 +277,9 @@ struct eolc_ctx {
   cudaEvent_t aux_fork = nullptr, aux_join = nullptr;
   std::vector<int> host_tri;  // triangle list of the current topology
   std::vector<int> eol_nodes; // node of every EoL_index (EOL topologies)
+  // multipliers of the last eolc_step_contacts, by contact (source, kinds,
+  // obstacle and cloth vertices): the next step's QP starts from them
+  std::map<std::array<int, 9>, double> contact_lambda;
   eolc_lpc *lpc = nullptr;    // attached learned preconditioner (not owned)
   const eolc_lpc *lpc_cached = nullptr;  // network whose G the resident solver holds
   int lpc_uses = 0;           // solves that G has served

@@ -67,7 +67,7 @@ class IneqInfo(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("solves", ctypes.c_int), ("outer", ctypes.c_int),
                 ("iterations", ctypes.c_int), ("n_active", ctypes.c_int),
                 ("max_violation", ctypes.c_double), ("rel_res", ctypes.c_double),
-                ("solve_kernel_ms", ctypes.c_double)]
+                ("solve_kernel_ms", ctypes.c_double), ("fallbacks", ctypes.c_int)]
 
 
 class BatchInfo(ctypes.Structure):
@@ -117,7 +117,7 @@ EXPORTS = ["eolc_version", "eolc_launch_count", "eolc_create", "eolc_destroy", "
            "eolc_batch_set_jacobi_reference", "eolc_lpc_blocks", "eolc_export_obj",
            "eolc_export_obj_text", "eolc_velocity_solve_ineq", "eolc_contact_rows",
            "eolc_step_contacts", "eolc_set_topology_device", "eolc_topology_arrays",
-           "eolc_edge_list", "eolc_set_topology_eol"]
+           "eolc_edge_list", "eolc_set_topology_eol", "eolc_clear_contact_multipliers"]
 
 
 def load_library(path=LIB_PATH):
@@ -190,6 +190,7 @@ def load_library(path=LIB_PATH):
                                            ctypes.c_void_p, ctypes.c_int]
     L.eolc_topology_arrays.argtypes = [_V, _I, _I, _I, _I, _I, _I, _I]
     L.eolc_edge_list.argtypes = [_V, _I, ctypes.c_int, _I]
+    L.eolc_clear_contact_multipliers.argtypes = [_V]
     L.eolc_set_topology_eol.argtypes = [_V, ctypes.c_int, _I, ctypes.c_int, _I, ctypes.c_int,
                                         _I, ctypes.c_int]
     L.eolc_step_contacts.argtypes = [_V, _D, _D, _D, ctypes.POINTER(Material), _D,
@@ -389,6 +390,9 @@ class Context:
                                     threshold, ctypes.byref(opts), ctypes.byref(info))
         self._check(st)
         return info
+
+    def clear_contact_multipliers(self):
+        self._check(lib.eolc_clear_contact_multipliers(self._h))
 
     def step(self, x, X, v, mat, grav, h, fixed_dofs, fixed_vel, opts=None):
         """Cloth::step on host arrays; x, v updated in place."""

@@ -233,6 +233,8 @@ typedef struct {
   double max_violation; /* max(0, Aineq v - bineq) / max|v| at the end     */
   double rel_res;       /* relative residual of the last linear solve      */
   double solve_kernel_ms; /* device time of the PCG kernels, summed        */
+  int fallbacks;        /* linear solves retried with block Jacobi after a
+                           breakdown of the requested preconditioner       */
 } eolc_ineq_info;
 eolc_status eolc_velocity_solve_ineq(eolc_ctx *ctx, const double *b_h,
                                      const int *fixed_dofs_h,
@@ -414,8 +416,13 @@ eolc_status eolc_contact_rows(const eolc_contact *contacts, int n_contacts,
  * eolc_step: pins beq = 0.99 v + c, CD2 of the step's positions against the
  * boxes and point obstacles (as eolc_cd2), the inequality rows of
  * Constraints.cpp:422-468 (eolc_contact_rows), Forces::fill, the QP of
- * eolc_velocity_solve_ineq warm-started from v, x += h v.  info (may be
- * NULL) reports the QP solve. */
+ * eolc_velocity_solve_ineq warm-started from v and, for every contact that
+ * the previous call on this context also had (same obstacle, kind and
+ * vertices), from its multiplier, x += h v.  info (may be NULL) reports the
+ * QP solve. */
+/* Forgets the multipliers eolc_step_contacts carries to the next call (after
+ * a jump in the scene, or to time cold QP solves). */
+eolc_status eolc_clear_contact_multipliers(eolc_ctx *ctx);
 eolc_status eolc_step_contacts(eolc_ctx *ctx, double *x_h, const double *X_h,
                                double *v_h, const eolc_material *mat,
                                const double grav[3], double h,

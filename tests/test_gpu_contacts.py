@@ -201,3 +201,37 @@ def test_contact_steps_track_the_oracle(eolc, precision, tol):
         x, v = xg, vg
     print("rows / active / solves per step:", rows)
     assert all(m > 0 for m, _, _ in rows)
+
+
+def test_carried_multipliers_change_the_path_not_the_answer(eolc):
+    """eolc_step_contacts starts each persisting contact from the previous
+    call's multiplier: the same step repeated from the same state gives the
+    same velocities (FP64, 1e-8) in fewer linear solves."""
+    quads = 24
+    x0, X, tri, center, snaps = scenes.drape_positions(quads, 40)
+    n = len(x0) // 3
+    hinge = O.hinges(n, tri)
+    box = O.axis_box(center, (0.4, 0.4, 0.2))
+    ids = O.corner_ids(quads + 1, quads + 1)
+    fixed = np.array([3 * ids[k] + c for k in (3, 4) for c in range(3)], np.int32)
+    ctx = eolc.Context(0)
+    ctx.set_topology(n, tri, hinge)
+    mat = eolc.Material(**scenes.material_c1())
+    v0 = np.random.default_rng(4).normal(0, 0.02, 3 * n)
+    v0[2::3] -= 0.4
+    opts = eolc.SolveOpts(rel_tol=1e-10, precision=eolc.PREC_FP64)
+    out = []
+    for k in range(2):
+        x, v = snaps[14].copy(), v0.copy()
+        info = ctx.step_contacts(x, X, v, mat, scenes.GRAV, scenes.H, fixed, np.zeros(len(fixed)),
+                                 boxes=[eolc.Box(box.dim, box.E1)], threshold=1e-3, opts=opts)
+        assert info.status == eolc.OK
+        out.append((v, info.solves))
+    print("solves cold %d, warm %d" % (out[0][1], out[1][1]))
+    assert _relmax(out[1][0], out[0][0]) <= 1e-8
+    assert out[1][1] < out[0][1]
+    ctx.clear_contact_multipliers()
+    x, v = snaps[14].copy(), v0.copy()
+    info = ctx.step_contacts(x, X, v, mat, scenes.GRAV, scenes.H, fixed, np.zeros(len(fixed)),
+                             boxes=[eolc.Box(box.dim, box.E1)], threshold=1e-3, opts=opts)
+    assert info.solves == out[0][1]

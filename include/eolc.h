@@ -4,9 +4,13 @@
  * One library (libeolc.so) replaces, for the non-EOL, non-remeshing path:
  *   Forces::fill                     src/Forces.cpp:912-930   (Forces.h:40)
  *   GeneralizedSolver::velocitySolve src/GeneralizedSolver.cpp:107-173
- *                                    (GeneralizedSolver.h:26-30), for the
- *                                    equality-constrained (pinned-corner) case
- *   Cloth::solve / Cloth::step       src/Cloth.cpp:343-413 (minus dumps)
+ *                                    (GeneralizedSolver.h:26-30): pinned DOFs,
+ *                                    and the contact QP with inequality rows
+ *   Constraints::fill contact rows   src/Constraints.cpp:422-468
+ *   Cloth::solve / Cloth::step       src/Cloth.cpp:343-413 (minus dumps),
+ *                                    with or without contacts
+ *   Forces::fill EOL branches        src/Forces.cpp:127-329, 399-497,
+ *                                    541-683, 746-884
  *   CD2 / btc::boxTriCollision /     src/Collisions.cpp:55-78,
  *   btc::pointTriCollision           src/boxTriCollision.cpp:602-1224
  *   BrenderManager::exportBrender /  src/BrenderManager.cpp:34-84,

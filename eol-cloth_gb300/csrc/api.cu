@@ -99,9 +99,19 @@ eolc_status set_pins(eolc_ctx *ctx, const int *dofs_h, const double *vel_h,
   return EOLC_OK;
 }
 
+// Eulerian node k repeats the position and material coordinates of its EOL
+// node (only the resident solver's partition reads them).
+__global__ void eol_positions_kernel(int n_real, int n_eol, const int *eol_node, double *x,
+                                     double *X) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_eol) return;
+  const int v = eol_node[k];
+  for (int c = 0; c < 3; ++c) x[3 * (n_real + k) + c] = x[3 * v + c];
+  for (int c = 0; c < 2; ++c) X[2 * (n_real + k) + c] = X[2 * v + c];
+}
+
 // Positions x (3 n_real) and material coordinates X (2 n_real) of the mesh
-// nodes; an Eulerian node's slots repeat its EOL node's (only the resident
-// solver's partition reads them).
+// nodes, then the Eulerian nodes' copies.
 eolc_status upload_positions(eolc_ctx *ctx, const double *x_h, const double *X_h,
                              cudaStream_t s) {
   const DevTopology &T = ctx->topo;
@@ -110,12 +120,11 @@ eolc_status upload_positions(eolc_ctx *ctx, const double *x_h, const double *X_h
                                                 cudaMemcpyHostToDevice, s));
   if (X_h) EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->X.p, X_h, sizeof(double) * 2 * n,
                                                 cudaMemcpyHostToDevice, s));
-  for (size_t k = 0; k < ctx->eol_nodes.size(); ++k) {
-    const int v = ctx->eol_nodes[k];
-    if (x_h) EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->x.p + 3 * (n + k), ctx->x.p + 3 * v,
-                                                  sizeof(double) * 3, cudaMemcpyDeviceToDevice, s));
-    if (X_h) EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->X.p + 2 * (n + k), ctx->X.p + 2 * v,
-                                                  sizeof(double) * 2, cudaMemcpyDeviceToDevice, s));
+  if (T.n_eol > 0) {
+    eol_positions_kernel<<<(T.n_eol + 127) / 128, 128, 0, s>>>(n, T.n_eol, T.eol_node.p,
+                                                               ctx->x.p, ctx->X.p);
+    ctx->launches += 1;
+    EOLC_CHECK_CUDA(ctx, cudaGetLastError());
   }
   return EOLC_OK;
 }
@@ -750,7 +759,6 @@ eolc_status eolc_set_topology_batched(eolc_ctx *ctx, int n_inst, const int *node
   EOLC_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
   ctx->host_tri.assign(tri_h, tri_h + size_t(n_tri) * 3);
   ctx->node_off.assign(node_off_h, node_off_h + n_inst + 1);
-  ctx->eol_nodes.clear();
   return reset_after_topology(ctx, s);
 }
 
@@ -776,7 +784,6 @@ eolc_status eolc_set_topology_device(eolc_ctx *ctx, int n_nodes, const int *tri_
   EOLC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->node_inst.p, 0, sizeof(int) * n_nodes, s));
   ctx->host_tri.clear();  // downloaded on first use
   ctx->node_off.assign({0, n_nodes});
-  ctx->eol_nodes.clear();
   return reset_after_topology(ctx, s);
 }
 
@@ -812,7 +819,6 @@ eolc_status eolc_set_topology_eol(eolc_ctx *ctx, int n_nodes, const int *tri_h, 
   EOLC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->node_inst.p, 0, sizeof(int) * T.n_nodes, s));
   ctx->host_tri.assign(tri_h, tri_h + size_t(n_tri) * 3);
   ctx->node_off.assign({0, T.n_nodes});
-  ctx->eol_nodes.assign(eol_nodes_h, eol_nodes_h + n_eol);
   return reset_after_topology(ctx, s);
 }
 

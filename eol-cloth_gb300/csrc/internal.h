@@ -276,7 +276,6 @@ struct eolc_ctx {
   cudaStream_t aux = nullptr;
   cudaEvent_t aux_fork = nullptr, aux_join = nullptr;
   std::vector<int> host_tri;  // triangle list of the current topology
-  std::vector<int> eol_nodes; // node of every EoL_index (EOL topologies)
   // multipliers of the last eolc_step_contacts, by contact (source, kinds,
   // obstacle and cloth vertices): the next step's QP starts from them
   std::map<std::array<int, 9>, double> contact_lambda;

@@ -449,7 +449,7 @@ eolc_status eolc_step_contacts(eolc_ctx *ctx, double *x_h, const double *X_h,
  * produces, minimising sum_k |F (G A w_k - w_k)|^2 / |F w_k|^2 over probe
  * vectors w_k.  The reference has no preconditioner beyond Eigen's default
  * Jacobi (GeneralizedSolver.cpp:123-126); point Jacobi stays the fallback
- * (eolc_solve_opts.fallback_factor) and the judge (same FP64 residual). */
+ * (eolc_solve_opts.fallback_factor) and the yardstick (same FP64 residual). */
 typedef struct eolc_lpc eolc_lpc;
 eolc_status eolc_lpc_create(eolc_lpc **out, int device, unsigned seed);
 void eolc_lpc_destroy(eolc_lpc *lpc);

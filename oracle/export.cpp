@@ -5,7 +5,7 @@
 // the triangle list.  Node normals restate ArcSim normal<WS>
 // (geometry.cpp:302-316) in FP64 with contraction off.
 //
-// TEST INFRASTRUCTURE ONLY (the checker of the device export).
+// TEST INFRASTRUCTURE ONLY (what the device export is compared with).
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>

@@ -1,7 +1,7 @@
 /*
  * oracle.h — CPU restatement of the reference's hot path.  TEST
  * INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and bench.py's CPU
- * baseline leg call it as the checker.  The product library (libeolc.so)
+ * baseline leg call it to compare against.  The product library (libeolc.so)
  * never links, loads or calls anything here.
  *
  * Parity pins: the element routines are checked against the reference's own

@@ -1,7 +1,7 @@
 """ctypes front end of the CPU oracle (oracle/*.cpp -> oracle/liboracle.so).
 
 TEST INFRASTRUCTURE ONLY.  tests/, __graft_entry__.smoke() and bench.py's CPU
-baseline leg use it as the checker; the product library never imports it.
+baseline leg use it to compare against; the product library never imports it.
 The C++ sources restate the reference's hot path (file:line citations in each
 function); see oracle/oracle.h for what is pinned and how.
 """

@@ -1,5 +1,5 @@
 """Oracle of the contact-constrained velocity solve — TEST INFRASTRUCTURE ONLY
-(tests/ and bench.py's CPU baseline use it as the checker).
+(tests/ and bench.py's CPU baseline compare against it).
 
 GeneralizedSolver::velocitySolve with collisions (GeneralizedSolver.cpp:
 138-170) hands Mosek or Gurobi the QP of QuadProg.h (MATLAB quadprog

@@ -1,6 +1,6 @@
 """Batched stepping: many sheets of uneven size in one persistent launch.
 
-The judge of every batched result is the one-sheet path (itself checked
+Every batched result is compared with the one-sheet path (itself checked
 against the oracle in test_gpu_parity.py): from the same state, a batched
 step of every instance must give the velocities and positions of a one-sheet
 step of that instance with its own material, to the tolerance the two

@@ -1,6 +1,6 @@
 """GPU parity tests through the C ABI (libeolc.so) against the CPU oracle.
 
-Tolerances (stated per the spec contract):
+Tolerances:
   * FP64 path: f, M and MDK BSR values within 1e-10 relative (max-norm);
     velocities of an FP64 solve at tol 1e-12 within 1e-10 of the oracle's
     direct solution.

@@ -1,7 +1,7 @@
 """Patch-local preconditioner (EOLC_PC_PATCH): same FP64 relative residual as
 Jacobi-PCG, the same velocities, and far fewer iterations.
 
-The judge is the Jacobi path (itself checked against the oracle's Eigen-style
+The comparison is the Jacobi path (itself checked against the oracle's Eigen-style
 CG and direct solve in test_gpu_parity.py) and, on the small sheet, the
 oracle's direct solve.
 """

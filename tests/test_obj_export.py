@@ -25,7 +25,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 @pytest.fixture(scope="module")
-def fmt_checker(tmp_path_factory):
+def fmt_prog(tmp_path_factory):
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(nvcc):
         pytest.skip("nvcc not available")
@@ -37,8 +37,8 @@ def fmt_checker(tmp_path_factory):
     return exe
 
 
-def test_formatter_matches_printf(fmt_checker):
-    out = subprocess.run([fmt_checker, "300000"], capture_output=True, text=True)
+def test_formatter_matches_printf(fmt_prog):
+    out = subprocess.run([fmt_prog, "300000"], capture_output=True, text=True)
     print(out.stdout.strip())
     assert out.returncode == 0, out.stdout + out.stderr
     assert "mismatches 0" in out.stdout

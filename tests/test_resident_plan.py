@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 @pytest.fixture(scope="module")
-def checker(tmp_path_factory):
+def plan_prog(tmp_path_factory):
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(nvcc):
         pytest.skip("nvcc not available")
@@ -42,7 +42,7 @@ def bsr_pattern(n, tri, hinge):
     return m.indptr.astype(np.int32), m.indices.astype(np.int32)
 
 
-def run(checker, tmp_path, s):
+def run(plan_prog, tmp_path, s):
     rp, ci = bsr_pattern(s["n"], s["tri"], s["hinge"])
     path = tmp_path / "pattern.bin"
     with open(path, "wb") as f:
@@ -50,17 +50,17 @@ def run(checker, tmp_path, s):
         rp.tofile(f)
         ci.tofile(f)
         np.asarray(s["X"], np.float64).reshape(-1).tofile(f)
-    out = subprocess.run([checker, str(path)], capture_output=True, text=True)
+    out = subprocess.run([plan_prog, str(path)], capture_output=True, text=True)
     print(out.stdout.strip())
     assert out.returncode == 0, out.stdout + out.stderr
     assert "problems 0" in out.stdout
 
 
 @pytest.mark.parametrize("quads", [8, 20, 64, 256])
-def test_sheet_plans(checker, tmp_path, quads):
-    run(checker, tmp_path, scenes.sheet(quads))
+def test_sheet_plans(plan_prog, tmp_path, quads):
+    run(plan_prog, tmp_path, scenes.sheet(quads))
 
 
 @pytest.mark.parametrize("n_tri", [5000, 50000])
-def test_irregular_plans(checker, tmp_path, n_tri):
-    run(checker, tmp_path, scenes.delaunay_sheet(n_tri, np.random.default_rng(n_tri)))
+def test_irregular_plans(plan_prog, tmp_path, n_tri):
+    run(plan_prog, tmp_path, scenes.delaunay_sheet(n_tri, np.random.default_rng(n_tri)))

@@ -99,3 +99,30 @@ def test_contact_rows_match_oracle():
     assert np.array_equal(C.indices, C_ref.indices)
     assert np.array_equal(C.data, C_ref.data)
     assert np.array_equal(d, d_ref)
+
+
+def test_contact_rows_capacity_and_kinds():
+    """eolc_contact_rows (host only): rows only for the three kinds of
+    Constraints.cpp:422-468, in contact order, and EOLC_CAPACITY with the
+    needed count when the buffers are short."""
+    import ctypes
+    import eolc
+    F, b, cons, n = _drape_problem(snap=9)
+    cons = list(cons)
+    lib_cons = [eolc.Contact.from_buffer_copy(bytes(c)) for c in cons]
+    odd = eolc.Contact.from_buffer_copy(bytes(cons[0]))
+    odd.count1, odd.count2 = 2, 1  # no row for this kind
+    lib_cons.insert(1, odd)
+    C, d = eolc.contact_rows(lib_cons, n)
+    assert C.shape[0] == len(cons)
+    arr = (eolc.Contact * len(lib_cons))(*lib_cons)
+    ptr = np.zeros(3, np.int32)
+    col = np.zeros(18, np.int32)
+    val = np.zeros(18)
+    dd = np.zeros(2)
+    m = ctypes.c_int()
+    st = eolc.lib.eolc_contact_rows(ctypes.cast(arr, ctypes.c_void_p), len(lib_cons), 2,
+                                    eolc._i(ptr), eolc._i(col), eolc._d(val), eolc._d(dd),
+                                    ctypes.byref(m))
+    assert st == eolc.CAPACITY and m.value == len(cons)
+    assert ptr[0] == 0 and ptr[1] > 0  # the rows that fit are written

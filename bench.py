@@ -318,6 +318,24 @@ def arm_refresh(arm):
     return 4 if arm in ("learned-r4", "patch-r4") else 1
 
 
+def max_over_ranks(value, world, dev):
+    """Largest `value` over the ranks, returned on every rank: the job takes
+    as long as its slowest replica.  `dev` holds the tensor the process
+    group's backend reduces (the rank's GPU under NCCL, the CPU under gloo)."""
+    if world == 1:
+        return value
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return t.item()
+
+
+def job_rate(world, steps, total_ms):
+    """Whole-job steps/s: each of `world` replicas runs `steps` steps and
+    the job ends with the slowest one, `total_ms` after it started."""
+    return world * steps / (total_ms / 1e3)
+
+
 def time_arm(ctx, sc, mat, opts, x_w, v_w, steps, stream, flush, world, dev, refresh=1):
     """K steps from the post-warm-up state, each bracketed by CUDA events on
     the library's stream with L2 flushed before it; max over ranks."""
@@ -345,13 +363,9 @@ def time_arm(ctx, sc, mat, opts, x_w, v_w, steps, stream, flush, world, dev, ref
         iters.append(info.iterations)
         fallback += info.used_fallback
     torch.cuda.synchronize()
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = t.item()
+    total_ms = max_over_ranks(sum(step_ms), world, dev)
     ctx.set_learned_refresh(1)
-    return {"steps_per_s": world * steps / (total_ms / 1e3), "ms_per_step": total_ms / steps,
+    return {"steps_per_s": job_rate(world, steps, total_ms), "ms_per_step": total_ms / steps,
             "mean_pcg_iters": statistics.mean(iters), "pcg_kernel_ms": statistics.mean(kern_ms),
             "assemble_ms": statistics.mean(asm_ms), "fallbacks": fallback,
             "launches": ctx.launch_count() - launches0}
@@ -673,6 +687,8 @@ def run_ours(args, rank, world, local_rank):
     vh = torch.empty(3 * sc["n"], dtype=torch.float64).pin_memory().numpy()
     Xh = torch.empty(2 * sc["n"], dtype=torch.float64).pin_memory().numpy()
     xh[:] = x_w; vh[:] = v_w; Xh[:] = sc["X"]
+    if world > 1:
+        torch.distributed.barrier()
     e2e_ms = []
     for k in range(args.steps):
         with torch.cuda.stream(stream):
@@ -681,12 +697,8 @@ def run_ours(args, rank, world, local_rank):
         t0 = time.perf_counter()
         ctx.step(xh, Xh, vh, mat, GRAV, H, sc["fixed"], sc["fixed_vel"], opts)
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
-    e2e_total = sum(e2e_ms)
-    if world > 1:
-        t = torch.tensor([e2e_total], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_total = t.item()
-    e2e_val = world * args.steps / (e2e_total / 1e3)
+    e2e_total = max_over_ranks(sum(e2e_ms), world, dev)
+    e2e_val = job_rate(world, args.steps, e2e_total)
 
     if rank != 0:
         return

@@ -79,7 +79,8 @@ eolc_status check_opts(eolc_ctx *ctx, const eolc_solve_opts *o) {
   return EOLC_OK;
 }
 
-// Uploads the fixed DOF list when it changed; rebuilds the pinned mask.
+// Uploads the fixed DOF list (and their velocities, when given) and rebuilds
+// the 3N-byte pinned mask, on every call: a step may change its pins.
 eolc_status set_pins(eolc_ctx *ctx, const int *dofs_h, const double *vel_h,
                      int n_fixed, cudaStream_t s) {
   int n = 3 * ctx->topo.n_nodes;

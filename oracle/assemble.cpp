@@ -272,7 +272,7 @@ int orc_velocity_solve(const orc_forces *F, const double *b,
 }
 
 // Dense LDL^T (no pivoting; the reduced system is symmetric) for small
-// systems: the FP64 reference solution the iterative results are judged by.
+// systems: the FP64 reference solution the iterative results are measured against.
 int orc_velocity_solve_direct(const orc_forces *F, const double *b,
                               const int *fixed_dofs, const double *beq,
                               int n_fixed, double *v_out) {

@@ -90,7 +90,7 @@ int orc_velocity_solve(const orc_forces *F, const double *b,
                        double *relres);
 
 /* Direct FP64 reference for the same reduced system (dense LDL^T on small
- * systems only, n_free <= 6000): the "truth" the CG results are judged by. */
+ * systems only, n_free <= 6000): the "truth" the CG results are measured against. */
 int orc_velocity_solve_direct(const orc_forces *F, const double *b,
                               const int *fixed_dofs, const double *beq,
                               int n_fixed, double *v_out);

@@ -53,9 +53,11 @@
 
 #include <algorithm>
 #include <functional>
+#include <memory>
 #include <cmath>
 #include <string>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "cg_common.cuh"
@@ -1617,9 +1619,35 @@ struct Bisector {
 
 }  // namespace
 
+// Allocator whose value-initialisation leaves trivially constructible
+// elements unwritten.  The plan's largest arrays are written in full by the
+// host worker threads; with it they are paged in by those threads as they
+// fill them instead of by one thread zero-filling them first.
+template <typename T>
+struct UninitAlloc : std::allocator<T> {
+  template <typename U>
+  struct rebind {
+    using other = UninitAlloc<U>;
+  };
+  UninitAlloc() = default;
+  template <typename U>
+  UninitAlloc(const UninitAlloc<U> &) noexcept {}
+  template <typename U>
+  void construct(U *p) noexcept {
+    ::new (static_cast<void *>(p)) U;
+  }
+  template <typename U, typename... A>
+  void construct(U *p, A &&...a) {
+    ::new (static_cast<void *>(p)) U(std::forward<A>(a)...);
+  }
+};
+template <typename T>
+using RawVec = std::vector<T, UninitAlloc<T>>;
+
 struct PatchPlan {
   int G = 0;
-  std::vector<int> perm, rowptr, colidx, src, tr, diag, patch_row, hnptr, hnode;
+  std::vector<int> perm, rowptr, diag, patch_row, hnptr, hnode;
+  RawVec<int> colidx, src, tr;  // every entry written by the permutation pass
   std::vector<int> fptr, fblk, rcnt, wbase;  // shared-memory image (load_patch)
   std::vector<unsigned> fword;
   // coarse space: n_agg aggregates of patches (patch_agg), the
@@ -1630,8 +1658,8 @@ struct PatchPlan {
   // per coarse block (a, b): the (patch, target) records of cpart that sum
   // to it, patches in order (cl_ptr over n_agg^2 blocks, cl_idx = c kMaxTgt + t)
   std::vector<int> cl_ptr, cl_idx;
-  std::vector<int16_t> bsl;   // per slice slot and lane: local row, or -1 - halo slot
-  std::vector<int> gsrc;      // per slice slot and lane: block in the original order, or -1
+  RawVec<int16_t> bsl;        // per slice slot and lane: local row, or -1 - halo slot
+  RawVec<int> gsrc;           // per slice slot and lane: block in the original order, or -1
   std::vector<int> slice_off, slice_len;  // per (patch, warp)
 };
 
@@ -1685,7 +1713,8 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
   std::vector<int> iperm(N);
   for (int k = 0; k < N; ++k) iperm[perm[k]] = k;
   // permuted pattern, source blocks, transposes, diagonals
-  std::vector<int> prow(N + 1, 0), pcol(NB), psrc(NB), ptr(NB), pdiag(N, -1);
+  std::vector<int> prow(N + 1, 0), pdiag(N, -1);
+  RawVec<int> pcol(NB), psrc(NB), ptr(NB);
   for (int i = 0; i < N; ++i) prow[i + 1] = prow[i] + rowptr[perm[i] + 1] - rowptr[perm[i]];
   parallel_ranges(N, T, [&](int lo, int hi, int) {
     std::vector<std::pair<int, int>> tmp;
@@ -1949,19 +1978,27 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
     out.slice_off[q] = slots;
     slots += out.slice_len[q];
   }
-  out.bsl.assign(size_t(slots) * 32, 0);
-  out.gsrc.assign(size_t(slots) * 32, -1);
+  // a patch's slots are one contiguous range: the thread that owns the patch
+  // writes the whole range (padding lanes: row 0, no source block)
+  out.bsl.resize(size_t(slots) * 32);
+  out.gsrc.resize(size_t(slots) * 32);
   parallel_ranges(G, T, [&](int c_lo, int c_hi, int) {
-  for (int c = c_lo; c < c_hi; ++c)
-    for (int w = 0; w < kWarps; ++w) {
-      const int r0 = out.patch_row[c] + 32 * w, r1 = std::min(out.patch_row[c + 1], r0 + 32);
-      const int off = out.slice_off[size_t(c) * kWarps + w];
-      for (int i = r0; i < r1; ++i)
-        for (int k = out.rowptr[i]; k < out.rowptr[i + 1]; ++k) {
-          const size_t q = size_t(off + k - out.rowptr[i]) * 32 + (i - r0);
-          out.bsl[q] = bmap[k];
-          out.gsrc[q] = out.src[k];
-        }
+    for (int c = c_lo; c < c_hi; ++c) {
+      const size_t q0 = size_t(out.slice_off[size_t(c) * kWarps]) * 32;
+      const size_t q1 = c + 1 < G ? size_t(out.slice_off[size_t(c + 1) * kWarps]) * 32
+                                  : size_t(slots) * 32;
+      std::fill(out.bsl.begin() + q0, out.bsl.begin() + q1, int16_t(0));
+      std::fill(out.gsrc.begin() + q0, out.gsrc.begin() + q1, -1);
+      for (int w = 0; w < kWarps; ++w) {
+        const int r0 = out.patch_row[c] + 32 * w, r1 = std::min(out.patch_row[c + 1], r0 + 32);
+        const int off = out.slice_off[size_t(c) * kWarps + w];
+        for (int i = r0; i < r1; ++i)
+          for (int k = out.rowptr[i]; k < out.rowptr[i + 1]; ++k) {
+            const size_t q = size_t(off + k - out.rowptr[i]) * 32 + (i - r0);
+            out.bsl[q] = bmap[k];
+            out.gsrc[q] = out.src[k];
+          }
+      }
     }
   });
   return "";

@@ -1772,6 +1772,10 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
   std::vector<Image> img(G);
   parallel_ranges(G, T, [&](int c_lo, int c_hi, int) {
     std::vector<int> seen(N, -1), hidx(N, 0);  // halo index of an outside node, per patch
+    // per-row lists, cleared for every patch (their capacity carries over)
+    std::vector<std::vector<std::pair<int, int>>> fw;
+    std::vector<std::vector<int>> tcol, spos;
+    std::vector<int> fi;
     for (int c = c_lo; c < c_hi; ++c) {
       Image &I = img[c];
       const int r0 = patch_row[c], r1 = patch_row[c + 1], np = r1 - r0;
@@ -1781,9 +1785,15 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
       }
       // per row: forward entries (block, column) internal then halo;
       // transposed entries (column j < row, ascending)
-      std::vector<std::vector<std::pair<int, int>>> fw(np);
-      std::vector<std::vector<int>> tcol(np);
-      std::vector<int> fi(np, 0);
+      fw.resize(np);
+      tcol.resize(np);
+      spos.resize(np);
+      for (int l = 0; l < np; ++l) {
+        fw[l].clear();
+        tcol[l].clear();
+        spos[l].clear();
+      }
+      fi.assign(np, 0);
       for (int i = r0; i < r1 && I.err.empty(); ++i) {
         const int l = i - r0;
         for (int k = prow[i]; k < prow[i + 1]; ++k) {
@@ -1818,7 +1828,6 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
         continue;
       }
       // slot positions
-      std::vector<std::vector<int>> spos(np);
       int nslot = 0;
       for (int w = 0; w < kWarps; ++w) {
         const int l0 = 32 * w, l1 = std::min(np, l0 + 32);

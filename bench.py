@@ -46,12 +46,11 @@ QUADS = 256
 
 def scene(quads):
     import numpy as np
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O  # mesh builders only (topology input, not the path)
+    import eolc
     r = quads + 1
-    x, X, tri = O.grid2(r, r)
-    hinge = O.hinges(r * r, tri)
-    ids = O.corner_ids(r, r)
+    x, X, tri = eolc.sheet_mesh(r, r)
+    hinge = eolc.mesh_hinges(tri)
+    ids = eolc.corner_ids(r, r)
     fixed = np.array([3 * ids[k] + c for k in (3, 4) for c in range(3)], np.int32)
     return dict(x=x, X=X, tri=tri, hinge=hinge, fixed=fixed, fixed_vel=np.zeros(len(fixed)),
                 n=r * r)
@@ -433,10 +432,10 @@ def run_contacts(args, local_rank, stream, flush, steps=5):
     import scenes as S
     x0, X, tri, center, snaps = S.drape_positions(QUADS, 40)
     n = len(x0) // 3
-    hinge = O.hinges(n, tri)
-    box = O.axis_box(center, (0.4, 0.4, 0.2))
+    hinge = eolc.mesh_hinges(tri)
+    box = O.axis_box(center, (0.4, 0.4, 0.2))  # the oracle's box, for its CD2 below
     ebox = eolc.Box(box.dim, box.E1)
-    ids = O.corner_ids(QUADS + 1, QUADS + 1)
+    ids = eolc.corner_ids(QUADS + 1, QUADS + 1)
     fixed = np.array([3 * ids[k] + c for k in (3, 4) for c in range(3)], np.int32)
     fvel = np.zeros(len(fixed))
     ctx = eolc.Context(local_rank)
@@ -505,14 +504,14 @@ def run_contacts(args, local_rank, stream, flush, steps=5):
     q = 24
     x0s, Xs, tris, cs, snapss = S.drape_positions(q, 40)
     ns = len(x0s) // 3
-    hs = O.hinges(ns, tris)
+    hs = eolc.mesh_hinges(tris)
     bs = O.axis_box(cs, (0.4, 0.4, 0.2))
     xq = snapss[9]
     F = O.Forces(xq, Xs, tris, hs, O.material(), GRAV, H)
     vq = rng.normal(0, 0.02, 3 * ns)
     vq[2::3] -= 0.4
     bq = F.rhs(vq, H)
-    ids = O.corner_ids(q + 1, q + 1)
+    ids = eolc.corner_ids(q + 1, q + 1)
     fq = np.array([3 * ids[k] + c for k in (3, 4) for c in range(3)], np.int32)
     beq = 0.99 * vq[fq]
     C, d = qp_ref.contact_rows(O.cd2(xq, tris, [bs], threshold=1e-3), ns)
@@ -540,6 +539,65 @@ def run_contacts(args, local_rank, stream, flush, steps=5):
     out["workload"] = ("256x256-quad sheet draped over a 0.4 x 0.4 box (snapshot 14 of the "
                        "seeded drape), 2 corners pinned, patch-PCG, rel-res 1e-8, host buffers")
     return out
+
+
+def run_cd2(args, local_rank, stream, steps=200, cpu_sample=40):
+    """CD2 at configuration 2's size: a 128x128-quad sheet (16,641 nodes,
+    32,768 triangles) over a 0.4 x 0.4 x 0.2 m box 0.05 m below it, threshold
+    1e-3, positions of the seeded 200-step drape (jitter N(0, 1e-4)).  Every
+    step is one eolc_cd2 call with host positions in and host contacts out
+    (wall clock) and the same call's span on the stream (CUDA events); the
+    contact sets of the timed calls are compared with the oracle's bytes.
+    CPU baseline: the oracle's CD2 on every fifth step, one thread."""
+    import ctypes
+    import numpy as np
+    import torch
+    import eolc
+    import oracle as O
+    import scenes as S
+    x0, X, tri, center, snaps = S.drape_positions(128, steps, seed=2024)
+    n = len(x0) // 3
+    ctx = eolc.Context(local_rank)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_topology(n, tri, eolc.mesh_hinges(tri))
+    ob = O.axis_box(center, (0.4, 0.4, 0.2))  # the oracle's box (parity check below)
+    gb = eolc.Box(list(ob.dim), list(ob.E1))
+    ctx.cd2(snaps[0], boxes=[gb], threshold=1e-3)  # edge list and perturbation built
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    wall, dev, raw, launches0 = [], [], [], ctx.launch_count()
+    for x in snaps:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ev0.record(stream)
+        raw.append(ctx.cd2(x, boxes=[gb], threshold=1e-3, raw=True))
+        ev1.record(stream)
+        wall.append(1e3 * (time.perf_counter() - t0))
+        ev1.synchronize()
+        dev.append(ev0.elapsed_time(ev1))
+    launches = (ctx.launch_count() - launches0) / steps
+    size = ctypes.sizeof(eolc.Contact)
+    contacts = [len(r) // size for r in raw]
+    exact = all(raw[k] == O.cd2(snaps[k], tri, boxes=[ob], threshold=1e-3, raw=True)
+                for k in range(0, steps, 10))
+    picks = list(range(0, steps, steps // cpu_sample))[:cpu_sample]
+    t0 = time.perf_counter()
+    for k in picks:
+        O.cd2(snaps[k], tri, boxes=[ob], threshold=1e-3)
+    cpu_s = (time.perf_counter() - t0) / len(picks)
+    med = lambda v: float(np.median(v))
+    return {"workload": "CD2, 128x128-quad sheet (16641 nodes, 32768 tris, 49408 edges) over a "
+                        "0.4x0.4x0.2 box, threshold 1e-3, 200 drape steps, jitter N(0,1e-4)",
+            "ms_per_call": med(wall), "calls_per_s": 1e3 / med(wall),
+            "ms_per_call_stream": med(dev), "mean_contacts": float(np.mean(contacts)),
+            "max_contacts": int(max(contacts)), "gpu_launches_per_call": launches,
+            "bit_exact_vs_oracle": exact,
+            "bit_exact_checked": "every 10th of the timed calls (the full 200-step check is "
+                                 "tests/test_gpu_c2.py)",
+            "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "calls/s", "cores": 1, "kind": "port",
+                             "sample": "the oracle's CD2 on %d of the 200 steps (every %dth)"
+                                       % (len(picks), steps // cpu_sample)},
+            "note": "ms_per_call: host positions in, host contacts out, through the C ABI "
+                    "(eolc_cd2); ms_per_call_stream: the same call on the stream's clock"}
 
 
 def run_refresh(args, local_rank, stream, sc, reps=3):
@@ -763,8 +821,19 @@ def run_ours(args, rank, world, local_rank):
                              "(traffic) and are bound by synchronisation latency"},
         "clocks": clk.summary(),
     }
+    # the metric's own comparison at the top level: the fastest learned arm
+    # against the resident Jacobi arm, both to the same FP64 residual
+    learned_arms = [a for a in results if a.startswith("learned")]
+    if learned_arms and "jacobi" in results:
+        bl = max(learned_arms, key=lambda a: results[a]["steps_per_s"])
+        line["learned_arm"] = bl
+        line["learned_steps_per_s"] = results[bl]["steps_per_s"]
+        line["jacobi_steps_per_s"] = results["jacobi"]["steps_per_s"]
+        line["learned_vs_jacobi"] = results[bl]["steps_per_s"] / results["jacobi"]["steps_per_s"]
     if cpu:
         line["cpu_baseline"] = cpu
+    if world == 1 and not args.no_cd2:
+        line["cd2"] = optional_line(lambda: run_cd2(args, local_rank, stream))
     if world == 1 and not args.no_export:
         line["obj_export"] = optional_line(lambda: run_export(ctx, sc, x_w, stream))
     if world == 1 and not args.no_contacts:
@@ -793,6 +862,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-sheets line")
     ap.add_argument("--no-export", action="store_true", help="skip the OBJ export line")
+    ap.add_argument("--no-cd2", action="store_true", help="skip the CD2 (configuration 2) line")
     ap.add_argument("--no-contacts", action="store_true", help="skip the contact-step line")
     ap.add_argument("--no-refresh", action="store_true", help="skip the topology-refresh line")
     ap.add_argument("--no-eol", action="store_true", help="skip the EOL-fill line")

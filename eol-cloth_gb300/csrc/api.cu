@@ -221,6 +221,7 @@ PcgArgs batch_pcg_args(eolc_ctx *ctx, const eolc_solve_opts *o, double *v) {
   a.rel_tol = o->rel_tol;
   a.max_iter = o->max_iter;
   a.learned = nullptr;
+  a.spin_limit = ctx->spin_limit;
   return a;
 }
 
@@ -434,6 +435,7 @@ PcgArgs default_pcg_args(eolc_ctx *ctx, const eolc_solve_opts *o) {
   a.max_iter = o->max_iter;
   a.learned = nullptr;
   a.X = ctx->X.p;
+  a.spin_limit = ctx->spin_limit;
   return a;
 }
 
@@ -637,6 +639,12 @@ eolc_status eolc_set_learned_refresh(eolc_ctx *ctx, int solves) {
 eolc_status eolc_set_coarse_refresh(eolc_ctx *ctx, int solves) {
   if (!ctx || solves < 1) return EOLC_BAD_ARG;
   ctx->coarse_refresh = solves;
+  return EOLC_OK;
+}
+
+eolc_status eolc_set_wait_limit(eolc_ctx *ctx, long long polls) {
+  if (!ctx || polls < 0) return EOLC_BAD_ARG;
+  ctx->spin_limit = polls;
   return EOLC_OK;
 }
 

@@ -88,17 +88,20 @@ __device__ __forceinline__ void block_sum3(typename Acc<T>::V &a, typename Acc<T
   a = red[3 * NW]; b = red[3 * NW + 1]; c = red[3 * NW + 2];
 }
 
-constexpr long long kSpinLimit = 1ll << 25;  // polls before a grid barrier gives up
+// Polls before a bounded device wait (grid barrier, neighbour exchange)
+// gives up: the default of eolc_set_wait_limit, seconds of polling.
+constexpr long long kDefaultSpinLimit = 1ll << 25;
 
 // ---- grid barrier -----------------------------------------------------------
 // Monotonic arrival counter: CTA thread 0 adds 1 with release semantics and
-// polls (acquire) until the count reaches n_ctas * epoch.  Bounded spin: on
-// expiry the barrier records EOLC_TIMEOUT and returns false.  While it waits
+// polls (acquire) until the count reaches n_ctas * epoch.  Bounded spin: after
+// `limit` polls the barrier records EOLC_TIMEOUT and returns false.  While it waits
 // it reads the status every 1024 polls, so that a CTA that gave up elsewhere
 // ends the others' waits early; a barrier that completes does not read it
 // (one L2 round trip fewer per barrier).
 __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned nblocks,
-                                             unsigned &epoch, DevStatus *st) {
+                                             unsigned &epoch, DevStatus *st,
+                                             long long limit) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -110,7 +113,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned nblocks,
     long long spins = 0;
     while (count.load(cuda::memory_order_acquire) < target) {
       ++spins;
-      if (spins > kSpinLimit) {
+      if (spins > limit) {
         atomicCAS(&st->status, EOLC_OK, EOLC_TIMEOUT);
         ok = 0;
         break;
@@ -166,6 +169,7 @@ struct Params {
   double *part;             // partial sums: 2 sets x 3 values x n_ctas
   unsigned *bar;
   DevStatus *st;
+  long long spin_limit;     // polls before a grid barrier gives up
   double tol2;              // tol^2 (scaled by ||rhs||^2 on the device)
   int max_iter;
   int block_pc;             // 0 = point Jacobi, 1 = block Jacobi

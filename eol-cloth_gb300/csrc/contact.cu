@@ -28,6 +28,7 @@
 // terms in a fixed order (per-block and per-node lists built on the host):
 // results are bit-reproducible.
 #include <cuda_runtime.h>
+#include <math_constants.h>
 
 #include <algorithm>
 #include <cmath>
@@ -79,11 +80,12 @@ __global__ void ineq_setup_kernel(int m, const int *__restrict__ rnode,
   rho[i] = cnt > 0 && g2 > 0 ? kKappa * (tr / (3.0 * cnt)) / g2 : 0.0;
 }
 
-// max |v| over the 3N DOFs.
+// max |v| over the 3N DOFs; a non-finite entry makes it +inf (fmax alone
+// would drop a NaN), which the host reports as EOLC_NONFINITE.
 __global__ void absmax_kernel(int n, const double *__restrict__ v, unsigned long long *stat) {
   double mx = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
-    mx = fmax(mx, fabs(v[k]));
+    mx = isfinite(v[k]) ? fmax(mx, fabs(v[k])) : CUDART_INF;
   for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   if ((threadIdx.x & 31) == 0) atomic_max_nonneg(stat + kStatVmax, mx);
 }
@@ -561,6 +563,11 @@ eolc_status ineq_solve_device(eolc_ctx *ctx, int n_ineq, const int *ineq_ptr_h,
     pending = stat_h[kStatChanges];
     I.outer = outer + 1;
     const double vmax = as_double(stat_h[kStatVmax]);
+    if (!std::isfinite(vmax)) {
+      I.status = EOLC_NONFINITE;
+      ctx->err = "non-finite velocity in the contact solve";
+      return EOLC_NONFINITE;
+    }
     I.max_violation = vmax > 0 ? as_double(stat_h[kStatViol]) / vmax : as_double(stat_h[kStatViol]);
     I.n_active = int(stat_h[kStatActive]);
     converged = as_double(stat_h[kStatDlam]) <= tol * std::max(vmax, 1e-300);

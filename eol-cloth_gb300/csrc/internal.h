@@ -143,6 +143,7 @@ struct PcgArgs {
   const float *learned;  // learned approximate inverse blocks (n_blocks*9)
   const double *X = nullptr;  // material coordinates (2N, device; optional):
                               // partition hint for the resident solvers
+  long long spin_limit = 0;   // polls before a device wait gives up (0: default)
 };
 eolc_status run_pcg(SolveWork *&w, const PcgArgs &a, eolc_solve_info *info,
                     cudaStream_t s, std::string &err, long long &launches);
@@ -284,6 +285,7 @@ struct eolc_ctx {
   int lpc_uses = 0;           // solves that G has served
   int lpc_refresh = 1;        // re-evaluate the network every lpc_refresh solves
   int coarse_refresh = 1;     // rebuild the patch PC's coarse operator every ... solves
+  long long spin_limit = 0;   // polls before a device wait gives up (0: the default)
   eolc::CollideWork *cd_work = nullptr;
   eolc::ExportWork *ex_work = nullptr;
   eolc::IneqWork *iq_work = nullptr;

@@ -150,6 +150,7 @@ struct ResParams {
   double *part;
   unsigned *bar;
   DevStatus *st;
+  long long spin_limit;                    // polls before a device wait gives up
 };
 
 struct ResSmem {
@@ -326,6 +327,7 @@ struct GridSum {
   int G, cta;
   unsigned epoch;
   int pset;
+  long long limit;  // polls before the grid barrier gives up
   struct NoPre {
     __device__ void operator()() const {}
   };
@@ -356,7 +358,7 @@ struct GridSum {
       }
       if (lane == 0) { pp[3 * cta] = x; pp[3 * cta + 1] = y; pp[3 * cta + 2] = z; }
     }
-    if (!grid_barrier(bar, G, epoch, st)) return false;
+    if (!grid_barrier(bar, G, epoch, st, limit)) return false;
     pre();
     if (warp == 0) {
       // every load issued before the first add: one L2 round trip
@@ -439,7 +441,7 @@ struct GridSum {
         d[2] = make_float4(f[8], 0.f, 0.f, 0.f);
       }
     }
-    if (!grid_barrier(bar, G, epoch, st)) return false;
+    if (!grid_barrier(bar, G, epoch, st, limit)) return false;
     pre();
     for (int t = threadIdx.x; t < 3 * G; t += kRThreads)
       reinterpret_cast<float4 *>(cs)[t] = __ldcg(reinterpret_cast<const float4 *>(pc) + t);
@@ -473,7 +475,7 @@ struct GridSum {
     pset ^= 1;
     return true;
   }
-  __device__ bool barrier() { return grid_barrier(bar, G, epoch, st); }
+  __device__ bool barrier() { return grid_barrier(bar, G, epoch, st, limit); }
 };
 
 // ---- Jacobi PCG, one grid barrier per iteration -------------------------------
@@ -505,7 +507,7 @@ __global__ void __launch_bounds__(kRThreads, 1) jacobi_resident_kernel(ResParams
   const int cta = blockIdx.x, i = threadIdx.x;
   const int p0 = P.patch_row[cta], np = P.patch_row[cta + 1] - p0;
   const int nh = P.hnptr[cta + 1] - P.hnptr[cta];
-  GridSum sync{P.part, P.bar, P.st, P.n_ctas, cta, 0u, 0};
+  GridSum sync{P.part, P.bar, P.st, P.n_ctas, cta, 0u, 0, P.spin_limit};
   RowMeta M;
   load_patch(P, sm, cta, p0, np, M);
   const bool own = i < np;
@@ -701,11 +703,11 @@ __device__ __forceinline__ void publish_tagged(unsigned long long *tw, int N, in
   st_tag2(q, tag_word(tag, v.x), tag_word(tag, v.y));
   st_tag2(q + 2, tag_word(tag, v.z), tag_word(tag, 0.f));
 }
-// Polls node's words until they carry the tag; false after kSpinLimit polls.
+// Polls node's words until they carry the tag; false after `limit` polls.
 __device__ __forceinline__ bool poll_tagged(const unsigned long long *tw, int N, int node,
-                                            unsigned tag, V4<float> &v) {
+                                            unsigned tag, V4<float> &v, long long limit) {
   const unsigned long long *q = tw + (size_t(tag & 1u) * N + node) * 4;
-  for (long long spin = 0; spin < kSpinLimit; ++spin) {
+  for (long long spin = 0; spin < limit; ++spin) {
     unsigned long long a, b, c, d;
     ld_tag2(q, a, b);
     ld_tag2(q + 2, c, d);
@@ -1002,7 +1004,7 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
   const int cta = blockIdx.x, i = threadIdx.x;
   const int p0 = P.patch_row[cta], np = P.patch_row[cta + 1] - p0;
   const int nh = P.hnptr[cta + 1] - P.hnptr[cta];
-  GridSum sync{P.part, P.bar, P.st, P.n_ctas, cta, 0u, 0};
+  GridSum sync{P.part, P.bar, P.st, P.n_ctas, cta, 0u, 0, P.spin_limit};
   RowMeta M;
   load_patch(P, sm, cta, p0, np, M);
   __syncthreads();
@@ -1099,7 +1101,7 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
     }                                                                        \
     if (hj >= 0) {                                                           \
       V4<float> uj{};                                                        \
-      if (!poll_tagged(P.tw, N, hj, tag_, uj)) {                             \
+      if (!poll_tagged(P.tw, N, hj, tag_, uj, P.spin_limit)) {                             \
         atomicCAS(&P.st->status, EOLC_OK, EOLC_TIMEOUT);                     \
         s_fail = 1;                                                          \
       }                                                                      \
@@ -1259,7 +1261,7 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
   const int p0 = P.patch_row[cta], np = P.patch_row[cta + 1] - p0;
   const int nh = P.hnptr[cta + 1] - P.hnptr[cta];
   const int N = P.n_nodes;
-  GridSum sync{P.part, P.bar, P.st, P.n_ctas, cta, 0u, 0};
+  GridSum sync{P.part, P.bar, P.st, P.n_ctas, cta, 0u, 0, P.spin_limit};
   RowMeta M;
   load_patch(P, sm, cta, p0, np, M);
   const bool own = i < np;
@@ -1329,7 +1331,7 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
     }                                                                      \
     if (hj >= 0) {                                                         \
       V4<float> uj{};                                                      \
-      if (!poll_tagged(P.tw, N, hj, tag_, uj)) {                           \
+      if (!poll_tagged(P.tw, N, hj, tag_, uj, P.spin_limit)) {                           \
         atomicCAS(&P.st->status, EOLC_OK, EOLC_TIMEOUT);                   \
         s_fail = 1;                                                        \
       }                                                                    \
@@ -2241,6 +2243,7 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, i
   P.part = w->part.p;
   P.bar = w->bar.p;
   P.st = w->st.p;
+  P.spin_limit = a.spin_limit > 0 ? a.spin_limit : kDefaultSpinLimit;
   void *args[] = {&P};
   if (!w->ev0) { cudaEventCreate(&w->ev0); cudaEventCreate(&w->ev1); }
   cudaEventRecord(w->ev0, s);

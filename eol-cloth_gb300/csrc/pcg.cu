@@ -104,7 +104,7 @@ cg_kernel(Params<T> P) {
     if (threadIdx.x == 0) {                                             \
       pp[3 * cta] = a; pp[3 * cta + 1] = b; pp[3 * cta + 2] = c;        \
     }                                                                   \
-    if (!grid_barrier(P.bar, G, epoch, P.st)) return;                   \
+    if (!grid_barrier(P.bar, G, epoch, P.st, P.spin_limit)) return;                   \
     reduce_partials3<C0, T>(pp, G, a, b, c, red);                           \
     pset ^= 1;                                                          \
   } while (0)
@@ -148,7 +148,7 @@ cg_kernel(Params<T> P) {
         P.x64[i] = x;
         P.xacc[i] = V4<T>{T(0), T(0), T(0), T(0)};
       }
-    if (!grid_barrier(P.bar, G, epoch, P.st)) return;
+    if (!grid_barrier(P.bar, G, epoch, P.st, P.spin_limit)) return;
     // RU2: r = rhs - A x64 (FP64), s = A p
     double rr64d = 0;
     ru_residual<C0>(P, tiles, ntiles, cur, smem, rr64d);
@@ -219,7 +219,7 @@ pcg_general_kernel(Params<T> P, const T *Gm) {
     if (threadIdx.x == 0) {                                             \
       pp[3 * cta] = a; pp[3 * cta + 1] = b; pp[3 * cta + 2] = c;        \
     }                                                                   \
-    if (!grid_barrier(P.bar, G, epoch, P.st)) return;                   \
+    if (!grid_barrier(P.bar, G, epoch, P.st, P.spin_limit)) return;                   \
     reduce_partials3<C0, T>(pp, G, a, b, c, red);                           \
     pset ^= 1;                                                          \
   } while (0)
@@ -263,7 +263,7 @@ pcg_general_kernel(Params<T> P, const T *Gm) {
         P.x64[i] = x;
         P.xacc[i] = V4<T>{T(0), T(0), T(0), T(0)};
       }
-    if (!grid_barrier(P.bar, G, epoch, P.st)) return;
+    if (!grid_barrier(P.bar, G, epoch, P.st, P.spin_limit)) return;
     double rr64d = 0;
     gen_ru_residual<C0>(P, tiles, ntiles, rcur, smem, rr64d);
     V rr64 = A::from_d(rr64d), e1 = A::zero(), e2 = A::zero();
@@ -417,6 +417,7 @@ eolc_status run_pcg_t(SolveWork *&w, const PcgArgs &a, eolc_solve_info *info,
   P.st = w->st.p;
   P.max_iter = a.max_iter;
   P.block_pc = bpc;
+  P.spin_limit = a.spin_limit > 0 ? a.spin_limit : kDefaultSpinLimit;
   P.tol2 = a.rel_tol * a.rel_tol;
   void *args[] = {&P};
   if (!w->ev0) { cudaEventCreate(&w->ev0); cudaEventCreate(&w->ev1); }
@@ -535,6 +536,7 @@ eolc_status run_pcg_general_f(SolveWork *&w, const PcgArgs &a, const float *Gm,
   P.tile_row = w->tile_row.p; P.tile_wptr = w->tile_wptr.p; P.wlist = w->wlist.p;
   P.cta_tile = w->cta_tile.p; P.rhs = rhs; P.x64 = x64; P.pc = pc; P.fmask = fmask;
   P.part = w->part.p; P.bar = w->bar.p; P.st = w->st.p; P.max_iter = a.max_iter; P.block_pc = 0;
+  P.spin_limit = a.spin_limit > 0 ? a.spin_limit : kDefaultSpinLimit;
   P.tol2 = a.rel_tol * a.rel_tol;
   void *args[] = {&P, &Gm};
   if (!w->ev0) { cudaEventCreate(&w->ev0); cudaEventCreate(&w->ev1); }
@@ -688,6 +690,12 @@ extern "C" eolc_status eolc_velocity_solve_static(
                    lcol).empty())
     return EOLC_BAD_ARG;
   lcol.resize(lcol.size() + 8, 0);
+  // the tiling's arrays must fit their fixed slots of the scratch array
+  // (windows never exceed the blocks and tiles never exceed the rows, but a
+  // broken invariant must not write past a slot)
+  if (wlist.size() > size_t(EOLC_STATIC_MAX_BLOCKS) || tiles.size() > size_t(n_nodes) + 1 ||
+      wptr.size() > size_t(n_nodes) + 1 || lcol.size() > size_t(EOLC_STATIC_MAX_BLOCKS) + 8)
+    return EOLC_CAPACITY;
   const int nt = int(tiles.size()) - 1;
   int n_sm = 0;
   cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
@@ -785,6 +793,7 @@ extern "C" eolc_status eolc_velocity_solve_static(
   P.st = d_st;
   P.max_iter = max_iter;
   P.block_pc = 0;
+  P.spin_limit = kDefaultSpinLimit;
   P.tol2 = rel_tol * rel_tol;
   const size_t smem = smem_bytes<T>();
   if (cudaFuncSetAttribute(cg_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,

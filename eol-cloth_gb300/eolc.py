@@ -117,7 +117,8 @@ EXPORTS = ["eolc_version", "eolc_launch_count", "eolc_create", "eolc_destroy", "
            "eolc_batch_set_jacobi_reference", "eolc_lpc_blocks", "eolc_export_obj",
            "eolc_export_obj_text", "eolc_velocity_solve_ineq", "eolc_contact_rows",
            "eolc_step_contacts", "eolc_set_topology_device", "eolc_topology_arrays",
-           "eolc_edge_list", "eolc_set_topology_eol", "eolc_clear_contact_multipliers"]
+           "eolc_edge_list", "eolc_set_topology_eol", "eolc_clear_contact_multipliers",
+           "eolc_set_wait_limit"]
 
 
 def load_library(path=LIB_PATH):
@@ -171,6 +172,7 @@ def load_library(path=LIB_PATH):
     L.eolc_set_jacobi_reference.argtypes = [_V, ctypes.c_int]
     L.eolc_set_learned_refresh.argtypes = [_V, ctypes.c_int]
     L.eolc_set_coarse_refresh.argtypes = [_V, ctypes.c_int]
+    L.eolc_set_wait_limit.argtypes = [_V, ctypes.c_longlong]
     L.eolc_batch_set_jacobi_reference.argtypes = [_V, _I, ctypes.c_int]
     L.eolc_set_topology_batched.argtypes = [_V, ctypes.c_int, _I, _I, _I, _I, _I]
     L.eolc_set_instance_materials.argtypes = [_V, ctypes.POINTER(Material), ctypes.c_int]
@@ -426,8 +428,10 @@ class Context:
         self._check(st)
         return info
 
-    def cd2(self, x, boxes=(), points=None, normals=None, threshold=1e-3, capacity=None):
-        """CD2 contact list (point obstacles first, then each box)."""
+    def cd2(self, x, boxes=(), points=None, normals=None, threshold=1e-3, capacity=None,
+            raw=False):
+        """CD2 contact list (point obstacles first, then each box); raw=True
+        returns the contacts' bytes (eolc_contact records, in order)."""
         x = _f64(x)
         boxes = list(boxes)
         barr = (Box * max(1, len(boxes)))(*boxes)
@@ -440,8 +444,10 @@ class Context:
         st = lib.eolc_cd2(self._h, _d(x), barr, len(boxes), _d(pts), _d(nrm), npts, threshold,
                           out, cap, ctypes.byref(n))
         if st == CAPACITY and capacity is None:
-            return self.cd2(x, boxes, points, normals, threshold, capacity=n.value)
+            return self.cd2(x, boxes, points, normals, threshold, capacity=n.value, raw=raw)
         self._check(st)
+        if raw:
+            return ctypes.string_at(out, ctypes.sizeof(Contact) * n.value)
         return [out[k] for k in range(n.value)]
 
     # ---- OBJ export ------------------------------------------------------------
@@ -501,6 +507,11 @@ class Context:
 
     def set_learned_refresh(self, solves):
         self._check(lib.eolc_set_learned_refresh(self._h, solves))
+
+    def set_wait_limit(self, polls):
+        """Polls before a device wait of this context's solves gives up with
+        TIMEOUT (eolc_set_wait_limit; 0 restores the default)."""
+        self._check(lib.eolc_set_wait_limit(self._h, polls))
 
     def set_coarse_refresh(self, solves):
         """Rebuild the patch preconditioner's coarse operator every `solves`
@@ -612,6 +623,91 @@ class LearnedPC:
     def attach(self, ctx):
         ctx._check(lib.eolc_attach_preconditioner(ctx.handle, self._h))
         ctx._lpc = self  # keep the network alive while attached
+
+
+# ---------------------------------------------------------------------------
+# Mesh input (host side, numpy): the sheets the benchmark scenes use
+# ---------------------------------------------------------------------------
+# Corner convention of the scene files (simulationSettings*.json): corner1
+# (0, 0), corner2 (1, 0), corner3 (0, 1), corner4 (1, 1), rows (x, y, z, X, Y).
+UNIT_CORNERS = np.array([[0, 0, 0, 0, 0], [1, 0, 0, 1, 0],
+                         [0, 1, 0, 0, 1], [1, 1, 0, 1, 1]], dtype=np.float64)
+
+
+def sheet_mesh(r0, r1, corners=UNIT_CORNERS):
+    """Grid of r0 x r1 nodes with two triangles per quad -> (x, X, tri).
+    Node k = i r1 + j sits at the bilinear blend of the four corners, blended
+    as Cloth::build blends them (Cloth.cpp:63-76: (1 - s) a + s b per
+    component, first along i, then along j); quad (i, j) gives the triangles
+    (k, k + 1, k + r1 + 1) and (k, k + r1 + 1, k + r1)."""
+    c = np.asarray(corners, np.float64).reshape(4, 5)
+    u = np.arange(r0) / (r0 - 1.0)
+    v = np.arange(r1) / (r1 - 1.0)
+
+    def blend(s, a, b):
+        return (1 - s)[:, None] * a[None, :] + s[:, None] * b[None, :]
+
+    a0, a1 = blend(u, c[0], c[2]), blend(u, c[1], c[3])  # (r0, 5) each
+    pts = (1 - v)[None, :, None] * a0[:, None, :] + v[None, :, None] * a1[:, None, :]
+    pts = pts.reshape(-1, 5)
+    x = np.ascontiguousarray(pts[:, :3]).ravel()
+    X = np.ascontiguousarray(pts[:, 3:]).ravel()
+    i, j = np.meshgrid(np.arange(r0 - 1), np.arange(r1 - 1), indexing="ij")
+    k0 = (i * r1 + j).ravel()
+    t = np.empty((2 * len(k0), 3), np.int32)
+    t[0::2] = np.stack([k0, k0 + 1, k0 + r1 + 1], 1)
+    t[1::2] = np.stack([k0, k0 + r1 + 1, k0 + r1], 1)
+    return x, X, t
+
+
+def mesh_hinges(tri):
+    """Bending hinges (x0, x1, x2, x3) of a triangle list, one per edge with
+    two faces, in ArcSim's edge order (Mesh::add(Face), mesh.cpp:356-378):
+    each face, in order, creates its missing edges (v[i], v[i+1]); a face
+    registers on side 0 of its edge (v[i+1], v[i+2]) when that edge's first
+    node is v[i+1], else on side 1 (a later face overwrites).  x0, x1 are the
+    edge's nodes, x2 / x3 the other vertex of the side-0 / side-1 face
+    (Forces.cpp:687-697)."""
+    tri = np.asarray(tri, np.int64).reshape(-1, 3)
+    nf = len(tri)
+    if nf == 0:
+        return np.zeros((0, 4), np.int32)
+    a = tri.ravel()                          # v[i] of (face, i)
+    b = tri[:, [1, 2, 0]].ravel()            # v[i+1]
+    key = np.minimum(a, b) * (int(tri.max()) + 1) + np.maximum(a, b)
+    uk, first, inv = np.unique(key, return_index=True, return_inverse=True)
+    order = np.argsort(first, kind="stable")          # edges in creation order
+    rank = np.empty(len(uk), np.int64)
+    rank[order] = np.arange(len(uk))
+    eid = rank[inv]                                    # edge of (face, i) = (v[i], v[i+1])
+    n0, n1 = a[first[order]], b[first[order]]
+    # face f registers on edge (v[i+1], v[i+2]) = the edge created at slot
+    # (f, i+1); its side follows whether n0 is v[i+1]
+    f = np.repeat(np.arange(nf), 3)
+    slot_next = (np.arange(3 * nf).reshape(nf, 3)[:, [1, 2, 0]]).ravel()
+    e_reg = eid[slot_next]
+    first_node = a[slot_next]
+    side0 = n0[e_reg] == first_node
+    f0 = np.full(len(uk), -1, np.int64)
+    f1 = np.full(len(uk), -1, np.int64)
+    np.maximum.at(f0, e_reg[side0], f[side0])
+    np.maximum.at(f1, e_reg[~side0], f[~side0])
+    keep = (f0 >= 0) & (f1 >= 0)
+    e0, e1 = n0[keep], n1[keep]
+
+    def other(fa):  # get_other_vert (mesh.hpp:276-280)
+        v = tri[fa]
+        pick = np.where((v[:, 0] != e0) & (v[:, 0] != e1), v[:, 0],
+                        np.where((v[:, 1] != e0) & (v[:, 1] != e1), v[:, 1], v[:, 2]))
+        return pick
+
+    return np.stack([e0, e1, other(f0[keep]), other(f1[keep])], 1).astype(np.int32)
+
+
+def corner_ids(r0, r1):
+    """Node ids of the pinned corners 1-4 of a scene's cloth
+    (parseParams.cpp:298-305)."""
+    return {1: 0, 2: r0 * (r1 - 1), 3: r0 * r1 - 1, 4: r0 - 1}
 
 
 def contact_rows(contacts, n_nodes):

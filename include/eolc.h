@@ -494,6 +494,16 @@ eolc_status eolc_set_learned_refresh(eolc_ctx *ctx, int solves);
  * reuse it in between (a lagged coarse correction: still symmetric positive
  * definite, so PCG stays exact).  A new topology forces a rebuild. */
 eolc_status eolc_set_coarse_refresh(eolc_ctx *ctx, int solves);
+/* Bound of every device-side wait of this context's solves: the grid
+ * barriers of the persistent PCG kernels and the neighbour exchange of the
+ * resident kernels poll at most `polls` times, then record EOLC_TIMEOUT;
+ * every CTA of the launch then leaves (the others see the status or run out
+ * of polls themselves) and the call returns EOLC_TIMEOUT with the context
+ * still usable.  0 restores the default (2^25 polls, seconds).  The
+ * reference has no device and no wait to bound; this is the library's
+ * failure detection for a stalled SM (a small limit makes a healthy solve
+ * report EOLC_TIMEOUT, which is how the tests exercise the path). */
+eolc_status eolc_set_wait_limit(eolc_ctx *ctx, long long polls);
 /* Iteration count of a plain Jacobi solve that the learned solve's fallback
  * cap (fallback_factor x this count) refers to; set automatically by every
  * successful Jacobi solve on the context. */
@@ -535,13 +545,16 @@ eolc_status eolc_export_obj_text(eolc_ctx *ctx, int frame, double time,
  * process exits).  No context is needed and nothing is allocated on the
  * device.
  *   rowptr_h/colidx_h: the BSR pattern (host; eolc_bsr_pattern's layout),
- *   mdk_d: FP32 block values (device, 9 per block), b_d: 3N right-hand side
- *   b of Cloth.cpp:345 (device), fixed_dofs_h/beq_h: pinned DOFs and their
- *   values (host), v_d: 3N solution (device, written).
+ *   mdk_d: FP32 block values (device, 9 per block), b_d: the 3N right-hand
+ *   side -(M v + h f) of the implicit-Euler step (device),
+ *   fixed_dofs_h/beq_h: pinned DOFs and their values (host), v_d: 3N
+ *   solution (device, written).
  * Limits: n_nodes <= EOLC_STATIC_MAX_NODES and n_blocks <=
  * EOLC_STATIC_MAX_BLOCKS, else EOLC_CAPACITY.  The first call on a device
- * looks up the array's device address with that device current (make it
- * before any stream capture).  Every call shares the array and it keeps the
+ * looks up the array's device address with that device current.  The call
+ * copies its tiling from host memory and synchronizes the stream, so it
+ * cannot be made while the stream is being captured into a CUDA graph.
+ * Every call shares the array and it keeps the
  * previous call's contents (the call clears what must start at zero), so
  * calls whose GPU work overlaps — two streams, or two threads — race and
  * must be serialized by the caller.  stream: a cudaStream_t (NULL: the

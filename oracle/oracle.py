@@ -297,7 +297,9 @@ def axis_box(center, dim):
                (ctypes.c_double * 16)(*E1.flatten(order="F")))
 
 
-def cd2(x, tri, boxes=(), points=None, normals=None, threshold=1e-3, cap=None):
+def cd2(x, tri, boxes=(), points=None, normals=None, threshold=1e-3, cap=None, raw=False):
+    """CD2 (Collisions.cpp:55-78) of the restated boxTriCollision: the
+    contact list, or with raw=True the contacts' bytes in order."""
     tri = np.ascontiguousarray(tri, dtype=np.int32)
     n_nodes = len(x) // 3
     pts = np.zeros(3) if points is None else np.ascontiguousarray(points, np.float64)
@@ -310,7 +312,9 @@ def cd2(x, tri, boxes=(), points=None, normals=None, threshold=1e-3, cap=None):
     n = lib().orc_cd2(n_nodes, dp(x), ip(tri), len(tri), barr, len(boxes), dp(pts),
                       dp(nrm), npts, ctypes.c_double(threshold), out, cap)
     if n > cap:
-        return cd2(x, tri, boxes, points, normals, threshold, cap=n)
+        return cd2(x, tri, boxes, points, normals, threshold, cap=n, raw=raw)
+    if raw:
+        return ctypes.string_at(out, ctypes.sizeof(Contact) * n)
     return [out[k] for k in range(n)]
 
 

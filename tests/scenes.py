@@ -7,7 +7,7 @@ and bench.py all run the same workloads.
 """
 import numpy as np
 
-import oracle as O
+import eolc  # the library's own mesh input builders (numpy; no GPU needed)
 
 GRAV = [0.0, 0.0, -9.8]
 H = 5e-3
@@ -23,9 +23,9 @@ def sheet(quads, pins=(3, 4)):
     named corners (ids of parseParams.cpp:298-305, all three axes, zero
     scripted velocity)."""
     r = quads + 1
-    x, X, tri = O.grid2(r, r)
-    hinge = O.hinges(r * r, tri)
-    ids = O.corner_ids(r, r)
+    x, X, tri = eolc.sheet_mesh(r, r)
+    hinge = eolc.mesh_hinges(tri)
+    ids = eolc.corner_ids(r, r)
     fixed = np.array([3 * ids[k] + c for k in pins for c in range(3)], np.int32)
     return dict(x=x, X=X, tri=tri, hinge=hinge, fixed=fixed,
                 fixed_vel=np.zeros(len(fixed)), n=r * r)
@@ -40,7 +40,7 @@ def drape_positions(quads, steps, seed=7, jitter=1e-4, box_dim=(0.4, 0.4, 0.2),
     all occur.  Each snapshot is jittered N(0, jitter) from a seeded
     generator.  Returns (x0, X, tri, box_center, snapshots)."""
     r = quads + 1
-    x0, X, tri = O.grid2(r, r)
+    x0, X, tri = eolc.sheet_mesh(r, r)
     rng = np.random.default_rng(seed)
     xy = x0.reshape(-1, 3)[:, :2]
     half = np.array(box_dim[:2]) / 2
@@ -127,7 +127,7 @@ def delaunay_sheet(n_tri, rng, gradient=3.0):
     X = pts[used]
     n = len(X)
     x = np.concatenate([X, np.zeros((n, 1))], 1).ravel()
-    hinge = O.hinges(n, tri)
+    hinge = eolc.mesh_hinges(tri)
     corners = [int(np.argmin((X[:, 0] - cx) ** 2 + (X[:, 1] - 1.0) ** 2)) for cx in (0.0, 1.0)]
     fixed = np.array([3 * k + c for k in corners for c in range(3)], np.int32)
     return dict(x=x, X=X.ravel(), tri=tri, hinge=hinge, fixed=fixed, fixed_vel=np.zeros(len(fixed)),

@@ -171,6 +171,20 @@ eolc_status assemble(eolc_ctx *ctx, const eolc_material &mat, const double g[3],
   if (prec == EOLC_PREC_FP64) EOLC_CHECK_CUDA(ctx, ctx->A64.resize(nb9 + 16));
   if (want_M) EOLC_CHECK_CUDA(ctx, ctx->Mblk.resize(nb9));
   {
+    // the shared-memory assembly's tiles, once per topology and precision
+    // (never while the stream is being captured: the build synchronizes;
+    // batched steps build them before their capture)
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    EOLC_CHECK_CUDA(ctx, cudaStreamIsCapturing(s, &cs));
+    if (cs == cudaStreamCaptureStatusNone) {
+      const std::string msg = ensure_assembly_tiles(ctx->topo, prec, s, ctx->launches);
+      if (!msg.empty()) {
+        ctx->err = msg;
+        return EOLC_CUDA_ERROR;
+      }
+    }
+  }
+  {
     const size_t need = assemble_scratch_bytes(ctx->topo, prec);
     if (ctx->elem.n < need) EOLC_CHECK_CUDA(ctx, ctx->elem.resize(need));
   }
@@ -181,12 +195,12 @@ eolc_status assemble(eolc_ctx *ctx, const eolc_material &mat, const double g[3],
   launch_forces_rhs(ctx->topo, ctx->x.p, ctx->X.p, ctx->v.p, md, mats, node_inst, prec,
                     ctx->elem.p, ctx->f.p, want_b ? ctx->b.p : nullptr, ctx->aux);
   EOLC_CHECK_CUDA(ctx, cudaEventRecord(ctx->aux_join, ctx->aux));
-  launch_assemble_blocks(ctx->topo, ctx->x.p, ctx->X.p, md, mats, node_inst, prec, ctx->elem.p,
-                         prec == EOLC_PREC_FP64 ? ctx->A64.p : nullptr,
-                         prec == EOLC_PREC_FP64 ? nullptr : ctx->A32.p,
-                         want_M ? ctx->Mblk.p : nullptr, s);
+  const int nk = launch_assemble_blocks(
+      ctx->topo, ctx->x.p, ctx->X.p, md, mats, node_inst, prec, ctx->elem.p,
+      prec == EOLC_PREC_FP64 ? ctx->A64.p : nullptr,
+      prec == EOLC_PREC_FP64 ? nullptr : ctx->A32.p, want_M ? ctx->Mblk.p : nullptr, s);
   EOLC_CHECK_CUDA(ctx, cudaStreamWaitEvent(s, ctx->aux_join, 0));
-  ctx->launches += ctx->topo.n_hinge > 0 ? 5 : 4;
+  ctx->launches += nk + 2;  // + the two force kernels
   if (eol) {
     ctx->launches += 1;
     if (want_b) {
@@ -1187,6 +1201,11 @@ eolc_status eolc_step_batched(eolc_ctx *ctx, int n_steps, const double grav[3], 
     std::string msg;
     if ((st = batch_prepare(ctx->bwork, a, ctx->node_off, ctx->batch_config, s, msg)) != EOLC_OK)
       return fail(ctx, st, msg.c_str());
+  }
+  {
+    // the assembly tiles must exist before a capture records the assembly
+    const std::string msg = ensure_assembly_tiles(ctx->topo, opts->precision, s, ctx->launches);
+    if (!msg.empty()) return fail(ctx, EOLC_CUDA_ERROR, msg.c_str());
   }
   if (opts->precond == EOLC_PC_LEARNED)
     return step_batched_learned(ctx, n_steps, grav, h, opts, inst_info_h, total, s);

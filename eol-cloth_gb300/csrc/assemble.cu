@@ -3,14 +3,32 @@
 //
 // Replaces the triplet loops of faceBasedF / edgeBasedF and the two
 // setFromTriplets calls (Forces.cpp:331-930) plus b = -(M v + h f)
-// (Cloth.cpp:345).  Design: an element pass (one thread per triangle, one
-// per hinge) evaluates each element once and writes its 3x3 blocks (9 per
-// triangle: d_B h^2 K_e; 16 per hinge: d_B h^2 K_b) and the triangle's mass
-// t8 to a contribution buffer; then one thread per BSR block sums the
-// contributions that land in it in the reference's insertion order (faces
-// ascending, then hinges ascending) and writes the block once.  No atomics:
-// results are bit-reproducible run to run.
+// (Cloth.cpp:345).
+//
+// Matrix blocks, one launch (tile_blocks_kernel): the block rows are cut into
+// tiles of consecutive rows whose element blocks fit in shared memory.  A CTA
+// takes one tile.  Every (element, local vertex) pair whose vertex is a row
+// of the tile is a task: it evaluates that row's blocks of the element (3 for
+// a triangle, d_B h^2 K_e plus the mass t8/12 or t8/24; 4 for a hinge,
+// d_B h^2 K_b) into shared memory.  Then each output value (block, entry) of
+// the tile sums the contributions that land in its block, in the reference's
+// insertion order (faces ascending with their mass terms, then hinges
+// ascending), from shared memory, and is stored once: consecutive threads
+// store consecutive words, so the BSR is written with full-sector coalesced
+// stores and nothing but the BSR goes to memory.  No atomics: bit-
+// reproducible.  Element matrices are symmetric: a block (a, b) with a > b is
+// the transpose of the evaluated (b, a), as in the element pass below, so
+// the assembled matrix is exactly symmetric.
+//
+// EOL topologies (and meshes whose rows do not fit a tile) take the two-pass
+// path: an element pass (one thread per triangle, one per hinge) writes every
+// element block to a contribution buffer and one thread per BSR block sums
+// them in the same order.
 #include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
 
 #include "elements.cuh"
 #include "internal.h"
@@ -228,6 +246,143 @@ gather_blocks_kernel(int n_blocks, const int *__restrict__ cptr, const int *__re
   }
 }
 
+// ---- shared-memory tiled assembly ---------------------------------------------
+constexpr int kTileThreads = 256;
+constexpr int kTileBytes = 112640;  // two CTAs per SM
+// slots (3x3 blocks + a mass word) of one tile
+template <typename T>
+__host__ __device__ constexpr int tile_slots() { return kTileBytes / (10 * int(sizeof(T))); }
+
+// Row blocks (la, 0..n-1) of element e into shared memory at base: a block
+// (la, lb) with la <= lb is evaluated, (la, lb) with la > lb is the
+// transpose of the evaluated (lb, la).
+template <typename T>
+__device__ __forceinline__ void store_block(T *sk, int slot, const T blk[9], bool transpose) {
+  T *o = sk + size_t(slot) * 9;
+  if (!transpose) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) o[k] = blk[k];
+  } else {
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) o[3 * c + r] = blk[3 * r + c];
+  }
+}
+
+// FP32: two CTAs per SM (128 registers); FP64: one, without spills
+template <typename T, bool WANT_M>
+__global__ void __launch_bounds__(kTileThreads, sizeof(T) == 4 ? 2 : 1)
+tile_blocks_kernel(const int *__restrict__ tile_row, const int *__restrict__ rowptr,
+                   const int *__restrict__ cptr, const unsigned short *__restrict__ aslot,
+                   const int *__restrict__ nf_ptr, const int *__restrict__ nf_list,
+                   const int *__restrict__ nh_ptr, const int *__restrict__ nh_list,
+                   const int *__restrict__ tri, const int *__restrict__ hinge,
+                   const double *__restrict__ x, const double *__restrict__ X, MaterialD m0,
+                   const MaterialD *__restrict__ mats, const int *__restrict__ node_inst,
+                   double *__restrict__ A64, float *__restrict__ A32,
+                   double *__restrict__ Mblk) {
+  extern __shared__ __align__(16) unsigned char tsm[];
+  constexpr int kSlots = tile_slots<T>();
+  T *sk = reinterpret_cast<T *>(tsm);  // kSlots x 9
+  T *smass = sk + size_t(kSlots) * 9;  // kSlots
+  const int r0 = tile_row[blockIdx.x], r1 = tile_row[blockIdx.x + 1];
+  const int fa = nf_ptr[r0], nf = nf_ptr[r1] - fa;
+  const int ha = nh_ptr[r0], nh = nh_ptr[r1] - ha;
+  // triangle tasks: slots 3k .. 3k + 2
+  for (int k = threadIdx.x; k < nf; k += kTileThreads) {
+    const int code = __ldg(nf_list + fa + k);
+    const int e = code >> 2, la = code & 3;
+    const int a = __ldg(tri + 3 * e), b = __ldg(tri + 3 * e + 1), c = __ldg(tri + 3 * e + 2);
+    MaterialD m = m0;
+    if (mats) m = mats[node_inst[a]];  // batched: the element's instance
+    const Tri<T> q = make_tri<T>(x, X, a, b, c);
+    const T mu = T(m.mu), lam = T(m.lam), dh2 = T(m.dh2);
+    const T t8 = T(m.rho) * T(2) * q.A;
+#pragma unroll 1
+    for (int lb = 0; lb < 3; ++lb) {
+      T blk[9];
+#pragma unroll
+      for (int j = 0; j < 9; ++j) blk[j] = T(0);
+      add_membrane_block<T, T>(q, min(la, lb), max(la, lb), mu, lam, dh2, blk);
+      store_block(sk, 3 * k + lb, blk, la > lb);
+      smass[3 * k + lb] = la == lb ? t8 / T(12) : t8 / T(24);
+    }
+  }
+  // hinge tasks: slots 3 nf + 4k .. + 3
+  for (int k = threadIdx.x; k < nh; k += kTileThreads) {
+    const int code = __ldg(nh_list + ha + k);
+    const int e = code >> 2, la = code & 3;
+    const int *hv = hinge + 4 * e;
+    const int v0 = __ldg(hv), v1 = __ldg(hv + 1), v2 = __ldg(hv + 2), v3n = __ldg(hv + 3);
+    MaterialD m = m0;
+    if (mats) m = mats[node_inst[v0]];
+    const Hinge<T> H = make_hinge<T>(x, X, v0, v1, v2, v3n, T(m.beta));
+    const T dh2 = T(m.dh2);
+#pragma unroll 1
+    for (int lb = 0; lb < 4; ++lb) {
+      T blk[9];
+#pragma unroll
+      for (int j = 0; j < 9; ++j) blk[j] = T(0);
+      add_bending_block<T, T>(H, min(la, lb), max(la, lb), dh2, blk);
+      store_block(sk, 3 * nf + 4 * k + lb, blk, la > lb);
+    }
+  }
+  __syncthreads();
+  // one thread per (block, entry) of the tile: the contributions in insertion
+  // order; consecutive threads write consecutive words
+  const int b0 = rowptr[r0], nv = (rowptr[r1] - b0) * 9;
+  for (int idx = threadIdx.x; idx < nv; idx += kTileThreads) {
+    const int bl = b0 + idx / 9, j = idx - (idx / 9) * 9;
+    const bool on_diag = j == 0 || j == 4 || j == 8;
+    T acc = T(0), macc = T(0);
+    const int c0 = __ldg(cptr + bl), c1 = __ldg(cptr + bl + 1);
+    for (int q = c0; q < c1; ++q) {
+      const unsigned sl = __ldg(aslot + q);
+      const unsigned sidx = sl & 0x7fffu;
+      acc += sk[size_t(sidx) * 9 + j];
+      if ((sl & 0x8000u) && on_diag) {  // a triangle's mass term
+        const T mm = smass[sidx];
+        acc += mm;
+        if (WANT_M) macc += mm;
+      }
+    }
+    const size_t o = size_t(b0) * 9 + idx;
+    if (A64) A64[o] = double(acc);
+    if (A32) A32[o] = float(acc);
+    if (WANT_M) Mblk[o] = double(macc);
+  }
+}
+
+// Slot of every contribution: thread per block b (row i); the contribution
+// (element e, local row la, local column lb) lands in the slot of the task
+// (e, la) of row i, i.e. the position of e in i's triangle or hinge list
+// relative to the tile's first row, + lb.
+__global__ void tile_slots_kernel(int n_blocks, const int *__restrict__ blk_row,
+                                  const int *__restrict__ cptr, const int *__restrict__ contrib,
+                                  const int *__restrict__ row_tile, const int *__restrict__ tile_row,
+                                  const int *__restrict__ nf_ptr, const int *__restrict__ nf_list,
+                                  const int *__restrict__ nh_ptr, const int *__restrict__ nh_list,
+                                  unsigned short *__restrict__ aslot, int *__restrict__ err) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n_blocks) return;
+  const int i = blk_row[b], t = row_tile[i], r0 = tile_row[t], r1 = tile_row[t + 1];
+  const int nft = nf_ptr[r1] - nf_ptr[r0];
+  for (int q = cptr[b]; q < cptr[b + 1]; ++q) {
+    const int code = contrib[q];
+    const int e = code >> 7, la = (code >> 3) & 3, lb = code & 3;
+    const bool h = (code & kHingeBit) != 0;
+    const int want = (e << 2) | la;
+    const int *lst = h ? nh_list : nf_list;
+    const int p0 = h ? nh_ptr[i] : nf_ptr[i], p1 = h ? nh_ptr[i + 1] : nf_ptr[i + 1];
+    int p = p0;
+    while (p < p1 && lst[p] != want) ++p;
+    if (p == p1) { atomicOr(err, 1); continue; }
+    const int slot = h ? 3 * nft + 4 * (p - nh_ptr[r0]) + lb : 3 * (p - nf_ptr[r0]) + lb;
+    aslot[q] = (unsigned short)(slot | (h ? 0 : 0x8000));
+  }
+}
+
 // Forces, FP64 in every precision mode (the FP64 refinement residual of the
 // mixed solve is only as accurate as b; near rest FP32 membrane forces are
 // rounding noise as large as the gravity loads).  Two passes, so that each
@@ -304,12 +459,91 @@ forces_rhs_kernel(int n_nodes, const int *__restrict__ nf_ptr,
 
 }  // namespace
 
-void launch_assemble_blocks(const DevTopology &T, const double *x,
-                            const double *X, const MaterialD &m,
-                            const MaterialD *mats, const int *node_inst,
-                            int prec, void *elem, double *A64, float *A32, double *Mblk,
-                            cudaStream_t s) {
+template <typename E>
+void launch_tiled(const DevTopology &T, int w, const double *x, const double *X,
+                  const MaterialD &m, const MaterialD *mats, const int *node_inst, double *A64,
+                  float *A32, double *Mblk, cudaStream_t s) {
+  const size_t smem = size_t(tile_slots<E>()) * 10 * sizeof(E);
+  if (Mblk) {
+    cudaFuncSetAttribute(tile_blocks_kernel<E, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(smem));
+    tile_blocks_kernel<E, true><<<T.atiles[w], kTileThreads, smem, s>>>(
+        T.atile_row[w].p, T.rowptr.p, T.cptr.p, T.aslot[w].p, T.nf_ptr.p, T.nf_list.p,
+        T.nh_ptr.p, T.nh_list.p, T.tri.p, T.hinge.p, x, X, m, mats, node_inst, A64, A32, Mblk);
+  } else {
+    cudaFuncSetAttribute(tile_blocks_kernel<E, false>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    tile_blocks_kernel<E, false><<<T.atiles[w], kTileThreads, smem, s>>>(
+        T.atile_row[w].p, T.rowptr.p, T.cptr.p, T.aslot[w].p, T.nf_ptr.p, T.nf_list.p,
+        T.nh_ptr.p, T.nh_list.p, T.tri.p, T.hinge.p, x, X, m, mats, node_inst, A64, A32, nullptr);
+  }
+}
+
+std::string ensure_assembly_tiles(DevTopology &T, int prec, cudaStream_t s, long long &launches) {
+  const int w = prec == EOLC_PREC_FP64 ? 1 : 0;
+  if (T.n_eol > 0 || T.atiles[w] >= 0) return "";
+  const int N = T.n_nodes;
+  const int cap = w ? tile_slots<double>() : tile_slots<float>();
+#define AT(expr)                                                                    \
+  do {                                                                              \
+    cudaError_t e_ = (expr);                                                        \
+    if (e_ != cudaSuccess) return std::string(#expr ": ") + cudaGetErrorString(e_); \
+  } while (0)
+  std::vector<int> nf(N + 1), nh(N + 1);
+  AT(cudaMemcpyAsync(nf.data(), T.nf_ptr.p, sizeof(int) * (N + 1), cudaMemcpyDeviceToHost, s));
+  AT(cudaMemcpyAsync(nh.data(), T.nh_ptr.p, sizeof(int) * (N + 1), cudaMemcpyDeviceToHost, s));
+  AT(cudaStreamSynchronize(s));
+  // greedy: grow each tile row by row while its slots fit
+  std::vector<int> tile_row(1, 0), row_tile(N);
+  int start = 0;
+  while (start < N) {
+    int end = start;
+    while (end < N) {
+      const long long slots = 3ll * (nf[end + 1] - nf[start]) + 4ll * (nh[end + 1] - nh[start]);
+      if (slots > cap) break;
+      ++end;
+    }
+    if (end == start) {  // one row's blocks exceed a tile: the two-pass path
+      T.atiles[w] = 0;
+      return "";
+    }
+    for (int i = start; i < end; ++i) row_tile[i] = int(tile_row.size()) - 1;
+    tile_row.push_back(end);
+    start = end;
+  }
+  DevBuf<int> drt, derr;
+  const size_t ncon = T.contrib.n;
+  AT(T.atile_row[w].upload(tile_row.data(), tile_row.size(), s));
+  AT(drt.upload(row_tile.data(), row_tile.size(), s));
+  AT(T.aslot[w].resize(std::max<size_t>(ncon, 1)));
+  AT(derr.resize(1));
+  AT(cudaMemsetAsync(derr.p, 0, sizeof(int), s));
+  tile_slots_kernel<<<(T.n_blocks + 127) / 128, 128, 0, s>>>(
+      T.n_blocks, T.blk_row.p, T.cptr.p, T.contrib.p, drt.p, T.atile_row[w].p, T.nf_ptr.p,
+      T.nf_list.p, T.nh_ptr.p, T.nh_list.p, T.aslot[w].p, derr.p);
+  launches += 1;
+  int err = 0;
+  AT(cudaGetLastError());
+  AT(cudaMemcpyAsync(&err, derr.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  AT(cudaStreamSynchronize(s));
+#undef AT
+  if (err) return "assembly tiles: a contribution without its element task";
+  T.atiles[w] = int(tile_row.size()) - 1;
+  return "";
+}
+
+int launch_assemble_blocks(const DevTopology &T, const double *x,
+                           const double *X, const MaterialD &m,
+                           const MaterialD *mats, const int *node_inst,
+                           int prec, void *elem, double *A64, float *A32, double *Mblk,
+                           cudaStream_t s) {
   const int nb = T.n_blocks, nt = T.n_tri, nh = T.n_hinge;
+  const int w = prec == EOLC_PREC_FP64 ? 1 : 0;
+  if (T.n_eol == 0 && T.atiles[w] > 0) {
+    if (w) launch_tiled<double>(T, w, x, X, m, mats, node_inst, A64, A32, Mblk, s);
+    else launch_tiled<float>(T, w, x, X, m, mats, node_inst, A64, A32, Mblk, s);
+    return 1;
+  }
   if (prec == EOLC_PREC_FP64) {
     double *Kt = static_cast<double *>(elem), *t8 = Kt + size_t(nt) * 81, *Kh = t8 + nt;
     tri_blocks_kernel<double><<<(nt + 127) / 128, 128, 0, s>>>(nt, T.tri.p, x, X, m, mats,
@@ -331,6 +565,7 @@ void launch_assemble_blocks(const DevTopology &T, const double *x,
         nb, T.cptr.p, T.contrib.p, Kt, t8, Kh, A64, A32, Mblk, T.n_real, T.n_nodes,
         T.blk_row.p, T.colidx.p, T.tri.p, T.hinge.p, x, X);
   }
+  return nh > 0 ? 3 : 2;
 }
 
 // Bending force of hinge e on its local vertex a: c (a x s0_v + b x s1_v),
@@ -422,9 +657,11 @@ bsr_rhs_kernel(int n_nodes, const int *__restrict__ rowptr, const int *__restric
   for (int r = 0; r < 3; ++r) b[3 * i + r] = -(mv[r] + h * f[3 * i + r]);
 }
 
-// The force pass's per-triangle words follow the element blocks, 256-byte
-// aligned.
+// The force pass's per-triangle words follow the element blocks of the
+// two-pass assembly, 256-byte aligned (the tiled assembly needs none).
 size_t forces_scratch_offset(const DevTopology &T, int prec) {
+  const int w = prec == EOLC_PREC_FP64 ? 1 : 0;
+  if (T.n_eol == 0 && T.atiles[w] > 0) return 0;
   const size_t e = prec == EOLC_PREC_FP64 ? sizeof(double) : sizeof(float);
   return (e * (size_t(T.n_tri) * 82 + size_t(T.n_hinge) * 144) + 255) / 256 * 256;
 }

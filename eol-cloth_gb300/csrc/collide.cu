@@ -968,6 +968,7 @@ extern "C" eolc_status eolc_cd2(eolc_ctx *ctx, const double *x_h,
   int aparts = std::max(1, std::min(64, (N + kCThreads - 1) / kCThreads));
   aabb_partial_kernel<<<aparts, kCThreads, 0, s>>>(N, W.v2.p, W.aabb_part.p);
   aabb_final_kernel<<<1, 32, 0, s>>>(aparts, W.aabb_part.p, W.aabb.p);
+  ctx->launches += 4;
   // vertex-face queries (points and box corners) against the cloth faces
   if (nq > 0) {
     dim3 grid(vf_parts, nq);
@@ -976,10 +977,13 @@ extern "C" eolc_status eolc_cd2(eolc_ctx *ctx, const double *x_h,
                                                 threshold, W.part_d.p, W.part_j.p);
     vf_pick_kernel<<<(nq + 127) / 128, 128, 0, s>>>(nq, vf_parts, W.part_d.p, W.part_j.p,
                                                     W.best_q.p);
+    ctx->launches += 2;
   }
   // item info in output order
-  if (n_points > 0)
+  if (n_points > 0) {
     copy_best_kernel<<<(n_points + 127) / 128, 128, 0, s>>>(n_points, W.best_q.p, W.info.p);
+    ctx->launches += 1;
+  }
   for (int b = 0; b < n_boxes; ++b) {
     const Seg &sv = T.s[1 + 3 * b], &sc = T.s[2 + 3 * b], &se = T.s[3 + 3 * b];
     v2f1_kernel<<<(N + 127) / 128, 128, 0, s>>>(N, F, W.v2.p, W.boxes.p + b, threshold,
@@ -988,6 +992,7 @@ extern "C" eolc_status eolc_cd2(eolc_ctx *ctx, const double *x_h,
     ee_mask_kernel<<<(E + 127) / 128, 128, 0, s>>>(E, W.edges.p, W.v2.p, W.fn0.p,
                                                    W.boxes.p + b, threshold,
                                                    W.info.p + se.start);
+    ctx->launches += 3;
   }
   if (L > 0) {
     scan_reduce_kernel<<<n_scan, kCThreads, 0, s>>>(L, T, W.info.p, W.bsum.p);
@@ -1005,6 +1010,7 @@ extern "C" eolc_status eolc_cd2(eolc_ctx *ctx, const double *x_h,
     wa.capacity = capacity;
     wa.out = W.out.p;
     write_kernel<<<(L + 127) / 128, 128, 0, s>>>(L, T, wa);
+    ctx->launches += 4;
   }
   CK(cudaGetLastError());
   int sc[2] = {0, 0};

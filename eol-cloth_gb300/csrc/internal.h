@@ -78,6 +78,14 @@ struct DevTopology {
   DevBuf<int> tri, hinge, rowptr, colidx, blk_row, diag, cptr, contrib,
       nf_ptr, nf_list, eol, eol_node;
   DevBuf<int> nh_ptr, nh_list;  // node -> hinges (hinge << 2 | local vertex), n_real rows
+  // Row tiles of the shared-memory assembly (assemble.cu), per element size
+  // (0: FP32, 1: FP64), built on first use: tile boundaries (block rows) and
+  // the tile-local shared-memory slot of every contribution (parallel to
+  // contrib; bit 15 set for a triangle's).  atiles: tile count, -1 not built,
+  // 0 when some row does not fit a tile (the two-pass assembly runs).
+  int atiles[2] = {-1, -1};
+  DevBuf<int> atile_row[2];
+  DevBuf<unsigned short> aslot[2];
 };
 
 struct MaterialD {
@@ -108,11 +116,16 @@ std::string build_edges_device(EdgeScratch *&w, const int *tri_d, int nf, DevBuf
 // instead of m for batched topologies.
 // elem: device scratch of assemble_scratch_bytes(T, prec) for the element
 // blocks.  Launches the triangle pass, the hinge pass and the block gather.
-void launch_assemble_blocks(const DevTopology &T, const double *x,
-                            const double *X, const MaterialD &m,
-                            const MaterialD *mats, const int *node_inst,
-                            int prec, void *elem, double *A64, float *A32, double *Mblk,
-                            cudaStream_t s);
+// Returns the number of kernels launched: one for the shared-memory tiled
+// assembly (non-EOL topologies whose tiles are built), else three.
+int launch_assemble_blocks(const DevTopology &T, const double *x,
+                           const double *X, const MaterialD &m,
+                           const MaterialD *mats, const int *node_inst,
+                           int prec, void *elem, double *A64, float *A32, double *Mblk,
+                           cudaStream_t s);
+// Builds T's row tiles for precision prec if they are not built yet (a no-op
+// for EOL topologies).  "" on success.
+std::string ensure_assembly_tiles(DevTopology &T, int prec, cudaStream_t s, long long &launches);
 size_t assemble_scratch_bytes(const DevTopology &T, int prec);
 // Forces and right-hand side, always in FP64 (the FP64 refinement residual
 // of the mixed-precision solve is only as accurate as b): a triangle pass and

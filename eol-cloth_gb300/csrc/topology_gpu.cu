@@ -464,6 +464,7 @@ std::string build_topology_device(TopoScratch *&w, int N, const int *tri_d, int 
   T.n_nodes = Nt;
   T.n_real = N;
   T.n_eol = n_eol;
+  T.atiles[0] = T.atiles[1] = -1;  // assembly tiles follow the new pattern
   T.n_tri = n_tri;
   T.n_hinge = n_hinge;
   T.n_blocks = nblk;

@@ -18,7 +18,9 @@
 // stores and nothing but the BSR goes to memory.  No atomics: bit-
 // reproducible.  Element matrices are symmetric: a block (a, b) with a > b is
 // the transpose of the evaluated (b, a), as in the element pass below, so
-// the assembled matrix is exactly symmetric.
+// every off-diagonal BSR block is the exact transpose of its partner (both
+// sum the same elements in the same order); diagonal blocks are symmetric up
+// to the rounding of the element formulas.
 //
 // EOL topologies (and meshes whose rows do not fit a tile) take the two-pass
 // path: an element pass (one thread per triangle, one per hinge) writes every

@@ -131,6 +131,36 @@ def cpu_step_seconds(sc, x, v, max_seconds=40.0):
     return time.perf_counter() - t0, it
 
 
+def batch_cpu_baseline(B, x, v, n_sample=16):
+    """The oracle's step (triplet assembly + FP64 Jacobi CG to 1e-8) on
+    n_sample instances spanning the batch's size range (evenly spaced ranks
+    by node count), from the batch's state, one thread; the whole batch's
+    time is estimated as the sample's time x (all nodes / sampled nodes)."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O  # the CPU baseline leg: the oracle is the thing timed here
+    sizes = np.array([s["n"] for s in B["sheets"]])
+    order = np.argsort(sizes, kind="stable")
+    picks = sorted(set(int(order[k]) for k in
+                       np.linspace(0, len(order) - 1, n_sample).round().astype(int)))
+    off = B["node_off"]
+    secs, nodes = 0.0, 0
+    for k in picks:
+        s, m = B["sheets"][k], B["mats"][k]
+        xk = x[3 * off[k]:3 * off[k + 1]].copy()
+        vk = v[3 * off[k]:3 * off[k + 1]].copy()
+        t0 = time.perf_counter()
+        O.step(xk, s["X"], vk, s["tri"], s["hinge"], O.material(**m), GRAV, H, s["fixed"],
+               s["fixed_vel"], tol=1e-8)
+        secs += time.perf_counter() - t0
+        nodes += s["n"]
+    est = secs * float(sizes.sum()) / nodes
+    return {"value": len(B["sheets"]) / est, "unit": "sheet-steps/s", "cores": 1, "kind": "port",
+            "sample": "oracle steps of %d of the %d instances (evenly spaced by size) from the "
+                      "post-warm-up state, %.1f s; the batch's time scaled by node count"
+                      % (len(picks), len(B["sheets"]), secs)}
+
+
 def run_batched(args, local_rank, stream, flush):
     """Batched workload: 256 independent sheets, side ~ U{16..96} quads, E ~
     U(20, 100) (seeded), corners 3 and 4 pinned, all stepped by one graph
@@ -168,6 +198,8 @@ def run_batched(args, local_rank, stream, flush):
     launches = ctx.launch_count() - launches0
     total = sum(step_ms)
     n_nodes = int(B["node_off"][-1])
+    x_w, v_w = ctx.state_download()
+    cpu = optional_line(lambda: batch_cpu_baseline(B, x_w, v_w))
     return {
         "workload": "%d sheets, side U{16..96} quads (seed 3), E U(20,100), %d nodes total,"
                     " 2 corners pinned each" % (args.batch_sheets, n_nodes),
@@ -182,6 +214,7 @@ def run_batched(args, local_rank, stream, flush):
         "gpu_launches_per_step": launches / args.steps,
         "host_setup_s": setup_s,
         "l2": "flushed (256 MiB write) before each step",
+        "cpu_baseline": cpu,
     }
 
 
@@ -237,13 +270,14 @@ def run_delaunay(args, local_rank, stream, flush):
                      "mean_pcg_iters_per_sheet": iters / (args.steps * len(B["sheets"])),
                      "fallbacks": fb, "max_rel_res": worst}
     n_tri = sum(len(s["tri"]) for s in B["sheets"])
+    cpu = optional_line(lambda: batch_cpu_baseline(B, x_w, v_w))
     return {"workload": "%d Delaunay sheets, U(5k, 50k) triangles (seed 5), %d triangles and %d "
                         "nodes in total, top corners pinned" % (len(B["sheets"]), n_tri,
                                                                  int(B["node_off"][-1])),
             "arms": out, "learned_vs_jacobi": out["learned"]["sheet_steps_per_s"] /
             out["jacobi"]["sheet_steps_per_s"],
             "autotuned_config": eolc.batch_config_name(chosen), "host_setup_s": setup_s,
-            "l2": "flushed (256 MiB write) before each step"}
+            "l2": "flushed (256 MiB write) before each step", "cpu_baseline": cpu}
 
 
 def run_reference(args, rank):
@@ -333,6 +367,96 @@ def job_rate(world, steps, total_ms):
     """Whole-job steps/s: each of `world` replicas runs `steps` steps and
     the job ends with the slowest one, `total_ms` after it started."""
     return world * steps / (total_ms / 1e3)
+
+
+def shard_instances(sizes, world):
+    """Deterministic node-count-balanced split of a batch's instances over
+    `world` ranks (the batched configurations shard by instance, with no
+    data-path exchange): instances in decreasing size, ties by index, each
+    to the rank with the fewest nodes so far, ties to the lower rank.
+    Returns every rank's instance indices, ascending."""
+    order = sorted(range(len(sizes)), key=lambda k: (-int(sizes[k]), k))
+    load, out = [0] * world, [[] for _ in range(world)]
+    for k in order:
+        r = min(range(world), key=lambda q: (load[q], q))
+        out[r].append(k)
+        load[r] += int(sizes[k])
+    return [sorted(o) for o in out]
+
+
+def sub_batch(B, idx):
+    """The batch of instances idx (ascending) of batch B, in the layout of
+    scenes.batch: per-instance scenes and materials, concatenated state and
+    global fixed DOFs."""
+    import numpy as np
+    sheets = [B["sheets"][k] for k in idx]
+    mats = [B["mats"][k] for k in idx]
+    off = [0]
+    for s in sheets:
+        off.append(off[-1] + s["n"])
+    bo = B["node_off"]
+    x = np.concatenate([B["x"][3 * bo[k]:3 * bo[k + 1]] for k in idx])
+    X = np.concatenate([B["X"][2 * bo[k]:2 * bo[k + 1]] for k in idx])
+    v = np.concatenate([B["v"][3 * bo[k]:3 * bo[k + 1]] for k in idx])
+    fixed = np.concatenate([s["fixed"] + 3 * o for s, o in zip(sheets, off[:-1])]).astype(np.int32)
+    return dict(sheets=sheets, mats=mats, node_off=np.array(off), x=x, X=X, v=v, fixed=fixed,
+                fixed_vel=np.zeros(len(fixed)))
+
+
+def merge_shards(n_inst, parts):
+    """Per-instance results of every rank, parts[r] = [(instance, value), ...],
+    merged into instance order; every instance must come exactly once."""
+    out = [None] * n_inst
+    for part in parts:
+        for k, val in part:
+            if out[k] is not None:
+                raise ValueError("instance %d stepped twice" % k)
+            out[k] = val
+    missing = [k for k in range(n_inst) if out[k] is None]
+    if missing:
+        raise ValueError("instances %s not stepped" % missing[:8])
+    return out
+
+
+def run_batched_sharded(args, rank, world, local_rank, stream, flush, dev):
+    """Configuration 3 split over the ranks by instance (shard_instances):
+    each rank steps its share in one batched launch per step; the job's
+    sheet-steps/s is all instances x K over the slowest rank's time."""
+    import numpy as np
+    import torch
+    import eolc
+    import scenes
+    B = scenes.batch(args.batch_sheets, lo=16, hi=96, seed=3)
+    mine = shard_instances([s["n"] for s in B["sheets"]], world)[rank]
+    S = sub_batch(B, mine)
+    ctx = eolc.Context(local_rank)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_topology_batched([(s["n"], s["tri"], s["hinge"]) for s in S["sheets"]])
+    ctx.set_instance_materials([eolc.Material(**m) for m in S["mats"]])
+    ctx.state_upload(S["x"], S["X"], S["v"])
+    opts = eolc.SolveOpts(rel_tol=1e-8, precision=eolc.PREC_MIXED, precond=eolc.PC_JACOBI)
+    ctx.step_batched(args.warmup, GRAV, H, S["fixed"], S["fixed_vel"], opts)
+    torch.distributed.barrier()
+    torch.cuda.synchronize()
+    step_ms = []
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        ctx.step_batched(1, GRAV, H, S["fixed"], S["fixed_vel"], opts)
+        e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+    total = max_over_ranks(sum(step_ms), world, dev)
+    return {"workload": "%d sheets, side U{16..96} quads (seed 3), split over %d ranks by "
+                        "instance (node-count balanced), %d on this rank"
+                        % (args.batch_sheets, world, len(mine)),
+            "sheet_steps_per_s": args.batch_sheets * args.steps / (total / 1e3),
+            "ms_per_batch_step": total / args.steps, "scaling": "strong",
+            "note": "unmeasured on hardware until a multi-GPU run happens; no collective on "
+                    "the data path (the timed-interval maximum only)"}
 
 
 def time_arm(ctx, sc, mat, opts, x_w, v_w, steps, stream, flush, world, dev, refresh=1):
@@ -757,6 +881,10 @@ def run_ours(args, rank, world, local_rank):
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
     e2e_total = max_over_ranks(sum(e2e_ms), world, dev)
     e2e_val = job_rate(world, args.steps, e2e_total)
+    sharded = None
+    if world > 1 and not args.no_batch:
+        sharded = optional_line(lambda: run_batched_sharded(args, rank, world, local_rank, stream,
+                                                            flush, dev))
 
     if rank != 0:
         return
@@ -832,6 +960,8 @@ def run_ours(args, rank, world, local_rank):
         line["learned_vs_jacobi"] = results[bl]["steps_per_s"] / results["jacobi"]["steps_per_s"]
     if cpu:
         line["cpu_baseline"] = cpu
+    if sharded is not None:
+        line["batched_sharded"] = sharded
     if world == 1 and not args.no_cd2:
         line["cd2"] = optional_line(lambda: run_cd2(args, local_rank, stream))
     if world == 1 and not args.no_export:

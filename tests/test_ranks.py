@@ -87,3 +87,79 @@ def test_reference_arm_runs_on_rank_zero_only():
                        capture_output=True, text=True, timeout=120)
     assert p.returncode == 0, p.stderr
     assert p.stdout.strip() == ""
+
+
+SHARD_WORKER = r"""
+import json, os, sys
+sys.path.insert(0, os.environ["BENCH_ROOT"])
+for sub in ("oracle", "tests", "eol-cloth_gb300"):
+    sys.path.insert(0, os.path.join(os.environ["BENCH_ROOT"], sub))
+import numpy as np
+import torch.distributed as dist
+import bench, scenes, oracle as O
+rank, world = int(os.environ["RANK"]), int(os.environ["WORLD_SIZE"])
+dist.init_process_group("gloo")
+B = scenes.batch(9, lo=3, hi=10, seed=4)
+mine = bench.shard_instances([s["n"] for s in B["sheets"]], world)[rank]
+S = bench.sub_batch(B, mine)
+part = []
+for j, k in enumerate(mine):
+    s, m = S["sheets"][j], S["mats"][j]
+    o = S["node_off"]
+    x, v = S["x"][3 * o[j]:3 * o[j + 1]].copy(), S["v"][3 * o[j]:3 * o[j + 1]].copy()
+    for _ in range(2):
+        O.step(x, s["X"], v, s["tri"], s["hinge"], O.material(**m), scenes.GRAV, scenes.H,
+               s["fixed"], s["fixed_vel"], tol=1e-10)
+    part.append((k, x.tobytes().hex() + ":" + v.tobytes().hex()))
+parts = [None] * world
+dist.all_gather_object(parts, part)
+merged = bench.merge_shards(len(B["sheets"]), parts)
+print(json.dumps({"rank": rank, "mine": mine, "merged": merged}))
+dist.destroy_process_group()
+"""
+
+
+def test_batched_instances_shard_across_ranks():
+    """World size 2: the batch is split by instance (node-count balanced),
+    every instance is stepped exactly once, and the merged states equal a
+    single rank stepping every instance, bit for bit (here with the oracle's
+    step on the CPU standing in for the GPU's batched step)."""
+    outs = _run_ranks(2, {}, [sys.executable, "-c", SHARD_WORKER], timeout=300)
+    got = []
+    for rc, o, e in outs:
+        assert rc == 0, e
+        got.append(json.loads(o.strip().splitlines()[-1]))
+    mine = [g["mine"] for g in sorted(got, key=lambda g: g["rank"])]
+    assert sorted(mine[0] + mine[1]) == list(range(9)) and not set(mine[0]) & set(mine[1])
+    assert got[0]["merged"] == got[1]["merged"]
+    sys.path.insert(0, ROOT)
+    for sub in ("oracle", "tests", "eol-cloth_gb300"):
+        sys.path.insert(0, os.path.join(ROOT, sub))
+    import oracle as O
+    import scenes
+    B = scenes.batch(9, lo=3, hi=10, seed=4)
+    off = B["node_off"]
+    for k, s in enumerate(B["sheets"]):
+        x = B["x"][3 * off[k]:3 * off[k + 1]].copy()
+        v = B["v"][3 * off[k]:3 * off[k + 1]].copy()
+        for _ in range(2):
+            O.step(x, s["X"], v, s["tri"], s["hinge"], O.material(**B["mats"][k]), scenes.GRAV,
+                   scenes.H, s["fixed"], s["fixed_vel"], tol=1e-10)
+        assert got[0]["merged"][k] == x.tobytes().hex() + ":" + v.tobytes().hex()
+
+
+def test_shard_split_is_balanced_and_deterministic():
+    sys.path.insert(0, ROOT)
+    import bench
+    sizes = [100, 90, 80, 10, 10, 10, 5]
+    a = bench.shard_instances(sizes, 2)
+    assert a == bench.shard_instances(sizes, 2)
+    loads = [sum(sizes[k] for k in part) for part in a]
+    assert abs(loads[0] - loads[1]) <= max(sizes)
+    assert sorted(a[0] + a[1]) == list(range(len(sizes)))
+    assert bench.shard_instances(sizes, 1) == [list(range(len(sizes)))]
+    import pytest
+    with pytest.raises(ValueError):
+        bench.merge_shards(2, [[(0, 1)], [(0, 1), (1, 2)]])
+    with pytest.raises(ValueError):
+        bench.merge_shards(3, [[(0, 1)], [(1, 2)]])

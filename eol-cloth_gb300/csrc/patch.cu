@@ -75,13 +75,13 @@ struct RCfg {  // CTA shape of the resident kernels (block_sum3 / reduce_partial
 constexpr int kRThreads = RCfg::kThreads;
 constexpr int kMaxRows = 464;       // rows of one patch (one thread each)
 constexpr int kTargetRows = 448;    // rows per patch the partition aims for
-constexpr int kMaxFwd = 3328;       // forward records: off-diagonal upper + halo blocks
+constexpr int kMaxFwd = 3312;       // forward records: off-diagonal upper + halo blocks
 constexpr int kMaxSlots = 2688;     // transposed products (one per off-diagonal upper block)
 constexpr int kMaxHaloNodes = 384;  // distinct outside nodes the halo blocks touch
 constexpr int kMaxCount = 255;      // records or slots of one row (8-bit counts)
 constexpr int kWarps = kRThreads / 32;
 constexpr float kLoFrac = 30.f;     // Chebyshev interval [lmax / 30, lmax]
-constexpr int kMaxAgg = 42;         // coarse aggregates (3 coarse unknowns each)
+constexpr int kMaxAgg = 152;        // coarse aggregates (3 coarse unknowns each): one per patch
 constexpr int kMaxTgt = 16;         // aggregates one patch's rows couple to
 constexpr int kCoarseWords = 12;    // per-CTA coarse partials: sums of r, w, s (+ pad)
 constexpr float kBoundMargin = 1.02f;
@@ -111,8 +111,10 @@ constexpr size_t kOffDs = kOffXh + size_t(kMaxHaloNodes) * 16;
 constexpr size_t kOffHnode = kOffDs + size_t(kMaxRows) * 16;
 constexpr size_t kResidentSmem = al16(kOffHnode + size_t(kMaxHaloNodes) * 4);
 static_assert(kResidentSmem <= 222 * 1024, "resident image exceeds shared memory");
-// the coarse set-up and reductions use the slot and vector images as scratch
-static_assert(size_t(3 * kMaxAgg) * (3 * kMaxAgg) * 4 <= kOffHnode - kOffS, "coarse matrix scratch");
+// the coarse set-up and reductions use the slot image as scratch
+static_assert(size_t(kMaxAgg) * 40 + (kRThreads / 32 + 1) * 4 <= size_t(kMaxSlots) * 16,
+              "coarse row-block scratch");
+static_assert(3 * kMaxAgg <= kRThreads, "one coarse column per thread");
 static_assert(size_t(kCoarseWords) * 32 * 6 * 4 <= size_t(kMaxSlots) * 16, "coarse partial scratch");
 
 struct ResParams {
@@ -142,9 +144,11 @@ struct ResParams {
   // patch and of every halo node, per patch its target
   // aggregates; cpart: per (patch, target) the CTA's sum of masked blocks;
   // partc: per-CTA sums of r, w, s, [2][G][kCoarseWords]
-  int n_agg, coarse_fresh;                 // fresh: rebuild X_own (else reuse Xg)
+  // Xc: the coarse inverse (3 n_agg square), kept across solves; Xn, Yc:
+  // Newton-Schulz scratch of the same size
+  int n_agg, coarse_fresh, coarse_cold;    // fresh: update Xc; cold: from X0
   const int *patch_agg, *hagg, *ctgt, *cl_ptr, *cl_idx;
-  float *cpart, *partc, *Xg;               // Xg: every CTA's X_own of the last build
+  float *cpart, *partc, *Xc, *Xn, *Yc;
   unsigned long long *tw;                  // neighbour exchange: tagged u, [2][N][4] words
   unsigned seq;                            // launch number in the tags (1..4095)
   double *part;
@@ -797,6 +801,196 @@ __device__ void inverse3_masked(const float (&D)[9], const float (&m)[3], float 
 // by in-place Gauss-Jordan (SPD: no pivoting) and keeps the three rows of
 // its own aggregate of (X + X^T) / 2 in X_own.  Returns false when the grid
 // barrier timed out.
+// 3x3 inverse of an SPD block (cofactors).
+__device__ __forceinline__ void inverse3_spd(const float a[9], float o[9]) {
+  const float c00 = a[4] * a[8] - a[5] * a[7], c01 = a[5] * a[6] - a[3] * a[8],
+              c02 = a[3] * a[7] - a[4] * a[6];
+  const float det = a[0] * c00 + a[1] * c01 + a[2] * c02;
+  const float id = det != 0.f ? 1.f / det : 0.f;
+  o[0] = c00 * id; o[1] = (a[2] * a[7] - a[1] * a[8]) * id; o[2] = (a[1] * a[5] - a[2] * a[4]) * id;
+  o[3] = c01 * id; o[4] = (a[0] * a[8] - a[2] * a[6]) * id; o[5] = (a[2] * a[3] - a[0] * a[5]) * id;
+  o[6] = c02 * id; o[7] = (a[1] * a[6] - a[0] * a[7]) * id; o[8] = (a[0] * a[4] - a[1] * a[3]) * id;
+}
+
+// The coarse inverse X = A_c^-1 (n_c = 3 n_agg square, FP32, in global memory
+// and kept from solve to solve) by Newton-Schulz: X <- 2 X - X A_c X, whose
+// error E = I - A_c X squares at every update.  CTA a (a < n_agg) owns the
+// three rows of aggregate a: the symmetrised blocks (a, b) of A_c from the
+// per-(patch, target) sums in cpart (contributor lists, fixed order) go to a
+// compact list in shared memory (deterministic compaction); then
+//   Y = A_c X      rows of a (threads over columns), ||Y - I||_F^2 summed
+//                  over the grid (one reduction, every CTA takes the same
+//                  decision);
+//   Xn = 2 X - X Y rows of a (X rows staged in X_own), grid barrier;
+//   X = (Xn + Xn^T) / 2  rows of a, grid barrier.
+// A warm solve (X of the last solve; A_c changes slowly from step to step)
+// makes one update, or none when X already inverts the new A_c to 1e-4.  A
+// cold solve (the plan's first, or an X that no longer contracts) starts from
+// X0 = blockdiag(A_aa)^-1 / kMaxTgt — eigenvalues of X0 A_c in (0, 1], as no
+// aggregate couples to more than kMaxTgt aggregates and every scaled block
+// has norm <= 1 — and iterates to 1e-3 (at most kNsMaxIter updates).  X stays
+// symmetric positive definite, so M = M_patch + R^T X R keeps PCG exact.
+// An axis of an aggregate without free DOFs (a zero row of A_c) gets a unit
+// diagonal (its residual sums are zero).  On exit X_own holds the rows of
+// this CTA's aggregate.  Returns false when a grid barrier timed out.
+constexpr int kNsMaxIter = 64;
+__device__ bool coarse_inverse(const ResParams &P, const ResSmem &sm, int cta, GridSum &sync,
+                               Acc<float>::V *red, float *X_own) {
+  using Ac = Acc<float>;
+  const int n_agg = P.n_agg, nc = 3 * n_agg;
+  const int a = cta;
+  const bool rows = a < n_agg;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float *blk = reinterpret_cast<float *>(sm.slot);        // compact blocks, 9 floats each
+  int *bid = reinterpret_cast<int *>(blk + 9 * kMaxAgg);  // their column aggregates
+  int *wcnt = bid + kMaxAgg;                               // per-warp counts (compaction)
+  int *nblk = wcnt + kWarps;
+  // symmetrised block (a, b) of A_c, masked axes made unit
+  {
+    const int b = threadIdx.x;
+    float v[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) v[q] = 0.f;
+    bool nz = false;
+    if (rows && b < n_agg) {
+      const int j0 = P.cl_ptr[size_t(a) * n_agg + b], j1 = P.cl_ptr[size_t(a) * n_agg + b + 1];
+      const int t0 = P.cl_ptr[size_t(b) * n_agg + a], t1 = P.cl_ptr[size_t(b) * n_agg + a + 1];
+      nz = j1 > j0 || t1 > t0;
+      float u[9], t[9];
+#pragma unroll
+      for (int q = 0; q < 9; ++q) { u[q] = 0.f; t[q] = 0.f; }
+      for (int j = j0; j < j1; ++j) {
+        const float *src = P.cpart + size_t(P.cl_idx[j]) * 9;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) u[q] += __ldcg(src + q);
+      }
+      for (int j = t0; j < t1; ++j) {
+        const float *src = P.cpart + size_t(P.cl_idx[j]) * 9;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) t[q] += __ldcg(src + q);
+      }
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) v[3 * r + c] = 0.5f * (u[3 * r + c] + t[3 * c + r]);
+      if (b == a) {
+        nz = true;
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          if (!(v[4 * c] > 0.f)) {
+#pragma unroll
+            for (int q = 0; q < 3; ++q) { v[3 * c + q] = 0.f; v[3 * q + c] = 0.f; }
+            v[4 * c] = 1.f;
+          }
+      }
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, nz);
+    if (lane == 0) wcnt[warp] = __popc(bal);
+    __syncthreads();
+    int base = 0;
+    for (int w2 = 0; w2 < warp; ++w2) base += wcnt[w2];
+    if (nz) {
+      const int k = base + __popc(bal & ((1u << lane) - 1u));
+#pragma unroll
+      for (int q = 0; q < 9; ++q) blk[9 * k + q] = v[q];
+      bid[k] = b;
+    }
+    if (threadIdx.x == 0) {
+      int tot = 0;
+      for (int w2 = 0; w2 < kWarps; ++w2) tot += wcnt[w2];
+      *nblk = tot;
+    }
+    __syncthreads();
+  }
+  const int nb = *nblk;
+  const int j = threadIdx.x;  // the column this thread updates (nc <= kRThreads)
+  bool cold = P.coarse_cold != 0;
+  auto write_x0 = [&]() {  // rows of a of X0 = blockdiag(A_aa)^-1 / kMaxTgt
+    if (!rows || j >= nc) return;
+    float d[9], di[9];
+    for (int k = 0; k < nb; ++k)
+      if (bid[k] == a)
+        for (int q = 0; q < 9; ++q) d[q] = blk[9 * k + q];
+    inverse3_spd(d, di);
+    for (int r = 0; r < 3; ++r) {
+      const int c = j - 3 * a;
+      P.Xc[size_t(3 * a + r) * nc + j] =
+          (c >= 0 && c < 3) ? di[3 * r + c] * (1.f / float(kMaxTgt)) : 0.f;
+    }
+  };
+  if (cold) {
+    write_x0();
+    if (!sync.barrier()) return false;
+  }
+  bool use = true;  // false: drop the coarse correction (non-finite A_c)
+  for (int it = 0;; ++it) {
+    // Y = A_c X, rows of a; the grid sum of ||Y - I||_F^2
+    float part = 0.f;
+    if (rows && j < nc) {
+      float y[3] = {0.f, 0.f, 0.f};
+      for (int k = 0; k < nb; ++k) {
+        const float *bk = blk + 9 * k;
+        const float *xb = P.Xc + size_t(3 * bid[k]) * nc + j;
+        const float x0 = __ldcg(xb), x1 = __ldcg(xb + nc), x2 = __ldcg(xb + 2 * size_t(nc));
+#pragma unroll
+        for (int r = 0; r < 3; ++r) y[r] += bk[3 * r] * x0 + bk[3 * r + 1] * x1 + bk[3 * r + 2] * x2;
+      }
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        P.Yc[size_t(3 * a + r) * nc + j] = y[r];
+        const float e = y[r] - (j == 3 * a + r ? 1.f : 0.f);
+        part += e * e;
+      }
+    }
+    Ac::V e2 = Ac::from_d(double(part)), z1 = Ac::zero(), z2 = Ac::zero();
+    if (!sync(e2, z1, z2, red)) return false;
+    const float r2 = Ac::to_t(e2);
+    if (!isfinite(r2)) { use = false; break; }
+    if (r2 <= (cold ? 1e-6f : 1e-8f) * float(nc)) break;  // X inverts A_c closely enough
+    if (!cold && !(r2 < 1.f)) {  // X no longer contracts: start again from X0
+      cold = true;
+      write_x0();
+      if (!sync.barrier()) return false;
+      continue;
+    }
+    if (cold && it >= kNsMaxIter) break;
+    // Xn = 2 X - X Y, rows of a (the rows of X staged in X_own)
+    if (rows)
+      for (int q = threadIdx.x; q < 3 * nc; q += kRThreads)
+        X_own[q] = __ldcg(P.Xc + size_t(3 * a + q / nc) * nc + q % nc);
+    __syncthreads();
+    if (rows && j < nc) {
+      float t[3] = {0.f, 0.f, 0.f};
+      const float *yc = P.Yc + j;
+#pragma unroll 4
+      for (int k = 0; k < nc; ++k) {
+        const float yk = __ldcg(yc + size_t(k) * nc);
+        t[0] += X_own[k] * yk;
+        t[1] += X_own[nc + k] * yk;
+        t[2] += X_own[2 * nc + k] * yk;
+      }
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+        P.Xn[size_t(3 * a + r) * nc + j] = 2.f * X_own[r * nc + j] - t[r];
+    }
+    if (!sync.barrier()) return false;
+    // X = (Xn + Xn^T) / 2, rows of a
+    if (rows && j < nc)
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+        P.Xc[size_t(3 * a + r) * nc + j] =
+            0.5f * (__ldcg(P.Xn + size_t(3 * a + r) * nc + j) + __ldcg(P.Xn + size_t(j) * nc + 3 * a + r));
+    if (!sync.barrier()) return false;
+    if (!cold) break;  // warm: one update
+  }
+  // the rows of this CTA's aggregate
+  const int ag = P.patch_agg[cta];
+  for (int q = threadIdx.x; q < 3 * nc; q += kRThreads)
+    X_own[q] = use ? __ldcg(P.Xc + size_t(3 * ag + q / nc) * nc + q % nc) : 0.f;
+  __syncthreads();
+  return true;
+}
+
 // CTA sum of nine floats (fixed trees); thread 0 writes it to out9 (global).
 __device__ void cta_sum9(float (&v)[9], float *tmp, float *out9) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -825,7 +1019,7 @@ __device__ void cta_sum9(float (&v)[9], float *tmp, float *out9) {
 
 __device__ bool coarse_setup(const ResParams &P, const ResSmem &sm, const RowMeta &M, int cta,
                              int p0, bool own, const V4<float> &m, GridSum &sync, float *tmp,
-                             float *gj, float *X_own) {
+                             Acc<float>::V *red, float *X_own) {
   const unsigned lt = (1u << (threadIdx.x & 31)) - 1u;
   const int n_agg = P.n_agg, nc = 3 * n_agg;
   const int *tg = P.ctgt + size_t(cta) * kMaxTgt;
@@ -887,84 +1081,7 @@ __device__ bool coarse_setup(const ResParams &P, const ResSmem &sm, const RowMet
   }
   (void)p0;
   if (!sync.barrier()) return false;
-  // dense A_c in the free shared memory (slot, vector images): block (a, b)
-  // summed over the patches of a in order
-  float *Ac = reinterpret_cast<float *>(sm.slot);
-  for (int pr = threadIdx.x; pr < n_agg * n_agg; pr += kRThreads) {
-    const int a = pr / n_agg, b = pr % n_agg;
-    float blk[9];
-#pragma unroll
-    for (int q = 0; q < 9; ++q) blk[q] = 0.f;
-    for (int j = P.cl_ptr[pr]; j < P.cl_ptr[pr + 1]; ++j) {
-      const float *src = P.cpart + size_t(P.cl_idx[j]) * 9;
-#pragma unroll
-      for (int q = 0; q < 9; ++q) blk[q] += __ldcg(src + q);
-    }
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) Ac[size_t(3 * a + r) * nc + 3 * b + c] = blk[3 * r + c];
-  }
-  __syncthreads();
-  for (int q = threadIdx.x; q < nc * nc; q += kRThreads) {  // symmetrise
-    const int r = q / nc, c = q % nc;
-    if (r < c) {
-      const float v = 0.5f * (Ac[size_t(r) * nc + c] + Ac[size_t(c) * nc + r]);
-      Ac[size_t(r) * nc + c] = v;
-      Ac[size_t(c) * nc + r] = v;
-    }
-  }
-  // free coarse DOFs only: an axis with no free DOF in its aggregate has a
-  // zero row; it becomes the identity there (its residual sum is zero)
-  __syncthreads();
-  for (int r = threadIdx.x; r < nc; r += kRThreads)
-    if (!(Ac[size_t(r) * nc + r] > 0.f)) {
-      for (int c = 0; c < nc; ++c) { Ac[size_t(r) * nc + c] = 0.f; Ac[size_t(c) * nc + r] = 0.f; }
-      Ac[size_t(r) * nc + r] = 1.f;
-    }
-  __syncthreads();
-  // in-place Gauss-Jordan, two barriers per pivot: the old pivot row and
-  // column are staged (gj), then every entry is updated from them (rows over
-  // warps, columns over lanes, the pivot row segment in registers):
-  //   row k: a_kj p (j != k), p;  others: a_ij - a_ik p a_kj (j != k), -a_ik p
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  constexpr int kJ = (3 * kMaxAgg + 31) / 32;
-  float *rowk = gj, *colk = gj + 3 * kMaxAgg;
-  for (int k = 0; k < nc; ++k) {
-    for (int j = threadIdx.x; j < nc; j += kRThreads) {
-      rowk[j] = Ac[size_t(k) * nc + j];
-      colk[j] = Ac[size_t(j) * nc + k];
-    }
-    __syncthreads();
-    const float pinv = 1.f / rowk[k];
-    float rkp[kJ];
-#pragma unroll
-    for (int q = 0; q < kJ; ++q) {
-      const int j = lane + 32 * q;
-      rkp[q] = j < nc ? rowk[j] * pinv : 0.f;
-    }
-    for (int i = warp; i < nc; i += kWarps) {
-      float *ri = Ac + size_t(i) * nc;
-      const float f = colk[i];
-#pragma unroll
-      for (int q = 0; q < kJ; ++q) {
-        const int j = lane + 32 * q;
-        if (j >= nc) continue;
-        float v;
-        if (i == k) v = j == k ? pinv : rkp[q];
-        else v = j == k ? -f * pinv : ri[j] - f * rkp[q];
-        ri[j] = v;
-      }
-    }
-    __syncthreads();
-  }
-  const int ag = tg[0];
-  for (int q = threadIdx.x; q < 3 * nc; q += kRThreads) {
-    const int r = 3 * ag + q / nc, c = q % nc;
-    X_own[q] = 0.5f * (Ac[size_t(r) * nc + c] + Ac[size_t(c) * nc + r]);
-  }
-  __syncthreads();
-  return true;
+  return coarse_inverse(P, sm, cta, sync, red, X_own);
 }
 
 // After with_coarse: g[3 q + c] = (X_own R q)_c for q = r, w, s, from every
@@ -999,7 +1116,6 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
   __shared__ int s_fail;
   __shared__ float s_tmp9[9 * kWarps], s_X[3 * 3 * kMaxAgg], s_g[9];
   __shared__ int s_pagg[32 * kPartPerLane];  // aggregate of every patch
-  __shared__ float s_gj[2 * 3 * kMaxAgg];     // coarse set-up: pivot row and column
   const ResSmem sm = carve(smem);
   const int cta = blockIdx.x, i = threadIdx.x;
   const int p0 = P.patch_row[cta], np = P.patch_row[cta + 1] - p0;
@@ -1074,11 +1190,12 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
   float ce[3] = {0.f, 0.f, 0.f};  // this patch's coarse correction for the next u
   if (coarse) {
     const int nc3 = 9 * P.n_agg;  // X_own: 3 rows of 3 n_agg
-    if (P.coarse_fresh) {
-      if (!coarse_setup(P, sm, M, cta, p0, own, m, sync, s_tmp9, s_gj, s_X)) return;
-      for (int q = i; q < nc3; q += kRThreads) P.Xg[size_t(cta) * 9 * kMaxAgg + q] = s_X[q];
-    } else {
-      for (int q = i; q < nc3; q += kRThreads) s_X[q] = P.Xg[size_t(cta) * 9 * kMaxAgg + q];
+    if (P.coarse_fresh) {  // update the coarse inverse for this matrix
+      if (!coarse_setup(P, sm, M, cta, p0, own, m, sync, s_tmp9, red, s_X)) return;
+    } else {  // reuse the last one: the rows of this CTA's aggregate
+      const int ag = P.patch_agg[cta];
+      for (int q = i; q < nc3; q += kRThreads)
+        s_X[q] = __ldcg(P.Xc + size_t(3 * ag + q / (3 * P.n_agg)) * (3 * P.n_agg) + q % (3 * P.n_agg));
       __syncthreads();
     }
     V z0 = A::zero(), z1 = A::zero(), z2 = A::zero();
@@ -1255,7 +1372,6 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
   __shared__ int s_fail;
   __shared__ float s_tmp9[9 * kWarps], s_X[3 * 3 * kMaxAgg], s_g[9];
   __shared__ int s_pagg[32 * kPartPerLane];  // aggregate of every patch
-  __shared__ float s_gj[2 * 3 * kMaxAgg];     // coarse set-up: pivot row and column
   const ResSmem sm = carve(smem);
   const int cta = blockIdx.x, i = threadIdx.x;
   const int p0 = P.patch_row[cta], np = P.patch_row[cta + 1] - p0;
@@ -1299,11 +1415,12 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
   float ce[3] = {0.f, 0.f, 0.f};
   if (coarse) {
     const int nc3 = 9 * P.n_agg;
-    if (P.coarse_fresh) {
-      if (!coarse_setup(P, sm, M, cta, p0, own, m, sync, s_tmp9, s_gj, s_X)) return;
-      for (int q = i; q < nc3; q += kRThreads) P.Xg[size_t(cta) * 9 * kMaxAgg + q] = s_X[q];
-    } else {
-      for (int q = i; q < nc3; q += kRThreads) s_X[q] = P.Xg[size_t(cta) * 9 * kMaxAgg + q];
+    if (P.coarse_fresh) {  // update the coarse inverse for this matrix
+      if (!coarse_setup(P, sm, M, cta, p0, own, m, sync, s_tmp9, red, s_X)) return;
+    } else {  // reuse the last one: the rows of this CTA's aggregate
+      const int ag = P.patch_agg[cta];
+      for (int q = i; q < nc3; q += kRThreads)
+        s_X[q] = __ldcg(P.Xc + size_t(3 * ag + q / (3 * P.n_agg)) * (3 * P.n_agg) + q % (3 * P.n_agg));
       __syncthreads();
     }
     V z0 = A::zero(), z1 = A::zero(), z2 = A::zero();
@@ -1885,12 +2002,15 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
   }
   for (int j : hnode) rcnt[j] |= 1 << 24;  // a halo node of some patch: it publishes
   // coarse aggregates: recursive coordinate bisection of the patch centroids
-  // (material coordinates) into n_agg compact groups; without coordinates,
-  // runs of consecutive patches of the bisection order
-  const int n_agg = std::min(G, kMaxAgg);
+  // (material coordinates) into n_agg compact groups (one patch each when
+  // the device has room: n_agg = G); without coordinates, runs of
+  // consecutive patches of the bisection order.  Fewer aggregates when some
+  // patch or aggregate couples to more than kMaxTgt aggregates (the coarse
+  // inverse's starting guess relies on that bound).
+  int n_agg = std::min(G, kMaxAgg);
   std::vector<int> patch_agg(G), node_patch(N), hagg(hnode.size());
-  if (X) {
-    std::vector<double> cx(G, 0.0), cy(G, 0.0);
+  std::vector<double> cx(G, 0.0), cy(G, 0.0);
+  if (X)
     for (int c = 0; c < G; ++c) {
       for (int i = patch_row[c]; i < patch_row[c + 1]; ++i) {
         cx[c] += (*X)[2 * size_t(perm[i])];
@@ -1900,46 +2020,59 @@ std::string build_patch_plan(int N, const std::vector<int> &rowptr,
       cx[c] /= np;
       cy[c] /= np;
     }
-    std::vector<int> ids(G);
-    for (int c = 0; c < G; ++c) ids[c] = c;
-    int next = 0;
-    std::function<void(int, int, int)> split = [&](int lo, int hi, int k) {
-      if (k <= 1) {
-        for (int q = lo; q < hi; ++q) patch_agg[ids[q]] = next;
-        ++next;
-        return;
-      }
-      double x0 = 1e300, x1 = -1e300, y0 = 1e300, y1 = -1e300;
-      for (int q = lo; q < hi; ++q) {
-        x0 = std::min(x0, cx[ids[q]]); x1 = std::max(x1, cx[ids[q]]);
-        y0 = std::min(y0, cy[ids[q]]); y1 = std::max(y1, cy[ids[q]]);
-      }
-      const bool by_x = x1 - x0 >= y1 - y0;
-      std::sort(ids.begin() + lo, ids.begin() + hi, [&](int a, int b) {
-        const double va = by_x ? cx[a] : cy[a], vb = by_x ? cx[b] : cy[b];
-        return va < vb || (va == vb && a < b);
-      });
-      const int k1 = k / 2;
-      const int mid = lo + int((long long)(hi - lo) * k1 / k);
-      split(lo, mid, k1);
-      split(mid, hi, k - k1);
-    };
-    split(0, G, n_agg);
-  } else {
-    for (int c = 0; c < G; ++c) patch_agg[c] = int((long long)c * n_agg / G);
-  }
   for (int c = 0; c < G; ++c)
     for (int i = patch_row[c]; i < patch_row[c + 1]; ++i) node_patch[i] = c;
   std::vector<int> ctgt(size_t(G) * kMaxTgt, -1);
-  for (int c = 0; c < G; ++c) {
-    std::vector<int> t = {patch_agg[c]};
-    for (int h = hnptr[c]; h < hnptr[c + 1]; ++h) {
-      hagg[h] = patch_agg[node_patch[hnode[h]]];
-      if (std::find(t.begin(), t.end(), hagg[h]) == t.end()) t.push_back(hagg[h]);
+  for (;;) {
+    if (X) {
+      std::vector<int> ids(G);
+      for (int c = 0; c < G; ++c) ids[c] = c;
+      int next = 0;
+      std::function<void(int, int, int)> split = [&](int lo, int hi, int k) {
+        if (k <= 1) {
+          for (int q = lo; q < hi; ++q) patch_agg[ids[q]] = next;
+          ++next;
+          return;
+        }
+        double x0 = 1e300, x1 = -1e300, y0 = 1e300, y1 = -1e300;
+        for (int q = lo; q < hi; ++q) {
+          x0 = std::min(x0, cx[ids[q]]); x1 = std::max(x1, cx[ids[q]]);
+          y0 = std::min(y0, cy[ids[q]]); y1 = std::max(y1, cy[ids[q]]);
+        }
+        const bool by_x = x1 - x0 >= y1 - y0;
+        std::sort(ids.begin() + lo, ids.begin() + hi, [&](int a, int b) {
+          const double va = by_x ? cx[a] : cy[a], vb = by_x ? cx[b] : cy[b];
+          return va < vb || (va == vb && a < b);
+        });
+        const int k1 = k / 2;
+        const int mid = lo + int((long long)(hi - lo) * k1 / k);
+        split(lo, mid, k1);
+        split(mid, hi, k - k1);
+      };
+      split(0, G, n_agg);
+    } else {
+      for (int c = 0; c < G; ++c) patch_agg[c] = int((long long)c * n_agg / G);
     }
-    if (int(t.size()) > kMaxTgt) return "patch couples to too many coarse aggregates";
-    std::sort(t.begin() + 1, t.end());
-    std::copy(t.begin(), t.end(), ctgt.begin() + size_t(c) * kMaxTgt);
+    bool fits = true;
+    std::fill(ctgt.begin(), ctgt.end(), -1);
+    std::vector<std::vector<int>> arow(n_agg);  // aggregates each aggregate couples to
+    for (int c = 0; c < G && fits; ++c) {
+      std::vector<int> t = {patch_agg[c]};
+      for (int h = hnptr[c]; h < hnptr[c + 1]; ++h) {
+        hagg[h] = patch_agg[node_patch[hnode[h]]];
+        if (std::find(t.begin(), t.end(), hagg[h]) == t.end()) t.push_back(hagg[h]);
+      }
+      if (int(t.size()) > kMaxTgt) { fits = false; break; }
+      std::sort(t.begin() + 1, t.end());
+      std::copy(t.begin(), t.end(), ctgt.begin() + size_t(c) * kMaxTgt);
+      std::vector<int> &r = arow[patch_agg[c]];
+      for (int b : t)
+        if (std::find(r.begin(), r.end(), b) == r.end()) r.push_back(b);
+      if (int(r.size()) > kMaxTgt) fits = false;
+    }
+    if (fits) break;
+    if (n_agg == 1) return "patch couples to too many coarse aggregates";
+    n_agg = std::max(1, n_agg * 2 / 3);
   }
   std::vector<std::vector<int>> members(n_agg);
   for (int c = 0; c < G; ++c) members[patch_agg[c]].push_back(c);
@@ -2024,7 +2157,7 @@ struct PatchWork {
   DevBuf<unsigned long long> tw;  // neighbour exchange: tagged values, zeroed once per plan
   int n_agg = 0;                  // coarse aggregates of the plan
   DevBuf<int> patch_agg, hagg, ctgt, cl_ptr, cl_idx;
-  DevBuf<float> cpart, partc, Xg;
+  DevBuf<float> cpart, partc, Xc, Xn, Yc;
   DevBuf<double> npart;           // per set-up block: partial of ||rhs||^2
   int coarse_age = -1;            // solves since the coarse operator was built (-1: never)
   unsigned seq = 0;               // launches (tag generation)
@@ -2095,7 +2228,9 @@ eolc_status patch_plan(PatchWork *w, const DevTopology &Tp, const double *X_d, i
       upload_vec(w->hagg, L.hagg, s), upload_vec(w->cl_ptr, L.cl_ptr, s),
       upload_vec(w->cl_idx, L.cl_idx, s),
       w->cpart.resize(size_t(L.G) * kMaxTgt * 9),
-      w->Xg.resize(size_t(L.G) * 9 * kMaxAgg),
+      w->Xc.resize(size_t(9) * L.n_agg * L.n_agg + 1),
+      w->Xn.resize(size_t(9) * L.n_agg * L.n_agg + 1),
+      w->Yc.resize(size_t(9) * L.n_agg * L.n_agg + 1),
       w->partc.resize(size_t(2) * kCoarseWords * L.G),
       w->tw.resize(size_t(8) * N),
       cudaMemsetAsync(w->tw.p, 0, sizeof(unsigned long long) * 8 * size_t(N), s),
@@ -2225,11 +2360,15 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, i
   P.slice_len = w->slice_len.p;
   P.n_agg = ((patch_pc || learned) && coarse) ? w->n_agg : 0;
   P.coarse_fresh = 1;
-  if (P.n_agg > 0) {  // rebuild the coarse operator, or reuse the last one
+  P.coarse_cold = 1;
+  if (P.n_agg > 0) {  // update the coarse inverse, or reuse the last one
+    P.coarse_cold = w->coarse_age < 0 ? 1 : 0;
     P.coarse_fresh = (w->coarse_age < 0 || w->coarse_age + 1 >= coarse_refresh) ? 1 : 0;
     w->coarse_age = P.coarse_fresh ? 0 : w->coarse_age + 1;
   }
-  P.Xg = w->Xg.p;
+  P.Xc = w->Xc.p;
+  P.Xn = w->Xn.p;
+  P.Yc = w->Yc.p;
   P.patch_agg = w->patch_agg.p;
   P.hagg = w->hagg.p;
   P.ctgt = w->ctgt.p;

@@ -17,10 +17,11 @@
 // store consecutive words, so the BSR is written with full-sector coalesced
 // stores and nothing but the BSR goes to memory.  No atomics: bit-
 // reproducible.  Element matrices are symmetric: a block (a, b) with a > b is
-// the transpose of the evaluated (b, a), as in the element pass below, so
-// every off-diagonal BSR block is the exact transpose of its partner (both
-// sum the same elements in the same order); diagonal blocks are symmetric up
-// to the rounding of the element formulas.
+// the transpose of the evaluated (b, a), and a block and its partner sum the
+// same elements in the same order.  The block formulas are compiled once per
+// local row (vertex selections folded to constants), so the two evaluations
+// of an element block may contract their multiply-adds differently: the
+// matrix is symmetric to the last bit of its precision, not exactly.
 //
 // EOL topologies (and meshes whose rows do not fit a tile) take the two-pass
 // path: an element pass (one thread per triangle, one per hinge) writes every
@@ -272,6 +273,94 @@ __device__ __forceinline__ void store_block(T *sk, int slot, const T blk[9], boo
   }
 }
 
+// Per-step inputs of the tiled kernel, one launch (prep_kernel), written to
+// the assembly scratch:
+//   xhl   FP32 path: every node's position split into float hi / lo words,
+//         (hi.xyz, lo.xyz) as two float4, so that an edge vector is
+//         (hi_b - hi_a) + (lo_b - lo_a) in FP32 — the FP64 difference to FP32
+//         precision without FP64 arithmetic in the element loop;
+//   fgeo  per triangle the material-space part (signed area, shape-function
+//         gradients; 8 words), hgeo per hinge 3 |X1 - X0|^2 / cross2(...) —
+//         X only, in the element's precision.
+template <typename T>
+__global__ void prep_kernel(int n_nodes, int n_tri, int n_hinge, const double *__restrict__ x,
+                            const double *__restrict__ X, const int *__restrict__ tri,
+                            const int *__restrict__ hinge, float4 *__restrict__ xhl,
+                            T *__restrict__ fgeo, T *__restrict__ hgeo) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (xhl && k < n_nodes) {
+    float h[3], l[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const double v = x[3 * size_t(k) + c];
+      h[c] = __double2float_rn(v);
+      l[c] = __double2float_rn(v - double(h[c]));
+    }
+    xhl[2 * size_t(k)] = make_float4(h[0], h[1], h[2], 0.f);
+    xhl[2 * size_t(k) + 1] = make_float4(l[0], l[1], l[2], 0.f);
+  }
+  if (k < n_tri) {
+    const TriGeo<T> g = make_tri_geo<T>(X, tri[3 * k], tri[3 * k + 1], tri[3 * k + 2]);
+    T *o = fgeo + 8 * size_t(k);
+    o[0] = g.A;
+    o[1] = g.g[0][0]; o[2] = g.g[0][1];
+    o[3] = g.g[1][0]; o[4] = g.g[1][1];
+    o[5] = g.g[2][0]; o[6] = g.g[2][1];
+    o[7] = T(0);
+  }
+  if (k < n_hinge) {
+    const int *v = hinge + 4 * k;
+    hgeo[k] = hinge_geo<T>(X, v[0], v[1], v[2], v[3]);
+  }
+}
+
+// x_i - x_j in the element's precision: from the hi / lo split (FP32) or
+// the FP64 positions.
+struct PosHL {
+  const float4 *hl;
+  __device__ __forceinline__ void load(int i, float4 &h, float4 &l) const {
+    h = __ldg(hl + 2 * size_t(i));
+    l = __ldg(hl + 2 * size_t(i) + 1);
+  }
+};
+__device__ __forceinline__ v3<float> hl_diff(const float4 &hi, const float4 &li, const float4 &hj,
+                                             const float4 &lj) {
+  return mk3<float>((hi.x - hj.x) + (li.x - lj.x), (hi.y - hj.y) + (li.y - lj.y),
+                    (hi.z - hj.z) + (li.z - lj.z));
+}
+
+// The row blocks (LA, 0..2) of a triangle / (LA, 0..3) of a hinge into
+// shared memory, block LB at slot base + LB stride (consecutive tasks in
+// consecutive slots: a 9-word stride between the threads of a warp, free of
+// bank conflicts).  LA is a compile-time row (one instance per
+// local vertex), so the vertex selections of the block formulas fold to
+// constants; a block (LA, LB) with LA > LB is the transpose of the evaluated
+// (LB, LA).
+template <typename T, int LA>
+__device__ __forceinline__ void face_row(const Tri<T> &q, T mu, T lam, T dh2, T t8, T *sk,
+                                         T *smass, int base, int stride) {
+#pragma unroll
+  for (int lb = 0; lb < 3; ++lb) {
+    T blk[9];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) blk[j] = T(0);
+    add_membrane_block<T, T>(q, LA < lb ? LA : lb, LA < lb ? lb : LA, mu, lam, dh2, blk);
+    store_block(sk, base + lb * stride, blk, LA > lb);
+    smass[base + lb * stride] = LA == lb ? t8 / T(12) : t8 / T(24);
+  }
+}
+template <typename T, int LA>
+__device__ __forceinline__ void hinge_row(const Hinge<T> &H, T dh2, T *sk, int base, int stride) {
+#pragma unroll
+  for (int lb = 0; lb < 4; ++lb) {
+    T blk[9];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) blk[j] = T(0);
+    add_bending_block<T, T>(H, LA < lb ? LA : lb, LA < lb ? lb : LA, dh2, blk);
+    store_block(sk, base + lb * stride, blk, LA > lb);
+  }
+}
+
 // FP32: two CTAs per SM (128 registers); FP64: one, without spills
 template <typename T, bool WANT_M>
 __global__ void __launch_bounds__(kTileThreads, sizeof(T) == 4 ? 2 : 1)
@@ -280,38 +369,52 @@ tile_blocks_kernel(const int *__restrict__ tile_row, const int *__restrict__ row
                    const int *__restrict__ nf_ptr, const int *__restrict__ nf_list,
                    const int *__restrict__ nh_ptr, const int *__restrict__ nh_list,
                    const int *__restrict__ tri, const int *__restrict__ hinge,
-                   const double *__restrict__ x, const double *__restrict__ X, MaterialD m0,
+                   const double *__restrict__ x, const float4 *__restrict__ xhl,
+                   const T *__restrict__ fgeo, const T *__restrict__ hgeo, MaterialD m0,
                    const MaterialD *__restrict__ mats, const int *__restrict__ node_inst,
                    double *__restrict__ A64, float *__restrict__ A32,
                    double *__restrict__ Mblk) {
   extern __shared__ __align__(16) unsigned char tsm[];
   constexpr int kSlots = tile_slots<T>();
+  constexpr bool kHL = sizeof(T) == 4;  // FP32: positions from the hi / lo split
   T *sk = reinterpret_cast<T *>(tsm);  // kSlots x 9
   T *smass = sk + size_t(kSlots) * 9;  // kSlots
+  const PosHL P{xhl};
   const int r0 = tile_row[blockIdx.x], r1 = tile_row[blockIdx.x + 1];
   const int fa = nf_ptr[r0], nf = nf_ptr[r1] - fa;
   const int ha = nh_ptr[r0], nh = nh_ptr[r1] - ha;
-  // triangle tasks: slots 3k .. 3k + 2
+  // triangle task k: slots k + lb nf; hinge task k: 3 nf + k + lb nh
   for (int k = threadIdx.x; k < nf; k += kTileThreads) {
     const int code = __ldg(nf_list + fa + k);
     const int e = code >> 2, la = code & 3;
     const int a = __ldg(tri + 3 * e), b = __ldg(tri + 3 * e + 1), c = __ldg(tri + 3 * e + 2);
     MaterialD m = m0;
     if (mats) m = mats[node_inst[a]];  // batched: the element's instance
-    const Tri<T> q = make_tri<T>(x, X, a, b, c);
+    TriGeo<T> geo;
+    const T *gp = fgeo + 8 * size_t(e);
+    geo.A = gp[0];
+    geo.g[0][0] = gp[1]; geo.g[0][1] = gp[2];
+    geo.g[1][0] = gp[3]; geo.g[1][1] = gp[4];
+    geo.g[2][0] = gp[5]; geo.g[2][1] = gp[6];
+    v3<T> e0, e1;
+    if constexpr (kHL) {
+      float4 ha4, la4, hb4, lb4, hc4, lc4;
+      P.load(a, ha4, la4); P.load(b, hb4, lb4); P.load(c, hc4, lc4);
+      e0 = hl_diff(hb4, lb4, ha4, la4);
+      e1 = hl_diff(hc4, lc4, ha4, la4);
+    } else {
+      e0 = dpos<T>(x, b, a);
+      e1 = dpos<T>(x, c, a);
+    }
+    const Tri<T> q = make_tri_from<T>(e0, e1, geo);
     const T mu = T(m.mu), lam = T(m.lam), dh2 = T(m.dh2);
     const T t8 = T(m.rho) * T(2) * q.A;
-#pragma unroll 1
-    for (int lb = 0; lb < 3; ++lb) {
-      T blk[9];
-#pragma unroll
-      for (int j = 0; j < 9; ++j) blk[j] = T(0);
-      add_membrane_block<T, T>(q, min(la, lb), max(la, lb), mu, lam, dh2, blk);
-      store_block(sk, 3 * k + lb, blk, la > lb);
-      smass[3 * k + lb] = la == lb ? t8 / T(12) : t8 / T(24);
+    switch (la) {
+      case 0: face_row<T, 0>(q, mu, lam, dh2, t8, sk, smass, k, nf); break;
+      case 1: face_row<T, 1>(q, mu, lam, dh2, t8, sk, smass, k, nf); break;
+      default: face_row<T, 2>(q, mu, lam, dh2, t8, sk, smass, k, nf); break;
     }
   }
-  // hinge tasks: slots 3 nf + 4k .. + 3
   for (int k = threadIdx.x; k < nh; k += kTileThreads) {
     const int code = __ldg(nh_list + ha + k);
     const int e = code >> 2, la = code & 3;
@@ -319,15 +422,26 @@ tile_blocks_kernel(const int *__restrict__ tile_row, const int *__restrict__ row
     const int v0 = __ldg(hv), v1 = __ldg(hv + 1), v2 = __ldg(hv + 2), v3n = __ldg(hv + 3);
     MaterialD m = m0;
     if (mats) m = mats[node_inst[v0]];
-    const Hinge<T> H = make_hinge<T>(x, X, v0, v1, v2, v3n, T(m.beta));
+    v3<T> pp, qv, qq;
+    if constexpr (kHL) {
+      float4 h0, l0, h1, l1, h2, l2, h3, l3;
+      P.load(v0, h0, l0); P.load(v1, h1, l1); P.load(v2, h2, l2); P.load(v3n, h3, l3);
+      pp = hl_diff(h1, l1, h0, l0);
+      qv = hl_diff(h2, l2, h0, l0);
+      qq = hl_diff(h3, l3, h1, l1);
+    } else {
+      pp = dpos<T>(x, v1, v0);
+      qv = dpos<T>(x, v2, v0);
+      qq = dpos<T>(x, v3n, v1);
+    }
+    const Hinge<T> H = make_hinge_from<T>(pp, qv, qq, hgeo[e] * T(m.beta));
     const T dh2 = T(m.dh2);
-#pragma unroll 1
-    for (int lb = 0; lb < 4; ++lb) {
-      T blk[9];
-#pragma unroll
-      for (int j = 0; j < 9; ++j) blk[j] = T(0);
-      add_bending_block<T, T>(H, min(la, lb), max(la, lb), dh2, blk);
-      store_block(sk, 3 * nf + 4 * k + lb, blk, la > lb);
+    const int base = 3 * nf + k;
+    switch (la) {
+      case 0: hinge_row<T, 0>(H, dh2, sk, base, nh); break;
+      case 1: hinge_row<T, 1>(H, dh2, sk, base, nh); break;
+      case 2: hinge_row<T, 2>(H, dh2, sk, base, nh); break;
+      default: hinge_row<T, 3>(H, dh2, sk, base, nh); break;
     }
   }
   __syncthreads();
@@ -357,9 +471,10 @@ tile_blocks_kernel(const int *__restrict__ tile_row, const int *__restrict__ row
 }
 
 // Slot of every contribution: thread per block b (row i); the contribution
-// (element e, local row la, local column lb) lands in the slot of the task
-// (e, la) of row i, i.e. the position of e in i's triangle or hinge list
-// relative to the tile's first row, + lb.
+// (element e, local row la, local column lb) lands in block lb of the task
+// (e, la) of row i, whose index k is the position of e in i's triangle or
+// hinge list relative to the tile's first row: slot k + lb nf for a
+// triangle, 3 nf + k + lb nh for a hinge (nf, nh: the tile's task counts).
 __global__ void tile_slots_kernel(int n_blocks, const int *__restrict__ blk_row,
                                   const int *__restrict__ cptr, const int *__restrict__ contrib,
                                   const int *__restrict__ row_tile, const int *__restrict__ tile_row,
@@ -369,7 +484,7 @@ __global__ void tile_slots_kernel(int n_blocks, const int *__restrict__ blk_row,
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= n_blocks) return;
   const int i = blk_row[b], t = row_tile[i], r0 = tile_row[t], r1 = tile_row[t + 1];
-  const int nft = nf_ptr[r1] - nf_ptr[r0];
+  const int nft = nf_ptr[r1] - nf_ptr[r0], nht = nh_ptr[r1] - nh_ptr[r0];
   for (int q = cptr[b]; q < cptr[b + 1]; ++q) {
     const int code = contrib[q];
     const int e = code >> 7, la = (code >> 3) & 3, lb = code & 3;
@@ -380,7 +495,7 @@ __global__ void tile_slots_kernel(int n_blocks, const int *__restrict__ blk_row,
     int p = p0;
     while (p < p1 && lst[p] != want) ++p;
     if (p == p1) { atomicOr(err, 1); continue; }
-    const int slot = h ? 3 * nft + 4 * (p - nh_ptr[r0]) + lb : 3 * (p - nf_ptr[r0]) + lb;
+    const int slot = h ? 3 * nft + (p - nh_ptr[r0]) + lb * nht : (p - nf_ptr[r0]) + lb * nft;
     aslot[q] = (unsigned short)(slot | (h ? 0 : 0x8000));
   }
 }
@@ -461,23 +576,47 @@ forces_rhs_kernel(int n_nodes, const int *__restrict__ nf_ptr,
 
 }  // namespace
 
+constexpr size_t al256(size_t b) { return (b + 255) / 256 * 256; }
+
+// Scratch of the tiled path (prep_kernel's outputs): xhl (FP32 path), fgeo,
+// hgeo, each 256-byte aligned.
+size_t tiled_prep_bytes(const DevTopology &T, int prec) {
+  const size_t e = prec == EOLC_PREC_FP64 ? sizeof(double) : sizeof(float);
+  const size_t xhl = prec == EOLC_PREC_FP64 ? 0 : al256(size_t(T.n_nodes) * 2 * sizeof(float4));
+  return xhl + al256(size_t(T.n_tri) * 8 * e) + al256(size_t(std::max(1, T.n_hinge)) * e);
+}
+
 template <typename E>
 void launch_tiled(const DevTopology &T, int w, const double *x, const double *X,
-                  const MaterialD &m, const MaterialD *mats, const int *node_inst, double *A64,
-                  float *A32, double *Mblk, cudaStream_t s) {
+                  const MaterialD &m, const MaterialD *mats, const int *node_inst, void *elem,
+                  double *A64, float *A32, double *Mblk, cudaStream_t s) {
+  char *sp = static_cast<char *>(elem);
+  float4 *xhl = nullptr;
+  if (sizeof(E) == 4) {
+    xhl = reinterpret_cast<float4 *>(sp);
+    sp += al256(size_t(T.n_nodes) * 2 * sizeof(float4));
+  }
+  E *fgeo = reinterpret_cast<E *>(sp);
+  sp += al256(size_t(T.n_tri) * 8 * sizeof(E));
+  E *hgeo = reinterpret_cast<E *>(sp);
+  const int np = std::max(T.n_nodes, std::max(T.n_tri, T.n_hinge));
+  prep_kernel<E><<<(np + 255) / 256, 256, 0, s>>>(T.n_nodes, T.n_tri, T.n_hinge, x, X, T.tri.p,
+                                                  T.hinge.p, xhl, fgeo, hgeo);
   const size_t smem = size_t(tile_slots<E>()) * 10 * sizeof(E);
   if (Mblk) {
     cudaFuncSetAttribute(tile_blocks_kernel<E, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          int(smem));
     tile_blocks_kernel<E, true><<<T.atiles[w], kTileThreads, smem, s>>>(
         T.atile_row[w].p, T.rowptr.p, T.cptr.p, T.aslot[w].p, T.nf_ptr.p, T.nf_list.p,
-        T.nh_ptr.p, T.nh_list.p, T.tri.p, T.hinge.p, x, X, m, mats, node_inst, A64, A32, Mblk);
+        T.nh_ptr.p, T.nh_list.p, T.tri.p, T.hinge.p, x, xhl, fgeo, hgeo, m, mats, node_inst,
+        A64, A32, Mblk);
   } else {
     cudaFuncSetAttribute(tile_blocks_kernel<E, false>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     tile_blocks_kernel<E, false><<<T.atiles[w], kTileThreads, smem, s>>>(
         T.atile_row[w].p, T.rowptr.p, T.cptr.p, T.aslot[w].p, T.nf_ptr.p, T.nf_list.p,
-        T.nh_ptr.p, T.nh_list.p, T.tri.p, T.hinge.p, x, X, m, mats, node_inst, A64, A32, nullptr);
+        T.nh_ptr.p, T.nh_list.p, T.tri.p, T.hinge.p, x, xhl, fgeo, hgeo, m, mats, node_inst,
+        A64, A32, nullptr);
   }
 }
 
@@ -542,9 +681,9 @@ int launch_assemble_blocks(const DevTopology &T, const double *x,
   const int nb = T.n_blocks, nt = T.n_tri, nh = T.n_hinge;
   const int w = prec == EOLC_PREC_FP64 ? 1 : 0;
   if (T.n_eol == 0 && T.atiles[w] > 0) {
-    if (w) launch_tiled<double>(T, w, x, X, m, mats, node_inst, A64, A32, Mblk, s);
-    else launch_tiled<float>(T, w, x, X, m, mats, node_inst, A64, A32, Mblk, s);
-    return 1;
+    if (w) launch_tiled<double>(T, w, x, X, m, mats, node_inst, elem, A64, A32, Mblk, s);
+    else launch_tiled<float>(T, w, x, X, m, mats, node_inst, elem, A64, A32, Mblk, s);
+    return 2;
   }
   if (prec == EOLC_PREC_FP64) {
     double *Kt = static_cast<double *>(elem), *t8 = Kt + size_t(nt) * 81, *Kh = t8 + nt;
@@ -660,10 +799,10 @@ bsr_rhs_kernel(int n_nodes, const int *__restrict__ rowptr, const int *__restric
 }
 
 // The force pass's per-triangle words follow the element blocks of the
-// two-pass assembly, 256-byte aligned (the tiled assembly needs none).
+// two-pass assembly, or the tiled path's per-step inputs, 256-byte aligned.
 size_t forces_scratch_offset(const DevTopology &T, int prec) {
   const int w = prec == EOLC_PREC_FP64 ? 1 : 0;
-  if (T.n_eol == 0 && T.atiles[w] > 0) return 0;
+  if (T.n_eol == 0 && T.atiles[w] > 0) return tiled_prep_bytes(T, prec);
   const size_t e = prec == EOLC_PREC_FP64 ? sizeof(double) : sizeof(float);
   return (e * (size_t(T.n_tri) * 82 + size_t(T.n_hinge) * 144) + 255) / 256 * 256;
 }

@@ -82,13 +82,16 @@ struct Tri {
   T S[2][2];    // strain R^T Fm - I
 };
 
-// Builds the triangle quantities for face (a, b, c).  Follows the frame of
-// faceBasedF (Forces.cpp:355-368) and poldec (Forces.cpp:33-52).
+// Material-space part of face (a, b, c): signed area and shape-function
+// gradients (depend on X only, so they can be computed once per topology).
 template <typename T>
-__device__ __forceinline__ Tri<T> make_tri(const double *x, const double *X,
-                                           int a, int b, int c) {
-  Tri<T> q;
-  v3<T> e0 = dpos<T>(x, b, a), e1 = dpos<T>(x, c, a);
+struct TriGeo {
+  T A;
+  T g[3][2];
+};
+template <typename T>
+__device__ __forceinline__ TriGeo<T> make_tri_geo(const double *X, int a, int b, int c) {
+  TriGeo<T> q;
   T d00 = T(X[2 * b] - X[2 * a]), d10 = T(X[2 * b + 1] - X[2 * a + 1]);
   T d01 = T(X[2 * c] - X[2 * a]), d11 = T(X[2 * c + 1] - X[2 * a + 1]);
   T t7 = d00 * d11 - d01 * d10;
@@ -100,6 +103,21 @@ __device__ __forceinline__ Tri<T> make_tri(const double *x, const double *X,
   q.g[2][1] = d00 * it7;
   q.g[0][0] = -q.g[1][0] - q.g[2][0];
   q.g[0][1] = -q.g[1][1] - q.g[2][1];
+  return q;
+}
+
+// The triangle quantities from the edge vectors e0 = x_b - x_a, e1 = x_c -
+// x_a and the material-space part.  Follows the frame of faceBasedF
+// (Forces.cpp:355-368) and poldec (Forces.cpp:33-52).
+template <typename T>
+__device__ __forceinline__ Tri<T> make_tri_from(v3<T> e0, v3<T> e1, const TriGeo<T> &geo) {
+  Tri<T> q;
+  q.A = geo.A;
+#pragma unroll
+  for (int v = 0; v < 3; ++v) {
+    q.g[v][0] = geo.g[v][0];
+    q.g[v][1] = geo.g[v][1];
+  }
   // Fm = e0 gb^T + e1 gc^T (3x2)
   v3<T> F0 = q.g[1][0] * e0 + q.g[2][0] * e1;
   v3<T> F1 = q.g[1][1] * e0 + q.g[2][1] * e1;
@@ -128,6 +146,13 @@ __device__ __forceinline__ Tri<T> make_tri(const double *x, const double *X,
   q.S[1][0] = dot(r1, F0);
   q.S[1][1] = dot(r1, F1) - T(1);
   return q;
+}
+
+// Builds the triangle quantities for face (a, b, c) from the node positions.
+template <typename T>
+__device__ __forceinline__ Tri<T> make_tri(const double *x, const double *X,
+                                           int a, int b, int c) {
+  return make_tri_from<T>(dpos<T>(x, b, a), dpos<T>(x, c, a), make_tri_geo<T>(X, a, b, c));
 }
 
 // Membrane stiffness block K_{la,lb} (3x3, row-major) added into acc with
@@ -178,18 +203,24 @@ struct Hinge {
   v3<T> p, q, qq;  // x1-x0, x2-x0, x3-x1
 };
 
+// Material-space part of a hinge: c = 3 beta |X1 - X0|^2 / cross2(X1 - X0,
+// X2 - X3) as c_geo beta (X only: once per topology).
 template <typename T>
-__device__ __forceinline__ Hinge<T> make_hinge(const double *x,
-                                               const double *X, int i0, int i1,
-                                               int i2, int i3, T beta) {
-  Hinge<T> H;
+__device__ __forceinline__ T hinge_geo(const double *X, int i0, int i1, int i2, int i3) {
   T dXx = T(X[2 * i1] - X[2 * i0]), dXy = T(X[2 * i1 + 1] - X[2 * i0 + 1]);
   T c2 = dXx * T(X[2 * i2 + 1] - X[2 * i3 + 1]) -
          dXy * T(X[2 * i2] - X[2 * i3]);
-  H.c = T(3) * beta * (dXx * dXx + dXy * dXy) / c2;
-  H.p = dpos<T>(x, i1, i0);
-  H.q = dpos<T>(x, i2, i0);
-  H.qq = dpos<T>(x, i3, i1);
+  return T(3) * (dXx * dXx + dXy * dXy) / c2;
+}
+
+// The hinge quantities from p = x1 - x0, q = x2 - x0, qq = x3 - x1 and c.
+template <typename T>
+__device__ __forceinline__ Hinge<T> make_hinge_from(v3<T> p, v3<T> q, v3<T> qq, T c) {
+  Hinge<T> H;
+  H.c = c;
+  H.p = p;
+  H.q = q;
+  H.qq = qq;
   v3<T> n0 = cross(H.p, H.q), n1 = cross(-H.p, H.qq);
   H.ir0 = rsqrt_t(dot(n0, n0));
   H.ir1 = rsqrt_t(dot(n1, n1));
@@ -201,6 +232,17 @@ __device__ __forceinline__ Hinge<T> make_hinge(const double *x,
   H.a = H.ir0 * H.pw;
   H.b = H.ir1 * H.pu;
   return H;
+}
+
+template <typename T>
+__device__ __forceinline__ Hinge<T> make_hinge(const double *x,
+                                               const double *X, int i0, int i1,
+                                               int i2, int i3, T beta) {
+  T dXx = T(X[2 * i1] - X[2 * i0]), dXy = T(X[2 * i1 + 1] - X[2 * i0 + 1]);
+  T c2 = dXx * T(X[2 * i2 + 1] - X[2 * i3 + 1]) -
+         dXy * T(X[2 * i2] - X[2 * i3]);
+  return make_hinge_from<T>(dpos<T>(x, i1, i0), dpos<T>(x, i2, i0), dpos<T>(x, i3, i1),
+                            T(3) * beta * (dXx * dXx + dXy * dXy) / c2);
 }
 
 // Jacobian vectors: dn0/dx_v = [s0_v]x, dn1/dx_v = [s1_v]x.

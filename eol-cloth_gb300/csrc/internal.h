@@ -116,8 +116,9 @@ std::string build_edges_device(EdgeScratch *&w, const int *tri_d, int nf, DevBuf
 // instead of m for batched topologies.
 // elem: device scratch of assemble_scratch_bytes(T, prec) for the element
 // blocks.  Launches the triangle pass, the hinge pass and the block gather.
-// Returns the number of kernels launched: one for the shared-memory tiled
-// assembly (non-EOL topologies whose tiles are built), else three.
+// Returns the number of kernels launched: two (per-step inputs, then the
+// shared-memory tiled assembly) on non-EOL topologies whose tiles are built,
+// else the two-pass path's three (two without hinges).
 int launch_assemble_blocks(const DevTopology &T, const double *x,
                            const double *X, const MaterialD &m,
                            const MaterialD *mats, const int *node_inst,

@@ -790,17 +790,16 @@ __device__ void inverse3_masked(const float (&D)[9], const float (&m)[3], float 
 }
 
 // ---- coarse correction of the patch preconditioner ---------------------------
-// Coarse space: the three translations of each aggregate of patches (compact
-// groups of patches: R sums the free DOFs of an aggregate per axis, P = R^T).  The
-// preconditioner is M = M_patch + R^T A_c^-1 R with A_c = R A R^T (masked).
+// Coarse space: the three translations of each aggregate of patches (one
+// patch each, or compact groups of patches: R sums the free DOFs of an
+// aggregate per axis, P = R^T).  The preconditioner is M = M_patch + R^T X R
+// with X ~ A_c^-1, A_c = R A R^T (masked).
 //
 // coarse_setup (once per solve, every CTA): the CTA's sums of masked blocks
 // per target aggregate (fixed trees, deterministic) go to cpart; after a
-// grid barrier every CTA assembles the dense A_c (3 n_agg square) in the
-// free part of its shared memory in patch order, symmetrises it, inverts it
-// by in-place Gauss-Jordan (SPD: no pivoting) and keeps the three rows of
-// its own aggregate of (X + X^T) / 2 in X_own.  Returns false when the grid
-// barrier timed out.
+// grid barrier, coarse_inverse updates X for this A_c and leaves the three
+// rows of the CTA's aggregate in X_own.  Returns false when a grid barrier
+// timed out.
 // 3x3 inverse of an SPD block (cofactors).
 __device__ __forceinline__ void inverse3_spd(const float a[9], float o[9]) {
   const float c00 = a[4] * a[8] - a[5] * a[7], c01 = a[5] * a[6] - a[3] * a[8],

@@ -108,10 +108,11 @@ typedef struct {
  * block-Jacobi-preconditioned, unit-diagonal-scaled principal submatrix of
  * each patch on [l/30, l], l an upper bound of its spectrum (symmetric
  * positive definite), applied with SM-local barriers.  Coarse level (unless
- * no_coarse): the translations of up to 42 aggregates of patches, with the
- * coarse matrix R A R^T assembled and inverted on the device (see
- * eolc_set_coarse_refresh).  Every solve converges on the same FP64 relative
- * residual.  Meshes too large for the resident image stream the matrix
+ * no_coarse): the translations of one aggregate per patch (or of compact
+ * groups of patches), with the coarse matrix R A R^T assembled on the device
+ * and its inverse updated there by Newton-Schulz iterations from the last
+ * solve's (see eolc_set_coarse_refresh).  Every solve converges on the same
+ * FP64 relative residual.  Meshes too large for the resident image stream the matrix
  * (Jacobi) or are rejected with EOLC_BAD_ARG (EOLC_PC_PATCH). */
 
 typedef struct {
@@ -489,10 +490,11 @@ eolc_status eolc_attach_preconditioner(eolc_ctx *ctx, eolc_lpc *lpc);
  * iterations).  Applies to the shared-memory-resident solve; re-attaching a
  * network (eolc_attach_preconditioner) forces a new evaluation. */
 eolc_status eolc_set_learned_refresh(eolc_ctx *ctx, int solves);
-/* Rebuild the coarse operator of the two-level patch preconditioner (its
- * assembly and inverse) every `solves` EOLC_PC_PATCH solves (default 1) and
- * reuse it in between (a lagged coarse correction: still symmetric positive
- * definite, so PCG stays exact).  A new topology forces a rebuild. */
+/* Update the coarse operator of the two-level patch preconditioner (its
+ * assembly and the Newton-Schulz update of its inverse) every `solves`
+ * EOLC_PC_PATCH solves (default 1) and reuse it in between (a lagged coarse
+ * correction: still symmetric positive definite, so PCG stays exact).  A new
+ * topology starts the inverse again from its block-diagonal guess. */
 eolc_status eolc_set_coarse_refresh(eolc_ctx *ctx, int solves);
 /* Bound of every device-side wait of this context's solves: the grid
  * barriers of the persistent PCG kernels and the neighbour exchange of the

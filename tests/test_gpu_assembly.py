@@ -2,12 +2,12 @@
 with the oracle's Forces::fill (Forces.cpp:331-930: triplets summed in
 insertion order) on an irregular mesh whose rows have uneven valence and span
 many tiles, and, at the full 256 x 256-quad size, the properties that do not
-need the oracle: off-diagonal blocks that are exact transposes of their
-partners (each element block (a, b), a > b, is the transpose of the
-evaluated (b, a), and both sums run over the same elements in the same
-order), diagonal blocks symmetric up to the rounding of the element
-formulas, bit-identical results run to run, and the FP32 matrix within FP32
-rounding of the FP64 one."""
+need the oracle: a matrix symmetric to the rounding of its precision (each
+element block (a, b), a > b, is the transpose of the evaluated (b, a), and
+both sums run over the same elements in the same order; the block formula
+is compiled once per local row, so the two evaluations may round a last bit
+differently), bit-identical results run to run, and the FP32 matrix within
+FP32 rounding of the FP64 one."""
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -63,10 +63,9 @@ def test_full_size_matrix_symmetric_and_reproducible(eolc, precision):
     blk = A.reshape(-1, 3, 3)
     where = {(int(i), int(j)): k for k, (i, j) in enumerate(zip(row, ci))}
     partner = np.array([where[(int(j), int(i))] for i, j in zip(row, ci)])
-    off = row != ci
-    assert np.array_equal(blk[off], blk[partner[off]].transpose(0, 2, 1))
-    dia = blk[~off]
-    assert np.abs(dia - dia.transpose(0, 2, 1)).max() <= 1e-6 * np.abs(dia).max()
+    eps = 1e-6 if precision == "mixed" else 1e-14
+    asym = np.abs(blk - blk[partner].transpose(0, 2, 1)).max()
+    assert asym <= eps * np.abs(blk).max(), asym
     K = eolc.bsr_to_csr(ctx, A)
     if precision == "mixed":
         _, _, D = ctx.forces_fill(x, s["X"], _mat(eolc), scenes.GRAV, scenes.H, eolc.PREC_FP64,

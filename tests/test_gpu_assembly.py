@@ -7,7 +7,8 @@ element block (a, b), a > b, is the transpose of the evaluated (b, a), and
 both sums run over the same elements in the same order; the block formula
 is compiled once per local row, so the two evaluations may round a last bit
 differently), bit-identical results run to run, and the FP32 matrix within
-FP32 rounding of the FP64 one."""
+FP32 rounding of the FP64 one (1e-5 of the largest entry, as the mixed parity
+tests against the oracle)."""
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -71,4 +72,4 @@ def test_full_size_matrix_symmetric_and_reproducible(eolc, precision):
         _, _, D = ctx.forces_fill(x, s["X"], _mat(eolc), scenes.GRAV, scenes.H, eolc.PREC_FP64,
                                   want_M=False)
         Kd = eolc.bsr_to_csr(ctx, D)
-        assert abs(K - Kd).max() <= 1e-6 * abs(Kd).max()
+        assert abs(K - Kd).max() <= 1e-5 * abs(Kd).max()  # the mixed parity tolerance

@@ -76,3 +76,23 @@ def test_c2_contact_set_bit_exact_200_steps(eolc, oracle):
     # vertex / box face, box corner / cloth face and edge / edge contacts
     assert {(3, 1), (1, 3), (2, 2)} <= kinds, kinds
     assert steps_with_contacts > C2_STEPS // 2 and total > 100000, (steps_with_contacts, total)
+
+
+def test_cd2_matches_reference_fixtures(eolc):
+    """eolc_cd2 returns the reference's own contact records (fixtures from
+    src/boxTriCollision.cpp compiled unmodified), bit for bit and in order,
+    on the drape, point-obstacle and configuration-2 snapshots."""
+    import test_oracle_golden as TG
+    g = np.load(TG.CD_GOLD)
+    n = 0
+    for name in TG.CD_SCENES:
+        ctx = eolc.Context(0)
+        tri = g[name + "_tri"]
+        nn = len(g[name + "_x"][0]) // 3
+        ctx.set_topology(nn, tri, eolc.mesh_hinges(tri))
+        for x, tri, boxes, pts, nrm, thr, want in TG.cd_cases(g, name):
+            gb = [eolc.Box(list(b.dim), list(b.E1)) for b in boxes]
+            got = ctx.cd2(x, boxes=gb, points=pts, normals=nrm, threshold=thr, raw=True)
+            assert got == want, "%s: %s" % (name, _first_difference(eolc, got, want))
+            n += len(want) // ctypes.sizeof(eolc.Contact)
+    assert n > 2500

@@ -84,3 +84,69 @@ def test_element_derivatives_consistent(oracle):
         Wm, fm, _ = oracle.bending(x - d, X, 1e-3)
         assert abs(-(Wp - Wm) / (2 * eps) - f[i]) <= 1e-5 * np.abs(f).max()
         assert np.abs(-(fp - fm) / (2 * eps) - K[:, i]).max() <= 1e-5 * np.abs(K).max()
+
+
+# ---- collision detection: the reference's own boxTriCollision.cpp -----------
+CD_GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "cd_ref.npz")
+CD_SCENES = ("drape24", "points16", "drape128")
+
+
+def cd_cases(g, name):
+    """(positions, tri, boxes, points, normals, threshold, contact bytes) of
+    every snapshot of one fixture scene (tests/golden/make_cd_golden.py)."""
+    import oracle as O
+    tri = g[name + "_tri"]
+    boxes = [O.axis_box([0, 0, 0], d) for d in g[name + "_dim"]]
+    for b, E1 in zip(boxes, g[name + "_E1"]):
+        for k in range(16):
+            b.E1[k] = E1[k]
+    pts = g[name + "_pts"] if name + "_pts" in g.files else None
+    nrm = g[name + "_nrm"] if name + "_nrm" in g.files else None
+    size = 264  # sizeof(eolc_contact)
+    counts = g[name + "_n"]
+    offs = np.concatenate([[0], np.cumsum(counts)]) * size
+    raw = g[name + "_contacts"]
+    for k, x in enumerate(g[name + "_x"]):
+        yield x, tri, boxes, pts, nrm, float(g[name + "_thr"]), raw[offs[k]:offs[k + 1]].tobytes()
+
+
+@pytest.mark.parametrize("name", CD_SCENES)
+def test_cd2_matches_reference_fixtures(oracle, name):
+    """The restated CD2 returns the reference's own contact records, bit for
+    bit and in order (fixtures from src/boxTriCollision.cpp compiled
+    unmodified)."""
+    g = np.load(CD_GOLD)
+    n = 0
+    for x, tri, boxes, pts, nrm, thr, want in cd_cases(g, name):
+        got = oracle.cd2(x, tri, boxes=boxes, points=pts, normals=nrm, threshold=thr, raw=True)
+        assert got == want
+        n += len(want) // 264
+    assert n > 0
+
+
+def test_reference_cd_library_matches_oracle(oracle):
+    """Where the reference sources were present at build time, the compiled
+    reference CD2 itself (oracle/_ref/libeolc_ref_cd.so) against the oracle
+    on fresh seeded snapshots."""
+    import ctypes
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                        "oracle", "_ref", "libeolc_ref_cd.so")
+    if not os.path.exists(path):
+        pytest.skip("reference collision library not built (reference sources absent)")
+    import scenes
+    L = ctypes.CDLL(path)
+    x0, X, tri, center, snaps = scenes.drape_positions(20, 16, seed=11)
+    box = oracle.axis_box(center, (0.4, 0.4, 0.2))
+    barr = (oracle.Box * 1)(box)
+    tri32 = np.ascontiguousarray(tri, np.int32)
+    total = 0
+    for x in snaps:
+        cap = 4 * (len(x) // 3) + 64
+        out = (oracle.Contact * cap)()
+        z = np.zeros(3)
+        k = L.ref_cd2(len(x) // 3, oracle.dp(x), oracle.ip(tri32), len(tri32), barr, 1,
+                      oracle.dp(z), oracle.dp(z), 0, ctypes.c_double(1e-3), out, cap)
+        got = ctypes.string_at(out, ctypes.sizeof(oracle.Contact) * k)
+        assert got == oracle.cd2(x, tri, boxes=[box], threshold=1e-3, raw=True)
+        total += k
+    assert total > 0

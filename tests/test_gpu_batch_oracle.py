@@ -77,12 +77,13 @@ def _check(B, picks, x, v, vb, tol):
     return worst
 
 
-def _moving_state(B, seed):
-    """Positions jittered by 0.2 mm (at most 3% of the smallest element, so
-    every MDK stays positive definite) and a random velocity field, so the
-    step's solve is not the pure gravity load of a sheet at rest."""
+def _moving_state(B, seed, jitter=2e-4):
+    """Positions jittered by `jitter` (0.2 mm: at most 3% of the smallest
+    element of the regular sheets, so every MDK stays positive definite) and
+    a random velocity field, so the step's solve is not the pure gravity load
+    of a sheet at rest."""
     rng = np.random.default_rng(seed)
-    x = B["x"] + rng.normal(0, 2e-4, B["x"].size)
+    x = B["x"] + rng.normal(0, jitter, B["x"].size)
     v = rng.normal(0, 0.05, B["x"].size)
     return x, v
 
@@ -109,7 +110,9 @@ def test_config3_batch_matches_oracle(eolc, precision):
 def test_config5_learned_batch_matches_oracle(eolc):
     B = scenes.delaunay_batch(64)  # U(5k, 50k) triangles, seed 5
     assert len(B["sheets"]) == 64
-    x, v = _moving_state(B, 53)
+    # positions at rest: the Delaunay sheets have sliver triangles that a
+    # jitter can invert; the random velocities still load the solve
+    x, v = _moving_state(B, 53, jitter=0.0)
     lpc = eolc.LearnedPC(0)
     lpc.set_params(np.load(WEIGHTS))
     ctx = _batched_step(eolc, B, x, v, lpc)

@@ -349,16 +349,22 @@ __device__ __forceinline__ void face_row(const Tri<T> &q, T mu, T lam, T dh2, T 
     smass[base + lb * stride] = LA == lb ? t8 / T(12) : t8 / T(24);
   }
 }
+// Hinge blocks by the grouped form of the bending Hessian (bend_block: eight
+// outer products per block on per-vertex vectors the compiler computes once
+// per task).
+template <typename T, int LA, int LB>
+__device__ __forceinline__ void hinge_pair(const Hinge<T> &H, T dh2, T *sk, int slot) {
+  constexpr int V = LA < LB ? LA : LB, W = LA < LB ? LB : LA;
+  T blk[9];
+  bend_block<T, V, W>(H, bend_left<T, V>(H), bend_right<T, W>(H), dh2, blk);
+  store_block(sk, slot, blk, LA > LB);
+}
 template <typename T, int LA>
 __device__ __forceinline__ void hinge_row(const Hinge<T> &H, T dh2, T *sk, int base, int stride) {
-#pragma unroll
-  for (int lb = 0; lb < 4; ++lb) {
-    T blk[9];
-#pragma unroll
-    for (int j = 0; j < 9; ++j) blk[j] = T(0);
-    add_bending_block<T, T>(H, LA < lb ? LA : lb, LA < lb ? lb : LA, dh2, blk);
-    store_block(sk, base + lb * stride, blk, LA > lb);
-  }
+  hinge_pair<T, LA, 0>(H, dh2, sk, base);
+  hinge_pair<T, LA, 1>(H, dh2, sk, base + stride);
+  hinge_pair<T, LA, 2>(H, dh2, sk, base + 2 * stride);
+  hinge_pair<T, LA, 3>(H, dh2, sk, base + 3 * stride);
 }
 
 // FP32: two CTAs per SM (128 registers); FP64: one, without spills

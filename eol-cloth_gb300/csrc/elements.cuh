@@ -320,3 +320,103 @@ __device__ __forceinline__ void add_bending_block(const Hinge<T> &H, int v,
 }
 
 }  // namespace eolc
+
+namespace eolc {
+
+// ---------------------------------------------------------------------------
+// The bending blocks of one hinge row, grouped for the row-task assembly.
+// K_vw = k H_vw with k = -s c and H_vw = Hessian of n0^.n1^ (add_bending_block
+// above), written as sums of outer products grouped by their left vector:
+//   H_vw = d I + U0v R1w' + PW0v R2w' + W1v R3w' + PU1v R4w' + U1v R5w'
+//        + W0v R6w' + s0w T0v' + s1w T1v' + [k0 a + k1 b]x
+// with, per vertex x, the Jacobian vectors s0x, s1x, the crosses U0x = u x
+// s0x, PW0x = pw x s0x, W0x = w x s0x, U1x = u x s1x, W1x = w x s1x, PU1x =
+// pu x s1x, and
+//   R1x = i00 (PW0x - phi U0x) + i01 (phi W1x - U1x)   R2x = i00 U0x
+//   R3x = i11 (PU1x - phi W1x) + i01 (phi U0x - W0x)   R4x = i11 W1x
+//   R5x = -i01 U0x    R6x = -i01 W1x
+//   T0x = -i00 phi s0x - i01 s1x    T1x = -i11 phi s1x - i01 s0x
+//   d = i00 phi s0v.s0w + i11 phi s1v.s1w + i01 (s0v.s1w + s1v.s0w).
+// Eight outer products per block on vectors computed once per vertex (the
+// expanded form has sixteen and recomputes the crosses per block); the
+// terms are the same, reassociated.
+template <typename T>
+struct BendLeft {  // what vertex v contributes as the block's row side
+  v3<T> s0, s1, U0, PW0, W1, PU1, U1, W0;
+};
+template <typename T>
+struct BendRight {  // what vertex w contributes as the block's column side
+  v3<T> s0, s1, R1, R2, R3, R4, R5, R6;
+};
+
+template <typename T, int V>
+__device__ __forceinline__ BendLeft<T> bend_left(const Hinge<T> &H) {
+  BendLeft<T> L;
+  L.s0 = hinge_s0(H, V);
+  L.s1 = hinge_s1(H, V);
+  L.U0 = cross(H.u, L.s0);
+  L.PW0 = cross(H.pw, L.s0);
+  L.W0 = cross(H.w, L.s0);
+  L.U1 = cross(H.u, L.s1);
+  L.W1 = cross(H.w, L.s1);
+  L.PU1 = cross(H.pu, L.s1);
+  return L;
+}
+
+template <typename T, int W>
+__device__ __forceinline__ BendRight<T> bend_right(const Hinge<T> &H) {
+  const T i00 = -H.ir0 * H.ir0, i11 = -H.ir1 * H.ir1, i01 = H.ir0 * H.ir1, phi = H.phi;
+  BendRight<T> R;
+  R.s0 = hinge_s0(H, W);
+  R.s1 = hinge_s1(H, W);
+  const v3<T> U0 = cross(H.u, R.s0), PW0 = cross(H.pw, R.s0), W0 = cross(H.w, R.s0);
+  const v3<T> U1 = cross(H.u, R.s1), W1 = cross(H.w, R.s1), PU1 = cross(H.pu, R.s1);
+  R.R1 = i00 * (PW0 - phi * U0) + i01 * (phi * W1 - U1);
+  R.R2 = i00 * U0;
+  R.R3 = i11 * (PU1 - phi * W1) + i01 * (phi * U0 - W0);
+  R.R4 = i11 * W1;
+  R.R5 = -i01 * U0;
+  R.R6 = -i01 * W1;
+  return R;
+}
+
+template <typename T>
+__device__ __forceinline__ void outer_add(T *o, v3<T> l, v3<T> r) {
+  o[0] += l.x * r.x; o[1] += l.x * r.y; o[2] += l.x * r.z;
+  o[3] += l.y * r.x; o[4] += l.y * r.y; o[5] += l.y * r.z;
+  o[6] += l.z * r.x; o[7] += l.z * r.y; o[8] += l.z * r.z;
+}
+
+// K_vw (3x3, row-major) times s into blk (overwritten).
+template <typename T, int V, int W>
+__device__ __forceinline__ void bend_block(const Hinge<T> &H, const BendLeft<T> &L,
+                                           const BendRight<T> &R, T s, T *blk) {
+  const T i00 = -H.ir0 * H.ir0, i11 = -H.ir1 * H.ir1, i01 = H.ir0 * H.ir1, phi = H.phi;
+  const v3<T> T0 = (-i00 * phi) * L.s0 - i01 * L.s1;
+  const v3<T> T1 = (-i11 * phi) * L.s1 - i01 * L.s0;
+  const T d = i00 * phi * dot(L.s0, R.s0) + i11 * phi * dot(L.s1, R.s1) +
+              i01 * (dot(L.s0, R.s1) + dot(L.s1, R.s0));
+  T h[9] = {d, T(0), T(0), T(0), d, T(0), T(0), T(0), d};
+  outer_add(h, L.U0, R.R1);
+  outer_add(h, L.PW0, R.R2);
+  outer_add(h, L.W1, R.R3);
+  outer_add(h, L.PU1, R.R4);
+  outer_add(h, L.U1, R.R5);
+  outer_add(h, L.W0, R.R6);
+  outer_add(h, R.s0, T0);
+  outer_add(h, R.s1, T1);
+  // curvature terms k0 [a]x + k1 [b]x (the vertex pattern of add_bending_block)
+  constexpr int cP0[4] = {-1, 1, 0, 0}, cQ0[4] = {-1, 0, 1, 0};
+  constexpr int cP1[4] = {1, -1, 0, 0}, cQ1[4] = {0, -1, 0, 1};
+  constexpr int k0 = cQ0[V] * cP0[W] - cP0[V] * cQ0[W];
+  constexpr int k1 = cQ1[V] * cP1[W] - cP1[V] * cQ1[W];
+  const v3<T> sk = T(k0) * H.a + T(k1) * H.b;
+  h[1] -= sk.z; h[2] += sk.y;
+  h[3] += sk.z; h[5] -= sk.x;
+  h[6] -= sk.y; h[7] += sk.x;
+  const T k = -s * H.c;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) blk[q] = k * h[q];
+}
+
+}  // namespace eolc

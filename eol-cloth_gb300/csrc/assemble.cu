@@ -372,8 +372,8 @@ template <typename T, bool WANT_M>
 __global__ void __launch_bounds__(kTileThreads, sizeof(T) == 4 ? 2 : 1)
 tile_blocks_kernel(const int *__restrict__ tile_row, const int *__restrict__ rowptr,
                    const int *__restrict__ cptr, const unsigned short *__restrict__ aslot,
-                   const int *__restrict__ nf_ptr, const int *__restrict__ nf_list,
-                   const int *__restrict__ nh_ptr, const int *__restrict__ nh_list,
+                   const int *__restrict__ nf_ptr, const int *__restrict__ task_f,
+                   const int *__restrict__ nh_ptr, const int *__restrict__ task_h,
                    const int *__restrict__ tri, const int *__restrict__ hinge,
                    const double *__restrict__ x, const float4 *__restrict__ xhl,
                    const T *__restrict__ fgeo, const T *__restrict__ hgeo, MaterialD m0,
@@ -391,7 +391,7 @@ tile_blocks_kernel(const int *__restrict__ tile_row, const int *__restrict__ row
   const int ha = nh_ptr[r0], nh = nh_ptr[r1] - ha;
   // triangle task k: slots k + lb nf; hinge task k: 3 nf + k + lb nh
   for (int k = threadIdx.x; k < nf; k += kTileThreads) {
-    const int code = __ldg(nf_list + fa + k);
+    const int code = __ldg(task_f + fa + k);
     const int e = code >> 2, la = code & 3;
     const int a = __ldg(tri + 3 * e), b = __ldg(tri + 3 * e + 1), c = __ldg(tri + 3 * e + 2);
     MaterialD m = m0;
@@ -422,7 +422,7 @@ tile_blocks_kernel(const int *__restrict__ tile_row, const int *__restrict__ row
     }
   }
   for (int k = threadIdx.x; k < nh; k += kTileThreads) {
-    const int code = __ldg(nh_list + ha + k);
+    const int code = __ldg(task_h + ha + k);
     const int e = code >> 2, la = code & 3;
     const int *hv = hinge + 4 * e;
     const int v0 = __ldg(hv), v1 = __ldg(hv + 1), v2 = __ldg(hv + 2), v3n = __ldg(hv + 3);
@@ -478,14 +478,15 @@ tile_blocks_kernel(const int *__restrict__ tile_row, const int *__restrict__ row
 
 // Slot of every contribution: thread per block b (row i); the contribution
 // (element e, local row la, local column lb) lands in block lb of the task
-// (e, la) of row i, whose index k is the position of e in i's triangle or
-// hinge list relative to the tile's first row: slot k + lb nf for a
-// triangle, 3 nf + k + lb nh for a hinge (nf, nh: the tile's task counts).
+// (e, la) of row i: its entry p in i's triangle or hinge list has position
+// k = pos[p] in the tile's task order, slot k + lb nf for a triangle, 3 nf +
+// k + lb nh for a hinge (nf, nh: the tile's task counts).
 __global__ void tile_slots_kernel(int n_blocks, const int *__restrict__ blk_row,
                                   const int *__restrict__ cptr, const int *__restrict__ contrib,
                                   const int *__restrict__ row_tile, const int *__restrict__ tile_row,
                                   const int *__restrict__ nf_ptr, const int *__restrict__ nf_list,
                                   const int *__restrict__ nh_ptr, const int *__restrict__ nh_list,
+                                  const int *__restrict__ pos_f, const int *__restrict__ pos_h,
                                   unsigned short *__restrict__ aslot, int *__restrict__ err) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= n_blocks) return;
@@ -501,7 +502,7 @@ __global__ void tile_slots_kernel(int n_blocks, const int *__restrict__ blk_row,
     int p = p0;
     while (p < p1 && lst[p] != want) ++p;
     if (p == p1) { atomicOr(err, 1); continue; }
-    const int slot = h ? 3 * nft + (p - nh_ptr[r0]) + lb * nht : (p - nf_ptr[r0]) + lb * nft;
+    const int slot = h ? 3 * nft + pos_h[p] + lb * nht : pos_f[p] + lb * nft;
     aslot[q] = (unsigned short)(slot | (h ? 0 : 0x8000));
   }
 }
@@ -613,15 +614,15 @@ void launch_tiled(const DevTopology &T, int w, const double *x, const double *X,
     cudaFuncSetAttribute(tile_blocks_kernel<E, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          int(smem));
     tile_blocks_kernel<E, true><<<T.atiles[w], kTileThreads, smem, s>>>(
-        T.atile_row[w].p, T.rowptr.p, T.cptr.p, T.aslot[w].p, T.nf_ptr.p, T.nf_list.p,
-        T.nh_ptr.p, T.nh_list.p, T.tri.p, T.hinge.p, x, xhl, fgeo, hgeo, m, mats, node_inst,
+        T.atile_row[w].p, T.rowptr.p, T.cptr.p, T.aslot[w].p, T.nf_ptr.p, T.atask_f[w].p,
+        T.nh_ptr.p, T.atask_h[w].p, T.tri.p, T.hinge.p, x, xhl, fgeo, hgeo, m, mats, node_inst,
         A64, A32, Mblk);
   } else {
     cudaFuncSetAttribute(tile_blocks_kernel<E, false>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     tile_blocks_kernel<E, false><<<T.atiles[w], kTileThreads, smem, s>>>(
-        T.atile_row[w].p, T.rowptr.p, T.cptr.p, T.aslot[w].p, T.nf_ptr.p, T.nf_list.p,
-        T.nh_ptr.p, T.nh_list.p, T.tri.p, T.hinge.p, x, xhl, fgeo, hgeo, m, mats, node_inst,
+        T.atile_row[w].p, T.rowptr.p, T.cptr.p, T.aslot[w].p, T.nf_ptr.p, T.atask_f[w].p,
+        T.nh_ptr.p, T.atask_h[w].p, T.tri.p, T.hinge.p, x, xhl, fgeo, hgeo, m, mats, node_inst,
         A64, A32, nullptr);
   }
 }
@@ -658,6 +659,33 @@ std::string ensure_assembly_tiles(DevTopology &T, int prec, cudaStream_t s, long
     tile_row.push_back(end);
     start = end;
   }
+  // every tile's tasks reordered by local vertex (stable), and each list
+  // entry's position in its tile's order
+  const size_t nfl = size_t(nf[N]), nhl = size_t(nh[N]);
+  std::vector<int> fl(std::max<size_t>(nfl, 1)), hl(std::max<size_t>(nhl, 1));
+  AT(cudaMemcpyAsync(fl.data(), T.nf_list.p, sizeof(int) * nfl, cudaMemcpyDeviceToHost, s));
+  if (nhl > 0)
+    AT(cudaMemcpyAsync(hl.data(), T.nh_list.p, sizeof(int) * nhl, cudaMemcpyDeviceToHost, s));
+  AT(cudaStreamSynchronize(s));
+  std::vector<int> tf(fl.size()), th(hl.size()), pf(fl.size()), ph(hl.size());
+  auto reorder = [](const std::vector<int> &lst, int a, int b, int nv, std::vector<int> &task,
+                    std::vector<int> &pos) {
+    int k = 0;
+    for (int v = 0; v < nv; ++v)
+      for (int p = a; p < b; ++p)
+        if ((lst[p] & 3) == v) {
+          task[a + k] = lst[p];
+          pos[p] = k++;
+        }
+  };
+  for (size_t t = 0; t + 1 < tile_row.size(); ++t) {
+    reorder(fl, nf[tile_row[t]], nf[tile_row[t + 1]], 3, tf, pf);
+    reorder(hl, nh[tile_row[t]], nh[tile_row[t + 1]], 4, th, ph);
+  }
+  AT(T.atask_f[w].upload(tf.data(), tf.size(), s));
+  AT(T.atask_h[w].upload(th.data(), th.size(), s));
+  AT(T.apos_f[w].upload(pf.data(), pf.size(), s));
+  AT(T.apos_h[w].upload(ph.data(), ph.size(), s));
   DevBuf<int> drt, derr;
   const size_t ncon = T.contrib.n;
   AT(T.atile_row[w].upload(tile_row.data(), tile_row.size(), s));
@@ -667,7 +695,7 @@ std::string ensure_assembly_tiles(DevTopology &T, int prec, cudaStream_t s, long
   AT(cudaMemsetAsync(derr.p, 0, sizeof(int), s));
   tile_slots_kernel<<<(T.n_blocks + 127) / 128, 128, 0, s>>>(
       T.n_blocks, T.blk_row.p, T.cptr.p, T.contrib.p, drt.p, T.atile_row[w].p, T.nf_ptr.p,
-      T.nf_list.p, T.nh_ptr.p, T.nh_list.p, T.aslot[w].p, derr.p);
+      T.nf_list.p, T.nh_ptr.p, T.nh_list.p, T.apos_f[w].p, T.apos_h[w].p, T.aslot[w].p, derr.p);
   launches += 1;
   int err = 0;
   AT(cudaGetLastError());

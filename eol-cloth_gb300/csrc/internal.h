@@ -83,8 +83,11 @@ struct DevTopology {
   // the tile-local shared-memory slot of every contribution (parallel to
   // contrib; bit 15 set for a triangle's).  atiles: tile count, -1 not built,
   // 0 when some row does not fit a tile (the two-pass assembly runs).
+  // atask_f/h: each tile's triangle / hinge entries of nf_list / nh_list
+  // reordered by local vertex (the warps of a tile then run one specialised
+  // row evaluation each); apos_f/h: an entry's position in that order.
   int atiles[2] = {-1, -1};
-  DevBuf<int> atile_row[2];
+  DevBuf<int> atile_row[2], atask_f[2], atask_h[2], apos_f[2], apos_h[2];
   DevBuf<unsigned short> aslot[2];
 };
 

@@ -24,7 +24,17 @@ namespace eolc {
 namespace cgc {
 namespace {
 
-constexpr double kDelta = 0.1;  // reliable-update trigger: residual drop since the last one
+// Reliable-update trigger: the iterated residual has dropped by this factor
+// since the last true-residual recomputation (convergence is only ever
+// declared on a recomputed residual).  kDelta: one recomputation per decade,
+// the best for the long Jacobi iterations (at 1e-2 the FP32 recurrence
+// drifts enough to cost them ~7% more iterations at 256^2); kDeltaTwoLevel:
+// one per two decades for the two-level preconditioners, whose ~115
+// iterations make the FP64 recomputation (an FP64 product, about 1/64 of the
+// FP32 rate on this GPU) a large share of the solve — still below
+// sqrt(FP32 epsilon) of drift between updates, and the same iteration count.
+constexpr double kDelta = 0.1;
+constexpr double kDeltaTwoLevel = 0.01;
 
 // THREADS threads per CTA, ROWT threads per block row, VALKB KiB of staged
 // values + local columns, WINF window nodes per tile in FP32 (3/4 of it in

@@ -1174,7 +1174,7 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
   __syncthreads();  // ds is reused by the local solves
 
   const V tol2 = A::from_d(P.tol2 * __ldcg(&P.st->rhs_norm2));
-  const V delta2 = A::from_d(kDelta * kDelta);
+  const V delta2 = A::from_d(kDeltaTwoLevel * kDeltaTwoLevel);
   const int N = P.n_nodes;
   const int hj = i < nh ? sm.hnode[i] : -1;
   if (i == 0) s_fail = 0;
@@ -1400,7 +1400,7 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
     }
   };
   const V tol2 = A::from_d(P.tol2 * __ldcg(&P.st->rhs_norm2));
-  const V delta2 = A::from_d(kDelta * kDelta);
+  const V delta2 = A::from_d(kDeltaTwoLevel * kDeltaTwoLevel);
   unsigned epoch = 0;
   int cur = 0;
   __syncthreads();  // the resident image is complete

@@ -254,7 +254,16 @@ constexpr int kTileThreads = 256;
 constexpr int kTileBytes = 112640;  // two CTAs per SM
 // slots (3x3 blocks + a mass word) of one tile
 template <typename T>
-__host__ __device__ constexpr int tile_slots() { return kTileBytes / (10 * int(sizeof(T))); }
+__host__ __device__ constexpr int tile_slots() {
+  // slots of 9 values + a mass word, and 4 bytes per slot for the staged
+  // gather lists (a 16-bit slot per contribution — one per slot — and a
+  // 16-bit contribution offset per block — at most one block per slot)
+  return (kTileBytes - 16) / (10 * int(sizeof(T)) + 4);
+}
+template <typename T>
+__host__ __device__ constexpr size_t tile_smem_bytes() {
+  return size_t(tile_slots<T>()) * (10 * sizeof(T) + 4) + 16;
+}
 
 // Row blocks (la, 0..n-1) of element e into shared memory at base: a block
 // (la, lb) with la <= lb is evaluated, (la, lb) with la > lb is the
@@ -385,8 +394,17 @@ tile_blocks_kernel(const int *__restrict__ tile_row, const int *__restrict__ row
   constexpr bool kHL = sizeof(T) == 4;  // FP32: positions from the hi / lo split
   T *sk = reinterpret_cast<T *>(tsm);  // kSlots x 9
   T *smass = sk + size_t(kSlots) * 9;  // kSlots
+  // the tile's gather lists, staged with one coalesced sweep: the slot of
+  // every contribution and every block's first contribution, tile-relative
+  unsigned short *s_slot = reinterpret_cast<unsigned short *>(smass + kSlots);
+  unsigned short *s_cptr = s_slot + kSlots;  // kSlots + 1 entries
   const PosHL P{xhl};
   const int r0 = tile_row[blockIdx.x], r1 = tile_row[blockIdx.x + 1];
+  const int b0 = rowptr[r0], nb = rowptr[r1] - b0;
+  const int cb = __ldg(cptr + b0), nc = __ldg(cptr + b0 + nb) - cb;
+  for (int q = threadIdx.x; q < nc; q += kTileThreads) s_slot[q] = __ldg(aslot + cb + q);
+  for (int q = threadIdx.x; q <= nb; q += kTileThreads)
+    s_cptr[q] = (unsigned short)(__ldg(cptr + b0 + q) - cb);
   const int fa = nf_ptr[r0], nf = nf_ptr[r1] - fa;
   const int ha = nh_ptr[r0], nh = nh_ptr[r1] - ha;
   // triangle task k: slots k + lb nf; hinge task k: 3 nf + k + lb nh
@@ -453,14 +471,14 @@ tile_blocks_kernel(const int *__restrict__ tile_row, const int *__restrict__ row
   __syncthreads();
   // one thread per (block, entry) of the tile: the contributions in insertion
   // order; consecutive threads write consecutive words
-  const int b0 = rowptr[r0], nv = (rowptr[r1] - b0) * 9;
+  const int nv = nb * 9;
   for (int idx = threadIdx.x; idx < nv; idx += kTileThreads) {
-    const int bl = b0 + idx / 9, j = idx - (idx / 9) * 9;
+    const int bt = idx / 9, j = idx - bt * 9;
     const bool on_diag = j == 0 || j == 4 || j == 8;
     T acc = T(0), macc = T(0);
-    const int c0 = __ldg(cptr + bl), c1 = __ldg(cptr + bl + 1);
+    const int c0 = s_cptr[bt], c1 = s_cptr[bt + 1];
     for (int q = c0; q < c1; ++q) {
-      const unsigned sl = __ldg(aslot + q);
+      const unsigned sl = s_slot[q];
       const unsigned sidx = sl & 0x7fffu;
       acc += sk[size_t(sidx) * 9 + j];
       if ((sl & 0x8000u) && on_diag) {  // a triangle's mass term
@@ -609,7 +627,7 @@ void launch_tiled(const DevTopology &T, int w, const double *x, const double *X,
   const int np = std::max(T.n_nodes, std::max(T.n_tri, T.n_hinge));
   prep_kernel<E><<<(np + 255) / 256, 256, 0, s>>>(T.n_nodes, T.n_tri, T.n_hinge, x, X, T.tri.p,
                                                   T.hinge.p, xhl, fgeo, hgeo);
-  const size_t smem = size_t(tile_slots<E>()) * 10 * sizeof(E);
+  const size_t smem = tile_smem_bytes<E>();
   if (Mblk) {
     cudaFuncSetAttribute(tile_blocks_kernel<E, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          int(smem));

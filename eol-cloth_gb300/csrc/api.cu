@@ -85,6 +85,14 @@ eolc_status set_pins(eolc_ctx *ctx, const int *dofs_h, const double *vel_h,
                      int n_fixed, cudaStream_t s) {
   int n = 3 * ctx->topo.n_nodes;
   if (n_fixed < 0 || (n_fixed > 0 && !dofs_h)) return fail(ctx, EOLC_BAD_ARG, "bad fixed list");
+  // the same list as the last upload on this topology: nothing to do (a new
+  // topology resets n_fixed_dev)
+  if (ctx->n_fixed_dev == n_fixed && int(ctx->pin_dofs_h.size()) == n_fixed &&
+      std::equal(dofs_h, dofs_h + n_fixed, ctx->pin_dofs_h.begin()) &&
+      (!vel_h || (int(ctx->pin_vel_h.size()) == n_fixed &&
+                  std::equal(vel_h, vel_h + n_fixed, ctx->pin_vel_h.begin()))) &&
+      ctx->beq_full.n == size_t(n))
+    return EOLC_OK;
   std::vector<uint8_t> mask(n, 0);
   for (int k = 0; k < n_fixed; ++k) {
     if (dofs_h[k] < 0 || dofs_h[k] >= n) return fail(ctx, EOLC_BAD_ARG, "fixed dof out of range");
@@ -96,6 +104,9 @@ eolc_status set_pins(eolc_ctx *ctx, const int *dofs_h, const double *vel_h,
   EOLC_CHECK_CUDA(ctx, ctx->fixed_dofs.upload(dofs_h, n_fixed, s));
   if (vel_h) EOLC_CHECK_CUDA(ctx, ctx->fixed_vel.upload(vel_h, n_fixed, s));
   ctx->n_fixed_dev = n_fixed;
+  ctx->pin_dofs_h.assign(dofs_h, dofs_h + n_fixed);
+  if (vel_h) ctx->pin_vel_h.assign(vel_h, vel_h + n_fixed);
+  else ctx->pin_vel_h.clear();  // the device copy may be stale: compare next time
   EOLC_CHECK_CUDA(ctx, ctx->beq_full.resize(n));
   return EOLC_OK;
 }

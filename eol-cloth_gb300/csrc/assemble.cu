@@ -629,15 +629,11 @@ void launch_tiled(const DevTopology &T, int w, const double *x, const double *X,
                                                   T.hinge.p, xhl, fgeo, hgeo);
   const size_t smem = tile_smem_bytes<E>();
   if (Mblk) {
-    cudaFuncSetAttribute(tile_blocks_kernel<E, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         int(smem));
     tile_blocks_kernel<E, true><<<T.atiles[w], kTileThreads, smem, s>>>(
         T.atile_row[w].p, T.rowptr.p, T.cptr.p, T.aslot[w].p, T.nf_ptr.p, T.atask_f[w].p,
         T.nh_ptr.p, T.atask_h[w].p, T.tri.p, T.hinge.p, x, xhl, fgeo, hgeo, m, mats, node_inst,
         A64, A32, Mblk);
   } else {
-    cudaFuncSetAttribute(tile_blocks_kernel<E, false>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     tile_blocks_kernel<E, false><<<T.atiles[w], kTileThreads, smem, s>>>(
         T.atile_row[w].p, T.rowptr.p, T.cptr.p, T.aslot[w].p, T.nf_ptr.p, T.atask_f[w].p,
         T.nh_ptr.p, T.atask_h[w].p, T.tri.p, T.hinge.p, x, xhl, fgeo, hgeo, m, mats, node_inst,
@@ -719,8 +715,24 @@ std::string ensure_assembly_tiles(DevTopology &T, int prec, cudaStream_t s, long
   AT(cudaGetLastError());
   AT(cudaMemcpyAsync(&err, derr.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   AT(cudaStreamSynchronize(s));
-#undef AT
   if (err) return "assembly tiles: a contribution without its element task";
+  // the kernels' shared-memory size, once per topology and device
+  if (w) {
+    AT(cudaFuncSetAttribute(tile_blocks_kernel<double, true>,
+                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            int(tile_smem_bytes<double>())));
+    AT(cudaFuncSetAttribute(tile_blocks_kernel<double, false>,
+                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            int(tile_smem_bytes<double>())));
+  } else {
+    AT(cudaFuncSetAttribute(tile_blocks_kernel<float, true>,
+                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            int(tile_smem_bytes<float>())));
+    AT(cudaFuncSetAttribute(tile_blocks_kernel<float, false>,
+                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            int(tile_smem_bytes<float>())));
+  }
+#undef AT
   T.atiles[w] = int(tile_row.size()) - 1;
   return "";
 }

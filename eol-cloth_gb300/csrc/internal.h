@@ -283,6 +283,10 @@ struct eolc_ctx {
   eolc::DevBuf<uint8_t> pinned;
   eolc::DevBuf<int> fixed_dofs;
   eolc::DevBuf<double> fixed_vel;
+  // the fixed list of the last upload (host copies), so that an unchanged
+  // list is not rebuilt and uploaded again on every step
+  std::vector<int> pin_dofs_h;
+  std::vector<double> pin_vel_h;
   int n_fixed_dev = -1;
   eolc::SolveWork *work = nullptr;
   eolc::PatchWork *pwork = nullptr;

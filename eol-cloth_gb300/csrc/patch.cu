@@ -2159,6 +2159,8 @@ struct PatchWork {
   DevBuf<float> cpart, partc, Xc, Xn, Yc;
   DevBuf<double> npart;           // per set-up block: partial of ||rhs||^2
   int coarse_age = -1;            // solves since the coarse operator was built (-1: never)
+  int launch_ok[3] = {0, 0, 0};   // per kernel (Jacobi, patch, learned): attribute set and
+                                  // the grid checked to fit co-resident on this device
   unsigned seq = 0;               // launches (tag generation)
   DevBuf<int16_t> bsl;
   DevBuf<int> gsrc, slice_off, slice_len;
@@ -2279,14 +2281,18 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, i
   const void *fn = patch_pc  ? (const void *)patch_resident_kernel
                    : learned ? (const void *)learned_resident_kernel
                              : (const void *)jacobi_resident_kernel;
-  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kResidentSmem));
-  int dev = 0, n_sm = 0, per_sm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kRThreads, kResidentSmem);
-  if (per_sm < 1 || G > per_sm * n_sm) {
-    err = "resident kernel does not fit on the device";
-    return EOLC_CUDA_ERROR;
+  const int fk = patch_pc ? 1 : learned ? 2 : 0;
+  if (!w->launch_ok[fk]) {  // once per plan (the plan is per device)
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kResidentSmem));
+    int dev = 0, n_sm = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kRThreads, kResidentSmem);
+    if (per_sm < 1 || G > per_sm * n_sm) {
+      err = "resident kernel does not fit on the device";
+      return EOLC_CUDA_ERROR;
+    }
+    w->launch_ok[fk] = 1;
   }
   const int bpc = (mode == ResidentPC::kJacobi && a.precond == EOLC_PC_BLOCK_JACOBI) ? 1 : 0;
   unsigned char *vp = w->vecs.p;

@@ -536,7 +536,14 @@ __global__ void tile_slots_kernel(int n_blocks, const int *__restrict__ blk_row,
 //                        Forces.cpp:498-501; bending adds no force there,
 //                        Forces.cpp:885-908), then b_i = -((M v)_i + h f_i)
 //                        (Cloth.cpp:345).
-constexpr int kForceWords = 10;  // 3 x 3 vertex forces + t8
+// Per-triangle words of the force pass: the membrane force on each vertex
+// (9), t8, and the terms every incident node would otherwise divide out
+// again (FP64 division is a long software sequence on this GPU's FP64 pipe):
+// the gravity force t8 g / 6 (3) and the mass entries t8 / 12, t8 / 24 —
+// the same expressions, evaluated once per triangle instead of once per
+// (node, triangle) pair.
+constexpr int kForceWords = 16;
+constexpr int kFwT8 = 9, kFwGrav = 10, kFwMdiag = 13, kFwMoff = 14;
 
 __global__ void __launch_bounds__(128)
 tri_forces_kernel(int n_tri, const int *__restrict__ tri, const double *__restrict__ x,
@@ -556,7 +563,14 @@ tri_forces_kernel(int n_tri, const int *__restrict__ tri, const double *__restri
     out[3 * la + 1] = fm.y;
     out[3 * la + 2] = fm.z;
   }
-  out[9] = m.rho * 2.0 * q.A;
+  const double t8 = m.rho * 2.0 * q.A;
+  out[kFwT8] = t8;
+  out[kFwGrav] = t8 * m.g[0] / 6.0;
+  out[kFwGrav + 1] = t8 * m.g[1] / 6.0;
+  out[kFwGrav + 2] = t8 * m.g[2] / 6.0;
+  out[kFwMdiag] = t8 / 12.0;
+  out[kFwMoff] = t8 / 24.0;
+  out[15] = 0.0;
 }
 
 __global__ void __launch_bounds__(128)
@@ -574,15 +588,15 @@ forces_rhs_kernel(int n_nodes, const int *__restrict__ nf_ptr,
     const int code = __ldg(nf_list + q);
     const int e = code >> 2, la = code & 3;
     const double *fe = Ft + size_t(e) * kForceWords;
-    const double t8 = __ldg(fe + 9);
-    fx += __ldg(fe + 3 * la) + t8 * m.g[0] / 6.0;
-    fy += __ldg(fe + 3 * la + 1) + t8 * m.g[1] / 6.0;
-    fz += __ldg(fe + 3 * la + 2) + t8 * m.g[2] / 6.0;
+    fx += __ldg(fe + 3 * la) + __ldg(fe + kFwGrav);
+    fy += __ldg(fe + 3 * la + 1) + __ldg(fe + kFwGrav + 1);
+    fz += __ldg(fe + 3 * la + 2) + __ldg(fe + kFwGrav + 2);
     if (b) {
+      const double mdiag = __ldg(fe + kFwMdiag), moff = __ldg(fe + kFwMoff);
 #pragma unroll
       for (int w = 0; w < 3; ++w) {
         const int vw = __ldg(tri + 3 * e + w);
-        const double mm = w == la ? t8 / 12.0 : t8 / 24.0;
+        const double mm = w == la ? mdiag : moff;
         mvx += mm * v[3 * vw];
         mvy += mm * v[3 * vw + 1];
         mvz += mm * v[3 * vw + 2];
@@ -822,7 +836,7 @@ eol_forces_kernel(int n_nodes, int n_real, const int *__restrict__ eol,
     double F[3][2];
     face_grad(x, X, tri[3 * t], tri[3 * t + 1], tri[3 * t + 2], F);
     const double *fe = Ft + size_t(t) * kForceWords;
-    const double t8 = fe[9];
+    const double t8 = fe[kFwT8];
     for (int j = 0; j < 2; ++j) {
       double sm = 0, si = 0;
       for (int p = 0; p < 3; ++p) {

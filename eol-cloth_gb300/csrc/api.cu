@@ -426,7 +426,7 @@ eolc_status step_batched_learned(eolc_ctx *ctx, int n_steps, const double grav[3
     const float *Gm = nullptr;
     std::string msg = learned_forward(ctx->lpc, ctx, ctx->pinned.p, &Gm, s);
     if (!msg.empty()) return fail(ctx, EOLC_CUDA_ERROR, msg.c_str());
-    ctx->launches += 8;  // network forward kernels
+    ctx->launches += kLearnedForwardLaunches;
     PcgArgs a = batch_pcg_args(ctx, opts, ctx->v.p);
     if ((st = batch_enqueue_learned(ctx->bwork, a, Gm, opts->fallback_factor, ctx->node_inst.p, s,
                                     ctx->err, ctx->launches)) != EOLC_OK)
@@ -486,7 +486,7 @@ eolc_status solve_with_args(eolc_ctx *ctx, const eolc_solve_opts *o, const PcgAr
     if (!reuse) {
       std::string msg = learned_forward(ctx->lpc, ctx, ctx->pinned.p, &Gm, s);
       if (!msg.empty()) return fail(ctx, EOLC_CUDA_ERROR, msg.c_str());
-      ctx->launches += 8;  // network forward kernels
+      ctx->launches += kLearnedForwardLaunches;
       ctx->lpc_cached = resident ? ctx->lpc : nullptr;
       ctx->lpc_uses = 0;
     }

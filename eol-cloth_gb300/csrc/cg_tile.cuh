@@ -547,12 +547,19 @@ __device__ void setup_node(int i, const int *rowptr, const int *colidx,
                            int block_pc, V4<double> *rhs, V4<double> *x64,
                            V4<T> *r, V4<T> *p, V4<T> *s, V4<T> *xacc, T *pc,
                            V4<T> *fmask) {
+  // a = (A beq)_i.  beq is zero off the pinned DOFs, and a column block
+  // whose three beq entries are zero adds exact zeros (finite blocks), so it
+  // is skipped without reading the block: same sums, same order.
   double a[3] = {0, 0, 0};
   for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
-    int j = colidx[k];
+    const int j = colidx[k];
+    const double q[3] = {beq_full[3 * j], beq_full[3 * j + 1], beq_full[3 * j + 2]};
+    if (((__double_as_longlong(q[0]) | __double_as_longlong(q[1]) | __double_as_longlong(q[2]))
+         << 1) == 0)
+      continue;
     const T *blk = A + size_t(k) * 9;
     for (int rr = 0; rr < 3; ++rr)
-      for (int c = 0; c < 3; ++c) a[rr] += double(blk[3 * rr + c]) * beq_full[3 * j + c];
+      for (int c = 0; c < 3; ++c) a[rr] += double(blk[3 * rr + c]) * q[c];
   }
   T m[3];
   double e[3];

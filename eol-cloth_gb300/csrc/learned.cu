@@ -34,6 +34,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "tc.cuh"
 
 namespace eolc {
 namespace lpc {
@@ -163,6 +164,7 @@ __global__ void reduce_parts_kernel(int nparts, int n, const float *__restrict__
 struct Graph {
   int n = 0, m = 0, nb = 0;
   DevBuf<int> ei, ej, bij, bji, inc_ptr, inc, diag, rowptr, colidx;
+  DevBuf<int> inc_o;     // per incidence entry: the edge's other node
   DevBuf<int> blk_edge;  // per block: edge id (off-diagonal) or -1
   DevBuf<float> deg_inv;
 };
@@ -192,12 +194,18 @@ std::string build_graph(const HostTopology &H, Graph &G, cudaStream_t s) {
     inc[pos[ei[e]]++] = 2 * e;
     inc[pos[ej[e]]++] = 2 * e + 1;
   }
+  std::vector<int> inc_o(inc.size());
+  for (size_t q = 0; q < inc.size(); ++q) {
+    const int e = inc[q] >> 1;
+    inc_o[q] = (inc[q] & 1) ? ei[e] : ej[e];
+  }
   std::vector<float> dinv(n);
   for (int i = 0; i < n; ++i) dinv[i] = ptr[i + 1] > ptr[i] ? 1.f / float(ptr[i + 1] - ptr[i]) : 0.f;
   G.n = n; G.m = m; G.nb = nb;
   cudaError_t es[] = {G.ei.upload(ei.data(), m, s), G.ej.upload(ej.data(), m, s),
                       G.bij.upload(bij.data(), m, s), G.bji.upload(bji.data(), m, s),
                       G.inc_ptr.upload(ptr.data(), n + 1, s), G.inc.upload(inc.data(), inc.size(), s),
+                      G.inc_o.upload(inc_o.data(), inc_o.size(), s),
                       G.diag.upload(H.diag.data(), n, s), G.rowptr.upload(H.rowptr.data(), n + 1, s),
                       G.colidx.upload(H.colidx.data(), nb, s),
                       G.blk_edge.upload(blk_edge.data(), nb, s),
@@ -332,100 +340,221 @@ __global__ void edge_concat_bwd_kernel(int n, const int *inc_ptr, const int *inc
   dh[size_t(i) * kH + c] += acc;
 }
 
-// ---- inference forward, fused ------------------------------------------------
-// One message-passing layer per launch, without the per-edge gate matrix:
-// a CTA takes kLayerNodes nodes; each warp aggregates its nodes (lane c
-// handles channels c and c + 32) with the gate g_e = sigmoid(x_e Wg + bg)
-// evaluated on the fly, then the CTA applies the 128 -> 64 layer to
-// [h, agg] from shared memory.  Every sum runs in the order of the training
-// kernels (dense_fwd_kernel, aggregate_fwd_kernel), so the activations are
-// the same numbers.
-constexpr int kLayerNodes = 32;
-constexpr int kLayerThreads = 256;
+// ---- inference forward on the tensor cores --------------------------------------
+// One message-passing layer per launch.  A CTA takes kTcM = 128 nodes (the
+// MMA's M): each warp aggregates its nodes (lane c handles channels c and
+// c + 32) with the gate g_e = sigmoid(x_e Wg + bg) evaluated on the fly, and
+// writes [h, agg] as three BF16 terms into K-major shared-memory tiles; one
+// thread then issues the 128 x 64 x 128 product with W (BF16) as
+// 8 K-steps x 3 terms of tcgen05.mma into a TMEM accumulator, and the eight
+// warps read it back (warp w: rows 32 (w % 4) .., columns 32 (w / 4) ..),
+// add the bias and apply relu.  The last layer keeps h3 on chip: its rows go
+// back into shared memory as the A operand of a second product with
+// [Wo_i | Wo_j | Wt] (64 x 39, padded to 48), which gives every node's share
+// of the edge head (h3_i Wo_i, h3_j Wo_j) and theta = h3 Wt + bt.
+// The training forward (dense_fwd_kernel, aggregate_fwd_kernel) computes the
+// same network on the CUDA cores; the two agree to FP32 rounding.
+constexpr int kTcM = 128;
+constexpr int kTcThreads = 256;
+constexpr int kLayerK = 2 * kH;                      // [h, agg]
+constexpr int kLayerPart = kTcM * kLayerK * 2;       // one BF16 term tile (32 KB)
+constexpr int kLayerB = kH * kLayerK * 2;            // W^T (16 KB)
+constexpr int kHeadN = 48;                           // [Wo_i | Wo_j | Wt] padded
+constexpr int kHeadCols = 2 * kOE + kON;             // 39 used head columns
+constexpr int kLayerSmem = tc::kSplit * kLayerPart + kLayerB + 16;  // two CTAs per SM
+constexpr long long kTcWaitLimit = 1ll << 20;
+// MMA completions that did not arrive within kTcWaitLimit polls (their rows
+// are written as NaN, which the solve reports as non-finite)
+__device__ unsigned int g_tc_timeouts = 0;
 
-__global__ void __launch_bounds__(kLayerThreads)
-layer_fused_kernel(int n, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
-                   const int *__restrict__ ei, const int *__restrict__ ej,
-                   const float *__restrict__ deg_inv, const float *__restrict__ fE,
-                   const float *__restrict__ Wg, const float *__restrict__ Wl,
-                   const float *__restrict__ h_in, float *__restrict__ h_out) {
-  __shared__ float sWl[2 * kH * kH + kH];  // W then b, BF16-rounded W
-  __shared__ float sWg[kFE * kH + kH];
-  __shared__ float sCat[kLayerNodes][2 * kH];
-  for (int k = threadIdx.x; k < 2 * kH * kH; k += kLayerThreads) sWl[k] = bf16r(Wl[k]);
-  for (int k = threadIdx.x; k < kH; k += kLayerThreads) sWl[2 * kH * kH + k] = Wl[2 * kH * kH + k];
-  for (int k = threadIdx.x; k < kFE * kH; k += kLayerThreads) sWg[k] = bf16r(Wg[k]);
-  for (int k = threadIdx.x; k < kH; k += kLayerThreads) sWg[kFE * kH + k] = Wg[kFE * kH + k];
-  __syncthreads();
-  const int node0 = blockIdx.x * kLayerNodes;
+template <bool LAST>
+__global__ void __launch_bounds__(kTcThreads, 2)
+layer_tc_kernel(int n, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
+                const int *__restrict__ inc_o, const float *__restrict__ deg_inv, const float *__restrict__ fE,
+                const float *__restrict__ Wg, const float *__restrict__ Wl,
+                const float *__restrict__ Wo, const float *__restrict__ Wt,
+                const float *__restrict__ h_in, float *__restrict__ h_out,
+                float *__restrict__ head, float *__restrict__ theta) {
+  extern __shared__ __align__(1024) uint8_t tc_smem[];
+  uint8_t *sA = tc_smem;                             // kSplit tiles, 128 x 128
+  uint8_t *sB = tc_smem + tc::kSplit * kLayerPart;        // W^T, 64 x 128
+  uint64_t *bar = reinterpret_cast<uint64_t *>(sB + kLayerB);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
+  constexpr uint32_t kCols = LAST ? 128 : 64;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int ln = warp; ln < kLayerNodes; ln += kLayerThreads / 32) {
-    const int i = node0 + ln;
-    float a0 = 0.f, a1 = 0.f;
+  const int node0 = blockIdx.x * kTcM;
+  if (warp == 0) tc::tmem_alloc(tslot, kCols);
+  if (threadIdx.x == 32) tc::mbar_init(bar, 1);
+  for (int q = threadIdx.x; q < kLayerK * kH; q += kTcThreads) {
+    const int k = q / kH, c = q % kH;
+    *reinterpret_cast<__nv_bfloat16 *>(sB + tc::tile_off(c, k, kLayerK)) =
+        __float2bfloat16_rn(Wl[q]);
+  }
+  // Aggregation: a half-warp per node, four channels per lane.  The node's
+  // incidence entries (edge, other node) are read by the lanes at once and
+  // broadcast, so the per-edge loads of the gate features and the
+  // neighbour's h row are independent of each other.
+  const int half = lane >> 4, hl = lane & 15, c4 = 4 * hl;
+  float wg[kFE][4], bg[4];
+#pragma unroll
+  for (int k = 0; k < kFE; ++k)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) wg[k][c] = bf16r(Wg[k * kH + c4 + c]);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) bg[c] = Wg[kFE * kH + c4 + c];
+  for (int pr = warp; pr < kTcM / 2; pr += kTcThreads / 32) {
+    const int ln = 2 * pr + half, i = node0 + ln;
+    float4 hv = make_float4(0.f, 0.f, 0.f, 0.f);
+    float a[4] = {0.f, 0.f, 0.f, 0.f};
+    int q0 = 0, deg = 0;
     if (i < n) {
-      for (int q = inc_ptr[i]; q < inc_ptr[i + 1]; ++q) {
-        const int e = inc[q] >> 1, side = inc[q] & 1;
-        const int o = side ? ei[e] : ej[e];
-        const float *x = fE + size_t(e) * kFE;
-        float g0 = sWg[kFE * kH + lane], g1 = sWg[kFE * kH + lane + 32];
-        for (int k = 0; k < kFE; ++k) {
-          const float xk = __ldg(x + k);
-          g0 += xk * sWg[k * kH + lane];
-          g1 += xk * sWg[k * kH + lane + 32];
-        }
-        a0 += sigm(g0) * __ldg(h_in + size_t(o) * kH + lane);
-        a1 += sigm(g1) * __ldg(h_in + size_t(o) * kH + lane + 32);
+      q0 = inc_ptr[i];
+      deg = inc_ptr[i + 1] - q0;
+      hv = __ldg(reinterpret_cast<const float4 *>(h_in + size_t(i) * kH + c4));
+    }
+    const int maxdeg = max(deg, __shfl_xor_sync(0xffffffffu, deg, 16));
+    for (int base = 0; base < maxdeg; base += 16) {
+      int me = 0, mo = 0;
+      if (base + hl < deg) {
+        me = inc[q0 + base + hl] >> 1;
+        mo = inc_o[q0 + base + hl];
       }
-      sCat[ln][lane] = __ldg(h_in + size_t(i) * kH + lane);
-      sCat[ln][lane + 32] = __ldg(h_in + size_t(i) * kH + lane + 32);
-      sCat[ln][kH + lane] = a0 * deg_inv[i];
-      sCat[ln][kH + lane + 32] = a1 * deg_inv[i];
+      const int cnt = min(16, maxdeg - base);
+#pragma unroll 2
+      for (int t = 0; t < cnt; ++t) {
+        const int e = __shfl_sync(0xffffffffu, me, t, 16);
+        const int o = __shfl_sync(0xffffffffu, mo, t, 16);
+        if (base + t < deg) {
+          const float *x = fE + size_t(e) * kFE;
+          float g[4] = {bg[0], bg[1], bg[2], bg[3]};
+#pragma unroll
+          for (int k = 0; k < kFE; ++k) {
+            const float xk = __ldg(x + k);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) g[c] += xk * wg[k][c];
+          }
+          const float4 ho = __ldg(reinterpret_cast<const float4 *>(h_in + size_t(o) * kH + c4));
+          a[0] += sigm(g[0]) * ho.x;
+          a[1] += sigm(g[1]) * ho.y;
+          a[2] += sigm(g[2]) * ho.z;
+          a[3] += sigm(g[3]) * ho.w;
+        }
+      }
+    }
+    if (i < n) {
+      const float d = deg_inv[i];
+      for (int c = 0; c < 4; ++c) a[c] *= d;
+    }
+    tc::put3x4(sA, kLayerPart, ln, c4, kLayerK, hv.x, hv.y, hv.z, hv.w);
+    tc::put3x4(sA, kLayerPart, ln, kH + c4, kLayerK, a[0], a[1], a[2], a[3]);
+  }
+  tc::fence_smem_to_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const uint32_t a_base = tc::smem_u32(sA), b_base = tc::smem_u32(sB);
+  if (threadIdx.x == 0) {
+    constexpr uint32_t idesc = tc::idesc_bf16(kTcM, kH);
+    for (int s = 0; s < kLayerK / 16; ++s)
+      for (int p = 0; p < tc::kSplit; ++p)
+        tc::mma_bf16(tmem, tc::smem_desc(a_base + p * kLayerPart + 256 * s, 128, kLayerK * 16),
+                     tc::smem_desc(b_base + 256 * s, 128, kLayerK * 16), idesc,
+                     uint32_t(s | p));
+    tc::mma_commit(bar);
+  }
+  const bool ok0 = __all_sync(0xffffffffu, tc::mbar_wait(bar, 0, kTcWaitLimit));
+  bool ok = ok0;
+  tc::fence_after_sync();
+  const int row = 32 * (warp & 3) + lane, c0 = 32 * (warp >> 2);
+  const int i = node0 + row;
+  const uint32_t lane_addr = uint32_t(32 * (warp & 3)) << 16;
+  float v[32];
+  if (ok) tc::tmem_ld32(tmem + lane_addr + c0, v);
+  const float *bias = Wl + 2 * kH * kH;
+#pragma unroll
+  for (int k = 0; k < 32; ++k)
+    v[k] = ok ? fmaxf(v[k] + __ldg(bias + c0 + k), 0.f) : __int_as_float(0x7fc00000);
+  if (!LAST) {
+    if (i < n) {
+      float4 *dst = reinterpret_cast<float4 *>(h_out + size_t(i) * kH + c0);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) dst[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+    }
+  } else {
+    // the layer product has completed: h3 rows (zero past n) go into the
+    // first kSplit x 16 KB of the A tiles as the 128 x 64 A operand of the
+    // head product, the head weights^T (48 x 64) after them
+    constexpr int kPart2 = kTcM * kH * 2;
+    uint8_t *sH = sA + tc::kSplit * kPart2;
+#pragma unroll
+    for (int k = 0; k < 32; ++k) tc::put3(sA, kPart2, row, c0 + k, kH, i < n ? v[k] : 0.f);
+    for (int q = threadIdx.x; q < kHeadN * kH; q += kTcThreads) {
+      const int k = q / kHeadN, c = q % kHeadN;
+      float w = 0.f;
+      if (c < kOE) w = Wo[k * kOE + c];                         // h3_i rows of Wo
+      else if (c < 2 * kOE) w = Wo[(kH + k) * kOE + c - kOE];   // h3_j rows of Wo
+      else if (c < kHeadCols) w = Wt[k * kON + c - 2 * kOE];
+      *reinterpret_cast<__nv_bfloat16 *>(sH + tc::tile_off(c, k, kH)) = __float2bfloat16_rn(w);
+    }
+    tc::fence_smem_to_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (threadIdx.x == 0 && ok0) {
+      constexpr uint32_t idesc = tc::idesc_bf16(kTcM, kHeadN);
+      const uint32_t h_base = tc::smem_u32(sH);
+      for (int s = 0; s < kH / 16; ++s)
+        for (int p = 0; p < tc::kSplit; ++p)
+          tc::mma_bf16(tmem + kH, tc::smem_desc(a_base + p * kPart2 + 256 * s, 128, kH * 16),
+                       tc::smem_desc(h_base + 256 * s, 128, kH * 16), idesc, uint32_t(s | p));
+      tc::mma_commit(bar);
+    }
+    ok = ok && __all_sync(0xffffffffu, tc::mbar_wait(bar, 1, kTcWaitLimit));
+    tc::fence_after_sync();
+    if (ok) tc::tmem_ld32(tmem + lane_addr + kH + c0, v);
+    if (i < n) {
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        const int c = c0 + k;
+        const float x = ok ? v[k] : __int_as_float(0x7fc00000);
+        if (c < 2 * kOE) head[size_t(i) * 2 * kOE + c] = x;
+        else if (c < kHeadCols) theta[size_t(i) * kON + c - 2 * kOE] = x + __ldg(Wt + kH * kON + c - 2 * kOE);
+      }
     }
   }
-  __syncthreads();
-  const int c = threadIdx.x % kH, g = threadIdx.x / kH;  // 4 node groups
-  for (int ln = g; ln < kLayerNodes; ln += kLayerThreads / kH) {
-    const int i = node0 + ln;
-    if (i >= n) break;
-    float acc = sWl[2 * kH * kH + c];
-    for (int k = 0; k < 2 * kH; ++k) acc += sCat[ln][k] * sWl[k * kH + c];
-    h_out[size_t(i) * kH + c] = fmaxf(acc, 0.f);
+  if (!ok) {
+    if (lane == 0) atomicAdd(&g_tc_timeouts, 1u);
+    tc::mbar_wait(bar, ok0 ? 1 : 0, kTcWaitLimit);  // let an MMA in flight land
   }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, kCols);
 }
 
-// Edge head o_e = [h3_i, h3_j, x_e] Wo + bo (18 outputs), one thread per edge,
-// summed in the order of the training kernel.
+// Edge head o_e = h3_i Wo_i + h3_j Wo_j + (bo + x_e Wo_x) (18 outputs), from
+// the per-node shares of layer_tc_kernel<true>; one thread per edge.
 __global__ void __launch_bounds__(128)
-edge_out_kernel(int m, const int *__restrict__ ei, const int *__restrict__ ej,
-                const float *__restrict__ h, const float *__restrict__ fE,
-                const float *__restrict__ Wo, float *__restrict__ o) {
-  __shared__ float sW[kEdgeIn * kOE + kOE];
-  for (int k = threadIdx.x; k < kEdgeIn * kOE; k += blockDim.x) sW[k] = bf16r(Wo[k]);
-  for (int k = threadIdx.x; k < kOE; k += blockDim.x) sW[kEdgeIn * kOE + k] = Wo[kEdgeIn * kOE + k];
+edge_head_kernel(int m, const int *__restrict__ ei, const int *__restrict__ ej,
+                 const float *__restrict__ head, const float *__restrict__ fE,
+                 const float *__restrict__ Wo, float *__restrict__ o) {
+  __shared__ float sW[kFE * kOE + kOE];
+  for (int k = threadIdx.x; k < kFE * kOE; k += blockDim.x) sW[k] = bf16r(Wo[2 * kH * kOE + k]);
+  for (int k = threadIdx.x; k < kOE; k += blockDim.x) sW[kFE * kOE + k] = Wo[kEdgeIn * kOE + k];
   __syncthreads();
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= m) return;
   float acc[kOE];
 #pragma unroll
-  for (int c = 0; c < kOE; ++c) acc[c] = sW[kEdgeIn * kOE + c];
-  const float *hi = h + size_t(ei[e]) * kH, *hj = h + size_t(ej[e]) * kH;
-  for (int k = 0; k < kH; ++k) {
-    const float x = __ldg(hi + k);
-#pragma unroll
-    for (int c = 0; c < kOE; ++c) acc[c] += x * sW[k * kOE + c];
-  }
-  for (int k = 0; k < kH; ++k) {
-    const float x = __ldg(hj + k);
-#pragma unroll
-    for (int c = 0; c < kOE; ++c) acc[c] += x * sW[(kH + k) * kOE + c];
-  }
+  for (int c = 0; c < kOE; ++c) acc[c] = sW[kFE * kOE + c];
   for (int k = 0; k < kFE; ++k) {
     const float x = __ldg(fE + size_t(e) * kFE + k);
 #pragma unroll
-    for (int c = 0; c < kOE; ++c) acc[c] += x * sW[(2 * kH + k) * kOE + c];
+    for (int c = 0; c < kOE; ++c) acc[c] += x * sW[k * kOE + c];
   }
+  const float *hi = head + size_t(ei[e]) * 2 * kOE, *hj = head + size_t(ej[e]) * 2 * kOE + kOE;
 #pragma unroll
-  for (int c = 0; c < kOE; ++c) o[size_t(e) * kOE + c] = acc[c];
+  for (int c = 0; c < kOE; ++c) o[size_t(e) * kOE + c] = (__ldg(hi + c) + __ldg(hj + c)) + acc[c];
 }
 
 // ---- G assembly -----------------------------------------------------------------
@@ -629,6 +758,7 @@ struct LearnedPC {
   bool topo_train = false;  // training buffers allocated for this topology
   lpc::Graph G;
   DevBuf<float> fN, dvec, fE, h[4], cat[3], gate, eX, o, theta;
+  DevBuf<float> head;  // inference: per-node shares of the edge head (2 x 18)
   DevBuf<float> dh, dcat, dgate, deX, dO, dtheta, dGv, tmpX;
   DevBuf<float> Gv;
   // training set: one topology, many systems
@@ -767,26 +897,40 @@ std::string backward(LearnedPC &P, const Graph &G, const uint8_t *pinned, cudaSt
 namespace eolc {
 namespace lpc {
 
-// Inference forward (8 launches): features, h0, three fused layers, theta,
-// the edge head, G assembly.  Fills P.Gv; the same numbers as forward().
+// Inference forward (kForwardLaunches = 7 launches): features, h0, layers 1
+// and 2, layer 3 with the node-side heads, the edge head, G assembly.  Fills
+// P.Gv; the network of forward() to FP32 rounding.
 std::string forward_fused(LearnedPC &P, const Graph &G, const int *blk_row, const float *A,
                           const uint8_t *pinned, cudaStream_t s) {
   const Layout &L = P.L;
   const float *W = P.params.p;
   const int n = G.n, m = G.m;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  static bool attr_set[2][64] = {};
+  if (dev < 64 && !attr_set[0][dev]) {
+    cudaFuncSetAttribute(layer_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kLayerSmem);
+    cudaFuncSetAttribute(layer_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kLayerSmem);
+    attr_set[0][dev] = true;
+  }
   features_kernel<<<nblk(std::max(n, m), 256), 256, 0, s>>>(n, m, G.rowptr.p, G.diag.p, A, pinned,
                                                           G.ei.p, G.ej.p, G.bij.p, P.fN.p,
                                                           P.dvec.p, P.fE.p);
   dense_fwd_kernel<<<nblk(n, 64), 256, size_t(kFN * kH + kH) * sizeof(float), s>>>(
       n, kFN, kH, P.fN.p, W + L.Wn, W + L.Wn + kFN * kH, kRelu, P.h[0].p);
-  for (int l = 0; l < kLayers; ++l)
-    layer_fused_kernel<<<nblk(n, kLayerNodes), kLayerThreads, 0, s>>>(
-        n, G.inc_ptr.p, G.inc.p, G.ei.p, G.ej.p, G.deg_inv.p, P.fE.p, W + L.Wg, W + L.Wl[l],
-        P.h[l].p, P.h[l + 1].p);
-  dense_fwd_kernel<<<nblk(n, 64), 256, size_t(kH * kON + kON) * sizeof(float), s>>>(
-      n, kH, kON, P.h[3].p, W + L.Wt, W + L.Wt + kH * kON, kNone, P.theta.p);
-  edge_out_kernel<<<nblk(m, 128), 128, 0, s>>>(m, G.ei.p, G.ej.p, P.h[3].p, P.fE.p, W + L.Wo,
-                                               P.o.p);
+  const int grid = nblk(n, kTcM);
+  for (int l = 0; l + 1 < kLayers; ++l)
+    layer_tc_kernel<false><<<grid, kTcThreads, kLayerSmem, s>>>(
+        n, G.inc_ptr.p, G.inc.p, G.inc_o.p, G.deg_inv.p, P.fE.p, W + L.Wg, W + L.Wl[l],
+        W + L.Wo, W + L.Wt, P.h[l].p, P.h[l + 1].p, nullptr, nullptr);
+  layer_tc_kernel<true><<<grid, kTcThreads, kLayerSmem, s>>>(
+      n, G.inc_ptr.p, G.inc.p, G.inc_o.p, G.deg_inv.p, P.fE.p, W + L.Wg,
+      W + L.Wl[kLayers - 1], W + L.Wo, W + L.Wt, P.h[kLayers - 1].p, nullptr, P.head.p,
+      P.theta.p);
+  edge_head_kernel<<<nblk(m, 128), 128, 0, s>>>(m, G.ei.p, G.ej.p, P.head.p, P.fE.p, W + L.Wo,
+                                                P.o.p);
   g_assemble_kernel<<<nblk(G.nb, 128), 128, 0, s>>>(G.nb, blk_row, G.colidx.p, G.blk_edge.p,
                                                    G.inc_ptr.p, G.inc.p, G.ei.p, G.ej.p, P.o.p,
                                                    P.theta.p, P.dvec.p, pinned, P.Gv.p);
@@ -804,6 +948,7 @@ std::string ensure_buffers(LearnedPC &P, int n, int m, int nb, bool train) {
         P.fN.resize(N * kFN), P.dvec.resize(N * 3), P.fE.resize(M * kFE),
         P.h[0].resize(N * kH), P.h[1].resize(N * kH), P.h[2].resize(N * kH),
         P.h[3].resize(N * kH), P.o.resize(M * kOE), P.theta.resize(N * kON),
+        P.head.resize(N * 2 * kOE),
         P.Gv.resize(size_t(nb) * 9 + 16)};
     for (cudaError_t e : es)
       if (e != cudaSuccess) return cudaGetErrorString(e);

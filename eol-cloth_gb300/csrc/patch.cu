@@ -1601,14 +1601,14 @@ __global__ void slice_blocks_kernel(int n_lanes, const int *__restrict__ gsrc,
   for (int c = 0; c < 9; ++c) d[32 * c] = k >= 0 ? __ldg(G + size_t(k) * 9 + c) : 0.f;
 }
 
+// Ap[k] = A[src[k]], one float per thread: consecutive threads read and
+// write consecutive words (the permuted rows keep their blocks together).
 __global__ void permute_blocks_kernel(int nb, const int *__restrict__ src,
                                       const float *__restrict__ A, float *__restrict__ Ap) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nb) return;
-  const float *s = A + size_t(src[k]) * 9;
-  float *d = Ap + size_t(k) * 9;
-#pragma unroll
-  for (int c = 0; c < 9; ++c) d[c] = __ldg(s + c);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 9ll * nb) return;
+  const int k = int(t / 9), c = int(t - 9ll * k);
+  Ap[t] = __ldg(A + size_t(__ldg(src + k)) * 9 + c);
 }
 
 __global__ void permute_vectors_kernel(int n, const int *__restrict__ perm,
@@ -2309,7 +2309,7 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, i
   V4<float> *xacc = vr + 10 * N;  // set-up output, unused (increments live in registers)
   P.q = vr + 11 * N;
   float *pc = reinterpret_cast<float *>(w->pc.p);
-  const int nbk = (NB + 255) / 256, nn = (N + 127) / 128;
+  const int nbk = int((9ll * NB + 255) / 256), nn = (N + 127) / 128;
   permute_blocks_kernel<<<nbk, 256, 0, s>>>(NB, w->src.p, a.A32, w->Ap.p);
   if (learned && !Gm && !w->Gs.p) {
     err = "no learned preconditioner blocks";

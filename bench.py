@@ -666,7 +666,56 @@ def run_contacts(args, local_rank, stream, flush, steps=5):
                                                   "same problem"}}
     out["workload"] = ("256x256-quad sheet draped over a 0.4 x 0.4 box (snapshot 14 of the "
                        "seeded drape), 2 corners pinned, patch-PCG, rel-res 1e-8, host buffers")
+    out["trajectory"] = optional_line(lambda: contact_trajectory(args, local_rank, stream))
     return out
+
+
+def contact_trajectory(args, local_rank, stream, quads=128, steps=80):
+    """Consecutive Cloth::steps with contacts: the configuration-2 sheet
+    (128x128 quads, positions jittered N(0, 1e-4) from seed 2) dropped flat,
+    unpinned, onto the 0.4 x 0.4 x 0.2 box whose top face starts 0.05 m
+    below it; every step runs CD2 and the contact QP (eolc_step_contacts,
+    multipliers carried from step to step)."""
+    import numpy as np
+    import torch
+    import eolc
+    r = quads + 1
+    x0, X, tri = eolc.sheet_mesh(r, r)
+    n = len(x0) // 3
+    hinge = eolc.mesh_hinges(tri)
+    x = x0 + np.random.default_rng(2).normal(0.0, 1e-4, x0.size)
+    v = np.zeros(3 * n)
+    E1 = np.eye(4)
+    E1[:3, 3] = [0.5, 0.5, -0.05 - 0.1]
+    box = eolc.Box((0.4, 0.4, 0.2), E1.T.ravel())
+    ctx = eolc.Context(local_rank)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_topology(n, tri, hinge)
+    mat = eolc.Material(**MAT)
+    opts = arm_opts(eolc, "patch", args.degree)
+    none = np.zeros(0, np.int32)
+    ms, rows, solves, status = [], [], [], "ok"
+    for k in range(steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        try:
+            info = ctx.step_contacts(x, X, v, mat, GRAV, H, none, np.zeros(0), boxes=[box],
+                                     threshold=1e-3, opts=opts)
+        except Exception as e:  # an indefinite MDK ends the trajectory
+            status = "stopped at step %d: %s" % (k, str(e)[:120])
+            break
+        ms.append(1e3 * (time.perf_counter() - t0))
+        rows.append(int(info.n_active))
+        solves.append(int(info.solves))
+    touch = [k for k, m in enumerate(rows) if m > 0]
+    return {"workload": "128x128-quad sheet (16,641 nodes) dropped flat, unpinned, onto the "
+                        "0.4 x 0.4 x 0.2 box 0.05 m below; patch-PCG, rel-res 1e-8, host buffers",
+            "steps_done": len(ms), "status": status,
+            "first_contact_step": touch[0] if touch else None,
+            "ms_per_step_free": float(np.median(ms[:touch[0]])) if touch and touch[0] > 0 else None,
+            "ms_per_step_contact": float(np.median([ms[k] for k in touch])) if touch else None,
+            "max_active_rows": max(rows) if rows else 0,
+            "mean_qp_solves_in_contact": float(np.mean([solves[k] for k in touch])) if touch else None}
 
 
 def run_cd2(args, local_rank, stream, steps=200, cpu_sample=40):

@@ -340,11 +340,57 @@ __global__ void edge_concat_bwd_kernel(int n, const int *inc_ptr, const int *inc
   dh[size_t(i) * kH + c] += acc;
 }
 
+// ---- inference forward: edge gates and the input layer ----------------------------
+// One thread per (edge, four channels): gate_e = sigmoid(x_e Wg + bg), shared
+// by the three message-passing layers; then one thread per (node, four
+// channels): h0_i = relu(f_i Wn + bn).  Both summed in the order of
+// dense_fwd_kernel; the BF16-rounded weights sit in shared memory.
+__global__ void __launch_bounds__(256)
+gate_h0_kernel(int m, int n, const float *__restrict__ fE, const float *__restrict__ Wg,
+               const float *__restrict__ fN, const float *__restrict__ Wn,
+               float *__restrict__ gate, float *__restrict__ h0) {
+  __shared__ float4 sg[kFE + 1][kH / 4], sn[kFN + 1][kH / 4];
+  for (int q = threadIdx.x; q < (kFE + 1) * kH; q += blockDim.x) {
+    const float w = q < kFE * kH ? bf16r(Wg[q]) : Wg[q];
+    reinterpret_cast<float *>(sg)[q] = w;
+  }
+  for (int q = threadIdx.x; q < (kFN + 1) * kH; q += blockDim.x) {
+    const float w = q < kFN * kH ? bf16r(Wn[q]) : Wn[q];
+    reinterpret_cast<float *>(sn)[q] = w;
+  }
+  __syncthreads();
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int groups = kH / 4;
+  if (t < m * groups) {
+    const int e = t / groups, c = t % groups;
+    float4 g = sg[kFE][c];
+#pragma unroll
+    for (int k = 0; k < kFE; ++k) {
+      const float x = __ldg(fE + size_t(e) * kFE + k);
+      const float4 w = sg[k][c];
+      g.x += x * w.x; g.y += x * w.y; g.z += x * w.z; g.w += x * w.w;
+    }
+    reinterpret_cast<float4 *>(gate)[t] = make_float4(sigm(g.x), sigm(g.y), sigm(g.z), sigm(g.w));
+  } else if (t < (m + n) * groups) {
+    const int u = t - m * groups;
+    const int i = u / groups, c = u % groups;
+    float4 a = sn[kFN][c];
+#pragma unroll
+    for (int k = 0; k < kFN; ++k) {
+      const float x = __ldg(fN + size_t(i) * kFN + k);
+      const float4 w = sn[k][c];
+      a.x += x * w.x; a.y += x * w.y; a.z += x * w.z; a.w += x * w.w;
+    }
+    reinterpret_cast<float4 *>(h0)[u] =
+        make_float4(fmaxf(a.x, 0.f), fmaxf(a.y, 0.f), fmaxf(a.z, 0.f), fmaxf(a.w, 0.f));
+  }
+}
+
 // ---- inference forward on the tensor cores --------------------------------------
 // One message-passing layer per launch.  A CTA takes kTcM = 128 nodes (the
-// MMA's M): each warp aggregates its nodes (lane c handles channels c and
-// c + 32) with the gate g_e = sigmoid(x_e Wg + bg) evaluated on the fly, and
-// writes [h, agg] as three BF16 terms into K-major shared-memory tiles; one
+// MMA's M): half-warps aggregate its nodes with the precomputed edge gates
+// (four channels per lane) and write [h, agg] as three BF16 terms into
+// K-major shared-memory tiles; one
 // thread then issues the 128 x 64 x 128 product with W (BF16) as
 // 8 K-steps x 3 terms of tcgen05.mma into a TMEM accumulator, and the eight
 // warps read it back (warp w: rows 32 (w % 4) .., columns 32 (w / 4) ..),
@@ -370,8 +416,8 @@ __device__ unsigned int g_tc_timeouts = 0;
 template <bool LAST>
 __global__ void __launch_bounds__(kTcThreads, 2)
 layer_tc_kernel(int n, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
-                const int *__restrict__ inc_o, const float *__restrict__ deg_inv, const float *__restrict__ fE,
-                const float *__restrict__ Wg, const float *__restrict__ Wl,
+                const int *__restrict__ inc_o, const float *__restrict__ deg_inv,
+                const float *__restrict__ gate, const float *__restrict__ Wl,
                 const float *__restrict__ Wo, const float *__restrict__ Wt,
                 const float *__restrict__ h_in, float *__restrict__ h_out,
                 float *__restrict__ head, float *__restrict__ theta) {
@@ -392,16 +438,9 @@ layer_tc_kernel(int n, const int *__restrict__ inc_ptr, const int *__restrict__ 
   }
   // Aggregation: a half-warp per node, four channels per lane.  The node's
   // incidence entries (edge, other node) are read by the lanes at once and
-  // broadcast, so the per-edge loads of the gate features and the
-  // neighbour's h row are independent of each other.
+  // broadcast, so the per-edge loads of the gate and of the neighbour's h
+  // row are independent of each other.
   const int half = lane >> 4, hl = lane & 15, c4 = 4 * hl;
-  float wg[kFE][4], bg[4];
-#pragma unroll
-  for (int k = 0; k < kFE; ++k)
-#pragma unroll
-    for (int c = 0; c < 4; ++c) wg[k][c] = bf16r(Wg[k * kH + c4 + c]);
-#pragma unroll
-  for (int c = 0; c < 4; ++c) bg[c] = Wg[kFE * kH + c4 + c];
   for (int pr = warp; pr < kTcM / 2; pr += kTcThreads / 32) {
     const int ln = 2 * pr + half, i = node0 + ln;
     float4 hv = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -420,24 +459,17 @@ layer_tc_kernel(int n, const int *__restrict__ inc_ptr, const int *__restrict__ 
         mo = inc_o[q0 + base + hl];
       }
       const int cnt = min(16, maxdeg - base);
-#pragma unroll 2
+#pragma unroll 4
       for (int t = 0; t < cnt; ++t) {
         const int e = __shfl_sync(0xffffffffu, me, t, 16);
         const int o = __shfl_sync(0xffffffffu, mo, t, 16);
         if (base + t < deg) {
-          const float *x = fE + size_t(e) * kFE;
-          float g[4] = {bg[0], bg[1], bg[2], bg[3]};
-#pragma unroll
-          for (int k = 0; k < kFE; ++k) {
-            const float xk = __ldg(x + k);
-#pragma unroll
-            for (int c = 0; c < 4; ++c) g[c] += xk * wg[k][c];
-          }
+          const float4 g = __ldg(reinterpret_cast<const float4 *>(gate + size_t(e) * kH + c4));
           const float4 ho = __ldg(reinterpret_cast<const float4 *>(h_in + size_t(o) * kH + c4));
-          a[0] += sigm(g[0]) * ho.x;
-          a[1] += sigm(g[1]) * ho.y;
-          a[2] += sigm(g[2]) * ho.z;
-          a[3] += sigm(g[3]) * ho.w;
+          a[0] += g.x * ho.x;
+          a[1] += g.y * ho.y;
+          a[2] += g.z * ho.z;
+          a[3] += g.w * ho.w;
         }
       }
     }
@@ -532,31 +564,6 @@ layer_tc_kernel(int n, const int *__restrict__ inc_ptr, const int *__restrict__ 
   if (warp == 0) tc::tmem_dealloc(tmem, kCols);
 }
 
-// Edge head o_e = h3_i Wo_i + h3_j Wo_j + (bo + x_e Wo_x) (18 outputs), from
-// the per-node shares of layer_tc_kernel<true>; one thread per edge.
-__global__ void __launch_bounds__(128)
-edge_head_kernel(int m, const int *__restrict__ ei, const int *__restrict__ ej,
-                 const float *__restrict__ head, const float *__restrict__ fE,
-                 const float *__restrict__ Wo, float *__restrict__ o) {
-  __shared__ float sW[kFE * kOE + kOE];
-  for (int k = threadIdx.x; k < kFE * kOE; k += blockDim.x) sW[k] = bf16r(Wo[2 * kH * kOE + k]);
-  for (int k = threadIdx.x; k < kOE; k += blockDim.x) sW[kFE * kOE + k] = Wo[kEdgeIn * kOE + k];
-  __syncthreads();
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= m) return;
-  float acc[kOE];
-#pragma unroll
-  for (int c = 0; c < kOE; ++c) acc[c] = sW[kFE * kOE + c];
-  for (int k = 0; k < kFE; ++k) {
-    const float x = __ldg(fE + size_t(e) * kFE + k);
-#pragma unroll
-    for (int c = 0; c < kOE; ++c) acc[c] += x * sW[k * kOE + c];
-  }
-  const float *hi = head + size_t(ei[e]) * 2 * kOE, *hj = head + size_t(ej[e]) * 2 * kOE + kOE;
-#pragma unroll
-  for (int c = 0; c < kOE; ++c) o[size_t(e) * kOE + c] = (__ldg(hi + c) + __ldg(hj + c)) + acc[c];
-}
-
 // ---- G assembly -----------------------------------------------------------------
 // 3x3 helpers, row-major
 __device__ __forceinline__ void mmT(const float *P, const float *Q, float *R) {  // R = P Q^T
@@ -608,6 +615,89 @@ __global__ void g_assemble_kernel(int nb, const int *blk_row, const int *colidx,
       bool free_ac = !pinned[3 * i + a] && !pinned[3 * j + c];
       Gv[size_t(b) * 9 + 3 * a + c] = free_ac ? acc[3 * a + c] : 0.f;
     }
+}
+
+// Inference G assembly in two passes over the graph instead of one thread
+// per block.  edge_blocks_kernel, one thread per edge e = (i, j): the edge
+// head o_e = h3_i Wo_i + h3_j Wo_j + (bo + x_e Wo_x) from the per-node
+// shares of layer_tc_kernel<true>, U_e and V_e (kept for the diagonal pass)
+// and the two off-diagonal blocks G_ij = U V^T, G_ji = V U^T.
+// node_blocks_kernel, one thread per node: G_ii = Lambda_i + the U U^T or
+// V V^T terms of its incident edges, in incidence order.  The blocks are the
+// ones g_assemble_kernel forms from the same o and theta.
+__global__ void __launch_bounds__(128)
+edge_blocks_kernel(int m, const int *__restrict__ ei, const int *__restrict__ ej,
+                   const int *__restrict__ bij, const int *__restrict__ bji,
+                   const float *__restrict__ head, const float *__restrict__ fE,
+                   const float *__restrict__ Wo, const float *__restrict__ dvec,
+                   const uint8_t *__restrict__ pinned, float *__restrict__ uv,
+                   float *__restrict__ Gv) {
+  __shared__ float sW[kFE * kOE + kOE];
+  for (int k = threadIdx.x; k < kFE * kOE; k += blockDim.x) sW[k] = bf16r(Wo[2 * kH * kOE + k]);
+  for (int k = threadIdx.x; k < kOE; k += blockDim.x) sW[kFE * kOE + k] = Wo[kEdgeIn * kOE + k];
+  __syncthreads();
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m) return;
+  const int i = ei[e], j = ej[e];
+  float acc[kOE];
+#pragma unroll
+  for (int c = 0; c < kOE; ++c) acc[c] = sW[kFE * kOE + c];
+  for (int k = 0; k < kFE; ++k) {
+    const float x = __ldg(fE + size_t(e) * kFE + k);
+#pragma unroll
+    for (int c = 0; c < kOE; ++c) acc[c] += x * sW[k * kOE + c];
+  }
+  const float *hi = head + size_t(i) * 2 * kOE, *hj = head + size_t(j) * 2 * kOE + kOE;
+  float U[9], V[9];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float si = rsqrtf(dvec[3 * i + a]), sj = rsqrtf(dvec[3 * j + a]);
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      U[3 * a + b] = si * ((__ldg(hi + 3 * a + b) + __ldg(hj + 3 * a + b)) + acc[3 * a + b]);
+      V[3 * a + b] = sj * ((__ldg(hi + 9 + 3 * a + b) + __ldg(hj + 9 + 3 * a + b)) +
+                           acc[9 + 3 * a + b]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    uv[size_t(e) * 18 + k] = U[k];
+    uv[size_t(e) * 18 + 9 + k] = V[k];
+  }
+  float R[9];
+  mmT(U, V, R);
+  for (int a = 0; a < 3; ++a)
+    for (int c = 0; c < 3; ++c)
+      Gv[size_t(bij[e]) * 9 + 3 * a + c] =
+          (!pinned[3 * i + a] && !pinned[3 * j + c]) ? R[3 * a + c] : 0.f;
+  mmT(V, U, R);
+  for (int a = 0; a < 3; ++a)
+    for (int c = 0; c < 3; ++c)
+      Gv[size_t(bji[e]) * 9 + 3 * a + c] =
+          (!pinned[3 * j + a] && !pinned[3 * i + c]) ? R[3 * a + c] : 0.f;
+}
+
+__global__ void __launch_bounds__(128)
+node_blocks_kernel(int n, const int *__restrict__ diag, const int *__restrict__ inc_ptr,
+                   const int *__restrict__ inc, const float *__restrict__ uv,
+                   const float *__restrict__ theta, const float *__restrict__ dvec,
+                   const uint8_t *__restrict__ pinned, float *__restrict__ Gv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float acc[9];
+  for (int k = 0; k < 9; ++k) acc[k] = 0.f;
+  for (int a = 0; a < 3; ++a) acc[4 * a] = softplus(theta[3 * i + a]) / dvec[3 * i + a];
+  for (int q = inc_ptr[i]; q < inc_ptr[i + 1]; ++q) {
+    const int e = inc[q] >> 1, side = inc[q] & 1;
+    float P[9], R[9];
+    for (int k = 0; k < 9; ++k) P[k] = __ldg(uv + size_t(e) * 18 + 9 * side + k);
+    mmT(P, P, R);
+    for (int k = 0; k < 9; ++k) acc[k] += R[k];
+  }
+  for (int a = 0; a < 3; ++a)
+    for (int c = 0; c < 3; ++c)
+      Gv[size_t(diag[i]) * 9 + 3 * a + c] =
+          (!pinned[3 * i + a] && !pinned[3 * i + c]) ? acc[3 * a + c] : 0.f;
 }
 
 // dG (masked) -> d o_e (18) per edge and d theta per node.
@@ -759,6 +849,7 @@ struct LearnedPC {
   lpc::Graph G;
   DevBuf<float> fN, dvec, fE, h[4], cat[3], gate, eX, o, theta;
   DevBuf<float> head;  // inference: per-node shares of the edge head (2 x 18)
+  DevBuf<float> uv;    // inference: U_e, V_e per edge (2 x 9)
   DevBuf<float> dh, dcat, dgate, deX, dO, dtheta, dGv, tmpX;
   DevBuf<float> Gv;
   // training set: one topology, many systems
@@ -897,8 +988,9 @@ std::string backward(LearnedPC &P, const Graph &G, const uint8_t *pinned, cudaSt
 namespace eolc {
 namespace lpc {
 
-// Inference forward (kForwardLaunches = 7 launches): features, h0, layers 1
-// and 2, layer 3 with the node-side heads, the edge head, G assembly.  Fills
+// Inference forward (kLearnedForwardLaunches = 7 launches): features, edge
+// gates with h0, layers 1 and 2, layer 3 with the node-side heads, the edge
+// head with the off-diagonal blocks of G, the diagonal blocks.  Fills
 // P.Gv; the network of forward() to FP32 rounding.
 std::string forward_fused(LearnedPC &P, const Graph &G, const int *blk_row, const float *A,
                           const uint8_t *pinned, cudaStream_t s) {
@@ -918,22 +1010,24 @@ std::string forward_fused(LearnedPC &P, const Graph &G, const int *blk_row, cons
   features_kernel<<<nblk(std::max(n, m), 256), 256, 0, s>>>(n, m, G.rowptr.p, G.diag.p, A, pinned,
                                                           G.ei.p, G.ej.p, G.bij.p, P.fN.p,
                                                           P.dvec.p, P.fE.p);
-  dense_fwd_kernel<<<nblk(n, 64), 256, size_t(kFN * kH + kH) * sizeof(float), s>>>(
-      n, kFN, kH, P.fN.p, W + L.Wn, W + L.Wn + kFN * kH, kRelu, P.h[0].p);
+  const int gh = (m + n) * (kH / 4);
+  gate_h0_kernel<<<(gh + 255) / 256, 256, 0, s>>>(m, n, P.fE.p, W + L.Wg, P.fN.p, W + L.Wn,
+                                                  P.gate.p, P.h[0].p);
   const int grid = nblk(n, kTcM);
   for (int l = 0; l + 1 < kLayers; ++l)
     layer_tc_kernel<false><<<grid, kTcThreads, kLayerSmem, s>>>(
-        n, G.inc_ptr.p, G.inc.p, G.inc_o.p, G.deg_inv.p, P.fE.p, W + L.Wg, W + L.Wl[l],
+        n, G.inc_ptr.p, G.inc.p, G.inc_o.p, G.deg_inv.p, P.gate.p, W + L.Wl[l],
         W + L.Wo, W + L.Wt, P.h[l].p, P.h[l + 1].p, nullptr, nullptr);
   layer_tc_kernel<true><<<grid, kTcThreads, kLayerSmem, s>>>(
-      n, G.inc_ptr.p, G.inc.p, G.inc_o.p, G.deg_inv.p, P.fE.p, W + L.Wg,
+      n, G.inc_ptr.p, G.inc.p, G.inc_o.p, G.deg_inv.p, P.gate.p,
       W + L.Wl[kLayers - 1], W + L.Wo, W + L.Wt, P.h[kLayers - 1].p, nullptr, P.head.p,
       P.theta.p);
-  edge_head_kernel<<<nblk(m, 128), 128, 0, s>>>(m, G.ei.p, G.ej.p, P.head.p, P.fE.p, W + L.Wo,
-                                                P.o.p);
-  g_assemble_kernel<<<nblk(G.nb, 128), 128, 0, s>>>(G.nb, blk_row, G.colidx.p, G.blk_edge.p,
-                                                   G.inc_ptr.p, G.inc.p, G.ei.p, G.ej.p, P.o.p,
-                                                   P.theta.p, P.dvec.p, pinned, P.Gv.p);
+  (void)blk_row;
+  edge_blocks_kernel<<<nblk(m, 128), 128, 0, s>>>(m, G.ei.p, G.ej.p, G.bij.p, G.bji.p, P.head.p,
+                                                  P.fE.p, W + L.Wo, P.dvec.p, pinned, P.uv.p,
+                                                  P.Gv.p);
+  node_blocks_kernel<<<nblk(n, 128), 128, 0, s>>>(n, G.diag.p, G.inc_ptr.p, G.inc.p, P.uv.p,
+                                                  P.theta.p, P.dvec.p, pinned, P.Gv.p);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? "" : cudaGetErrorString(e);
 }
@@ -948,7 +1042,7 @@ std::string ensure_buffers(LearnedPC &P, int n, int m, int nb, bool train) {
         P.fN.resize(N * kFN), P.dvec.resize(N * 3), P.fE.resize(M * kFE),
         P.h[0].resize(N * kH), P.h[1].resize(N * kH), P.h[2].resize(N * kH),
         P.h[3].resize(N * kH), P.o.resize(M * kOE), P.theta.resize(N * kON),
-        P.head.resize(N * 2 * kOE),
+        P.head.resize(N * 2 * kOE), P.gate.resize(M * kH), P.uv.resize(M * 18),
         P.Gv.resize(size_t(nb) * 9 + 16)};
     for (cudaError_t e : es)
       if (e != cudaSuccess) return cudaGetErrorString(e);
@@ -956,7 +1050,7 @@ std::string ensure_buffers(LearnedPC &P, int n, int m, int nb, bool train) {
   if (!train) return "";
   cudaError_t es[] = {
       P.cat[0].resize(N * 2 * kH), P.cat[1].resize(N * 2 * kH), P.cat[2].resize(N * 2 * kH),
-      P.gate.resize(M * kH), P.eX.resize(M * kEdgeIn),
+      P.eX.resize(M * kEdgeIn),
       P.dh.resize(N * kH), P.dcat.resize(N * 2 * kH),
       P.dgate.resize(M * kH), P.deX.resize(M * kEdgeIn), P.dO.resize(M * kOE),
       P.dtheta.resize(N * kON), P.dGv.resize(size_t(nb) * 9), P.tmpX.resize(N * kH),

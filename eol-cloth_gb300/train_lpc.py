@@ -13,14 +13,15 @@ conjugate-gradient iteration count depends on); probes="smooth": the step's
 velocity and two seeded smooth random fields.
 
 meshes="mixed" (generate_mixed): the systems come from one batched context
-holding a 48x48 grid and six irregular Delaunay sheets, so the network also
-sees remeshed-like stencils.
+holding a 48x48 grid, a 256x256 grid (the benchmark sheet; --big) and six
+irregular Delaunay sheets, so the network sees the benchmark's stencil and
+remeshed-like ones.
 
 Training: eolc_lpc_train (Adam on the GPU, the library's own forward and
-backward kernels).  The committed weights come from:
+backward kernels).  The committed weights come from the defaults, i.e.:
 
-    python eol-cloth_gb300/train_lpc.py --systems 1000 --epochs 20 --lr 3e-3 --probes white \
-        --meshes mixed --seed 1 --out eol-cloth_gb300/weights/lpc.npy
+    python eol-cloth_gb300/train_lpc.py --systems 2000 --epochs 20 --lr 3e-3 --probes white \
+        --meshes mixed --big 256 --seed 1 --out eol-cloth_gb300/weights/lpc.npy
 """
 import argparse
 import os
@@ -147,10 +148,11 @@ def generate(lpc, n_systems, quads=64, steps_per_run=50, seed=1, device=0, ctx=N
 
 
 def generate_mixed(lpc, n_systems, seed=1, steps_per_run=40, device=0, n_delaunay=6,
-                   quads=48, probes="white"):
+                   quads=48, big=0, probes="white"):
     """Training systems on one batched topology that holds a quads x quads
-    grid sheet and n_delaunay irregular Delaunay sheets of 1,500-6,000
-    triangles (density gradient along x), so the network sees regular and
+    grid sheet, a big x big grid sheet (big > 0: the benchmark's own size)
+    and n_delaunay irregular Delaunay sheets of 1,500-6,000 triangles
+    (density gradient along x), so the network sees regular and
     remeshed-like stencils.  Per run: random pins per instance (a non-empty
     subset of the corners plus a few boundary nodes), random wind, E ~ U(20,
     100) and a density giving h^2 K / M of 64^2..256^2 sheets; every batched
@@ -159,9 +161,10 @@ def generate_mixed(lpc, n_systems, seed=1, steps_per_run=40, device=0, n_delauna
     import scenes  # mesh generators shared with the tests
     rng = np.random.default_rng(seed)
     sheets = []
-    x0, X, tri, hinge, corners = grid_sheet(quads)
-    sheets.append(dict(x=x0, X=X, tri=tri, hinge=hinge, n=len(x0) // 3,
-                       corners=[corners[c] for c in (1, 2, 3, 4)]))
+    for q in ([quads] + ([big] if big > 0 else [])):
+        x0, X, tri, hinge, corners = grid_sheet(q)
+        sheets.append(dict(x=x0, X=X, tri=tri, hinge=hinge, n=len(x0) // 3,
+                           corners=[corners[c] for c in (1, 2, 3, 4)]))
     for k in range(n_delaunay):
         d = scenes.delaunay_sheet(int(rng.integers(1500, 6001)), rng)
         Xd = d["X"].reshape(-1, 2)
@@ -206,7 +209,7 @@ def generate_mixed(lpc, n_systems, seed=1, steps_per_run=40, device=0, n_delauna
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--systems", type=int, default=1000)
+    ap.add_argument("--systems", type=int, default=2000)
     ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--lr", type=float, default=3e-3)
     ap.add_argument("--quads", type=int, default=64)
@@ -215,12 +218,14 @@ def main():
     ap.add_argument("--meshes", default="mixed", choices=["grid", "mixed"],
                     help="grid: one quads x quads sheet; mixed: a batch of a grid and "
                          "irregular Delaunay sheets")
+    ap.add_argument("--big", type=int, default=256,
+                    help="mixed: also a big x big grid sheet in the batch (0: none)")
     ap.add_argument("--out", default=os.path.join(HERE, "weights", "lpc.npy"))
     args = ap.parse_args()
     lpc = eolc.LearnedPC(0, seed=args.seed)
     t0 = time.time()
     if args.meshes == "mixed":
-        generate_mixed(lpc, args.systems, seed=args.seed, probes=args.probes)
+        generate_mixed(lpc, args.systems, seed=args.seed, big=args.big, probes=args.probes)
     else:
         generate(lpc, args.systems, quads=args.quads, seed=args.seed, probes=args.probes)
     t1 = time.time()

@@ -324,7 +324,8 @@ ARM_KERNEL = {"jacobi": "jacobi_resident_kernel", "block": "jacobi_resident_kern
               "patch": "patch_resident_kernel", "patch-1l": "patch_resident_kernel",
               "patch-r4": "patch_resident_kernel",
               "learned": "learned_resident_kernel", "learned-1l": "learned_resident_kernel",
-              "learned-r4": "learned_resident_kernel", "jacobi-streamed": "cg_kernel"}
+              "learned-r4": "learned_resident_kernel", "learned-r2": "learned_resident_kernel",
+              "jacobi-streamed": "cg_kernel"}
 
 
 def arm_opts(eolc, arm, degree):
@@ -341,7 +342,7 @@ def arm_opts(eolc, arm, degree):
         return eolc.SolveOpts(precond=eolc.PC_PATCH, degree=degree, **base)
     if arm == "patch-1l":
         return eolc.SolveOpts(precond=eolc.PC_PATCH, degree=degree, no_coarse=1, **base)
-    if arm in ("learned", "learned-r4"):
+    if arm in ("learned", "learned-r2", "learned-r4"):
         return eolc.SolveOpts(precond=eolc.PC_LEARNED, fallback_factor=2, **base)
     if arm == "learned-1l":
         return eolc.SolveOpts(precond=eolc.PC_LEARNED, fallback_factor=2, no_coarse=1, **base)
@@ -349,10 +350,11 @@ def arm_opts(eolc, arm, degree):
 
 
 def arm_refresh(arm):
-    """Refresh interval of an arm: learned-r4 re-evaluates the learned
-    preconditioner every 4 solves (eolc_set_learned_refresh), patch-r4
-    rebuilds the coarse operator every 4 solves (eolc_set_coarse_refresh)."""
-    return 4 if arm in ("learned-r4", "patch-r4") else 1
+    """Refresh interval of an arm: learned-rK re-evaluates the learned
+    preconditioner (and its coarse operator) every K solves
+    (eolc_set_learned_refresh), patch-r4 rebuilds the coarse operator every 4
+    solves (eolc_set_coarse_refresh)."""
+    return {"learned-r4": 4, "patch-r4": 4, "learned-r2": 2}.get(arm, 1)
 
 
 def max_over_ranks(value, world, dev):
@@ -505,7 +507,8 @@ def run_export(ctx, sc, x, stream, frames=10):
     import tempfile
     import numpy as np
     import torch
-    import oracle as O
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O  # CPU side only: the text the frame must equal
     ctx.state_upload(x, sc["X"], np.zeros_like(x))
     a, b = ctx.export_obj_text(1, H)  # warm-up (buffers)
     t0 = time.perf_counter()
@@ -546,6 +549,15 @@ def run_export(ctx, sc, x, stream, frames=10):
                     "fwrite calls to a temporary directory"}
 
 
+def axis_box(eolc, center, dim):
+    """Axis-aligned box obstacle (eolc.Box): frame = translation to center,
+    stored column-major as the reference's Eigen::Matrix4d."""
+    import numpy as np
+    E1 = np.eye(4)
+    E1[:3, 3] = center
+    return eolc.Box(dim, E1.flatten(order="F"))
+
+
 def run_contacts(args, local_rank, stream, flush, steps=5):
     """Cloth::step with the contact QP (eolc_step_contacts) on the 256x256-quad
     sheet draped over a box (10.6k CD2 contacts), against the plain step on the
@@ -555,14 +567,15 @@ def run_contacts(args, local_rank, stream, flush, steps=5):
     import numpy as np
     import torch
     import eolc
-    import oracle as O
-    import qp_ref
     import scenes as S
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O  # CPU side only: the oracle's CD2 row count and QP below
+    import qp_ref
     x0, X, tri, center, snaps = S.drape_positions(QUADS, 40)
     n = len(x0) // 3
     hinge = eolc.mesh_hinges(tri)
-    box = O.axis_box(center, (0.4, 0.4, 0.2))  # the oracle's box, for its CD2 below
-    ebox = eolc.Box(box.dim, box.E1)
+    ebox = axis_box(eolc, center, (0.4, 0.4, 0.2))
+    box = O.axis_box(center, (0.4, 0.4, 0.2))  # the same box for the oracle's CD2
     ids = eolc.corner_ids(QUADS + 1, QUADS + 1)
     fixed = np.array([3 * ids[k] + c for k in (3, 4) for c in range(3)], np.int32)
     fvel = np.zeros(len(fixed))
@@ -685,9 +698,7 @@ def contact_trajectory(args, local_rank, stream, quads=128, steps=80):
     hinge = eolc.mesh_hinges(tri)
     x = x0 + np.random.default_rng(2).normal(0.0, 1e-4, x0.size)
     v = np.zeros(3 * n)
-    E1 = np.eye(4)
-    E1[:3, 3] = [0.5, 0.5, -0.05 - 0.1]
-    box = eolc.Box((0.4, 0.4, 0.2), E1.T.ravel())
+    box = axis_box(eolc, [0.5, 0.5, -0.05 - 0.1], (0.4, 0.4, 0.2))
     ctx = eolc.Context(local_rank)
     ctx.set_stream(stream.cuda_stream)
     ctx.set_topology(n, tri, hinge)
@@ -730,15 +741,16 @@ def run_cd2(args, local_rank, stream, steps=200, cpu_sample=40):
     import numpy as np
     import torch
     import eolc
-    import oracle as O
     import scenes as S
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O  # CPU side only: the contact bytes to match and the baseline
     x0, X, tri, center, snaps = S.drape_positions(128, steps, seed=2024)
     n = len(x0) // 3
     ctx = eolc.Context(local_rank)
     ctx.set_stream(stream.cuda_stream)
     ctx.set_topology(n, tri, eolc.mesh_hinges(tri))
     ob = O.axis_box(center, (0.4, 0.4, 0.2))  # the oracle's box (parity check below)
-    gb = eolc.Box(list(ob.dim), list(ob.E1))
+    gb = axis_box(eolc, center, (0.4, 0.4, 0.2))
     ctx.cd2(snaps[0], boxes=[gb], threshold=1e-3)  # edge list and perturbation built
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     wall, dev, raw, launches0 = [], [], [], ctx.launch_count()
@@ -888,8 +900,8 @@ def run_ours(args, rank, world, local_rank):
     lpc = None
     weights = os.path.join(ROOT, "eol-cloth_gb300", "weights", "lpc.npy")
     arms = args.precond.split(",") if args.precond != "all" else \
-        ["jacobi", "jacobi-streamed", "patch", "patch-r4", "patch-1l", "learned", "learned-r4",
-         "learned-1l"]
+        ["jacobi", "jacobi-streamed", "patch", "patch-r4", "patch-1l", "learned", "learned-r2",
+         "learned-r4", "learned-1l"]
     if any(a.startswith("learned") for a in arms):
         if os.path.exists(weights):
             lpc = eolc.LearnedPC(local_rank)

@@ -341,10 +341,12 @@ __global__ void edge_concat_bwd_kernel(int n, const int *inc_ptr, const int *inc
 }
 
 // ---- inference forward: edge gates and the input layer ----------------------------
-// One thread per (edge, four channels): gate_e = sigmoid(x_e Wg + bg), shared
-// by the three message-passing layers; then one thread per (node, four
-// channels): h0_i = relu(f_i Wn + bn).  Both summed in the order of
-// dense_fwd_kernel; the BF16-rounded weights sit in shared memory.
+// Per (edge, four channels): gate_e = sigmoid(x_e Wg + bg), shared by the
+// three message-passing layers; then per (node, four channels):
+// h0_i = relu(f_i Wn + bn).  Both summed in the order of dense_fwd_kernel;
+// the BF16-rounded weights sit in shared memory, and each thread takes
+// kGateItems items so the staging is paid once per 2,048 items.
+constexpr int kGateItems = 8;
 __global__ void __launch_bounds__(256)
 gate_h0_kernel(int m, int n, const float *__restrict__ fE, const float *__restrict__ Wg,
                const float *__restrict__ fN, const float *__restrict__ Wn,
@@ -359,8 +361,9 @@ gate_h0_kernel(int m, int n, const float *__restrict__ fE, const float *__restri
     reinterpret_cast<float *>(sn)[q] = w;
   }
   __syncthreads();
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int groups = kH / 4;
+  const int t0 = blockIdx.x * blockDim.x * kGateItems + threadIdx.x;
+  for (int t = t0; t < min(t0 + blockDim.x * kGateItems, (m + n) * groups); t += blockDim.x) {
   if (t < m * groups) {
     const int e = t / groups, c = t % groups;
     float4 g = sg[kFE][c];
@@ -383,6 +386,7 @@ gate_h0_kernel(int m, int n, const float *__restrict__ fE, const float *__restri
     }
     reinterpret_cast<float4 *>(h0)[u] =
         make_float4(fmaxf(a.x, 0.f), fmaxf(a.y, 0.f), fmaxf(a.z, 0.f), fmaxf(a.w, 0.f));
+  }
   }
 }
 
@@ -1011,8 +1015,8 @@ std::string forward_fused(LearnedPC &P, const Graph &G, const int *blk_row, cons
                                                           G.ei.p, G.ej.p, G.bij.p, P.fN.p,
                                                           P.dvec.p, P.fE.p);
   const int gh = (m + n) * (kH / 4);
-  gate_h0_kernel<<<(gh + 255) / 256, 256, 0, s>>>(m, n, P.fE.p, W + L.Wg, P.fN.p, W + L.Wn,
-                                                  P.gate.p, P.h[0].p);
+  gate_h0_kernel<<<(gh + 256 * kGateItems - 1) / (256 * kGateItems), 256, 0, s>>>(
+      m, n, P.fE.p, W + L.Wg, P.fN.p, W + L.Wn, P.gate.p, P.h[0].p);
   const int grid = nblk(n, kTcM);
   for (int l = 0; l + 1 < kLayers; ++l)
     layer_tc_kernel<false><<<grid, kTcThreads, kLayerSmem, s>>>(

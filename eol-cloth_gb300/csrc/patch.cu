@@ -1350,15 +1350,18 @@ __device__ __forceinline__ V4<float> apply_G(const ResParams &P, const ResSmem &
   const int sl = cta * (kRThreads / 32) + warp;
   const int off = P.slice_off[sl], len = P.slice_len[sl];
   float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+  const float4 *G4 = reinterpret_cast<const float4 *>(P.Gs);
 #pragma unroll 2
   for (int k = 0; k < len; ++k) {
     const size_t slot = size_t(off + k);
-    const int m = P.bsl[slot * 32 + lane];
+    const float4 ga = __ldg(G4 + (slot * 3 + 0) * 32 + lane);
+    const float4 gb = __ldg(G4 + (slot * 3 + 1) * 32 + lane);
+    const float4 gc = __ldg(G4 + (slot * 3 + 2) * 32 + lane);
+    const int m = __float_as_int(gc.y);
     const float4 x = m >= 0 ? sm.xs[m] : sm.xh[-1 - m];
-    const float *v = P.Gs + slot * 9 * 32 + lane;
-    a0 += __ldg(v) * x.x + __ldg(v + 32) * x.y + __ldg(v + 64) * x.z;
-    a1 += __ldg(v + 96) * x.x + __ldg(v + 128) * x.y + __ldg(v + 160) * x.z;
-    a2 += __ldg(v + 192) * x.x + __ldg(v + 224) * x.y + __ldg(v + 256) * x.z;
+    a0 += ga.x * x.x + ga.y * x.y + ga.z * x.z;
+    a1 += ga.w * x.x + gb.x * x.y + gb.y * x.z;
+    a2 += gb.z * x.x + gb.w * x.y + gc.x * x.z;
   }
   return V4<float>{a0, a1, a2, 0.f};
 }
@@ -1590,15 +1593,22 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
 // ---- per-solve permutation kernels --------------------------------------------
 // Warp-slice layout of the learned G (see apply_G): gsrc holds, per slot and
 // lane, the block of G in the context's order, or -1 for padding.
+// A slot-lane record is 12 words in three float4s, each float4 of a slot
+// stored lane-contiguous (512 bytes per warp load): (g0..g3), (g4..g7),
+// (g8, column as int bits, 0, 0) -- three loads per block instead of ten.
 __global__ void slice_blocks_kernel(int n_lanes, const int *__restrict__ gsrc,
-                                    const float *__restrict__ G, float *__restrict__ Gs) {
+                                    const int16_t *__restrict__ bsl, const float *__restrict__ G,
+                                    float4 *__restrict__ Gs) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= n_lanes) return;
   const int k = gsrc[idx];
   const size_t slot = size_t(idx >> 5), lane = size_t(idx & 31);
-  float *d = Gs + slot * 9 * 32 + lane;
+  float g[9];
 #pragma unroll
-  for (int c = 0; c < 9; ++c) d[32 * c] = k >= 0 ? __ldg(G + size_t(k) * 9 + c) : 0.f;
+  for (int c = 0; c < 9; ++c) g[c] = k >= 0 ? __ldg(G + size_t(k) * 9 + c) : 0.f;
+  Gs[(slot * 3 + 0) * 32 + lane] = make_float4(g[0], g[1], g[2], g[3]);
+  Gs[(slot * 3 + 1) * 32 + lane] = make_float4(g[4], g[5], g[6], g[7]);
+  Gs[(slot * 3 + 2) * 32 + lane] = make_float4(g[8], __int_as_float(int(bsl[idx])), 0.f, 0.f);
 }
 
 // Ap[k] = A[src[k]], one float per thread: consecutive threads read and
@@ -2317,11 +2327,12 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, i
   }
   if (learned && Gm) {  // Gm == nullptr: keep the sliced G of the last solve
     const int n_lanes = int(w->gsrc.n);
-    if (w->Gs.resize(size_t(n_lanes) * 9) != cudaSuccess) {
+    if (w->Gs.resize(size_t(n_lanes) * 12) != cudaSuccess) {
       err = "device allocation failed";
       return EOLC_CUDA_ERROR;
     }
-    slice_blocks_kernel<<<(n_lanes + 255) / 256, 256, 0, s>>>(n_lanes, w->gsrc.p, Gm, w->Gs.p);
+    slice_blocks_kernel<<<(n_lanes + 255) / 256, 256, 0, s>>>(
+        n_lanes, w->gsrc.p, w->bsl.p, Gm, reinterpret_cast<float4 *>(w->Gs.p));
     launches += 1;
   }
   permute_vectors_kernel<<<nn, 128, 0, s>>>(N, w->perm.p, a.b, a.beq_full, a.pinned, w->bp.p,

@@ -239,7 +239,7 @@ eolc_status run_pcg_learned(SolveWork *&w, const PcgArgs &a, const float *Gm,
 struct eolc_lpc;
 namespace eolc {
 // kernel launches of one learned_forward call
-constexpr int kLearnedForwardLaunches = 7;
+constexpr int kLearnedForwardLaunches = 10;
 std::string learned_forward(eolc_lpc *P, eolc_ctx *ctx, const uint8_t *pinned_d,
                             const float **G_out, cudaStream_t s);
 }

@@ -72,7 +72,7 @@ __device__ __forceinline__ float bf16r(float w) {
 __device__ __forceinline__ float softplus(float x) {
   return x > 20.f ? x : log1pf(expf(x));
 }
-__device__ __forceinline__ float sigm(float x) { return 1.f / (1.f + expf(-x)); }
+__device__ __forceinline__ float sigm(float x) { return __fdividef(1.f, 1.f + __expf(-x)); }
 
 enum Act { kNone = 0, kRelu = 1, kSigmoid = 2 };
 
@@ -220,30 +220,44 @@ std::string build_graph(const HostTopology &H, Graph &G, cudaStream_t s) {
 //        normalised by its mean diagonal (6 unique entries), pinned fraction];
 //        d = diag(A_ii) (3)
 // edge: A_ij / sqrt(m_i m_j) (9), m = mean diagonal
+// Node rows: eight lanes per node, each lane the norms of every eighth block
+// of the row (consecutive lanes read consecutive blocks), summed by a fixed
+// shuffle tree; then one thread per edge.
 __global__ void features_kernel(int n, int m, const int *rowptr, const int *diag, const float *A,
                                 const uint8_t *pinned, const int *ei, const int *ej,
                                 const int *bij, float *fN, float *dvec, float *fE) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < n) {
-    const float *D = A + size_t(diag[t]) * 9;
-    float mdiag = (D[0] + D[4] + D[8]) / 3.f;
-    float *f = fN + size_t(t) * kFN;
-    // scale-free coupling strength: sum of off-diagonal block norms over the
-    // diagonal block's norm (large when stiffness dominates mass)
-    float off = 0.f, dn = 0.f;
-    for (int k = 0; k < 9; ++k) dn += D[k] * D[k];
-    for (int k = rowptr[t]; k < rowptr[t + 1]; ++k) {
-      if (k == diag[t]) continue;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int node = t >> 3, sub = t & 7;
+  float off = 0.f;
+  int dk = 0;
+  if (node < n) {
+    dk = diag[node];
+    for (int k = rowptr[node] + sub; k < rowptr[node + 1]; k += 8) {
+      if (k == dk) continue;
       const float *B = A + size_t(k) * 9;
       float b2 = 0.f;
       for (int q = 0; q < 9; ++q) b2 += B[q] * B[q];
       off += sqrtf(b2);
     }
-    f[0] = logf(1e-12f + off / sqrtf(dn));
-    f[1] = D[0] / mdiag; f[2] = D[4] / mdiag; f[3] = D[8] / mdiag;
-    f[4] = D[1] / mdiag; f[5] = D[2] / mdiag; f[6] = D[5] / mdiag;
-    f[7] = (pinned[3 * t] + pinned[3 * t + 1] + pinned[3 * t + 2]) / 3.f;
-    dvec[3 * t] = D[0]; dvec[3 * t + 1] = D[4]; dvec[3 * t + 2] = D[8];
+  }
+  off += __shfl_xor_sync(0xffffffffu, off, 4);  // every lane of the warp takes part
+  off += __shfl_xor_sync(0xffffffffu, off, 2);
+  off += __shfl_xor_sync(0xffffffffu, off, 1);
+  if (node < n) {
+    if (sub == 0) {
+      const float *D = A + size_t(dk) * 9;
+      const float mdiag = (D[0] + D[4] + D[8]) / 3.f;
+      float *f = fN + size_t(node) * kFN;
+      // scale-free coupling strength: sum of off-diagonal block norms over
+      // the diagonal block's norm (large when stiffness dominates mass)
+      float dn = 0.f;
+      for (int k = 0; k < 9; ++k) dn += D[k] * D[k];
+      f[0] = logf(1e-12f + off / sqrtf(dn));
+      f[1] = D[0] / mdiag; f[2] = D[4] / mdiag; f[3] = D[8] / mdiag;
+      f[4] = D[1] / mdiag; f[5] = D[2] / mdiag; f[6] = D[5] / mdiag;
+      f[7] = (pinned[3 * node] + pinned[3 * node + 1] + pinned[3 * node + 2]) / 3.f;
+      dvec[3 * node] = D[0]; dvec[3 * node + 1] = D[4]; dvec[3 * node + 2] = D[8];
+    }
   }
   if (t < m) {
     const int i = ei[t], j = ej[t];
@@ -390,11 +404,58 @@ gate_h0_kernel(int m, int n, const float *__restrict__ fE, const float *__restri
   }
 }
 
+// agg_i = deg_inv_i * sum over the incidence entries of i (in order) of
+// gate_e * h_other: a half-warp per node, four channels per lane.  The
+// node's entries (edge, other node) are read by its lanes at once and
+// broadcast, so the per-edge loads of the gate and of the neighbour's h row
+// are independent of each other; no shared memory, so the SM keeps 64
+// warps of gathers in flight.  The sums are those of aggregate_fwd_kernel.
+__global__ void __launch_bounds__(256)
+aggregate_kernel(int n, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
+                 const int *__restrict__ inc_o, const float *__restrict__ deg_inv,
+                 const float *__restrict__ gate, const float *__restrict__ h_in,
+                 float *__restrict__ agg) {
+  const int lane = threadIdx.x & 31, hl = lane & 15, c4 = 4 * hl;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;
+  float a[4] = {0.f, 0.f, 0.f, 0.f};
+  int q0 = 0, deg = 0;
+  if (i < n) {
+    q0 = inc_ptr[i];
+    deg = inc_ptr[i + 1] - q0;
+  }
+  const int maxdeg = max(deg, __shfl_xor_sync(0xffffffffu, deg, 16));
+  for (int base = 0; base < maxdeg; base += 16) {
+    int me = 0, mo = 0;
+    if (base + hl < deg) {
+      me = inc[q0 + base + hl] >> 1;
+      mo = inc_o[q0 + base + hl];
+    }
+    const int cnt = min(16, maxdeg - base);
+#pragma unroll 4
+    for (int t = 0; t < cnt; ++t) {
+      const int e = __shfl_sync(0xffffffffu, me, t, 16);
+      const int o = __shfl_sync(0xffffffffu, mo, t, 16);
+      if (base + t < deg) {
+        const float4 g = __ldg(reinterpret_cast<const float4 *>(gate + size_t(e) * kH + c4));
+        const float4 ho = __ldg(reinterpret_cast<const float4 *>(h_in + size_t(o) * kH + c4));
+        a[0] += g.x * ho.x;
+        a[1] += g.y * ho.y;
+        a[2] += g.z * ho.z;
+        a[3] += g.w * ho.w;
+      }
+    }
+  }
+  if (i < n) {
+    const float d = deg_inv[i];
+    reinterpret_cast<float4 *>(agg)[size_t(i) * (kH / 4) + hl] =
+        make_float4(a[0] * d, a[1] * d, a[2] * d, a[3] * d);
+  }
+}
+
 // ---- inference forward on the tensor cores --------------------------------------
 // One message-passing layer per launch.  A CTA takes kTcM = 128 nodes (the
-// MMA's M): half-warps aggregate its nodes with the precomputed edge gates
-// (four channels per lane) and write [h, agg] as three BF16 terms into
-// K-major shared-memory tiles; one
+// MMA's M): its rows of [h, agg] (agg from aggregate_kernel) go as three
+// BF16 terms into K-major shared-memory tiles; one
 // thread then issues the 128 x 64 x 128 product with W (BF16) as
 // 8 K-steps x 3 terms of tcgen05.mma into a TMEM accumulator, and the eight
 // warps read it back (warp w: rows 32 (w % 4) .., columns 32 (w / 4) ..),
@@ -419,9 +480,7 @@ __device__ unsigned int g_tc_timeouts = 0;
 
 template <bool LAST>
 __global__ void __launch_bounds__(kTcThreads, 2)
-layer_tc_kernel(int n, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
-                const int *__restrict__ inc_o, const float *__restrict__ deg_inv,
-                const float *__restrict__ gate, const float *__restrict__ Wl,
+layer_tc_kernel(int n, const float *__restrict__ agg, const float *__restrict__ Wl,
                 const float *__restrict__ Wo, const float *__restrict__ Wt,
                 const float *__restrict__ h_in, float *__restrict__ h_out,
                 float *__restrict__ head, float *__restrict__ theta) {
@@ -440,49 +499,18 @@ layer_tc_kernel(int n, const int *__restrict__ inc_ptr, const int *__restrict__ 
     *reinterpret_cast<__nv_bfloat16 *>(sB + tc::tile_off(c, k, kLayerK)) =
         __float2bfloat16_rn(Wl[q]);
   }
-  // Aggregation: a half-warp per node, four channels per lane.  The node's
-  // incidence entries (edge, other node) are read by the lanes at once and
-  // broadcast, so the per-edge loads of the gate and of the neighbour's h
-  // row are independent of each other.
+  // [h, agg] rows of the tile (zero past n): a half-warp per row, four
+  // channels per lane, as three BF16 terms
   const int half = lane >> 4, hl = lane & 15, c4 = 4 * hl;
   for (int pr = warp; pr < kTcM / 2; pr += kTcThreads / 32) {
     const int ln = 2 * pr + half, i = node0 + ln;
-    float4 hv = make_float4(0.f, 0.f, 0.f, 0.f);
-    float a[4] = {0.f, 0.f, 0.f, 0.f};
-    int q0 = 0, deg = 0;
+    float4 hv = make_float4(0.f, 0.f, 0.f, 0.f), av = hv;
     if (i < n) {
-      q0 = inc_ptr[i];
-      deg = inc_ptr[i + 1] - q0;
       hv = __ldg(reinterpret_cast<const float4 *>(h_in + size_t(i) * kH + c4));
-    }
-    const int maxdeg = max(deg, __shfl_xor_sync(0xffffffffu, deg, 16));
-    for (int base = 0; base < maxdeg; base += 16) {
-      int me = 0, mo = 0;
-      if (base + hl < deg) {
-        me = inc[q0 + base + hl] >> 1;
-        mo = inc_o[q0 + base + hl];
-      }
-      const int cnt = min(16, maxdeg - base);
-#pragma unroll 4
-      for (int t = 0; t < cnt; ++t) {
-        const int e = __shfl_sync(0xffffffffu, me, t, 16);
-        const int o = __shfl_sync(0xffffffffu, mo, t, 16);
-        if (base + t < deg) {
-          const float4 g = __ldg(reinterpret_cast<const float4 *>(gate + size_t(e) * kH + c4));
-          const float4 ho = __ldg(reinterpret_cast<const float4 *>(h_in + size_t(o) * kH + c4));
-          a[0] += g.x * ho.x;
-          a[1] += g.y * ho.y;
-          a[2] += g.z * ho.z;
-          a[3] += g.w * ho.w;
-        }
-      }
-    }
-    if (i < n) {
-      const float d = deg_inv[i];
-      for (int c = 0; c < 4; ++c) a[c] *= d;
+      av = __ldg(reinterpret_cast<const float4 *>(agg + size_t(i) * kH + c4));
     }
     tc::put3x4(sA, kLayerPart, ln, c4, kLayerK, hv.x, hv.y, hv.z, hv.w);
-    tc::put3x4(sA, kLayerPart, ln, kH + c4, kLayerK, a[0], a[1], a[2], a[3]);
+    tc::put3x4(sA, kLayerPart, ln, kH + c4, kLayerK, av.x, av.y, av.z, av.w);
   }
   tc::fence_smem_to_async();
   tc::fence_before_sync();
@@ -549,13 +577,22 @@ layer_tc_kernel(int n, const int *__restrict__ inc_ptr, const int *__restrict__ 
     ok = ok && __all_sync(0xffffffffu, tc::mbar_wait(bar, 1, kTcWaitLimit));
     tc::fence_after_sync();
     if (ok) tc::tmem_ld32(tmem + lane_addr + kH + c0, v);
-    if (i < n) {
+    if (!ok)
 #pragma unroll
-      for (int k = 0; k < 32; ++k) {
-        const int c = c0 + k;
-        const float x = ok ? v[k] : __int_as_float(0x7fc00000);
-        if (c < 2 * kOE) head[size_t(i) * 2 * kOE + c] = x;
-        else if (c < kHeadCols) theta[size_t(i) * kON + c - 2 * kOE] = x + __ldg(Wt + kH * kON + c - 2 * kOE);
+      for (int k = 0; k < 32; ++k) v[k] = __int_as_float(0x7fc00000);
+    if (i < n) {
+      // head row: 36 floats (144 bytes, 16-byte aligned) as float4 stores;
+      // columns 36..38 are theta
+      float4 *hrow = reinterpret_cast<float4 *>(head + size_t(i) * 2 * kOE);
+      if (c0 == 0) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+          hrow[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+      } else {
+        hrow[8] = make_float4(v[0], v[1], v[2], v[3]);
+#pragma unroll
+        for (int k = 0; k < kON; ++k)
+          theta[size_t(i) * kON + k] = v[4 + k] + __ldg(Wt + kH * kON + k);
       }
     }
   }
@@ -637,48 +674,63 @@ edge_blocks_kernel(int m, const int *__restrict__ ei, const int *__restrict__ ej
                    const uint8_t *__restrict__ pinned, float *__restrict__ uv,
                    float *__restrict__ Gv) {
   __shared__ float sW[kFE * kOE + kOE];
+  // per warp: its 32 edges' U, V (18 each) and two blocks (9 each), written
+  // back to global memory lane-contiguously
+  __shared__ float sOut[4][32 * 36];
   for (int k = threadIdx.x; k < kFE * kOE; k += blockDim.x) sW[k] = bf16r(Wo[2 * kH * kOE + k]);
   for (int k = threadIdx.x; k < kOE; k += blockDim.x) sW[kFE * kOE + k] = Wo[kEdgeIn * kOE + k];
   __syncthreads();
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= m) return;
-  const int i = ei[e], j = ej[e];
-  float acc[kOE];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int e0 = blockIdx.x * blockDim.x + 32 * warp, e = e0 + lane;
+  float *so = sOut[warp];
+  if (e < m) {
+    const int i = ei[e], j = ej[e];
+    float acc[kOE];
 #pragma unroll
-  for (int c = 0; c < kOE; ++c) acc[c] = sW[kFE * kOE + c];
-  for (int k = 0; k < kFE; ++k) {
-    const float x = __ldg(fE + size_t(e) * kFE + k);
+    for (int c = 0; c < kOE; ++c) acc[c] = sW[kFE * kOE + c];
+    for (int k = 0; k < kFE; ++k) {
+      const float x = __ldg(fE + size_t(e) * kFE + k);
 #pragma unroll
-    for (int c = 0; c < kOE; ++c) acc[c] += x * sW[k * kOE + c];
-  }
-  const float *hi = head + size_t(i) * 2 * kOE, *hj = head + size_t(j) * 2 * kOE + kOE;
-  float U[9], V[9];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    const float si = rsqrtf(dvec[3 * i + a]), sj = rsqrtf(dvec[3 * j + a]);
-#pragma unroll
-    for (int b = 0; b < 3; ++b) {
-      U[3 * a + b] = si * ((__ldg(hi + 3 * a + b) + __ldg(hj + 3 * a + b)) + acc[3 * a + b]);
-      V[3 * a + b] = sj * ((__ldg(hi + 9 + 3 * a + b) + __ldg(hj + 9 + 3 * a + b)) +
-                           acc[9 + 3 * a + b]);
+      for (int c = 0; c < kOE; ++c) acc[c] += x * sW[k * kOE + c];
     }
-  }
+    const float *hi = head + size_t(i) * 2 * kOE, *hj = head + size_t(j) * 2 * kOE + kOE;
+    float U[9], V[9];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) {
-    uv[size_t(e) * 18 + k] = U[k];
-    uv[size_t(e) * 18 + 9 + k] = V[k];
+    for (int a = 0; a < 3; ++a) {
+      const float si = rsqrtf(dvec[3 * i + a]), sj = rsqrtf(dvec[3 * j + a]);
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        U[3 * a + b] = si * ((__ldg(hi + 3 * a + b) + __ldg(hj + 3 * a + b)) + acc[3 * a + b]);
+        V[3 * a + b] = sj * ((__ldg(hi + 9 + 3 * a + b) + __ldg(hj + 9 + 3 * a + b)) +
+                             acc[9 + 3 * a + b]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      so[18 * lane + k] = U[k];
+      so[18 * lane + 9 + k] = V[k];
+    }
+    float R[9];
+    mmT(U, V, R);
+    for (int a = 0; a < 3; ++a)
+      for (int c = 0; c < 3; ++c)
+        so[576 + 9 * lane + 3 * a + c] =
+            (!pinned[3 * i + a] && !pinned[3 * j + c]) ? R[3 * a + c] : 0.f;
+    mmT(V, U, R);
+    for (int a = 0; a < 3; ++a)
+      for (int c = 0; c < 3; ++c)
+        so[864 + 9 * lane + 3 * a + c] =
+            (!pinned[3 * j + a] && !pinned[3 * i + c]) ? R[3 * a + c] : 0.f;
   }
-  float R[9];
-  mmT(U, V, R);
-  for (int a = 0; a < 3; ++a)
-    for (int c = 0; c < 3; ++c)
-      Gv[size_t(bij[e]) * 9 + 3 * a + c] =
-          (!pinned[3 * i + a] && !pinned[3 * j + c]) ? R[3 * a + c] : 0.f;
-  mmT(V, U, R);
-  for (int a = 0; a < 3; ++a)
-    for (int c = 0; c < 3; ++c)
-      Gv[size_t(bji[e]) * 9 + 3 * a + c] =
-          (!pinned[3 * j + a] && !pinned[3 * i + c]) ? R[3 * a + c] : 0.f;
+  __syncwarp();
+  const int ne = min(32, m - e0);
+  if (ne <= 0) return;
+  for (int t = lane; t < 18 * ne; t += 32) uv[size_t(e0) * 18 + t] = so[t];
+  for (int t = lane; t < 9 * ne; t += 32) {
+    const int q = t / 9, c = t - 9 * q;
+    Gv[size_t(__ldg(bij + e0 + q)) * 9 + c] = so[576 + t];
+    Gv[size_t(__ldg(bji + e0 + q)) * 9 + c] = so[864 + t];
+  }
 }
 
 __global__ void __launch_bounds__(128)
@@ -854,6 +906,7 @@ struct LearnedPC {
   DevBuf<float> fN, dvec, fE, h[4], cat[3], gate, eX, o, theta;
   DevBuf<float> head;  // inference: per-node shares of the edge head (2 x 18)
   DevBuf<float> uv;    // inference: U_e, V_e per edge (2 x 9)
+  DevBuf<float> agg;   // inference: a layer's aggregated neighbour rows
   DevBuf<float> dh, dcat, dgate, deX, dO, dtheta, dGv, tmpX;
   DevBuf<float> Gv;
   // training set: one topology, many systems
@@ -910,7 +963,7 @@ std::string forward(LearnedPC &P, const Graph &G, const int *blk_row, const floa
   const Layout &L = P.L;
   const float *W = P.params.p;
   const int n = G.n, m = G.m;
-  features_kernel<<<nblk(std::max(n, m), 256), 256, 0, s>>>(n, m, G.rowptr.p, G.diag.p, A, pinned,
+  features_kernel<<<nblk(std::max(8 * n, m), 256), 256, 0, s>>>(n, m, G.rowptr.p, G.diag.p, A, pinned,
                                                           G.ei.p, G.ej.p, G.bij.p, P.fN.p,
                                                           P.dvec.p, P.fE.p);
   auto dense = [&](int rows, int in, int out, const float *X, int woff, int boff, int act, float *Y) {
@@ -992,9 +1045,10 @@ std::string backward(LearnedPC &P, const Graph &G, const uint8_t *pinned, cudaSt
 namespace eolc {
 namespace lpc {
 
-// Inference forward (kLearnedForwardLaunches = 7 launches): features, edge
-// gates with h0, layers 1 and 2, layer 3 with the node-side heads, the edge
-// head with the off-diagonal blocks of G, the diagonal blocks.  Fills
+// Inference forward (kLearnedForwardLaunches = 10 launches): features, edge
+// gates with h0, three (aggregation, layer) pairs -- the last layer with the
+// node-side heads --, the edge head with the off-diagonal blocks of G, the
+// diagonal blocks.  Fills
 // P.Gv; the network of forward() to FP32 rounding.
 std::string forward_fused(LearnedPC &P, const Graph &G, const int *blk_row, const float *A,
                           const uint8_t *pinned, cudaStream_t s) {
@@ -1011,20 +1065,23 @@ std::string forward_fused(LearnedPC &P, const Graph &G, const int *blk_row, cons
                          kLayerSmem);
     attr_set[0][dev] = true;
   }
-  features_kernel<<<nblk(std::max(n, m), 256), 256, 0, s>>>(n, m, G.rowptr.p, G.diag.p, A, pinned,
+  features_kernel<<<nblk(std::max(8 * n, m), 256), 256, 0, s>>>(n, m, G.rowptr.p, G.diag.p, A, pinned,
                                                           G.ei.p, G.ej.p, G.bij.p, P.fN.p,
                                                           P.dvec.p, P.fE.p);
   const int gh = (m + n) * (kH / 4);
   gate_h0_kernel<<<(gh + 256 * kGateItems - 1) / (256 * kGateItems), 256, 0, s>>>(
       m, n, P.fE.p, W + L.Wg, P.fN.p, W + L.Wn, P.gate.p, P.h[0].p);
-  const int grid = nblk(n, kTcM);
-  for (int l = 0; l + 1 < kLayers; ++l)
+  const int grid = nblk(n, kTcM), agrid = nblk(16 * n, 256);
+  for (int l = 0; l + 1 < kLayers; ++l) {
+    aggregate_kernel<<<agrid, 256, 0, s>>>(n, G.inc_ptr.p, G.inc.p, G.inc_o.p, G.deg_inv.p,
+                                          P.gate.p, P.h[l].p, P.agg.p);
     layer_tc_kernel<false><<<grid, kTcThreads, kLayerSmem, s>>>(
-        n, G.inc_ptr.p, G.inc.p, G.inc_o.p, G.deg_inv.p, P.gate.p, W + L.Wl[l],
-        W + L.Wo, W + L.Wt, P.h[l].p, P.h[l + 1].p, nullptr, nullptr);
+        n, P.agg.p, W + L.Wl[l], W + L.Wo, W + L.Wt, P.h[l].p, P.h[l + 1].p, nullptr, nullptr);
+  }
+  aggregate_kernel<<<agrid, 256, 0, s>>>(n, G.inc_ptr.p, G.inc.p, G.inc_o.p, G.deg_inv.p,
+                                        P.gate.p, P.h[kLayers - 1].p, P.agg.p);
   layer_tc_kernel<true><<<grid, kTcThreads, kLayerSmem, s>>>(
-      n, G.inc_ptr.p, G.inc.p, G.inc_o.p, G.deg_inv.p, P.gate.p,
-      W + L.Wl[kLayers - 1], W + L.Wo, W + L.Wt, P.h[kLayers - 1].p, nullptr, P.head.p,
+      n, P.agg.p, W + L.Wl[kLayers - 1], W + L.Wo, W + L.Wt, P.h[kLayers - 1].p, nullptr, P.head.p,
       P.theta.p);
   (void)blk_row;
   edge_blocks_kernel<<<nblk(m, 128), 128, 0, s>>>(m, G.ei.p, G.ej.p, G.bij.p, G.bji.p, P.head.p,
@@ -1047,6 +1104,7 @@ std::string ensure_buffers(LearnedPC &P, int n, int m, int nb, bool train) {
         P.h[0].resize(N * kH), P.h[1].resize(N * kH), P.h[2].resize(N * kH),
         P.h[3].resize(N * kH), P.o.resize(M * kOE), P.theta.resize(N * kON),
         P.head.resize(N * 2 * kOE), P.gate.resize(M * kH), P.uv.resize(M * 18),
+        P.agg.resize(N * kH),
         P.Gv.resize(size_t(nb) * 9 + 16)};
     for (cudaError_t e : es)
       if (e != cudaSuccess) return cudaGetErrorString(e);

@@ -212,6 +212,10 @@ def main():
     ap.add_argument("--systems", type=int, default=2000)
     ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--lr", type=float, default=3e-3)
+    ap.add_argument("--lr-final", type=float, default=None,
+                    help="cosine decay of the learning rate from --lr to this over the epochs "
+                         "(one eolc_lpc_train call per epoch, Adam state carried); default: "
+                         "constant --lr in one call")
     ap.add_argument("--quads", type=int, default=64)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--probes", default="white", choices=["white", "smooth"])
@@ -229,7 +233,15 @@ def main():
     else:
         generate(lpc, args.systems, quads=args.quads, seed=args.seed, probes=args.probes)
     t1 = time.time()
-    losses = lpc.train(args.epochs, lr=args.lr, seed=args.seed)
+    if args.lr_final is None:
+        losses = lpc.train(args.epochs, lr=args.lr, seed=args.seed)
+    else:
+        losses = []
+        for e in range(args.epochs):
+            w = 0.5 * (1 + np.cos(np.pi * e / max(1, args.epochs - 1)))
+            lr = args.lr_final + (args.lr - args.lr_final) * w
+            losses.append(lpc.train(1, lr=lr, seed=args.seed * 1000 + e)[0])
+            print("epoch %d lr %.2e loss %.4f" % (e, lr, losses[-1]), flush=True)
     t2 = time.time()
     os.makedirs(os.path.dirname(args.out), exist_ok=True)
     np.save(args.out, lpc.get_params())

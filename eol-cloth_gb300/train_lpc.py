@@ -20,8 +20,8 @@ remeshed-like ones.
 Training: eolc_lpc_train (Adam on the GPU, the library's own forward and
 backward kernels).  The committed weights come from the defaults, i.e.:
 
-    python eol-cloth_gb300/train_lpc.py --systems 2000 --epochs 20 --lr 3e-3 --probes white \
-        --meshes mixed --big 256 --seed 1 --out eol-cloth_gb300/weights/lpc.npy
+    python eol-cloth_gb300/train_lpc.py --systems 2000 --epochs 40 --lr 3e-3 --lr-final 1e-4 \
+        --probes white --meshes mixed --big 256 --seed 1 --out eol-cloth_gb300/weights/lpc.npy
 """
 import argparse
 import os
@@ -210,11 +210,11 @@ def generate_mixed(lpc, n_systems, seed=1, steps_per_run=40, device=0, n_delauna
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--systems", type=int, default=2000)
-    ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--epochs", type=int, default=40)
     ap.add_argument("--lr", type=float, default=3e-3)
-    ap.add_argument("--lr-final", type=float, default=None,
+    ap.add_argument("--lr-final", type=float, default=1e-4,
                     help="cosine decay of the learning rate from --lr to this over the epochs "
-                         "(one eolc_lpc_train call per epoch, Adam state carried); default: "
+                         "(one eolc_lpc_train call per epoch, Adam state carried); 0: "
                          "constant --lr in one call")
     ap.add_argument("--quads", type=int, default=64)
     ap.add_argument("--seed", type=int, default=1)
@@ -233,7 +233,7 @@ def main():
     else:
         generate(lpc, args.systems, quads=args.quads, seed=args.seed, probes=args.probes)
     t1 = time.time()
-    if args.lr_final is None:
+    if not args.lr_final:
         losses = lpc.train(args.epochs, lr=args.lr, seed=args.seed)
     else:
         losses = []

@@ -238,16 +238,20 @@ def test_carried_multipliers_change_the_path_not_the_answer(eolc):
 
 
 def test_dropped_sheet_contact_trajectory(eolc):
-    """Consecutive Cloth::steps with contacts: a 20x20-quad sheet (jittered
-    N(0, 1e-4), unpinned) dropped flat onto the 0.4 x 0.4 x 0.2 box whose top
-    face starts 0.05 m below it.  Every GPU step (FP64, multipliers carried
-    from step to step) against the oracle's exact-QP step from the same
-    state; contacts arrive once the sheet reaches the box."""
-    quads = 20
+    """Consecutive Cloth::steps with contacts on the configuration-2 sheet:
+    128x128 quads (positions jittered N(0, 1e-4), seed 2), unpinned, dropped
+    flat onto the 0.4 x 0.4 x 0.2 box whose top face starts 0.05 m below it
+    (mixed precision, patch-PCG to rel-res 1e-8, multipliers carried from
+    step to step).  Every step converges with every contact row satisfied to
+    the QP's bound, the first contacts arrive when free fall says (semi-
+    implicit Euler: g h^2 k (k + 1) / 2 = 0.05 - 1e-3 at k = 20), and the
+    sheet's centre then rests on the box top.  Per-step velocities against
+    the exact QP are tested on the 24x24 drape above."""
+    quads = 128
     r = quads + 1
     x0, X, tri = eolc.sheet_mesh(r, r)
     n = len(x0) // 3
-    hinge = O.hinges(n, tri)
+    hinge = eolc.mesh_hinges(tri)
     box = O.axis_box([0.5, 0.5, -0.15], (0.4, 0.4, 0.2))
     ctx = eolc.Context(0)
     ctx.set_topology(n, tri, hinge)
@@ -255,15 +259,16 @@ def test_dropped_sheet_contact_trajectory(eolc):
     x = x0 + np.random.default_rng(2).normal(0.0, 1e-4, x0.size)
     v = np.zeros(3 * n)
     none = np.zeros(0, np.int32)
-    opts = eolc.SolveOpts(rel_tol=1e-10, precision=eolc.PREC_FP64)
-    rows = []
-    for k in range(36):
-        xo, vo, m = _oracle_contact_step(x, X, v, tri, hinge, box, none, np.zeros(0))
+    opts = eolc.SolveOpts(rel_tol=1e-8, precision=eolc.PREC_MIXED, precond=eolc.PC_PATCH,
+                          degree=5)
+    active = []
+    for k in range(40):
         info = ctx.step_contacts(x, X, v, mat, scenes.GRAV, scenes.H, none, np.zeros(0),
                                  boxes=[eolc.Box(box.dim, box.E1)], threshold=1e-3, opts=opts)
         assert info.status == eolc.OK, k
-        assert _relmax(v, vo) <= 1e-7, (k, _relmax(v, vo))
-        assert np.abs(x - xo).max() <= scenes.H * 1e-7 * np.abs(vo).max() + 1e-15
-        rows.append(m)
-    print("contact rows per step:", rows)
-    assert rows[0] == 0 and max(rows[-8:]) > 0
+        assert info.max_violation <= 1e-6, (k, info.max_violation)
+        active.append(info.n_active)
+    print("active contact rows per step:", active)
+    assert max(active[:19]) == 0 and min(active[21:]) > 0
+    centre = x.reshape(-1, 3)[(r // 2) * r + r // 2]
+    assert abs(centre[2] - (-0.05)) <= 2e-3, centre

@@ -501,16 +501,28 @@ layer_tc_kernel(int n, const float *__restrict__ agg, const float *__restrict__ 
   }
   // [h, agg] rows of the tile (zero past n): a half-warp per row, four
   // channels per lane, as three BF16 terms
+  // (the loads of four row pairs are issued before their stores)
   const int half = lane >> 4, hl = lane & 15, c4 = 4 * hl;
-  for (int pr = warp; pr < kTcM / 2; pr += kTcThreads / 32) {
-    const int ln = 2 * pr + half, i = node0 + ln;
-    float4 hv = make_float4(0.f, 0.f, 0.f, 0.f), av = hv;
-    if (i < n) {
-      hv = __ldg(reinterpret_cast<const float4 *>(h_in + size_t(i) * kH + c4));
-      av = __ldg(reinterpret_cast<const float4 *>(agg + size_t(i) * kH + c4));
+  constexpr int kPairIters = kTcM / 2 / (kTcThreads / 32), kBatch = 4;
+  static_assert(kPairIters % kBatch == 0, "row batches");
+  for (int b0 = 0; b0 < kPairIters; b0 += kBatch) {
+    float4 hv[kBatch], av[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int i = node0 + 2 * (warp + (kTcThreads / 32) * (b0 + u)) + half;
+      hv[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+      av[u] = hv[u];
+      if (i < n) {
+        hv[u] = __ldg(reinterpret_cast<const float4 *>(h_in + size_t(i) * kH + c4));
+        av[u] = __ldg(reinterpret_cast<const float4 *>(agg + size_t(i) * kH + c4));
+      }
     }
-    tc::put3x4(sA, kLayerPart, ln, c4, kLayerK, hv.x, hv.y, hv.z, hv.w);
-    tc::put3x4(sA, kLayerPart, ln, kH + c4, kLayerK, av.x, av.y, av.z, av.w);
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int ln = 2 * (warp + (kTcThreads / 32) * (b0 + u)) + half;
+      tc::put3x4(sA, kLayerPart, ln, c4, kLayerK, hv[u].x, hv[u].y, hv[u].z, hv[u].w);
+      tc::put3x4(sA, kLayerPart, ln, kH + c4, kLayerK, av[u].x, av[u].y, av[u].z, av[u].w);
+    }
   }
   tc::fence_smem_to_async();
   tc::fence_before_sync();

@@ -50,6 +50,7 @@
 // 123-126); the result meets the same criterion.
 #include <cuda/atomic>
 #include <cuda_runtime.h>
+#include <cuda_bf16.h>
 
 #include <algorithm>
 #include <functional>
@@ -136,6 +137,7 @@ struct ResParams {
   const V4<float> *fmask;
   const float *pc;                         // Jacobi: 4 per node, block: 9
   const float *Gs;                         // learned PC: G in warp slices (below)
+  long long g_lanes;                       // slot-lanes of those slices
   const int16_t *bsl;                      // per slice slot: local row (>= 0) or
                                            // -1 - halo window slot
   const int *slice_off, *slice_len;        // per (CTA, warp) slice: first slot, slots
@@ -1350,18 +1352,20 @@ __device__ __forceinline__ V4<float> apply_G(const ResParams &P, const ResSmem &
   const int sl = cta * (kRThreads / 32) + warp;
   const int off = P.slice_off[sl], len = P.slice_len[sl];
   float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-  const float4 *G4 = reinterpret_cast<const float4 *>(P.Gs);
-#pragma unroll 2
+  const uint4 *GA = reinterpret_cast<const uint4 *>(P.Gs);
+  const uint32_t *GB = reinterpret_cast<const uint32_t *>(GA + P.g_lanes);
+  const auto lo = [](uint32_t w) { return __uint_as_float(w << 16); };
+  const auto hi = [](uint32_t w) { return __uint_as_float(w & 0xffff0000u); };
+#pragma unroll 3
   for (int k = 0; k < len; ++k) {
-    const size_t slot = size_t(off + k);
-    const float4 ga = __ldg(G4 + (slot * 3 + 0) * 32 + lane);
-    const float4 gb = __ldg(G4 + (slot * 3 + 1) * 32 + lane);
-    const float4 gc = __ldg(G4 + (slot * 3 + 2) * 32 + lane);
-    const int m = __float_as_int(gc.y);
+    const size_t q = size_t(off + k) * 32 + lane;
+    const uint4 ga = __ldg(GA + q);
+    const uint32_t gb = __ldg(GB + q);
+    const int m = int(int16_t(gb >> 16));
     const float4 x = m >= 0 ? sm.xs[m] : sm.xh[-1 - m];
-    a0 += ga.x * x.x + ga.y * x.y + ga.z * x.z;
-    a1 += ga.w * x.x + gb.x * x.y + gb.y * x.z;
-    a2 += gb.z * x.x + gb.w * x.y + gc.x * x.z;
+    a0 += lo(ga.x) * x.x + hi(ga.x) * x.y + lo(ga.y) * x.z;
+    a1 += hi(ga.y) * x.x + lo(ga.z) * x.y + hi(ga.z) * x.z;
+    a2 += lo(ga.w) * x.x + hi(ga.w) * x.y + lo(gb) * x.z;
   }
   return V4<float>{a0, a1, a2, 0.f};
 }
@@ -1593,22 +1597,26 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
 // ---- per-solve permutation kernels --------------------------------------------
 // Warp-slice layout of the learned G (see apply_G): gsrc holds, per slot and
 // lane, the block of G in the context's order, or -1 for padding.
-// A slot-lane record is 12 words in three float4s, each float4 of a slot
-// stored lane-contiguous (512 bytes per warp load): (g0..g3), (g4..g7),
-// (g8, column as int bits, 0, 0) -- three loads per block instead of ten.
+// A slot-lane record is 20 bytes: the block's nine values rounded to BF16
+// (G is a preconditioner: any symmetric positive definite G keeps PCG exact,
+// and rounding G_ij and G_ji = G_ij^T alike keeps it symmetric) and the
+// column, in two lane-contiguous arrays: g0..g7 as a uint4 (512 bytes per
+// warp load), (g8 | column << 16) as a uint32 after all the uint4s.
+__device__ __forceinline__ uint32_t bf16_bits(float x) {
+  const __nv_bfloat16 b = __float2bfloat16_rn(x);
+  return uint32_t(*reinterpret_cast<const unsigned short *>(&b));
+}
 __global__ void slice_blocks_kernel(int n_lanes, const int *__restrict__ gsrc,
                                     const int16_t *__restrict__ bsl, const float *__restrict__ G,
-                                    float4 *__restrict__ Gs) {
+                                    uint4 *__restrict__ GA, uint32_t *__restrict__ GB) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= n_lanes) return;
   const int k = gsrc[idx];
-  const size_t slot = size_t(idx >> 5), lane = size_t(idx & 31);
-  float g[9];
+  uint32_t g[9];
 #pragma unroll
-  for (int c = 0; c < 9; ++c) g[c] = k >= 0 ? __ldg(G + size_t(k) * 9 + c) : 0.f;
-  Gs[(slot * 3 + 0) * 32 + lane] = make_float4(g[0], g[1], g[2], g[3]);
-  Gs[(slot * 3 + 1) * 32 + lane] = make_float4(g[4], g[5], g[6], g[7]);
-  Gs[(slot * 3 + 2) * 32 + lane] = make_float4(g[8], __int_as_float(int(bsl[idx])), 0.f, 0.f);
+  for (int c = 0; c < 9; ++c) g[c] = bf16_bits(k >= 0 ? __ldg(G + size_t(k) * 9 + c) : 0.f);
+  GA[idx] = make_uint4(g[0] | g[1] << 16, g[2] | g[3] << 16, g[4] | g[5] << 16, g[6] | g[7] << 16);
+  GB[idx] = g[8] | uint32_t(uint16_t(bsl[idx])) << 16;
 }
 
 // Ap[k] = A[src[k]], one float per thread: consecutive threads read and
@@ -2327,12 +2335,13 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, i
   }
   if (learned && Gm) {  // Gm == nullptr: keep the sliced G of the last solve
     const int n_lanes = int(w->gsrc.n);
-    if (w->Gs.resize(size_t(n_lanes) * 12) != cudaSuccess) {
+    if (w->Gs.resize(size_t(n_lanes) * 5) != cudaSuccess) {  // 20 bytes per slot-lane
       err = "device allocation failed";
       return EOLC_CUDA_ERROR;
     }
+    uint4 *GA = reinterpret_cast<uint4 *>(w->Gs.p);
     slice_blocks_kernel<<<(n_lanes + 255) / 256, 256, 0, s>>>(
-        n_lanes, w->gsrc.p, w->bsl.p, Gm, reinterpret_cast<float4 *>(w->Gs.p));
+        n_lanes, w->gsrc.p, w->bsl.p, Gm, GA, reinterpret_cast<uint32_t *>(GA + n_lanes));
     launches += 1;
   }
   permute_vectors_kernel<<<nn, 128, 0, s>>>(N, w->perm.p, a.b, a.beq_full, a.pinned, w->bp.p,
@@ -2371,6 +2380,7 @@ eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, i
   P.fmask = fmask;
   P.pc = pc;
   P.Gs = learned ? w->Gs.p : nullptr;
+  P.g_lanes = learned ? (long long)w->gsrc.n : 0;
   P.bsl = w->bsl.p;
   P.slice_off = w->slice_off.p;
   P.slice_len = w->slice_len.p;

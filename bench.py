@@ -350,11 +350,13 @@ def arm_opts(eolc, arm, degree):
 
 
 def arm_refresh(arm):
-    """Refresh interval of an arm: learned-rK re-evaluates the learned
-    preconditioner (and its coarse operator) every K solves
-    (eolc_set_learned_refresh), patch-r4 rebuilds the coarse operator every 4
-    solves (eolc_set_coarse_refresh)."""
-    return {"learned-r4": 4, "patch-r4": 4, "learned-r2": 2}.get(arm, 1)
+    """(network, coarse) refresh intervals of an arm: learned-rK re-evaluates
+    the network every K solves (eolc_set_learned_refresh; learned: every
+    solve); every learned arm and patch-r4 update the coarse inverse every 4
+    solves (eolc_set_coarse_refresh), the other arms every solve."""
+    net = {"learned-r4": 4, "learned-r2": 2}.get(arm, 1)
+    coarse = 4 if arm.startswith("learned") or arm == "patch-r4" else 1
+    return net, coarse
 
 
 def max_over_ranks(value, world, dev):
@@ -465,12 +467,12 @@ def run_batched_sharded(args, rank, world, local_rank, stream, flush, dev):
                     "the data path (the timed-interval maximum only)"}
 
 
-def time_arm(ctx, sc, mat, opts, x_w, v_w, steps, stream, flush, world, dev, refresh=1):
+def time_arm(ctx, sc, mat, opts, x_w, v_w, steps, stream, flush, world, dev, refresh=(1, 1)):
     """K steps from the post-warm-up state, each bracketed by CUDA events on
     the library's stream with L2 flushed before it; max over ranks."""
     import torch
-    ctx.set_learned_refresh(refresh)
-    ctx.set_coarse_refresh(refresh)
+    ctx.set_learned_refresh(refresh[0])
+    ctx.set_coarse_refresh(refresh[1])
     ctx.state_upload(x_w, sc["X"], v_w)
     if world > 1:
         torch.distributed.barrier()
@@ -494,6 +496,7 @@ def time_arm(ctx, sc, mat, opts, x_w, v_w, steps, stream, flush, world, dev, ref
     torch.cuda.synchronize()
     total_ms = max_over_ranks(sum(step_ms), world, dev)
     ctx.set_learned_refresh(1)
+    ctx.set_coarse_refresh(1)
     return {"steps_per_s": job_rate(world, steps, total_ms), "ms_per_step": total_ms / steps,
             "mean_pcg_iters": statistics.mean(iters), "pcg_kernel_ms": statistics.mean(kern_ms),
             "assemble_ms": statistics.mean(asm_ms), "fallbacks": fallback,
@@ -929,7 +932,8 @@ def run_ours(args, rank, world, local_rank):
 
     # e2e: the best arm through eolc_step with pinned host buffers
     opts = arm_opts(eolc, best, args.degree)
-    ctx.set_learned_refresh(arm_refresh(best))
+    ctx.set_learned_refresh(arm_refresh(best)[0])
+    ctx.set_coarse_refresh(arm_refresh(best)[1])
     xh = torch.empty(3 * sc["n"], dtype=torch.float64).pin_memory().numpy()
     vh = torch.empty(3 * sc["n"], dtype=torch.float64).pin_memory().numpy()
     Xh = torch.empty(2 * sc["n"], dtype=torch.float64).pin_memory().numpy()

@@ -564,7 +564,9 @@ layer_tc_kernel(int n, const float *__restrict__ agg, const float *__restrict__ 
     constexpr int kPart2 = kTcM * kH * 2;
     uint8_t *sH = sA + tc::kSplit * kPart2;
 #pragma unroll
-    for (int k = 0; k < 32; ++k) tc::put3(sA, kPart2, row, c0 + k, kH, i < n ? v[k] : 0.f);
+    for (int k = 0; k < 32; k += 4)
+      tc::put3x4(sA, kPart2, row, c0 + k, kH, i < n ? v[k] : 0.f, i < n ? v[k + 1] : 0.f,
+                 i < n ? v[k + 2] : 0.f, i < n ? v[k + 3] : 0.f);
     for (int q = threadIdx.x; q < kHeadN * kH; q += kTcThreads) {
       const int k = q / kHeadN, c = q % kHeadN;
       float w = 0.f;

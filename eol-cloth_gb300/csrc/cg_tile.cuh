@@ -28,13 +28,17 @@ namespace {
 // since the last true-residual recomputation (convergence is only ever
 // declared on a recomputed residual).  kDelta: one recomputation per decade,
 // the best for the long Jacobi iterations (at 1e-2 the FP32 recurrence
-// drifts enough to cost them ~7% more iterations at 256^2); kDeltaTwoLevel:
-// one per two decades for the two-level preconditioners, whose ~115
-// iterations make the FP64 recomputation (an FP64 product, about 1/64 of the
-// FP32 rate on this GPU) a large share of the solve — still below
-// sqrt(FP32 epsilon) of drift between updates, and the same iteration count.
+// drifts enough to cost them ~7% more iterations at 256^2).  The two-level
+// kernels' ~115-200 iterations make the FP64 recomputation (an FP64 product,
+// about 1/64 of the FP32 rate on this GPU) a large share of the solve:
+// kDeltaPatch, one per three decades for the patch-Chebyshev method (the
+// same iteration count, 2% faster than one per two decades at 256^2);
+// kDeltaLearned, one per two decades for the learned G, whose recurrence
+// drifts further (one per three decades left solves unconverged at twice
+// Jacobi's iteration count).
 constexpr double kDelta = 0.1;
-constexpr double kDeltaTwoLevel = 0.01;
+constexpr double kDeltaPatch = 1e-3;
+constexpr double kDeltaLearned = 1e-2;
 
 // THREADS threads per CTA, ROWT threads per block row, VALKB KiB of staged
 // values + local columns, WINF window nodes per tile in FP32 (3/4 of it in

@@ -1176,7 +1176,7 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
   __syncthreads();  // ds is reused by the local solves
 
   const V tol2 = A::from_d(P.tol2 * __ldcg(&P.st->rhs_norm2));
-  const V delta2 = A::from_d(kDeltaTwoLevel * kDeltaTwoLevel);
+  const V delta2 = A::from_d(kDeltaPatch * kDeltaPatch);
   const int N = P.n_nodes;
   const int hj = i < nh ? sm.hnode[i] : -1;
   if (i == 0) s_fail = 0;
@@ -1407,7 +1407,7 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
     }
   };
   const V tol2 = A::from_d(P.tol2 * __ldcg(&P.st->rhs_norm2));
-  const V delta2 = A::from_d(kDeltaTwoLevel * kDeltaTwoLevel);
+  const V delta2 = A::from_d(kDeltaLearned * kDeltaLearned);
   unsigned epoch = 0;
   int cur = 0;
   __syncthreads();  // the resident image is complete

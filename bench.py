@@ -923,9 +923,16 @@ def run_ours(args, rank, world, local_rank):
             ctx.state_upload(x_w, sc["X"], v_w)
             ctx.step_resident(1, mat, GRAV, H, sc["fixed"], sc["fixed_vel"],
                               arm_opts(eolc, arm, args.degree))
-        results = {arm: time_arm(ctx, sc, mat, arm_opts(eolc, arm, args.degree), x_w, v_w,
-                                 args.steps, stream, flush, world, dev, arm_refresh(arm))
-                   for arm in arms}
+        results, failed = {}, {}
+        for arm in arms:
+            try:
+                results[arm] = time_arm(ctx, sc, mat, arm_opts(eolc, arm, args.degree), x_w,
+                                        v_w, args.steps, stream, flush, world, dev,
+                                        arm_refresh(arm))
+            except Exception as e:  # a failed arm is reported, the others still run
+                failed[arm] = "%s: %s" % (type(e).__name__, str(e)[:200])
+                ctx.set_learned_refresh(1)
+                ctx.set_coarse_refresh(1)
     best = max(results, key=lambda a: results[a]["steps_per_s"])
     res = results[best]
     value = res["steps_per_s"]
@@ -1027,6 +1034,7 @@ def run_ours(args, rank, world, local_rank):
                                " 852481 blocks, 2 corners pinned, rel-res 1e-8 (FP64)",
                    "solver": "%s-PCG (fastest arm)" % best,
                    "arms": arms_out,
+                   "failed_arms": failed,
                    "learned_vs_jacobi_steps_ratio": {
                        a: results[a]["steps_per_s"] / results["jacobi"]["steps_per_s"]
                        for a in results if a.startswith("learned") and "jacobi" in results},

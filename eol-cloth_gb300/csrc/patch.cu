@@ -1176,14 +1176,17 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
   __syncthreads();  // ds is reused by the local solves
 
   const V tol2 = A::from_d(P.tol2 * __ldcg(&P.st->rhs_norm2));
-  const V delta2 = A::from_d(kDeltaPatch * kDeltaPatch);
+  // coarse correction: A_c^-1 rows of this aggregate, then e for r_0
+  const bool coarse = P.n_agg > 0;
+  // one reliable update per three decades with the coarse correction, per
+  // two without it (the one-level method's ~290 iterations drift further)
+  const V delta2 = coarse ? A::from_d(kDeltaPatch * kDeltaPatch)
+                          : A::from_d(kDeltaLearned * kDeltaLearned);
   const int N = P.n_nodes;
   const int hj = i < nh ? sm.hnode[i] : -1;
   if (i == 0) s_fail = 0;
   unsigned epoch = 0;
   V4<float> s{}, w{}, u{};
-  // coarse correction: A_c^-1 rows of this aggregate, then e for r_0
-  const bool coarse = P.n_agg > 0;
   float *cs = reinterpret_cast<float *>(sm.slot);  // every CTA's coarse partials
   if (i < 9) s_g[i] = 0.f;
   if (coarse)

@@ -445,7 +445,9 @@ eolc_status eolc_step_contacts(eolc_ctx *ctx, double *x_h, const double *X_h,
  * symmetric positive definite approximate inverse
  *   G = F (Lambda + sum_e [U_e; V_e][U_e; V_e]^T) F
  * (F: free-DOF mask, Lambda: positive scaled Jacobi, one rank-3 PSD term per
- * stencil edge), applied inside PCG (EOLC_PC_LEARNED).  Trained on the GPU by
+ * stencil edge), applied inside PCG (EOLC_PC_LEARNED).  Inference runs the
+ * dense layers on the tensor cores (tcgen05.mma, FP32 activations as three
+ * BF16 terms); the resident solve streams G in BF16.  Trained on the GPU by
  * the library's own forward/backward kernels on systems the simulator
  * produces, minimising sum_k |F (G A w_k - w_k)|^2 / |F w_k|^2 over probe
  * vectors w_k.  The reference has no preconditioner beyond Eigen's default
@@ -473,7 +475,8 @@ eolc_status eolc_lpc_add_system(eolc_lpc *lpc, eolc_ctx *ctx,
 int eolc_lpc_num_systems(const eolc_lpc *lpc);
 /* The approximate inverse G (n_blocks x 9 FP32 values, the BSR pattern of
  * MDK) the network produces for the context's current FP32 MDK with the
- * given pinned DOFs: the blocks EOLC_PC_LEARNED applies. */
+ * given pinned DOFs: the blocks EOLC_PC_LEARNED applies (the resident
+ * solver applies them rounded to BF16). */
 eolc_status eolc_lpc_blocks(eolc_lpc *lpc, eolc_ctx *ctx, const int *fixed_dofs_h,
                             int n_fixed, float *G_h);
 eolc_status eolc_lpc_clear_systems(eolc_lpc *lpc);

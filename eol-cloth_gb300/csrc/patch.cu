@@ -201,13 +201,25 @@ __device__ void load_patch(const ResParams &P, const ResSmem &sm, int cta, int p
                            RowMeta &M) {
   const int i = threadIdx.x, warp = i >> 5;
   const int f0 = P.fptr[cta], nrec = P.fptr[cta + 1] - f0;
-  for (int q = i; q < nrec; q += kRThreads) {
-    float v[9];
-    sym_block(P.A, P.tr, P.fblk[f0 + q], v);
-    float4 *rec = sm.fval + size_t(q) * 3;
-    rec[0] = make_float4(__uint_as_float(P.fword[f0 + q]), v[0], v[1], v[2]);
-    rec[1] = make_float4(v[3], v[4], v[5], v[6]);
-    rec[2] = make_float4(v[7], v[8], 0.f, 0.f);
+  // two records per pass, their index and value loads issued together
+  for (int q0 = i; q0 < nrec; q0 += 2 * kRThreads) {
+    const int q1 = q0 + kRThreads;
+    const bool has1 = q1 < nrec;
+    const int k0 = __ldg(P.fblk + f0 + q0), k1 = has1 ? __ldg(P.fblk + f0 + q1) : k0;
+    const unsigned w0 = __ldg(P.fword + f0 + q0), w1 = has1 ? __ldg(P.fword + f0 + q1) : 0u;
+    float v0[9], v1[9];
+    sym_block(P.A, P.tr, k0, v0);
+    sym_block(P.A, P.tr, k1, v1);
+    float4 *rec = sm.fval + size_t(q0) * 3;
+    rec[0] = make_float4(__uint_as_float(w0), v0[0], v0[1], v0[2]);
+    rec[1] = make_float4(v0[3], v0[4], v0[5], v0[6]);
+    rec[2] = make_float4(v0[7], v0[8], 0.f, 0.f);
+    if (has1) {
+      rec = sm.fval + size_t(q1) * 3;
+      rec[0] = make_float4(__uint_as_float(w1), v1[0], v1[1], v1[2]);
+      rec[1] = make_float4(v1[3], v1[4], v1[5], v1[6]);
+      rec[2] = make_float4(v1[7], v1[8], 0.f, 0.f);
+    }
   }
   M.fi = M.ft = M.tc = 0;
   M.bnd = false;

@@ -293,6 +293,76 @@ __device__ __forceinline__ float3 spmv(const ResSmem &sm, const RowMeta &M, cons
   return make_float3(a0, a1, a2);
 }
 
+// The same product in two passes around the halo exchange, with the same
+// per-row sums in the same order, so the neighbours' publication of u lands
+// while the patch-internal part runs (the halo poll follows it: 3-4% off the
+// two-level iterations at 256^2).  spmv_internal: the diagonal block and the
+// patch-internal forward records (which also scatter their transposed
+// products to the slots), needing only the patch part of x.
+// spmv_halo_slots, after a CTA barrier that follows the halo values' arrival:
+// the halo records (they scatter nothing), then the row's slots.
+__device__ __forceinline__ float3 spmv_internal(const ResSmem &sm, const RowMeta &M,
+                                                const float4 *x, float4 xo) {
+  const unsigned lt = (1u << (threadIdx.x & 31)) - 1u;
+  float a0 = M.d[0] * xo.x + M.d[1] * xo.y + M.d[2] * xo.z;
+  float a1 = M.d[1] * xo.x + M.d[3] * xo.y + M.d[4] * xo.z;
+  float a2 = M.d[2] * xo.x + M.d[4] * xo.y + M.d[5] * xo.z;
+  const int kmax = __reduce_max_sync(0xffffffffu, M.fi);
+  int base = M.fbase;
+#pragma unroll 2
+  for (int k = 0; k < kmax; ++k) {
+    const unsigned act = __ballot_sync(0xffffffffu, k < M.ft);
+    if (k < M.fi) {
+      const int e = base + __popc(act & lt);
+      const float4 q0 = sm.fval[3 * e], q1 = sm.fval[3 * e + 1], q2 = sm.fval[3 * e + 2];
+      const unsigned w = __float_as_uint(q0.x);
+      const float4 xv = x[w & 0xffffu];
+      a0 += q0.y * xv.x + q0.z * xv.y + q0.w * xv.z;
+      a1 += q1.x * xv.x + q1.y * xv.y + q1.z * xv.z;
+      a2 += q1.w * xv.x + q2.x * xv.y + q2.y * xv.z;
+      const unsigned sl = w >> 16;
+      if (sl != 0xffffu)
+        sm.slot[sl] = make_float4(q0.y * xo.x + q1.x * xo.y + q1.w * xo.z,
+                                  q0.z * xo.x + q1.y * xo.y + q2.x * xo.z,
+                                  q0.w * xo.x + q1.z * xo.y + q2.y * xo.z, 0.f);
+    }
+    base += __popc(act);
+  }
+  return make_float3(a0, a1, a2);
+}
+__device__ __forceinline__ float3 spmv_halo_slots(const ResSmem &sm, const RowMeta &M,
+                                                  const float4 *x, float3 acc) {
+  const unsigned lt = (1u << (threadIdx.x & 31)) - 1u;
+  float a0 = acc.x, a1 = acc.y, a2 = acc.z;
+  const int kmax = __reduce_max_sync(0xffffffffu, M.ft);
+  int base = M.fbase;
+#pragma unroll 2
+  for (int k = 0; k < kmax; ++k) {
+    const unsigned act = __ballot_sync(0xffffffffu, k < M.ft);
+    if (k >= M.fi && k < M.ft) {
+      const int e = base + __popc(act & lt);
+      const float4 q0 = sm.fval[3 * e], q1 = sm.fval[3 * e + 1], q2 = sm.fval[3 * e + 2];
+      const float4 xv = x[__float_as_uint(q0.x) & 0xffffu];
+      a0 += q0.y * xv.x + q0.z * xv.y + q0.w * xv.z;
+      a1 += q1.x * xv.x + q1.y * xv.y + q1.z * xv.z;
+      a2 += q1.w * xv.x + q2.x * xv.y + q2.y * xv.z;
+    }
+    base += __popc(act);
+  }
+  const int tmax = __reduce_max_sync(0xffffffffu, M.tc);
+  int sb = M.sbase;
+#pragma unroll 2
+  for (int k = 0; k < tmax; ++k) {
+    const unsigned act = __ballot_sync(0xffffffffu, k < M.tc);
+    if (k < M.tc) {
+      const float4 c = sm.slot[sb + __popc(act & lt)];
+      a0 += c.x; a1 += c.y; a2 += c.z;
+    }
+    sb += __popc(act);
+  }
+  return make_float3(a0, a1, a2);
+}
+
 __device__ __forceinline__ V4<double> true_residual(const ResParams &P, int row,
                                                    const V4<float> &m) {
   double a0 = 0.0, a1 = 0.0, a2 = 0.0;
@@ -1232,16 +1302,18 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
       sm.xs[i] = f4(u);                                                      \
       if (M.bnd) publish_tagged(P.tw, N, row, tag_, u);                      \
     }                                                                        \
+    __syncthreads();                                                         \
+    const float3 ti_ = spmv_internal(sm, M, sm.xs, f4(u));                   \
     if (hj >= 0) {                                                           \
       V4<float> uj{};                                                        \
-      if (!poll_tagged(P.tw, N, hj, tag_, uj, P.spin_limit)) {                             \
+      if (!poll_tagged(P.tw, N, hj, tag_, uj, P.spin_limit)) {               \
         atomicCAS(&P.st->status, EOLC_OK, EOLC_TIMEOUT);                     \
         s_fail = 1;                                                          \
       }                                                                      \
       sm.xh[i] = f4(uj);                                                     \
     }                                                                        \
     __syncthreads();                                                         \
-    const float3 t_ = spmv<true>(sm, M, sm.xs, f4(u));                       \
+    const float3 t_ = spmv_halo_slots(sm, M, sm.xs, ti_);                    \
     if (own) {                                                               \
       w = V4<float>{t_.x * m.x, t_.y * m.y, t_.z * m.z, 0.f};                \
       g = A::addf(g, dot3(r, u));                                            \
@@ -1455,28 +1527,28 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
 #define EOLC_LPC_UW(c, g, d, q)                                            \
   do {                                                                     \
     __syncthreads();                                                       \
+    epoch += 1u;                                                           \
+    const unsigned tag_ = exch_tag(P.seq, epoch);                          \
     if (own) {                                                             \
       const V4<float> g_ = apply_G(P, sm, cta);                            \
       u = V4<float>{(g_.x + ce[0]) * m.x, (g_.y + ce[1]) * m.y,            \
                     (g_.z + ce[2]) * m.z, 0.f};                            \
+      if (M.bnd) publish_tagged(P.tw, N, row, tag_, u); /* pre-barrier */  \
     }                                                                      \
     __syncthreads();                                                       \
-    epoch += 1u;                                                           \
-    const unsigned tag_ = exch_tag(P.seq, epoch);                          \
-    if (own) {                                                             \
-      sm.xs[i] = f4(u);                                                    \
-      if (M.bnd) publish_tagged(P.tw, N, row, tag_, u);                    \
-    }                                                                      \
+    if (own) sm.xs[i] = f4(u);                                             \
+    __syncthreads();                                                       \
+    const float3 ti_ = spmv_internal(sm, M, sm.xs, f4(u));                 \
     if (hj >= 0) {                                                         \
       V4<float> uj{};                                                      \
-      if (!poll_tagged(P.tw, N, hj, tag_, uj, P.spin_limit)) {                           \
+      if (!poll_tagged(P.tw, N, hj, tag_, uj, P.spin_limit)) {             \
         atomicCAS(&P.st->status, EOLC_OK, EOLC_TIMEOUT);                   \
         s_fail = 1;                                                        \
       }                                                                    \
       sm.xh[i] = f4(uj);                                                   \
     }                                                                      \
     __syncthreads();                                                       \
-    const float3 t_ = spmv<true>(sm, M, sm.xs, f4(u));                     \
+    const float3 t_ = spmv_halo_slots(sm, M, sm.xs, ti_);                  \
     if (own) {                                                             \
       w = V4<float>{t_.x * m.x, t_.y * m.y, t_.z * m.z, 0.f};              \
       P.w[c][row] = w;                                                     \

@@ -1434,7 +1434,30 @@ __global__ void __launch_bounds__(kRThreads, 1) patch_resident_kernel(ResParams 
 // One grid barrier and one neighbour exchange per iteration.  G is read from
 // global memory (L2); A is the resident image.
 
-__device__ __forceinline__ V4<float> apply_G(const ResParams &P, const ResSmem &sm, int cta) {
+// The first kGPre slots of this lane's G slice, loaded ahead: G is constant
+// during the solve, so these loads are issued before the CTA barrier that
+// precedes the product and their L2 round trip overlaps the barrier.
+constexpr int kGPre = 1;
+struct GPre {
+  uint4 a[kGPre];
+  uint32_t b[kGPre];
+};
+__device__ __forceinline__ void g_prefetch(const ResParams &P, int cta, GPre &g) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sl = cta * (kRThreads / 32) + warp;
+  const int off = P.slice_off[sl], len = P.slice_len[sl];
+  const uint4 *GA = reinterpret_cast<const uint4 *>(P.Gs);
+  const uint32_t *GB = reinterpret_cast<const uint32_t *>(GA + P.g_lanes);
+#pragma unroll
+  for (int k = 0; k < kGPre; ++k) {
+    const size_t q = size_t(off + k) * 32 + lane;
+    g.a[k] = k < len ? __ldg(GA + q) : make_uint4(0u, 0u, 0u, 0u);
+    g.b[k] = k < len ? __ldg(GB + q) : 0u;
+  }
+}
+
+__device__ __forceinline__ V4<float> apply_G(const ResParams &P, const ResSmem &sm, int cta,
+                                             const GPre &g) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int sl = cta * (kRThreads / 32) + warp;
   const int off = P.slice_off[sl], len = P.slice_len[sl];
@@ -1443,16 +1466,20 @@ __device__ __forceinline__ V4<float> apply_G(const ResParams &P, const ResSmem &
   const uint32_t *GB = reinterpret_cast<const uint32_t *>(GA + P.g_lanes);
   const auto lo = [](uint32_t w) { return __uint_as_float(w << 16); };
   const auto hi = [](uint32_t w) { return __uint_as_float(w & 0xffff0000u); };
-#pragma unroll 3
-  for (int k = 0; k < len; ++k) {
-    const size_t q = size_t(off + k) * 32 + lane;
-    const uint4 ga = __ldg(GA + q);
-    const uint32_t gb = __ldg(GB + q);
+  const auto block = [&](const uint4 &ga, uint32_t gb) {
     const int m = int(int16_t(gb >> 16));
     const float4 x = m >= 0 ? sm.xs[m] : sm.xh[-1 - m];
     a0 += lo(ga.x) * x.x + hi(ga.x) * x.y + lo(ga.y) * x.z;
     a1 += hi(ga.y) * x.x + lo(ga.z) * x.y + hi(ga.z) * x.z;
     a2 += lo(ga.w) * x.x + hi(ga.w) * x.y + lo(gb) * x.z;
+  };
+#pragma unroll
+  for (int k = 0; k < kGPre; ++k)
+    if (k < len) block(g.a[k], g.b[k]);
+#pragma unroll 3
+  for (int k = kGPre; k < len; ++k) {
+    const size_t q = size_t(off + k) * 32 + lane;
+    block(__ldg(GA + q), __ldg(GB + q));
   }
   return V4<float>{a0, a1, a2, 0.f};
 }
@@ -1526,11 +1553,13 @@ __global__ void __launch_bounds__(kRThreads, 1) learned_resident_kernel(ResParam
   // published to w[c]; then the dots of this step
 #define EOLC_LPC_UW(c, g, d, q)                                            \
   do {                                                                     \
+    GPre gp_;                                                              \
+    if (own) g_prefetch(P, cta, gp_);                                      \
     __syncthreads();                                                       \
     epoch += 1u;                                                           \
     const unsigned tag_ = exch_tag(P.seq, epoch);                          \
     if (own) {                                                             \
-      const V4<float> g_ = apply_G(P, sm, cta);                            \
+      const V4<float> g_ = apply_G(P, sm, cta, gp_);                       \
       u = V4<float>{(g_.x + ce[0]) * m.x, (g_.y + ce[1]) * m.y,            \
                     (g_.z + ce[2]) * m.z, 0.f};                            \
       if (M.bnd) publish_tagged(P.tw, N, row, tag_, u); /* pre-barrier */  \

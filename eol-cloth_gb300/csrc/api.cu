@@ -60,6 +60,20 @@ __global__ void integrate_kernel(int n, double h, const double *v, double *x) {
   if (i < n) x[i] = x[i] + h * v[i];
 }
 
+// Cloth.cpp:394-410 on a topology with EOL nodes: x += h v on the n_real
+// mesh nodes, and u += h vE for EOL node k (Eulerian velocity at block row
+// n_real + k, DOFs 0 and 1).
+__global__ void integrate_eol_kernel(int n_real, int n_eol, const int *__restrict__ eol_node,
+                                     double h, const double *__restrict__ v, double *__restrict__ x,
+                                     double *__restrict__ u) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < 3 * n_real) x[i] = x[i] + h * v[i];
+  if (i < n_eol) {
+    const int a = eol_node[i];
+    for (int j = 0; j < 2; ++j) u[2 * a + j] = u[2 * a + j] + h * v[3 * (n_real + i) + j];
+  }
+}
+
 eolc_status need_topology(eolc_ctx *ctx) {
   if (!ctx) return EOLC_BAD_ARG;
   if (!ctx->has_topology) return fail(ctx, EOLC_NO_TOPOLOGY, "no topology set");
@@ -1133,6 +1147,55 @@ eolc_status eolc_step_contacts(eolc_ctx *ctx, double *x_h, const double *X_h, do
   integrate_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, h, ctx->v.p, ctx->x.p);
   ctx->launches += 1;
   return eolc_state_download(ctx, x_h, v_h);
+}
+
+eolc_status eolc_step_eol(eolc_ctx *ctx, double *x_h, double *u_h, double *v_h,
+                          const eolc_material *mat, const double grav[3], double h,
+                          const int *fixed_dofs_h, const double *fixed_vel_h, int n_fixed,
+                          const eolc_rows *eq, const eolc_rows *ineq,
+                          const eolc_solve_opts *opts, eolc_ineq_info *info) {
+  eolc_status st = need_topology(ctx);
+  if (st != EOLC_OK) return st;
+  if ((st = check_opts(ctx, opts)) != EOLC_OK) return st;
+  if (!x_h || !u_h || !v_h || !mat || !grav) return fail(ctx, EOLC_BAD_ARG, "null state");
+  if (n_fixed > 0 && (!fixed_dofs_h || !fixed_vel_h)) return fail(ctx, EOLC_BAD_ARG, "null fixed list");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = stream_of(ctx);
+  const DevTopology &T = ctx->topo;
+  const int n = 3 * T.n_nodes;
+  if ((st = ensure_state(ctx)) != EOLC_OK) return st;
+  if ((st = upload_positions(ctx, x_h, u_h, s)) != EOLC_OK) return st;
+  EOLC_CHECK_CUDA(ctx, ctx->v.upload(v_h, n, s));
+  // pins from the current velocity (Constraints.cpp:472-496)
+  if ((st = set_pins(ctx, fixed_dofs_h, fixed_vel_h, n_fixed, s)) != EOLC_OK) return st;
+  EOLC_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->beq_full.p, 0, sizeof(double) * n, s));
+  if (n_fixed > 0) {
+    pins_kernel<<<(n_fixed + 127) / 128, 128, 0, s>>>(n_fixed, ctx->fixed_dofs.p, ctx->fixed_vel.p,
+                                                     ctx->v.p, ctx->beq_full.p);
+    ctx->launches += 1;
+  }
+  // Forces::fill with the EOL branches and b = -(M v + h f) (Cloth.cpp:345)
+  if ((st = assemble(ctx, *mat, grav, h, opts->precision, false, true, s)) != EOLC_OK) return st;
+  ctx->last_precision = opts->precision;
+  // the QP with the rows of Constraints::fill
+  const QpRows none{0, nullptr, nullptr, nullptr, nullptr};
+  const QpRows qe = eq ? QpRows{eq->n_rows, eq->ptr, eq->col, eq->val, eq->rhs} : none;
+  const QpRows qi = ineq ? QpRows{ineq->n_rows, ineq->ptr, ineq->col, ineq->val, ineq->rhs} : none;
+  st = qp_solve_device(ctx, qe, qi, opts, nullptr, nullptr, info);
+  if (st != EOLC_OK) return st;
+  const int items = std::max(3 * T.n_real, T.n_eol);
+  integrate_eol_kernel<<<(items + 255) / 256, 256, 0, s>>>(
+      T.n_real, T.n_eol, T.n_eol > 0 ? T.eol_node.p : nullptr, h, ctx->v.p, ctx->x.p, ctx->X.p);
+  ctx->launches += 1;
+  EOLC_CHECK_CUDA(ctx, cudaGetLastError());
+  EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(x_h, ctx->x.p, sizeof(double) * 3 * T.n_real,
+                                       cudaMemcpyDeviceToHost, s));
+  EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(u_h, ctx->X.p, sizeof(double) * 2 * T.n_real,
+                                       cudaMemcpyDeviceToHost, s));
+  EOLC_CHECK_CUDA(ctx, cudaMemcpyAsync(v_h, ctx->v.p, sizeof(double) * n,
+                                       cudaMemcpyDeviceToHost, s));
+  EOLC_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
+  return EOLC_OK;
 }
 
 eolc_status eolc_clear_contact_multipliers(eolc_ctx *ctx) {

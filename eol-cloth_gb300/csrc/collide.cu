@@ -858,7 +858,6 @@ extern "C" eolc_status eolc_cd2(eolc_ctx *ctx, const double *x_h,
                                 eolc_contact *out_h, int capacity, int *n_out) {
   if (!ctx) return EOLC_BAD_ARG;
   if (!ctx->has_topology) { ctx->err = "no topology set"; return EOLC_NO_TOPOLOGY; }
-  if (refuse_eol(ctx) != EOLC_OK) return EOLC_BAD_ARG;
   if (!x_h || n_boxes < 0 || n_points < 0 || capacity < 0 || !n_out ||
       (n_boxes > 0 && !boxes) || (n_points > 0 && (!points_h || !normals_h)) ||
       (capacity > 0 && !out_h)) {
@@ -868,7 +867,9 @@ extern "C" eolc_status eolc_cd2(eolc_ctx *ctx, const double *x_h,
   if (1 + 3 * n_boxes > kMaxSegs) { ctx->err = "too many boxes"; return EOLC_BAD_ARG; }
   cudaSetDevice(ctx->device);
   cudaStream_t s = ctx->stream;
-  const int N = ctx->topo.n_nodes, F = ctx->topo.n_tri;
+  // the mesh nodes (a topology with EOL nodes adds Eulerian block rows,
+  // which CD2 does not see: Collisions.cpp:55-78 packs the mesh nodes)
+  const int N = ctx->topo.n_real, F = ctx->topo.n_tri;
   if (!ctx->cd_work) ctx->cd_work = new CollideWork();
   CollideWork &W = *ctx->cd_work;
 #define CK(expr)                                                        \

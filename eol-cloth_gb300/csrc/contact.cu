@@ -6,14 +6,18 @@
 //
 // with the inequality rows of Constraints::fill (Constraints.cpp:422-468 for
 // the CD2 contacts of a non-EOL mesh: one row per contact over one to three
-// cloth nodes).
+// cloth nodes), and, for EOL meshes, its general equality rows E v = e
+// (Constraints.cpp:147-415: the EOL nodes' rows on their Lagrangian and
+// Eulerian DOFs).
 //
 // Method: augmented Lagrangian (method of multipliers) on the inequality
 // rows, each augmented-Lagrangian minimisation by semismooth Newton:
 //   W = { i : lam_i + rho_i (C v - d)_i > 0 }
 //   (MDK + sum_{i in W} rho_i c_i c_i') v = -(b + sum_{i in W} c_i (lam_i - rho_i d_i))
 // repeated until W stops changing, then lam <- max(0, lam + rho (C v - d)),
-// until max_i |lam_new - lam|_i / rho_i <= 10 rel_tol max|v|.  At every
+// until max_i |lam_new - lam|_i / rho_i <= 10 rel_tol max|v|.  Equality rows
+// are the same terms with every row always in W and lam <- lam + rho (E v - e)
+// unclamped (the method of multipliers for equalities).  At every
 // augmented-Lagrangian minimiser MDK v + b + C' lam_new = 0 holds (to the
 // linear solve's tolerance), so the stopping test bounds the remaining
 // infeasibility and complementarity.  rho_i = 100 x (mean diagonal of MDK over
@@ -57,27 +61,30 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long *p, double 
   atomicMax(p, static_cast<unsigned long long>(__double_as_longlong(x)));
 }
 
-// rho_i from the diagonal blocks of the row's nodes (unpenalised MDK).
+// rho_i from the diagonal blocks of the row's nodes (unpenalised MDK): the
+// mean diagonal entry over the row's DOFs.  An Eulerian node (block row >=
+// n_real) has two DOFs; its padded third diagonal entry (1) is left out.
 template <typename T>
-__global__ void ineq_setup_kernel(int m, const int *__restrict__ rnode,
+__global__ void ineq_setup_kernel(int m, int n_real, const int *__restrict__ rnode,
                                   const double *__restrict__ rg, const int *__restrict__ diag,
                                   const T *__restrict__ A, double *__restrict__ rho) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
   double tr = 0, g2 = 0;
-  int cnt = 0;
+  int ndof = 0;
   for (int p = 0; p < kRowNodes; ++p) {
     const int a = rnode[kRowNodes * i + p];
     if (a < 0) continue;
     const T *blk = A + size_t(diag[a]) * 9;
-    tr += double(blk[0]) + double(blk[4]) + double(blk[8]);
+    const bool eul = a >= n_real;
+    tr += eul ? double(blk[0]) + double(blk[4]) : double(blk[0]) + double(blk[4]) + double(blk[8]);
     for (int c = 0; c < 3; ++c) {
       const double g = rg[(kRowNodes * i + p) * 3 + c];
       g2 += g * g;
     }
-    ++cnt;
+    ndof += eul ? 2 : 3;
   }
-  rho[i] = cnt > 0 && g2 > 0 ? kKappa * (tr / (3.0 * cnt)) / g2 : 0.0;
+  rho[i] = ndof > 0 && g2 > 0 ? kKappa * (tr / double(ndof)) / g2 : 0.0;
 }
 
 // max |v| over the 3N DOFs; a non-finite entry makes it +inf (fmax alone
@@ -93,8 +100,9 @@ __global__ void absmax_kernel(int n, const double *__restrict__ v, unsigned long
 // Per row: r = C_i v - d_i.  update = 1: lam <- max(0, lam + rho r) with the
 // largest |change| / rho, violation and active count recorded.  Then the
 // active flag for the next solve, lam + rho r > 0, and the count of flags
-// that changed.
-__global__ void ineq_eval_kernel(int m, const int *__restrict__ rnode,
+// that changed.  Rows below m_eq are equalities: lam <- lam + rho r, |r| is
+// their violation, and they are always active.
+__global__ void ineq_eval_kernel(int m, int m_eq, const int *__restrict__ rnode,
                                  const double *__restrict__ rg, const double *__restrict__ v,
                                  const double *__restrict__ rho, const double *__restrict__ d,
                                  double *__restrict__ lam, uint8_t *__restrict__ act,
@@ -112,15 +120,16 @@ __global__ void ineq_eval_kernel(int m, const int *__restrict__ rnode,
   cv[i] = s;
   const double r = s - d[i], ri = rho[i];
   double l = lam[i];
+  const bool eq = i < m_eq;
   if (update) {
-    const double ln = fmax(0.0, l + ri * r);
+    const double ln = eq ? l + ri * r : fmax(0.0, l + ri * r);
     if (ri > 0) atomic_max_nonneg(stat + kStatDlam, fabs(ln - l) / ri);
-    atomic_max_nonneg(stat + kStatViol, fmax(0.0, r));
-    if (ln > 0) atomicAdd(stat + kStatActive, 1ull);
+    atomic_max_nonneg(stat + kStatViol, eq ? fabs(r) : fmax(0.0, r));
+    if (!eq && ln > 0) atomicAdd(stat + kStatActive, 1ull);
     lam[i] = ln;
     l = ln;
   }
-  const uint8_t na = ri > 0 && l + ri * r > 0;
+  const uint8_t na = ri > 0 && (eq || l + ri * r > 0);
   if (na != act[i]) {
     atomicAdd(stat + kStatChanges, 1ull);
     act[i] = na;
@@ -308,39 +317,51 @@ namespace eolc {
 
 // The QP on the context's device state: MDK (last assembly), b, the pinned
 // mask and beq_full, v as the initial guess (overwritten with the solution).
-eolc_status ineq_solve_device(eolc_ctx *ctx, int n_ineq, const int *ineq_ptr_h,
-                              const int *ineq_col_h, const double *ineq_val_h,
-                              const double *bineq_h, const eolc_solve_opts *opts,
-                              double *lambda_h, eolc_ineq_info *info,
-                              const double *lambda0_h) {
-  if (n_ineq < 0 || (n_ineq > 0 && (!ineq_ptr_h || !ineq_col_h || !ineq_val_h || !bineq_h)))
+// Rows 0 .. eq.m - 1 of the solve are the equality rows, then the inequality
+// rows; lambda0_h (optional) holds initial inequality multipliers.
+eolc_status qp_solve_device(eolc_ctx *ctx, const QpRows &eq, const QpRows &iq,
+                            const eolc_solve_opts *opts, double *lambda_eq_h,
+                            double *lambda_h, eolc_ineq_info *info,
+                            const double *lambda0_h) {
+  if (eq.m < 0 || (eq.m > 0 && (!eq.ptr || !eq.col || !eq.val || !eq.rhs)))
+    return bad(ctx, "null equality rows");
+  if (iq.m < 0 || (iq.m > 0 && (!iq.ptr || !iq.col || !iq.val || !iq.rhs)))
     return bad(ctx, "null inequality rows");
   const HostTopology *Hp = host_topology(ctx);
   if (!Hp) return EOLC_CUDA_ERROR;
   const HostTopology &H = *Hp;
-  const int N = H.n_nodes, n = 3 * N, m = n_ineq;
+  const int N = H.n_nodes, n = 3 * N, m_eq = eq.m, m = eq.m + iq.m;
+  const int n_real = ctx->topo.n_real;
+  if (eq.m >= (1 << 27) || iq.m >= (1 << 27) || m >= (1 << 27))
+    return bad(ctx, "too many constraint rows");
   // rows grouped by node (first-appearance order), columns checked
   std::vector<int> rnode(size_t(kRowNodes) * std::max(1, m), -1);
   std::vector<double> rg(size_t(kRowNodes) * 3 * std::max(1, m), 0.0);
   std::vector<double> d(std::max(1, m), 0.0);
   for (int i = 0; i < m; ++i) {
-    if (ineq_ptr_h[i + 1] < ineq_ptr_h[i]) return bad(ctx, "inequality row pointers decrease");
+    const bool is_eq = i < m_eq;
+    const QpRows &R = is_eq ? eq : iq;
+    const int r = is_eq ? i : i - m_eq;
+    const char *kind = is_eq ? "equality" : "inequality";
+    if (R.ptr[r + 1] < R.ptr[r]) return bad(ctx, std::string(kind) + " row pointers decrease");
     int cnt = 0;
-    for (int q = ineq_ptr_h[i]; q < ineq_ptr_h[i + 1]; ++q) {
-      const int col = ineq_col_h[q];
-      if (col < 0 || col >= n) return bad(ctx, "inequality column out of range");
-      if (!std::isfinite(ineq_val_h[q])) return bad(ctx, "non-finite inequality coefficient");
+    for (int q = R.ptr[r]; q < R.ptr[r + 1]; ++q) {
+      const int col = R.col[q];
+      if (col < 0 || col >= n) return bad(ctx, std::string(kind) + " column out of range");
+      if (col / 3 >= n_real && col % 3 == 2)
+        return bad(ctx, std::string(kind) + " row on the padded DOF of an Eulerian node");
+      if (!std::isfinite(R.val[q])) return bad(ctx, std::string("non-finite ") + kind + " coefficient");
       const int a = col / 3;
       int p = 0;
       while (p < cnt && rnode[kRowNodes * i + p] != a) ++p;
       if (p == cnt) {
-        if (cnt == kRowNodes) return bad(ctx, "an inequality row touches more than 4 nodes");
+        if (cnt == kRowNodes) return bad(ctx, std::string("an ") + kind + " row touches more than 4 nodes");
         rnode[kRowNodes * i + cnt++] = a;
       }
-      rg[(size_t(kRowNodes) * i + p) * 3 + col % 3] += ineq_val_h[q];
+      rg[(size_t(kRowNodes) * i + p) * 3 + col % 3] += R.val[q];
     }
-    d[i] = bineq_h[i];
-    if (!std::isfinite(d[i])) return bad(ctx, "non-finite bineq");
+    d[i] = R.rhs[r];
+    if (!std::isfinite(d[i])) return bad(ctx, is_eq ? "non-finite beq" : "non-finite bineq");
   }
   // per-block and per-node term lists (blocks of every node pair of a row)
   std::vector<long long> bitems;  // (block << 32) | (row << 4 | pa << 2 | pb)
@@ -355,11 +376,10 @@ eolc_status ineq_solve_device(eolc_ctx *ctx, int n_ineq, const int *ineq_ptr_h,
         if (bn < 0) continue;
         const int blk = find_block(H, a, bn);
         if (blk < 0)
-          return bad(ctx, "an inequality row couples nodes that share no element");
+          return bad(ctx, "a constraint row couples nodes that share no element");
         bitems.push_back((long long)blk << 32 | (i << 4 | pa << 2 | pb));
       }
     }
-  if (m >= (1 << 27)) return bad(ctx, "too many inequality rows");
   std::sort(bitems.begin(), bitems.end());
   std::sort(nitems.begin(), nitems.end());
   std::vector<int> ublk, uptr, uitem, unode, nptr, nitem;
@@ -419,8 +439,9 @@ eolc_status ineq_solve_device(eolc_ctx *ctx, int n_ineq, const int *ineq_ptr_h,
   IQ_CHECK(W.part.resize(size_t(2) * nbr));
   W.part_h.resize(size_t(2) * nbr);
   IQ_CHECK(cudaMemsetAsync(W.lam.p, 0, sizeof(double) * std::max(1, m), s));
-  if (lambda0_h && m > 0)  // warm start: the active set starts from these
-    IQ_CHECK(cudaMemcpyAsync(W.lam.p, lambda0_h, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  if (lambda0_h && iq.m > 0)  // warm start: the active set starts from these
+    IQ_CHECK(cudaMemcpyAsync(W.lam.p + m_eq, lambda0_h, sizeof(double) * iq.m,
+                             cudaMemcpyHostToDevice, s));
   IQ_CHECK(cudaMemsetAsync(W.act.p, 0, std::max(1, m), s));
   IQ_CHECK(cudaMemcpyAsync(W.bpen.p, ctx->b.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
   // the learned network approximates the inverse of MDK, not of the
@@ -437,8 +458,8 @@ eolc_status ineq_solve_device(eolc_ctx *ctx, int n_ineq, const int *ineq_ptr_h,
                              cudaMemcpyDeviceToDevice, s));
     a.A64 = W.A64.p;
     if (m > 0)
-      ineq_setup_kernel<double><<<grid(m), kThreads, 0, s>>>(m, W.rnode.p, W.rg.p, ctx->topo.diag.p,
-                                                             ctx->A64.p, W.rho.p);
+      ineq_setup_kernel<double><<<grid(m), kThreads, 0, s>>>(m, n_real, W.rnode.p, W.rg.p,
+                                                             ctx->topo.diag.p, ctx->A64.p, W.rho.p);
   } else {
     IQ_CHECK(W.A32.resize(nb9 + 16));
     IQ_CHECK(cudaMemcpyAsync(W.A32.p, ctx->A32.p, sizeof(float) * (nb9 + 16),
@@ -446,8 +467,8 @@ eolc_status ineq_solve_device(eolc_ctx *ctx, int n_ineq, const int *ineq_ptr_h,
     a.A32 = W.A32.p;
     a.A64 = nullptr;
     if (m > 0)
-      ineq_setup_kernel<float><<<grid(m), kThreads, 0, s>>>(m, W.rnode.p, W.rg.p, ctx->topo.diag.p,
-                                                            ctx->A32.p, W.rho.p);
+      ineq_setup_kernel<float><<<grid(m), kThreads, 0, s>>>(m, n_real, W.rnode.p, W.rg.p,
+                                                            ctx->topo.diag.p, ctx->A32.p, W.rho.p);
   }
   ctx->launches += m > 0 ? 1 : 0;
   unsigned long long stat_h[kStatWords];
@@ -455,8 +476,9 @@ eolc_status ineq_solve_device(eolc_ctx *ctx, int n_ineq, const int *ineq_ptr_h,
   auto eval = [&](int update) -> eolc_status {
     IQ_CHECK(cudaMemsetAsync(W.stat.p, 0, sizeof(unsigned long long) * kStatWords, s));
     if (m > 0) {
-      ineq_eval_kernel<<<grid(m), kThreads, 0, s>>>(m, W.rnode.p, W.rg.p, ctx->v.p, W.rho.p, W.d.p,
-                                                    W.lam.p, W.act.p, W.cv.p, update, W.stat.p);
+      ineq_eval_kernel<<<grid(m), kThreads, 0, s>>>(m, m_eq, W.rnode.p, W.rg.p, ctx->v.p, W.rho.p,
+                                                    W.d.p, W.lam.p, W.act.p, W.cv.p, update,
+                                                    W.stat.p);
       ++ctx->launches;
     }
     if (update) {
@@ -572,12 +594,26 @@ eolc_status ineq_solve_device(eolc_ctx *ctx, int n_ineq, const int *ineq_ptr_h,
     I.n_active = int(stat_h[kStatActive]);
     converged = as_double(stat_h[kStatDlam]) <= tol * std::max(vmax, 1e-300);
   }
-  if (lambda_h && m > 0)
-    IQ_CHECK(cudaMemcpyAsync(lambda_h, W.lam.p, sizeof(double) * m, cudaMemcpyDeviceToHost, s));
+  if (lambda_eq_h && m_eq > 0)
+    IQ_CHECK(cudaMemcpyAsync(lambda_eq_h, W.lam.p, sizeof(double) * m_eq, cudaMemcpyDeviceToHost,
+                             s));
+  if (lambda_h && iq.m > 0)
+    IQ_CHECK(cudaMemcpyAsync(lambda_h, W.lam.p + m_eq, sizeof(double) * iq.m,
+                             cudaMemcpyDeviceToHost, s));
   IQ_CHECK(cudaStreamSynchronize(s));
   I.status = converged ? EOLC_OK : EOLC_NOT_CONVERGED;
   if (!converged) ctx->err = "multiplier updates did not converge";
   return eolc_status(I.status);
+}
+
+eolc_status ineq_solve_device(eolc_ctx *ctx, int n_ineq, const int *ineq_ptr_h,
+                              const int *ineq_col_h, const double *ineq_val_h,
+                              const double *bineq_h, const eolc_solve_opts *opts,
+                              double *lambda_h, eolc_ineq_info *info,
+                              const double *lambda0_h) {
+  const QpRows none{0, nullptr, nullptr, nullptr, nullptr};
+  const QpRows iq{n_ineq, ineq_ptr_h, ineq_col_h, ineq_val_h, bineq_h};
+  return qp_solve_device(ctx, none, iq, opts, nullptr, lambda_h, info, lambda0_h);
 }
 
 }  // namespace eolc
@@ -606,6 +642,38 @@ extern "C" eolc_status eolc_velocity_solve_ineq(
   IQ_CHECK(ctx->v.upload(v_h, n, s));  // initial guess
   st = ineq_solve_device(ctx, n_ineq, ineq_ptr_h, ineq_col_h, ineq_val_h, bineq_h, opts,
                          lambda_h, info);
+  IQ_CHECK(cudaMemcpyAsync(v_h, ctx->v.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  IQ_CHECK(cudaStreamSynchronize(s));
+  return st;
+}
+
+extern "C" eolc_status eolc_velocity_solve_qp(eolc_ctx *ctx, const double *b_h,
+                                              const int *fixed_dofs_h, const double *beq_h,
+                                              int n_fixed, const eolc_rows *eq,
+                                              const eolc_rows *ineq, const eolc_solve_opts *opts,
+                                              double *v_h, double *lambda_eq_h,
+                                              double *lambda_ineq_h, eolc_ineq_info *info) {
+  if (!ctx) return EOLC_BAD_ARG;
+  if (!ctx->has_topology) {
+    ctx->err = "no topology set";
+    return EOLC_NO_TOPOLOGY;
+  }
+  if (!opts) return bad(ctx, "null solve options");
+  if (!b_h || !v_h || (n_fixed > 0 && !beq_h)) return bad(ctx, "null input");
+  if (ctx->last_precision < 0) return bad(ctx, "no matrix assembled");
+  if (opts->precision != ctx->last_precision)
+    return bad(ctx, "solve precision differs from the assembled matrix");
+  const QpRows qe = eq ? QpRows{eq->n_rows, eq->ptr, eq->col, eq->val, eq->rhs}
+                       : QpRows{0, nullptr, nullptr, nullptr, nullptr};
+  const QpRows qi = ineq ? QpRows{ineq->n_rows, ineq->ptr, ineq->col, ineq->val, ineq->rhs}
+                         : QpRows{0, nullptr, nullptr, nullptr, nullptr};
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = ctx->stream;
+  const int n = 3 * ctx->topo.n_nodes;
+  eolc_status st = prepare_pins_rhs(ctx, b_h, fixed_dofs_h, beq_h, n_fixed, s);
+  if (st != EOLC_OK) return st;
+  IQ_CHECK(ctx->v.upload(v_h, n, s));  // initial guess
+  st = qp_solve_device(ctx, qe, qi, opts, lambda_eq_h, lambda_ineq_h, info);
   IQ_CHECK(cudaMemcpyAsync(v_h, ctx->v.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   IQ_CHECK(cudaStreamSynchronize(s));
   return st;

@@ -255,8 +255,20 @@ PcgArgs default_pcg_args(eolc_ctx *ctx, const eolc_solve_opts *o);
 // The solver dispatch of eolc_velocity_solve on explicit arguments.
 eolc_status solve_with_args(eolc_ctx *ctx, const eolc_solve_opts *o, const PcgArgs &a,
                             eolc_solve_info *info, cudaStream_t s);
-// The contact QP (contact.cu) on the device state: MDK, b, pins, v (initial
-// guess in, solution out); lambda0_h (optional): initial multipliers.
+// General rows of the QP in CSR over the DOFs of the topology's block rows.
+struct QpRows {
+  int m;
+  const int *ptr, *col;
+  const double *val, *rhs;
+};
+// The QP (contact.cu) with equality and inequality rows on the device state:
+// MDK, b, pins, v (initial guess in, solution out); lambda0_h (optional):
+// initial inequality multipliers.
+eolc_status qp_solve_device(eolc_ctx *ctx, const QpRows &eq, const QpRows &iq,
+                            const eolc_solve_opts *opts, double *lambda_eq_h,
+                            double *lambda_h, eolc_ineq_info *info,
+                            const double *lambda0_h = nullptr);
+// The contact QP: qp_solve_device without equality rows.
 eolc_status ineq_solve_device(eolc_ctx *ctx, int n_ineq, const int *ineq_ptr_h,
                               const int *ineq_col_h, const double *ineq_val_h,
                               const double *bineq_h, const eolc_solve_opts *opts,

@@ -102,6 +102,20 @@ _D = ctypes.POINTER(ctypes.c_double)
 _I = ctypes.POINTER(ctypes.c_int)
 _V = ctypes.c_void_p
 
+
+class Rows(ctypes.Structure):
+    """eolc_rows: constraint rows in CSR over the DOFs of the block rows."""
+    _fields_ = [("n_rows", ctypes.c_int), ("capacity", ctypes.c_int), ("ptr", _I),
+                ("col", _I), ("val", _D), ("rhs", _D)]
+
+
+class EolMesh(ctypes.Structure):
+    """eolc_eol_mesh: the mesh state Constraints::fill reads."""
+    _fields_ = [("n_nodes", ctypes.c_int), ("x", _D), ("u", _D), ("tri", _I),
+                ("n_tri", ctypes.c_int), ("edges", _I), ("preserve", _I),
+                ("n_edges", ctypes.c_int), ("eol_nodes", _I), ("corner_id", _I),
+                ("cd_edge", _I), ("n_eol", ctypes.c_int)]
+
 # Every symbol the C ABI exports (include/eolc.h).
 EXPORTS = ["eolc_version", "eolc_launch_count", "eolc_create", "eolc_destroy", "eolc_last_error", "eolc_set_stream",
            "eolc_set_topology", "eolc_bsr_pattern", "eolc_forces_fill", "eolc_velocity_solve",
@@ -118,6 +132,7 @@ EXPORTS = ["eolc_version", "eolc_launch_count", "eolc_create", "eolc_destroy", "
            "eolc_export_obj_text", "eolc_velocity_solve_ineq", "eolc_contact_rows",
            "eolc_step_contacts", "eolc_set_topology_device", "eolc_topology_arrays",
            "eolc_edge_list", "eolc_set_topology_eol", "eolc_clear_contact_multipliers",
+           "eolc_velocity_solve_qp", "eolc_constraint_rows", "eolc_step_eol",
            "eolc_set_wait_limit"]
 
 
@@ -201,6 +216,15 @@ def load_library(path=LIB_PATH):
                                      ctypes.POINTER(SolveOpts), ctypes.POINTER(IneqInfo)]
     L.eolc_contact_rows.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _I, _I, _D, _D,
                                     _I]
+    L.eolc_velocity_solve_qp.argtypes = [_V, _D, _I, _D, ctypes.c_int, ctypes.POINTER(Rows),
+                                         ctypes.POINTER(Rows), ctypes.POINTER(SolveOpts), _D, _D,
+                                         _D, ctypes.POINTER(IneqInfo)]
+    L.eolc_constraint_rows.argtypes = [ctypes.POINTER(EolMesh), ctypes.POINTER(Box),
+                                       ctypes.c_int, _D, ctypes.c_int, ctypes.c_void_p,
+                                       ctypes.c_int, ctypes.POINTER(Rows), ctypes.POINTER(Rows)]
+    L.eolc_step_eol.argtypes = [_V, _D, _D, _D, ctypes.POINTER(Material), _D, ctypes.c_double,
+                                _I, _D, ctypes.c_int, ctypes.POINTER(Rows), ctypes.POINTER(Rows),
+                                ctypes.POINTER(SolveOpts), ctypes.POINTER(IneqInfo)]
     L.eolc_export_obj_text.argtypes = [_V, ctypes.c_int, ctypes.c_double, ctypes.c_char_p,
                                        ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
     for name in EXPORTS:
@@ -373,6 +397,43 @@ class Context:
                                           ctypes.byref(opts), _d(v), _d(lam), ctypes.byref(info))
         self._check(st)
         return v, lam[:m], info
+
+    def velocity_solve_qp(self, b, fixed_dofs, beq, eq=None, ineq=None, opts=None, v0=None):
+        """The QP with equality and inequality rows (eolc_velocity_solve_qp)
+        on the last fill's MDK; eq / ineq are RowSet (or None).  b, v over the
+        block rows' DOFs (the extended layout on an EOL topology).  Returns
+        (v, lambda_eq, lambda_ineq, IneqInfo)."""
+        opts = opts or SolveOpts()
+        b, fixed_dofs, beq = _f64(b), _i32(fixed_dofs), _f64(beq)
+        eq = eq or RowSet.empty()
+        ineq = ineq or RowSet.empty()
+        re, ri = eq.as_c(), ineq.as_c()
+        v = np.zeros(3 * self.n_nodes) if v0 is None else _f64(v0).copy()
+        le, li = np.zeros(max(1, eq.m)), np.zeros(max(1, ineq.m))
+        info = IneqInfo()
+        st = lib.eolc_velocity_solve_qp(self._h, _d(b), _i(fixed_dofs), _d(beq),
+                                        len(fixed_dofs), ctypes.byref(re), ctypes.byref(ri),
+                                        ctypes.byref(opts), _d(v), _d(le), _d(li),
+                                        ctypes.byref(info))
+        self._check(st)
+        return v, le[:eq.m], li[:ineq.m], info
+
+    def step_eol(self, x, u, v, mat, grav, h, fixed_dofs, fixed_vel, eq=None, ineq=None,
+                 opts=None):
+        """Cloth::step of an EOL mesh (eolc_step_eol) with the rows of
+        Constraints::fill (constraint_rows); x (3N), u (2N) and v (extended
+        layout) are updated in place.  Returns the QP's IneqInfo."""
+        opts = opts or SolveOpts()
+        fixed_dofs, fixed_vel = _i32(fixed_dofs), _f64(fixed_vel)
+        eq = eq or RowSet.empty()
+        ineq = ineq or RowSet.empty()
+        re, ri = eq.as_c(), ineq.as_c()
+        info = IneqInfo()
+        st = lib.eolc_step_eol(self._h, _d(x), _d(u), _d(v), ctypes.byref(mat), _d(_f64(grav)), h,
+                               _i(fixed_dofs), _d(fixed_vel), len(fixed_dofs), ctypes.byref(re),
+                               ctypes.byref(ri), ctypes.byref(opts), ctypes.byref(info))
+        self._check(st)
+        return info
 
     def step_contacts(self, x, X, v, mat, grav, h, fixed_dofs, fixed_vel, boxes=(), points=None,
                       normals=None, threshold=1e-3, opts=None):
@@ -702,6 +763,95 @@ def mesh_hinges(tri):
         return pick
 
     return np.stack([e0, e1, other(f0[keep]), other(f1[keep])], 1).astype(np.int32)
+
+
+def mesh_edges(tri):
+    """The edges of a triangle list in ArcSim's mesh.edges order
+    (Mesh::add(Face), mesh.cpp:356-363: each face, in order, creates its
+    missing edges (v[i], v[i+1])): (n_edges, 2) int32 of Edge::n[0], n[1]."""
+    tri = np.asarray(tri, np.int64).reshape(-1, 3)
+    if len(tri) == 0:
+        return np.zeros((0, 2), np.int32)
+    a = tri.ravel()
+    b = tri[:, [1, 2, 0]].ravel()
+    key = np.minimum(a, b) * (int(tri.max()) + 1) + np.maximum(a, b)
+    _, first = np.unique(key, return_index=True)
+    first = np.sort(first)
+    return np.stack([a[first], b[first]], 1).astype(np.int32)
+
+
+class RowSet:
+    """Constraint rows as CSR arrays (ptr, col, val) with right-hand sides."""
+
+    def __init__(self, ptr, col, val, rhs):
+        self.ptr, self.col, self.val, self.rhs = _i32(ptr), _i32(col), _f64(val), _f64(rhs)
+
+    @staticmethod
+    def empty():
+        return RowSet(np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0), np.zeros(0))
+
+    @staticmethod
+    def from_csr(A, rhs):
+        import scipy.sparse as sp
+        A = sp.csr_matrix(A)
+        return RowSet(A.indptr, A.indices, A.data, rhs)
+
+    @property
+    def m(self):
+        return len(self.ptr) - 1
+
+    def csr(self, n_dofs):
+        import scipy.sparse as sp
+        return sp.csr_matrix((self.val, self.col, self.ptr), shape=(self.m, n_dofs))
+
+    def as_c(self):
+        """An eolc_rows view of the arrays (kept alive by this object)."""
+        self._col = self.col if len(self.col) else np.zeros(1, np.int32)
+        self._val = self.val if len(self.val) else np.zeros(1)
+        self._rhs = self.rhs if len(self.rhs) else np.zeros(1)
+        return Rows(self.m, self.m, _i(self.ptr), _i(self._col), _d(self._val), _d(self._rhs))
+
+
+def constraint_rows(x, u, tri, edges, eol_nodes, corner_id, cd_edge, preserve=None, boxes=(),
+                    point_normals=None, contacts=()):
+    """Constraints::fill for an EOL mesh (eolc_constraint_rows, host only):
+    (equality RowSet, inequality RowSet) over the extended layout."""
+    x, u, tri, edges = _f64(x), _f64(u), _i32(tri), _i32(edges)
+    eol, cid, cde = _i32(eol_nodes), _i32(corner_id), _i32(cd_edge)
+    pres = None if preserve is None else _i32(preserve)
+    n = len(x) // 3
+    one = np.zeros(1, np.int32)
+    mesh = EolMesh(n, _d(x), _d(u), _i(tri), len(tri.reshape(-1, 3)),
+                   _i(edges if len(edges) else one), _i(pres) if pres is not None else None,
+                   len(edges.reshape(-1, 2)), _i(eol if len(eol) else one),
+                   _i(cid if len(cid) else one), _i(cde if len(cde) else one), len(eol))
+    boxes = list(boxes)
+    barr = (Box * max(1, len(boxes)))(*boxes)
+    pn = np.zeros(3) if point_normals is None else _f64(point_normals)
+    npts = 0 if point_normals is None else len(pn.reshape(-1, 3))
+    contacts = list(contacts)
+    carr = (Contact * max(1, len(contacts)))(*contacts)
+    cap_e, cap_i = 3 * len(eol) + 1, 3 * len(eol) + len(contacts) + 1
+    while True:
+        bufs = []
+        for cap in (cap_e, cap_i):
+            ptr, col = np.zeros(cap + 1, np.int32), np.zeros(9 * cap, np.int32)
+            val, rhs = np.zeros(9 * cap), np.zeros(cap)
+            bufs.append((Rows(0, cap, _i(ptr), _i(col), _d(val), _d(rhs)), ptr, col, val, rhs))
+        st = lib.eolc_constraint_rows(ctypes.byref(mesh), barr, len(boxes), _d(pn), npts,
+                                      ctypes.cast(carr, ctypes.c_void_p), len(contacts),
+                                      ctypes.byref(bufs[0][0]), ctypes.byref(bufs[1][0]))
+        if st == CAPACITY:
+            cap_e, cap_i = max(cap_e, bufs[0][0].n_rows), max(cap_i, bufs[1][0].n_rows)
+            continue
+        if st != OK:
+            raise EolcError(st, "eolc_constraint_rows: bad arguments")
+        out = []
+        for R, ptr, col, val, rhs in bufs:
+            m = R.n_rows
+            q = int(ptr[m])
+            out.append(RowSet(ptr[:m + 1].copy(), col[:q].copy(), val[:q].copy(), rhs[:m].copy()))
+        return out[0], out[1]
 
 
 def corner_ids(r0, r1):

@@ -170,8 +170,10 @@ eolc_status eolc_set_topology_device(eolc_ctx *ctx, int n_nodes,
  * deformation gradient; a hinge's F is the mean of its two faces') and
  * forces (-F' f on the Eulerian DOFs; a hinge with an EOL vertex also adds
  * its bending force); eolc_velocity_solve takes b, v and the fixed DOFs in
- * the extended layout.  Steps, collisions, export, batches, contact rows and
- * the learned preconditioner refuse EOL topologies (EOLC_BAD_ARG). */
+ * the extended layout; eolc_cd2 runs on the mesh nodes,
+ * eolc_velocity_solve_qp takes the EOL rows of eolc_constraint_rows and
+ * eolc_step_eol steps the mesh.  The other steps, export, batches and the
+ * learned preconditioner refuse EOL topologies (EOLC_BAD_ARG). */
 eolc_status eolc_set_topology_eol(eolc_ctx *ctx, int n_nodes, const int *tri_h,
                                   int n_tri, const int *hinge_h, int n_hinge,
                                   const int *eol_nodes_h, int n_eol);
@@ -250,6 +252,45 @@ eolc_status eolc_velocity_solve_ineq(eolc_ctx *ctx, const double *b_h,
                                      const double *bineq_h,
                                      const eolc_solve_opts *opts, double *v_h,
                                      double *lambda_h, eolc_ineq_info *info);
+
+/* Constraint rows in CSR over the DOFs of the context's block rows (a
+ * topology with EOL nodes: the extended layout of eolc_set_topology_eol,
+ * Eulerian DOF j of EOL node k at 3 (n_nodes + k) + j).  As input: n_rows,
+ * ptr (n_rows + 1 offsets), col, val (duplicates are summed) and rhs (beq or
+ * bineq per row).  As output of eolc_constraint_rows: capacity is the number
+ * of rows the arrays hold (ptr capacity + 1 entries, col / val 9 capacity,
+ * rhs capacity) and n_rows receives the count. */
+typedef struct {
+  int n_rows;
+  int capacity;
+  int *ptr;
+  int *col;
+  double *val;
+  double *rhs;
+} eolc_rows;
+
+/* ---- GeneralizedSolver::velocitySolve with equality rows -----------------
+ * The whole QP of GeneralizedSolver.cpp:138-170 (quadprog convention,
+ * QuadProg.h:8-9):
+ *   argmin 1/2 v'MDK v + b'v  s.t.  v[fixed_dofs[k]] = beq[k],
+ *                                   Aeq v = beq_rows,  Aineq v <= bineq,
+ * on the MDK of the last eolc_forces_fill, on plain and EOL topologies: the
+ * rows Constraints::fill builds for an EOL mesh (eolc_constraint_rows) have
+ * this form, and the pins stay a DOF list (addFixed's unit rows,
+ * Constraints.cpp:114-119).  b_h, v_h: 3 x (block rows) values; a row on a
+ * padded Eulerian DOF is EOLC_BAD_ARG.  Same method, stopping test and
+ * options as eolc_velocity_solve_ineq, with every equality row always active
+ * and its multiplier unclamped.  eq / ineq may be NULL (no rows).
+ * lambda_eq_h (eq->n_rows) and lambda_ineq_h (ineq->n_rows) are optional:
+ * MDK v + b + Aeq' lambda_eq + Aineq' lambda_ineq = 0 on the free DOFs.
+ * info->max_violation covers |Aeq v - beq| as well. */
+eolc_status eolc_velocity_solve_qp(eolc_ctx *ctx, const double *b_h,
+                                   const int *fixed_dofs_h, const double *beq_h,
+                                   int n_fixed, const eolc_rows *eq,
+                                   const eolc_rows *ineq,
+                                   const eolc_solve_opts *opts, double *v_h,
+                                   double *lambda_eq_h, double *lambda_ineq_h,
+                                   eolc_ineq_info *info);
 
 /* ---- Cloth::step (Cloth.cpp:359-413, non-EOL, no remeshing, no QP) -----
  * One implicit-Euler step on host buffers: Forces::fill, pinned-corner
@@ -388,7 +429,9 @@ typedef struct {
 
 /* Contact set of CD2 for the current topology: point obstacles first
  * (pointTriCollision, EOL=false), then each box in order
- * (boxTriCollision, EOL=false).  x_h: cloth node positions (3N).
+ * (boxTriCollision, EOL=false).  x_h: cloth node positions (3N; on a
+ * topology with EOL nodes the N mesh nodes, as Collisions.cpp:55-78 packs
+ * them).
  * points_h / normals_h: n_points x 3.  Writes at most capacity contacts;
  * *n_out receives the total count (EOLC_CAPACITY if it exceeds capacity). */
 eolc_status eolc_cd2(eolc_ctx *ctx, const double *x_h, const eolc_box *boxes,
@@ -416,6 +459,50 @@ eolc_status eolc_contact_rows(const eolc_contact *contacts, int n_contacts,
                               double *ineq_val_h, double *bineq_h,
                               int *n_rows);
 
+/* ---- Constraints::fill for an EOL mesh (Constraints.cpp:147-468) ---------
+ * The mesh state Constraints::fill reads after EOL preprocessing: positions
+ * (Node::x, 3 n_nodes), material coordinates (Vert::u, 2 n_nodes), faces
+ * (Face::v, n_tri x 3), the edges in mesh.edges order (Edge::n[0], n[1],
+ * n_edges x 2; Node::adje lists a node's edges in this order) with their
+ * Edge::preserve flags (may be NULL: none), and per EoL_index k (as
+ * eolc_set_topology_eol): the node, Node::cornerID (constraint-table column
+ * of the box corner or point obstacle it sits on, or -1) and
+ * Node::cdEdges[0] (the column of the box edge, read when cornerID < 0). */
+typedef struct {
+  int n_nodes;
+  const double *x;
+  const double *u;
+  const int *tri;
+  int n_tri;
+  const int *edges;
+  const int *preserve;
+  int n_edges;
+  const int *eol_nodes;
+  const int *corner_id;
+  const int *cd_edge;
+  int n_eol;
+} eolc_eol_mesh;
+
+/* The equality and inequality rows of Constraints::fill, without the pins
+ * (those stay a DOF list): for each EOL node in node order, the rows of
+ * :147-415 — at a box corner or point obstacle the normal row (inequality)
+ * and its two orthogonal rows (equalities where the node is locally flat or
+ * at a point, else inequalities); on a box edge the node-normal inequality
+ * and the flat equality, or the edge's two face rows; then one Eulerian
+ * equality, across the border at a boundary node, along the preserved edges
+ * inside — then the CD2 contact rows of :422-468 (eolc_contact_rows'),
+ * skipping contacts on EOL nodes.  The constraint table (:40-105) comes from
+ * the point obstacles' normals and the boxes: columns n_points + 20 b + p
+ * (corner p) and n_points + 20 b + 8 + e (edge e), the numbering of
+ * Box.cpp's tables.  Obstacles are static (eolc_box has no velocity), so
+ * every right-hand side is 0, as the reference's for boxes at rest.
+ * Columns use the extended layout (eolc_rows).  Host only.  EOLC_CAPACITY
+ * when eq or ineq is too small (n_rows has the need). */
+eolc_status eolc_constraint_rows(const eolc_eol_mesh *mesh, const eolc_box *boxes,
+                                 int n_boxes, const double *point_normals_h,
+                                 int n_points, const eolc_contact *contacts,
+                                 int n_contacts, eolc_rows *eq, eolc_rows *ineq);
+
 /* ---- Cloth::step with collisions (Cloth.cpp:359-413, non-EOL, no remesh) --
  * One implicit-Euler step with the contact QP, on host buffers like
  * eolc_step: pins beq = 0.99 v + c, CD2 of the step's positions against the
@@ -438,6 +525,23 @@ eolc_status eolc_step_contacts(eolc_ctx *ctx, double *x_h, const double *X_h,
                                const double *normals_h, int n_points,
                                double threshold, const eolc_solve_opts *opts,
                                eolc_ineq_info *info);
+
+/* ---- Cloth::step of an EOL mesh (Cloth.cpp:359-413, no remeshing) --------
+ * One implicit-Euler step on host buffers with the rows of Constraints::fill
+ * given (eolc_constraint_rows on the step's state): pins beq = 0.99 v + c,
+ * Forces::fill with the EOL branches, b = -(M v + h f), the QP of
+ * eolc_velocity_solve_qp, x += h v on the mesh nodes and, for every EOL node,
+ * u += h vE with its Eulerian velocity (Cloth.cpp:394-410).  x_h (3 n_nodes)
+ * and u_h (2 n_nodes, the material coordinates X) are updated in place; v_h
+ * has 3 x (block rows) values in the extended layout (the Eulerian
+ * velocities at 3 (n_nodes + k)) and is updated in place.  Also runs on a
+ * topology without EOL nodes (u is then unchanged). */
+eolc_status eolc_step_eol(eolc_ctx *ctx, double *x_h, double *u_h, double *v_h,
+                          const eolc_material *mat, const double grav[3],
+                          double h, const int *fixed_dofs_h,
+                          const double *fixed_vel_h, int n_fixed,
+                          const eolc_rows *eq, const eolc_rows *ineq,
+                          const eolc_solve_opts *opts, eolc_ineq_info *info);
 
 /* ---- learned preconditioner ------------------------------------------------
  * A 3-layer message-passing network (hidden width 64, BF16 weights, FP32

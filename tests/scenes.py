@@ -150,3 +150,34 @@ def delaunay_batch(n_meshes, tri_lo=5000, tri_hi=50000, seed=5):
     fixed = np.concatenate([s["fixed"] + 3 * o for s, o in zip(sheets, off[:-1])]).astype(np.int32)
     return dict(sheets=sheets, mats=mats, node_off=np.array(off), x=x, X=X,
                 v=np.zeros_like(x), fixed=fixed, fixed_vel=np.zeros(len(fixed)))
+
+
+def eol_edge_sheet(quads, pins=True):
+    """A unit sheet lying on a box whose +x/+z edge runs along y at x = 0.5,
+    z = 0 (box 1 x 2 x 0.2 centred at (0, 0.5, -0.1)): the half x < 0.5 rests
+    on the top face, the half x > 0.5 hangs free, and the column of nodes on
+    the edge line are the EOL nodes (EoL_index in node order), each on box
+    edge 10 (faces +x and +z, constraint-table column 18 with no point
+    obstacles), the edges between them preserved.  quads must be even.
+    pins=True pins the two corners on the far side of the top face (x = 0).
+    Returns the mesh, the EOL tables, the obstacle (as an axis-aligned box
+    centre and dimensions) and the pins."""
+    assert quads % 2 == 0
+    r = quads + 1
+    x, X, tri = eolc.sheet_mesh(r, r)
+    xy = x.reshape(-1, 3)
+    eol = np.flatnonzero(np.abs(xy[:, 0] - 0.5) < 1e-12).astype(np.int32)
+    edges = eolc.mesh_edges(tri)
+    is_eol = np.zeros(len(xy), bool)
+    is_eol[eol] = True
+    preserve = (is_eol[edges[:, 0]] & is_eol[edges[:, 1]]).astype(np.int32)
+    fixed = np.zeros(0, np.int32)
+    if pins:
+        far = np.flatnonzero((np.abs(xy[:, 0]) < 1e-12) &
+                             ((np.abs(xy[:, 1]) < 1e-12) | (np.abs(xy[:, 1] - 1) < 1e-12)))
+        fixed = np.array([3 * a + c for a in far for c in range(3)], np.int32)
+    return dict(x=x, X=X, tri=tri, hinge=eolc.mesh_hinges(tri), edges=edges, eol=eol,
+                preserve=preserve, corner=-np.ones(len(eol), np.int32),
+                cd=np.full(len(eol), 8 + 10, np.int32), box_center=[0.0, 0.5, -0.1],
+                box_dim=[1.0, 2.0, 0.2], fixed=fixed, fixed_vel=np.zeros(len(fixed)),
+                n=len(xy))

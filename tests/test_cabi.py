@@ -44,12 +44,15 @@ def test_struct_layouts_match_c(built, tmp_path):
     src = tmp_path / "layout.c"
     src.write_text(
         '#include <stddef.h>\n#include <stdio.h>\n#include "%s"\n'
-        'int main(void){printf("%%zu %%zu %%zu %%zu %%zu %%zu %%zu %%zu %%zu %%zu %%zu %%zu\\n",'
+        'int main(void){printf("%%zu %%zu %%zu %%zu %%zu %%zu %%zu %%zu %%zu %%zu %%zu %%zu'
+        ' %%zu %%zu %%zu %%zu %%zu\\n",'
         ' sizeof(eolc_contact), offsetof(eolc_contact, count1), offsetof(eolc_contact, source),'
         ' sizeof(eolc_box), sizeof(eolc_material), sizeof(eolc_solve_opts),'
         ' sizeof(eolc_solve_info), sizeof(eolc_batch_info), offsetof(eolc_batch_info, iterations),'
         ' offsetof(eolc_batch_info, step_ms), sizeof(eolc_ineq_info),'
-        ' offsetof(eolc_ineq_info, max_violation)); return 0;}\n'
+        ' offsetof(eolc_ineq_info, max_violation), sizeof(eolc_rows), offsetof(eolc_rows, rhs),'
+        ' sizeof(eolc_eol_mesh), offsetof(eolc_eol_mesh, edges), offsetof(eolc_eol_mesh, n_eol));'
+        ' return 0;}\n'
         % HEADER)
     exe = tmp_path / "layout"
     subprocess.check_call(["gcc", str(src), "-o", str(exe)])
@@ -58,7 +61,9 @@ def test_struct_layouts_match_c(built, tmp_path):
             ctypes.sizeof(eolc.Box), ctypes.sizeof(eolc.Material), ctypes.sizeof(eolc.SolveOpts),
             ctypes.sizeof(eolc.SolveInfo), ctypes.sizeof(eolc.BatchInfo),
             eolc.BatchInfo.iterations.offset, eolc.BatchInfo.step_ms.offset,
-            ctypes.sizeof(eolc.IneqInfo), eolc.IneqInfo.max_violation.offset]
+            ctypes.sizeof(eolc.IneqInfo), eolc.IneqInfo.max_violation.offset,
+            ctypes.sizeof(eolc.Rows), eolc.Rows.rhs.offset, ctypes.sizeof(eolc.EolMesh),
+            eolc.EolMesh.edges.offset, eolc.EolMesh.n_eol.offset]
     assert got == want
 
 

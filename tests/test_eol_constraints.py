@@ -1,0 +1,187 @@
+"""Constraints::fill for EOL meshes on the CPU (Constraints.cpp:135-468):
+
+* the library's host-side row builder eolc_constraint_rows produces the
+  oracle's restatement (oracle/eol_ref.py) row for row, in the reference's
+  order, on the box-edge sheet in every branch — locally flat and bent edge
+  nodes, boundary and interior Eulerian rows, corner and point-obstacle
+  nodes (flat and bent), rotated boxes, CD2 contact rows with the EOL nodes'
+  contacts skipped;
+* it reports capacity and rejects bad tables;
+* the oracle's QP with equality rows (solve_qp_eq) equals the minimiser found
+  by enumerating active sets on small random QPs, and an oracle EOL step
+  keeps its equality rows and contacts.
+"""
+import itertools
+
+import numpy as np
+import pytest
+
+import eol_ref as R
+import eolc
+import oracle as O
+import scenes
+
+
+def _boxes(s, rot=0.0):
+    """The scene's box as (oracle Box, library Box); rot: rotation about z
+    applied to the frame (the rows only read the table, so any frame will do
+    for the builders' comparison)."""
+    E1 = np.eye(4)
+    c, sn = np.cos(rot), np.sin(rot)
+    E1[:3, :3] = [[c, -sn, 0], [sn, c, 0], [0, 0, 1]]
+    E1[:3, 3] = s["box_center"]
+    flat = list(E1.flatten(order="F"))
+    ob = O.axis_box(s["box_center"], s["box_dim"])
+    for k in range(16):
+        ob.E1[k] = flat[k]
+    return ob, eolc.Box(s["box_dim"], flat)
+
+
+def _compare(s, x, u, corner, cd, preserve, rot=0.0, point_normals=None, contacts=()):
+    ob, lb = _boxes(s, rot)
+    Aeq, beq, C, d = R.constraint_rows(x, u, s["tri"], s["edges"], s["eol"], corner, cd, preserve,
+                                       [ob], point_normals, contacts)
+    lc = [eolc.Contact.from_buffer_copy(bytes(c)) for c in contacts]
+    E, I = eolc.constraint_rows(x, u, s["tri"], s["edges"], s["eol"], corner, cd, preserve,
+                                [lb], point_normals, lc)
+    n, ne = s["n"], len(s["eol"])
+    idx = eolc.eol_reference_index(n, ne)
+    nd = 3 * (n + ne)
+    Eg, Ig = E.csr(nd)[:, idx], I.csr(nd)[:, idx]
+    assert (E.m, I.m) == (Aeq.shape[0], C.shape[0])
+    tol = 1e-15
+    assert np.abs((Eg - Aeq).toarray()).max(initial=0.0) <= tol
+    assert np.abs((Ig - C).toarray()).max(initial=0.0) <= tol
+    assert not E.rhs.any() and not I.rhs.any()
+    # no row of the builder touches a padded Eulerian DOF
+    pad = set((3 * (n + np.arange(ne)) + 2).tolist())
+    assert not pad & set(E.col.tolist()) and not pad & set(I.col.tolist())
+    return Aeq, C
+
+
+def test_rows_flat_sheet_on_box_edge():
+    s = scenes.eol_edge_sheet(10)
+    ob, _ = _boxes(s)
+    contacts = O.cd2(s["x"], s["tri"], [ob], threshold=1e-3)
+    Aeq, C = _compare(s, s["x"], s["X"], s["corner"], s["cd"], s["preserve"], contacts=contacts)
+    ne = len(s["eol"])
+    # flat edge nodes: one node-normal inequality and one flat equality each,
+    # plus one Eulerian equality; the EOL nodes' contacts are skipped
+    assert Aeq.shape[0] == 2 * ne
+    n_kept = sum(1 for c in contacts if c.verts2[0] not in set(s["eol"].tolist()))
+    assert C.shape[0] == ne + n_kept
+    assert n_kept < len(contacts)
+
+
+# jitter amplitudes that bend 11, 1 and 7 of the 11 EOL nodes past 0.1 rad
+@pytest.mark.parametrize("seed,amp", [(1, 0.02), (2, 0.002), (3, 0.004)])
+def test_rows_bent_nodes_and_interior_directions(seed, amp):
+    s = scenes.eol_edge_sheet(10)
+    rng = np.random.default_rng(seed)
+    x = s["x"] + rng.normal(0, amp, s["x"].size)
+    u = s["X"] + rng.normal(0, 0.01, s["X"].size)     # interior directions differ
+    pres = (rng.random(len(s["edges"])) < 0.3).astype(np.int32) | s["preserve"]
+    _compare(s, x, u, s["corner"], s["cd"], pres, rot=0.3 * seed)
+
+
+@pytest.mark.parametrize("bend", [0.0, 0.05])
+def test_rows_corner_and_point_nodes(bend):
+    s = scenes.eol_edge_sheet(10)
+    rng = np.random.default_rng(4)
+    x = s["x"] + rng.normal(0, bend, s["x"].size)
+    ne = len(s["eol"])
+    pn = np.array([[0.0, 0.0, 1.0], [0.6, 0.0, 0.8]])
+    corner = -np.ones(ne, np.int32)
+    corner[0], corner[1], corner[ne - 1] = 0, 1, 2 + 3     # two points, one box corner
+    cd = s["cd"] + 2                                        # two point columns come first
+    Aeq, C = _compare(s, x, s["X"], corner, cd, s["preserve"], rot=0.7, point_normals=pn)
+    assert Aeq.shape[0] > 0 and C.shape[0] > 0
+
+
+def test_rows_capacity_and_bad_arguments():
+    s = scenes.eol_edge_sheet(6)
+    ne = len(s["eol"])
+    x, u = eolc._f64(s["x"]), eolc._f64(s["X"])
+    tri, edges = eolc._i32(s["tri"]), eolc._i32(s["edges"])
+    eol, corner, cd = eolc._i32(s["eol"]), eolc._i32(s["corner"]), eolc._i32(s["cd"])
+    pres = eolc._i32(s["preserve"])
+    _, lb = _boxes(s)
+    barr = (eolc.Box * 1)(lb)
+
+    def call(cap_e, cap_i, cd_arr=cd):
+        mesh = eolc.EolMesh(s["n"], eolc._d(x), eolc._d(u), eolc._i(tri), len(tri),
+                            eolc._i(edges), eolc._i(pres), len(edges), eolc._i(eol),
+                            eolc._i(corner), eolc._i(cd_arr), ne)
+        bufs = []
+        for cap in (cap_e, cap_i):
+            a = (np.zeros(cap + 1, np.int32), np.zeros(9 * max(cap, 1), np.int32),
+                 np.zeros(9 * max(cap, 1)), np.zeros(max(cap, 1)))
+            bufs.append((eolc.Rows(0, cap, eolc._i(a[0]), eolc._i(a[1]), eolc._d(a[2]),
+                                   eolc._d(a[3])), a))
+        st = eolc.lib.eolc_constraint_rows(mesh, barr, 1, None, 0, None, 0, bufs[0][0], bufs[1][0])
+        return st, bufs[0][0].n_rows, bufs[1][0].n_rows, bufs
+
+    st, me, mi, _ = call(100, 100)
+    assert st == eolc.OK and (me, mi) == (2 * ne, ne)
+    st, me2, mi2, bufs = call(3, 100)
+    assert st == eolc.CAPACITY and (me2, mi2) == (me, mi)
+    assert bufs[0][1][0][3] > 0                 # the rows that fit are written
+    st, *_ = call(100, 100, eolc._i32(np.full(ne, 20, np.int32)))  # one box: columns 0..19
+    assert st == eolc.BAD_ARG
+
+
+def _enumerate_eq(A, b, E, e, C, d):
+    n, m, me = A.shape[0], C.shape[0], E.shape[0]
+    best = None
+    for k in range(m + 1):
+        for W in itertools.combinations(range(m), k):
+            G = np.vstack([E, C[list(W)]])
+            K = np.block([[A, G.T], [G, np.zeros((len(G), len(G)))]])
+            sol = np.linalg.solve(K, np.concatenate([-b, e, d[list(W)]]))
+            v, lw = sol[:n], sol[n + me:]
+            if (lw >= -1e-12).all() and (C @ v - d <= 1e-10).all():
+                obj = 0.5 * v @ A @ v + b @ v
+                if best is None or obj < best[0] - 1e-14:
+                    best = (obj, v)
+    return best[1]
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_qp_with_equality_rows_matches_enumeration(seed):
+    rng = np.random.default_rng(seed)
+    n, me, m = 9, 2, 5
+    B = rng.normal(size=(n, n))
+    A = B @ B.T + 0.5 * np.eye(n)
+    b = rng.normal(size=n)
+    E, e = rng.normal(size=(me, n)), rng.normal(size=me)
+    C, d = rng.normal(size=(m, n)), rng.normal(size=m) * 0.3
+    v, le, li, _ = R.solve_qp_eq(A, b, [], [], E, e, C, d)
+    ve = _enumerate_eq(A, b, E, e, C, d)
+    assert np.abs(v - ve).max() <= 1e-10 * max(1.0, np.abs(ve).max())
+    assert np.abs(E @ v - e).max() <= 1e-10
+    assert np.abs(A @ v + b + E.T @ le + C.T @ li).max() <= 1e-9
+    assert (li >= 0).all()
+
+
+def test_oracle_eol_step_keeps_rows():
+    s = scenes.eol_edge_sheet(8)
+    ob, _ = _boxes(s)
+    x, u = s["x"].copy(), s["X"].copy()
+    n, ne = s["n"], len(s["eol"])
+    v = np.zeros(3 * n + 2 * ne)
+    mat, g, h = O.material(), scenes.GRAV, scenes.H
+    for _ in range(3):
+        contacts = O.cd2(x, s["tri"], [ob], threshold=1e-3)
+        rows = R.constraint_rows(x, u, s["tri"], s["edges"], s["eol"], s["corner"], s["cd"],
+                                 s["preserve"], [ob], None, contacts)
+        u0 = u.copy()
+        R.step(x, u, v, s["tri"], s["hinge"], s["eol"], mat, g, h, s["fixed"], s["fixed_vel"],
+               rows)
+        Aeq, _, C, _ = rows
+        vm = np.abs(v).max()
+        assert np.abs(Aeq @ v).max() <= 1e-10 * vm
+        assert (C @ v).max() <= 1e-10 * vm
+        # only the EOL nodes' material coordinates move
+        moved = np.flatnonzero(np.abs(u - u0).reshape(-1, 2).max(1) > 0)
+        assert set(moved.tolist()) <= set(s["eol"].tolist())
+    assert np.abs(v[3 * n:]).max() > 0  # material flows across the edge

@@ -843,7 +843,8 @@ def run_eol(args, local_rank, stream, sc, reps=5):
     import numpy as np
     import torch
     import eolc
-    import oracle as O
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O  # CPU side only: the baseline below
     r = QUADS + 1
     eol = (r // 2) * r + np.arange(r)  # node k = i r + j; the row i = r // 2
     rng = np.random.default_rng(8)
@@ -874,6 +875,78 @@ def run_eol(args, local_rank, stream, sc, reps=5):
                            "sample": "one oracle Forces::fill with the same EOL nodes"}
     out["note"] = ("wall time of eolc_forces_fill including the upload of x, X and the "
                    "download of f, M and MDK")
+    return out
+
+
+def run_eol_step(args, local_rank, stream, steps=8, cpu_quads=16, cpu_steps=3):
+    """Cloth::step of an EOL mesh: a sheet lying on a box whose edge runs
+    under its middle column of nodes (the EOL nodes, on box edge 10), the
+    hanging half pulling material over the edge through the Eulerian DOFs.
+    Each step is CD2 (eolc_cd2), the rows of Constraints::fill
+    (eolc_constraint_rows) and eolc_step_eol (forces with the EOL branches,
+    the QP with the EOL equality and inequality rows and the contact rows,
+    x += h v, u += h vE), host arrays in and out, wall clock.  Sheets of 16
+    and 128 quads per side; CPU baseline: the oracle's step (its restated
+    rows, EOL fill and exact active-set QP) on the 16-quad sheet."""
+    import numpy as np
+    import torch
+    import eolc
+    import scenes as S
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O  # CPU side only: the baseline below
+    import eol_ref
+    mat = eolc.Material(**MAT)
+    opts = arm_opts(eolc, "jacobi", args.degree)
+    out = {}
+    for q in (cpu_quads, 128):
+        sc = S.eol_edge_sheet(q)
+        n, ne = sc["n"], len(sc["eol"])
+        ctx = eolc.Context(local_rank)
+        ctx.set_stream(stream.cuda_stream)
+        ctx.set_topology_eol(n, sc["tri"], sc["hinge"], sc["eol"])
+        box = axis_box(eolc, sc["box_center"], sc["box_dim"])
+        x, u, v = sc["x"].copy(), sc["X"].copy(), np.zeros(3 * (n + ne))
+        ts, rows, solves, active = [], [], [], []
+        for k in range(steps + 2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            contacts = ctx.cd2(x, [box], threshold=1e-3)
+            E, I = eolc.constraint_rows(x, u, sc["tri"], sc["edges"], sc["eol"], sc["corner"],
+                                        sc["cd"], sc["preserve"], [box], None, contacts)
+            info = ctx.step_eol(x, u, v, mat, GRAV, H, sc["fixed"], sc["fixed_vel"], E, I, opts)
+            if k >= 2:  # the first two steps build the plans and the contact set grows
+                ts.append(time.perf_counter() - t0)
+                rows.append(E.m + I.m)
+                solves.append(info.solves)
+                active.append(info.n_active)
+        out["sheet_%d" % q] = {"nodes": n, "eol_nodes": ne, "ms_per_step": round(
+            1e3 * float(np.median(ts)), 3), "steps_per_s": 1.0 / float(np.median(ts)),
+            "rows": int(np.median(rows)), "active_contacts": int(np.median(active)),
+            "linear_solves": float(np.mean(solves)),
+            "material_flow": float(np.abs(u - sc["X"]).max())}
+    sc = S.eol_edge_sheet(cpu_quads)
+    ob = O.axis_box(sc["box_center"], sc["box_dim"])
+    n, ne = sc["n"], len(sc["eol"])
+    x, u, v = sc["x"].copy(), sc["X"].copy(), np.zeros(3 * n + 2 * ne)
+    cpu = []
+    for k in range(cpu_steps):
+        t0 = time.perf_counter()
+        c = O.cd2(x, sc["tri"], [ob], threshold=1e-3)
+        r = eol_ref.constraint_rows(x, u, sc["tri"], sc["edges"], sc["eol"], sc["corner"],
+                                    sc["cd"], sc["preserve"], [ob], None, c)
+        eol_ref.step(x, u, v, sc["tri"], sc["hinge"], sc["eol"], O.material(), GRAV, H,
+                     sc["fixed"], sc["fixed_vel"], r)
+        if k >= 1:
+            cpu.append(time.perf_counter() - t0)
+    out["workload"] = ("EOL sheet on a box edge (middle node column = EOL nodes), CD2 + "
+                       "Constraints::fill rows + Cloth::step with the QP, mixed precision, "
+                       "Jacobi PCG inside the QP")
+    out["cpu_baseline"] = {"value": 1.0 / float(np.median(cpu)), "unit": "steps/s", "cores": 1,
+                           "kind": "port",
+                           "sample": "oracle EOL steps 2-%d of the %d-quad sheet (exact "
+                                     "active-set QP, scipy sparse LU)" % (cpu_steps, cpu_quads)}
+    out["note"] = ("steps 3 onward of each trajectory (the first two build the plans and the "
+                   "top half's contact set); host arrays in and out through the C ABI")
     return out
 
 
@@ -1072,6 +1145,7 @@ def run_ours(args, rank, world, local_rank):
         line["topology_refresh"] = optional_line(lambda: run_refresh(args, local_rank, stream, sc))
     if world == 1 and not args.no_eol:
         line["eol_fill"] = optional_line(lambda: run_eol(args, local_rank, stream, sc))
+        line["eol_step"] = optional_line(lambda: run_eol_step(args, local_rank, stream))
     if world == 1 and not args.no_batch:
         line["batched"] = optional_line(lambda: run_batched(args, local_rank, stream, flush))
         line["batched_delaunay_learned"] = optional_line(
@@ -1095,7 +1169,7 @@ def main():
     ap.add_argument("--no-cd2", action="store_true", help="skip the CD2 (configuration 2) line")
     ap.add_argument("--no-contacts", action="store_true", help="skip the contact-step line")
     ap.add_argument("--no-refresh", action="store_true", help="skip the topology-refresh line")
-    ap.add_argument("--no-eol", action="store_true", help="skip the EOL-fill line")
+    ap.add_argument("--no-eol", action="store_true", help="skip the EOL fill and EOL step lines")
     ap.add_argument("--batch-sheets", type=int, default=256)
     ap.add_argument("--delaunay-meshes", type=int, default=64)
     args = ap.parse_args()

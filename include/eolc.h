@@ -1,7 +1,7 @@
 /*
  * eolc.h — C ABI of the GB300-native EOL-Cloth hot path.
  *
- * One library (libeolc.so) replaces, for the non-EOL, non-remeshing path:
+ * One library (libeolc.so) replaces, for the non-remeshing path:
  *   Forces::fill                     src/Forces.cpp:912-930   (Forces.h:40)
  *   GeneralizedSolver::velocitySolve src/GeneralizedSolver.cpp:107-173
  *                                    (GeneralizedSolver.h:26-30): pinned DOFs,
@@ -11,6 +11,8 @@
  *                                    with or without contacts
  *   Forces::fill EOL branches        src/Forces.cpp:127-329, 399-497,
  *                                    541-683, 746-884
+ *   Constraints::fill EOL rows and   src/Constraints.cpp:135-468,
+ *   Cloth::step of EOL meshes        src/Cloth.cpp:359-413 (no remeshing)
  *   CD2 / btc::boxTriCollision /     src/Collisions.cpp:55-78,
  *   btc::pointTriCollision           src/boxTriCollision.cpp:602-1224
  *   BrenderManager::exportBrender /  src/BrenderManager.cpp:34-84,

@@ -954,21 +954,36 @@ class GeneralizedSolver:
     def velocitySolve(self, fixedPoints, collisions, MDK, b, Aeq, beq, Aineq, bineq, v):
         """Same arguments as GeneralizedSolver::velocitySolve
         (GeneralizedSolver.cpp:107-173).  MDK must be the matrix of the
-        context's last fill (it stays resident on the GPU).  Aeq must consist
-        of unit rows (pinned DOFs, Constraints.cpp:114-119).  With
-        collisions=True the QP with Aineq v <= bineq (which the reference
-        hands to Mosek/Gurobi) is solved by eolc_velocity_solve_ineq.  v is
-        the initial guess and is overwritten in place."""
+        context's last fill (it stays resident on the GPU); DOFs are the
+        context's block rows (the extended layout on an EOL topology).  The
+        unit rows of Aeq (pinned DOFs, Constraints.cpp:114-119) become fixed
+        DOFs; any other Aeq rows (the EOL rows of Constraints.cpp:147-415)
+        go to eolc_velocity_solve_qp with Aineq.  With collisions=True the QP
+        with Aineq v <= bineq (which the reference hands to Mosek/Gurobi) is
+        solved on the GPU as well.  v is the initial guess and is overwritten
+        in place."""
         import scipy.sparse as sp
         fixed = np.zeros(0, np.int32)
         beqv = np.zeros(0)
+        general = None
         if fixedPoints and Aeq is not None and Aeq.shape[0] > 0:
             A = sp.csr_matrix(Aeq)
-            if np.any(np.diff(A.indptr) != 1) or np.any(A.data != 1.0):
-                raise EolcError(BAD_ARG, "Aeq must consist of unit rows")
-            fixed = A.indices.astype(np.int32)
-            beqv = np.asarray(beq, dtype=np.float64)
-        if collisions and Aineq is not None and Aineq.shape[0] > 0:
+            A.sort_indices()
+            beq_all = np.asarray(beq, dtype=np.float64)
+            unit = (np.diff(A.indptr) == 1)
+            unit[unit] = A.data[A.indptr[:-1][unit]] == 1.0
+            fixed = A.indices[A.indptr[:-1][unit]].astype(np.int32)
+            beqv = beq_all[unit]
+            if not unit.all():
+                general = RowSet.from_csr(A[~unit], beq_all[~unit])
+        if general is not None:
+            ineq = (RowSet.from_csr(Aineq, bineq) if collisions and Aineq is not None
+                    and Aineq.shape[0] > 0 else None)
+            out, self.lambda_eq, lam, info = self.ctx.velocity_solve_qp(
+                b, fixed, beqv, general, ineq, self.opts, v0=v)
+            if ineq is not None:
+                self.lambda_ineq = lam
+        elif collisions and Aineq is not None and Aineq.shape[0] > 0:
             out, self.lambda_ineq, info = self.ctx.velocity_solve_ineq(
                 b, fixed, beqv, Aineq, bineq, self.opts, v0=v)
         else:

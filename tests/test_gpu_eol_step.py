@@ -13,6 +13,14 @@ edge through the EOL nodes' Eulerian DOFs.
   mesh — x, the material coordinates u of the EOL nodes and v in the
   reference's 3N + 2E layout (FP64 within 1e-7, mixed within 1e-5 of the
   largest velocity or displacement);
+* the same with the EOL line's end nodes tagged as box-corner nodes and its
+  middle node on a point obstacle (the corner and point branches of
+  Constraints.cpp:148-262; the rows read only the tagged table column, so
+  the box stays the one whose edges lie off the sheet: box edges crossing
+  the cloth give edge-edge rows that depend on vertex-face rows, on which
+  the augmented Lagrangian's multipliers converge too slowly);
+* GeneralizedSolver.velocitySolve (eolc.py) with the reference's Aeq —
+  pinned unit rows and the EOL rows together — equals the QP entry point;
 * a row on a padded Eulerian DOF is rejected.
 """
 import numpy as np
@@ -128,6 +136,76 @@ def test_steps_track_oracle(eolc, precision):
     # material crossed the edge: the EOL nodes' u moved, nothing else did
     moved = np.flatnonzero(np.abs(ug - s["X"]).reshape(-1, 2).max(1) > 0)
     assert len(moved) > 0 and set(moved.tolist()) <= set(s["eol"].tolist())
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_corner_and_point_nodes_step(eolc, precision):
+    s = scenes.eol_edge_sheet(10)
+    n, ne = s["n"], len(s["eol"])
+    idx = eolc.eol_reference_index(n, ne)
+    ctx = eolc.Context(0)
+    ctx.set_topology_eol(n, s["tri"], s["hinge"], s["eol"])
+    ob = O.axis_box(s["box_center"], s["box_dim"])
+    lb = eolc.Box(s["box_dim"], list(ob.E1))
+    mid = ne // 2
+    pts, nrm = s["x"].reshape(-1, 3)[s["eol"][mid]].copy(), np.array([0.0, 0.0, 1.0])
+    corner = s["corner"].copy()
+    # the line's ends on corners 5 (+x, -y, +z) and 7 (+x, +y, +z); the
+    # point obstacle's column comes first
+    corner[0], corner[-1], corner[mid] = 1 + 5, 1 + 7, 0
+    cd = s["cd"] + 1
+    mat, mat_o, g, h = eolc.Material(**scenes.material_c1()), O.material(), scenes.GRAV, scenes.H
+    xg, ug, vg = s["x"].copy(), s["X"].copy(), np.zeros(3 * (n + ne))
+    xo, uo, vo = s["x"].copy(), s["X"].copy(), np.zeros(3 * n + 2 * ne)
+    tol = 1e-7 if precision == 0 else 1e-5
+    kinds = set()
+    for k in range(3):
+        con = ctx.cd2(xg, [lb], points=pts, normals=nrm, threshold=1e-3)
+        kinds |= {(c.count1, c.count2, c.source > 0) for c in con}
+        E, I = eolc.constraint_rows(xg, ug, s["tri"], s["edges"], s["eol"], corner, cd,
+                                    s["preserve"], [lb], nrm, con)
+        info = ctx.step_eol(xg, ug, vg, mat, g, h, s["fixed"], s["fixed_vel"], E, I,
+                            eolc.SolveOpts(precision=precision))
+        assert info.status == eolc.OK
+        co = O.cd2(xo, s["tri"], [ob], points=pts, normals=nrm, threshold=1e-3)
+        rows = R.constraint_rows(xo, uo, s["tri"], s["edges"], s["eol"], corner, cd,
+                                 s["preserve"], [ob], nrm, co)
+        R.step(xo, uo, vo, s["tri"], s["hinge"], s["eol"], mat_o, g, h, s["fixed"],
+               s["fixed_vel"], rows)
+        vm = np.abs(vo).max()
+        ev = np.abs(vg[idx] - vo).max() / vm
+        ex = np.abs(xg - xo).max() / (h * vm)
+        eu = np.abs(ug - uo).max() / (h * vm)
+        print("step %d: %d eq, %d ineq rows, v %.2e x %.2e u %.2e" % (k, E.m, I.m, ev, ex, eu))
+        assert ev <= tol and ex <= tol and eu <= tol
+    assert {(3, 1, True), (1, 3, False)} <= kinds  # box vertex-face, point-face
+    # the corner nodes' material coordinates move freely (no Eulerian row)
+    assert np.abs(ug.reshape(-1, 2)[s["eol"][[0, -1]]] - s["X"].reshape(-1, 2)[s["eol"][[0, -1]]]).max() > 0
+
+
+def test_generalized_solver_takes_eol_rows(eolc):
+    s, ctx, ob, lb = _setup(eolc)
+    n, ne = s["n"], len(s["eol"])
+    mat = eolc.Material(**scenes.material_c1())
+    x, u = s["x"].copy(), s["X"].copy()
+    E, I, _, _ = _rows_both(eolc, s, ctx, ob, lb, x, u)
+    forces = eolc.Forces(ctx, eolc.PREC_FP64)
+    forces.fill(x, u, mat, scenes.GRAV, scenes.H)
+    b = -scenes.H * forces.f
+    nd = 3 * (n + ne)
+    # the reference's Aeq: the EOL equality rows, then addFixed's unit rows
+    import scipy.sparse as sp
+    pins = sp.csr_matrix((np.ones(len(s["fixed"])), (np.arange(len(s["fixed"])), s["fixed"])),
+                         shape=(len(s["fixed"]), nd))
+    Aeq = sp.vstack([E.csr(nd), pins]).tocsr()
+    beq = np.concatenate([E.rhs, np.zeros(len(s["fixed"]))])
+    gs = eolc.GeneralizedSolver(ctx, eolc.SolveOpts(precision=0))
+    v = np.zeros(nd)
+    assert gs.velocitySolve(True, True, forces.MDK, b, Aeq, beq, I.csr(nd), I.rhs, v)
+    vq, _, _, info = ctx.velocity_solve_qp(b, s["fixed"], np.zeros(len(s["fixed"])), E, I,
+                                           eolc.SolveOpts(precision=0))
+    assert info.status == eolc.OK
+    assert np.abs(v - vq).max() <= 1e-12 * np.abs(vq).max()
 
 
 def test_row_on_padded_dof_rejected(eolc):

@@ -942,6 +942,44 @@ class Forces:
         self.MDK = bsr_to_csr(self.ctx, MDK)
 
 
+class Constraints:
+    """Constraints (src/Constraints.h): fill() builds Aeq, beq, Aineq, bineq
+    as Constraints::fill does (Constraints.cpp:135-513), over the context's
+    DOFs (the extended layout on an EOL topology): the EOL nodes' rows and
+    the CD2 contact rows through eolc_constraint_rows, then the pinned DOFs'
+    unit rows with beq = 0.99 v + c (addFixed, :114-119, :472-496).  Row
+    order is the reference's: Aeq = EOL equalities, then pins; Aineq = EOL
+    inequalities, then contacts."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        self.hasFixed = False
+        self.hasCollisions = False
+        self.Aeq = self.beq = self.Aineq = self.bineq = None
+
+    def fill(self, x, u, v, tri, edges, eol_nodes, corner_id, cd_edge, preserve=None,
+             boxes=(), points=None, normals=None, fixed_dofs=(), fixed_vel=(),
+             threshold=1e-3, contacts=None):
+        """contacts: the CD2 contact list of x (None: eolc_cd2 on this
+        context).  v: current velocities (the pins' beq)."""
+        import scipy.sparse as sp
+        if contacts is None:
+            contacts = self.ctx.cd2(x, boxes, points, normals, threshold)
+        E, I = constraint_rows(x, u, tri, edges, eol_nodes, corner_id, cd_edge, preserve,
+                               boxes, normals, contacts)
+        nd = len(v)
+        fixed = _i32(fixed_dofs)
+        pins = sp.csr_matrix((np.ones(len(fixed)), (np.arange(len(fixed)), fixed)),
+                             shape=(len(fixed), nd))
+        self.Aeq = sp.vstack([E.csr(nd), pins]).tocsr()
+        self.beq = np.concatenate([E.rhs, 0.99 * _f64(v)[fixed] + _f64(fixed_vel)])
+        self.Aineq = I.csr(nd)
+        self.bineq = I.rhs.copy()
+        self.hasFixed = len(fixed) > 0
+        self.hasCollisions = I.m > 0
+        return self
+
+
 class GeneralizedSolver:
     """GeneralizedSolver (src/GeneralizedSolver.h): velocitySolve on the GPU,
     with or without contact rows."""

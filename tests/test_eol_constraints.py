@@ -185,3 +185,31 @@ def test_oracle_eol_step_keeps_rows():
         moved = np.flatnonzero(np.abs(u - u0).reshape(-1, 2).max(1) > 0)
         assert set(moved.tolist()) <= set(s["eol"].tolist())
     assert np.abs(v[3 * n:]).max() > 0  # material flows across the edge
+
+
+def test_constraints_mirror_builds_the_reference_rows():
+    """eolc.Constraints.fill: the EOL equalities then the pins' unit rows in
+    Aeq (beq = 0.99 v + c), the EOL inequalities then the contact rows in
+    Aineq, all in the extended layout."""
+    s = scenes.eol_edge_sheet(8)
+    ob, lb = _boxes(s)
+    rng = np.random.default_rng(9)
+    x = s["x"] + rng.normal(0, 1e-3, s["x"].size)
+    n, ne = s["n"], len(s["eol"])
+    v = rng.normal(0, 0.1, 3 * (n + ne))
+    fvel = rng.normal(0, 0.01, len(s["fixed"]))
+    con = O.cd2(x, s["tri"], [ob], threshold=1e-3)
+    lc = [eolc.Contact.from_buffer_copy(bytes(c)) for c in con]
+    C = eolc.Constraints(None).fill(x, s["X"], v, s["tri"], s["edges"], s["eol"], s["corner"],
+                                    s["cd"], s["preserve"], [lb], fixed_dofs=s["fixed"],
+                                    fixed_vel=fvel, contacts=lc)
+    Aeq, _, Ai, _ = R.constraint_rows(x, s["X"], s["tri"], s["edges"], s["eol"], s["corner"],
+                                      s["cd"], s["preserve"], [ob], None, con)
+    idx = eolc.eol_reference_index(n, ne)
+    me = Aeq.shape[0]
+    assert C.Aeq.shape[0] == me + len(s["fixed"]) and C.hasFixed and C.hasCollisions
+    assert np.abs((C.Aeq[:me][:, idx] - Aeq).toarray()).max() <= 1e-15
+    pins = C.Aeq[me:].toarray()
+    assert (pins[np.arange(len(s["fixed"])), s["fixed"]] == 1).all() and pins.sum() == len(s["fixed"])
+    assert np.array_equal(C.beq[me:], 0.99 * v[s["fixed"]] + fvel)
+    assert np.abs((C.Aineq[:, idx] - Ai).toarray()).max() <= 1e-15

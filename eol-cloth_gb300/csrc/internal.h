@@ -338,9 +338,11 @@ struct eolc_ctx {
 };
 
 namespace eolc {
-// Entry points that take positions or states of every block row (steps,
-// collisions, export, batches, contact rows) refuse topologies with EOL
-// nodes, whose Eulerian rows have no positions of their own.
+// Entry points that take positions or states of every block row (the plain
+// and contact steps, export, batches, the plain contact QP) refuse
+// topologies with EOL nodes, whose Eulerian rows have no positions of their
+// own; eolc_cd2 runs on the mesh nodes and eolc_step_eol / the general QP
+// take the extended layout.
 inline eolc_status refuse_eol(eolc_ctx *ctx) {
   if (ctx && ctx->topo.n_eol > 0) {
     ctx->err = "not available on a topology with EOL nodes";

@@ -910,7 +910,7 @@ def run_eol_step(args, local_rank, stream, steps=8, cpu_quads=16, cpu_steps=3):
         for k in range(steps + 2):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            contacts = ctx.cd2(x, [box], threshold=1e-3)
+            contacts = ctx.cd2(x, [box], threshold=1e-3, array=True)
             E, I = eolc.constraint_rows(x, u, sc["tri"], sc["edges"], sc["eol"], sc["corner"],
                                         sc["cd"], sc["preserve"], [box], None, contacts)
             info = ctx.step_eol(x, u, v, mat, GRAV, H, sc["fixed"], sc["fixed_vel"], E, I, opts)

@@ -27,7 +27,6 @@
 // 146-150; a mesh with one vertex per node has no seams).  Zero vectors stay
 // zero under normalisation, as with Eigen's normalized().
 #include <cmath>
-#include <map>
 #include <string>
 #include <utility>
 #include <vector>
@@ -176,51 +175,36 @@ extern "C" eolc_status eolc_constraint_rows(const eolc_eol_mesh *mesh, const eol
     return V3{{t[0], t[1], t[2]}};
   };
 
-  // node -> faces (ascending) and node -> edges (mesh.edges order), faces
-  // per edge
-  std::vector<int> nf_ptr(N + 1, 0), ne_ptr(N + 1, 0);
-  for (int t = 0; t < 3 * M.n_tri; ++t) ++nf_ptr[M.tri[t] + 1];
-  for (int t = 0; t < 2 * M.n_edges; ++t) ++ne_ptr[M.edges[t] + 1];
-  for (int a = 0; a < N; ++a) {
-    nf_ptr[a + 1] += nf_ptr[a];
-    ne_ptr[a + 1] += ne_ptr[a];
-  }
-  std::vector<int> nf(nf_ptr[N]), ne(ne_ptr[N]);
-  {
-    std::vector<int> fill(nf_ptr.begin(), nf_ptr.end() - 1);
-    for (int f = 0; f < M.n_tri; ++f)
-      for (int i = 0; i < 3; ++i) {
-        const int a = M.tri[3 * f + i];
-        nf[fill[a]++] = f;
-      }
-    std::vector<int> efill(ne_ptr.begin(), ne_ptr.end() - 1);
-    for (int e = 0; e < M.n_edges; ++e)
-      for (int i = 0; i < 2; ++i) {
-        const int a = M.edges[2 * e + i];
-        ne[efill[a]++] = e;
-      }
-  }
-  std::map<std::pair<int, int>, int> faces_of_edge;
+  // per EOL node (EoL_index k): its faces (ascending) and its edges
+  // (mesh.edges order).  An edge of EOL node k is a boundary edge when fewer
+  // than two of k's faces hold its other node.
+  std::vector<std::vector<int>> nf(M.n_eol), ne(M.n_eol);
   for (int f = 0; f < M.n_tri; ++f)
     for (int i = 0; i < 3; ++i) {
-      int a = M.tri[3 * f + i], b = M.tri[3 * f + (i + 1) % 3];
-      if (a > b) std::swap(a, b);
-      ++faces_of_edge[{a, b}];
+      const int k = eol_index[M.tri[3 * f + i]];
+      if (k >= 0) nf[k].push_back(f);
     }
-  auto boundary_edge = [&](int e) {
-    int a = M.edges[2 * e], b = M.edges[2 * e + 1];
-    if (a > b) std::swap(a, b);
-    auto it = faces_of_edge.find({a, b});
-    return it == faces_of_edge.end() || it->second < 2;
+  for (int e = 0; e < M.n_edges; ++e)
+    for (int i = 0; i < 2; ++i) {
+      const int k = eol_index[M.edges[2 * e + i]];
+      if (k >= 0) ne[k].push_back(e);
+    }
+  auto boundary_edge = [&](int k, int a, int e) {
+    const int b = M.edges[2 * e] == a ? M.edges[2 * e + 1] : M.edges[2 * e];
+    int cnt = 0;
+    for (const int f : nf[k]) {
+      const int *v = M.tri + 3 * f;
+      cnt += v[0] == b || v[1] == b || v[2] == b;
+    }
+    return cnt < 2;
   };
   auto face_normal = [&](int f) {
     const V3 x0 = X(M.tri[3 * f]), x1 = X(M.tri[3 * f + 1]), x2 = X(M.tri[3 * f + 2]);
     return normalized(cross(sub(x1, x0), sub(x2, x0)));
   };
-  auto node_normal = [&](int a) {
+  auto node_normal = [&](int k, int a) {
     V3 n{{0, 0, 0}};
-    for (int q = nf_ptr[a]; q < nf_ptr[a + 1]; ++q) {
-      const int f = nf[q];
+    for (const int f : nf[k]) {
       const int *v = M.tri + 3 * f;
       const int j = v[0] == a ? 0 : v[1] == a ? 1 : 2;
       const V3 e1 = sub(X(v[(j + 1) % 3]), X(a)), e2 = sub(X(v[(j + 2) % 3]), X(a));
@@ -228,11 +212,11 @@ extern "C" eolc_status eolc_constraint_rows(const eolc_eol_mesh *mesh, const eol
     }
     return normalized(n);
   };
-  auto flat = [&](int a, double limit) {
-    if (nf_ptr[a + 1] == nf_ptr[a]) return true;
-    const V3 n0 = normalized(face_normal(nf[nf_ptr[a]]));
-    for (int q = nf_ptr[a] + 1; q < nf_ptr[a + 1]; ++q) {
-      const V3 n1 = normalized(face_normal(nf[q]));
+  auto flat = [&](int k, double limit) {
+    if (nf[k].empty()) return true;
+    const V3 n0 = normalized(face_normal(nf[k][0]));
+    for (size_t q = 1; q < nf[k].size(); ++q) {
+      const V3 n1 = normalized(face_normal(nf[k][q]));
       const double c = std::fmin(std::fmax(dot(n0, n1), -1.0), 1.0);
       if (std::acos(c) > limit) return false;
     }
@@ -253,7 +237,7 @@ extern "C" eolc_status eolc_constraint_rows(const eolc_eol_mesh *mesh, const eol
       const V3 o1{{0.0, -nor.v[2], nor.v[1]}};
       const V3 o2 = normalized(normalized(cross(o1, nor)));
       const V3 mnor = scale(nor, -1.0);
-      if (flat(a, 0.5) || corner < n_points) {
+      if (flat(k, 0.5) || corner < n_points) {
         I.node_row(a, mnor);
         E.node_row(a, o1);
         E.node_row(a, o2);
@@ -265,8 +249,8 @@ extern "C" eolc_status eolc_constraint_rows(const eolc_eol_mesh *mesh, const eol
       continue;
     }
     const int cd = M.cd_edge[k];  // :263-415
-    if (flat(a, 0.1)) {
-      const V3 n = node_normal(a);
+    if (flat(k, 0.1)) {
+      const V3 n = node_normal(k, a);
       I.node_row(a, scale(n, -1.0));
       E.node_row(a, scale(cross(n, column(cd, 2)), -1.0));
     } else {
@@ -275,8 +259,8 @@ extern "C" eolc_status eolc_constraint_rows(const eolc_eol_mesh *mesh, const eol
     }
     const int dof[2] = {3 * (N + k), 3 * (N + k) + 1};
     int border = -1;
-    for (int q = ne_ptr[a]; q < ne_ptr[a + 1] && border < 0; ++q)
-      if (boundary_edge(ne[q])) border = ne[q];
+    for (size_t q = 0; q < ne[k].size() && border < 0; ++q)
+      if (boundary_edge(k, a, ne[k][q])) border = ne[k][q];
     double g[2];
     if (border >= 0) {
       const int o = M.edges[2 * border] == a ? M.edges[2 * border + 1] : M.edges[2 * border];
@@ -285,8 +269,7 @@ extern "C" eolc_status eolc_constraint_rows(const eolc_eol_mesh *mesh, const eol
       g[1] = d.second;
     } else {
       double t0 = 0, t1 = 0;
-      for (int q = ne_ptr[a]; q < ne_ptr[a + 1]; ++q) {
-        const int e = ne[q];
+      for (const int e : ne[k]) {
         if (!M.preserve || !M.preserve[e]) continue;
         const int n0 = M.edges[2 * e], n1 = M.edges[2 * e + 1];
         const bool far0 = std::sqrt(dot(U(n0), U(n0))) > std::sqrt(dot(U(n1), U(n1)));

@@ -490,9 +490,11 @@ class Context:
         return info
 
     def cd2(self, x, boxes=(), points=None, normals=None, threshold=1e-3, capacity=None,
-            raw=False):
+            raw=False, array=False):
         """CD2 contact list (point obstacles first, then each box); raw=True
-        returns the contacts' bytes (eolc_contact records, in order)."""
+        returns the contacts' bytes (eolc_contact records, in order),
+        array=True a ctypes array of them (no per-contact objects: pass it to
+        constraint_rows as is)."""
         x = _f64(x)
         boxes = list(boxes)
         barr = (Box * max(1, len(boxes)))(*boxes)
@@ -505,10 +507,13 @@ class Context:
         st = lib.eolc_cd2(self._h, _d(x), barr, len(boxes), _d(pts), _d(nrm), npts, threshold,
                           out, cap, ctypes.byref(n))
         if st == CAPACITY and capacity is None:
-            return self.cd2(x, boxes, points, normals, threshold, capacity=n.value, raw=raw)
+            return self.cd2(x, boxes, points, normals, threshold, capacity=n.value, raw=raw,
+                            array=array)
         self._check(st)
         if raw:
             return ctypes.string_at(out, ctypes.sizeof(Contact) * n.value)
+        if array:
+            return (Contact * n.value).from_buffer(out)
         return [out[k] for k in range(n.value)]
 
     # ---- OBJ export ------------------------------------------------------------
@@ -829,8 +834,11 @@ def constraint_rows(x, u, tri, edges, eol_nodes, corner_id, cd_edge, preserve=No
     barr = (Box * max(1, len(boxes)))(*boxes)
     pn = np.zeros(3) if point_normals is None else _f64(point_normals)
     npts = 0 if point_normals is None else len(pn.reshape(-1, 3))
-    contacts = list(contacts)
-    carr = (Contact * max(1, len(contacts)))(*contacts)
+    if isinstance(contacts, ctypes.Array) and len(contacts) > 0:
+        carr = contacts  # eolc_contact records already in one array
+    else:
+        contacts = list(contacts)
+        carr = (Contact * max(1, len(contacts)))(*contacts)
     cap_e, cap_i = 3 * len(eol) + 1, 3 * len(eol) + len(contacts) + 1
     while True:
         bufs = []

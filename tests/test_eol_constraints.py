@@ -71,6 +71,17 @@ def test_rows_flat_sheet_on_box_edge():
     n_kept = sum(1 for c in contacts if c.verts2[0] not in set(s["eol"].tolist()))
     assert C.shape[0] == ne + n_kept
     assert n_kept < len(contacts)
+    # the contacts as one ctypes array (eolc Context.cd2(array=True)) give the same rows
+    lc = [eolc.Contact.from_buffer_copy(bytes(c)) for c in contacts]
+    arr = (eolc.Contact * len(lc))(*lc)
+    _, lb = _boxes(s)
+    E1, I1 = eolc.constraint_rows(s["x"], s["X"], s["tri"], s["edges"], s["eol"], s["corner"],
+                                  s["cd"], s["preserve"], [lb], None, lc)
+    E2, I2 = eolc.constraint_rows(s["x"], s["X"], s["tri"], s["edges"], s["eol"], s["corner"],
+                                  s["cd"], s["preserve"], [lb], None, arr)
+    for a, b in ((E1, E2), (I1, I2)):
+        assert all(np.array_equal(p, q) for p, q in
+                   ((a.ptr, b.ptr), (a.col, b.col), (a.val, b.val), (a.rhs, b.rhs)))
 
 
 # jitter amplitudes that bend 11, 1 and 7 of the 11 EOL nodes past 0.1 rad

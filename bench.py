@@ -885,8 +885,8 @@ def run_eol_step(args, local_rank, stream, steps=8, cpu_quads=16, cpu_steps=3):
     Each step is CD2 (eolc_cd2), the rows of Constraints::fill
     (eolc_constraint_rows) and eolc_step_eol (forces with the EOL branches,
     the QP with the EOL equality and inequality rows and the contact rows,
-    x += h v, u += h vE), host arrays in and out, wall clock.  Sheets of 16
-    and 128 quads per side; CPU baseline: the oracle's step (its restated
+    x += h v, u += h vE; patch PCG inside the QP), host arrays in and out,
+    wall clock.  Sheets of 16 and 128 quads per side; CPU baseline: the oracle's step (its restated
     rows, EOL fill and exact active-set QP) on the 16-quad sheet."""
     import numpy as np
     import torch
@@ -896,7 +896,7 @@ def run_eol_step(args, local_rank, stream, steps=8, cpu_quads=16, cpu_steps=3):
     import oracle as O  # CPU side only: the baseline below
     import eol_ref
     mat = eolc.Material(**MAT)
-    opts = arm_opts(eolc, "jacobi", args.degree)
+    opts = arm_opts(eolc, "patch", args.degree)
     out = {}
     for q in (cpu_quads, 128):
         sc = S.eol_edge_sheet(q)
@@ -940,7 +940,7 @@ def run_eol_step(args, local_rank, stream, steps=8, cpu_quads=16, cpu_steps=3):
             cpu.append(time.perf_counter() - t0)
     out["workload"] = ("EOL sheet on a box edge (middle node column = EOL nodes), CD2 + "
                        "Constraints::fill rows + Cloth::step with the QP, mixed precision, "
-                       "Jacobi PCG inside the QP")
+                       "patch PCG inside the QP")
     out["cpu_baseline"] = {"value": 1.0 / float(np.median(cpu)), "unit": "steps/s", "cores": 1,
                            "kind": "port",
                            "sample": "oracle EOL steps 2-%d of the %d-quad sheet (exact "

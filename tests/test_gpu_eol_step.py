@@ -107,8 +107,8 @@ def test_qp_matches_oracle(eolc, precision):
     assert (li >= 0).all() and info.n_active == int((li > 0).sum())
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_steps_track_oracle(eolc, precision):
+@pytest.mark.parametrize("precision,precond", [(0, 0), (1, 0), (1, 3)])
+def test_steps_track_oracle(eolc, precision, precond):
     s, ctx, ob, lb = _setup(eolc)
     n, ne = s["n"], len(s["eol"])
     idx = eolc.eol_reference_index(n, ne)
@@ -116,7 +116,7 @@ def test_steps_track_oracle(eolc, precision):
     xg, ug, vg = s["x"].copy(), s["X"].copy(), np.zeros(3 * (n + ne))
     xo, uo, vo = s["x"].copy(), s["X"].copy(), np.zeros(3 * n + 2 * ne)
     tol = 1e-7 if precision == 0 else 1e-5
-    opts = eolc.SolveOpts(precision=precision)
+    opts = eolc.SolveOpts(precision=precision, precond=precond)  # Jacobi or patch PCG
     for k in range(4):
         E, I, _, _ = _rows_both(eolc, s, ctx, ob, lb, xg, ug)
         info = ctx.step_eol(xg, ug, vg, mat, g, h, s["fixed"], s["fixed_vel"], E, I, opts)

@@ -21,6 +21,11 @@ edge through the EOL nodes' Eulerian DOFs.
   the augmented Lagrangian's multipliers converge too slowly);
 * GeneralizedSolver.velocitySolve (eolc.py) with the reference's Aeq —
   pinned unit rows and the EOL rows together — equals the QP entry point;
+* EOL steps with the topology rebuilt before every step (as after each
+  remesh) equal the steps on one topology: bit for bit in FP64, within the
+  solve tolerance in mixed precision (the resident solver's patches are cut
+  from the material coordinates at the first solve after a topology change,
+  and the EOL nodes' material coordinates move every step);
 * a row on a padded Eulerian DOF is rejected.
 """
 import numpy as np
@@ -206,6 +211,36 @@ def test_generalized_solver_takes_eol_rows(eolc):
                                            eolc.SolveOpts(precision=0))
     assert info.status == eolc.OK
     assert np.abs(v - vq).max() <= 1e-12 * np.abs(vq).max()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_steps_after_topology_refresh(eolc, precision):
+    s, ctx, ob, lb = _setup(eolc)
+    n, ne = s["n"], len(s["eol"])
+    mat, g, h = eolc.Material(**scenes.material_c1()), scenes.GRAV, scenes.H
+    opts = eolc.SolveOpts(precision=precision)
+    runs = []
+    for refresh in (False, True):
+        c = eolc.Context(0)
+        c.set_topology_eol(n, s["tri"], s["hinge"], s["eol"])
+        x, u, v = s["x"].copy(), s["X"].copy(), np.zeros(3 * (n + ne))
+        for _ in range(3):
+            if refresh:
+                c.set_topology_eol(n, s["tri"], s["hinge"], s["eol"])
+            con = c.cd2(x, [lb], threshold=1e-3, array=True)
+            E, I = eolc.constraint_rows(x, u, s["tri"], s["edges"], s["eol"], s["corner"],
+                                        s["cd"], s["preserve"], [lb], None, con)
+            assert c.step_eol(x, u, v, mat, g, h, s["fixed"], s["fixed_vel"], E, I,
+                              opts).status == eolc.OK
+        runs.append((x, u, v))
+    if precision == 0:
+        for a, b in zip(*runs):
+            assert np.array_equal(a, b)
+    else:
+        (x0, u0, v0), (x1, u1, v1) = runs
+        vm = np.abs(v0).max()
+        assert np.abs(v1 - v0).max() <= 1e-5 * vm
+        assert max(np.abs(x1 - x0).max(), np.abs(u1 - u0).max()) <= 1e-5 * h * vm
 
 
 def test_row_on_padded_dof_rejected(eolc):

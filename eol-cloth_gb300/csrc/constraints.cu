@@ -16,8 +16,14 @@
 //     edge in Node::adje order, inside the mesh the normalised sum of the
 //     preserved edges' unit directions, each pointing to its end nearer the
 //     material origin (:389-403).
-// Then the CD2 contact rows of :422-468 that touch no EOL node.  The moving
-// obstacle terms (:165-172, :274-281) vanish: boxes here are at rest.
+// Then the CD2 contact rows of :422-468 that touch no EOL node.  A node on
+// a moving box (Box::v, angular then linear velocity, not zero) gets the
+// right-hand sides of :165-172 and :270-277: with xl = E1^-1 [x; 1],
+// et = Rigid::integrate(E1, v, h) (Rigid.cpp:79-111) and
+// xdot = (et xl - E1 xl) / h, each row's bineq / beq is its direction dotted
+// with xdot, signs as the reference writes them (the inequality rows of the
+// two orthogonal directions at a bent corner take +o xdot, every other
+// inequality -g xdot).  E1 is a rigid frame, so E1^-1 = [R' -R'p].
 //
 // Geometry follows ArcSim's definitions: face normal normalize((x1 - x0) x
 // (x2 - x0)) (mesh.cpp:135-139), node normal normal<WS> (geometry.cpp:
@@ -64,6 +70,83 @@ const int kEdgeAlong[12] = {4, 2, 2, 4, 0, 0, 4, 0, 2, 0, 2, 4};
 const int kCornerEdges[8][3] = {{0, 1, 4}, {0, 2, 5}, {1, 3, 7}, {2, 3, 9},
                                 {4, 6, 8}, {5, 6, 10}, {7, 8, 11}, {9, 10, 11}};
 constexpr int kBoxColumns = 20;  // 8 corners, then 12 edges
+
+// A box's motion over one step, for the moving-obstacle right-hand sides:
+// E1, its rigid inverse and et = Rigid::integrate(E1, v, h) = E1 phib, all
+// column-major 4x4.
+struct BoxMotion {
+  bool moving = false;
+  double E1[16], E1inv[16], et[16];
+};
+
+BoxMotion box_motion(const eolc_box &b, const double *vel, double h) {
+  BoxMotion m;
+  for (int k = 0; k < 16; ++k) m.E1[k] = b.E1[k];
+  if (!vel) return m;
+  const V3 w0{{vel[0], vel[1], vel[2]}}, v0{{vel[3], vel[4], vel[5]}};
+  m.moving = std::sqrt(dot(w0, w0)) != 0.0 || std::sqrt(dot(v0, v0)) != 0.0;
+  if (!m.moving) return m;
+  // rigid inverse [R' -R'p]
+  for (int k = 0; k < 16; ++k) m.E1inv[k] = 0.0;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) m.E1inv[4 * c + r] = b.E1[4 * r + c];
+  for (int r = 0; r < 3; ++r) {
+    double t = 0;
+    for (int k = 0; k < 3; ++k) t += b.E1[4 * r + k] * b.E1[12 + k];
+    m.E1inv[12 + r] = -t;
+  }
+  m.E1inv[15] = 1.0;
+  // phib of Rigid::integrate: translation h v, or the Rodrigues rotation
+  // with the screw's translation when |w| > 1e-10
+  double P[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+  for (int r = 0; r < 3; ++r) P[12 + r] = h * v0.v[r];
+  const double wlen = std::sqrt(dot(w0, w0));
+  if (wlen > 1e-10) {
+    const V3 w = divide(w0, wlen), v = divide(v0, wlen);
+    const double c = std::cos(wlen * h), sn = std::sin(wlen * h), c1 = 1.0 - c;
+    const double X = w.v[0], Y = w.v[1], Z = w.v[2];
+    const double R[3][3] = {{c + X * X * c1, -Z * sn + X * Y * c1, Y * sn + X * Z * c1},
+                            {Z * sn + X * Y * c1, c + Y * Y * c1, -X * sn + Y * Z * c1},
+                            {-Y * sn + X * Z * c1, X * sn + Y * Z * c1, c + Z * Z * c1}};
+    const V3 cc = cross(w, v);
+    V3 d;
+    for (int r = 0; r < 3; ++r) {
+      const double a0 = (r == 0 ? 1.0 : 0.0) - R[r][0], a1 = (r == 1 ? 1.0 : 0.0) - R[r][1],
+                   a2 = (r == 2 ? 1.0 : 0.0) - R[r][2];
+      d.v[r] = a0 * cc.v[0] + a1 * cc.v[1] + a2 * cc.v[2];
+    }
+    const double wv = dot(w, v);
+    for (int r = 0; r < 3; ++r) {
+      for (int c2 = 0; c2 < 3; ++c2) P[4 * c2 + r] = R[r][c2];
+      P[12 + r] = (wv * wlen * h) * w.v[r] + d.v[r];
+    }
+  }
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) {
+      double t = 0;
+      for (int k = 0; k < 4; ++k) t += m.E1[4 * k + r] * P[4 * c + k];
+      m.et[4 * c + r] = t;
+    }
+  return m;
+}
+
+// xdot = (et xl - E1 xl) / h with xl = E1^-1 [x; 1].
+V3 box_point_velocity(const BoxMotion &m, const V3 &x, double h) {
+  double xl[4];
+  for (int r = 0; r < 4; ++r)
+    xl[r] = m.E1inv[r] * x.v[0] + m.E1inv[4 + r] * x.v[1] + m.E1inv[8 + r] * x.v[2] +
+            m.E1inv[12 + r];
+  V3 out;
+  for (int r = 0; r < 3; ++r) {
+    double a = 0, b = 0;
+    for (int k = 0; k < 4; ++k) {
+      a += m.et[4 * k + r] * xl[k];
+      b += m.E1[4 * k + r] * xl[k];
+    }
+    out.v[r] = (a - b) / h;
+  }
+  return out;
+}
 
 // Constraint table (Constraints::updateTable, :76-105): 9 values per column.
 std::vector<double> constraint_table(const eolc_box *boxes, int n_boxes, const double *pn,
@@ -130,11 +213,13 @@ eolc_status bad(const char * /*reason*/) { return EOLC_BAD_ARG; }
 }  // namespace
 
 extern "C" eolc_status eolc_constraint_rows(const eolc_eol_mesh *mesh, const eolc_box *boxes,
-                                            int n_boxes, const double *point_normals_h,
-                                            int n_points, const eolc_contact *contacts,
-                                            int n_contacts, eolc_rows *eq, eolc_rows *ineq) {
+                                            const double *box_velocity_h, int n_boxes,
+                                            const double *point_normals_h, int n_points,
+                                            const eolc_contact *contacts, int n_contacts,
+                                            double h, eolc_rows *eq, eolc_rows *ineq) {
   if (!mesh || !eq || !ineq || n_boxes < 0 || n_points < 0 || n_contacts < 0)
     return bad("null argument");
+  if (box_velocity_h && !(h > 0)) return bad("moving boxes need h > 0");
   const eolc_eol_mesh &M = *mesh;
   const int N = M.n_nodes;
   if (N <= 0 || M.n_tri <= 0 || M.n_edges < 0 || M.n_eol < 0 || M.n_eol > N || !M.x || !M.u ||
@@ -168,6 +253,18 @@ extern "C" eolc_status eolc_constraint_rows(const eolc_eol_mesh *mesh, const eol
     if (a < 0 || a >= N || b < 0 || b >= N || a == b) return bad("bad edge");
   }
   const std::vector<double> table = constraint_table(boxes, n_boxes, point_normals_h, n_points);
+  std::vector<BoxMotion> motion(n_boxes);
+  for (int b = 0; b < n_boxes; ++b)
+    motion[b] = box_motion(boxes[b], box_velocity_h ? box_velocity_h + 6 * b : nullptr, h);
+  // the velocity of node a's point on the box of table column col; false
+  // (no right-hand side) for point obstacles and boxes at rest
+  auto xdot_of = [&](int col, int a, V3 &xd) {
+    if (col < n_points) return false;
+    const BoxMotion &m = motion[(col - n_points) / kBoxColumns];
+    if (!m.moving) return false;
+    xd = box_point_velocity(m, V3{{M.x[3 * a], M.x[3 * a + 1], M.x[3 * a + 2]}}, h);
+    return true;
+  };
   auto X = [&](int a) { return V3{{M.x[3 * a], M.x[3 * a + 1], M.x[3 * a + 2]}}; };
   auto U = [&](int a) { return V3{{M.u[2 * a], M.u[2 * a + 1], 0.0}}; };
   auto column = [&](int col, int r) {
@@ -237,25 +334,31 @@ extern "C" eolc_status eolc_constraint_rows(const eolc_eol_mesh *mesh, const eol
       const V3 o1{{0.0, -nor.v[2], nor.v[1]}};
       const V3 o2 = normalized(normalized(cross(o1, nor)));
       const V3 mnor = scale(nor, -1.0);
+      V3 xd;
+      const bool mv = xdot_of(corner, a, xd);
+      auto rhs = [&](const V3 &g, double sign) { return mv ? sign * dot(g, xd) : 0.0; };
       if (flat(k, 0.5) || corner < n_points) {
-        I.node_row(a, mnor);
-        E.node_row(a, o1);
-        E.node_row(a, o2);
+        I.node_row(a, mnor, rhs(nor, -1.0));
+        E.node_row(a, o1, rhs(o1, 1.0));
+        E.node_row(a, o2, rhs(o2, 1.0));
       } else {
-        I.node_row(a, mnor);
-        I.node_row(a, scale(o1, -1.0));
-        I.node_row(a, scale(o2, -1.0));
+        I.node_row(a, mnor, rhs(nor, -1.0));
+        I.node_row(a, scale(o1, -1.0), rhs(o1, 1.0));
+        I.node_row(a, scale(o2, -1.0), rhs(o2, 1.0));
       }
       continue;
     }
     const int cd = M.cd_edge[k];  // :263-415
+    V3 xd;
+    const bool mv = xdot_of(cd, a, xd);
+    auto rhs = [&](const V3 &g) { return mv ? -dot(g, xd) : 0.0; };
     if (flat(k, 0.1)) {
-      const V3 n = node_normal(k, a);
-      I.node_row(a, scale(n, -1.0));
-      E.node_row(a, scale(cross(n, column(cd, 2)), -1.0));
+      const V3 n = node_normal(k, a), fc = cross(n, column(cd, 2));
+      I.node_row(a, scale(n, -1.0), rhs(n));
+      E.node_row(a, scale(fc, -1.0), rhs(fc));
     } else {
-      I.node_row(a, scale(column(cd, 0), -1.0));
-      I.node_row(a, scale(column(cd, 1), -1.0));
+      I.node_row(a, scale(column(cd, 0), -1.0), rhs(column(cd, 0)));
+      I.node_row(a, scale(column(cd, 1), -1.0), rhs(column(cd, 1)));
     }
     const int dof[2] = {3 * (N + k), 3 * (N + k) + 1};
     int border = -1;

@@ -219,9 +219,10 @@ def load_library(path=LIB_PATH):
     L.eolc_velocity_solve_qp.argtypes = [_V, _D, _I, _D, ctypes.c_int, ctypes.POINTER(Rows),
                                          ctypes.POINTER(Rows), ctypes.POINTER(SolveOpts), _D, _D,
                                          _D, ctypes.POINTER(IneqInfo)]
-    L.eolc_constraint_rows.argtypes = [ctypes.POINTER(EolMesh), ctypes.POINTER(Box),
+    L.eolc_constraint_rows.argtypes = [ctypes.POINTER(EolMesh), ctypes.POINTER(Box), _D,
                                        ctypes.c_int, _D, ctypes.c_int, ctypes.c_void_p,
-                                       ctypes.c_int, ctypes.POINTER(Rows), ctypes.POINTER(Rows)]
+                                       ctypes.c_int, ctypes.c_double, ctypes.POINTER(Rows),
+                                       ctypes.POINTER(Rows)]
     L.eolc_step_eol.argtypes = [_V, _D, _D, _D, ctypes.POINTER(Material), _D, ctypes.c_double,
                                 _I, _D, ctypes.c_int, ctypes.POINTER(Rows), ctypes.POINTER(Rows),
                                 ctypes.POINTER(SolveOpts), ctypes.POINTER(IneqInfo)]
@@ -818,9 +819,11 @@ class RowSet:
 
 
 def constraint_rows(x, u, tri, edges, eol_nodes, corner_id, cd_edge, preserve=None, boxes=(),
-                    point_normals=None, contacts=()):
+                    point_normals=None, contacts=(), box_velocity=None, h=0.0):
     """Constraints::fill for an EOL mesh (eolc_constraint_rows, host only):
-    (equality RowSet, inequality RowSet) over the extended layout."""
+    (equality RowSet, inequality RowSet) over the extended layout.
+    box_velocity: None (boxes at rest) or (n_boxes, 6) Box::v, angular then
+    linear; h: the step (needed with moving boxes)."""
     x, u, tri, edges = _f64(x), _f64(u), _i32(tri), _i32(edges)
     eol, cid, cde = _i32(eol_nodes), _i32(corner_id), _i32(cd_edge)
     pres = None if preserve is None else _i32(preserve)
@@ -832,6 +835,7 @@ def constraint_rows(x, u, tri, edges, eol_nodes, corner_id, cd_edge, preserve=No
                    _i(cid if len(cid) else one), _i(cde if len(cde) else one), len(eol))
     boxes = list(boxes)
     barr = (Box * max(1, len(boxes)))(*boxes)
+    bv = None if box_velocity is None or not boxes else _f64(box_velocity)
     pn = np.zeros(3) if point_normals is None else _f64(point_normals)
     npts = 0 if point_normals is None else len(pn.reshape(-1, 3))
     if isinstance(contacts, ctypes.Array) and len(contacts) > 0:
@@ -846,8 +850,9 @@ def constraint_rows(x, u, tri, edges, eol_nodes, corner_id, cd_edge, preserve=No
             ptr, col = np.zeros(cap + 1, np.int32), np.zeros(9 * cap, np.int32)
             val, rhs = np.zeros(9 * cap), np.zeros(cap)
             bufs.append((Rows(0, cap, _i(ptr), _i(col), _d(val), _d(rhs)), ptr, col, val, rhs))
-        st = lib.eolc_constraint_rows(ctypes.byref(mesh), barr, len(boxes), _d(pn), npts,
-                                      ctypes.cast(carr, ctypes.c_void_p), len(contacts),
+        st = lib.eolc_constraint_rows(ctypes.byref(mesh), barr, _d(bv) if bv is not None else None,
+                                      len(boxes), _d(pn), npts,
+                                      ctypes.cast(carr, ctypes.c_void_p), len(contacts), h,
                                       ctypes.byref(bufs[0][0]), ctypes.byref(bufs[1][0]))
         if st == CAPACITY:
             cap_e, cap_i = max(cap_e, bufs[0][0].n_rows), max(cap_i, bufs[1][0].n_rows)
@@ -967,14 +972,15 @@ class Constraints:
 
     def fill(self, x, u, v, tri, edges, eol_nodes, corner_id, cd_edge, preserve=None,
              boxes=(), points=None, normals=None, fixed_dofs=(), fixed_vel=(),
-             threshold=1e-3, contacts=None):
+             threshold=1e-3, contacts=None, box_velocity=None, h=0.0):
         """contacts: the CD2 contact list of x (None: eolc_cd2 on this
-        context).  v: current velocities (the pins' beq)."""
+        context).  v: current velocities (the pins' beq).  box_velocity, h:
+        moving boxes (Box::v per box) and the step."""
         import scipy.sparse as sp
         if contacts is None:
             contacts = self.ctx.cd2(x, boxes, points, normals, threshold)
         E, I = constraint_rows(x, u, tri, edges, eol_nodes, corner_id, cd_edge, preserve,
-                               boxes, normals, contacts)
+                               boxes, normals, contacts, box_velocity, h)
         nd = len(v)
         fixed = _i32(fixed_dofs)
         pins = sp.csr_matrix((np.ones(len(fixed)), (np.arange(len(fixed)), fixed)),

@@ -496,14 +496,18 @@ typedef struct {
  * skipping contacts on EOL nodes.  The constraint table (:40-105) comes from
  * the point obstacles' normals and the boxes: columns n_points + 20 b + p
  * (corner p) and n_points + 20 b + 8 + e (edge e), the numbering of
- * Box.cpp's tables.  Obstacles are static (eolc_box has no velocity), so
- * every right-hand side is 0, as the reference's for boxes at rest.
- * Columns use the extended layout (eolc_rows).  Host only.  EOLC_CAPACITY
- * when eq or ineq is too small (n_rows has the need). */
+ * Box.cpp's tables.  box_velocity_h (may be NULL: boxes at rest): per box
+ * Box::v, the angular then the linear velocity (6 values); a node on a
+ * moving box gets the right-hand sides of :165-172 and :270-277 (its point's
+ * velocity over the step h, Rigid::integrate, dotted with each row's
+ * direction); every other right-hand side is 0.  Columns use the extended
+ * layout (eolc_rows).  Host only.  EOLC_CAPACITY when eq or ineq is too small
+ * (n_rows has the need). */
 eolc_status eolc_constraint_rows(const eolc_eol_mesh *mesh, const eolc_box *boxes,
-                                 int n_boxes, const double *point_normals_h,
-                                 int n_points, const eolc_contact *contacts,
-                                 int n_contacts, eolc_rows *eq, eolc_rows *ineq);
+                                 const double *box_velocity_h, int n_boxes,
+                                 const double *point_normals_h, int n_points,
+                                 const eolc_contact *contacts, int n_contacts,
+                                 double h, eolc_rows *eq, eolc_rows *ineq);
 
 /* ---- Cloth::step with collisions (Cloth.cpp:359-413, non-EOL, no remesh) --
  * One implicit-Euler step with the contact QP, on host buffers like

@@ -2,9 +2,9 @@
 (tests/ compare the library against it; nothing in the product imports it).
 
 constraint_rows() restates Constraints::fill for a mesh with EOL nodes
-(Constraints.cpp:135-468, static obstacles) in the reference's DOF layout:
-the 3N Lagrangian DOFs, then two Eulerian DOFs per EOL node at 3N + 2k
-(EoL_index k).  It reads the mesh the way ArcSim's objects hold it:
+(Constraints.cpp:135-468, boxes at rest or moving) in the reference's DOF
+layout: the 3N Lagrangian DOFs, then two Eulerian DOFs per EOL node at
+3N + 2k (EoL_index k).  It reads the mesh the way ArcSim's objects hold it:
 
   * Vert::adjf of a node = its faces in ascending order (Mesh::add(Face),
     mesh.cpp:365-378, appends each face to its vertices' lists);
@@ -19,7 +19,11 @@ the 3N Lagrangian DOFs, then two Eulerian DOFs per EOL node at 3N + 2k
 
 The constraint table follows Constraints::updateTable (:76-105) with the box
 tables of Box.cpp:25-72 (face normals rotated by E1, corner normals from the
-three edges' six faces, per edge its two faces and the face along it).
+three edges' six faces, per edge its two faces and the face along it).  A
+node on a moving box (Box::v = (w, v) not zero) gets the right-hand sides of
+:165-172 and :270-277 from its point's velocity over the step,
+xdot = (Rigid::integrate(E1, Box::v, h) xl - E1 xl) / h with xl = E1^-1 x
+(Rigid.cpp:79-111, restated with numpy's matrix products).
 
 solve_qp_eq() extends qp_ref.solve_qp with general equality rows: a primal
 active-set method on the sparse KKT system whose working set always holds
@@ -86,6 +90,32 @@ def constraint_table(boxes, point_normals):
     return np.array(cols, np.float64).reshape(-1, 9)
 
 
+def rigid_integrate(E0, phi, h):
+    """Rigid::integrate (Rigid.cpp:79-111): E0 times the screw motion of
+    phi = (w, v) over h (Rodrigues rotation when |w| > 1e-10)."""
+    w, v = np.array(phi[:3], float), np.array(phi[3:], float)
+    P = np.eye(4)
+    P[:3, 3] = h * v
+    wlen = np.linalg.norm(w)
+    if wlen > 1e-10:
+        w, v = w / wlen, v / wlen
+        K = np.array([[0, -w[2], w[1]], [w[2], 0, -w[0]], [-w[1], w[0], 0]])
+        c, s = np.cos(wlen * h), np.sin(wlen * h)
+        R = c * np.eye(3) + s * K + (1 - c) * np.outer(w, w)
+        P[:3, :3] = R
+        P[:3, 3] = (w @ v) * wlen * h * w + (np.eye(3) - R) @ np.cross(w, v)
+    return E0 @ P
+
+
+def point_velocity(E1, phi, h, x):
+    """xdot of Constraints.cpp:168-170 for a point x on a moving box."""
+    Einv = np.eye(4)
+    Einv[:3, :3] = E1[:3, :3].T
+    Einv[:3, 3] = -E1[:3, :3].T @ E1[:3, 3]
+    xl = Einv @ np.append(np.asarray(x, float), 1.0)
+    return ((rigid_integrate(E1, phi, h) @ xl - E1 @ xl) / h)[:3]
+
+
 class _Mesh:
     """The ArcSim adjacency that Constraints::fill walks."""
 
@@ -141,19 +171,33 @@ class _Mesh:
 
 
 def constraint_rows(x, u, tri, edges, eol_nodes, corner_id, cd_edge, preserve=None, boxes=(),
-                    point_normals=None, contacts=()):
+                    point_normals=None, contacts=(), box_velocity=None, h=0.0):
     """(Aeq, beq, Aineq, bineq) of Constraints::fill without the pins, over
-    the reference's 3N + 2E DOFs, rows in the reference's order."""
+    the reference's 3N + 2E DOFs, rows in the reference's order.
+    box_velocity: None or per box Box::v (w, v); h: the step."""
     M = _Mesh(x, u, tri, edges, preserve)
     N = len(M.x)
     n_eol = len(eol_nodes)
     eol_index = {int(a): k for k, a in enumerate(eol_nodes)}
     n_points = 0 if point_normals is None else len(np.asarray(point_normals).reshape(-1, 3))
-    T = constraint_table(list(boxes), point_normals)
-    eq, iq = [], []
+    boxes = list(boxes)
+    T = constraint_table(boxes, point_normals)
+    eq, iq, beq, bineq = [], [], [], []
 
-    def node_row(rows, a, g):
+    def xdot(col, a):
+        """The node's point velocity on the moving box of column col, or None."""
+        if col < n_points or box_velocity is None:
+            return None
+        b = (col - n_points) // 20
+        phi = np.asarray(box_velocity, float).reshape(-1, 6)[b]
+        if np.linalg.norm(phi[:3]) == 0.0 and np.linalg.norm(phi[3:]) == 0.0:
+            return None
+        E1 = np.array(list(boxes[b].E1)).reshape(4, 4, order="F")
+        return point_velocity(E1, phi, h, M.x[a])
+
+    def node_row(rows, a, g, value=0.0):
         rows.append([(3 * a + c, g[c]) for c in range(3)])
+        (beq if rows is eq else bineq).append(value)
 
     for a in range(N):
         if a not in eol_index:
@@ -164,24 +208,28 @@ def constraint_rows(x, u, tri, edges, eol_nodes, corner_id, cd_edge, preserve=No
             nor = list(T[cid, 0:3])
             o1 = [0.0, -nor[2], nor[1]]
             o2 = _normalize(_normalize(_cross(o1, nor)))
+            xd = xdot(cid, a)
+            r = (lambda g, sgn: 0.0 if xd is None else sgn * float(np.dot(g, xd)))
             if M.flat(a, 0.5) or cid < n_points:
-                node_row(iq, a, [-c for c in nor])
-                node_row(eq, a, o1)
-                node_row(eq, a, o2)
+                node_row(iq, a, [-c for c in nor], value=r(nor, -1))
+                node_row(eq, a, o1, value=r(o1, 1))
+                node_row(eq, a, o2, value=r(o2, 1))
             else:
-                node_row(iq, a, [-c for c in nor])
-                node_row(iq, a, [-c for c in o1])
-                node_row(iq, a, [-c for c in o2])
+                node_row(iq, a, [-c for c in nor], value=r(nor, -1))
+                node_row(iq, a, [-c for c in o1], value=r(o1, 1))
+                node_row(iq, a, [-c for c in o2], value=r(o2, 1))
             continue
         cd = int(cd_edge[k])                               # :263-415
+        xd = xdot(cd, a)
+        r = (lambda g: 0.0 if xd is None else -float(np.dot(g, xd)))
         if M.flat(a, 0.1):
             n = M.node_n(a)
-            node_row(iq, a, [-c for c in n])
             fc = _cross(n, list(T[cd, 6:9]))
-            node_row(eq, a, [-c for c in fc])
+            node_row(iq, a, [-c for c in n], value=r(n))
+            node_row(eq, a, [-c for c in fc], value=r(fc))
         else:
-            node_row(iq, a, [-c for c in T[cd, 0:3]])
-            node_row(iq, a, [-c for c in T[cd, 3:6]])
+            node_row(iq, a, [-c for c in T[cd, 0:3]], value=r(T[cd, 0:3]))
+            node_row(iq, a, [-c for c in T[cd, 3:6]], value=r(T[cd, 3:6]))
         bnd = [e for e in M.adje[a] if M.boundary[e]]
         if bnd:
             e = bnd[0]
@@ -201,6 +249,7 @@ def constraint_rows(x, u, tri, edges, eol_nodes, corner_id, cd_edge, preserve=No
                 t = [t[0] + d[0], t[1] + d[1]]
             g = _normalize(t)
         eq.append([(3 * N + 2 * k, g[0]), (3 * N + 2 * k + 1, g[1])])
+        beq.append(0.0)
     for c in contacts:                                     # :422-468
         if c.count1 == 3 and c.count2 == 1:
             terms = [(c.verts2[0], [-v for v in c.nor1])]
@@ -213,6 +262,7 @@ def constraint_rows(x, u, tri, edges, eol_nodes, corner_id, cd_edge, preserve=No
         if any(int(vtx) in eol_index for vtx, _ in terms):
             continue
         iq.append([(3 * int(vtx) + i, g[i]) for vtx, g in terms for i in range(3)])
+        bineq.append(0.0)
     n_dofs = 3 * N + 2 * n_eol
 
     def csr(rows):
@@ -221,7 +271,7 @@ def constraint_rows(x, u, tri, edges, eol_nodes, corner_id, cd_edge, preserve=No
         v = [g for row in rows for _, g in row]
         return sp.csr_matrix((v, (r, cidx)), shape=(len(rows), n_dofs))
 
-    return csr(eq), np.zeros(len(eq)), csr(iq), np.zeros(len(iq))
+    return csr(eq), np.array(beq, float), csr(iq), np.array(bineq, float)
 
 
 def solve_qp_eq(A, b, fixed_dofs, beq, Aeq, e, C, d, max_iter=None):

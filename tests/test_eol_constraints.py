@@ -129,7 +129,8 @@ def test_rows_capacity_and_bad_arguments():
                  np.zeros(9 * max(cap, 1)), np.zeros(max(cap, 1)))
             bufs.append((eolc.Rows(0, cap, eolc._i(a[0]), eolc._i(a[1]), eolc._d(a[2]),
                                    eolc._d(a[3])), a))
-        st = eolc.lib.eolc_constraint_rows(mesh, barr, 1, None, 0, None, 0, bufs[0][0], bufs[1][0])
+        st = eolc.lib.eolc_constraint_rows(mesh, barr, None, 1, None, 0, None, 0, 0.0, bufs[0][0],
+                                           bufs[1][0])
         return st, bufs[0][0].n_rows, bufs[1][0].n_rows, bufs
 
     st, me, mi, _ = call(100, 100)
@@ -224,3 +225,57 @@ def test_constraints_mirror_builds_the_reference_rows():
     assert (pins[np.arange(len(s["fixed"])), s["fixed"]] == 1).all() and pins.sum() == len(s["fixed"])
     assert np.array_equal(C.beq[me:], 0.99 * v[s["fixed"]] + fvel)
     assert np.abs((C.Aineq[:, idx] - Ai).toarray()).max() <= 1e-15
+
+
+@pytest.mark.parametrize("amp", [0.0, 0.004, 0.05])
+def test_rows_on_moving_boxes(amp):
+    """Boxes with Box::v (spinning and translating): the right-hand sides of
+    Constraints.cpp:165-172 and :270-277 on edge nodes (flat and bent) and
+    corner nodes (flat and bent), against the oracle's Rigid::integrate and
+    point velocities; a box at rest keeps zero right-hand sides."""
+    s = scenes.eol_edge_sheet(10)
+    rng = np.random.default_rng(11)
+    x = s["x"] + rng.normal(0, amp, s["x"].size)
+    ne = len(s["eol"])
+    corner = s["corner"].copy()
+    corner[0], corner[-1] = 20 + 5, 20 + 7           # corners of the second box
+    cd = s["cd"].copy()
+    ob0, lb0 = _boxes(s, rot=0.2)
+    ob1, lb1 = _boxes(s, rot=-0.4)
+    vel = np.array([[0.3, -0.2, 0.5, 0.05, 0.02, -0.1],   # box 0: spin and drift
+                    [0.0, 0.0, 0.0, 0.0, 0.0, 0.2]])      # box 1: translation only
+    h = scenes.H
+    Aeq, beq, Ai, bi = R.constraint_rows(x, s["X"], s["tri"], s["edges"], s["eol"], corner, cd,
+                                         s["preserve"], [ob0, ob1], None, (), vel, h)
+    E, I = eolc.constraint_rows(x, s["X"], s["tri"], s["edges"], s["eol"], corner, cd,
+                                s["preserve"], [lb0, lb1], None, (), vel, h)
+    idx = eolc.eol_reference_index(s["n"], ne)
+    nd = 3 * (s["n"] + ne)
+    assert np.abs((E.csr(nd)[:, idx] - Aeq).toarray()).max() <= 1e-15
+    assert np.abs((I.csr(nd)[:, idx] - Ai).toarray()).max() <= 1e-15
+    scale = max(np.abs(beq).max(), np.abs(bi).max())
+    assert scale > 0.01                                # the motion reaches the rows
+    assert np.abs(E.rhs - beq).max() <= 1e-13 * scale
+    assert np.abs(I.rhs - bi).max() <= 1e-13 * scale
+    # the same boxes at rest: zero right-hand sides
+    E0, I0 = eolc.constraint_rows(x, s["X"], s["tri"], s["edges"], s["eol"], corner, cd,
+                                  s["preserve"], [lb0, lb1], None, (), np.zeros((2, 6)), h)
+    assert not E0.rhs.any() and not I0.rhs.any()
+
+
+def test_rigid_integrate_matches_the_exponential_map():
+    """The oracle's Rigid::integrate is the rigid motion exp(h [w v]) applied
+    after E0 (checked against scipy's matrix exponential of the twist)."""
+    import scipy.linalg as sl
+    rng = np.random.default_rng(2)
+    for _ in range(5):
+        phi = rng.normal(size=6)
+        E0 = np.eye(4)
+        E0[:3, :3] = sl.expm(np.cross(np.eye(3), rng.normal(size=3)))
+        E0[:3, 3] = rng.normal(size=3)
+        w, v = phi[:3], phi[3:]
+        T = np.zeros((4, 4))
+        T[:3, :3] = np.cross(np.eye(3), w)
+        T[:3, 3] = v
+        h = 0.01
+        assert np.abs(R.rigid_integrate(E0, phi, h) - E0 @ sl.expm(h * T)).max() <= 1e-12

@@ -21,6 +21,10 @@ edge through the EOL nodes' Eulerian DOFs.
   the augmented Lagrangian's multipliers converge too slowly);
 * GeneralizedSolver.velocitySolve (eolc.py) with the reference's Aeq —
   pinned unit rows and the EOL rows together — equals the QP entry point;
+* steps on a moving box (Box::v: a spin and a lift), whose rows carry the
+  moving-obstacle right-hand sides, track the oracle (FP64 solved to rel_tol
+  1e-10: the QP stops on its infeasibility, 10 rel_tol max|v|, which with
+  non-zero right-hand sides leaves ~1e-6 of max|v| at rel_tol 1e-8);
 * EOL steps with the topology rebuilt before every step (as after each
   remesh) equal the steps on one topology: bit for bit in FP64, within the
   solve tolerance in mixed precision (the resident solver's patches are cut
@@ -211,6 +215,37 @@ def test_generalized_solver_takes_eol_rows(eolc):
                                            eolc.SolveOpts(precision=0))
     assert info.status == eolc.OK
     assert np.abs(v - vq).max() <= 1e-12 * np.abs(vq).max()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_steps_on_moving_box(eolc, precision):
+    s, ctx, ob, lb = _setup(eolc)
+    n, ne = s["n"], len(s["eol"])
+    idx = eolc.eol_reference_index(n, ne)
+    vel = np.array([0.0, 0.2, 0.0, 0.0, 0.0, 0.05])  # spin about y, lift 5 cm/s
+    mat, mat_o, g, h = eolc.Material(**scenes.material_c1()), O.material(), scenes.GRAV, scenes.H
+    xg, ug, vg = s["x"].copy(), s["X"].copy(), np.zeros(3 * (n + ne))
+    xo, uo, vo = s["x"].copy(), s["X"].copy(), np.zeros(3 * n + 2 * ne)
+    tol = 1e-7 if precision == 0 else 1e-5
+    opts = eolc.SolveOpts(precision=precision, rel_tol=1e-10 if precision == 0 else 1e-8)
+    for k in range(3):
+        con = ctx.cd2(xg, [lb], threshold=1e-3, array=True)
+        E, I = eolc.constraint_rows(xg, ug, s["tri"], s["edges"], s["eol"], s["corner"], s["cd"],
+                                    s["preserve"], [lb], None, con, vel[None, :], h)
+        assert np.abs(E.rhs).max() > 0 and np.abs(I.rhs).max() > 0
+        info = ctx.step_eol(xg, ug, vg, mat, g, h, s["fixed"], s["fixed_vel"], E, I, opts)
+        assert info.status == eolc.OK
+        rows = R.constraint_rows(xo, uo, s["tri"], s["edges"], s["eol"], s["corner"], s["cd"],
+                                 s["preserve"], [ob], None,
+                                 O.cd2(xo, s["tri"], [ob], threshold=1e-3), vel[None, :], h)
+        R.step(xo, uo, vo, s["tri"], s["hinge"], s["eol"], mat_o, g, h, s["fixed"],
+               s["fixed_vel"], rows)
+        vm = np.abs(vo).max()
+        ev = np.abs(vg[idx] - vo).max() / vm
+        ex = np.abs(xg - xo).max() / (h * vm)
+        eu = np.abs(ug - uo).max() / (h * vm)
+        print("moving box step %d: v %.2e x %.2e u %.2e" % (k, ev, ex, eu))
+        assert ev <= tol and ex <= tol and eu <= tol
 
 
 @pytest.mark.parametrize("precision", [0, 1])

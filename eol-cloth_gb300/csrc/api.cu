@@ -672,12 +672,15 @@ eolc_status eolc_attach_preconditioner(eolc_ctx *ctx, eolc_lpc *lpc) {
 eolc_status eolc_set_learned_refresh(eolc_ctx *ctx, int solves) {
   if (!ctx || solves < 1) return EOLC_BAD_ARG;
   ctx->lpc_refresh = solves;
+  ctx->lpc_cached = nullptr;  // the count restarts: the next solve runs the network
+  ctx->lpc_uses = 0;
   return EOLC_OK;
 }
 
 eolc_status eolc_set_coarse_refresh(eolc_ctx *ctx, int solves) {
   if (!ctx || solves < 1) return EOLC_BAD_ARG;
   ctx->coarse_refresh = solves;
+  coarse_update_next(ctx->pwork);  // the count restarts at the next solve
   return EOLC_OK;
 }
 

@@ -211,6 +211,8 @@ eolc_status batch_read_records(BatchSolveWork *w, std::vector<BatchRecord> &out,
 enum class ResidentPC { kJacobi, kPatch, kLearned };
 struct PatchWork;
 void free_patch_work(PatchWork *w);
+// The next resident solve updates the coarse inverse (eolc_set_coarse_refresh).
+void coarse_update_next(PatchWork *w);
 bool resident_fits(PatchWork *&w, const DevTopology &T, const double *X_d, cudaStream_t s);
 eolc_status run_pcg_resident(PatchWork *&w, const PcgArgs &a, ResidentPC mode, int degree,
                              const float *Gm, eolc_solve_info *info, cudaStream_t s,

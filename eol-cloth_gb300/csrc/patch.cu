@@ -2382,6 +2382,12 @@ eolc_status patch_plan(PatchWork *w, const DevTopology &Tp, const double *X_d, i
 
 }  // namespace
 
+// The next resident solve updates the coarse inverse (from the current one)
+// whatever its age; no effect before the first coarse build.
+void coarse_update_next(PatchWork *w) {
+  if (w && w->coarse_age >= 0) w->coarse_age = 1 << 20;
+}
+
 bool resident_fits(PatchWork *&w, const DevTopology &Tp, const double *X_d, cudaStream_t s) {
   int dev = 0, n_sm = 0;
   cudaGetDevice(&dev);

@@ -600,14 +600,16 @@ eolc_status eolc_attach_preconditioner(eolc_ctx *ctx, eolc_lpc *lpc);
 /* Evaluate the attached network every `solves` learned solves (default 1)
  * and keep its G in between (a lagged preconditioner: any symmetric positive
  * definite G leaves PCG exact, and the Jacobi fallback still bounds the
- * iterations).  Applies to the shared-memory-resident solve; re-attaching a
- * network (eolc_attach_preconditioner) forces a new evaluation. */
+ * iterations).  Applies to the shared-memory-resident solve.  Every call
+ * restarts the count: the next solve evaluates the network (as does
+ * re-attaching one, eolc_attach_preconditioner). */
 eolc_status eolc_set_learned_refresh(eolc_ctx *ctx, int solves);
 /* Update the coarse operator of the two-level patch preconditioner (its
  * assembly and the Newton-Schulz update of its inverse) every `solves`
  * EOLC_PC_PATCH solves (default 1) and reuse it in between (a lagged coarse
- * correction: still symmetric positive definite, so PCG stays exact).  A new
- * topology starts the inverse again from its block-diagonal guess. */
+ * correction: still symmetric positive definite, so PCG stays exact).  Every
+ * call restarts the count: the next solve updates the coarse operator.  A
+ * new topology starts the inverse again from its block-diagonal guess. */
 eolc_status eolc_set_coarse_refresh(eolc_ctx *ctx, int solves);
 /* Bound of every device-side wait of this context's solves: the grid
  * barriers of the persistent PCG kernels and the neighbour exchange of the

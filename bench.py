@@ -22,7 +22,11 @@ Arms:
 
 Timing: W warm-up steps, then K steps each bracketed by CUDA events on the
 library's stream, with L2 flushed (a 256 MiB write) before every step and
-outside the timed interval; max over ranks.  `e2e` runs the same steps
+outside the timed interval; max over ranks.  Every arm starts from the same
+post-warm-up state after one untimed step of its own from that state, and
+its first timed step re-evaluates the learned network and updates the
+coarse inverse (the refresh counts restart), so no arm inherits another's
+solver state.  `e2e` runs the same steps
 through the host-buffer call eolc_step (H2D of x, X, v and D2H of x, v inside
 the timed region).  The roofline entry is for the fastest arm's solver
 kernel, which dominates the step: its algorithmic HBM bytes per launch (the

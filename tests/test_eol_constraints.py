@@ -279,3 +279,35 @@ def test_rigid_integrate_matches_the_exponential_map():
         T[:3, 3] = v
         h = 0.01
         assert np.abs(R.rigid_integrate(E0, phi, h) - E0 @ sl.expm(h * T)).max() <= 1e-12
+
+
+def test_rows_of_the_flat_box_edge_sheet_by_hand():
+    """The rows Constraints.cpp:263-403 give on a flat 4x4-quad sheet whose
+    middle node column lies on the +x/+z edge of an axis-aligned box, worked
+    out by hand from the reference's expressions: every EOL node is flat
+    (all normals +z), so it gets the inequality -n = (0, 0, -1) and the
+    equality -(n x t) = (1, 0, 0) with t = +y (the edge's third table
+    direction); the Eulerian row is (0, -1) at the two boundary nodes (the
+    border expression with the first boundary edge, (u_y - u'_y, -u_x - u'_x)
+    normalised) and at the interior ones (the preserved edges' unit
+    directions toward the end nearer the material origin, summed and
+    normalised).  Both the library and the oracle must give exactly these."""
+    s = scenes.eol_edge_sheet(4)
+    n, ne = s["n"], len(s["eol"])
+    nd = 3 * (n + ne)
+    eq = np.zeros((2 * ne, nd))
+    iq = np.zeros((ne, nd))
+    for k, a in enumerate(s["eol"]):
+        eq[2 * k, 3 * a] = 1.0                      # -(n x t) on the node
+        eq[2 * k + 1, 3 * (n + k) + 1] = -1.0       # the Eulerian row (0, -1)
+        iq[k, 3 * a + 2] = -1.0                     # -n on the node
+    ob, lb = _boxes(s)
+    E, I = eolc.constraint_rows(s["x"], s["X"], s["tri"], s["edges"], s["eol"], s["corner"],
+                                s["cd"], s["preserve"], [lb], None, ())
+    assert np.array_equal(E.csr(nd).toarray(), eq)
+    assert np.array_equal(I.csr(nd).toarray(), iq)
+    Aeq, _, Ai, _ = R.constraint_rows(s["x"], s["X"], s["tri"], s["edges"], s["eol"], s["corner"],
+                                      s["cd"], s["preserve"], [ob], None, ())
+    idx = eolc.eol_reference_index(n, ne)
+    assert np.array_equal(Aeq.toarray(), eq[:, idx])
+    assert np.array_equal(Ai.toarray(), iq[:, idx])

@@ -311,3 +311,27 @@ def test_rows_of_the_flat_box_edge_sheet_by_hand():
     idx = eolc.eol_reference_index(n, ne)
     assert np.array_equal(Aeq.toarray(), eq[:, idx])
     assert np.array_equal(Ai.toarray(), iq[:, idx])
+
+
+def test_corner_rows_by_hand():
+    """A flat node tagged with corner 5 (+x, -y, +z) of an axis-aligned box
+    (Constraints.cpp:148-215): the table normal nor = (1, -1, 1)/sqrt(3) as
+    the inequality -nor, and the equalities o1 = (0, -nor_z, nor_y) =
+    (0, -1, -1)/sqrt(3) and o2 = (o1 x nor)/|o1 x nor| = (-2, -1, 1)/sqrt(6);
+    no Eulerian row."""
+    s = scenes.eol_edge_sheet(4)
+    n, ne = s["n"], len(s["eol"])
+    corner = s["corner"].copy()
+    corner[0] = 5
+    _, lb = _boxes(s)
+    E, I = eolc.constraint_rows(s["x"], s["X"], s["tri"], s["edges"], s["eol"], corner, s["cd"],
+                                s["preserve"], [lb], None, ())
+    a = int(s["eol"][0])
+    nd = 3 * (n + ne)
+    Ed, Id = E.csr(nd).toarray(), I.csr(nd).toarray()
+    r3, r6 = 1 / np.sqrt(3), 1 / np.sqrt(6)
+    assert np.abs(Id[0, 3 * a:3 * a + 3] - [-r3, r3, -r3]).max() <= 1e-15
+    assert np.abs(Ed[0, 3 * a:3 * a + 3] - [0, -r3, -r3]).max() <= 1e-15
+    assert np.abs(Ed[1, 3 * a:3 * a + 3] - [-2 * r6, -r6, r6]).max() <= 1e-15
+    assert not Ed[:2, 3 * n:].any()               # the corner node has no Eulerian row
+    assert E.m == 2 * ne and I.m == ne            # 2 + 1 rows for it and for each other
